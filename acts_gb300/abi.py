@@ -1,0 +1,260 @@
+"""ctypes mirror of the C ABI structs in include/cudakalman.h and include/ckgen.h.
+
+The layouts here must match the C headers field for field; tests/test_abi.py
+checks the sizes against the compiled library (ck_abi_struct_sizes).
+"""
+import ctypes as C
+
+import numpy as np
+
+# ---------------------------------------------------------------- constants
+CK_OK = 0
+CK_ERR_INVALID_ARGUMENT = 1
+CK_ERR_CUDA = 2
+CK_ERR_NO_DEVICE = 3
+CK_ERR_OUT_OF_MEMORY = 4
+CK_ERR_UNSUPPORTED = 5
+CK_ERR_BUDGET = 6
+CK_ERR_TIMEOUT = 7
+CK_ERR_NOT_READY = 8
+CK_ERR_SCRATCH_LIMIT = 9
+
+TRACK_STATUS = {
+    0: "OK",
+    1: "UpdateFailed",
+    2: "SmoothFailed",
+    3: "NoMeasurementFound",
+    4: "StepCountLimitReached",
+    5: "NextTargetLimitReached",
+    6: "StepSizeStalled",
+    7: "StepSizeAdjustmentFailed",
+    8: "GlobalPositionNotOnSurface",
+    9: "MagneticFieldOutOfBounds",
+    10: "TooManyStates",
+    11: "NotProcessed",
+    12: "InvalidInput",
+}
+
+FLAG_HAS_MEASUREMENT = 1 << 0
+FLAG_HAS_PARAMETERS = 1 << 1
+FLAG_IS_OUTLIER = 1 << 2
+FLAG_IS_HOLE = 1 << 3
+FLAG_HAS_MATERIAL = 1 << 4
+
+SURFACE_PLANE = 0
+SURFACE_CYLINDER = 1
+SURF_SENSITIVE = 1
+SURF_MATERIAL = 2
+
+FIELD_CONSTANT = 0
+FIELD_GRID_XYZ = 1
+
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+
+MEM_HOST = 0
+MEM_DEVICE = 1
+
+OUT_PREDICTED = 1 << 0
+OUT_FILTERED = 1 << 1
+OUT_SMOOTHED = 1 << 2
+OUT_JACOBIAN = 1 << 3
+OUT_ALL = OUT_PREDICTED | OUT_FILTERED | OUT_SMOOTHED | OUT_JACOBIAN
+
+CKG_TELESCOPE = 1
+CKG_BARREL = 2
+CKG_BARREL_MIXED = 3
+CKG_UNEVEN = 4
+CKG_SERVING = 5
+
+P_i32 = C.POINTER(C.c_int32)
+P_u32 = C.POINTER(C.c_uint32)
+P_f64 = C.POINTER(C.c_double)
+P_f32 = C.POINTER(C.c_float)
+P_u8 = C.POINTER(C.c_uint8)
+
+
+class ck_surface(C.Structure):
+    _fields_ = [
+        ("type", C.c_int32),
+        ("flags", C.c_int32),
+        ("rotation", C.c_double * 9),
+        ("center", C.c_double * 3),
+        ("radius", C.c_double),
+        ("half_length_z", C.c_double),
+        ("half_x", C.c_double),
+        ("half_y", C.c_double),
+        ("mat_thickness", C.c_float),
+        ("mat_x0", C.c_float),
+        ("mat_l0", C.c_float),
+        ("mat_ar", C.c_float),
+        ("mat_z", C.c_float),
+        ("mat_molar_rho", C.c_float),
+        ("mat_molar_electron_rho", C.c_float),
+        ("mat_mean_excitation", C.c_float),
+        ("split_factor", C.c_float),
+        ("reserved", C.c_float),
+    ]
+
+
+class ck_field(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("n", C.c_int32 * 3),
+        ("constant_tesla", C.c_double * 3),
+        ("min", C.c_double * 3),
+        ("max", C.c_double * 3),
+        ("values_tesla", P_f32),
+    ]
+
+
+class ck_options(C.Structure):
+    _fields_ = [
+        ("step_tolerance", C.c_double),
+        ("step_size_cutoff", C.c_double),
+        ("initial_step_size", C.c_double),
+        ("max_step_size", C.c_double),
+        ("max_rk_step_trials", C.c_uint32),
+        ("max_steps", C.c_uint32),
+        ("max_target_skipping", C.c_uint32),
+        ("loop_protection", C.c_int32),
+        ("path_limit", C.c_double),
+        ("loop_fraction", C.c_double),
+        ("surface_tolerance", C.c_double),
+        ("near_limit", C.c_double),
+        ("multiple_scattering", C.c_int32),
+        ("energy_loss", C.c_int32),
+        ("use_joseph", C.c_int32),
+        ("precision", C.c_int32),
+        ("outlier_chi2_cut", C.c_double),
+        ("reverse_filtering", C.c_int32),
+        ("free_to_bound_correction", C.c_int32),
+        ("reference_surface", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class ck_config(C.Structure):
+    _fields_ = [
+        ("device", C.c_int32),
+        ("n_surfaces", C.c_int32),
+        ("surfaces", C.POINTER(ck_surface)),
+        ("field", ck_field),
+        ("threads_per_block", C.c_int32),
+        ("blocks_per_sm", C.c_int32),
+        ("use_graph", C.c_int32),
+        ("reserved", C.c_int32),
+        ("autotune_cache", C.c_char_p),
+    ]
+
+
+class ck_batch_in(C.Structure):
+    _fields_ = [
+        ("n_tracks", C.c_int32),
+        ("memory", C.c_int32),
+        ("seq_offsets", P_i32),
+        ("seq_surfaces", P_i32),
+        ("meas_offsets", P_i32),
+        ("meas_surfaces", P_i32),
+        ("meas_values", P_f64),
+        ("meas_cov", P_f64),
+        ("start_params", P_f64),
+        ("start_cov", P_f64),
+        ("start_frames", P_f64),
+        ("particle", P_f32),
+        ("particle_pdg", P_i32),
+    ]
+
+
+class ck_batch_out(C.Structure):
+    _fields_ = [
+        ("max_states", C.c_int32),
+        ("components", C.c_uint32),
+        ("memory", C.c_int32),
+        ("reserved", C.c_int32),
+        ("status", P_i32),
+        ("n_states", P_i32),
+        ("n_measurements", P_i32),
+        ("n_holes", P_i32),
+        ("n_outliers", P_i32),
+        ("ndf", P_i32),
+        ("chi2_sum", P_f64),
+        ("state_surface", P_i32),
+        ("state_flags", P_u32),
+        ("state_path_length", P_f64),
+        ("state_chi2", P_f64),
+        ("predicted", P_f64),
+        ("predicted_cov", P_f64),
+        ("filtered", P_f64),
+        ("filtered_cov", P_f64),
+        ("smoothed", P_f64),
+        ("smoothed_cov", P_f64),
+        ("jacobian", P_f64),
+    ]
+
+
+class ck_server_config(C.Structure):
+    _fields_ = [
+        ("memory_budget_bytes", C.c_int64),
+        ("n_streams", C.c_int32),
+        ("max_states", C.c_int32),
+        ("max_batch_tracks", C.c_int32),
+        ("components", C.c_uint32),
+    ]
+
+
+class ckg_out(C.Structure):
+    _fields_ = [
+        ("max_per_track", C.c_int32),
+        ("seq_offsets", P_i32),
+        ("seq_surfaces", P_i32),
+        ("meas_offsets", P_i32),
+        ("meas_surfaces", P_i32),
+        ("meas_values", P_f64),
+        ("meas_cov", P_f64),
+        ("start_params", P_f64),
+        ("start_cov", P_f64),
+        ("start_frames", P_f64),
+        ("particle", P_f32),
+        ("particle_pdg", P_i32),
+        ("truth_meas", P_f64),
+        ("meas_outlier", P_u8),
+        ("truth_start", P_f64),
+    ]
+
+
+def ptr(a, ctype):
+    """ctypes pointer to a contiguous numpy array (None stays NULL)."""
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "array must be C-contiguous"
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+def default_options(**kw):
+    """Reference defaults (StepperPlainOptions, PropagatorPlainOptions,
+    DirectNavigator::Options, KalmanFitterOptions), see ck_options_default."""
+    o = ck_options()
+    o.step_tolerance = 1e-4
+    o.step_size_cutoff = 0.0
+    o.initial_step_size = 10000.0
+    o.max_step_size = np.finfo(np.float64).max
+    o.max_rk_step_trials = 10000
+    o.max_steps = 1000
+    o.max_target_skipping = 100
+    o.loop_protection = 1
+    o.path_limit = np.finfo(np.float64).max
+    o.loop_fraction = 0.5
+    o.surface_tolerance = 1e-4
+    o.near_limit = -0.1
+    o.multiple_scattering = 1
+    o.energy_loss = 1
+    o.use_joseph = 0
+    o.precision = PRECISION_FP64
+    o.outlier_chi2_cut = float("inf")
+    o.reverse_filtering = 0
+    o.free_to_bound_correction = 0
+    o.reference_surface = -1
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o

@@ -1,0 +1,768 @@
+// ck_api.cu — implementation of the C ABI declared in include/cudakalman.h.
+//
+// A ck_handle owns the resident detector (surface table, field map), the
+// grow-only device buffers of the batch pipeline, the scratch records of the
+// tracks in flight and the tuned launch shape. One handle serves one stream;
+// concurrent callers on the same handle are serialised by its mutex.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <limits>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "ck_api_internal.h"
+#include "ck_launch.h"
+
+using namespace ck;
+
+namespace ck {
+
+thread_local std::string g_lastError;
+
+ck_status fail(ck_status s, const std::string& msg) {
+  g_lastError = msg;
+  return s;
+}
+
+ck_status cudaFail(cudaError_t e, const char* what) {
+  return fail(e == cudaErrorMemoryAllocation ? CK_ERR_OUT_OF_MEMORY : CK_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+cudaError_t DevBuf::ensure(size_t bytes) {
+  if (bytes <= cap) return cudaSuccess;
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  size_t want = bytes + bytes / 4 + 256;
+  cudaError_t e = cudaMalloc(&p, want);
+  if (e != cudaSuccess) {
+    p = nullptr;
+    return e;
+  }
+  cap = want;
+  return cudaSuccess;
+}
+
+void DevBuf::release() {
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+}
+
+MatConst makeMatConst() {
+  // Interactions.cpp:23-31 constants, evaluated with the reference's
+  // long-double unit literals (Units.hpp:181-187)
+  auto MeV = [](long double x) { return (double)(1e-3 * x); };
+  auto eV = [](long double x) { return (double)(1e-9 * x); };
+  MatConst c;
+  c.Me = (float)MeV(0.5109989461L);
+  c.K = (float)(MeV(30.7075L) * 1.0);
+  c.plasmaScale = (float)eV(28.816L);
+  c.invCm3 = static_cast<float>(1 / (10.0 * 10.0 * 10.0));
+  c.highland = MeV(13.6L);
+  c.rossi = MeV(17.5L);
+  c.log10f = (float)std::log((double)10.0f);
+  c.pad = 0.0f;
+  return c;
+}
+
+DevSurface toDevSurface(const ck_surface& s) {
+  DevSurface d;
+  std::memset(&d, 0, sizeof(d));
+  for (int i = 0; i < 9; ++i) d.R[i] = s.rotation[i];
+  for (int i = 0; i < 3; ++i) d.c[i] = s.center[i];
+  d.radius = s.radius;
+  d.type = s.type;
+  d.flags = s.flags;
+  d.matI = s.mat_mean_excitation;
+  d.matNe = s.mat_molar_electron_rho;
+  // MaterialSlab(material, thickness) (MaterialSlab.hpp:119-128)
+  const float eps = 2 * std::numeric_limits<float>::epsilon();
+  d.thickness = s.mat_thickness;
+  d.tX0 = (eps < s.mat_x0) ? (s.mat_thickness / s.mat_x0) : 0.0f;
+  d.tL0 = (eps < s.mat_l0) ? (s.mat_thickness / s.mat_l0) : 0.0f;
+  d.split = s.split_factor;
+  d.vacuum = (s.mat_ar > 0.0f) ? 0 : 1;
+  return d;
+}
+
+DevOptions toDevOptions(const ck_options& o) {
+  DevOptions d;
+  d.stepTolerance = o.step_tolerance;
+  d.stepSizeCutOff = o.step_size_cutoff;
+  d.initialStepSize = o.initial_step_size;
+  d.maxStepSize = o.max_step_size;
+  d.pathLimit = o.path_limit;
+  d.loopFraction = o.loop_fraction;
+  d.surfaceTolerance = o.surface_tolerance;
+  d.nearLimit = o.near_limit;
+  d.outlierChi2Cut = o.outlier_chi2_cut;
+  d.maxRkTrials = o.max_rk_step_trials;
+  d.maxSteps = o.max_steps;
+  d.maxTargetSkipping = o.max_target_skipping;
+  d.loopProtection = o.loop_protection;
+  d.multipleScattering = o.multiple_scattering;
+  d.energyLoss = o.energy_loss;
+  d.joseph = o.use_joseph;
+  d.useOutlierCut = std::isinf(o.outlier_chi2_cut) ? 0 : 1;
+  return d;
+}
+
+ck_status validateOptions(const ck_options* o) {
+  if (!o) return fail(CK_ERR_INVALID_ARGUMENT, "options is NULL");
+  if (o->reverse_filtering)
+    return fail(CK_ERR_UNSUPPORTED, "reverse filtering is not in the declared extension set");
+  if (o->free_to_bound_correction)
+    return fail(CK_ERR_UNSUPPORTED, "free-to-bound correction is not supported");
+  if (o->reference_surface != -1)
+    return fail(CK_ERR_UNSUPPORTED, "extrapolation to a reference surface is not supported");
+  if (o->precision != CK_PRECISION_FP64 && o->precision != CK_PRECISION_MIXED)
+    return fail(CK_ERR_INVALID_ARGUMENT, "unknown precision");
+  if (!(o->step_tolerance > 0) || !(o->initial_step_size > 0))
+    return fail(CK_ERR_INVALID_ARGUMENT, "step tolerance and initial step size must be > 0");
+  if (o->max_steps == 0) return fail(CK_ERR_INVALID_ARGUMENT, "max_steps must be > 0");
+  return CK_OK;
+}
+
+}  // namespace ck
+
+// ------------------------------------------------------------ queue kernels
+namespace {
+
+constexpr int kBins = 64;
+
+__global__ void queueHistogram(const int32_t* __restrict__ off, int n, int32_t* bins) {
+  __shared__ int32_t h[kBins];
+  for (int i = threadIdx.x; i < kBins; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    int len = off[t + 1] - off[t];
+    len = len < 0 ? 0 : (len >= kBins ? kBins - 1 : len);
+    atomicAdd(&h[len], 1);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kBins; i += blockDim.x)
+    if (h[i]) atomicAdd(&bins[i], h[i]);
+}
+
+// exclusive scan over bins in descending length order -> cursor per bin
+__global__ void queueScan(int32_t* bins) {
+  if (threadIdx.x == 0) {
+    int32_t acc = 0;
+    for (int b = kBins - 1; b >= 0; --b) {
+      int32_t c = bins[b];
+      bins[b] = acc;
+      acc += c;
+    }
+  }
+}
+
+__global__ void queueScatter(const int32_t* __restrict__ off, int n, int32_t* cursor,
+                             int32_t* perm) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    int len = off[t + 1] - off[t];
+    len = len < 0 ? 0 : (len >= kBins ? kBins - 1 : len);
+    perm[atomicAdd(&cursor[len], 1)] = t;
+  }
+}
+
+}  // namespace
+
+// --------------------------------------------------------------- helpers
+namespace ck {
+
+size_t compBytes(int n, int maxStates, int C, size_t elem) {
+  return (size_t)n * (size_t)maxStates * (size_t)C * elem;
+}
+
+void loadTuneCache(ck_handle* h) {
+  if (h->cachePath.empty()) return;
+  std::ifstream f(h->cachePath);
+  int p, v, tpb, bps;
+  while (f >> p >> v >> tpb >> bps) {
+    if (p < 0 || p > 1 || v < 0 || v >= kNumFitVariants || tpb <= 0 || tpb > kFitMaxBlock ||
+        bps <= 0)
+      continue;
+    h->tune[p] = {v, tpb, bps, true};
+  }
+}
+
+void saveTuneCache(ck_handle* h) {
+  if (h->cachePath.empty()) return;
+  std::ofstream f(h->cachePath);
+  for (int p = 0; p < 2; ++p)
+    if (h->tune[p].tuned)
+      f << p << " " << h->tune[p].variant << " " << h->tune[p].tpb << " " << h->tune[p].bps << "\n";
+}
+
+cudaError_t launchFit(const FitParams& fp, int precision, const Tune& tn, int grid,
+                      cudaStream_t st) {
+  return precision == CK_PRECISION_MIXED ? launchFitMixed(fp, tn.variant, grid, tn.tpb, st)
+                                         : launchFitFP64(fp, tn.variant, grid, tn.tpb, st);
+}
+
+// Allocates (grow-only) the scratch of a batch pipeline. Never called while
+// a stream is being captured.
+ck_status preparePipeline(ck_handle* h, int n, int maxStates, const Tune& tn) {
+  const int grid = h->smCount * tn.bps;
+  const int nSlots = grid * tn.tpb;
+  cudaError_t e;
+  if ((e = h->rec.ensure(compBytes(nSlots, maxStates, kRecDoubles, sizeof(double)))) ||
+      (e = h->recMeta.ensure(compBytes(nSlots, maxStates, 2, sizeof(int32_t)))) ||
+      (e = h->recMetaD.ensure(compBytes(nSlots, maxStates, 2, sizeof(double)))) ||
+      (e = h->perm.ensure((size_t)n * sizeof(int32_t) + 16)) ||
+      (e = h->ticket.ensure(sizeof(int32_t) * (kBins + 1))))
+    return cudaFail(e, "scratch allocation");
+  return CK_OK;
+}
+
+// Records the whole batch pipeline (inputs already on the device, scratch
+// prepared) on `st`: queue reset, queue ordering, fit kernel.
+ck_status enqueuePipeline(ck_handle* h, const ck_options& opt, const ck_batch_in& din,
+                          const ck_batch_out& dout, const Tune& tn, cudaStream_t st,
+                          bool timed) {
+  const int n = din.n_tracks;
+  const int grid = h->smCount * tn.bps;
+  const int nSlots = grid * tn.tpb;
+  const int maxStates = dout.max_states;
+  cudaError_t e;
+  int32_t* dTicket = (int32_t*)h->ticket.p;
+  int32_t* dBins = dTicket + 1;
+  int launches = 0;
+  cudaMemsetAsync(dTicket, 0, sizeof(int32_t) * (kBins + 1), st);
+  const int32_t* perm = nullptr;
+  if (h->sortQueue && n > 0) {
+    const int tb = 256;
+    int gb = (n + tb - 1) / tb;
+    if (gb > h->smCount * 8) gb = h->smCount * 8;
+    queueHistogram<<<gb, tb, 0, st>>>(din.seq_offsets, n, dBins);
+    queueScan<<<1, 32, 0, st>>>(dBins);
+    queueScatter<<<gb, tb, 0, st>>>(din.seq_offsets, n, dBins, (int32_t*)h->perm.p);
+    launches += 3;
+    perm = (const int32_t*)h->perm.p;
+  }
+  FitParams fp;
+  std::memset(&fp, 0, sizeof(fp));
+  fp.n_tracks = n;
+  fp.n_queue = n;
+  fp.seq_off = din.seq_offsets;
+  fp.seq_surf = din.seq_surfaces;
+  fp.meas_off = din.meas_offsets;
+  fp.meas_surf = din.meas_surfaces;
+  fp.meas_val = din.meas_values;
+  fp.meas_cov = din.meas_cov;
+  fp.start_params = din.start_params;
+  fp.start_cov = din.start_cov;
+  fp.start_frames = din.start_frames;
+  fp.particle = din.particle;
+  fp.pdg = din.particle_pdg;
+  fp.perm = perm;
+  fp.ticket = dTicket;
+  fp.rec = (double*)h->rec.p;
+  fp.rec_meta = (int32_t*)h->recMeta.p;
+  fp.rec_meta_d = (double*)h->recMetaD.p;
+  fp.n_slots = nSlots;
+  fp.max_states = maxStates;
+  fp.out = dout;
+  fp.surfaces = h->dSurfaces;
+  fp.n_surfaces = h->nSurfaces;
+  fp.field = h->field;
+  fp.mc = h->mc;
+  fp.opt = toDevOptions(opt);
+  if (timed) cudaEventRecord(h->ev0, st);
+  if (n > 0) {
+    e = launchFit(fp, opt.precision, tn, grid, st);
+    if (e != cudaSuccess) return cudaFail(e, "fit kernel launch");
+    ++launches;
+  }
+  if (timed) cudaEventRecord(h->ev1, st);
+  h->lastLaunches = launches;
+  h->lastTimed = timed;
+  return CK_OK;
+}
+
+struct OutArrays {
+  void* host[18];
+  void* dev[18];
+  size_t bytes[18];
+  int count = 0;
+};
+
+}  // namespace ck
+
+// ------------------------------------------------------------------ C ABI
+extern "C" {
+
+void ck_options_default(ck_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->step_tolerance = 1e-4;
+  o->step_size_cutoff = 0.0;
+  o->initial_step_size = 10000.0;
+  o->max_step_size = std::numeric_limits<double>::max();
+  o->max_rk_step_trials = 10000;
+  o->max_steps = 1000;
+  o->max_target_skipping = 100;
+  o->loop_protection = 1;
+  o->path_limit = std::numeric_limits<double>::max();
+  o->loop_fraction = 0.5;
+  o->surface_tolerance = 1e-4;
+  o->near_limit = -0.1;
+  o->multiple_scattering = 1;
+  o->energy_loss = 1;
+  o->use_joseph = 0;
+  o->precision = CK_PRECISION_FP64;
+  o->outlier_chi2_cut = std::numeric_limits<double>::infinity();
+  o->reverse_filtering = 0;
+  o->free_to_bound_correction = 0;
+  o->reference_surface = -1;
+}
+
+int32_t ck_api_version(void) { return CK_API_VERSION; }
+
+const char* ck_status_string(ck_status s) {
+  switch (s) {
+    case CK_OK:
+      return "ok";
+    case CK_ERR_INVALID_ARGUMENT:
+      return "invalid argument";
+    case CK_ERR_CUDA:
+      return "CUDA error";
+    case CK_ERR_NO_DEVICE:
+      return "no CUDA device";
+    case CK_ERR_OUT_OF_MEMORY:
+      return "out of device memory";
+    case CK_ERR_UNSUPPORTED:
+      return "unsupported feature";
+    case CK_ERR_BUDGET:
+      return "request exceeds the memory budget";
+    case CK_ERR_TIMEOUT:
+      return "timeout";
+    case CK_ERR_NOT_READY:
+      return "not ready";
+    case CK_ERR_SCRATCH_LIMIT:
+      return "request exceeds the fixed scratch capacity";
+  }
+  return "unknown status";
+}
+
+const char* ck_last_error(void) { return g_lastError.c_str(); }
+
+// sizes of the ABI structs, for binding checks
+void ck_abi_struct_sizes(int64_t* out, int32_t n) {
+  const int64_t s[] = {(int64_t)sizeof(ck_surface),   (int64_t)sizeof(ck_field),
+                       (int64_t)sizeof(ck_options),   (int64_t)sizeof(ck_config),
+                       (int64_t)sizeof(ck_batch_in),  (int64_t)sizeof(ck_batch_out),
+                       (int64_t)sizeof(ck_server_config)};
+  for (int i = 0; i < n && i < (int)(sizeof(s) / sizeof(s[0])); ++i) out[i] = s[i];
+}
+
+ck_status ck_create(const ck_config* cfg, ck_handle** out) {
+  if (!cfg || !out) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) return fail(CK_ERR_NO_DEVICE, "no CUDA device visible");
+  if (cfg->device < 0 || cfg->device >= ndev) return fail(CK_ERR_INVALID_ARGUMENT, "bad device");
+  if (cfg->n_surfaces < 0 || (cfg->n_surfaces > 0 && !cfg->surfaces))
+    return fail(CK_ERR_INVALID_ARGUMENT, "bad surface table");
+  for (int i = 0; i < cfg->n_surfaces; ++i) {
+    const ck_surface& s = cfg->surfaces[i];
+    if (s.type != CK_SURFACE_PLANE && s.type != CK_SURFACE_CYLINDER)
+      return fail(CK_ERR_UNSUPPORTED, "surface " + std::to_string(i) + ": unsupported type");
+    if (s.type == CK_SURFACE_CYLINDER && !(s.radius > 0))
+      return fail(CK_ERR_INVALID_ARGUMENT, "surface " + std::to_string(i) + ": radius <= 0");
+  }
+  const ck_field& f = cfg->field;
+  if (f.kind != CK_FIELD_CONSTANT && f.kind != CK_FIELD_GRID_XYZ)
+    return fail(CK_ERR_UNSUPPORTED, "unsupported field kind");
+  if (f.kind == CK_FIELD_GRID_XYZ) {
+    for (int i = 0; i < 3; ++i)
+      if (f.n[i] < 2 || !(f.max[i] > f.min[i]))
+        return fail(CK_ERR_INVALID_ARGUMENT, "bad field grid axes");
+    if (!f.values_tesla) return fail(CK_ERR_INVALID_ARGUMENT, "field values missing");
+  }
+  if ((e = cudaSetDevice(cfg->device)) != cudaSuccess) return cudaFail(e, "cudaSetDevice");
+  ck_handle* h = new ck_handle();
+  h->device = cfg->device;
+  cudaDeviceGetAttribute(&h->smCount, cudaDevAttrMultiProcessorCount, cfg->device);
+  if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreate(&h->ev0)) != cudaSuccess ||
+      (e = cudaEventCreate(&h->ev1)) != cudaSuccess) {
+    delete h;
+    return cudaFail(e, "stream/event creation");
+  }
+  h->nSurfaces = cfg->n_surfaces;
+  h->hostSurfaces.assign(cfg->surfaces, cfg->surfaces + cfg->n_surfaces);
+  std::vector<DevSurface> ds;
+  for (int i = 0; i < cfg->n_surfaces; ++i) ds.push_back(toDevSurface(cfg->surfaces[i]));
+  if (!ds.empty()) {
+    if ((e = cudaMalloc(&h->dSurfaces, ds.size() * sizeof(DevSurface))) != cudaSuccess ||
+        (e = cudaMemcpy(h->dSurfaces, ds.data(), ds.size() * sizeof(DevSurface),
+                        cudaMemcpyHostToDevice)) != cudaSuccess) {
+      ck_destroy(h);
+      return cudaFail(e, "surface upload");
+    }
+  }
+  std::memset(&h->field, 0, sizeof(h->field));
+  h->field.kind = f.kind;
+  for (int i = 0; i < 3; ++i) h->field.b[i] = f.constant_tesla[i] * 0.000299792458;
+  h->hostField = f;
+  if (f.kind == CK_FIELD_GRID_XYZ) {
+    size_t nn = (size_t)f.n[0] * f.n[1] * f.n[2];
+    std::vector<float4> nodes(nn);
+    for (size_t i = 0; i < nn; ++i)
+      nodes[i] = make_float4(f.values_tesla[3 * i], f.values_tesla[3 * i + 1],
+                             f.values_tesla[3 * i + 2], 0.0f);
+    if ((e = cudaMalloc(&h->dNodes, nn * sizeof(float4))) != cudaSuccess ||
+        (e = cudaMemcpy(h->dNodes, nodes.data(), nn * sizeof(float4), cudaMemcpyHostToDevice)) !=
+            cudaSuccess) {
+      ck_destroy(h);
+      return cudaFail(e, "field upload");
+    }
+    for (int i = 0; i < 3; ++i) {
+      // fieldMapXYZ axis: n bins over [min, max + step) (Helpers.hpp:289-310)
+      h->field.n[i] = f.n[i];
+      double xmin = f.min[i], xmax = f.max[i];
+      double step = (xmax - xmin) / static_cast<double>(f.n[i] - 1);
+      xmax += step;
+      h->field.mn[i] = xmin;
+      h->field.width[i] = (xmax - xmin) / static_cast<double>(f.n[i]);
+      h->field.upper[i] = xmin + static_cast<double>(f.n[i] - 1) * h->field.width[i];
+    }
+    h->field.nodes = h->dNodes;
+  }
+  h->mc = makeMatConst();
+  h->useGraph = cfg->use_graph;
+  h->sortQueue = true;
+  if (cfg->autotune_cache) h->cachePath = cfg->autotune_cache;
+  for (int p = 0; p < 2; ++p) {
+    h->tune[p].variant = 0;
+    h->tune[p].tpb = cfg->threads_per_block > 0 ? std::min(cfg->threads_per_block, kFitMaxBlock)
+                                                : kFitMaxBlock;
+    h->tune[p].bps = cfg->blocks_per_sm > 0 ? cfg->blocks_per_sm : 0;
+    h->tune[p].tuned = false;
+  }
+  loadTuneCache(h);
+  for (int p = 0; p < 2; ++p) {
+    if (h->tune[p].bps <= 0) {
+      // default: as many resident blocks as the register budget allows
+      h->tune[p].bps = ck::occupancyBlocks(p, h->tune[p].variant, h->tune[p].tpb);
+      if (h->tune[p].bps <= 0) h->tune[p].bps = 1;
+    }
+  }
+  *out = h;
+  return CK_OK;
+}
+
+ck_status ck_destroy(ck_handle* h) {
+  if (!h) return CK_OK;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->graphExec) cudaGraphExecDestroy(h->graphExec);
+  for (auto& b : h->inBufs) b.release();
+  for (auto& b : h->outBufs) b.release();
+  h->rec.release();
+  h->recMeta.release();
+  h->recMetaD.release();
+  h->perm.release();
+  h->ticket.release();
+  h->unitBuf.release();
+  if (h->dSurfaces) cudaFree(h->dSurfaces);
+  if (h->dNodes) cudaFree(h->dNodes);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return CK_OK;
+}
+
+ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* in,
+                       ck_batch_out* out, void* stream) {
+  if (!h || !in || !out) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
+  ck_status vs = validateOptions(opt);
+  if (vs != CK_OK) return vs;
+  if (in->n_tracks < 0) return fail(CK_ERR_INVALID_ARGUMENT, "n_tracks < 0");
+  if (out->max_states <= 0) return fail(CK_ERR_INVALID_ARGUMENT, "max_states <= 0");
+  if (!out->status) return fail(CK_ERR_INVALID_ARGUMENT, "status array is required");
+  const bool needsCov[4] = {out->predicted != nullptr, out->filtered != nullptr,
+                            out->smoothed != nullptr, false};
+  if ((needsCov[0] && !out->predicted_cov) || (needsCov[1] && !out->filtered_cov) ||
+      (needsCov[2] && !out->smoothed_cov))
+    return fail(CK_ERR_INVALID_ARGUMENT, "parameter arrays need their covariance arrays");
+  std::lock_guard<std::mutex> lock(h->mu);
+  cudaSetDevice(h->device);
+  cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+  const int n = in->n_tracks;
+  const Tune tn = h->tune[opt->precision];
+  cudaError_t e;
+
+  // ---- inputs
+  ck_batch_in din = *in;
+  if (in->memory == CK_MEM_HOST && n > 0) {
+    if (!in->seq_offsets || !in->meas_offsets)
+      return fail(CK_ERR_INVALID_ARGUMENT, "offsets missing");
+    const int nSeq = in->seq_offsets[n], nMeas = in->meas_offsets[n];
+    if (nSeq < 0 || nMeas < 0) return fail(CK_ERR_INVALID_ARGUMENT, "negative CSR size");
+    struct Item {
+      const void* src;
+      size_t bytes;
+      const void** dst;
+    } items[] = {
+        {in->seq_offsets, sizeof(int32_t) * (n + 1), (const void**)&din.seq_offsets},
+        {in->seq_surfaces, sizeof(int32_t) * nSeq, (const void**)&din.seq_surfaces},
+        {in->meas_offsets, sizeof(int32_t) * (n + 1), (const void**)&din.meas_offsets},
+        {in->meas_surfaces, sizeof(int32_t) * nMeas, (const void**)&din.meas_surfaces},
+        {in->meas_values, sizeof(double) * 2 * nMeas, (const void**)&din.meas_values},
+        {in->meas_cov, sizeof(double) * 4 * nMeas, (const void**)&din.meas_cov},
+        {in->start_params, sizeof(double) * 6 * n, (const void**)&din.start_params},
+        {in->start_cov, sizeof(double) * 36 * n, (const void**)&din.start_cov},
+        {in->start_frames, sizeof(double) * 12 * n, (const void**)&din.start_frames},
+        {in->particle, sizeof(float) * 2 * n, (const void**)&din.particle},
+        {in->particle_pdg, sizeof(int32_t) * n, (const void**)&din.particle_pdg},
+    };
+    size_t h2d = 0;
+    for (int i = 0; i < 11; ++i) {
+      if (!items[i].src) {
+        if (i == 10) {
+          *items[i].dst = nullptr;
+          continue;
+        }
+        return fail(CK_ERR_INVALID_ARGUMENT, "input array missing");
+      }
+      if ((e = h->inBufs[i].ensure(items[i].bytes)) != cudaSuccess)
+        return cudaFail(e, "input buffer");
+      if (items[i].bytes &&
+          (e = cudaMemcpyAsync(h->inBufs[i].p, items[i].src, items[i].bytes,
+                               cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return cudaFail(e, "input copy");
+      *items[i].dst = h->inBufs[i].p;
+      h2d += items[i].bytes;
+    }
+    din.memory = CK_MEM_DEVICE;
+    h->lastH2D = h2d;
+  } else {
+    h->lastH2D = 0;
+  }
+
+  // ---- outputs
+  ck_batch_out dout = *out;
+  OutArrays oa;
+  if (out->memory == CK_MEM_HOST && n > 0) {
+    const int ms = out->max_states;
+    struct Item {
+      void** field;
+      size_t bytes;
+    } items[] = {
+        {(void**)&dout.status, sizeof(int32_t) * n},
+        {(void**)&dout.n_states, sizeof(int32_t) * n},
+        {(void**)&dout.n_measurements, sizeof(int32_t) * n},
+        {(void**)&dout.n_holes, sizeof(int32_t) * n},
+        {(void**)&dout.n_outliers, sizeof(int32_t) * n},
+        {(void**)&dout.ndf, sizeof(int32_t) * n},
+        {(void**)&dout.chi2_sum, sizeof(double) * n},
+        {(void**)&dout.state_surface, compBytes(n, ms, 1, 4)},
+        {(void**)&dout.state_flags, compBytes(n, ms, 1, 4)},
+        {(void**)&dout.state_path_length, compBytes(n, ms, 1, 8)},
+        {(void**)&dout.state_chi2, compBytes(n, ms, 1, 8)},
+        {(void**)&dout.predicted, compBytes(n, ms, 6, 8)},
+        {(void**)&dout.predicted_cov, compBytes(n, ms, 36, 8)},
+        {(void**)&dout.filtered, compBytes(n, ms, 6, 8)},
+        {(void**)&dout.filtered_cov, compBytes(n, ms, 36, 8)},
+        {(void**)&dout.smoothed, compBytes(n, ms, 6, 8)},
+        {(void**)&dout.smoothed_cov, compBytes(n, ms, 36, 8)},
+        {(void**)&dout.jacobian, compBytes(n, ms, 36, 8)},
+    };
+    for (int i = 0; i < 18; ++i) {
+      void* hostPtr = *items[i].field;
+      if (!hostPtr) continue;
+      if ((e = h->outBufs[i].ensure(items[i].bytes)) != cudaSuccess)
+        return cudaFail(e, "output buffer");
+      *items[i].field = h->outBufs[i].p;
+      oa.host[oa.count] = hostPtr;
+      oa.dev[oa.count] = h->outBufs[i].p;
+      oa.bytes[oa.count] = items[i].bytes;
+      ++oa.count;
+    }
+    dout.memory = CK_MEM_DEVICE;
+  }
+
+  // ---- pipeline (graph-captured for device-resident batches)
+  ck_status s = preparePipeline(h, n, out->max_states, tn);
+  if (s != CK_OK) return s;
+  const bool deviceOnly = in->memory == CK_MEM_DEVICE && out->memory == CK_MEM_DEVICE;
+  if (deviceOnly && h->useGraph && n > 0) {
+    GraphKey key;
+    key.in = *in;
+    key.out = *out;
+    key.opt = *opt;
+    key.tune = tn;
+    key.stream = st;
+    key.scratch[0] = h->rec.p;
+    key.scratch[1] = h->recMeta.p;
+    key.scratch[2] = h->recMetaD.p;
+    key.scratch[3] = h->perm.p;
+    key.scratch[4] = h->ticket.p;
+    key.sort = h->sortQueue;
+    if (!h->graphExec || std::memcmp(&key, &h->graphKey, sizeof(key)) != 0) {
+      if (h->graphExec) {
+        cudaGraphExecDestroy(h->graphExec);
+        h->graphExec = nullptr;
+      }
+      cudaGraph_t g;
+      if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        return cudaFail(e, "graph capture begin");
+      s = enqueuePipeline(h, *opt, din, dout, tn, st, true);
+      e = cudaStreamEndCapture(st, &g);
+      if (s != CK_OK) return s;
+      if (e != cudaSuccess) return cudaFail(e, "graph capture end");
+      e = cudaGraphInstantiate(&h->graphExec, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cudaFail(e, "graph instantiate");
+      h->graphKey = key;
+      h->graphLaunches = h->lastLaunches;
+    }
+    if ((e = cudaGraphLaunch(h->graphExec, st)) != cudaSuccess) return cudaFail(e, "graph launch");
+    h->lastLaunches = h->graphLaunches;
+    h->lastTimed = true;
+  } else {
+    s = enqueuePipeline(h, *opt, din, dout, tn, st, true);
+    if (s != CK_OK) return s;
+  }
+  size_t d2h = 0;
+  for (int i = 0; i < oa.count; ++i) {
+    if ((e = cudaMemcpyAsync(oa.host[i], oa.dev[i], oa.bytes[i], cudaMemcpyDeviceToHost, st)) !=
+        cudaSuccess)
+      return cudaFail(e, "output copy");
+    d2h += oa.bytes[i];
+  }
+  h->lastD2H = d2h;
+  if ((e = cudaGetLastError()) != cudaSuccess) return cudaFail(e, "batch pipeline");
+  return CK_OK;
+}
+
+ck_status ck_sync(ck_handle* h) {
+  if (!h) return fail(CK_ERR_INVALID_ARGUMENT, "NULL handle");
+  cudaSetDevice(h->device);
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return cudaFail(e, "stream synchronize");
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cudaFail(e, "device synchronize");
+  return CK_OK;
+}
+
+ck_status ck_last_kernel_ms(ck_handle* h, double* ms) {
+  if (!h || !ms) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!h->lastTimed) return fail(CK_ERR_NOT_READY, "no timed batch");
+  cudaSetDevice(h->device);
+  cudaError_t e = cudaEventSynchronize(h->ev1);
+  if (e != cudaSuccess) return cudaFail(e, "event synchronize");
+  float f = 0;
+  e = cudaEventElapsedTime(&f, h->ev0, h->ev1);
+  if (e != cudaSuccess) return cudaFail(e, "event elapsed");
+  *ms = f;
+  return CK_OK;
+}
+
+ck_status ck_last_launch_count(ck_handle* h, int32_t* n) {
+  if (!h || !n) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
+  *n = h->lastLaunches;
+  return CK_OK;
+}
+
+ck_status ck_last_transfer_bytes(ck_handle* h, int64_t* h2d, int64_t* d2h) {
+  if (!h || !h2d || !d2h) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
+  *h2d = (int64_t)h->lastH2D;
+  *d2h = (int64_t)h->lastD2H;
+  return CK_OK;
+}
+
+ck_status ck_get_launch_config(ck_handle* h, int32_t precision, int32_t* tpb, int32_t* bps) {
+  if (!h || !tpb || !bps || precision < 0 || precision > 1)
+    return fail(CK_ERR_INVALID_ARGUMENT, "bad argument");
+  *tpb = h->tune[precision].tpb;
+  *bps = h->tune[precision].bps;
+  return CK_OK;
+}
+
+ck_status ck_set_launch_config(ck_handle* h, int32_t precision, int32_t variant, int32_t tpb,
+                               int32_t bps) {
+  if (!h || precision < 0 || precision > 1 || variant < 0 || variant >= kNumFitVariants ||
+      tpb <= 0 || tpb > kFitMaxBlock || (tpb % 32) != 0 || bps <= 0)
+    return fail(CK_ERR_INVALID_ARGUMENT, "bad launch configuration");
+  std::lock_guard<std::mutex> lock(h->mu);
+  int maxB = occupancyBlocks(precision, variant, tpb);
+  if (bps > maxB) return fail(CK_ERR_INVALID_ARGUMENT, "more blocks per SM than fit");
+  h->tune[precision] = {variant, tpb, bps, true};
+  return CK_OK;
+}
+
+ck_status ck_sort_queue(ck_handle* h, int32_t enable) {
+  if (!h) return fail(CK_ERR_INVALID_ARGUMENT, "NULL handle");
+  std::lock_guard<std::mutex> lock(h->mu);
+  h->sortQueue = enable != 0;
+  if (h->graphExec) {
+    cudaGraphExecDestroy(h->graphExec);
+    h->graphExec = nullptr;
+  }
+  return CK_OK;
+}
+
+ck_status ck_autotune(ck_handle* h, const ck_options* opt, const ck_batch_in* in,
+                      ck_batch_out* out) {
+  if (!h || !in || !out) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
+  ck_status vs = validateOptions(opt);
+  if (vs != CK_OK) return vs;
+  if (in->memory != CK_MEM_DEVICE || out->memory != CK_MEM_DEVICE)
+    return fail(CK_ERR_INVALID_ARGUMENT, "autotuning needs a device-resident batch");
+  const int p = opt->precision;
+  Tune best = h->tune[p];
+  double bestMs = 1e30;
+  std::string log;
+  for (int v = 0; v < kNumFitVariants; ++v)
+    for (int tpb : {32, 64, 128}) {
+      const int maxB = occupancyBlocks(p, v, tpb);
+      if (maxB <= 0) continue;
+      std::vector<int> cands = {maxB, std::max(1, (maxB * 3) / 4), std::max(1, maxB / 2)};
+      for (size_t ci = 0; ci < cands.size(); ++ci) {
+        if (ci > 0 && cands[ci] == cands[ci - 1]) continue;
+        {
+          std::lock_guard<std::mutex> lock(h->mu);
+          h->tune[p] = {v, tpb, cands[ci], true};
+        }
+        double tot = 0;
+        for (int rep = 0; rep < 3; ++rep) {
+          ck_status s = ck_fit_batch(h, opt, in, out, nullptr);
+          if (s != CK_OK) return s;
+          double ms = 0;
+          if ((s = ck_last_kernel_ms(h, &ms)) != CK_OK) return s;
+          if (rep > 0) tot += ms;
+        }
+        const double ms = tot / 2;
+        char buf[128];
+        std::snprintf(buf, sizeof(buf), "v%d tpb%d bps%d %.3fms; ", v, tpb, cands[ci], ms);
+        log += buf;
+        if (ms < bestMs) {
+          bestMs = ms;
+          best = {v, tpb, cands[ci], true};
+        }
+      }
+    }
+  {
+    std::lock_guard<std::mutex> lock(h->mu);
+    h->tune[p] = best;
+    h->tuneLog = log;
+  }
+  saveTuneCache(h);
+  return CK_OK;
+}
+
+const char* ck_autotune_log(ck_handle* h) { return h ? h->tuneLog.c_str() : ""; }
+
+}  // extern "C"

@@ -1,0 +1,83 @@
+// ck_api_internal.h — the handle behind the C ABI (private).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "ck_internal.h"
+#include "cudakalman.h"
+
+namespace ck {
+
+// Grow-only device allocation.
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes);
+  void release();
+};
+
+// Launch shape of the fit kernel for one precision.
+struct Tune {
+  int variant;  // register-cap variant (0: 255, 1: 168, 2: 128 registers)
+  int tpb;      // threads per block
+  int bps;      // resident blocks per SM (grid = SMs * bps)
+  bool tuned;
+};
+
+// Identity of a captured batch pipeline.
+struct GraphKey {
+  ck_batch_in in;
+  ck_batch_out out;
+  ck_options opt;
+  Tune tune;
+  cudaStream_t stream;
+  void* scratch[5];
+  bool sort;
+  GraphKey() { std::memset(this, 0, sizeof(*this)); }
+};
+
+int occupancyBlocks(int precision, int variant, int tpb);
+
+extern thread_local std::string g_lastError;
+ck_status fail(ck_status s, const std::string& msg);
+ck_status cudaFail(cudaError_t e, const char* what);
+ck_status validateOptions(const ck_options* o);
+DevOptions toDevOptions(const ck_options& o);
+MatConst makeMatConst();
+DevSurface toDevSurface(const ck_surface& s);
+
+}  // namespace ck
+
+struct ck_handle {
+  int device = 0;
+  int smCount = 1;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  ck::DevSurface* dSurfaces = nullptr;
+  int nSurfaces = 0;
+  std::vector<ck_surface> hostSurfaces;
+  ck_field hostField{};
+  ck::DevField field{};
+  float4* dNodes = nullptr;
+  ck::MatConst mc{};
+  ck::Tune tune[2]{};
+  std::string cachePath;
+  std::string tuneLog;
+  int useGraph = 1;
+  bool sortQueue = true;
+  ck::DevBuf inBufs[11];
+  ck::DevBuf outBufs[18];
+  ck::DevBuf rec, recMeta, recMetaD, perm, ticket, unitBuf;
+  int lastLaunches = 0;
+  bool lastTimed = false;
+  size_t lastH2D = 0, lastD2H = 0;
+  cudaGraphExec_t graphExec = nullptr;
+  ck::GraphKey graphKey;
+  int graphLaunches = 0;
+  std::mutex mu;
+};

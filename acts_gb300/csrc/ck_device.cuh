@@ -1,0 +1,727 @@
+// ck_device.cuh — device building blocks of the CudaKalman fitter.
+//
+// One track is fitted by one thread. Everything here is a __device__
+// function on small register-resident arrays; the propagation scalar P is
+// double (plain FP64 form) or float (mixed form). The Kalman update, the 2x2
+// and 6x6 inverses and chi2 are always double.
+//
+// The algorithms restate the reference (paths relative to the acts repo):
+//   EigenStepper RKN4 + transport   Core/include/Acts/Propagator/EigenStepper.ipp:168-388,
+//                                   EigenStepperDefaultExtension.hpp:40-228
+//   surfaces                        Core/src/Surfaces/{Plane,Cylinder}Surface.cpp, Surface.cpp:249-306
+//   covariance transport            Core/src/Propagator/detail/CovarianceEngine.cpp:102-165,
+//                                   JacobianEngine.cpp:19-45,122-141
+//   material                        Core/src/Material/Interactions.cpp, PointwiseMaterialInteraction.*
+//   GainMatrixUpdater               Core/include/Acts/TrackFitting/detail/GainMatrixUpdaterImpl.hpp:21-91
+//   GainMatrixSmoother              Core/src/TrackFitting/GainMatrixSmoother.cpp:18-97
+// GB300-specific reformulations (same mathematics, different evaluation):
+//  * the 8x8 free transport Jacobian is never formed: the kernel transports
+//    T = jacTransport * jacToGlobal (8x6), of which only the 21 entries in
+//    rows 0-6 of the phi/theta/(q/p) columns change during a step;
+//  * covariances are kept as packed symmetric 6x6 (21 entries);
+//  * the bound-to-bound Jacobian is assembled from T with the sparsity of
+//    the free-to-bound Jacobian and the path-derivative correction.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+
+#include "ck_internal.h"
+
+namespace ck {
+
+#define CK_D __device__ __forceinline__
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kOnSurfaceTolerance = 1e-4;
+constexpr double kNotSet = 1.7976931348623157e308;  // DBL_MAX
+
+// packed symmetric index (upper triangle, row-major)
+CK_D constexpr int sidx(int i, int j) {
+  return (i <= j) ? (i * 6 - (i * (i - 1)) / 2 + (j - i)) : (j * 6 - (j * (j - 1)) / 2 + (i - j));
+}
+
+// -------------------------------------------------------- periodic helpers
+// Core/include/Acts/Utilities/detail/periodic.hpp:19-93
+template <typename S>
+CK_D S wrap_periodic(S value, S start, S range) {
+  S diff = value - start;
+  return ((S(0) <= diff) && (diff < range)) ? value : (value - range * floor(diff / range));
+}
+CK_D double radian_pos(double x) { return wrap_periodic<double>(x, 0.0, 2 * kPi); }
+CK_D double radian_sym(double x) { return wrap_periodic<double>(x, -kPi, 2 * kPi); }
+CK_D void normalizePhiTheta(double& phi, double& theta) {
+  theta = radian_pos(theta);
+  if (kPi < theta) {
+    phi = phi + kPi;
+    theta = 2 * kPi - theta;
+  }
+  phi = radian_sym(phi);
+}
+
+// ------------------------------------------------------------------ float
+// Correctly rounded float logarithm shared with the CPU oracle.
+CK_D float ck_logf(float x) { return (float)log((double)x); }
+// Un-contracted float arithmetic: the reference evaluates its material
+// physics in float without FMA; these intrinsics keep the device identical.
+CK_D float fm(float a, float b) { return __fmul_rn(a, b); }
+CK_D float fa(float a, float b) { return __fadd_rn(a, b); }
+CK_D float fs(float a, float b) { return __fsub_rn(a, b); }
+CK_D float fd(float a, float b) { return __fdiv_rn(a, b); }
+CK_D float fsq(float a) { return __fsqrt_rn(a); }
+CK_D double dm(double a, double b) { return __dmul_rn(a, b); }
+CK_D double da(double a, double b) { return __dadd_rn(a, b); }
+
+// ---------------------------------------------------------------- surface
+template <typename P>
+struct Surf {
+  P R[9];
+  P c[3];
+  P radius;
+  int type;
+  CK_D void load(const DevSurface* __restrict__ s) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) R[i] = (P)__ldg(&s->R[i]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) c[i] = (P)__ldg(&s->c[i]);
+    radius = (P)__ldg(&s->radius);
+    type = __ldg(&s->type);
+  }
+  CK_D void loadPlane(const double* __restrict__ f12) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) R[i] = (P)f12[i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) c[i] = (P)f12[9 + i];
+    radius = P(0);
+    type = CK_SURFACE_PLANE;
+  }
+  // R^T (p - c)
+  CK_D void toLocal3(const P p[3], P l[3]) const {
+    P d0 = p[0] - c[0], d1 = p[1] - c[1], d2 = p[2] - c[2];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) l[j] = R[0 * 3 + j] * d0 + R[1 * 3 + j] * d1 + R[2 * 3 + j] * d2;
+  }
+  CK_D void toGlobal3(const P l[3], P g[3]) const {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) g[i] = (R[i * 3 + 0] * l[0] + R[i * 3 + 1] * l[1] + R[i * 3 + 2] * l[2]) + c[i];
+  }
+};
+
+// intersection status: 0 unreachable, 1 reachable, 2 on surface
+template <typename P>
+CK_D int statusOf(P path, P tol) {
+  return (fabs(path) < fabs(tol)) ? 2 : 1;
+}
+
+// Surface::intersect with BoundaryTolerance::Infinite. Returns the number of
+// entries (1 for planes, 2 for cylinders), ordered by path length.
+template <typename P>
+CK_D int intersect(const Surf<P>& s, const P pos[3], const P dir[3], P tol, P path[2], int st[2]) {
+  if (s.type == CK_SURFACE_PLANE) {
+    // PlanarHelper.hpp:56-77
+    P n0 = s.R[2], n1 = s.R[5], n2 = s.R[8];
+    P denom = dir[0] * n0 + dir[1] * n1 + dir[2] * n2;
+    if (denom == P(0)) {
+      path[0] = P(0);
+      st[0] = 0;
+      return 1;
+    }
+    P pl = (n0 * (s.c[0] - pos[0]) + n1 * (s.c[1] - pos[1]) + n2 * (s.c[2] - pos[2])) / denom;
+    path[0] = pl;
+    st[0] = statusOf(pl, tol);
+    return 1;
+  }
+  // CylinderSurface::intersectionSolver + RealQuadraticEquation
+  P a0 = s.R[2], a1 = s.R[5], a2 = s.R[8];  // symmetry axis
+  P pc0 = pos[0] - s.c[0], pc1 = pos[1] - s.c[1], pc2 = pos[2] - s.c[2];
+  P px0 = pc1 * a2 - pc2 * a1, px1 = pc2 * a0 - pc0 * a2, px2 = pc0 * a1 - pc1 * a0;
+  P lx0 = dir[1] * a2 - dir[2] * a1, lx1 = dir[2] * a0 - dir[0] * a2, lx2 = dir[0] * a1 - dir[1] * a0;
+  P a = lx0 * lx0 + lx1 * lx1 + lx2 * lx2;
+  P b = P(2) * (lx0 * px0 + lx1 * px1 + lx2 * px2);
+  P cc = (px0 * px0 + px1 * px1 + px2 * px2) - s.radius * s.radius;
+  P disc = b * b - P(4) * a * cc;
+  if (!(disc >= P(0))) {
+    st[0] = st[1] = 0;
+    path[0] = path[1] = P(0);
+    return 2;
+  }
+  P sq = sqrt(disc);
+  P q = P(-0.5) * (b + (b > P(0) ? sq : -sq));
+  P first = q / a;
+  if (disc == P(0)) {
+    path[0] = path[1] = first;
+    st[0] = st[1] = statusOf(first, tol);
+    return 2;
+  }
+  P second = cc / q;
+  if (first <= second) {
+    path[0] = first;
+    path[1] = second;
+  } else {
+    path[0] = second;
+    path[1] = first;
+  }
+  st[0] = statusOf(path[0], tol);
+  st[1] = statusOf(path[1], tol);
+  return 2;
+}
+
+// Surface::globalToLocal (PlaneSurface.cpp:77-86, CylinderSurface.cpp:125-145)
+template <typename P>
+CK_D bool globalToLocal(const Surf<P>& s, const P pos[3], double tol, P loc[2]) {
+  P l[3];
+  s.toLocal3(pos, l);
+  if (s.type == CK_SURFACE_PLANE) {
+    if (fabs((double)l[2]) > fabs(tol)) return false;
+    loc[0] = l[0];
+    loc[1] = l[1];
+    return true;
+  }
+  double inttol = tol;
+  if (tol == kOnSurfaceTolerance) inttol = (double)s.radius * 0.0001;
+  if (inttol < 0.01) inttol = 0.01;
+  P r = sqrt(l[0] * l[0] + l[1] * l[1]);
+  if (fabs((double)(r - s.radius)) > inttol) return false;
+  loc[0] = s.radius * atan2(l[1], l[0]);
+  loc[1] = l[2];
+  return true;
+}
+
+// Surface::localToGlobal (PlaneSurface.cpp:72-75, CylinderSurface.cpp:116-123)
+template <typename P>
+CK_D void localToGlobal(const Surf<P>& s, const P loc[2], P g[3]) {
+  P l[3];
+  if (s.type == CK_SURFACE_PLANE) {
+    l[0] = loc[0];
+    l[1] = loc[1];
+    l[2] = P(0);
+  } else {
+    P phi = loc[0] / s.radius;
+    P sp, cp;
+    sincos(phi, &sp, &cp);
+    l[0] = s.radius * cp;
+    l[1] = s.radius * sp;
+    l[2] = loc[1];
+  }
+  s.toGlobal3(l, g);
+}
+
+// Reference frame columns x and y (the measurement frame), and z.
+// PlaneSurface: the rotation; CylinderSurface: (axis x normal, axis, normal).
+template <typename P>
+CK_D void referenceFrame(const Surf<P>& s, const P pos[3], P ex[3], P ey[3], P ez[3]) {
+  if (s.type == CK_SURFACE_PLANE) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      ex[i] = s.R[i * 3 + 0];
+      ey[i] = s.R[i * 3 + 1];
+      ez[i] = s.R[i * 3 + 2];
+    }
+    return;
+  }
+  P l[3];
+  s.toLocal3(pos, l);
+  P n2 = l[0] * l[0] + l[1] * l[1];
+  P nl0 = l[0], nl1 = l[1];
+  if (n2 > P(0)) {
+    P inv = sqrt(n2);
+    nl0 = l[0] / inv;
+    nl1 = l[1] / inv;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    ez[i] = s.R[i * 3 + 0] * nl0 + s.R[i * 3 + 1] * nl1;
+    ey[i] = s.R[i * 3 + 2];
+  }
+  P x0 = ey[1] * ez[2] - ey[2] * ez[1];
+  P x1 = ey[2] * ez[0] - ey[0] * ez[2];
+  P x2 = ey[0] * ez[1] - ey[1] * ez[0];
+  P xn = x0 * x0 + x1 * x1 + x2 * x2;
+  if (xn > P(0)) {
+    P nn = sqrt(xn);
+    x0 = x0 / nn;
+    x1 = x1 / nn;
+    x2 = x2 / nn;
+  }
+  ex[0] = x0;
+  ex[1] = x1;
+  ex[2] = x2;
+}
+
+// Surface::pathCorrection (PlaneSurface.cpp:155-160, CylinderSurface.cpp:165-171)
+template <typename P>
+CK_D P pathCorrection(const Surf<P>& s, const P pos[3], const P dir[3]) {
+  P ex[3], ey[3], ez[3];
+  if (s.type == CK_SURFACE_PLANE) {
+    P d = s.R[2] * dir[0] + s.R[5] * dir[1] + s.R[8] * dir[2];
+    return P(1) / fabs(d);
+  }
+  referenceFrame(s, pos, ex, ey, ez);
+  P cosAlpha = ez[0] * dir[0] + ez[1] * dir[1] + ez[2] * dir[2];
+  return fabs(P(1) / cosAlpha);
+}
+
+// VectorHelpers::evaluateTrigonomics (VectorHelpers.hpp:165-178)
+template <typename P>
+struct Trig {
+  P cosPhi, sinPhi, cosTheta, sinTheta, invSinTheta;
+};
+template <typename P>
+CK_D Trig<P> trig(const P d[3]) {
+  Trig<P> t;
+  t.cosTheta = d[2];
+  P az = fabs(d[2]);
+  t.sinTheta = sqrt((P(1) - az) * (P(1) + az));
+  t.invSinTheta = P(1) / t.sinTheta;
+  t.cosPhi = d[0] * t.invSinTheta;
+  t.sinPhi = d[1] * t.invSinTheta;
+  return t;
+}
+
+// ------------------------------------------------------ bound <-> free
+// TransformationHelpers.cpp:17-63
+template <typename P>
+CK_D void boundToFree(const Surf<P>& s, const double b[6], P f[8]) {
+  double sp, cp, st, ct;
+  sincos(b[2], &sp, &cp);
+  sincos(b[3], &st, &ct);
+  P dir[3] = {(P)(cp * st), (P)(sp * st), (P)ct};
+  P loc[2] = {(P)b[0], (P)b[1]};
+  P pos[3];
+  localToGlobal(s, loc, pos);
+  f[0] = pos[0];
+  f[1] = pos[1];
+  f[2] = pos[2];
+  f[3] = (P)b[5];
+  f[4] = dir[0];
+  f[5] = dir[1];
+  f[6] = dir[2];
+  f[7] = (P)b[4];
+}
+
+template <typename P>
+CK_D bool freeToBound(const P f[8], const Surf<P>& s, double b[6]) {
+  P pos[3] = {f[0], f[1], f[2]};
+  P loc[2];
+  if (!globalToLocal(s, pos, kOnSurfaceTolerance, loc)) return false;
+  b[0] = (double)loc[0];
+  b[1] = (double)loc[1];
+  b[5] = (double)f[3];
+  b[2] = (double)atan2(f[5], f[4]);
+  b[3] = (double)atan2(sqrt(f[4] * f[4] + f[5] * f[5]), f[6]);
+  b[4] = (double)f[7];
+  return true;
+}
+
+// Surface::boundToFreeJacobian in the reduced transport form:
+// T columns loc0/loc1 hold the frame (rows 0-2); the dynamic block holds
+// rows 0..6 of the phi, theta, q/p columns (Surface.cpp:249-268,
+// JacobianHelpers.hpp:26-43).
+template <typename P>
+struct Transport {
+  P loc[3][2];  // rows 0-2 of columns loc0, loc1 (constant during a segment)
+  P dyn[7][3];  // rows 0-6 of columns phi, theta, q/p
+};
+
+template <typename P>
+CK_D void initTransport(const Surf<P>& s, const P f[8], Transport<P>& T) {
+  P pos[3] = {f[0], f[1], f[2]};
+  P dir[3] = {f[4], f[5], f[6]};
+  P ex[3], ey[3], ez[3];
+  referenceFrame(s, pos, ex, ey, ez);
+  Trig<P> t = trig(dir);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    T.loc[i][0] = ex[i];
+    T.loc[i][1] = ey[i];
+  }
+#pragma unroll
+  for (int i = 0; i < 7; ++i)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) T.dyn[i][c] = P(0);
+  T.dyn[4][0] = -dir[1];
+  T.dyn[5][0] = dir[0];
+  T.dyn[6][0] = P(0);
+  T.dyn[4][1] = t.cosTheta * t.cosPhi;
+  T.dyn[5][1] = t.cosTheta * t.sinPhi;
+  T.dyn[6][1] = -t.sinTheta;
+}
+
+// ------------------------------------------------------------------ field
+template <typename P>
+CK_D bool getField(const DevField& F, const P p[3], P B[3]) {
+  if (F.kind == CK_FIELD_CONSTANT) {
+    B[0] = (P)F.b[0];
+    B[1] = (P)F.b[1];
+    B[2] = (P)F.b[2];
+    return true;
+  }
+  // InterpolatedBFieldMap::getField with the equidistant axes of
+  // fieldMapXYZ and the trilinear interpolate (z, then y, then x)
+  int bin[3];
+  P f[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    if (p[i] < (P)F.mn[i] || p[i] >= (P)F.upper[i]) return false;
+    P u = (p[i] - (P)F.mn[i]) / (P)F.width[i];
+    int bb = (int)floor(u);  // 0-based lower node
+    bb = max(0, min(bb, F.n[i] - 2));
+    bin[i] = bb;
+    P ll = (P)F.mn[i] + (P)bb * (P)F.width[i];
+    P ur = (P)F.mn[i] + (P)(bb + 1) * (P)F.width[i];
+    f[i] = (p[i] - ll) / (ur - ll);
+  }
+  const size_t nz = F.n[2], nyz = (size_t)F.n[1] * F.n[2];
+  const size_t base = bin[0] * nyz + bin[1] * nz + bin[2];
+  float4 v[8];
+#pragma unroll
+  for (int cx = 0; cx < 2; ++cx)
+#pragma unroll
+    for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+      for (int cz = 0; cz < 2; ++cz)
+        v[cx * 4 + cy * 2 + cz] = __ldg(&F.nodes[base + cx * nyz + cy * nz + cz]);
+  P r[4][3];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    r[i][0] = (P(1) - f[2]) * (P)v[2 * i].x + f[2] * (P)v[2 * i + 1].x;
+    r[i][1] = (P(1) - f[2]) * (P)v[2 * i].y + f[2] * (P)v[2 * i + 1].y;
+    r[i][2] = (P(1) - f[2]) * (P)v[2 * i].z + f[2] * (P)v[2 * i + 1].z;
+  }
+  P s0[3], s1[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    s0[c] = (P(1) - f[1]) * r[0][c] + f[1] * r[1][c];
+    s1[c] = (P(1) - f[1]) * r[2][c] + f[1] * r[3][c];
+  }
+  const P unit = (P)0.000299792458;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) B[c] = ((P(1) - f[0]) * s0[c] + f[0] * s1[c]) * unit;
+  return true;
+}
+
+// --------------------------------------------------------------- material
+// Interactions.cpp (float physics) with un-contracted float arithmetic.
+struct RelQ {
+  float q2OverBeta2, beta2, betaGamma, gamma;
+  CK_D RelQ(float mass, float qOverP, float absQ) {
+    q2OverBeta2 = fa(fm(absQ, absQ), fm(fm(mass, qOverP), fm(mass, qOverP)));
+    const float mOverP = fm(mass, fabsf(fd(qOverP, absQ)));
+    const float pOverM = fd(1.0f, mOverP);
+    beta2 = fd(1.0f, fa(1.0f, fm(mOverP, mOverP)));
+    betaGamma = pOverM;
+    gamma = fsq(fa(fm(1.0f, 1.0f), fm(pOverM, pOverM)));
+  }
+};
+
+CK_D float computeEpsilon(const MatConst& C, float Ne, float thickness, const RelQ& rq) {
+  return fm(fm(fm(fm(0.5f, C.K), Ne), thickness), rq.q2OverBeta2);
+}
+CK_D float computeDeltaHalf(const MatConst& C, float I, float Ne, const RelQ& rq) {
+  if (rq.betaGamma < 10.0f) return 0.0f;
+  const float plasmaEnergy = fm(C.plasmaScale, fsq(fd(Ne, C.invCm3)));
+  return fs(fa(ck_logf(rq.betaGamma), ck_logf(fd(plasmaEnergy, I))), 0.5f);
+}
+
+CK_D float energyLossBethe(const MatConst& C, float I, float Ne, float thickness, float m,
+                           float qOverP, float absQ) {
+  const RelQ rq(m, qOverP, absQ);
+  const float eps = computeEpsilon(C, Ne, thickness, rq);
+  const float dhalf = computeDeltaHalf(C, I, Ne, rq);
+  const float u = fm(fm(fm(2.0f, C.Me), rq.betaGamma), rq.betaGamma);
+  const float mfrac = fd(C.Me, m);
+  const float nominator = fm(fm(fm(2.0f, C.Me), rq.betaGamma), rq.betaGamma);
+  const float denom = fa(fa(1.0f, fm(fm(2.0f, rq.gamma), mfrac)), fm(mfrac, mfrac));
+  const float wmax = fd(nominator, denom);
+  const float running =
+      fs(fs(fa(ck_logf(fd(u, I)), ck_logf(fd(wmax, I))), fm(2.0f, rq.beta2)), fm(2.0f, dhalf));
+  return fm(eps, running);
+}
+
+CK_D float landauSigmaQOverP(const MatConst& C, float Ne, float thickness, float m, float qOverP,
+                             float absQ) {
+  const RelQ rq(m, qOverP, absQ);
+  const float fwhm = fm(4.0f, computeEpsilon(C, Ne, thickness, rq));
+  const float sigmaE = fm(fwhm, 0.42466090014400953f);
+  const float pInv = fd(qOverP, absQ);
+  const float qOverBeta = fsq(rq.q2OverBeta2);
+  return fm(fm(fm(qOverBeta, pInv), pInv), sigmaE);
+}
+
+CK_D float theta0(const MatConst& C, float tX0, int absPdg, float m, float qOverP, float absQ) {
+  const float momentumInv = fabsf(fd(qOverP, absQ));
+  const float q2OverBeta2 = RelQ(m, qOverP, absQ).q2OverBeta2;
+  const float t = fsq(fm(tX0, q2OverBeta2));
+  if (absPdg == 11) {
+    // Rossi-Greisen (Interactions.cpp:490-495), log10 = log / log(10)
+    const float lg = fd(ck_logf(fm(10.0f, tX0)), C.log10f);
+    return (float)dm(dm(dm(C.rossi, (double)momentumInv), (double)t),
+                     (double)fa(1.0f, fm(0.125f, lg)));
+  }
+  // Highland (Interactions.cpp:484-489): double product of the float terms
+  return (float)dm(dm(dm(C.highland, (double)momentumInv), (double)t),
+                   (double)fa(1.0f, fm(fm(0.038f, 2.0f), ck_logf(t))));
+}
+
+struct MatEffects {
+  double eLoss, varPhi, varTheta, varQoP;
+};
+
+// computeMaterialEffects (PointwiseMaterialInteraction.cpp:49-90) for a
+// slab scaled by `scale` (float, as MaterialSlab::scaleThickness receives).
+template <typename P>
+CK_D MatEffects materialEffects(const MatConst& C, const DevSurface* __restrict__ s, float f1,
+                                float f2, int absPdg, float mass, float absQ, const P dir[3],
+                                float qOverP, bool ms, bool el, bool& vacuum) {
+  MatEffects e{0.0, 0.0, 0.0, 0.0};
+  float thick = __ldg(&s->thickness);
+  float tX0 = __ldg(&s->tX0);
+  // MaterialSlab::scaleThickness twice: split/mode factor, then path correction
+  thick = fm(thick, f1);
+  tX0 = fm(tX0, f1);
+  thick = fm(thick, f2);
+  tX0 = fm(tX0, f2);
+  vacuum = (__ldg(&s->vacuum) != 0) || thick <= 0.0f;
+  if (vacuum) return e;
+  const float I = __ldg(&s->matI), Ne = __ldg(&s->matNe);
+  if (el) e.eLoss = (double)energyLossBethe(C, I, Ne, thick, mass, qOverP, absQ);
+  if (ms) {
+    const double th0 = (double)theta0(C, tX0, absPdg, mass, qOverP, absQ);
+    const double d0 = (double)dir[0], d1 = (double)dir[1], d2 = (double)dir[2];
+    const double nrm = sqrt(da(da(dm(d0, d0), dm(d1, d1)), dm(d2, d2)));
+    const double prp = sqrt(da(dm(d0, d0), dm(d1, d1)));
+    const double sigmaPhi = dm(th0, nrm / prp);
+    e.varPhi = dm(sigmaPhi, sigmaPhi);
+    e.varTheta = dm(th0, th0);
+  }
+  if (el) {
+    const double sq = (double)landauSigmaQOverP(C, Ne, thick, mass, qOverP, absQ);
+    e.varQoP = dm(sq, sq);
+  }
+  return e;
+}
+
+// ----------------------------------------------------------- 2x2 / 6x6 math
+struct Inv2 {
+  double a00, a01, a10, a11;
+};
+// Eigen's fixed 2x2 inverse (adjugate / determinant)
+CK_D Inv2 inverse2(double m00, double m01, double m10, double m11) {
+  double det = m00 * m11 - m01 * m10;
+  double invdet = 1.0 / det;
+  Inv2 r;
+  r.a00 = m11 * invdet;
+  r.a10 = -m10 * invdet;
+  r.a01 = -m01 * invdet;
+  r.a11 = m00 * invdet;
+  return r;
+}
+
+// 6x6 inverse of a symmetric matrix given packed, by LU with partial
+// pivoting (the algorithm of Eigen's fixed-size inverse for N > 4).
+CK_D void inverse6(const double* __restrict__ Cp, double inv[36]) {
+  double lu[36];
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 6; ++j) lu[i * 6 + j] = Cp[sidx(i, j)];
+  int perm[6] = {0, 1, 2, 3, 4, 5};
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    int p = k;
+    double best = fabs(lu[k * 6 + k]);
+#pragma unroll
+    for (int i = k + 1; i < 6; ++i) {
+      double v = fabs(lu[i * 6 + k]);
+      if (v > best) {
+        best = v;
+        p = i;
+      }
+    }
+    if (p != k) {
+      // swap rows k and p (register-resident: select per row)
+#pragma unroll
+      for (int i = k + 1; i < 6; ++i) {
+        if (i == p) {
+#pragma unroll
+          for (int j = 0; j < 6; ++j) {
+            double t = lu[k * 6 + j];
+            lu[k * 6 + j] = lu[i * 6 + j];
+            lu[i * 6 + j] = t;
+          }
+          int tp = perm[k];
+          perm[k] = perm[i];
+          perm[i] = tp;
+        }
+      }
+    }
+    double piv = lu[k * 6 + k];
+#pragma unroll
+    for (int i = k + 1; i < 6; ++i) {
+      double l = lu[i * 6 + k] / piv;
+      lu[i * 6 + k] = l;
+#pragma unroll
+      for (int j = k + 1; j < 6; ++j) lu[i * 6 + j] = lu[i * 6 + j] - l * lu[k * 6 + j];
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    double y[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      double s = (perm[i] == c) ? 1.0 : 0.0;
+#pragma unroll
+      for (int j = 0; j < i; ++j) s = s - lu[i * 6 + j] * y[j];
+      y[i] = s;
+    }
+#pragma unroll
+    for (int i = 5; i >= 0; --i) {
+      double s = y[i];
+#pragma unroll
+      for (int j = i + 1; j < 6; ++j) s = s - lu[i * 6 + j] * inv[j * 6 + c];
+      inv[i * 6 + c] = s / lu[i * 6 + i];
+    }
+  }
+}
+
+// ------------------------------------------------------ Kalman update (N=2)
+// GainMatrixUpdater::visitMeasurementImpl<2>. pred/P packed symmetric;
+// writes filt and F (packed). Returns false on NaN gain (UpdateFailed).
+CK_D bool kalmanUpdate(const double pred[6], const double Pp[21], double m0, double m1,
+                       const double V[4], bool joseph, double filt[6], double F[21],
+                       double& chi2) {
+  // S = H P H^T + V ; K = P H^T S^-1
+  Inv2 Si = inverse2(Pp[sidx(0, 0)] + V[0], Pp[sidx(0, 1)] + V[1], Pp[sidx(1, 0)] + V[2],
+                     Pp[sidx(1, 1)] + V[3]);
+  double K[6][2];
+  bool nan = false;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    double p0 = Pp[sidx(i, 0)], p1 = Pp[sidx(i, 1)];
+    K[i][0] = p0 * Si.a00 + p1 * Si.a10;
+    K[i][1] = p0 * Si.a01 + p1 * Si.a11;
+    nan |= isnan(K[i][0]) || isnan(K[i][1]);
+  }
+  if (nan) return false;
+  const double r0 = m0 - pred[0], r1 = m1 - pred[1];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) filt[i] = pred[i] + (K[i][0] * r0 + K[i][1] * r1);
+  normalizePhiTheta(filt[2], filt[3]);
+  // A P with A = I - K H : (AP)_ij = P_ij - K_i0 P_0j - K_i1 P_1j
+  if (!joseph) {
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int j = i; j < 6; ++j)
+        F[sidx(i, j)] = Pp[sidx(i, j)] - (K[i][0] * Pp[sidx(0, j)] + K[i][1] * Pp[sidx(1, j)]);
+  } else {
+    double AP[6][6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int j = 0; j < 6; ++j)
+        AP[i][j] = Pp[sidx(i, j)] - (K[i][0] * Pp[sidx(0, j)] + K[i][1] * Pp[sidx(1, j)]);
+    // (AP) A^T + K V K^T
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      double kv0 = K[i][0] * V[0] + K[i][1] * V[2];
+      double kv1 = K[i][0] * V[1] + K[i][1] * V[3];
+#pragma unroll
+      for (int j = i; j < 6; ++j) {
+        double apat = AP[i][j] - (AP[i][0] * K[j][0] + AP[i][1] * K[j][1]);
+        F[sidx(i, j)] = apat + (kv0 * K[j][0] + kv1 * K[j][1]);
+      }
+    }
+  }
+  // chi2 = r^T [(I - H K) V]^-1 r with r = m - H filt
+  const double s0 = m0 - filt[0], s1 = m1 - filt[1];
+  const double b00 = 1.0 - K[0][0], b01 = -K[0][1], b10 = -K[1][0], b11 = 1.0 - K[1][1];
+  Inv2 Mi = inverse2(b00 * V[0] + b01 * V[2], b00 * V[1] + b01 * V[3], b10 * V[0] + b11 * V[2],
+                     b10 * V[1] + b11 * V[3]);
+  const double t0 = s0 * Mi.a00 + s1 * Mi.a10;
+  const double t1 = s0 * Mi.a01 + s1 * Mi.a11;
+  chi2 = t0 * s0 + t1 * s1;
+  return true;
+}
+
+// calculatePredictedChi2 (TrackHelpers.hpp:563-694)
+CK_D double predictedChi2(const double pred[6], const double Pp[21], double m0, double m1,
+                          const double V[4]) {
+  const double r0 = m0 - pred[0], r1 = m1 - pred[1];
+  Inv2 Ri = inverse2(V[0] + Pp[sidx(0, 0)], V[1] + Pp[sidx(0, 1)], V[2] + Pp[sidx(1, 0)],
+                     V[3] + Pp[sidx(1, 1)]);
+  const double t0 = r0 * Ri.a00 + r1 * Ri.a10;
+  const double t1 = r0 * Ri.a01 + r1 * Ri.a11;
+  return t0 * r0 + t1 * r1;
+}
+
+// ---------------------------------------------------------------- smoother
+// GainMatrixSmoother::calculate. Inputs: filtered state k (filt, Pf packed),
+// state k+1 predicted (pp, Ppp packed), its Jacobian J (row-major 36) and its
+// smoothed state (ps, Psp packed). Outputs smoothed state k. False on NaN G.
+CK_D bool smoothStep(const double filt[6], const double Pf[21], const double pp[6],
+                     const double Ppp[21], const double* J, const double ps[6],
+                     const double Psp[21], double sm[6], double Ps[21]) {
+  double inv[36];
+  inverse6(Ppp, inv);
+  // G = (Pf J^T) Pinv
+  double PJ[36];
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) s += Pf[sidx(i, k)] * J[j * 6 + k];
+      PJ[i * 6 + j] = s;
+    }
+  double G[36];
+  bool nan = false;
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) s += PJ[i * 6 + k] * inv[k * 6 + j];
+      G[i * 6 + j] = s;
+      nan |= isnan(s);
+    }
+  if (nan) return false;
+  double d[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) d[i] = ps[i] - pp[i];
+  d[2] = radian_sym(d[2]);
+  d[3] = radian_sym(d[3]);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) s += G[i * 6 + k] * d[k];
+    sm[i] = filt[i] + s;
+  }
+  normalizePhiTheta(sm[2], sm[3]);
+  // Ps = Pf + G (Psp - Ppp) G^T
+  double GD[36];
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) s += G[i * 6 + k] * (Psp[sidx(k, j)] - Ppp[sidx(k, j)]);
+      GD[i * 6 + j] = s;
+    }
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = i; j < 6; ++j) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) s += GD[i * 6 + k] * G[j * 6 + k];
+      Ps[sidx(i, j)] = Pf[sidx(i, j)] + s;
+    }
+  return true;
+}
+
+}  // namespace ck

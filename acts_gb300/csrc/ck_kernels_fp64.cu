@@ -1,0 +1,46 @@
+// ck_kernels_fp64.cu — instantiations of the plain FP64 fit kernel.
+#include "ck_fitter.cuh"
+#include "ck_launch.h"
+
+namespace ck {
+
+// Register-cap variants of the persistent kernel (launch bounds 128 threads,
+// 1 / 3 / 4 resident blocks per SM -> 255 / 168 / 128 registers per thread).
+cudaError_t launchFitFP64(const FitParams& fp, int variant, int grid, int block,
+                          cudaStream_t st) {
+  switch (variant) {
+    case 0:
+      fitKernel<double, double, 128, 1><<<grid, block, 0, st>>>(fp);
+      break;
+    case 1:
+      fitKernel<double, double, 128, 3><<<grid, block, 0, st>>>(fp);
+      break;
+    default:
+      fitKernel<double, double, 128, 4><<<grid, block, 0, st>>>(fp);
+      break;
+  }
+  return cudaGetLastError();
+}
+
+int occupancyFP64(int variant, int tpb) {
+  int n = 0;
+  switch (variant) {
+    case 0:
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernel<double, double, 128, 1>, tpb, 0);
+      break;
+    case 1:
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernel<double, double, 128, 3>, tpb, 0);
+      break;
+    default:
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernel<double, double, 128, 4>, tpb, 0);
+      break;
+  }
+  return n;
+}
+
+int occupancyBlocks(int precision, int variant, int tpb) {
+  return precision == CK_PRECISION_MIXED ? occupancyMixed(variant, tpb)
+                                         : occupancyFP64(variant, tpb);
+}
+
+}  // namespace ck

@@ -1,0 +1,42 @@
+// ck_kernels_mixed.cu — instantiations of the mixed-precision fit kernel:
+// stepper, Jacobian transport, field interpolation and covariance transport
+// in FP32; Kalman update (Joseph form when selected), 2x2 inverse, smoother
+// gain inverse and chi2 in FP64.
+#include "ck_fitter.cuh"
+#include "ck_launch.h"
+
+namespace ck {
+
+cudaError_t launchFitMixed(const FitParams& fp, int variant, int grid, int block,
+                           cudaStream_t st) {
+  switch (variant) {
+    case 0:
+      fitKernel<float, float, 128, 1><<<grid, block, 0, st>>>(fp);
+      break;
+    case 1:
+      fitKernel<float, float, 128, 3><<<grid, block, 0, st>>>(fp);
+      break;
+    default:
+      fitKernel<float, float, 128, 4><<<grid, block, 0, st>>>(fp);
+      break;
+  }
+  return cudaGetLastError();
+}
+
+int occupancyMixed(int variant, int tpb) {
+  int n = 0;
+  switch (variant) {
+    case 0:
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernel<float, float, 128, 1>, tpb, 0);
+      break;
+    case 1:
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernel<float, float, 128, 3>, tpb, 0);
+      break;
+    default:
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernel<float, float, 128, 4>, tpb, 0);
+      break;
+  }
+  return n;
+}
+
+}  // namespace ck

@@ -1,0 +1,168 @@
+"""Python binding of the synthetic event generator (include/ckgen.h).
+
+make_workload() returns numpy arrays in the ck_batch_in layout plus the
+truth needed for pulls; Batch.as_batch_in() wraps them for the C ABI.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .build import LIBDIR, build_generator
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = os.path.join(LIBDIR, "libckgen.so")
+        if not os.path.exists(path):
+            build_generator()
+        L = C.CDLL(path)
+        L.ckg_geometry.restype = C.c_int32
+        L.ckg_geometry.argtypes = [C.c_int32, C.POINTER(abi.ck_surface), C.c_int32]
+        L.ckg_field_values.restype = C.c_int64
+        L.ckg_field_values.argtypes = [C.c_int32]
+        L.ckg_field.restype = None
+        L.ckg_field.argtypes = [C.c_int32, abi.P_f32, C.POINTER(abi.ck_field), C.c_int32]
+        L.ckg_generate.restype = C.c_int64
+        L.ckg_generate.argtypes = [C.c_int32, C.c_uint64, C.c_int64, C.c_int32,
+                                   C.POINTER(abi.ck_surface), C.c_int32,
+                                   C.POINTER(abi.ck_field), C.c_int32, C.POINTER(abi.ckg_out)]
+        L.ckg_event_sizes.restype = None
+        L.ckg_event_sizes.argtypes = [C.c_uint64, C.c_int32, C.c_double, C.c_int32, C.c_int32,
+                                      abi.P_i32]
+        _lib = L
+    return _lib
+
+
+class Detector:
+    """Surface table and field of a preset (owns the field value buffer)."""
+
+    def __init__(self, preset, n_threads=None):
+        L = lib()
+        self.preset = preset
+        arr = (abi.ck_surface * 64)()
+        n = L.ckg_geometry(preset, arr, 64)
+        if n < 0:
+            raise ValueError("unknown preset %r" % preset)
+        self.surfaces = (abi.ck_surface * n)(*arr[:n])
+        self.n_surfaces = n
+        nv = L.ckg_field_values(preset)
+        self.field_values = np.zeros(max(nv, 1), dtype=np.float32)
+        self.field = abi.ck_field()
+        L.ckg_field(preset, abi.ptr(self.field_values, C.c_float), C.byref(self.field),
+                    n_threads or os.cpu_count() or 1)
+
+
+class Batch:
+    """Host arrays of one batch of tracks in the ck_batch_in layout."""
+
+    def __init__(self, n, cap):
+        self.n = n
+        self.cap = cap
+        self.seq_offsets = np.zeros(n + 1, np.int32)
+        self.seq_surfaces = np.zeros(n * cap, np.int32)
+        self.meas_offsets = np.zeros(n + 1, np.int32)
+        self.meas_surfaces = np.zeros(n * cap, np.int32)
+        self.meas_values = np.zeros(n * cap * 2, np.float64)
+        self.meas_cov = np.zeros(n * cap * 4, np.float64)
+        self.start_params = np.zeros(n * 6, np.float64)
+        self.start_cov = np.zeros(n * 36, np.float64)
+        self.start_frames = np.zeros(n * 12, np.float64)
+        self.particle = np.zeros(n * 2, np.float32)
+        self.particle_pdg = np.zeros(n, np.int32)
+        self.truth_meas = np.zeros(n * cap * 6, np.float64)
+        self.meas_outlier = np.zeros(n * cap, np.uint8)
+        self.truth_start = np.zeros(n * 6, np.float64)
+
+    def trim(self):
+        ns = int(self.seq_offsets[-1])
+        nm = int(self.meas_offsets[-1])
+        self.seq_surfaces = np.ascontiguousarray(self.seq_surfaces[:ns])
+        self.meas_surfaces = np.ascontiguousarray(self.meas_surfaces[:nm])
+        self.meas_values = np.ascontiguousarray(self.meas_values[: 2 * nm])
+        self.meas_cov = np.ascontiguousarray(self.meas_cov[: 4 * nm])
+        self.truth_meas = np.ascontiguousarray(self.truth_meas[: 6 * nm])
+        self.meas_outlier = np.ascontiguousarray(self.meas_outlier[:nm])
+        return self
+
+    @property
+    def n_meas(self):
+        return int(self.meas_offsets[-1])
+
+    def as_batch_in(self, memory=abi.MEM_HOST):
+        b = abi.ck_batch_in()
+        b.n_tracks = self.n
+        b.memory = memory
+        b.seq_offsets = abi.ptr(self.seq_offsets, C.c_int32)
+        b.seq_surfaces = abi.ptr(self.seq_surfaces, C.c_int32)
+        b.meas_offsets = abi.ptr(self.meas_offsets, C.c_int32)
+        b.meas_surfaces = abi.ptr(self.meas_surfaces, C.c_int32)
+        b.meas_values = abi.ptr(self.meas_values, C.c_double)
+        b.meas_cov = abi.ptr(self.meas_cov, C.c_double)
+        b.start_params = abi.ptr(self.start_params, C.c_double)
+        b.start_cov = abi.ptr(self.start_cov, C.c_double)
+        b.start_frames = abi.ptr(self.start_frames, C.c_double)
+        b.particle = abi.ptr(self.particle, C.c_float)
+        b.particle_pdg = abi.ptr(self.particle_pdg, C.c_int32)
+        return b
+
+    def subset(self, idx):
+        """A new Batch holding tracks `idx` (in that order)."""
+        idx = np.asarray(idx, dtype=np.int64)
+        so, mo = self.seq_offsets, self.meas_offsets
+        out = Batch(len(idx), self.cap)
+        seq, ms, mv, mc, tm, mol = [], [], [], [], [], []
+        for j, t in enumerate(idx):
+            a, b = so[t], so[t + 1]
+            seq.append(self.seq_surfaces[a:b])
+            out.seq_offsets[j + 1] = out.seq_offsets[j] + (b - a)
+            a, b = mo[t], mo[t + 1]
+            ms.append(self.meas_surfaces[a:b])
+            mv.append(self.meas_values[2 * a:2 * b])
+            mc.append(self.meas_cov[4 * a:4 * b])
+            tm.append(self.truth_meas[6 * a:6 * b])
+            mol.append(self.meas_outlier[a:b])
+            out.meas_offsets[j + 1] = out.meas_offsets[j] + (b - a)
+        cat = lambda xs, dt: np.ascontiguousarray(np.concatenate(xs).astype(dt)) if xs else np.zeros(0, dt)
+        out.seq_surfaces = cat(seq, np.int32)
+        out.meas_surfaces = cat(ms, np.int32)
+        out.meas_values = cat(mv, np.float64)
+        out.meas_cov = cat(mc, np.float64)
+        out.truth_meas = cat(tm, np.float64)
+        out.meas_outlier = cat(mol, np.uint8)
+        for name, k in (("start_params", 6), ("start_cov", 36), ("start_frames", 12),
+                        ("particle", 2), ("truth_start", 6)):
+            src = getattr(self, name).reshape(self.n, k)
+            setattr(out, name, np.ascontiguousarray(src[idx].reshape(-1)))
+        out.particle_pdg = np.ascontiguousarray(self.particle_pdg[idx])
+        return out
+
+
+def generate(detector, n_tracks, seed=1, first_track=0, n_threads=None, cap=24):
+    L = lib()
+    b = Batch(n_tracks, cap)
+    o = abi.ckg_out()
+    o.max_per_track = cap
+    for name in ("seq_offsets", "seq_surfaces", "meas_offsets", "meas_surfaces", "particle_pdg"):
+        setattr(o, name, abi.ptr(getattr(b, name), C.c_int32))
+    for name in ("meas_values", "meas_cov", "start_params", "start_cov", "start_frames",
+                 "truth_meas", "truth_start"):
+        setattr(o, name, abi.ptr(getattr(b, name), C.c_double))
+    o.particle = abi.ptr(b.particle, C.c_float)
+    o.meas_outlier = abi.ptr(b.meas_outlier, C.c_uint8)
+    nm = L.ckg_generate(detector.preset, seed, first_track, n_tracks, detector.surfaces,
+                        detector.n_surfaces, C.byref(detector.field),
+                        n_threads or os.cpu_count() or 1, C.byref(o))
+    if nm < 0:
+        raise RuntimeError("generator failed")
+    return b.trim()
+
+
+def event_sizes(seed, n_events, mean=-1.0, lo=100, hi=20000):
+    out = np.zeros(n_events, np.int32)
+    lib().ckg_event_sizes(seed, n_events, mean, lo, hi, abi.ptr(out, C.c_int32))
+    return out

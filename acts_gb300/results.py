@@ -1,0 +1,65 @@
+"""Host-side result buffers in the ck_batch_out layout (include/cudakalman.h).
+
+Per-state arrays are structure-of-arrays with the track index innermost:
+element c of state k of track t is at [(k * C + c) * n + t]; the accessors
+below reshape them to [n, max_states, C] views for analysis.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+
+class Results:
+    def __init__(self, n, max_states=24, components=abi.OUT_ALL):
+        self.n = n
+        self.max_states = max_states
+        self.components = components
+        z = lambda k, dt: np.zeros(max_states * k * n, dt)
+        self.status = np.full(n, 11, np.int32)
+        self.n_states = np.zeros(n, np.int32)
+        self.n_measurements = np.zeros(n, np.int32)
+        self.n_holes = np.zeros(n, np.int32)
+        self.n_outliers = np.zeros(n, np.int32)
+        self.ndf = np.zeros(n, np.int32)
+        self.chi2_sum = np.zeros(n, np.float64)
+        self.state_surface = z(1, np.int32)
+        self.state_flags = z(1, np.uint32)
+        self.state_path_length = z(1, np.float64)
+        self.state_chi2 = z(1, np.float64)
+        self.predicted = z(6, np.float64) if components & abi.OUT_PREDICTED else None
+        self.predicted_cov = z(36, np.float64) if components & abi.OUT_PREDICTED else None
+        self.filtered = z(6, np.float64) if components & abi.OUT_FILTERED else None
+        self.filtered_cov = z(36, np.float64) if components & abi.OUT_FILTERED else None
+        self.smoothed = z(6, np.float64) if components & abi.OUT_SMOOTHED else None
+        self.smoothed_cov = z(36, np.float64) if components & abi.OUT_SMOOTHED else None
+        self.jacobian = z(36, np.float64) if components & abi.OUT_JACOBIAN else None
+
+    def as_batch_out(self):
+        o = abi.ck_batch_out()
+        o.max_states = self.max_states
+        o.components = self.components
+        o.memory = abi.MEM_HOST
+        for name in ("status", "n_states", "n_measurements", "n_holes", "n_outliers", "ndf",
+                     "state_surface"):
+            setattr(o, name, abi.ptr(getattr(self, name), C.c_int32))
+        o.state_flags = abi.ptr(self.state_flags, C.c_uint32)
+        for name in ("chi2_sum", "state_path_length", "state_chi2", "predicted", "predicted_cov",
+                     "filtered", "filtered_cov", "smoothed", "smoothed_cov", "jacobian"):
+            setattr(o, name, abi.ptr(getattr(self, name), C.c_double))
+        return o
+
+    def view(self, name, k=None):
+        """Array `name` as [n, max_states, C] (or [n, max_states] for scalars)."""
+        a = getattr(self, name)
+        if a is None:
+            return None
+        c = a.size // (self.max_states * self.n)
+        v = a.reshape(self.max_states, c, self.n).transpose(2, 0, 1)
+        return v[..., 0] if c == 1 else v
+
+    def track_states(self, t, name):
+        """States 0..n_states-1 of track t for array `name`."""
+        v = self.view(name)
+        return v[t, : self.n_states[t]]

@@ -1,0 +1,423 @@
+/*
+ * cudakalman.h — C ABI of ActsPlugins::CudaKalman, a batched Kalman track
+ * fitter for one NVIDIA GB300 (sm_103a).
+ *
+ * The ABI is the drop-in boundary for the reference call
+ *
+ *   Acts::KalmanFitter<Propagator<EigenStepper<>, DirectNavigator>,
+ *                      VectorMultiTrajectory>::fit(begin, end, startParameters,
+ *                                                  kfOptions, sSequence,
+ *                                                  trackContainer)
+ *   (Core/include/Acts/TrackFitting/KalmanFitter.hpp:719-731, the
+ *    DirectNavigator overload; fit_impl at :859-984)
+ *
+ * A foreign caller (ctypes, cgo, JNI, the C++ facade in
+ * acts_gb300/host/ActsPlugins/CudaKalman.hpp) binds these symbols. Every
+ * signature uses plain C types: pointers, sizes and POD structs. No C++, no
+ * torch and no CUDA types appear here; CUDA streams are passed as void*.
+ *
+ * Units are the reference's native units (Core/include/Acts/Definitions/
+ * Units.hpp:85-174): length mm, momentum/energy/mass GeV, time mm/c
+ * (1 ns = 299.792458 mm), magnetic field in GeV/(e*mm) (1 T = 0.000299792458).
+ *
+ * Parameter order follows Core/include/Acts/Definitions/TrackParametrization.hpp:
+ *   bound: loc0, loc1, phi, theta, q/p, t        (6)
+ *   free : x, y, z, t, dx, dy, dz, q/p           (8)
+ *
+ * Output arrays are structure-of-arrays with the track index innermost:
+ *   element c of state k of track t lives at  [(k * C + c) * n_tracks + t]
+ *   (C = 6 for parameter vectors, 36 for covariance / Jacobian matrices in
+ *   row-major order, 1 for scalars). Per-track scalars live at [t].
+ * States are stored in propagation order: k = 0 is the first track state and
+ * k = n_states[t]-1 is the tip (the last state that carries a source link),
+ * i.e. the order of Acts::TrackProxy::trackStates() after linkForward().
+ */
+#ifndef CUDAKALMAN_H
+#define CUDAKALMAN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CK_API_VERSION 1
+
+/* ---------------------------------------------------------------- status */
+
+/* Call-level status. */
+typedef enum ck_status {
+  CK_OK = 0,
+  CK_ERR_INVALID_ARGUMENT = 1, /* bad pointer, size or option */
+  CK_ERR_CUDA = 2,             /* a CUDA runtime call failed */
+  CK_ERR_NO_DEVICE = 3,        /* no CUDA device visible */
+  CK_ERR_OUT_OF_MEMORY = 4,    /* device allocation failed */
+  CK_ERR_UNSUPPORTED = 5,      /* a requested feature is outside the declared set */
+  CK_ERR_BUDGET = 6,           /* serving: request larger than the memory budget */
+  CK_ERR_TIMEOUT = 7,          /* a bounded wait ran out */
+  CK_ERR_NOT_READY = 8,        /* serving: nothing finished yet */
+  CK_ERR_SCRATCH_LIMIT = 9     /* request exceeds a fixed scratch capacity */
+} ck_status;
+
+/* Per-track status, one int32 per track. Mirrors the error enums the
+ * reference fit returns through Result<...>:
+ *   KalmanFitterError (Core/include/Acts/TrackFitting/KalmanFitterError.hpp:20-31)
+ *   PropagatorError::StepCountLimitReached / NextTargetLimitReached
+ *   EigenStepperError::StepSizeStalled / StepSizeAdjustmentFailed
+ *   SurfaceError::GlobalPositionNotOnSurface
+ *   MagneticFieldError::OutOfBounds                                       */
+enum {
+  CK_TRACK_OK = 0,
+  CK_TRACK_UPDATE_FAILED = 1,         /* NaN in the Kalman gain            */
+  CK_TRACK_SMOOTH_FAILED = 2,         /* NaN in the smoother gain          */
+  CK_TRACK_NO_MEASUREMENT_FOUND = 3,  /* forward filter produced no measurement */
+  CK_TRACK_STEP_COUNT_LIMIT = 4,      /* propagation exceeded maxSteps     */
+  CK_TRACK_NEXT_TARGET_LIMIT = 5,     /* maxTargetSkipping exceeded        */
+  CK_TRACK_STEP_SIZE_STALLED = 6,     /* |h| fell below stepSizeCutOff     */
+  CK_TRACK_STEP_ADJUST_FAILED = 7,    /* more than maxRungeKuttaStepTrials */
+  CK_TRACK_NOT_ON_SURFACE = 8,        /* globalToLocal failed              */
+  CK_TRACK_FIELD_OUT_OF_BOUNDS = 9,   /* grid field lookup outside the map */
+  CK_TRACK_TOO_MANY_STATES = 10,      /* more states than out->max_states  */
+  CK_TRACK_NOT_PROCESSED = 11,        /* the kernel did not reach the track */
+  CK_TRACK_INVALID_INPUT = 12         /* a surface id outside the table    */
+};
+
+/* Track-state type flags, bit positions of Acts::TrackStateFlag
+ * (Core/include/Acts/EventData/TrackStateType.hpp:30-48). */
+enum {
+  CK_FLAG_HAS_MEASUREMENT = 1u << 0,
+  CK_FLAG_HAS_PARAMETERS = 1u << 1,
+  CK_FLAG_IS_OUTLIER = 1u << 2,
+  CK_FLAG_IS_HOLE = 1u << 3,
+  CK_FLAG_HAS_MATERIAL = 1u << 4
+};
+
+/* ------------------------------------------------------------- geometry */
+
+enum { CK_SURFACE_PLANE = 0, CK_SURFACE_CYLINDER = 1 };
+enum { CK_SURF_SENSITIVE = 1, CK_SURF_MATERIAL = 2 };
+
+/* A surface of the flat surface table (the DirectNavigator sequence refers to
+ * surfaces by their index in this table).
+ *   Plane   : PlaneSurface (Core/src/Surfaces/PlaneSurface.cpp:60-191),
+ *             local frame = rotation columns, normal = column 2.
+ *   Cylinder: CylinderSurface (Core/src/Surfaces/CylinderSurface.cpp:90-277),
+ *             symmetry axis = rotation column 2, radius `radius`.
+ * Material is a homogeneous slab (HomogeneousSurfaceMaterial) with the
+ * reference's float Material fields (Core/include/Acts/Material/Material.hpp
+ * :135-145) and split factor (Core/src/Material/ISurfaceMaterial.cpp:18-46). */
+typedef struct ck_surface {
+  int32_t type;          /* CK_SURFACE_PLANE / CK_SURFACE_CYLINDER          */
+  int32_t flags;         /* CK_SURF_SENSITIVE | CK_SURF_MATERIAL            */
+  double rotation[9];    /* row-major 3x3, columns = local x, y, z axes     */
+  double center[3];
+  double radius;         /* cylinder radius (mm)                            */
+  double half_length_z;  /* cylinder bounds (used by the generator only)    */
+  double half_x, half_y; /* plane rectangle bounds (generator only)         */
+  float mat_thickness;   /* slab thickness (mm)                             */
+  float mat_x0, mat_l0;  /* radiation / nuclear interaction length (mm)     */
+  float mat_ar, mat_z;   /* relative atomic mass, nuclear charge            */
+  float mat_molar_rho;   /* molar density (mol / mm^3)                      */
+  float mat_molar_electron_rho; /* molar electron density = Z * molarRho    */
+  float mat_mean_excitation;    /* I (GeV)                                  */
+  float split_factor;    /* ISurfaceMaterial split factor (default 1)       */
+  float reserved;
+} ck_surface;
+
+/* ---------------------------------------------------------------- field */
+
+enum { CK_FIELD_CONSTANT = 0, CK_FIELD_GRID_XYZ = 1 };
+
+/* Magnetic field.
+ *   constant: ConstantBField (Core/include/Acts/MagneticField/ConstantBField.hpp:21-45)
+ *   grid    : InterpolatedBFieldMap built by fieldMapXYZ
+ *             (Core/src/MagneticField/BFieldMapUtils.cpp:106-186): grid
+ *             points at x = min[0] + i * (max[0]-min[0])/(n[0]-1), same for
+ *             y and z; trilinear interpolation (Core/include/Acts/Utilities/
+ *             Interpolation.hpp:96-120); lookups outside
+ *             [min, max) fail with CK_TRACK_FIELD_OUT_OF_BOUNDS.
+ * values: n[0]*n[1]*n[2]*3 floats in Tesla, layout [ix][iy][iz][3]. Host
+ * memory; the library copies it to the device at ck_create(). */
+typedef struct ck_field {
+  int32_t kind;
+  int32_t n[3];
+  double constant_tesla[3];
+  double min[3];
+  double max[3];
+  const float* values_tesla;
+} ck_field;
+
+/* ------------------------------------------------------------- options */
+
+enum { CK_PRECISION_FP64 = 0, CK_PRECISION_MIXED = 1 };
+
+/* Fit options. ck_options_default() fills the reference defaults:
+ *   StepperPlainOptions (Core/include/Acts/Propagator/StepperOptions.hpp:36-49)
+ *   PropagatorPlainOptions (Core/include/Acts/Propagator/PropagatorOptions.hpp:28-51)
+ *   DirectNavigator::Options (Core/include/Acts/Propagator/DirectNavigator.hpp:34-48)
+ *   KalmanFitterOptions (Core/include/Acts/TrackFitting/KalmanFitter.hpp:108-186)
+ *   GainMatrixUpdater (Joseph off) and a predicted-chi2 outlier cut
+ *   (Examples/Algorithms/TrackFitting/src/KalmanFitterFunction.cpp:60-68;
+ *    +inf = no outlier finder, the void outlier finder of the reference). */
+typedef struct ck_options {
+  double step_tolerance;        /* 1e-4                                    */
+  double step_size_cutoff;      /* 0                                       */
+  double initial_step_size;     /* 10 m                                    */
+  double max_step_size;         /* DBL_MAX                                 */
+  uint32_t max_rk_step_trials;  /* 10000                                   */
+  uint32_t max_steps;           /* 1000                                    */
+  uint32_t max_target_skipping; /* 100                                     */
+  int32_t loop_protection;      /* 1                                       */
+  double path_limit;            /* DBL_MAX                                 */
+  double loop_fraction;         /* 0.5                                     */
+  double surface_tolerance;     /* s_onSurfaceTolerance = 1e-4 mm          */
+  double near_limit;            /* DirectNavigator nearLimit = -100 um     */
+  int32_t multiple_scattering;  /* 1                                       */
+  int32_t energy_loss;          /* 1                                       */
+  int32_t use_joseph;           /* 0 (GainMatrixUpdater default)           */
+  int32_t precision;            /* CK_PRECISION_FP64 / CK_PRECISION_MIXED  */
+  double outlier_chi2_cut;      /* +inf                                    */
+  /* Extensions outside the reference's declared set are rejected with
+   * CK_ERR_UNSUPPORTED: reverse filtering, free-to-bound correction and
+   * extrapolation to a reference surface. */
+  int32_t reverse_filtering;    /* must be 0                               */
+  int32_t free_to_bound_correction; /* must be 0                           */
+  int32_t reference_surface;    /* must be -1 (none)                       */
+  int32_t reserved;
+} ck_options;
+
+/* --------------------------------------------------------------- handle */
+
+/* Static configuration of a fitter handle: the surface table and the field
+ * (both copied to the device and kept resident), tuning knobs and the device
+ * ordinal. */
+typedef struct ck_config {
+  int32_t device;              /* CUDA device ordinal                       */
+  int32_t n_surfaces;
+  const ck_surface* surfaces;  /* host pointer, copied                      */
+  ck_field field;              /* field values copied                       */
+  int32_t threads_per_block;   /* 0 = autotuned / default                   */
+  int32_t blocks_per_sm;       /* 0 = autotuned / default                   */
+  int32_t use_graph;           /* capture the batch pipeline in a CUDA graph */
+  int32_t reserved;
+  const char* autotune_cache;  /* path of the autotuner cache file or NULL  */
+} ck_config;
+
+typedef struct ck_handle ck_handle;
+
+/* Where the pointers of a batch live. */
+enum { CK_MEM_HOST = 0, CK_MEM_DEVICE = 1 };
+
+/* One batch of independent track fits: for every track the source links
+ * (calibrated 2D measurements on loc0/loc1, the pass-through calibrator of
+ * the reference tests), the start parameters with covariance on a per-track
+ * start plane, the particle hypothesis and the DirectNavigator surface
+ * sequence. CSR offsets have n_tracks+1 entries. */
+typedef struct ck_batch_in {
+  int32_t n_tracks;
+  int32_t memory;                /* CK_MEM_HOST or CK_MEM_DEVICE            */
+  const int32_t* seq_offsets;    /* [n_tracks+1]                            */
+  const int32_t* seq_surfaces;   /* [seq_offsets[n_tracks]] surface ids     */
+  const int32_t* meas_offsets;   /* [n_tracks+1]                            */
+  const int32_t* meas_surfaces;  /* [n_meas] surface id of each source link */
+  const double* meas_values;     /* [n_meas*2] (loc0, loc1)                 */
+  const double* meas_cov;        /* [n_meas*4] row-major 2x2                */
+  const double* start_params;    /* [n_tracks*6] bound parameters           */
+  const double* start_cov;       /* [n_tracks*36] row-major                 */
+  const double* start_frames;    /* [n_tracks*12] start plane: rotation (9,
+                                    row-major, columns = local axes) + center */
+  const float* particle;         /* [n_tracks*2] (mass GeV, |q|)            */
+  const int32_t* particle_pdg;   /* [n_tracks] absolute PDG id              */
+} ck_batch_in;
+
+/* Which per-state components to write (TrackStatePropMask analogue). */
+enum {
+  CK_OUT_PREDICTED = 1u << 0,
+  CK_OUT_FILTERED = 1u << 1,
+  CK_OUT_SMOOTHED = 1u << 2,
+  CK_OUT_JACOBIAN = 1u << 3
+};
+
+/* Results of a batch. Arrays the component mask does not select may be NULL.
+ * Layout: see the header comment (SoA, track index innermost). */
+typedef struct ck_batch_out {
+  int32_t max_states;        /* capacity per track                          */
+  uint32_t components;       /* CK_OUT_* mask                               */
+  int32_t memory;            /* CK_MEM_HOST or CK_MEM_DEVICE                */
+  int32_t reserved;
+  /* per track [n_tracks] */
+  int32_t* status;
+  int32_t* n_states;
+  int32_t* n_measurements;
+  int32_t* n_holes;
+  int32_t* n_outliers;
+  int32_t* ndf;
+  double* chi2_sum;          /* sum of measurement-state chi2                */
+  /* per state [max_states * C * n_tracks] */
+  int32_t* state_surface;    /* surface id (C = 1)                           */
+  uint32_t* state_flags;     /* CK_FLAG_* (C = 1)                            */
+  double* state_path_length; /* accumulated path at the state (C = 1)        */
+  double* state_chi2;        /* filtered chi2 of measurement states (C = 1)  */
+  double* predicted;         /* C = 6  */
+  double* predicted_cov;     /* C = 36 */
+  double* filtered;          /* C = 6  */
+  double* filtered_cov;      /* C = 36 */
+  double* smoothed;          /* C = 6  */
+  double* smoothed_cov;      /* C = 36 */
+  double* jacobian;          /* C = 36, transport from the previous state   */
+} ck_batch_out;
+
+/* Fills the reference defaults (see ck_options). Replaces the default member
+ * initialisers of the reference option structs. */
+void ck_options_default(ck_options* opt);
+
+/* Library and device information. */
+int32_t ck_api_version(void);
+const char* ck_status_string(ck_status s);
+const char* ck_last_error(void); /* thread-local message of the last failure */
+
+/* Creates a fitter handle: uploads the surface table and the field, creates
+ * the handle's stream and loads (or runs) the autotuner. Replaces the
+ * construction of KalmanFitter<Propagator<EigenStepper, DirectNavigator>>
+ * with its field provider (KalmanFitter.hpp:264-269, EigenStepper.ipp:20-22). */
+ck_status ck_create(const ck_config* cfg, ck_handle** out);
+ck_status ck_destroy(ck_handle* h);
+
+/* Fits every track of the batch: forward Kalman filter, then the RTS
+ * gain-matrix smoother (KalmanFitter::fit_impl, KalmanFitter.hpp:859-984),
+ * for the declared extension set (pass-through calibrator, GainMatrixUpdater,
+ * GainMatrixSmoother, predicted-chi2 outlier finder). Asynchronous on
+ * `stream` (NULL = the handle's stream); host-memory batches are staged
+ * through pinned buffers. Call ck_sync() before reading host outputs. */
+ck_status ck_fit_batch(ck_handle* h, const ck_options* opt,
+                       const ck_batch_in* in, ck_batch_out* out, void* stream);
+ck_status ck_sync(ck_handle* h);
+
+/* Kernel-only timing of the most recent batch (CUDA events recorded on the
+ * launching stream around the fit kernel): milliseconds. */
+ck_status ck_last_kernel_ms(ck_handle* h, double* ms);
+
+/* Number of kernels launched by the most recent ck_fit_batch call. */
+ck_status ck_last_launch_count(ck_handle* h, int32_t* n);
+
+/* Host<->device bytes moved by the most recent ck_fit_batch call (0 for
+ * device-resident batches). */
+ck_status ck_last_transfer_bytes(ck_handle* h, int64_t* h2d_bytes,
+                                 int64_t* d2h_bytes);
+
+/* Launch shape of the fit kernel (after autotuning). */
+ck_status ck_get_launch_config(ck_handle* h, int32_t precision,
+                               int32_t* threads_per_block,
+                               int32_t* blocks_per_sm);
+
+/* Pins the launch shape: register-cap variant (0: 255, 1: 168, 2: 128
+ * registers per thread), threads per block (multiple of 32, <= 128) and
+ * resident blocks per SM. */
+ck_status ck_set_launch_config(ck_handle* h, int32_t precision, int32_t variant,
+                               int32_t threads_per_block, int32_t blocks_per_sm);
+
+/* Enables (default) or disables ordering the work queue by descending
+ * surface-sequence length before the fit. */
+ck_status ck_sort_queue(ck_handle* h, int32_t enable);
+
+/* Text log of the last autotuner sweep (variant, block, blocks/SM, ms). */
+const char* ck_autotune_log(ck_handle* h);
+
+/* sizeof() of ck_surface, ck_field, ck_options, ck_config, ck_batch_in,
+ * ck_batch_out, ck_server_config (in that order), for binding checks. */
+void ck_abi_struct_sizes(int64_t* out, int32_t n);
+
+/* Runs the autotuner for `precision` on the given device-resident batch:
+ * sweeps threads per block and resident blocks per SM, times each variant
+ * with CUDA events and stores the fastest in the handle (and the cache file
+ * given at creation). */
+ck_status ck_autotune(ck_handle* h, const ck_options* opt,
+                      const ck_batch_in* in_device, ck_batch_out* out_device);
+
+/* ---------------------------------------------- unit operators (batched) */
+
+/* GainMatrixUpdater::operator() for N = 2 (loc0, loc1) on a batch of track
+ * states (Core/include/Acts/TrackFitting/detail/GainMatrixUpdaterImpl.hpp
+ * :21-91). Arrays are AoS per state: predicted[6], predicted_cov[36],
+ * meas[2], meas_cov[4]; outputs filtered[6], filtered_cov[36], chi2[1],
+ * status[1] (CK_TRACK_OK or CK_TRACK_UPDATE_FAILED). Host pointers;
+ * synchronous. */
+ck_status ck_gain_matrix_update(ck_handle* h, int32_t n, int32_t use_joseph,
+                                const double* predicted,
+                                const double* predicted_cov,
+                                const double* meas, const double* meas_cov,
+                                double* filtered, double* filtered_cov,
+                                double* chi2, int32_t* status);
+
+/* GainMatrixSmoother::operator() (Core/include/Acts/TrackFitting/
+ * GainMatrixSmoother.hpp:43-99, Core/src/TrackFitting/GainMatrixSmoother.cpp
+ * :18-97) on n_traj independent trajectories of n_states each, in forward
+ * order; AoS per state: predicted[6], predicted_cov[36], filtered[6],
+ * filtered_cov[36], jacobian[36]; outputs smoothed[6], smoothed_cov[36];
+ * status per trajectory. Host pointers; synchronous. */
+ck_status ck_gain_matrix_smooth(ck_handle* h, int32_t n_traj, int32_t n_states,
+                                const double* predicted,
+                                const double* predicted_cov,
+                                const double* filtered,
+                                const double* filtered_cov,
+                                const double* jacobian, double* smoothed,
+                                double* smoothed_cov, int32_t* status);
+
+/* Pointwise material effects (computeMaterialEffects,
+ * Core/src/Propagator/detail/PointwiseMaterialInteraction.cpp:49-90) for a
+ * batch of (slab, direction, q/p) inputs on the device: per input the
+ * surface id (its slab, scaled by `thickness_scale`), direction[3], q/p,
+ * mass, |q|, pdg; outputs eLoss, variancePhi, varianceTheta, varianceQOverP
+ * as double[4]. Host pointers; synchronous. */
+ck_status ck_material_effects(ck_handle* h, int32_t n, const int32_t* surface,
+                              const float* thickness_scale,
+                              const double* direction, const double* qop,
+                              const float* mass, const float* abs_q,
+                              const int32_t* pdg, int32_t multiple_scattering,
+                              int32_t energy_loss, double* effects);
+
+/* Field lookup on the device for n positions (getField of the handle's
+ * field); out[3*n] in GeV/(e*mm); status per point. Host pointers. */
+ck_status ck_field_lookup(ck_handle* h, int32_t n, const double* pos,
+                          double* out, int32_t* status);
+
+/* ------------------------------------------------------------- serving */
+
+/* Continuous-batching serving loop (host request thread + device-resident
+ * slot pool). Events are admitted against `memory_budget_bytes` as slots and
+ * memory free up; admitted events are co-batched and their fits overlap on
+ * the device across `n_streams` streams. */
+typedef struct ck_server ck_server;
+
+typedef struct ck_server_config {
+  int64_t memory_budget_bytes; /* device memory the pool may hold           */
+  int32_t n_streams;           /* concurrent batches in flight              */
+  int32_t max_states;          /* per-track state capacity                  */
+  int32_t max_batch_tracks;    /* largest co-batch                          */
+  uint32_t components;         /* CK_OUT_* written back to the host         */
+} ck_server_config;
+
+ck_status ck_server_create(ck_handle* h, const ck_options* opt,
+                           const ck_server_config* cfg, ck_server** out);
+/* Queues one event (host memory; the input is copied before return).
+ * Returns CK_ERR_BUDGET when the event alone exceeds the budget. */
+ck_status ck_server_submit(ck_server* s, int64_t event_id,
+                           const ck_batch_in* event);
+/* Pops one finished event: its id, the per-track outputs copied into `out`
+ * (host memory, sized for the event) and its latency in ms (submit to
+ * completion). CK_ERR_NOT_READY when none has finished; waits up to
+ * timeout_ms. */
+ck_status ck_server_poll(ck_server* s, int64_t* event_id, ck_batch_out* out,
+                         int32_t out_capacity_tracks, double* latency_ms,
+                         int32_t timeout_ms);
+/* Counters: events submitted, completed, tracks completed, bytes in use. */
+ck_status ck_server_stats(ck_server* s, int64_t* submitted, int64_t* completed,
+                          int64_t* tracks, int64_t* bytes_in_use);
+ck_status ck_server_destroy(ck_server* s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUDAKALMAN_H */

@@ -1,0 +1,255 @@
+// kf_oracle_capi.cpp — C entry points of the CPU oracle (test infrastructure).
+//
+// Loaded only by tests/, __graft_entry__.smoke() and bench.py's CPU legs,
+// always as the checker or the timed CPU baseline, never as the product.
+// Inputs and outputs use the public structs of include/cudakalman.h so that
+// the oracle and the CUDA fitter are fed from and compared on the very same
+// arrays.
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <thread>
+#include <vector>
+
+#include "kf_oracle.hpp"
+
+using namespace kfo;
+
+namespace {
+
+struct Ctx {
+  std::vector<Surface<double>> surfaces;
+  Fitter<double> fitter;
+};
+
+void writeTrack(const TrackOut& t, int tr, int n, const ck_batch_out* out) {
+  const int ms = out->max_states;
+  out->status[tr] = t.status;
+  if (out->n_states) out->n_states[tr] = (int)t.states.size();
+  if (out->n_measurements) out->n_measurements[tr] = t.nMeasurements;
+  if (out->n_holes) out->n_holes[tr] = t.nHoles;
+  if (out->n_outliers) out->n_outliers[tr] = t.nOutliers;
+  if (out->ndf) out->ndf[tr] = t.ndf;
+  if (out->chi2_sum) out->chi2_sum[tr] = t.chi2;
+  const int ns = (int)t.states.size();
+  if (ns > ms) {
+    out->status[tr] = CK_TRACK_TOO_MANY_STATES;
+    if (out->n_states) out->n_states[tr] = 0;
+    return;
+  }
+  auto at = [&](int k, int C, int c) -> size_t { return ((size_t)k * C + c) * n + tr; };
+  for (int k = 0; k < ns; ++k) {
+    const TrackOut::St& s = t.states[k];
+    if (out->state_surface) out->state_surface[at(k, 1, 0)] = s.surface;
+    if (out->state_flags) out->state_flags[at(k, 1, 0)] = s.flags;
+    if (out->state_path_length) out->state_path_length[at(k, 1, 0)] = s.pathLength;
+    if (out->state_chi2) out->state_chi2[at(k, 1, 0)] = s.chi2;
+    for (int c = 0; c < 6; ++c) {
+      if (out->predicted) out->predicted[at(k, 6, c)] = s.pred[c];
+      if (out->filtered) out->filtered[at(k, 6, c)] = s.filt[c];
+      if (out->smoothed) out->smoothed[at(k, 6, c)] = s.smth[c];
+    }
+    for (int c = 0; c < 36; ++c) {
+      if (out->predicted_cov) out->predicted_cov[at(k, 36, c)] = s.predCov[c];
+      if (out->filtered_cov) out->filtered_cov[at(k, 36, c)] = s.filtCov[c];
+      if (out->smoothed_cov) out->smoothed_cov[at(k, 36, c)] = s.smthCov[c];
+      if (out->jacobian) out->jacobian[at(k, 36, c)] = s.jac[c];
+    }
+  }
+}
+
+void fitOne(const Ctx& ctx, const ck_batch_in* in, int tr, TrackOut& t) {
+  const int ns = (int)ctx.surfaces.size();
+  for (int k = in->seq_offsets[tr]; k < in->seq_offsets[tr + 1]; ++k)
+    if (in->seq_surfaces[k] < 0 || in->seq_surfaces[k] >= ns) {
+      t.status = CK_TRACK_INVALID_INPUT;
+      return;
+    }
+  for (int k = in->meas_offsets[tr]; k < in->meas_offsets[tr + 1]; ++k)
+    if (in->meas_surfaces[k] < 0 || in->meas_surfaces[k] >= ns) {
+      t.status = CK_TRACK_INVALID_INPUT;
+      return;
+    }
+  std::vector<MeasRec<double>> meas;
+  for (int m = in->meas_offsets[tr]; m < in->meas_offsets[tr + 1]; ++m) {
+    MeasRec<double> r;
+    r.surface = in->meas_surfaces[m];
+    r.v[0] = in->meas_values[2 * m];
+    r.v[1] = in->meas_values[2 * m + 1];
+    for (int c = 0; c < 4; ++c) r.cov[c] = in->meas_cov[4 * m + c];
+    meas.push_back(r);
+  }
+  Surface<double> start = Surface<double>::plane(in->start_frames + 12 * (size_t)tr);
+  Vec<double, 6> sp = get6<double>(in->start_params + 6 * (size_t)tr);
+  Mat<double, 6, 6> sc = get36<double>(in->start_cov + 36 * (size_t)tr);
+  const int s0 = in->seq_offsets[tr], s1 = in->seq_offsets[tr + 1];
+  ctx.fitter.fit(start, sp, sc, in->particle[2 * tr], in->particle[2 * tr + 1],
+                 in->particle_pdg ? in->particle_pdg[tr] : 211, in->seq_surfaces + s0, s1 - s0,
+                 meas, t);
+}
+
+}  // namespace
+
+extern "C" {
+
+// Fits a host-memory batch on `n_threads` host threads (dynamic scheduling
+// over tracks). `coast` = 1 reproduces the reference termination exactly
+// (propagation continues to the path limit when outliers keep the track
+// incomplete); 0 stops after the last surface that carries a source link,
+// the termination rule of the CUDA fitter. Returns the wall time in seconds.
+double kfo_fit_batch(const ck_options* opt, int n_surfaces, const ck_surface* surfaces,
+                     const ck_field* field, const ck_batch_in* in, const ck_batch_out* out,
+                     int n_threads, int coast, int first, int count) {
+  Ctx ctx;
+  for (int i = 0; i < n_surfaces; ++i) ctx.surfaces.push_back(Surface<double>::fromCk(surfaces[i]));
+  ctx.fitter.surfaces = &ctx.surfaces;
+  ctx.fitter.field = Field<double>::make(*field);
+  ctx.fitter.mc = MatConst::make();
+  ctx.fitter.o = Options::fromCk(*opt, coast != 0);
+  const int n = in->n_tracks;
+  if (count < 0) count = n - first;
+  if (n_threads < 1) n_threads = 1;
+  std::atomic<int> next{first};
+  const int end = first + count;
+  auto t0 = std::chrono::steady_clock::now();
+  auto worker = [&]() {
+    TrackOut t;
+    while (true) {
+      int tr = next.fetch_add(1);
+      if (tr >= end) break;
+      t = TrackOut();
+      fitOne(ctx, in, tr, t);
+      if (out) writeTrack(t, tr, n, out);
+    }
+  };
+  if (n_threads == 1) {
+    worker();
+  } else {
+    std::vector<std::thread> th;
+    for (int i = 0; i < n_threads; ++i) th.emplace_back(worker);
+    for (auto& x : th) x.join();
+  }
+  auto t1 = std::chrono::steady_clock::now();
+  return std::chrono::duration<double>(t1 - t0).count();
+}
+
+// GainMatrixUpdater on n states (AoS), as ck_gain_matrix_update.
+void kfo_gain_matrix_update(int n, int joseph, const double* pred, const double* predCov,
+                            const double* meas, const double* measCov, double* filt,
+                            double* filtCov, double* chi2, int* status) {
+  for (int i = 0; i < n; ++i) {
+    Vec<double, 6> p = get6<double>(pred + 6 * i), f;
+    Mat<double, 6, 6> P = get36<double>(predCov + 36 * i), F;
+    double c2 = 0;
+    bool ok = gainMatrixUpdate(p, P, meas + 2 * i, measCov + 4 * i, joseph != 0, f, F, c2);
+    status[i] = ok ? CK_TRACK_OK : CK_TRACK_UPDATE_FAILED;
+    if (ok) {
+      put6(filt + 6 * i, f);
+      put36(filtCov + 36 * i, F);
+      chi2[i] = c2;
+    }
+  }
+}
+
+// GainMatrixSmoother on n_traj trajectories of n_states (forward order).
+void kfo_gain_matrix_smooth(int n_traj, int n_states, const double* pred, const double* predCov,
+                            const double* filt, const double* filtCov, const double* jac,
+                            double* smth, double* smthCov, int* status) {
+  for (int t = 0; t < n_traj; ++t) {
+    size_t b = (size_t)t * n_states;
+    int last = n_states - 1;
+    std::vector<Vec<double, 6>> S(n_states);
+    std::vector<Mat<double, 6, 6>> SC(n_states);
+    S[last] = get6<double>(filt + 6 * (b + last));
+    SC[last] = get36<double>(filtCov + 36 * (b + last));
+    status[t] = CK_TRACK_OK;
+    for (int k = last - 1; k >= 0; --k) {
+      bool ok = smoothStep(get6<double>(filt + 6 * (b + k)), get36<double>(filtCov + 36 * (b + k)),
+                           get6<double>(pred + 6 * (b + k + 1)),
+                           get36<double>(predCov + 36 * (b + k + 1)),
+                           get36<double>(jac + 36 * (b + k + 1)), S[k + 1], SC[k + 1], S[k], SC[k]);
+      if (!ok) {
+        status[t] = CK_TRACK_SMOOTH_FAILED;
+        break;
+      }
+    }
+    for (int k = 0; k < n_states; ++k) {
+      put6(smth + 6 * (b + k), S[k]);
+      put36(smthCov + 36 * (b + k), SC[k]);
+    }
+  }
+}
+
+// Interactions.cpp entry points for the material known-answer tests.
+// slab: thickness, X0, L0, Ar, Z, molarRho (mol/mm^3); which: 0 Bethe,
+// 1 Landau (most probable), 2 Landau sigma(q/p), 3 theta0, 4 Landau FWHM.
+float kfo_interaction(int which, float thickness, float X0, float L0, float Ar, float Z,
+                      float molarRho, int absPdg, float m, float qOverP, float absQ) {
+  ck_surface cs{};
+  cs.mat_thickness = thickness;
+  cs.mat_x0 = X0;
+  cs.mat_l0 = L0;
+  cs.mat_ar = Ar;
+  cs.mat_z = Z;
+  cs.mat_molar_rho = molarRho;
+  cs.mat_molar_electron_rho = Z * molarRho;
+  cs.mat_mean_excitation = (float)(lit_eV(16.0L) * std::pow(Z, 0.9f));
+  Slab s = Slab::make(cs);
+  MatConst C = MatConst::make();
+  switch (which) {
+    case 0:
+      return computeEnergyLossBethe(C, s, m, qOverP, absQ);
+    case 1:
+      return computeEnergyLossLandau(C, s, m, qOverP, absQ);
+    case 2:
+      return computeEnergyLossLandauSigmaQOverP(C, s, m, qOverP, absQ);
+    case 3:
+      return computeMultipleScatteringTheta0(C, s, absPdg, m, qOverP, absQ);
+    case 4: {
+      RelQ rq(m, qOverP, absQ);
+      return computeEnergyLossLandauFwhm(C, s, rq);
+    }
+    default:
+      return 0.0f;
+  }
+}
+
+// Material effects for a surface slab scaled by `scale` (as the fitter's
+// pathCorrection * split factor); returns eLoss, varPhi, varTheta, varQoP.
+void kfo_material_effects(const ck_surface* cs, float scale, const double* dir, double qop,
+                          float mass, float absQ, int pdg, int ms, int el, double* outv) {
+  Slab s = Slab::make(*cs);
+  s.scaleThickness(scale);
+  V3<double> d{{dir[0], dir[1], dir[2]}};
+  MatEffects e = computeMaterialEffects<double>(MatConst::make(), s, pdg, mass, absQ, d,
+                                                (float)qop, ms != 0, el != 0);
+  outv[0] = e.eLoss;
+  outv[1] = e.variancePhi;
+  outv[2] = e.varianceTheta;
+  outv[3] = e.varianceQoverP;
+}
+
+// Field lookup (status 0 ok, CK_TRACK_FIELD_OUT_OF_BOUNDS otherwise).
+void kfo_field_lookup(const ck_field* f, int n, const double* pos, double* outB, int* status) {
+  Field<double> F = Field<double>::make(*f);
+  for (int i = 0; i < n; ++i) {
+    V3<double> p{{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]}}, b;
+    bool ok = F.get(p, b);
+    status[i] = ok ? 0 : CK_TRACK_FIELD_OUT_OF_BOUNDS;
+    for (int c = 0; c < 3; ++c) outB[3 * i + c] = ok ? b[c] : 0.0;
+  }
+}
+
+// Counts how often glibc logf differs from the correctly rounded float
+// logarithm used by both implementations, over n inputs.
+int kfo_logf_mismatch(int n, const float* x) {
+  int bad = 0;
+  for (int i = 0; i < n; ++i)
+    if (std::log(x[i]) != ck_logf(x[i])) ++bad;
+  return bad;
+}
+
+int kfo_hardware_threads() { return (int)std::thread::hardware_concurrency(); }
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+"""ctypes binding of the CPU oracle (oracle/_build/libkforacle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU legs as the checker or the timed CPU baseline. The product
+package acts_gb300 never imports this module.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from acts_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libkforacle.so")
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+        L = C.CDLL(LIB)
+        L.kfo_fit_batch.restype = C.c_double
+        L.kfo_fit_batch.argtypes = [C.POINTER(abi.ck_options), C.c_int, C.POINTER(abi.ck_surface),
+                                    C.POINTER(abi.ck_field), C.POINTER(abi.ck_batch_in),
+                                    C.POINTER(abi.ck_batch_out), C.c_int, C.c_int, C.c_int,
+                                    C.c_int]
+        L.kfo_gain_matrix_update.restype = None
+        L.kfo_gain_matrix_update.argtypes = [C.c_int, C.c_int] + [abi.P_f64] * 7 + [abi.P_i32]
+        L.kfo_gain_matrix_smooth.restype = None
+        L.kfo_gain_matrix_smooth.argtypes = [C.c_int, C.c_int] + [abi.P_f64] * 7 + [abi.P_i32]
+        L.kfo_interaction.restype = C.c_float
+        L.kfo_interaction.argtypes = [C.c_int] + [C.c_float] * 6 + [C.c_int] + [C.c_float] * 3
+        L.kfo_material_effects.restype = None
+        L.kfo_material_effects.argtypes = [C.POINTER(abi.ck_surface), C.c_float, abi.P_f64,
+                                           C.c_double, C.c_float, C.c_float, C.c_int, C.c_int,
+                                           C.c_int, abi.P_f64]
+        L.kfo_field_lookup.restype = None
+        L.kfo_field_lookup.argtypes = [C.POINTER(abi.ck_field), C.c_int, abi.P_f64, abi.P_f64,
+                                       abi.P_i32]
+        L.kfo_logf_mismatch.restype = C.c_int
+        L.kfo_logf_mismatch.argtypes = [C.c_int, abi.P_f32]
+        L.kfo_hardware_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def fit_batch(detector, batch, options, results, n_threads=1, coast=False, first=0, count=-1):
+    """Fits `batch` (acts_gb300.generate.Batch) into `results`
+    (acts_gb300.results.Results). Returns the wall time in seconds."""
+    bi = batch.as_batch_in()
+    bo = results.as_batch_out()
+    return lib().kfo_fit_batch(C.byref(options), detector.n_surfaces, detector.surfaces,
+                               C.byref(detector.field), C.byref(bi), C.byref(bo), n_threads,
+                               1 if coast else 0, first, count)
+
+
+def time_batch(detector, batch, options, n_threads, first=0, count=-1):
+    """Fits without writing results (CPU baseline timing)."""
+    bi = batch.as_batch_in()
+    return lib().kfo_fit_batch(C.byref(options), detector.n_surfaces, detector.surfaces,
+                               C.byref(detector.field), C.byref(bi), None, n_threads, 0, first,
+                               count)
+
+
+def gain_matrix_update(pred, pred_cov, meas, meas_cov, joseph=False):
+    n = pred.shape[0]
+    f = np.zeros((n, 6))
+    fc = np.zeros((n, 36))
+    chi2 = np.zeros(n)
+    st = np.zeros(n, np.int32)
+    args = [np.ascontiguousarray(x, dtype=np.float64) for x in (pred, pred_cov, meas, meas_cov)]
+    lib().kfo_gain_matrix_update(n, int(joseph), *[abi.ptr(a, C.c_double) for a in args],
+                                 abi.ptr(f, C.c_double), abi.ptr(fc, C.c_double),
+                                 abi.ptr(chi2, C.c_double), abi.ptr(st, C.c_int32))
+    return f, fc.reshape(n, 6, 6), chi2, st
+
+
+def gain_matrix_smooth(pred, pred_cov, filt, filt_cov, jac):
+    """Arrays shaped [n_traj, n_states, ...]."""
+    nt, ns = pred.shape[:2]
+    s = np.zeros((nt, ns, 6))
+    sc = np.zeros((nt, ns, 36))
+    st = np.zeros(nt, np.int32)
+    args = [np.ascontiguousarray(x, dtype=np.float64) for x in (pred, pred_cov, filt, filt_cov, jac)]
+    lib().kfo_gain_matrix_smooth(nt, ns, *[abi.ptr(a, C.c_double) for a in args],
+                                 abi.ptr(s, C.c_double), abi.ptr(sc, C.c_double),
+                                 abi.ptr(st, C.c_int32))
+    return s, sc.reshape(nt, ns, 6, 6), st
+
+
+def interaction(which, thickness, X0, L0, Ar, Z, molar_rho, pdg, m, qop, absq):
+    return lib().kfo_interaction(which, thickness, X0, L0, Ar, Z, molar_rho, pdg, m, qop, absq)
+
+
+def material_effects(surface, scale, direction, qop, mass, absq, pdg, ms=True, el=True):
+    out = np.zeros(4)
+    d = np.ascontiguousarray(direction, dtype=np.float64)
+    lib().kfo_material_effects(C.byref(surface), scale, abi.ptr(d, C.c_double), qop, mass, absq,
+                               pdg, int(ms), int(el), abi.ptr(out, C.c_double))
+    return out
+
+
+def field_lookup(field, pos):
+    pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros_like(pos)
+    st = np.zeros(len(pos), np.int32)
+    lib().kfo_field_lookup(C.byref(field), len(pos), abi.ptr(pos, C.c_double),
+                           abi.ptr(out, C.c_double), abi.ptr(st, C.c_int32))
+    return out, st
+
+
+def logf_mismatch(x):
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    return lib().kfo_logf_mismatch(len(x), abi.ptr(x, C.c_float))
+
+
+def hardware_threads():
+    return lib().kfo_hardware_threads()

@@ -1,0 +1,68 @@
+"""Comparison of two Results (CUDA fitter vs oracle) with the stated
+tolerances: integers and flags bit-exact; floating point within `rtol`
+relative to max(|a|, |b|, natural scale of the entry)."""
+import numpy as np
+
+from acts_gb300 import abi
+
+
+def _sig(cov):
+    # per-state standard deviations from a [..., 36] covariance
+    d = cov[..., [0, 7, 14, 21, 28, 35]]
+    return np.sqrt(np.abs(d))
+
+
+def compare(gpu, ora, rtol=1e-9, fields=("predicted", "filtered", "smoothed")):
+    """Returns a dict of max normalised errors and mismatch counts."""
+    rep = {}
+    st_g, st_o = gpu.status, ora.status
+    rep["status_mismatch"] = int(np.sum(st_g != st_o))
+    ok = (st_g == 0) & (st_o == 0)
+    rep["n_ok"] = int(ok.sum())
+    for name in ("n_states", "n_measurements", "n_holes", "n_outliers", "ndf"):
+        rep[name + "_mismatch"] = int(np.sum(getattr(gpu, name)[ok] != getattr(ora, name)[ok]))
+    ms = gpu.max_states
+    valid = np.zeros((gpu.n, ms), bool)
+    for t in np.nonzero(ok)[0]:
+        valid[t, : gpu.n_states[t]] = True
+    rep["flags_mismatch"] = int(np.sum((gpu.view("state_flags") != ora.view("state_flags")) & valid))
+    rep["surface_mismatch"] = int(np.sum((gpu.view("state_surface") != ora.view("state_surface")) & valid))
+
+    def rel(a, b, floor):
+        return np.abs(a - b) / np.maximum(np.maximum(np.abs(a), np.abs(b)), floor)
+
+    m = valid
+    for name in ("state_path_length", "state_chi2"):
+        a, b = gpu.view(name)[m], ora.view(name)[m]
+        rep[name] = float(rel(a, b, 1.0).max()) if a.size else 0.0
+    rep["chi2_sum"] = float(rel(gpu.chi2_sum[ok], ora.chi2_sum[ok], 1.0).max()) if ok.any() else 0.0
+    for name in fields:
+        pa, pb = gpu.view(name), ora.view(name)
+        ca, cb = gpu.view(name + "_cov"), ora.view(name + "_cov")
+        if pa is None or pb is None:
+            continue
+        sig = _sig(cb)
+        rp = rel(pa, pb, sig)[m]
+        rep[name] = float(rp.max()) if rp.size else 0.0
+        scale = np.sqrt(np.abs(cb[..., [0, 7, 14, 21, 28, 35]]))
+        floor = (scale[..., :, None] * scale[..., None, :]).reshape(scale.shape[:-1] + (36,))
+        rc = rel(ca, cb, floor)[m]
+        rep[name + "_cov"] = float(rc.max()) if rc.size else 0.0
+    ja, jb = gpu.view("jacobian"), ora.view("jacobian")
+    if ja is not None and jb is not None:
+        jr = jb.reshape(jb.shape[:-1] + (6, 6))
+        rowmax = np.abs(jr).max(axis=-1, keepdims=True) * 1e-6
+        floor = np.broadcast_to(rowmax, jr.shape).reshape(jb.shape)
+        r = rel(ja, jb, floor)[m]
+        rep["jacobian"] = float(r.max()) if r.size else 0.0
+    return rep
+
+
+def assert_parity(rep, rtol=1e-9):
+    for k, v in rep.items():
+        if k.endswith("_mismatch"):
+            assert v == 0, (k, rep)
+    for k in ("state_path_length", "state_chi2", "chi2_sum", "predicted", "predicted_cov",
+              "filtered", "filtered_cov", "smoothed", "smoothed_cov", "jacobian"):
+        if k in rep:
+            assert rep[k] <= rtol, (k, rep[k], rep)

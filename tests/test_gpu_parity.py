@@ -1,0 +1,37 @@
+"""CUDA fitter (plain FP64 form) against the CPU oracle on the same seeded
+inputs: statuses, state counts, surfaces and type flags bit-exact; fitted
+parameters, covariances, Jacobians, path lengths and chi2 within 1e-9
+relative (scale floors: parameter sigma, sqrt(C_ii C_jj), 1 for chi2/path).
+"""
+import numpy as np
+import pytest
+
+from acts_gb300 import abi
+from acts_gb300.results import Results
+from conftest import batch, detector
+from oracle import kforacle
+from parity import assert_parity, compare
+
+RTOL = 1e-9
+
+CASES = [
+    ("telescope", abi.CKG_TELESCOPE, 1000, dict()),
+    ("barrel", abi.CKG_BARREL, 2000, dict()),
+    ("barrel_joseph", abi.CKG_BARREL, 1000, dict(use_joseph=1)),
+    ("uneven", abi.CKG_UNEVEN, 2000, dict(outlier_chi2_cut=15.0)),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,preset,n,kw", CASES, ids=[c[0] for c in CASES])
+def test_fp64_parity(fitter_factory, name, preset, n, kw):
+    det = detector(preset)
+    b = batch(preset, n)
+    opt = abi.default_options(**kw)
+    ora = Results(n, 24)
+    kforacle.fit_batch(det, b, opt, ora, n_threads=kforacle.hardware_threads())
+    gpu = fitter_factory(preset).fit_batch(b, opt, max_states=24)
+    rep = compare(gpu, ora, RTOL)
+    print(name, rep)
+    assert rep["n_ok"] > 0.9 * n
+    assert_parity(rep, RTOL)
