@@ -130,7 +130,7 @@ class ck_options(C.Structure):
         ("reverse_filtering", C.c_int32),
         ("free_to_bound_correction", C.c_int32),
         ("reference_surface", C.c_int32),
-        ("reserved", C.c_int32),
+        ("early_termination", C.c_int32),
     ]
 
 
@@ -255,6 +255,7 @@ def default_options(**kw):
     o.reverse_filtering = 0
     o.free_to_bound_correction = 0
     o.reference_surface = -1
+    o.early_termination = 0
     for k, v in kw.items():
         setattr(o, k, v)
     return o

@@ -111,6 +111,7 @@ DevOptions toDevOptions(const ck_options& o) {
   d.energyLoss = o.energy_loss;
   d.joseph = o.use_joseph;
   d.useOutlierCut = std::isinf(o.outlier_chi2_cut) ? 0 : 1;
+  d.earlyTermination = o.early_termination;
   return d;
 }
 
@@ -322,6 +323,7 @@ void ck_options_default(ck_options* o) {
   o->reverse_filtering = 0;
   o->free_to_bound_correction = 0;
   o->reference_surface = -1;
+  o->early_termination = 0;
 }
 
 int32_t ck_api_version(void) { return CK_API_VERSION; }

@@ -12,12 +12,13 @@
 // for the declared extension set (pass-through calibrator, GainMatrixUpdater,
 // GainMatrixSmoother, predicted-chi2 outlier finder).
 //
-// Termination differs in one documented point: the reference keeps
-// propagating after the last surface when outliers leave the track
-// "incomplete" (measurementStates < #measurements) until the loop-protection
-// path limit; states created after the last surface that carries a source
-// link are never part of the track (its tip is the last such state), so the
-// device stops there.
+// Termination follows the reference: when outliers leave the track
+// "incomplete" (measurementStates < #measurements) propagation continues
+// after the last surface until the loop-protection path limit, and errors on
+// the way (leaving the field map, step limits) fail the fit. States created
+// there lie beyond the track's tip, so this "coasting" phase transports no
+// covariance and stores no records. ck_options.early_termination stops at the
+// last surface that carries a source link instead.
 //
 // One thread fits one track; warps pull 32 consecutive queue slots at a time
 // from an atomic ticket (the queue is ordered by descending sequence length).
@@ -66,7 +67,7 @@ enum StepErr { kStepOk = 0, kStepField = 1, kStepStalled = 2, kStepAdjust = 3 };
 
 // EigenStepper::step with the default extension; transports T.
 template <typename P, typename CV>
-CK_D int rkStep(FitState<P, CV>& s, const DevField& F, const DevOptions& o) {
+CK_D int rkStep(FitState<P, CV>& s, const DevField& F, const DevOptions& o, bool transport) {
   const P pos[3] = {s.pars[0], s.pars[1], s.pars[2]};
   const P dir[3] = {s.pars[4], s.pars[5], s.pars[6]};
   const P qop = s.pars[7];
@@ -125,7 +126,7 @@ CK_D int rkStep(FitState<P, CV>& s, const DevField& F, const DevOptions& o) {
   const P dtds = sqrt(P(1) + mp * mp);
   s.pars[3] = s.pars[3] + h * dtds;
   s.deriv[3] = dtds;
-  {
+  if (transport) {
     P dk1dL[3], dk2dL[3], dk3dL[3], dk4dL[3], t[3];
     dk1dL[0] = dir[1] * B1[2] - dir[2] * B1[1];
     dk1dL[1] = dir[2] * B1[0] - dir[0] * B1[2];
@@ -454,6 +455,10 @@ CK_D void fitTrack(const FitParams& fp, int slot, int t) {
   int lastMeasurementIndex = -1;
   int measurementStates = 0;
   bool finished = false;
+  // After the last surface that carries a source link every further state
+  // lies beyond the track's tip: only the trajectory and the errors it may
+  // raise stay observable, so covariance and Jacobian transport stop.
+  bool coasting = false;
   int err = CK_TRACK_OK;
 
   auto intersectSurf = [&](int sid, P path[2], int st[2]) -> int {
@@ -520,6 +525,14 @@ CK_D void fitTrack(const FitParams& fp, int slot, int t) {
     const bool sensitive = (sflags & CK_SURF_SENSITIVE) != 0;
     const bool hasMat = (sflags & CK_SURF_MATERIAL) != 0;
     const bool preceding = measurementStates > 0;
+    if (coasting) {
+      if ((preceding && sensitive) || hasMat) {
+        double bp[6];
+        if (!freeToBound(s.pars, sf, bp)) return CK_TRACK_NOT_ON_SURFACE;
+        if (!material(sid, sf, 3)) return CK_TRACK_NOT_ON_SURFACE;
+      }
+      return CK_TRACK_OK;
+    }
     const int mi = findMeas(sid);
     if (mi >= 0) {
       transportToBound(s, sf);
@@ -599,8 +612,12 @@ CK_D void fitTrack(const FitParams& fp, int slot, int t) {
     }
     bool complete = measurementStates == nDistinct;
     // every later state would be created after the track's tip
-    if (!complete && lastSlSeq >= 0 && currentSurface >= 0 && surfaceIndex >= lastSlSeq)
-      complete = true;
+    if (!complete && lastSlSeq >= 0 && currentSurface >= 0 && surfaceIndex >= lastSlSeq) {
+      if (o.earlyTermination)
+        complete = true;
+      else
+        coasting = true;
+    }
     const bool pathReached = pathLimitReached(kfLimit);
     if (complete || pathReached) finished = true;
     return CK_TRACK_OK;
@@ -664,7 +681,7 @@ CK_D void fitTrack(const FitParams& fp, int slot, int t) {
     bool terminated = false;
     unsigned steps = 0;
     for (; err == CK_TRACK_OK && steps < o.maxSteps; ++steps) {
-      const int se = rkStep(s, fp.field, o);
+      const int se = rkStep(s, fp.field, o, !coasting);
       if (se != kStepOk) {
         err = se == kStepField ? CK_TRACK_FIELD_OUT_OF_BOUNDS
                                : (se == kStepStalled ? CK_TRACK_STEP_SIZE_STALLED

@@ -50,7 +50,7 @@ struct DevOptions {
   double pathLimit, loopFraction, surfaceTolerance, nearLimit, outlierChi2Cut;
   uint32_t maxRkTrials, maxSteps, maxTargetSkipping;
   int loopProtection, multipleScattering, energyLoss, joseph;
-  int useOutlierCut;
+  int useOutlierCut, earlyTermination;
 };
 
 // Record of one forward track state kept for the smoother (scratch).

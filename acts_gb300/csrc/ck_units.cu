@@ -272,3 +272,61 @@ ck_status ck_field_lookup(ck_handle* h, int32_t n, const double* pos, double* ou
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Arithmetic-pipe peak probes: independent FMA chains per thread, timed with
+// CUDA events; the roofline denominators of the FP64 / FP32 fit kernels.
+namespace {
+
+template <typename T>
+__global__ void fmaPeakKernel(T* out, int iters, T a, T b) {
+  T x0 = (T)threadIdx.x, x1 = x0 + T(1), x2 = x0 + T(2), x3 = x0 + T(3);
+  T x4 = x0 + T(4), x5 = x0 + T(5), x6 = x0 + T(6), x7 = x0 + T(7);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      x0 = fma(x0, a, b);
+      x1 = fma(x1, a, b);
+      x2 = fma(x2, a, b);
+      x3 = fma(x3, a, b);
+      x4 = fma(x4, a, b);
+      x5 = fma(x5, a, b);
+      x6 = fma(x6, a, b);
+      x7 = fma(x7, a, b);
+    }
+  }
+  const T s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+  if (s == T(-1)) out[blockIdx.x] = s;  // keeps the chains alive
+}
+
+}  // namespace
+
+extern "C" ck_status ck_fp_peak_gflops(ck_handle* h, int32_t precision, double* gflops) {
+  if (!h || !gflops) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
+  std::lock_guard<std::mutex> lock(h->mu);
+  cudaSetDevice(h->device);
+  cudaError_t e = h->unitBuf.ensure(sizeof(double) * 4096);
+  if (e != cudaSuccess) return cudaFail(e, "probe buffer");
+  const int blocks = h->smCount * 8, threads = 256;
+  const int iters = precision == CK_PRECISION_FP64 ? 64 : 2048;
+  cudaStream_t st = h->stream;
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(h->ev0, st);
+    if (precision == CK_PRECISION_FP64)
+      fmaPeakKernel<double><<<blocks, threads, 0, st>>>((double*)h->unitBuf.p, iters, 0.999999,
+                                                        1e-7);
+    else
+      fmaPeakKernel<float><<<blocks, threads, 0, st>>>((float*)h->unitBuf.p, iters, 0.999999f,
+                                                       1e-7f);
+    cudaEventRecord(h->ev1, st);
+    if ((e = cudaEventSynchronize(h->ev1)) != cudaSuccess) return cudaFail(e, "probe");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    if (rep > 0 && ms < best) best = ms;
+  }
+  const double flops = 2.0 * 8 * 16 * (double)iters * blocks * threads;
+  *gflops = flops / (best * 1e-3) / 1e9;
+  h->lastLaunches = 4;
+  return CK_OK;
+}

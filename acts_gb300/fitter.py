@@ -74,6 +74,7 @@ def lib():
                                           abi.P_f64, abi.P_f32, abi.P_f32, abi.P_i32, C.c_int32,
                                           C.c_int32, abi.P_f64]
         L.ck_field_lookup.argtypes = [C.c_void_p, C.c_int32, abi.P_f64, abi.P_f64, abi.P_i32]
+        L.ck_fp_peak_gflops.argtypes = [C.c_void_p, C.c_int32, P(C.c_double)]
         L.ck_abi_struct_sizes.argtypes = [P(C.c_int64), C.c_int32]
         L.ck_abi_struct_sizes.restype = None
         _lib = L
@@ -104,6 +105,7 @@ class KalmanFitterOptions:
     initial_step_size: float = 10000.0
     loop_protection: bool = True
     loop_fraction: float = 0.5
+    early_termination: bool = False
     extra: dict = dc_field(default_factory=dict)
 
     def to_ck(self):
@@ -121,6 +123,7 @@ class KalmanFitterOptions:
         o.initial_step_size = float(self.initial_step_size)
         o.loop_protection = int(self.loop_protection)
         o.loop_fraction = float(self.loop_fraction)
+        o.early_termination = int(self.early_termination)
         for k, v in self.extra.items():
             setattr(o, k, v)
         return o
@@ -268,6 +271,11 @@ class CudaKalman:
 
     def set_launch_config(self, precision, variant, tpb, bps):
         _check(lib().ck_set_launch_config(self._h, precision, variant, tpb, bps))
+
+    def fp_peak_gflops(self, precision):
+        g = C.c_double()
+        _check(lib().ck_fp_peak_gflops(self._h, precision, C.byref(g)))
+        return g.value
 
     def sort_queue(self, enable):
         _check(lib().ck_sort_queue(self._h, int(enable)))

@@ -184,7 +184,13 @@ typedef struct ck_options {
   int32_t reverse_filtering;    /* must be 0                               */
   int32_t free_to_bound_correction; /* must be 0                           */
   int32_t reference_surface;    /* must be -1 (none)                       */
-  int32_t reserved;
+  /* 0 (default, the reference's behaviour): when outliers keep the track
+   * incomplete, propagation continues after the last surface that carries a
+   * source link until the loop-protection path limit, and any propagation
+   * error on the way (e.g. leaving the field map) fails the fit. 1: stop
+   * after the last such surface (states beyond it are never part of the
+   * track), which turns those failures into successful fits. */
+  int32_t early_termination;
 } ck_options;
 
 /* --------------------------------------------------------------- handle */
@@ -323,6 +329,11 @@ ck_status ck_sort_queue(ck_handle* h, int32_t enable);
 
 /* Text log of the last autotuner sweep (variant, block, blocks/SM, ms). */
 const char* ck_autotune_log(ck_handle* h);
+
+/* Measured peak of the FP64 (precision = CK_PRECISION_FP64) or FP32 FMA
+ * pipe on the handle's device, in GFLOP/s (FMA = 2 flops), from a
+ * dependent-chain-free FMA loop timed with CUDA events. */
+ck_status ck_fp_peak_gflops(ck_handle* h, int32_t precision, double* gflops);
 
 /* sizeof() of ck_surface, ck_field, ck_options, ck_config, ck_batch_in,
  * ck_batch_out, ck_server_config (in that order), for binding checks. */

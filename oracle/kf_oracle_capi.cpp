@@ -96,8 +96,9 @@ extern "C" {
 // Fits a host-memory batch on `n_threads` host threads (dynamic scheduling
 // over tracks). `coast` = 1 reproduces the reference termination exactly
 // (propagation continues to the path limit when outliers keep the track
-// incomplete); 0 stops after the last surface that carries a source link,
-// the termination rule of the CUDA fitter. Returns the wall time in seconds.
+// incomplete); 0 stops after the last surface that carries a source link
+// (ck_options.early_termination); -1 follows the options. Returns the wall
+// time in seconds.
 double kfo_fit_batch(const ck_options* opt, int n_surfaces, const ck_surface* surfaces,
                      const ck_field* field, const ck_batch_in* in, const ck_batch_out* out,
                      int n_threads, int coast, int first, int count) {
@@ -106,7 +107,8 @@ double kfo_fit_batch(const ck_options* opt, int n_surfaces, const ck_surface* su
   ctx.fitter.surfaces = &ctx.surfaces;
   ctx.fitter.field = Field<double>::make(*field);
   ctx.fitter.mc = MatConst::make();
-  ctx.fitter.o = Options::fromCk(*opt, coast != 0);
+  const bool doCoast = coast < 0 ? (opt->early_termination == 0) : (coast != 0);
+  ctx.fitter.o = Options::fromCk(*opt, doCoast);
   const int n = in->n_tracks;
   if (count < 0) count = n - first;
   if (n_threads < 1) n_threads = 1;

@@ -44,25 +44,30 @@ def lib():
         L.kfo_logf_mismatch.restype = C.c_int
         L.kfo_logf_mismatch.argtypes = [C.c_int, abi.P_f32]
         L.kfo_hardware_threads.restype = C.c_int
+        L.kfo_count_flops.restype = C.c_int
+        L.kfo_count_flops.argtypes = [C.POINTER(abi.ck_options), C.c_int, C.POINTER(abi.ck_surface),
+                                      C.POINTER(abi.ck_field), C.POINTER(abi.ck_batch_in), C.c_int,
+                                      C.c_int, C.POINTER(C.c_uint64)]
         _lib = L
     return _lib
 
 
-def fit_batch(detector, batch, options, results, n_threads=1, coast=False, first=0, count=-1):
+def fit_batch(detector, batch, options, results, n_threads=1, coast=None, first=0, count=-1):
     """Fits `batch` (acts_gb300.generate.Batch) into `results`
     (acts_gb300.results.Results). Returns the wall time in seconds."""
     bi = batch.as_batch_in()
     bo = results.as_batch_out()
+    c = -1 if coast is None else (1 if coast else 0)
     return lib().kfo_fit_batch(C.byref(options), detector.n_surfaces, detector.surfaces,
                                C.byref(detector.field), C.byref(bi), C.byref(bo), n_threads,
-                               1 if coast else 0, first, count)
+                               c, first, count)
 
 
 def time_batch(detector, batch, options, n_threads, first=0, count=-1):
     """Fits without writing results (CPU baseline timing)."""
     bi = batch.as_batch_in()
     return lib().kfo_fit_batch(C.byref(options), detector.n_surfaces, detector.surfaces,
-                               C.byref(detector.field), C.byref(bi), None, n_threads, 0, first,
+                               C.byref(detector.field), C.byref(bi), None, n_threads, -1, first,
                                count)
 
 
@@ -120,3 +125,19 @@ def logf_mismatch(x):
 
 def hardware_threads():
     return lib().kfo_hardware_threads()
+
+
+def count_flops(detector, batch, options, first=0, count=200):
+    """Algorithmic FP64 operation counts of the reference formulation per
+    fitted track: dict with add, mul, div, sqrt, trans, cmp, flops, tracks."""
+    bi = batch.as_batch_in()
+    out = (C.c_uint64 * 6)()
+    ok = lib().kfo_count_flops(C.byref(options), detector.n_surfaces, detector.surfaces,
+                               C.byref(detector.field), C.byref(bi), first, count, out)
+    n = min(count, batch.n - first)
+    keys = ("add", "mul", "div", "sqrt", "trans", "cmp")
+    d = {k: out[i] / n for i, k in enumerate(keys)}
+    d["flops"] = d["add"] + d["mul"] + d["div"] + d["sqrt"]
+    d["tracks"] = n
+    d["ok"] = ok
+    return d

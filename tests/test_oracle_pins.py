@@ -1,0 +1,319 @@
+"""Pins the CPU oracle against the reference's own known answers (extracted
+into tests/golden/reference_known_answers.json by
+tests/golden/extract_known_answers.py) and against the structural checks of
+the reference's KalmanFitter tests. CPU only."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from acts_gb300 import abi
+from acts_gb300.results import Results
+from conftest import batch, detector
+from oracle import kforacle
+
+KA = json.load(open(os.path.join(os.path.dirname(__file__), "golden",
+                                 "reference_known_answers.json")))
+
+
+def _diag(v):
+    return np.diag(np.asarray(v, float)).reshape(36)
+
+
+# ------------------------------------------------ GainMatrixUpdaterTests.cpp
+def test_updater_known_answer():
+    u = KA["updater"]
+    f, fc, chi2, st = kforacle.gain_matrix_update(
+        np.array([u["pred"]]), np.array([_diag(u["pred_cov_diag"])]), np.array([u["meas"]]),
+        np.array([np.diag(u["meas_cov_diag"]).reshape(4)]))
+    assert st[0] == 0
+    np.testing.assert_allclose(f[0], u["exp_filtered"], atol=u["tol"])
+    np.testing.assert_allclose(np.diag(fc[0]), u["exp_filtered_cov_diag"], atol=u["tol"])
+    off = fc[0] - np.diag(np.diag(fc[0]))
+    assert np.abs(off).max() <= u["tol"]
+    assert abs(chi2[0] - u["exp_chi2"]) <= u["chi2_tol"]
+
+
+def test_updater_failed():
+    u = KA["updater"]
+    assert u["failed_case_pred_cov_zero"] and u["failed_case_meas_cov_zero"]
+    _, _, _, st = kforacle.gain_matrix_update(np.array([u["pred"]]), np.zeros((1, 36)),
+                                              np.array([u["meas"]]), np.zeros((1, 4)))
+    assert st[0] == 1  # KalmanFitterError::UpdateFailed
+
+
+def test_updater_joseph_equals_plain_on_known_answer():
+    u = KA["updater"]
+    args = (np.array([u["pred"]]), np.array([_diag(u["pred_cov_diag"])]), np.array([u["meas"]]),
+            np.array([np.diag(u["meas_cov_diag"]).reshape(4)]))
+    a = kforacle.gain_matrix_update(*args, joseph=False)
+    b = kforacle.gain_matrix_update(*args, joseph=True)
+    np.testing.assert_allclose(a[1], b[1], atol=1e-12)
+    np.testing.assert_allclose(a[2], b[2], rtol=1e-12)
+
+
+# ------------------------------------------------ GainMatrixSmootherTests.cpp
+def smoother_inputs():
+    s = KA["smoother"]
+    cov = _diag(s["cov_diag"])
+    pred = np.array([[st["predicted"] for st in s["states"]]])
+    filt = np.array([[st["filtered"] for st in s["states"]]])
+    covs = np.tile(cov, (1, 3, 1))
+    jac = np.tile(np.eye(6).reshape(36), (1, 3, 1))
+    return pred, covs, filt, covs.copy(), jac
+
+
+def test_smoother_known_answer():
+    s = KA["smoother"]
+    sm, smc, st = kforacle.gain_matrix_smooth(*smoother_inputs())
+    assert st[0] == 0
+    for k in range(3):
+        np.testing.assert_allclose(sm[0, k], s["exp_smoothed"][k], atol=s["tol"])
+        np.testing.assert_allclose(np.diag(smc[0, k]), s["exp_cov_diag"], atol=s["tol"])
+    # last state: smoothed == filtered; earlier ones differ
+    pred, _, filt, _, _ = smoother_inputs()
+    assert np.array_equal(sm[0, 2], filt[0, 2])
+    assert not np.array_equal(sm[0, 0], filt[0, 0])
+
+
+# ------------------------------------------------------ InteractionsTests.cpp
+SI = KA["silicon"]
+
+
+def _interaction(which, thickness, pdg, m, qop, absq):
+    return kforacle.interaction(which, thickness, SI["X0"], SI["L0"], SI["Ar"], SI["Z"],
+                                SI["molar_rho"], pdg, m, qop, absq)
+
+
+def _momenta():
+    low = np.arange(0.1, 10.0, 0.1)
+    med = np.arange(10.0, 100.0, 10.0)
+    high = np.arange(100.0, 10000.0, 100.0)
+    return np.concatenate([low, med, high])
+
+
+PARTICLES = [(11, 0.000511, -1.0), (13, 0.1057, -1.0), (211, 0.1396, 1.0), (2212, 0.9383, 1.0)]
+
+
+@pytest.mark.parametrize("thickness", KA["interactions"]["consistency"]["thickness"])
+@pytest.mark.parametrize("pdg,m,q", PARTICLES)
+def test_energy_loss_and_scattering_consistency(thickness, pdg, m, q):
+    for p in _momenta()[::7]:
+        qop = q / p
+        bethe = _interaction(0, thickness, pdg, m, qop, abs(q))
+        landau = _interaction(1, thickness, pdg, m, qop, abs(q))
+        sig_qop = _interaction(2, thickness, pdg, m, qop, abs(q))
+        sigma = _interaction(4, thickness, pdg, m, qop, abs(q)) * 0.42466090014400953
+        assert bethe > 0 and landau > 0 and sig_qop > 0 and sigma > 0
+        assert sigma <= bethe
+        t0 = _interaction(3, thickness, pdg, m, qop, abs(q))
+        assert t0 > 0
+        assert _interaction(3, thickness, pdg, m, -qop, abs(q)) == t0
+        assert _interaction(3, 2 * thickness, pdg, m, qop, abs(q)) > t0
+        assert _interaction(3, thickness, pdg, m, q / (2 * p), abs(q)) < t0
+
+
+def test_vacuum_has_no_interactions():
+    for which in range(5):
+        v = kforacle.interaction(which, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 13, 0.1057, 1.0, 1.0)
+        assert v == 0.0
+
+
+def test_silicon_bethe_against_pdg():
+    c = KA["interactions"]["silicon_bethe"]
+    # mass density of silicon in native units (Material::massDensity)
+    u = 0.93149410242
+    avogadro = 6.02214076e23
+    rho = SI["Ar"] * u * np.float32(SI["molar_rho"]) * avogadro
+    g = 1.0 / 1.782662e-24
+    for p, loss in zip(c["momentum"], c["loss_MeV_cm2_per_g"]):
+        de = _interaction(0, c["thickness"], 13, c["mass"], -1.0 / p, 1.0)
+        value = de / c["thickness"] / rho / (1e-3 * 100.0 / g)
+        assert abs(value - loss) / loss * 100 <= c["percent"], (p, value, loss)
+
+
+def test_silicon_landau():
+    c = KA["interactions"]["silicon_landau"]
+    de = _interaction(1, c["thickness"], 13, c["mass"], -1.0 / c["momentum"], 1.0) / 1e-3
+    assert abs(de - c["dE_MeV"]) / c["dE_MeV"] * 100 <= c["dE_percent"]
+    fw = _interaction(4, c["thickness"], 13, c["mass"], -1.0 / c["momentum"], 1.0) / 1e-3
+    assert abs(fw - c["fwhm_MeV"]) / c["fwhm_MeV"] * 100 <= c["fwhm_percent"]
+
+
+# ------------------------------------------------ InterpolatedBFieldMapTests.cpp
+def linear_grid():
+    """A small XYZ map filled with a trilinear function: interpolation must
+    reproduce it exactly (the RZ bilinear test of the reference, in 3D)."""
+    n = (5, 4, 7)
+    lo, hi = (-2.0, -1.5, -3.0), (2.0, 1.5, 3.0)
+    xs = [np.linspace(lo[i], hi[i], n[i]) for i in range(3)]
+    X, Y, Z = np.meshgrid(*xs, indexing="ij")
+    vals = np.stack([X * Y + Z, 3 * Y - X * Z, -2 * Z + X * Y * Z], axis=-1).astype(np.float32)
+    f = abi.ck_field()
+    f.kind = abi.FIELD_GRID_XYZ
+    for i in range(3):
+        f.n[i] = n[i]
+        f.min[i] = lo[i]
+        f.max[i] = hi[i]
+    vals = np.ascontiguousarray(vals.reshape(-1))
+    f.values_tesla = abi.ptr(vals, __import__("ctypes").c_float)
+    return f, vals, lo, hi
+
+
+def field_truth(p):
+    x, y, z = p[:, 0], p[:, 1], p[:, 2]
+    return np.stack([x * y + z, 3 * y - x * z, -2 * z + x * y * z], axis=-1) * 0.000299792458
+
+
+def test_field_map_trilinear_exact_and_bounds():
+    f, keep, lo, hi = linear_grid()
+    rng = np.random.default_rng(1)
+    pts = rng.uniform(lo, hi, size=(400, 3)) * 0.999
+    b, st = kforacle.field_lookup(f, pts)
+    assert (st == 0).all()
+    # exact up to the float32 node values
+    np.testing.assert_allclose(b, field_truth(pts), rtol=2e-6, atol=2e-9)
+    # isInside: [min, max) per axis
+    edge = np.array([[lo[0], 0.0, 0.0], [hi[0], 0.0, 0.0], [0.0, 0.0, hi[2] - 1e-9],
+                     [0.0, lo[1] - 1e-9, 0.0], [0.0, 0.0, 3.5]])
+    _, st = kforacle.field_lookup(f, edge)
+    assert list(st == 0) == [True, False, True, False, False]
+
+
+# --------------------------------------------- KalmanFitterTests.cpp structure
+def _fit(preset, b, **kw):
+    det = detector(preset)
+    res = Results(b.n, 24)
+    kforacle.fit_batch(det, b, abi.default_options(**kw), res, n_threads=4)
+    return res
+
+
+def test_kf_all_measurements():
+    b = batch(abi.CKG_TELESCOPE, 50)
+    r = _fit(abi.CKG_TELESCOPE, b)
+    assert (r.status == 0).all()
+    assert (r.n_measurements == np.diff(b.meas_offsets)).all()
+    assert (r.n_holes == 0).all() and (r.n_outliers == 0).all()
+    assert (r.ndf == 2 * r.n_measurements).all()
+
+
+def test_kf_hole_counted_once():
+    b = batch(abi.CKG_TELESCOPE, 20)
+    for remove in range(1, 9):  # interior measurements
+        keep = []
+        for t in range(b.n):
+            keep.append([m for m in range(b.meas_offsets[t], b.meas_offsets[t + 1])
+                         if m - b.meas_offsets[t] != remove])
+        nb = _drop_measurements(b, keep)
+        r = _fit(abi.CKG_TELESCOPE, nb)
+        assert (r.status == 0).all()
+        assert (r.n_holes == 1).all(), remove
+        assert (r.n_measurements == 9).all()
+
+
+def test_kf_outlier_flagged():
+    b = batch(abi.CKG_TELESCOPE, 20)
+    for replace in range(0, 10, 3):
+        nb = b.subset(np.arange(b.n))
+        for t in range(b.n):
+            m = nb.meas_offsets[t] + replace
+            nb.meas_values[2 * m] += 10.0  # 10 mm displacement as the reference test
+        r = _fit(abi.CKG_TELESCOPE, nb, outlier_chi2_cut=15.0)
+        assert (r.status == 0).all()
+        assert (r.n_outliers == 1).all(), replace
+        assert (r.n_measurements == 9).all()
+
+
+def test_kf_shuffled_source_links_identical():
+    b = batch(abi.CKG_BARREL, 50)
+    r1 = _fit(abi.CKG_BARREL, b)
+    nb = b.subset(np.arange(b.n))
+    rng = np.random.default_rng(5)
+    for t in range(b.n):
+        a, e = nb.meas_offsets[t], nb.meas_offsets[t + 1]
+        perm = rng.permutation(e - a)
+        nb.meas_surfaces[a:e] = nb.meas_surfaces[a:e][perm]
+        nb.meas_values[2 * a:2 * e] = nb.meas_values[2 * a:2 * e].reshape(-1, 2)[perm].reshape(-1)
+        nb.meas_cov[4 * a:4 * e] = nb.meas_cov[4 * a:4 * e].reshape(-1, 4)[perm].reshape(-1)
+    r2 = _fit(abi.CKG_BARREL, nb)
+    assert np.array_equal(r1.status, r2.status)
+    np.testing.assert_array_equal(r1.smoothed, r2.smoothed)
+
+
+def test_coasting_and_early_termination():
+    """The reference keeps propagating after the last surface when outliers
+    leave the track incomplete, until the loop-protection path limit; the
+    states it adds there are never part of the track. So: tracks that survive
+    this coasting are identical under both termination rules, and the tracks
+    that fail do so only through propagation errors after the tip (on the
+    uneven workload's field map: leaving the map), where the early rule
+    succeeds."""
+    preset = abi.CKG_UNEVEN
+    det = detector(preset)
+    b = batch(preset, 300)
+    r1, r2 = Results(b.n, 24), Results(b.n, 24)
+    kforacle.fit_batch(det, b, abi.default_options(outlier_chi2_cut=15.0), r1, n_threads=4)
+    kforacle.fit_batch(det, b, abi.default_options(outlier_chi2_cut=15.0, early_termination=1),
+                       r2, n_threads=4)
+    assert (r2.n_outliers > 0).sum() > 20  # the case is exercised
+    ok = r1.status == 0
+    assert ok.sum() > 100
+    assert (r2.status[ok] == 0).all()
+    for name in ("n_states", "n_measurements", "n_holes", "n_outliers"):
+        np.testing.assert_array_equal(getattr(r1, name)[ok], getattr(r2, name)[ok], err_msg=name)
+    for name in ("state_flags", "smoothed", "smoothed_cov", "filtered", "predicted", "jacobian"):
+        np.testing.assert_array_equal(r1.view(name)[ok], r2.view(name)[ok], err_msg=name)
+    failed = ~ok
+    assert set(np.unique(r1.status[failed])) <= {abi_status("MagneticFieldOutOfBounds"),
+                                                  abi_status("StepCountLimitReached")}
+    assert (r2.status[failed] == 0).all()
+    assert (r2.n_outliers[failed] > 0).all()
+
+
+def abi_status(name):
+    return [k for k, v in abi.TRACK_STATUS.items() if v == name][0]
+
+
+def test_no_measurement_found():
+    b = batch(abi.CKG_TELESCOPE, 5)
+    nb = _drop_measurements(b, [[] for _ in range(b.n)])
+    r = _fit(abi.CKG_TELESCOPE, nb)
+    assert (r.status == 3).all()  # KalmanFitterError::NoMeasurementFound
+
+
+def test_invalid_surface_id_rejected():
+    b = batch(abi.CKG_TELESCOPE, 5).subset(np.arange(5))
+    b.seq_surfaces[0] = 999
+    r = _fit(abi.CKG_TELESCOPE, b)
+    assert r.status[0] == 12 and (r.status[1:] == 0).all()
+
+
+def test_logf_restatement_mismatch_rate():
+    """ck_logf (correctly rounded) against glibc logf on the arguments the
+    material physics sees: the documented deviation is rare."""
+    rng = np.random.default_rng(3)
+    x = np.exp(rng.uniform(np.log(1e-6), np.log(1e6), 200000)).astype(np.float32)
+    bad = kforacle.logf_mismatch(x)
+    assert bad / len(x) < 1e-2, bad
+
+
+def _drop_measurements(b, keep):
+    from acts_gb300.generate import Batch
+
+    nb = b.subset(np.arange(b.n))
+    ms, mv, mc, tm, mo = [], [], [], [], [0]
+    for t in range(b.n):
+        for m in keep[t]:
+            ms.append(b.meas_surfaces[m])
+            mv.extend(b.meas_values[2 * m:2 * m + 2])
+            mc.extend(b.meas_cov[4 * m:4 * m + 4])
+            tm.extend(b.truth_meas[6 * m:6 * m + 6])
+        mo.append(len(ms))
+    nb.meas_surfaces = np.ascontiguousarray(np.array(ms, np.int32))
+    nb.meas_values = np.ascontiguousarray(np.array(mv, np.float64))
+    nb.meas_cov = np.ascontiguousarray(np.array(mc, np.float64))
+    nb.truth_meas = np.ascontiguousarray(np.array(tm, np.float64))
+    nb.meas_offsets = np.ascontiguousarray(np.array(mo, np.int32))
+    nb.meas_outlier = np.zeros(len(ms), np.uint8)
+    return nb
