@@ -1,0 +1,45 @@
+"""A fixed fit case for profilers (ncu launch lists and kernel captures).
+
+    python -m acts_gb300.profile_case --preset barrel --tracks 20000 --precision fp64,mixed
+
+Generates the preset's tracks, fits them once per requested precision
+(graph capture off, so every kernel is an ordinary launch) and prints the
+kernel time of each fit. Profile summaries under profiles/ name the exact
+command line they were produced with.
+"""
+import argparse
+import sys
+
+from . import abi, generate
+from .fitter import CudaKalman
+
+PRESETS = {"telescope": abi.CKG_TELESCOPE, "barrel": abi.CKG_BARREL, "uneven": abi.CKG_UNEVEN}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--preset", default="barrel", choices=sorted(PRESETS))
+    ap.add_argument("--tracks", type=int, default=20000)
+    ap.add_argument("--precision", default="fp64,mixed")
+    ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--seed", type=int, default=5)
+    ap.add_argument("--max-states", type=int, default=0)
+    a = ap.parse_args(argv)
+    preset = PRESETS[a.preset]
+    det = generate.Detector(preset)
+    b = generate.generate(det, a.tracks, seed=a.seed)
+    ms = a.max_states or (10 if preset != abi.CKG_UNEVEN else 20)
+    fit = CudaKalman.for_detector(det, use_graph=False)
+    for name in a.precision.split(","):
+        prec = abi.PRECISION_MIXED if name == "mixed" else abi.PRECISION_FP64
+        opt = abi.default_options(precision=prec,
+                                  outlier_chi2_cut=15.0 if preset == abi.CKG_UNEVEN else float("inf"))
+        for _ in range(a.repeat):
+            fit.fit_batch(b, opt, max_states=ms, components=abi.OUT_SMOOTHED)
+            print("%s %s %d tracks: kernel %.3f ms" % (a.preset, name, a.tracks, fit.last_kernel_ms()))
+    fit.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,71 @@
+"""Mixed-precision form (stepper, Jacobian transport, field in FP32; update,
+2x2 inverse, smoother-gain inverse and chi2 in FP64) against the FP64 oracle
+on the same seeded barrel tracks. Bounds: relative parameter error
+|x_mixed - x_fp64| / max(|x_fp64|, sigma_fp64) <= 1e-4 on the smoothed
+parameters of measurement states, and pull widths against the generator
+truth within 1 % of the FP64 widths."""
+import numpy as np
+import pytest
+
+from acts_gb300 import abi
+from acts_gb300.results import Results
+from conftest import batch, detector
+from oracle import kforacle
+
+REL_BOUND = 1e-4
+PULL_SHIFT = 0.01
+
+
+def _pulls(res, b):
+    fl = res.view("state_flags")
+    sm, smc, surf = res.view("smoothed"), res.view("smoothed_cov"), res.view("state_surface")
+    out = [[] for _ in range(5)]
+    tm = b.truth_meas.reshape(-1, 6)
+    for t in np.nonzero(res.status == 0)[0]:
+        lut = {int(b.meas_surfaces[m]): m for m in range(b.meas_offsets[t], b.meas_offsets[t + 1])}
+        for k in range(res.n_states[t]):
+            if not (fl[t, k] & abi.FLAG_HAS_MEASUREMENT) or (fl[t, k] & abi.FLAG_IS_OUTLIER):
+                continue
+            m = lut[int(surf[t, k])]
+            for i in range(5):
+                d = sm[t, k, i] - tm[m, i]
+                if i == 2:
+                    d = (d + np.pi) % (2 * np.pi) - np.pi
+                out[i].append(d / np.sqrt(smc[t, k, 7 * i]))
+    return [np.std(np.clip(np.array(p), -10, 10)) for p in out]
+
+
+@pytest.mark.gpu
+def test_mixed_precision_accuracy(fitter_factory):
+    preset = abi.CKG_BARREL
+    n = 20000
+    det = detector(preset)
+    b = batch(preset, n, seed=13)
+    ora = Results(n, 12)
+    kforacle.fit_batch(det, b, abi.default_options(), ora, n_threads=kforacle.hardware_threads())
+    mix = fitter_factory(preset).fit_batch(b, abi.default_options(precision=abi.PRECISION_MIXED),
+                                          max_states=12)
+    agree = np.mean(mix.status == ora.status)
+    assert agree > 0.999, agree
+    ok = (mix.status == 0) & (ora.status == 0)
+    assert np.array_equal(mix.n_states[ok], ora.n_states[ok])
+    fl = ora.view("state_flags")
+    valid = np.zeros(fl.shape, bool)
+    for t in np.nonzero(ok)[0]:
+        valid[t, : ora.n_states[t]] = True
+    meas = valid & ((fl & abi.FLAG_HAS_MEASUREMENT) != 0) & ((fl & abi.FLAG_IS_OUTLIER) == 0)
+    a, o = mix.view("smoothed"), ora.view("smoothed")
+    sig = np.sqrt(np.abs(ora.view("smoothed_cov")[..., [0, 7, 14, 21, 28, 35]]))
+    d = np.abs(a - o)
+    d[..., 2] = np.abs((a[..., 2] - o[..., 2] + np.pi) % (2 * np.pi) - np.pi)
+    rel = (d / np.maximum(np.abs(o), sig))[meas]
+    print("mixed: max rel %.3g p99 %.3g" % (rel.max(), np.quantile(rel, 0.99)))
+    assert rel.max() <= REL_BOUND
+    w64 = _pulls(ora, b)
+    wmx = _pulls(mix, b)
+    print("pull widths fp64", np.round(w64, 4), "mixed", np.round(wmx, 4))
+    for x, y in zip(w64, wmx):
+        assert abs(x - y) / x <= PULL_SHIFT
+    c64 = ora.chi2_sum[ok].sum() / ora.ndf[ok].sum()
+    cmx = mix.chi2_sum[ok].sum() / mix.ndf[ok].sum()
+    assert abs(c64 - cmx) / c64 < 1e-3

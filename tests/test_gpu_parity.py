@@ -14,17 +14,26 @@ from parity import assert_parity, compare
 
 RTOL = 1e-9
 
+# (name, preset, tracks, options, minimum fraction of successful fits). On
+# the uneven workload the reference's coasting after the last surface leaves
+# the field map for most tracks with an outlier (MagneticFieldError); those
+# failures are part of the parity check.
 CASES = [
-    ("telescope", abi.CKG_TELESCOPE, 1000, dict()),
-    ("barrel", abi.CKG_BARREL, 2000, dict()),
-    ("barrel_joseph", abi.CKG_BARREL, 1000, dict(use_joseph=1)),
-    ("uneven", abi.CKG_UNEVEN, 2000, dict(outlier_chi2_cut=15.0)),
+    ("telescope", abi.CKG_TELESCOPE, 1000, dict(), 0.99),
+    ("barrel", abi.CKG_BARREL, 2000, dict(), 0.99),
+    ("barrel_joseph", abi.CKG_BARREL, 1000, dict(use_joseph=1), 0.99),
+    ("uneven", abi.CKG_UNEVEN, 2000, dict(outlier_chi2_cut=15.0), 0.5),
+    ("uneven_early_termination", abi.CKG_UNEVEN, 2000,
+     dict(outlier_chi2_cut=15.0, early_termination=1), 0.99),
+    ("telescope_no_material_options", abi.CKG_TELESCOPE, 500,
+     dict(multiple_scattering=0, energy_loss=0), 0.99),
+    ("barrel_no_energy_loss", abi.CKG_BARREL, 500, dict(energy_loss=0), 0.99),
 ]
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name,preset,n,kw", CASES, ids=[c[0] for c in CASES])
-def test_fp64_parity(fitter_factory, name, preset, n, kw):
+@pytest.mark.parametrize("name,preset,n,kw,min_ok", CASES, ids=[c[0] for c in CASES])
+def test_fp64_parity(fitter_factory, name, preset, n, kw, min_ok):
     det = detector(preset)
     b = batch(preset, n)
     opt = abi.default_options(**kw)
@@ -33,5 +42,5 @@ def test_fp64_parity(fitter_factory, name, preset, n, kw):
     gpu = fitter_factory(preset).fit_batch(b, opt, max_states=24)
     rep = compare(gpu, ora, RTOL)
     print(name, rep)
-    assert rep["n_ok"] > 0.9 * n
+    assert rep["n_ok"] >= min_ok * n
     assert_parity(rep, RTOL)

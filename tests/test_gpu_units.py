@@ -1,0 +1,111 @@
+"""Unit operators of the CUDA fitter through the C ABI: the reference's own
+known answers (GainMatrixUpdater, GainMatrixSmoother), the float material
+physics bit-exact against the oracle, and the field lookup."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from acts_gb300 import abi
+from conftest import detector
+from oracle import kforacle
+
+KA = json.load(open(os.path.join(os.path.dirname(__file__), "golden",
+                                 "reference_known_answers.json")))
+
+
+def _diag(v):
+    return np.diag(np.asarray(v, float)).reshape(36)
+
+
+@pytest.mark.gpu
+def test_updater_known_answer_on_gpu(fitter_factory):
+    u = KA["updater"]
+    fit = fitter_factory(abi.CKG_TELESCOPE)
+    args = (np.array([u["pred"]]), np.array([_diag(u["pred_cov_diag"])]), np.array([u["meas"]]),
+            np.array([np.diag(u["meas_cov_diag"]).reshape(4)]))
+    f, fc, chi2, st = fit.gain_matrix_update(*args)
+    assert st[0] == 0
+    np.testing.assert_allclose(f[0], u["exp_filtered"], atol=u["tol"])
+    np.testing.assert_allclose(np.diag(fc[0]), u["exp_filtered_cov_diag"], atol=u["tol"])
+    assert abs(chi2[0] - u["exp_chi2"]) <= u["chi2_tol"]
+    # UpdateFailed on zero covariances
+    _, _, _, st = fit.gain_matrix_update(args[0], np.zeros((1, 36)), args[2], np.zeros((1, 4)))
+    assert st[0] == 1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("joseph", [False, True])
+def test_updater_random_states_match_oracle(fitter_factory, joseph):
+    rng = np.random.default_rng(4)
+    n = 2000
+    A = rng.normal(size=(n, 6, 6)) * np.array([0.1, 0.1, 0.01, 0.01, 0.001, 1.0])[None, :, None]
+    P = A @ A.transpose(0, 2, 1) + np.eye(6) * 1e-6
+    pred = rng.normal(size=(n, 6)) * 0.1
+    pred[:, 3] = 1.0 + 0.2 * rng.normal(size=n)
+    meas = pred[:, :2] + rng.normal(size=(n, 2)) * 0.05
+    V = np.zeros((n, 4))
+    V[:, 0] = 0.0025
+    V[:, 3] = 0.0025
+    fit = fitter_factory(abi.CKG_TELESCOPE)
+    g = fit.gain_matrix_update(pred, P.reshape(n, 36), meas, V, joseph)
+    o = kforacle.gain_matrix_update(pred, P.reshape(n, 36), meas, V, joseph)
+    assert (g[3] == o[3]).all()
+    np.testing.assert_allclose(g[0], o[0], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(g[1], o[1], rtol=1e-9, atol=1e-15)
+    np.testing.assert_allclose(g[2], o[2], rtol=1e-9)
+
+
+@pytest.mark.gpu
+def test_smoother_known_answer_on_gpu(fitter_factory):
+    s = KA["smoother"]
+    cov = _diag(s["cov_diag"])
+    pred = np.array([[st["predicted"] for st in s["states"]]])
+    filt = np.array([[st["filtered"] for st in s["states"]]])
+    covs = np.tile(cov, (1, 3, 1))
+    jac = np.tile(np.eye(6).reshape(36), (1, 3, 1))
+    fit = fitter_factory(abi.CKG_TELESCOPE)
+    sm, smc, st = fit.gain_matrix_smooth(pred, covs, filt, covs.copy(), jac)
+    assert st[0] == 0
+    for k in range(3):
+        np.testing.assert_allclose(sm[0, k], s["exp_smoothed"][k], atol=s["tol"])
+        np.testing.assert_allclose(np.diag(smc[0, k]), s["exp_cov_diag"], atol=s["tol"])
+
+
+@pytest.mark.gpu
+def test_material_effects_bit_exact(fitter_factory):
+    """The float Bethe / Landau / Highland physics is reproduced bit for bit
+    (un-contracted float arithmetic, shared correctly rounded logf)."""
+    det = detector(abi.CKG_BARREL)
+    fit = fitter_factory(abi.CKG_BARREL)
+    rng = np.random.default_rng(7)
+    n = 4000
+    sid = rng.integers(0, det.n_surfaces, n).astype(np.int32)
+    scale = rng.uniform(1.0, 3.0, n).astype(np.float32)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    p = np.exp(rng.uniform(np.log(0.05), np.log(500.0), n))
+    qop = np.where(rng.uniform(size=n) < 0.5, -1.0, 1.0) / p
+    mass = np.full(n, 0.13957039, np.float32)
+    absq = np.ones(n, np.float32)
+    pdg = np.full(n, 211, np.int32)
+    g = fit.material_effects(sid, scale, d, qop, mass, absq, pdg)
+    for i in range(0, n, 37):
+        o = kforacle.material_effects(det.surfaces[int(sid[i])], float(scale[i]), d[i], qop[i],
+                                      float(mass[i]), 1.0, 211)
+        assert np.array_equal(g[i], o), (i, g[i], o)
+
+
+@pytest.mark.gpu
+def test_field_lookup_matches_oracle(fitter_factory):
+    det = detector(abi.CKG_UNEVEN)
+    fit = fitter_factory(abi.CKG_UNEVEN)
+    rng = np.random.default_rng(2)
+    pts = rng.uniform([-1600, -1600, -3100], [1600, 1600, 3100], size=(20000, 3))
+    g, gs = fit.field_lookup(pts)
+    o, os_ = kforacle.field_lookup(det.field, pts)
+    assert np.array_equal(gs, os_)
+    ok = gs == 0
+    assert ok.sum() > 10000 and (~ok).sum() > 1000
+    np.testing.assert_allclose(g[ok], o[ok], rtol=1e-12, atol=1e-18)
