@@ -123,7 +123,7 @@ ck_status validateOptions(const ck_options* o) {
     return fail(CK_ERR_UNSUPPORTED, "free-to-bound correction is not supported");
   if (o->reference_surface != -1)
     return fail(CK_ERR_UNSUPPORTED, "extrapolation to a reference surface is not supported");
-  if (o->precision != CK_PRECISION_FP64 && o->precision != CK_PRECISION_MIXED)
+  if (o->precision < 0 || o->precision >= CK_NUM_PRECISIONS)
     return fail(CK_ERR_INVALID_ARGUMENT, "unknown precision");
   if (!(o->step_tolerance > 0) || !(o->initial_step_size > 0))
     return fail(CK_ERR_INVALID_ARGUMENT, "step tolerance and initial step size must be > 0");
@@ -187,7 +187,8 @@ void loadTuneCache(ck_handle* h) {
   std::ifstream f(h->cachePath);
   int p, v, tpb, bps;
   while (f >> p >> v >> tpb >> bps) {
-    if (p < 0 || p > 1 || v < 0 || v >= kNumFitVariants || tpb <= 0 || tpb > kFitMaxBlock ||
+    if (p < 0 || p >= CK_NUM_PRECISIONS || v < 0 || v >= kNumFitVariants || tpb <= 0 ||
+        tpb > kFitMaxBlock ||
         bps <= 0)
       continue;
     h->tune[p] = {v, tpb, bps, true};
@@ -197,43 +198,49 @@ void loadTuneCache(ck_handle* h) {
 void saveTuneCache(ck_handle* h) {
   if (h->cachePath.empty()) return;
   std::ofstream f(h->cachePath);
-  for (int p = 0; p < 2; ++p)
+  for (int p = 0; p < CK_NUM_PRECISIONS; ++p)
     if (h->tune[p].tuned)
       f << p << " " << h->tune[p].variant << " " << h->tune[p].tpb << " " << h->tune[p].bps << "\n";
 }
 
 cudaError_t launchFit(const FitParams& fp, int precision, const Tune& tn, int grid,
                       cudaStream_t st) {
-  return precision == CK_PRECISION_MIXED ? launchFitMixed(fp, tn.variant, grid, tn.tpb, st)
-                                         : launchFitFP64(fp, tn.variant, grid, tn.tpb, st);
+  switch (precision) {
+    case CK_PRECISION_MIXED: return launchFitMixed(fp, tn.variant, grid, tn.tpb, st);
+    case CK_PRECISION_MIXED_COV64: return launchFitMixedCov64(fp, tn.variant, grid, tn.tpb, st);
+    default: return launchFitFP64(fp, tn.variant, grid, tn.tpb, st);
+  }
 }
+
+int gridBlocksFor(ck_handle* h, const Tune& tn) { return h->smCount * tn.bps; }
 
 // Allocates (grow-only) the scratch of a batch pipeline. Never called while
 // a stream is being captured.
-ck_status preparePipeline(ck_handle* h, int n, int maxStates, const Tune& tn) {
-  const int grid = h->smCount * tn.bps;
-  const int nSlots = grid * tn.tpb;
+ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, const Tune& tn,
+                          int gridBlocks) {
+  (void)h;
+  const int nSlots = gridBlocks * tn.tpb;
   cudaError_t e;
-  if ((e = h->rec.ensure(compBytes(nSlots, maxStates, kRecDoubles, sizeof(double)))) ||
-      (e = h->recMeta.ensure(compBytes(nSlots, maxStates, 2, sizeof(int32_t)))) ||
-      (e = h->recMetaD.ensure(compBytes(nSlots, maxStates, 2, sizeof(double)))) ||
-      (e = h->perm.ensure((size_t)n * sizeof(int32_t) + 16)) ||
-      (e = h->ticket.ensure(sizeof(int32_t) * (kBins + 1))))
+  if ((e = c.rec.ensure(compBytes(nSlots, maxStates, kRecDoubles, sizeof(double)))) ||
+      (e = c.recMeta.ensure(compBytes(nSlots, maxStates, 2, sizeof(int32_t)))) ||
+      (e = c.recMetaD.ensure(compBytes(nSlots, maxStates, 2, sizeof(double)))) ||
+      (e = c.perm.ensure((size_t)n * sizeof(int32_t) + 16)) ||
+      (e = c.ticket.ensure(sizeof(int32_t) * (kBins + 1))))
     return cudaFail(e, "scratch allocation");
   return CK_OK;
 }
 
 // Records the whole batch pipeline (inputs already on the device, scratch
 // prepared) on `st`: queue reset, queue ordering, fit kernel.
-ck_status enqueuePipeline(ck_handle* h, const ck_options& opt, const ck_batch_in& din,
-                          const ck_batch_out& dout, const Tune& tn, cudaStream_t st,
-                          bool timed) {
+ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
+                          const ck_batch_in& din, const ck_batch_out& dout, const Tune& tn,
+                          cudaStream_t st, bool timed, int gridBlocks) {
   const int n = din.n_tracks;
-  const int grid = h->smCount * tn.bps;
+  const int grid = gridBlocks;
   const int nSlots = grid * tn.tpb;
   const int maxStates = dout.max_states;
   cudaError_t e;
-  int32_t* dTicket = (int32_t*)h->ticket.p;
+  int32_t* dTicket = (int32_t*)c.ticket.p;
   int32_t* dBins = dTicket + 1;
   int launches = 0;
   cudaMemsetAsync(dTicket, 0, sizeof(int32_t) * (kBins + 1), st);
@@ -244,9 +251,9 @@ ck_status enqueuePipeline(ck_handle* h, const ck_options& opt, const ck_batch_in
     if (gb > h->smCount * 8) gb = h->smCount * 8;
     queueHistogram<<<gb, tb, 0, st>>>(din.seq_offsets, n, dBins);
     queueScan<<<1, 32, 0, st>>>(dBins);
-    queueScatter<<<gb, tb, 0, st>>>(din.seq_offsets, n, dBins, (int32_t*)h->perm.p);
+    queueScatter<<<gb, tb, 0, st>>>(din.seq_offsets, n, dBins, (int32_t*)c.perm.p);
     launches += 3;
-    perm = (const int32_t*)h->perm.p;
+    perm = (const int32_t*)c.perm.p;
   }
   FitParams fp;
   std::memset(&fp, 0, sizeof(fp));
@@ -265,9 +272,9 @@ ck_status enqueuePipeline(ck_handle* h, const ck_options& opt, const ck_batch_in
   fp.pdg = din.particle_pdg;
   fp.perm = perm;
   fp.ticket = dTicket;
-  fp.rec = (double*)h->rec.p;
-  fp.rec_meta = (int32_t*)h->recMeta.p;
-  fp.rec_meta_d = (double*)h->recMetaD.p;
+  fp.rec = (double*)c.rec.p;
+  fp.rec_meta = (int32_t*)c.recMeta.p;
+  fp.rec_meta_d = (double*)c.recMetaD.p;
   fp.n_slots = nSlots;
   fp.max_states = maxStates;
   fp.out = dout;
@@ -444,7 +451,7 @@ ck_status ck_create(const ck_config* cfg, ck_handle** out) {
   h->useGraph = cfg->use_graph;
   h->sortQueue = true;
   if (cfg->autotune_cache) h->cachePath = cfg->autotune_cache;
-  for (int p = 0; p < 2; ++p) {
+  for (int p = 0; p < CK_NUM_PRECISIONS; ++p) {
     h->tune[p].variant = 0;
     h->tune[p].tpb = cfg->threads_per_block > 0 ? std::min(cfg->threads_per_block, kFitMaxBlock)
                                                 : kFitMaxBlock;
@@ -452,7 +459,7 @@ ck_status ck_create(const ck_config* cfg, ck_handle** out) {
     h->tune[p].tuned = false;
   }
   loadTuneCache(h);
-  for (int p = 0; p < 2; ++p) {
+  for (int p = 0; p < CK_NUM_PRECISIONS; ++p) {
     if (h->tune[p].bps <= 0) {
       // default: as many resident blocks as the register budget allows
       h->tune[p].bps = ck::occupancyBlocks(p, h->tune[p].variant, h->tune[p].tpb);
@@ -470,11 +477,7 @@ ck_status ck_destroy(ck_handle* h) {
   if (h->graphExec) cudaGraphExecDestroy(h->graphExec);
   for (auto& b : h->inBufs) b.release();
   for (auto& b : h->outBufs) b.release();
-  h->rec.release();
-  h->recMeta.release();
-  h->recMetaD.release();
-  h->perm.release();
-  h->ticket.release();
+  h->ctx.release();
   h->unitBuf.release();
   if (h->dSurfaces) cudaFree(h->dSurfaces);
   if (h->dNodes) cudaFree(h->dNodes);
@@ -596,7 +599,8 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
   }
 
   // ---- pipeline (graph-captured for device-resident batches)
-  ck_status s = preparePipeline(h, n, out->max_states, tn);
+  const int gridBlocks = gridBlocksFor(h, tn);
+  ck_status s = preparePipeline(h, h->ctx, n, out->max_states, tn, gridBlocks);
   if (s != CK_OK) return s;
   const bool deviceOnly = in->memory == CK_MEM_DEVICE && out->memory == CK_MEM_DEVICE;
   if (deviceOnly && h->useGraph && n > 0) {
@@ -606,11 +610,11 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
     key.opt = *opt;
     key.tune = tn;
     key.stream = st;
-    key.scratch[0] = h->rec.p;
-    key.scratch[1] = h->recMeta.p;
-    key.scratch[2] = h->recMetaD.p;
-    key.scratch[3] = h->perm.p;
-    key.scratch[4] = h->ticket.p;
+    key.scratch[0] = h->ctx.rec.p;
+    key.scratch[1] = h->ctx.recMeta.p;
+    key.scratch[2] = h->ctx.recMetaD.p;
+    key.scratch[3] = h->ctx.perm.p;
+    key.scratch[4] = h->ctx.ticket.p;
     key.sort = h->sortQueue;
     if (!h->graphExec || std::memcmp(&key, &h->graphKey, sizeof(key)) != 0) {
       if (h->graphExec) {
@@ -620,7 +624,7 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
       cudaGraph_t g;
       if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
         return cudaFail(e, "graph capture begin");
-      s = enqueuePipeline(h, *opt, din, dout, tn, st, true);
+      s = enqueuePipeline(h, h->ctx, *opt, din, dout, tn, st, true, gridBlocks);
       e = cudaStreamEndCapture(st, &g);
       if (s != CK_OK) return s;
       if (e != cudaSuccess) return cudaFail(e, "graph capture end");
@@ -634,7 +638,7 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
     h->lastLaunches = h->graphLaunches;
     h->lastTimed = true;
   } else {
-    s = enqueuePipeline(h, *opt, din, dout, tn, st, true);
+    s = enqueuePipeline(h, h->ctx, *opt, din, dout, tn, st, true, gridBlocks);
     if (s != CK_OK) return s;
   }
   size_t d2h = 0;
@@ -686,7 +690,7 @@ ck_status ck_last_transfer_bytes(ck_handle* h, int64_t* h2d, int64_t* d2h) {
 }
 
 ck_status ck_get_launch_config(ck_handle* h, int32_t precision, int32_t* tpb, int32_t* bps) {
-  if (!h || !tpb || !bps || precision < 0 || precision > 1)
+  if (!h || !tpb || !bps || precision < 0 || precision >= CK_NUM_PRECISIONS)
     return fail(CK_ERR_INVALID_ARGUMENT, "bad argument");
   *tpb = h->tune[precision].tpb;
   *bps = h->tune[precision].bps;
@@ -695,7 +699,7 @@ ck_status ck_get_launch_config(ck_handle* h, int32_t precision, int32_t* tpb, in
 
 ck_status ck_set_launch_config(ck_handle* h, int32_t precision, int32_t variant, int32_t tpb,
                                int32_t bps) {
-  if (!h || precision < 0 || precision > 1 || variant < 0 || variant >= kNumFitVariants ||
+  if (!h || precision < 0 || precision >= CK_NUM_PRECISIONS || variant < 0 || variant >= kNumFitVariants ||
       tpb <= 0 || tpb > kFitMaxBlock || (tpb % 32) != 0 || bps <= 0)
     return fail(CK_ERR_INVALID_ARGUMENT, "bad launch configuration");
   std::lock_guard<std::mutex> lock(h->mu);

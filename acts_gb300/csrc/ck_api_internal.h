@@ -43,6 +43,20 @@ struct GraphKey {
 
 int occupancyBlocks(int precision, int variant, int tpb);
 
+// Scratch of one batch pipeline in flight: records of the resident lanes,
+// the ordered work queue and its ticket. A handle owns one; the serving loop
+// owns one per stream.
+struct FitContext {
+  DevBuf rec, recMeta, recMetaD, perm, ticket;
+  void release() {
+    rec.release();
+    recMeta.release();
+    recMetaD.release();
+    perm.release();
+    ticket.release();
+  }
+};
+
 extern thread_local std::string g_lastError;
 ck_status fail(ck_status s, const std::string& msg);
 ck_status cudaFail(cudaError_t e, const char* what);
@@ -50,6 +64,12 @@ ck_status validateOptions(const ck_options* o);
 DevOptions toDevOptions(const ck_options& o);
 MatConst makeMatConst();
 DevSurface toDevSurface(const ck_surface& s);
+ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, const Tune& tn,
+                          int gridBlocks);
+ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
+                          const ck_batch_in& din, const ck_batch_out& dout, const Tune& tn,
+                          cudaStream_t st, bool timed, int gridBlocks);
+int gridBlocksFor(ck_handle* h, const Tune& tn);
 
 }  // namespace ck
 
@@ -65,14 +85,15 @@ struct ck_handle {
   ck::DevField field{};
   float4* dNodes = nullptr;
   ck::MatConst mc{};
-  ck::Tune tune[2]{};
+  ck::Tune tune[CK_NUM_PRECISIONS]{};
   std::string cachePath;
   std::string tuneLog;
   int useGraph = 1;
   bool sortQueue = true;
   ck::DevBuf inBufs[11];
   ck::DevBuf outBufs[18];
-  ck::DevBuf rec, recMeta, recMetaD, perm, ticket, unitBuf;
+  ck::FitContext ctx;
+  ck::DevBuf unitBuf;
   int lastLaunches = 0;
   bool lastTimed = false;
   size_t lastH2D = 0, lastD2H = 0;

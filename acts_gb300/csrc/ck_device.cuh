@@ -349,6 +349,9 @@ CK_D void initTransport(const Surf<P>& s, const P f[8], Transport<P>& T) {
 
 // ------------------------------------------------------------------ field
 template <typename P>
+CK_D bool getGridField(const DevField& F, const P p[3], P B[3]);
+
+template <typename P>
 CK_D bool getField(const DevField& F, const P p[3], P B[3]) {
   if (F.kind == CK_FIELD_CONSTANT) {
     B[0] = (P)F.b[0];
@@ -356,6 +359,11 @@ CK_D bool getField(const DevField& F, const P p[3], P B[3]) {
     B[2] = (P)F.b[2];
     return true;
   }
+  return getGridField(F, p, B);
+}
+
+template <typename P>
+CK_D bool getGridField(const DevField& F, const P p[3], P B[3]) {
   // InterpolatedBFieldMap::getField with the equidistant axes of
   // fieldMapXYZ and the trilinear interpolate (z, then y, then x)
   int bin[3];

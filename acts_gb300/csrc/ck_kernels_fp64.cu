@@ -39,8 +39,11 @@ int occupancyFP64(int variant, int tpb) {
 }
 
 int occupancyBlocks(int precision, int variant, int tpb) {
-  return precision == CK_PRECISION_MIXED ? occupancyMixed(variant, tpb)
-                                         : occupancyFP64(variant, tpb);
+  switch (precision) {
+    case CK_PRECISION_MIXED: return occupancyMixed(variant, tpb);
+    case CK_PRECISION_MIXED_COV64: return occupancyMixedCov64(variant, tpb);
+    default: return occupancyFP64(variant, tpb);
+  }
 }
 
 }  // namespace ck

@@ -14,8 +14,11 @@ cudaError_t launchFitFP64(const FitParams& fp, int variant, int grid, int block,
                           cudaStream_t st);
 cudaError_t launchFitMixed(const FitParams& fp, int variant, int grid, int block,
                            cudaStream_t st);
+cudaError_t launchFitMixedCov64(const FitParams& fp, int variant, int grid, int block,
+                                cudaStream_t st);
 int occupancyFP64(int variant, int tpb);
 int occupancyMixed(int variant, int tpb);
+int occupancyMixedCov64(int variant, int tpb);
 int occupancyBlocks(int precision, int variant, int tpb);
 
 }  // namespace ck

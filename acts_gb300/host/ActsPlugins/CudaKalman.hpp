@@ -1,0 +1,327 @@
+// ActsPlugins/CudaKalman.hpp — C++ facade of the CudaKalman fitter.
+//
+// Header-only host code over the C ABI (include/cudakalman.h). It mirrors
+// the call a reference user makes,
+//
+//   Acts::KalmanFitter<Propagator<EigenStepper<>, DirectNavigator>,
+//                      VectorMultiTrajectory>::fit(begin, end, startParameters,
+//                                                  kfOptions, sSequence,
+//                                                  trackContainer)
+//   (Core/include/Acts/TrackFitting/KalmanFitter.hpp:719-731)
+//
+// with the same argument meaning: an iterator range of source links, bound
+// start parameters, the fit options, the DirectNavigator surface sequence and
+// a track container the fitted track and its states are appended to; it
+// returns a Result that holds either the new track's index or the error the
+// reference would return. fitBatch() takes many tracks at once (the per-track
+// loop of TrackFittingAlgorithm::execute,
+// Examples/Algorithms/TrackFitting/src/TrackFittingAlgorithm.cpp:117-170).
+//
+// The ACTS types this build cannot include (Eigen/Boost are not available)
+// are represented by small structs with the same fields; a build against a
+// real ACTS installation maps Acts::BoundTrackParameters, SourceLink and
+// VectorMultiTrajectory onto them one to one.
+#pragma once
+
+#include <array>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <stdexcept>
+#include <string>
+#include <system_error>
+#include <vector>
+
+#include "cudakalman.h"
+
+namespace ActsPlugins {
+
+// Track-level errors, mirroring Acts::KalmanFitterError / PropagatorError /
+// EigenStepperError / SurfaceError / MagneticFieldError by name.
+enum class CudaKalmanError : int {
+  UpdateFailed = CK_TRACK_UPDATE_FAILED,
+  SmoothFailed = CK_TRACK_SMOOTH_FAILED,
+  NoMeasurementFound = CK_TRACK_NO_MEASUREMENT_FOUND,
+  StepCountLimitReached = CK_TRACK_STEP_COUNT_LIMIT,
+  NextTargetLimitReached = CK_TRACK_NEXT_TARGET_LIMIT,
+  StepSizeStalled = CK_TRACK_STEP_SIZE_STALLED,
+  StepSizeAdjustmentFailed = CK_TRACK_STEP_ADJUST_FAILED,
+  GlobalPositionNotOnSurface = CK_TRACK_NOT_ON_SURFACE,
+  MagneticFieldOutOfBounds = CK_TRACK_FIELD_OUT_OF_BOUNDS,
+  TooManyStates = CK_TRACK_TOO_MANY_STATES,
+  NotProcessed = CK_TRACK_NOT_PROCESSED,
+  InvalidInput = CK_TRACK_INVALID_INPUT,
+};
+
+inline const char* errorName(int code) {
+  switch (code) {
+    case CK_TRACK_UPDATE_FAILED: return "UpdateFailed";
+    case CK_TRACK_SMOOTH_FAILED: return "SmoothFailed";
+    case CK_TRACK_NO_MEASUREMENT_FOUND: return "NoMeasurementFound";
+    case CK_TRACK_STEP_COUNT_LIMIT: return "StepCountLimitReached";
+    case CK_TRACK_NEXT_TARGET_LIMIT: return "NextTargetLimitReached";
+    case CK_TRACK_STEP_SIZE_STALLED: return "StepSizeStalled";
+    case CK_TRACK_STEP_ADJUST_FAILED: return "StepSizeAdjustmentFailed";
+    case CK_TRACK_NOT_ON_SURFACE: return "GlobalPositionNotOnSurface";
+    case CK_TRACK_FIELD_OUT_OF_BOUNDS: return "MagneticFieldOutOfBounds";
+    case CK_TRACK_TOO_MANY_STATES: return "TooManyStates";
+    case CK_TRACK_NOT_PROCESSED: return "NotProcessed";
+    case CK_TRACK_INVALID_INPUT: return "InvalidInput";
+    default: return "ok";
+  }
+}
+
+// Acts::Result<T> analogue: a value or an error code.
+template <typename T>
+class Result {
+ public:
+  static Result success(T v) { return Result(std::move(v), 0); }
+  static Result failure(int e) { return Result(T{}, e); }
+  bool ok() const { return m_error == 0; }
+  const T& value() const {
+    if (!ok())
+      throw std::runtime_error(std::string("Result has error ") + ActsPlugins::errorName(m_error));
+    return m_value;
+  }
+  int error() const { return m_error; }
+  const char* errorName() const { return ActsPlugins::errorName(m_error); }
+
+ private:
+  Result(T v, int e) : m_value(std::move(v)), m_error(e) {}
+  T m_value;
+  int m_error;
+};
+
+using BoundVector = std::array<double, 6>;
+using BoundMatrix = std::array<double, 36>;  // row-major
+
+// Acts::BoundTrackParameters on a plane surface, with its particle
+// hypothesis (EventData/BoundTrackParameters.hpp, ParticleHypothesis.hpp).
+struct BoundTrackParameters {
+  BoundVector parameters{};      // loc0, loc1, phi, theta, q/p, t
+  BoundMatrix covariance{};      // row-major
+  std::array<double, 9> planeRotation{1, 0, 0, 0, 1, 0, 0, 0, 1};  // columns = local axes
+  std::array<double, 3> planeCenter{0, 0, 0};
+  float mass = 0.13957039f;      // GeV (float, as ParticleHypothesis stores it)
+  float absCharge = 1.0f;
+  int absPdg = 211;
+};
+
+// A source link after the pass-through calibrator: a 2D measurement on
+// (loc0, loc1) of a surface (TestSourceLink + testSourceLinkCalibrator).
+struct SourceLink {
+  int surface = -1;
+  std::array<double, 2> value{};
+  std::array<double, 4> covariance{};  // row-major 2x2
+};
+
+// KalmanFitterOptions + plain stepper / propagator options.
+struct KalmanFitterOptions {
+  ck_options options;
+  KalmanFitterOptions() { ck_options_default(&options); }
+};
+
+// One track state as VectorMultiTrajectory stores it
+// (EventData/VectorMultiTrajectory.hpp:187-200).
+struct TrackState {
+  int surface = -1;
+  uint32_t typeFlags = 0;
+  double pathLength = 0;
+  double chi2 = 0;
+  BoundVector predicted{}, filtered{}, smoothed{};
+  BoundMatrix predictedCovariance{}, filteredCovariance{}, smoothedCovariance{}, jacobian{};
+  bool isMeasurement() const {
+    return (typeFlags & CK_FLAG_HAS_MEASUREMENT) && !(typeFlags & CK_FLAG_IS_OUTLIER);
+  }
+  bool isOutlier() const { return typeFlags & CK_FLAG_IS_OUTLIER; }
+  bool isHole() const { return typeFlags & CK_FLAG_IS_HOLE; }
+};
+
+// Minimal TrackContainer: tracks own a contiguous range of states in
+// propagation order (trackStates() after linkForward()).
+struct Track {
+  size_t firstState = 0;
+  size_t nStates = 0;
+  size_t nMeasurements = 0, nHoles = 0, nOutliers = 0, nDoF = 0;
+  double chi2 = 0;
+};
+
+struct TrackContainer {
+  std::vector<TrackState> states;
+  std::vector<Track> tracks;
+  const TrackState* trackStates(size_t track) const { return states.data() + tracks[track].firstState; }
+};
+
+// One track of a batch.
+struct TrackInput {
+  const SourceLink* sourceLinks = nullptr;
+  size_t nSourceLinks = 0;
+  BoundTrackParameters start;
+  const int* surfaceSequence = nullptr;
+  size_t nSurfaces = 0;
+};
+
+class CudaKalman {
+ public:
+  struct Config {
+    std::vector<ck_surface> surfaces;
+    ck_field field{};
+    int device = 0;
+    bool useGraph = true;
+    int maxStates = 64;
+  };
+
+  explicit CudaKalman(Config cfg) : m_cfg(std::move(cfg)) {
+    ck_config c{};
+    c.device = m_cfg.device;
+    c.n_surfaces = static_cast<int32_t>(m_cfg.surfaces.size());
+    c.surfaces = m_cfg.surfaces.data();
+    c.field = m_cfg.field;
+    c.use_graph = m_cfg.useGraph ? 1 : 0;
+    ck_status s = ck_create(&c, &m_handle);
+    if (s != CK_OK) throw std::runtime_error(std::string("ck_create: ") + ck_last_error());
+  }
+  ~CudaKalman() {
+    if (m_handle) ck_destroy(m_handle);
+  }
+  CudaKalman(const CudaKalman&) = delete;
+  CudaKalman& operator=(const CudaKalman&) = delete;
+
+  // KalmanFitter::fit with a DirectNavigator surface sequence: a batch of one.
+  template <typename source_link_iterator_t>
+  Result<size_t> fit(source_link_iterator_t begin, source_link_iterator_t end,
+                     const BoundTrackParameters& start, const KalmanFitterOptions& options,
+                     const std::vector<int>& sSequence, TrackContainer& container) const {
+    std::vector<SourceLink> links(begin, end);
+    TrackInput in;
+    in.sourceLinks = links.data();
+    in.nSourceLinks = links.size();
+    in.start = start;
+    in.surfaceSequence = sSequence.data();
+    in.nSurfaces = sSequence.size();
+    std::vector<Result<size_t>> r = fitBatch(&in, 1, options, container);
+    return r.front();
+  }
+
+  // Fits n tracks in one call; one Result (track index or error) per input.
+  std::vector<Result<size_t>> fitBatch(const TrackInput* tracks, size_t n,
+                                       const KalmanFitterOptions& options,
+                                       TrackContainer& container) const {
+    std::vector<int32_t> seqOff(n + 1, 0), measOff(n + 1, 0), seq, measSurf, pdg(n);
+    std::vector<double> measVal, measCov, sp(6 * n), sc(36 * n), frames(12 * n);
+    std::vector<float> part(2 * n);
+    for (size_t t = 0; t < n; ++t) {
+      const TrackInput& ti = tracks[t];
+      for (size_t k = 0; k < ti.nSurfaces; ++k) seq.push_back(ti.surfaceSequence[k]);
+      seqOff[t + 1] = static_cast<int32_t>(seq.size());
+      for (size_t k = 0; k < ti.nSourceLinks; ++k) {
+        const SourceLink& sl = ti.sourceLinks[k];
+        measSurf.push_back(sl.surface);
+        measVal.insert(measVal.end(), sl.value.begin(), sl.value.end());
+        measCov.insert(measCov.end(), sl.covariance.begin(), sl.covariance.end());
+      }
+      measOff[t + 1] = static_cast<int32_t>(measSurf.size());
+      std::memcpy(&sp[6 * t], ti.start.parameters.data(), 6 * sizeof(double));
+      std::memcpy(&sc[36 * t], ti.start.covariance.data(), 36 * sizeof(double));
+      std::memcpy(&frames[12 * t], ti.start.planeRotation.data(), 9 * sizeof(double));
+      std::memcpy(&frames[12 * t + 9], ti.start.planeCenter.data(), 3 * sizeof(double));
+      part[2 * t] = ti.start.mass;
+      part[2 * t + 1] = ti.start.absCharge;
+      pdg[t] = ti.start.absPdg;
+    }
+    ck_batch_in in{};
+    in.n_tracks = static_cast<int32_t>(n);
+    in.memory = CK_MEM_HOST;
+    in.seq_offsets = seqOff.data();
+    in.seq_surfaces = seq.data();
+    in.meas_offsets = measOff.data();
+    in.meas_surfaces = measSurf.data();
+    in.meas_values = measVal.data();
+    in.meas_cov = measCov.data();
+    in.start_params = sp.data();
+    in.start_cov = sc.data();
+    in.start_frames = frames.data();
+    in.particle = part.data();
+    in.particle_pdg = pdg.data();
+
+    const int ms = m_cfg.maxStates;
+    const size_t S = static_cast<size_t>(ms) * n;
+    std::vector<int32_t> status(n), nStates(n), nMeas(n), nHoles(n), nOut(n), ndf(n), surf(S);
+    std::vector<uint32_t> flags(S);
+    std::vector<double> chi2(n), path(S), schi2(S), pr(6 * S), prc(36 * S), fi(6 * S), fic(36 * S),
+        sm(6 * S), smc(36 * S), jac(36 * S);
+    ck_batch_out out{};
+    out.max_states = ms;
+    out.components = CK_OUT_PREDICTED | CK_OUT_FILTERED | CK_OUT_SMOOTHED | CK_OUT_JACOBIAN;
+    out.memory = CK_MEM_HOST;
+    out.status = status.data();
+    out.n_states = nStates.data();
+    out.n_measurements = nMeas.data();
+    out.n_holes = nHoles.data();
+    out.n_outliers = nOut.data();
+    out.ndf = ndf.data();
+    out.chi2_sum = chi2.data();
+    out.state_surface = surf.data();
+    out.state_flags = flags.data();
+    out.state_path_length = path.data();
+    out.state_chi2 = schi2.data();
+    out.predicted = pr.data();
+    out.predicted_cov = prc.data();
+    out.filtered = fi.data();
+    out.filtered_cov = fic.data();
+    out.smoothed = sm.data();
+    out.smoothed_cov = smc.data();
+    out.jacobian = jac.data();
+    ck_status s = ck_fit_batch(m_handle, &options.options, &in, &out, nullptr);
+    if (s == CK_OK) s = ck_sync(m_handle);
+    if (s != CK_OK) throw std::runtime_error(std::string("ck_fit_batch: ") + ck_last_error());
+
+    std::vector<Result<size_t>> results;
+    results.reserve(n);
+    auto at = [&](size_t k, size_t C, size_t c, size_t t) { return (k * C + c) * n + t; };
+    for (size_t t = 0; t < n; ++t) {
+      if (status[t] != CK_TRACK_OK) {
+        results.push_back(Result<size_t>::failure(status[t]));
+        continue;
+      }
+      Track tr;
+      tr.firstState = container.states.size();
+      tr.nStates = static_cast<size_t>(nStates[t]);
+      tr.nMeasurements = static_cast<size_t>(nMeas[t]);
+      tr.nHoles = static_cast<size_t>(nHoles[t]);
+      tr.nOutliers = static_cast<size_t>(nOut[t]);
+      tr.nDoF = static_cast<size_t>(ndf[t]);
+      tr.chi2 = chi2[t];
+      for (size_t k = 0; k < tr.nStates; ++k) {
+        TrackState st;
+        st.surface = surf[at(k, 1, 0, t)];
+        st.typeFlags = flags[at(k, 1, 0, t)];
+        st.pathLength = path[at(k, 1, 0, t)];
+        st.chi2 = schi2[at(k, 1, 0, t)];
+        for (size_t c = 0; c < 6; ++c) {
+          st.predicted[c] = pr[at(k, 6, c, t)];
+          st.filtered[c] = fi[at(k, 6, c, t)];
+          st.smoothed[c] = sm[at(k, 6, c, t)];
+        }
+        for (size_t c = 0; c < 36; ++c) {
+          st.predictedCovariance[c] = prc[at(k, 36, c, t)];
+          st.filteredCovariance[c] = fic[at(k, 36, c, t)];
+          st.smoothedCovariance[c] = smc[at(k, 36, c, t)];
+          st.jacobian[c] = jac[at(k, 36, c, t)];
+        }
+        container.states.push_back(st);
+      }
+      container.tracks.push_back(tr);
+      results.push_back(Result<size_t>::success(container.tracks.size() - 1));
+    }
+    return results;
+  }
+
+  ck_handle* handle() const { return m_handle; }
+
+ private:
+  Config m_cfg;
+  ck_handle* m_handle = nullptr;
+};
+
+}  // namespace ActsPlugins

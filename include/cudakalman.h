@@ -150,7 +150,14 @@ typedef struct ck_field {
 
 /* ------------------------------------------------------------- options */
 
-enum { CK_PRECISION_FP64 = 0, CK_PRECISION_MIXED = 1 };
+/* FP64: everything in double (the reference's arithmetic).
+ * MIXED: stepper, Jacobian transport, field interpolation and covariance
+ *   transport in FP32; Kalman update (Joseph form when selected), 2x2
+ *   inverse, smoother-gain inverse and chi2 in FP64.
+ * MIXED_COV64: as MIXED, but the covariance is kept and transported in FP64
+ *   (the transport Jacobian itself stays FP32). */
+enum { CK_PRECISION_FP64 = 0, CK_PRECISION_MIXED = 1, CK_PRECISION_MIXED_COV64 = 2 };
+#define CK_NUM_PRECISIONS 3
 
 /* Fit options. ck_options_default() fills the reference defaults:
  *   StepperPlainOptions (Core/include/Acts/Propagator/StepperOptions.hpp:36-49)
@@ -176,7 +183,7 @@ typedef struct ck_options {
   int32_t multiple_scattering;  /* 1                                       */
   int32_t energy_loss;          /* 1                                       */
   int32_t use_joseph;           /* 0 (GainMatrixUpdater default)           */
-  int32_t precision;            /* CK_PRECISION_FP64 / CK_PRECISION_MIXED  */
+  int32_t precision;            /* CK_PRECISION_*                          */
   double outlier_chi2_cut;      /* +inf                                    */
   /* Extensions outside the reference's declared set are rejected with
    * CK_ERR_UNSUPPORTED: reverse filtering, free-to-bound correction and
@@ -425,6 +432,8 @@ ck_status ck_server_poll(ck_server* s, int64_t* event_id, ck_batch_out* out,
 /* Counters: events submitted, completed, tracks completed, bytes in use. */
 ck_status ck_server_stats(ck_server* s, int64_t* submitted, int64_t* completed,
                           int64_t* tracks, int64_t* bytes_in_use);
+/* Tracks one stream slot can hold (the largest event accepted). */
+int32_t ck_server_capacity(ck_server* s);
 ck_status ck_server_destroy(ck_server* s);
 
 #ifdef __cplusplus
