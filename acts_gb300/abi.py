@@ -51,8 +51,7 @@ FIELD_GRID_XYZ = 1
 
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
-PRECISION_MIXED_COV64 = 2
-NUM_PRECISIONS = 3
+NUM_PRECISIONS = 2
 
 MEM_HOST = 0
 MEM_DEVICE = 1

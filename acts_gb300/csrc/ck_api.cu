@@ -207,43 +207,55 @@ cudaError_t launchFit(const FitParams& fp, int precision, const Tune& tn, int gr
                       cudaStream_t st) {
   switch (precision) {
     case CK_PRECISION_MIXED: return launchFitMixed(fp, tn.variant, grid, tn.tpb, st);
-    case CK_PRECISION_MIXED_COV64: return launchFitMixedCov64(fp, tn.variant, grid, tn.tpb, st);
     default: return launchFitFP64(fp, tn.variant, grid, tn.tpb, st);
   }
 }
 
 int gridBlocksFor(ck_handle* h, const Tune& tn) { return h->smCount * tn.bps; }
 
-// Allocates (grow-only) the scratch of a batch pipeline. Never called while
-// a stream is being captured.
-ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, const Tune& tn,
-                          int gridBlocks) {
+size_t recordMatrixElem(int precision) {
+  return precision == CK_PRECISION_MIXED ? sizeof(float) : sizeof(double);
+}
+
+size_t recordBytesPerTrack(int maxStates, int precision) {
+  return (size_t)maxStates * (kRecParams * sizeof(double) + kRecMatrix * recordMatrixElem(precision) +
+                              2 * sizeof(int32_t) + 2 * sizeof(double)) +
+         2 * sizeof(int32_t);
+}
+
+// Allocates (grow-only) the scratch of a batch pipeline: the track-state
+// records of n tracks, the queue permutation and the tips. Never called
+// while a stream is being captured.
+ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, int precision) {
   (void)h;
-  const int nSlots = gridBlocks * tn.tpb;
   cudaError_t e;
-  if ((e = c.rec.ensure(compBytes(nSlots, maxStates, kRecDoubles, sizeof(double)))) ||
-      (e = c.recMeta.ensure(compBytes(nSlots, maxStates, 2, sizeof(int32_t)))) ||
-      (e = c.recMetaD.ensure(compBytes(nSlots, maxStates, 2, sizeof(double)))) ||
+  const size_t recBytes = compBytes(n, maxStates, kRecParams, sizeof(double)) +
+                          compBytes(n, maxStates, kRecMatrix, recordMatrixElem(precision));
+  if ((e = c.rec.ensure(recBytes)) ||
+      (e = c.recMeta.ensure(compBytes(n, maxStates, 2, sizeof(int32_t)))) ||
+      (e = c.recMetaD.ensure(compBytes(n, maxStates, 2, sizeof(double)))) ||
       (e = c.perm.ensure((size_t)n * sizeof(int32_t) + 16)) ||
+      (e = c.tip.ensure((size_t)n * sizeof(int32_t) + 16)) ||
       (e = c.ticket.ensure(sizeof(int32_t) * (kBins + 1))))
     return cudaFail(e, "scratch allocation");
   return CK_OK;
 }
 
 // Records the whole batch pipeline (inputs already on the device, scratch
-// prepared) on `st`: queue reset, queue ordering, fit kernel.
+// prepared) on `st`: queue reset, queue ordering, forward-filter kernel,
+// smoother kernel.
 ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
                           const ck_batch_in& din, const ck_batch_out& dout, const Tune& tn,
                           cudaStream_t st, bool timed, int gridBlocks) {
   const int n = din.n_tracks;
   const int grid = gridBlocks;
-  const int nSlots = grid * tn.tpb;
   const int maxStates = dout.max_states;
   cudaError_t e;
   int32_t* dTicket = (int32_t*)c.ticket.p;
   int32_t* dBins = dTicket + 1;
   int launches = 0;
   cudaMemsetAsync(dTicket, 0, sizeof(int32_t) * (kBins + 1), st);
+  if (n > 0) cudaMemsetAsync(c.tip.p, 0xff, sizeof(int32_t) * (size_t)n, st);
   const int32_t* perm = nullptr;
   if (h->sortQueue && n > 0) {
     const int tb = 256;
@@ -273,9 +285,11 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
   fp.perm = perm;
   fp.ticket = dTicket;
   fp.rec = (double*)c.rec.p;
+  fp.rec_mat = (void*)((double*)c.rec.p + (size_t)n * maxStates * kRecParams);
   fp.rec_meta = (int32_t*)c.recMeta.p;
   fp.rec_meta_d = (double*)c.recMetaD.p;
-  fp.n_slots = nSlots;
+  fp.tip = (int32_t*)c.tip.p;
+  fp.rec_stride = n;
   fp.max_states = maxStates;
   fp.out = dout;
   fp.surfaces = h->dSurfaces;
@@ -283,13 +297,24 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
   fp.field = h->field;
   fp.mc = h->mc;
   fp.opt = toDevOptions(opt);
-  if (timed) cudaEventRecord(h->ev0, st);
+  // inside a stream capture the timing events become event-record nodes of
+  // the graph (cudaEventRecordExternal), so they time every replay
+  unsigned recFlags = cudaEventRecordDefault;
+  if (timed) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive)
+      recFlags = cudaEventRecordExternal;
+    cudaEventRecordWithFlags(h->ev0, st, recFlags);
+  }
   if (n > 0) {
     e = launchFit(fp, opt.precision, tn, grid, st);
     if (e != cudaSuccess) return cudaFail(e, "fit kernel launch");
     ++launches;
+    e = launchSmooth(fp, opt.precision, st);
+    if (e != cudaSuccess) return cudaFail(e, "smoother kernel launch");
+    ++launches;
   }
-  if (timed) cudaEventRecord(h->ev1, st);
+  if (timed) cudaEventRecordWithFlags(h->ev1, st, recFlags);
   h->lastLaunches = launches;
   h->lastTimed = timed;
   return CK_OK;
@@ -600,7 +625,7 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
 
   // ---- pipeline (graph-captured for device-resident batches)
   const int gridBlocks = gridBlocksFor(h, tn);
-  ck_status s = preparePipeline(h, h->ctx, n, out->max_states, tn, gridBlocks);
+  ck_status s = preparePipeline(h, h->ctx, n, out->max_states, opt->precision);
   if (s != CK_OK) return s;
   const bool deviceOnly = in->memory == CK_MEM_DEVICE && out->memory == CK_MEM_DEVICE;
   if (deviceOnly && h->useGraph && n > 0) {
@@ -615,6 +640,7 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
     key.scratch[2] = h->ctx.recMetaD.p;
     key.scratch[3] = h->ctx.perm.p;
     key.scratch[4] = h->ctx.ticket.p;
+    key.scratch[5] = h->ctx.tip.p;
     key.sort = h->sortQueue;
     if (!h->graphExec || std::memcmp(&key, &h->graphKey, sizeof(key)) != 0) {
       if (h->graphExec) {

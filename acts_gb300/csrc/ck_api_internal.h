@@ -36,7 +36,7 @@ struct GraphKey {
   ck_options opt;
   Tune tune;
   cudaStream_t stream;
-  void* scratch[5];
+  void* scratch[6];
   bool sort;
   GraphKey() { std::memset(this, 0, sizeof(*this)); }
 };
@@ -47,8 +47,9 @@ int occupancyBlocks(int precision, int variant, int tpb);
 // the ordered work queue and its ticket. A handle owns one; the serving loop
 // owns one per stream.
 struct FitContext {
-  DevBuf rec, recMeta, recMetaD, perm, ticket;
+  DevBuf rec, recMeta, recMetaD, perm, ticket, tip;
   void release() {
+    tip.release();
     rec.release();
     recMeta.release();
     recMetaD.release();
@@ -64,8 +65,8 @@ ck_status validateOptions(const ck_options* o);
 DevOptions toDevOptions(const ck_options& o);
 MatConst makeMatConst();
 DevSurface toDevSurface(const ck_surface& s);
-ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, const Tune& tn,
-                          int gridBlocks);
+size_t recordBytesPerTrack(int maxStates, int precision);
+ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, int precision);
 ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
                           const ck_batch_in& din, const ck_batch_out& dout, const Tune& tn,
                           cudaStream_t st, bool timed, int gridBlocks);

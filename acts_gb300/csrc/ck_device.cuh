@@ -526,13 +526,15 @@ CK_D Inv2 inverse2(double m00, double m01, double m10, double m11) {
 }
 
 // 6x6 inverse of a symmetric matrix given packed, by LU with partial
-// pivoting (the algorithm of Eigen's fixed-size inverse for N > 4).
-CK_D void inverse6(const double* __restrict__ Cp, double inv[36]) {
+// pivoting (the algorithm of Eigen's fixed-size inverse for N > 4). The
+// divisions by the pivots are multiplications by one reciprocal per pivot.
+template <typename T>
+CK_D void inverse6(const T* __restrict__ Cp, double inv[36]) {
   double lu[36];
 #pragma unroll
   for (int i = 0; i < 6; ++i)
 #pragma unroll
-    for (int j = 0; j < 6; ++j) lu[i * 6 + j] = Cp[sidx(i, j)];
+    for (int j = 0; j < 6; ++j) lu[i * 6 + j] = (double)Cp[sidx(i, j)];
   int perm[6] = {0, 1, 2, 3, 4, 5};
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
@@ -563,15 +565,18 @@ CK_D void inverse6(const double* __restrict__ Cp, double inv[36]) {
         }
       }
     }
-    double piv = lu[k * 6 + k];
+    const double rpiv = 1.0 / lu[k * 6 + k];
 #pragma unroll
     for (int i = k + 1; i < 6; ++i) {
-      double l = lu[i * 6 + k] / piv;
+      double l = lu[i * 6 + k] * rpiv;
       lu[i * 6 + k] = l;
 #pragma unroll
       for (int j = k + 1; j < 6; ++j) lu[i * 6 + j] = lu[i * 6 + j] - l * lu[k * 6 + j];
     }
   }
+  double rdiag[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) rdiag[i] = 1.0 / lu[i * 6 + i];
 #pragma unroll
   for (int c = 0; c < 6; ++c) {
     double y[6];
@@ -587,7 +592,7 @@ CK_D void inverse6(const double* __restrict__ Cp, double inv[36]) {
       double s = y[i];
 #pragma unroll
       for (int j = i + 1; j < 6; ++j) s = s - lu[i * 6 + j] * inv[j * 6 + c];
-      inv[i * 6 + c] = s / lu[i * 6 + i];
+      inv[i * 6 + c] = s * rdiag[i];
     }
   }
 }
@@ -667,31 +672,35 @@ CK_D double predictedChi2(const double pred[6], const double Pp[21], double m0, 
 // GainMatrixSmoother::calculate. Inputs: filtered state k (filt, Pf packed),
 // state k+1 predicted (pp, Ppp packed), its Jacobian J (row-major 36) and its
 // smoothed state (ps, Psp packed). Outputs smoothed state k. False on NaN G.
-CK_D bool smoothStep(const double filt[6], const double Pf[21], const double pp[6],
-                     const double Ppp[21], const double* J, const double ps[6],
-                     const double Psp[21], double sm[6], double Ps[21]) {
+// The inverse of Ppp is taken in FP64; the gain and covariance products run
+// in GP (double in the plain form, float in the mixed form); parameters are
+// accumulated in FP64.
+template <typename GP>
+CK_D bool smoothStep(const double filt[6], const GP Pf[21], const double pp[6], const GP Ppp[21],
+                     const GP* J, const double ps[6], const GP Psp[21], double sm[6],
+                     GP Ps[21]) {
   double inv[36];
   inverse6(Ppp, inv);
   // G = (Pf J^T) Pinv
-  double PJ[36];
+  GP PJ[36];
 #pragma unroll
   for (int i = 0; i < 6; ++i)
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
-      double s = 0.0;
+      GP s = GP(0);
 #pragma unroll
       for (int k = 0; k < 6; ++k) s += Pf[sidx(i, k)] * J[j * 6 + k];
       PJ[i * 6 + j] = s;
     }
-  double G[36];
+  GP G[36];
   bool nan = false;
 #pragma unroll
   for (int i = 0; i < 6; ++i)
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
-      double s = 0.0;
+      GP s = GP(0);
 #pragma unroll
-      for (int k = 0; k < 6; ++k) s += PJ[i * 6 + k] * inv[k * 6 + j];
+      for (int k = 0; k < 6; ++k) s += PJ[i * 6 + k] * (GP)inv[k * 6 + j];
       G[i * 6 + j] = s;
       nan |= isnan(s);
     }
@@ -703,19 +712,19 @@ CK_D bool smoothStep(const double filt[6], const double Pf[21], const double pp[
   d[3] = radian_sym(d[3]);
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
-    double s = 0.0;
+    GP s = GP(0);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) s += G[i * 6 + k] * d[k];
-    sm[i] = filt[i] + s;
+    for (int k = 0; k < 6; ++k) s += G[i * 6 + k] * (GP)d[k];
+    sm[i] = filt[i] + (double)s;
   }
   normalizePhiTheta(sm[2], sm[3]);
   // Ps = Pf + G (Psp - Ppp) G^T
-  double GD[36];
+  GP GD[36];
 #pragma unroll
   for (int i = 0; i < 6; ++i)
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
-      double s = 0.0;
+      GP s = GP(0);
 #pragma unroll
       for (int k = 0; k < 6; ++k) s += G[i * 6 + k] * (Psp[sidx(k, j)] - Ppp[sidx(k, j)]);
       GD[i * 6 + j] = s;
@@ -724,7 +733,7 @@ CK_D bool smoothStep(const double filt[6], const double Pf[21], const double pp[
   for (int i = 0; i < 6; ++i)
 #pragma unroll
     for (int j = i; j < 6; ++j) {
-      double s = 0.0;
+      GP s = GP(0);
 #pragma unroll
       for (int k = 0; k < 6; ++k) s += GD[i * 6 + k] * G[j * 6 + k];
       Ps[sidx(i, j)] = Pf[sidx(i, j)] + s;

@@ -44,7 +44,7 @@ namespace ck {
 // and costs 5-10 %, so they stay inlined.
 #define CK_NI CK_D
 
-enum Phase { PH_FETCH = 0, PH_STEP = 1, PH_SURFACE = 2, PH_SMOOTH = 3, PH_DONE = 4 };
+enum Phase { PH_FETCH = 0, PH_STEP = 1, PH_SURFACE = 2, PH_DONE = 3 };
 
 // ChargeHypothesis::extractMomentum (ChargeHypothesis.hpp:70-90)
 template <typename P>
@@ -58,25 +58,32 @@ CK_D void cupdate(double& slot, double v) {
 }
 
 // scratch record access (one record set per resident lane)
+template <typename CV>
 struct Rec {
-  double* base;
+  double* par;
+  CV* mat;
   int ns;
   int slot;
-  CK_D double& at(int k, int f) const {
-    return base[((size_t)k * kRecDoubles + f) * (size_t)ns + slot];
-  }
+  CK_D Rec(const FitParams& fp, int s)
+      : par(fp.rec), mat(static_cast<CV*>(fp.rec_mat)), ns(fp.rec_stride), slot(s) {}
+  // bound parameters (FP64)
+  CK_D double& p(int k, int f) const { return par[((size_t)k * kRecParams + f) * (size_t)ns + slot]; }
+  // covariances and jacobian (CV)
+  CK_D CV& m(int k, int f) const { return mat[((size_t)k * kRecMatrix + f) * (size_t)ns + slot]; }
 };
 
 template <typename P, typename CV>
 struct Lane {
-  // ---- identity
+  // ---- identity: track index and queue position (which indexes the records)
   int phase;
   int t;
-  // ---- stepper (free parameters split by precision)
+  int q;
+  // ---- stepper: the free parameters are accumulated in FP64 in every form;
+  // the Runge-Kutta stages, field and transport are evaluated in P
   double pos[3];
-  P tim;
-  P dir[3];
-  P qop;
+  double tim;
+  double dir[3];
+  double qop;
   CV cov[21];
   Transport<P> T;
   P deriv[7];  // dir (3), dt/ds, k4 (3)
@@ -98,10 +105,6 @@ struct Lane {
   bool finished, coasting;
   double propLimit, kfLimit;
   int seq0, nSeq, m0, nMeas;
-  // ---- smoother / output
-  int smoothK, lastMeas, tip;
-  int nM, nH, nO, ndf;
-  double chi2sum;
 
   // ------------------------------------------------------------ helpers
   CK_D double stepValue() const {
@@ -119,6 +122,7 @@ struct Lane {
     if (out.n_outliers) out.n_outliers[t] = 0;
     if (out.ndf) out.ndf[t] = 0;
     if (out.chi2_sum) out.chi2_sum[t] = 0.0;
+    fp.tip[q] = -1;
     phase = PH_FETCH;
   }
 
@@ -132,12 +136,10 @@ struct Lane {
   CK_NI int intersectSurf(const FitParams& fp, int sid, double path[2], int st[2]) const {
     Surf<double> sf;
     sf.load(fp.surfaces + sid);
-    const double d[3] = {(double)dir[0], (double)dir[1], (double)dir[2]};
-    return intersect(sf, pos, d, fp.opt.surfaceTolerance, path, st);
+    return intersect(sf, pos, dir, fp.opt.surfaceTolerance, path, st);
   }
 
-  // Surface::globalToLocal with positions in double; the cylinder angle is
-  // evaluated in P.
+  // Surface::globalToLocal in double (the bound parameters are outputs)
   CK_NI bool toLocal(const Surf<double>& sf, double loc[2]) const {
     double l[3];
     sf.toLocal3(pos, l);
@@ -149,10 +151,9 @@ struct Lane {
     }
     double inttol = sf.radius * 0.0001;
     if (inttol < 0.01) inttol = 0.01;
-    const P l0 = (P)l[0], l1 = (P)l[1];
-    const P r = sqrt(l0 * l0 + l1 * l1);
-    if (fabs((double)r - sf.radius) > inttol) return false;
-    loc[0] = (double)((P)sf.radius * atan2(l1, l0));
+    const double r = sqrt(l[0] * l[0] + l[1] * l[1]);
+    if (fabs(r - sf.radius) > inttol) return false;
+    loc[0] = sf.radius * atan2(l[1], l[0]);
     loc[1] = l[2];
     return true;
   }
@@ -163,18 +164,18 @@ struct Lane {
     if (!toLocal(sf, loc)) return false;
     b[0] = loc[0];
     b[1] = loc[1];
-    b[5] = (double)tim;
-    b[2] = (double)atan2(dir[1], dir[0]);
-    b[3] = (double)atan2(sqrt(dir[0] * dir[0] + dir[1] * dir[1]), dir[2]);
-    b[4] = (double)qop;
+    b[5] = tim;
+    b[2] = atan2(dir[1], dir[0]);
+    b[3] = atan2(sqrt(dir[0] * dir[0] + dir[1] * dir[1]), dir[2]);
+    b[4] = qop;
     return true;
   }
 
   // transformBoundToFreeParameters (TransformationHelpers.cpp:17-39)
   CK_NI void boundToFree(const Surf<double>& sf, const double b[6]) {
-    P sp, cp, st, ct;
-    sincos((P)b[2], &sp, &cp);
-    sincos((P)b[3], &st, &ct);
+    double sp, cp, st, ct;
+    sincos(b[2], &sp, &cp);
+    sincos(b[3], &st, &ct);
     dir[0] = cp * st;
     dir[1] = sp * st;
     dir[2] = ct;
@@ -184,15 +185,15 @@ struct Lane {
       l[1] = b[1];
       l[2] = 0.0;
     } else {
-      P sphi, cphi;
-      sincos((P)(b[0] / sf.radius), &sphi, &cphi);
-      l[0] = sf.radius * (double)cphi;
-      l[1] = sf.radius * (double)sphi;
+      double sphi, cphi;
+      sincos(b[0] / sf.radius, &sphi, &cphi);
+      l[0] = sf.radius * cphi;
+      l[1] = sf.radius * sphi;
       l[2] = b[1];
     }
     sf.toGlobal3(l, pos);
-    tim = (P)b[5];
-    qop = (P)b[4];
+    tim = b[5];
+    qop = b[4];
   }
 
   // Surface::boundToFreeJacobian in transport form at the current state
@@ -205,7 +206,7 @@ struct Lane {
     sf.radius = (P)sfd.radius;
     sf.type = sfd.type;
     const P p[3] = {(P)pos[0], (P)pos[1], (P)pos[2]};
-    const P f[8] = {p[0], p[1], p[2], tim, dir[0], dir[1], dir[2], qop};
+    const P f[8] = {p[0], p[1], p[2], (P)tim, (P)dir[0], (P)dir[1], (P)dir[2], (P)qop};
     initTransport(sf, f, T);
   }
 
@@ -219,7 +220,7 @@ struct Lane {
     const double Bn = sqrt((double)B[0] * (double)B[0] + (double)B[1] * (double)B[1] +
                            (double)B[2] * (double)B[2]);
     if (Bn == 0.0) return limit;
-    const double pm = (double)absMomentum(absQ, qop);
+    const double pm = absMomentum(absQ, qop);
     const double ll = fp.opt.loopFraction * (2.0 * kPi * pm / Bn);
     if (fabs(ll) < fabs(limit)) limit = ll;
     return limit;
@@ -285,9 +286,10 @@ struct Lane {
   CK_NI bool material(const FitParams& fp, int sid, const Surf<double>& sfd, int mode) {
     const DevSurface* ds = fp.surfaces + sid;
     if (!(__ldg(&ds->flags) & CK_SURF_MATERIAL)) return true;
+    const P d[3] = {(P)dir[0], (P)dir[1], (P)dir[2]};
     P pc;
     if (sfd.type == CK_SURFACE_PLANE) {
-      pc = P(1) / fabs((P)sfd.R[2] * dir[0] + (P)sfd.R[5] * dir[1] + (P)sfd.R[8] * dir[2]);
+      pc = P(1) / fabs((P)sfd.R[2] * d[0] + (P)sfd.R[5] * d[1] + (P)sfd.R[8] * d[2]);
     } else {
       double l[3];
       sfd.toLocal3(pos, l);
@@ -302,7 +304,7 @@ struct Lane {
       P ez[3];
 #pragma unroll
       for (int i = 0; i < 3; ++i) ez[i] = (P)sfd.R[i * 3 + 0] * n0 + (P)sfd.R[i * 3 + 1] * n1;
-      pc = fabs(P(1) / (ez[0] * dir[0] + ez[1] * dir[1] + ez[2] * dir[2]));
+      pc = fabs(P(1) / (ez[0] * d[0] + ez[1] * d[1] + ez[2] * d[2]));
     }
     double loc[2];
     if (!toLocal(sfd, loc)) return false;
@@ -315,12 +317,12 @@ struct Lane {
     }
     bool vac = false;
     const float qOverPf = (float)qop;
-    const MatEffects e = materialEffects<P>(fp.mc, ds, f1, (float)pc, pdg, mass, absQ, dir,
+    const MatEffects e = materialEffects<P>(fp.mc, ds, f1, (float)pc, pdg, mass, absQ, d,
                                             qOverPf, fp.opt.multipleScattering != 0,
                                             fp.opt.energyLoss != 0, vac);
     if (vac) return true;
     const double massd = (double)mass;
-    const double mom = (double)absMomentum(absQ, qop);
+    const double mom = absMomentum(absQ, qop);
     const double nextE = sqrt(massd * massd + mom * mom) - e.eLoss;
     double nextP = 0.0;
     if (massd < nextE) {
@@ -329,7 +331,7 @@ struct Lane {
     }
     nextP = fmax(0.01, nextP);
     const float signedQ = (float)copysign((double)absQ, (double)qOverPf);
-    qop = (P)((double)signedQ / nextP);
+    qop = (double)signedQ / nextP;
     if (!coasting) {
       cov[sidx(2, 2)] = (CV)fmax(0.0, (double)cov[sidx(2, 2)] + e.varPhi);
       cov[sidx(3, 3)] = (CV)fmax(0.0, (double)cov[sidx(3, 3)] + e.varTheta);
@@ -341,7 +343,7 @@ struct Lane {
   // ------------------------------------------------- covariance transport
   // J = F2B (I + deriv fTP) T, C <- J C J^T, reinitialise T at the surface
   // (CovarianceEngine.cpp:102-165). J is returned for the record.
-  CK_NI void transportToBound(const Surf<double>& sfd, double Jout[36]) {
+  CK_NI void transportToBound(const Surf<double>& sfd, CV Jout[36]) {
     const P p[3] = {(P)pos[0], (P)pos[1], (P)pos[2]};
     Surf<P> sf;
 #pragma unroll
@@ -352,6 +354,7 @@ struct Lane {
     sf.type = sfd.type;
     P ex[3], ey[3], ez[3];
     referenceFrame(sf, p, ex, ey, ez);
+    const P dir[3] = {(P)this->dir[0], (P)this->dir[1], (P)this->dir[2]};
     const P dz = ez[0] * dir[0] + ez[1] * dir[1] + ez[2] * dir[2];
     const P idz = P(-1) / dz;
     const P f0 = ez[0] * idz, f1 = ez[1] * idz, f2 = ez[2] * idz;
@@ -391,7 +394,7 @@ struct Lane {
 #pragma unroll
     for (int r = 0; r < 6; ++r)
 #pragma unroll
-      for (int c = 0; c < 6; ++c) Jout[r * 6 + c] = (double)J[r][c];
+      for (int c = 0; c < 6; ++c) Jout[r * 6 + c] = (CV)J[r][c];
     // C <- J C J^T (packed); J row 4 is e4 and column 5 is e5
     CV JC[6][6];
 #pragma unroll
@@ -435,15 +438,15 @@ struct Lane {
 
   // --------------------------------------------------------------- actor
   CK_D void writeMeta(const FitParams& fp, int slot, int k, int sid, uint32_t flags, double chi2) {
-    fp.rec_meta[((size_t)k * 2 + 0) * (size_t)fp.n_slots + slot] = sid;
-    fp.rec_meta[((size_t)k * 2 + 1) * (size_t)fp.n_slots + slot] = (int32_t)flags;
-    fp.rec_meta_d[((size_t)k * 2 + 0) * (size_t)fp.n_slots + slot] = pathAcc;
-    fp.rec_meta_d[((size_t)k * 2 + 1) * (size_t)fp.n_slots + slot] = chi2;
+    fp.rec_meta[((size_t)k * 2 + 0) * (size_t)fp.rec_stride + slot] = sid;
+    fp.rec_meta[((size_t)k * 2 + 1) * (size_t)fp.rec_stride + slot] = (int32_t)flags;
+    fp.rec_meta_d[((size_t)k * 2 + 0) * (size_t)fp.rec_stride + slot] = pathAcc;
+    fp.rec_meta_d[((size_t)k * 2 + 1) * (size_t)fp.rec_stride + slot] = chi2;
   }
 
   // KalmanFitter::Actor::filter on surface `sid`
   CK_D int filter(const FitParams& fp, int slot, int sid) {
-    const Rec rec{fp.rec, fp.n_slots, slot};
+    const Rec<CV> rec(fp, slot);
     Surf<double> sf;
     sf.load(fp.surfaces + sid);
     const int sflags = __ldg(&fp.surfaces[sid].flags);
@@ -460,7 +463,7 @@ struct Lane {
     }
     const int mi = findMeas(fp, sid);
     if (mi >= 0) {
-      double J[36];
+      CV J[36];
       transportToBound(sf, J);
       if (!material(fp, sid, sf, 1)) return CK_TRACK_NOT_ON_SURFACE;
       double bp[6];
@@ -471,11 +474,11 @@ struct Lane {
 #pragma unroll
       for (int i = 0; i < 21; ++i) Pp[i] = (double)cov[i];
 #pragma unroll
-      for (int i = 0; i < 6; ++i) rec.at(k, kRecPred + i) = bp[i];
+      for (int i = 0; i < 6; ++i) rec.p(k, kRecPred + i) = bp[i];
 #pragma unroll
-      for (int i = 0; i < 21; ++i) rec.at(k, kRecPredCov + i) = Pp[i];
+      for (int i = 0; i < 21; ++i) rec.m(k, kRecPredCov + i) = cov[i];
 #pragma unroll
-      for (int i = 0; i < 36; ++i) rec.at(k, kRecJac + i) = J[i];
+      for (int i = 0; i < 36; ++i) rec.m(k, kRecJac + i) = J[i];
       uint32_t flags = CK_FLAG_HAS_PARAMETERS | (hasMat ? CK_FLAG_HAS_MATERIAL : 0u);
       const double mv0 = __ldg(&fp.meas_val[2 * (size_t)mi]);
       const double mv1 = __ldg(&fp.meas_val[2 * (size_t)mi + 1]);
@@ -491,21 +494,22 @@ struct Lane {
           return CK_TRACK_UPDATE_FAILED;
         flags |= CK_FLAG_HAS_MEASUREMENT;
 #pragma unroll
-        for (int i = 0; i < 6; ++i) rec.at(k, kRecFilt + i) = filt[i];
-#pragma unroll
-        for (int i = 0; i < 21; ++i) rec.at(k, kRecFiltCov + i) = F[i];
+        for (int i = 0; i < 6; ++i) rec.p(k, kRecFilt + i) = filt[i];
         // stepper.update (EigenStepper.ipp:128-138)
         boundToFree(sf, filt);
 #pragma unroll
-        for (int i = 0; i < 21; ++i) cov[i] = (CV)F[i];
+        for (int i = 0; i < 21; ++i) {
+          cov[i] = (CV)F[i];
+          rec.m(k, kRecFiltCov + i) = cov[i];
+        }
         initT(sf);
         ++measurementStates;
       } else {
         flags |= CK_FLAG_HAS_MEASUREMENT | CK_FLAG_IS_OUTLIER;
 #pragma unroll
-        for (int i = 0; i < 6; ++i) rec.at(k, kRecFilt + i) = bp[i];
+        for (int i = 0; i < 6; ++i) rec.p(k, kRecFilt + i) = bp[i];
 #pragma unroll
-        for (int i = 0; i < 21; ++i) rec.at(k, kRecFiltCov + i) = Pp[i];
+        for (int i = 0; i < 21; ++i) rec.m(k, kRecFiltCov + i) = cov[i];
       }
       writeMeta(fp, slot, k, sid, flags, chi2);
       if (!material(fp, sid, sf, 2)) return CK_TRACK_NOT_ON_SURFACE;
@@ -513,20 +517,22 @@ struct Lane {
     } else if ((preceding && sensitive) || hasMat) {
       double bp[6];
       if (!freeToBound(sf, bp)) return CK_TRACK_NOT_ON_SURFACE;
-      double J[36];
+      CV J[36];
       transportToBound(sf, J);
       if (nStates >= fp.max_states) return CK_TRACK_TOO_MANY_STATES;
       const int k = nStates++;
 #pragma unroll
-      for (int i = 0; i < 6; ++i) rec.at(k, kRecPred + i) = bp[i];
+      for (int i = 0; i < 6; ++i) {
+        rec.p(k, kRecPred + i) = bp[i];
+        rec.p(k, kRecFilt + i) = bp[i];
+      }
 #pragma unroll
-      for (int i = 0; i < 21; ++i) rec.at(k, kRecPredCov + i) = (double)cov[i];
+      for (int i = 0; i < 21; ++i) {
+        rec.m(k, kRecPredCov + i) = cov[i];
+        rec.m(k, kRecFiltCov + i) = cov[i];
+      }
 #pragma unroll
-      for (int i = 0; i < 36; ++i) rec.at(k, kRecJac + i) = J[i];
-#pragma unroll
-      for (int i = 0; i < 6; ++i) rec.at(k, kRecFilt + i) = bp[i];
-#pragma unroll
-      for (int i = 0; i < 21; ++i) rec.at(k, kRecFiltCov + i) = (double)cov[i];
+      for (int i = 0; i < 36; ++i) rec.m(k, kRecJac + i) = J[i];
       uint32_t flags = CK_FLAG_HAS_PARAMETERS | (hasMat ? CK_FLAG_HAS_MATERIAL : 0u);
       if (sensitive && preceding) flags |= CK_FLAG_IS_HOLE;
       writeMeta(fp, slot, k, sid, flags, 0.0);
@@ -687,6 +693,8 @@ struct Lane {
     }
     ++trials;
     const P pp[3] = {(P)pos[0], (P)pos[1], (P)pos[2]};
+    const P dir[3] = {(P)this->dir[0], (P)this->dir[1], (P)this->dir[2]};
+    const P qop = (P)this->qop;
     P B1[3], B2[3], B3[3];
     if (!getField(fp.field, pp, B1)) {
       fail(fp, CK_TRACK_FIELD_OUT_OF_BOUNDS);
@@ -747,7 +755,7 @@ struct Lane {
     const P pm = absMomentum(absQ, qop);
     const P mp = m / pm;
     const P dtds = sqrt(P(1) + mp * mp);
-    tim = tim + h * dtds;
+    tim = tim + (double)(h * dtds);
     if (!coasting) {
       deriv[3] = dtds;
       P dk1dL[3], dk2dL[3], dk3dL[3], dk4dL[3];
@@ -840,19 +848,20 @@ struct Lane {
       const P h6 = h * P(1.0 / 6.0);
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        pos[i] = pos[i] + (double)(h * dir[i] + hh6 * ((k1[i] + k2[i]) + k3[i]));
-        dir[i] = dir[i] + h6 * ((k1[i] + P(2) * (k2[i] + k3[i])) + k4[i]);
+        pos[i] = pos[i] + ((double)h * this->dir[i] + (double)(hh6 * ((k1[i] + k2[i]) + k3[i])));
+        this->dir[i] = this->dir[i] + (double)(h6 * ((k1[i] + P(2) * (k2[i] + k3[i])) + k4[i]));
       }
-      const P n2 = dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2];
-      const P inv = P(1) / sqrt(n2);
-      dir[0] = dir[0] * inv;
-      dir[1] = dir[1] * inv;
-      dir[2] = dir[2] * inv;
+      double* nd = this->dir;
+      const double n2 = nd[0] * nd[0] + nd[1] * nd[1] + nd[2] * nd[2];
+      const double inv = 1.0 / sqrt(n2);
+      nd[0] = nd[0] * inv;
+      nd[1] = nd[1] * inv;
+      nd[2] = nd[2] * inv;
     }
     if (!coasting) {
-      deriv[0] = dir[0];
-      deriv[1] = dir[1];
-      deriv[2] = dir[2];
+      deriv[0] = (P)this->dir[0];
+      deriv[1] = (P)this->dir[1];
+      deriv[2] = (P)this->dir[2];
       deriv[4] = k4[0];
       deriv[5] = k4[1];
       deriv[6] = k4[2];
@@ -892,17 +901,34 @@ struct Lane {
     afterAct(fp, slot);
   }
 
-  // end of propagation: NoMeasurementFound or start of the smoother
+  // end of propagation: NoMeasurementFound, or the track's tip is handed to
+  // the smoother kernel
   CK_D void endPropagation(const FitParams& fp, int slot) {
     if (measurementStates == 0) {
       fail(fp, CK_TRACK_NO_MEASUREMENT_FOUND);
       return;
     }
-    tip = lastMeasurementIndex;
+    fp.tip[slot] = lastMeasurementIndex;
+    phase = PH_FETCH;
+  }
+};
+
+// RTS smoother of one track over its records (GainMatrixSmoother, driven as
+// in KalmanFitter::finalize, KalmanFitter.hpp:795-984), then the track
+// summary (calculateTrackQuantities, TrackHelpers.hpp:421-448).
+template <typename CV>
+struct Smoother {
+  int t, q;
+  int lastMeas;
+  int nM, nH, nO, ndf;
+  double chi2sum;
+
+  CK_D void run(const FitParams& fp, int queuePos, int track, int tip) {
+    t = track;
+    q = queuePos;
     lastMeas = tip;
     for (int k = tip; k >= 0; --k) {
-      const uint32_t fl =
-          (uint32_t)fp.rec_meta[((size_t)k * 2 + 1) * (size_t)fp.n_slots + slot];
+      const uint32_t fl = (uint32_t)fp.rec_meta[((size_t)k * 2 + 1) * (size_t)fp.rec_stride + q];
       if ((fl & CK_FLAG_HAS_MEASUREMENT) && !(fl & CK_FLAG_IS_OUTLIER)) {
         lastMeas = k;
         break;
@@ -910,34 +936,78 @@ struct Lane {
     }
     nM = nH = nO = ndf = 0;
     chi2sum = 0.0;
-    const Rec rec{fp.rec, fp.n_slots, slot};
-    double sm[6], Ps[21];
+    const Rec<CV> rec(fp, q);
+    {
+      double sm[6];
+      CV Ps[21];
 #pragma unroll
-    for (int i = 0; i < 6; ++i) sm[i] = rec.at(tip, kRecFilt + i);
+      for (int i = 0; i < 6; ++i) sm[i] = rec.p(tip, kRecFilt + i);
 #pragma unroll
-    for (int i = 0; i < 21; ++i) Ps[i] = rec.at(tip, kRecFiltCov + i);
-    writeState(fp, slot, tip, sm, Ps, false);
-    smoothK = tip - 1;
-    if (smoothK < 0)
-      finalize(fp);
-    else
-      phase = PH_SMOOTH;
+      for (int i = 0; i < 21; ++i) Ps[i] = rec.m(tip, kRecFiltCov + i);
+      writeState(fp, tip, sm, Ps, false);
+    }
+    for (int k = tip - 1; k >= 0; --k) {
+      // the smoothed state of k+1 sits in the filtered fields of its record
+      double filt[6], pp[6], ps[6], sm[6];
+      CV Pf[21], Ppp[21], J[36], Psp[21], Ps[21];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) filt[i] = rec.p(k, kRecFilt + i);
+#pragma unroll
+      for (int i = 0; i < 21; ++i) Pf[i] = rec.m(k, kRecFiltCov + i);
+#pragma unroll
+      for (int i = 0; i < 6; ++i) pp[i] = rec.p(k + 1, kRecPred + i);
+#pragma unroll
+      for (int i = 0; i < 21; ++i) Ppp[i] = rec.m(k + 1, kRecPredCov + i);
+#pragma unroll
+      for (int i = 0; i < 36; ++i) J[i] = rec.m(k + 1, kRecJac + i);
+#pragma unroll
+      for (int i = 0; i < 6; ++i) ps[i] = rec.p(k + 1, kRecFilt + i);
+#pragma unroll
+      for (int i = 0; i < 21; ++i) Psp[i] = rec.m(k + 1, kRecFiltCov + i);
+      if (!smoothStep<CV>(filt, Pf, pp, Ppp, J, ps, Psp, sm, Ps)) {
+        failSmooth(fp);
+        return;
+      }
+      writeState(fp, k, sm, Ps, k == lastMeas);
+#pragma unroll
+      for (int i = 0; i < 6; ++i) rec.p(k, kRecFilt + i) = sm[i];
+#pragma unroll
+      for (int i = 0; i < 21; ++i) rec.m(k, kRecFiltCov + i) = Ps[i];
+    }
+    const ck_batch_out& out = fp.out;
+    out.status[t] = CK_TRACK_OK;
+    if (out.n_states) out.n_states[t] = tip + 1;
+    if (out.n_measurements) out.n_measurements[t] = nM;
+    if (out.n_holes) out.n_holes[t] = nH;
+    if (out.n_outliers) out.n_outliers[t] = nO;
+    if (out.ndf) out.ndf[t] = ndf;
+    if (out.chi2_sum) out.chi2_sum[t] = chi2sum;
   }
 
-  CK_NI void writeState(const FitParams& fp, int slot, int k, const double sm[6],
-                       const double Ps[21], bool filtOverride) {
+  CK_D void failSmooth(const FitParams& fp) {
     const ck_batch_out& out = fp.out;
-    const Rec rec{fp.rec, fp.n_slots, slot};
+    out.status[t] = CK_TRACK_SMOOTH_FAILED;
+    if (out.n_states) out.n_states[t] = 0;
+    if (out.n_measurements) out.n_measurements[t] = 0;
+    if (out.n_holes) out.n_holes[t] = 0;
+    if (out.n_outliers) out.n_outliers[t] = 0;
+    if (out.ndf) out.ndf[t] = 0;
+    if (out.chi2_sum) out.chi2_sum[t] = 0.0;
+  }
+
+  CK_D void writeState(const FitParams& fp, int k, const double sm[6], const CV Ps[21],
+                       bool filtOverride) {
+    const ck_batch_out& out = fp.out;
+    const Rec<CV> rec(fp, q);
     const size_t n = (size_t)fp.n_tracks;
     auto at = [&](int C, int c) -> size_t { return ((size_t)k * C + c) * n + t; };
-    const uint32_t fl = (uint32_t)fp.rec_meta[((size_t)k * 2 + 1) * (size_t)fp.n_slots + slot];
-    const double c2 = fp.rec_meta_d[((size_t)k * 2 + 1) * (size_t)fp.n_slots + slot];
-    if (out.state_surface)
-      out.state_surface[at(1, 0)] = fp.rec_meta[((size_t)k * 2 + 0) * (size_t)fp.n_slots + slot];
+    const size_t ms = (size_t)fp.rec_stride;
+    const uint32_t fl = (uint32_t)fp.rec_meta[((size_t)k * 2 + 1) * ms + q];
+    const double c2 = fp.rec_meta_d[((size_t)k * 2 + 1) * ms + q];
+    if (out.state_surface) out.state_surface[at(1, 0)] = fp.rec_meta[((size_t)k * 2 + 0) * ms + q];
     if (out.state_flags) out.state_flags[at(1, 0)] = fl;
     if (out.state_path_length)
-      out.state_path_length[at(1, 0)] =
-          fp.rec_meta_d[((size_t)k * 2 + 0) * (size_t)fp.n_slots + slot];
+      out.state_path_length[at(1, 0)] = fp.rec_meta_d[((size_t)k * 2 + 0) * ms + q];
     if (out.state_chi2) out.state_chi2[at(1, 0)] = c2;
     if (fl & CK_FLAG_IS_HOLE) {
       ++nH;
@@ -954,105 +1024,63 @@ struct Lane {
 #pragma unroll
       for (int i = 0; i < 6; ++i)
 #pragma unroll
-        for (int j = 0; j < 6; ++j) out.smoothed_cov[at(36, i * 6 + j)] = Ps[sidx(i, j)];
+        for (int j = i; j < 6; ++j) {
+          const double v = (double)Ps[sidx(i, j)];
+          out.smoothed_cov[at(36, i * 6 + j)] = v;
+          if (j != i) out.smoothed_cov[at(36, j * 6 + i)] = v;
+        }
     }
     if (out.filtered) {
 #pragma unroll
       for (int i = 0; i < 6; ++i)
-        out.filtered[at(6, i)] = filtOverride ? sm[i] : rec.at(k, kRecFilt + i);
+        out.filtered[at(6, i)] = filtOverride ? sm[i] : rec.p(k, kRecFilt + i);
 #pragma unroll
       for (int i = 0; i < 6; ++i)
 #pragma unroll
         for (int j = 0; j < 6; ++j)
           out.filtered_cov[at(36, i * 6 + j)] =
-              filtOverride ? Ps[sidx(i, j)] : rec.at(k, kRecFiltCov + sidx(i, j));
+              (double)(filtOverride ? Ps[sidx(i, j)] : rec.m(k, kRecFiltCov + sidx(i, j)));
     }
     if (out.predicted) {
 #pragma unroll
-      for (int i = 0; i < 6; ++i) out.predicted[at(6, i)] = rec.at(k, kRecPred + i);
+      for (int i = 0; i < 6; ++i) out.predicted[at(6, i)] = rec.p(k, kRecPred + i);
 #pragma unroll
       for (int i = 0; i < 6; ++i)
 #pragma unroll
         for (int j = 0; j < 6; ++j)
-          out.predicted_cov[at(36, i * 6 + j)] = rec.at(k, kRecPredCov + sidx(i, j));
+          out.predicted_cov[at(36, i * 6 + j)] = (double)rec.m(k, kRecPredCov + sidx(i, j));
     }
     if (out.jacobian) {
 #pragma unroll
-      for (int i = 0; i < 36; ++i) out.jacobian[at(36, i)] = rec.at(k, kRecJac + i);
+      for (int i = 0; i < 36; ++i) out.jacobian[at(36, i)] = (double)rec.m(k, kRecJac + i);
     }
-  }
-
-  // SMOOTH: one backward state (GainMatrixSmoother::calculate). The
-  // smoothed state of k+1 sits in the filtered fields of its record.
-  CK_D void smooth(const FitParams& fp, int slot) {
-    const Rec rec{fp.rec, fp.n_slots, slot};
-    const int k = smoothK;
-    double filt[6], Pf[21], pp[6], Ppp[21], J[36], ps[6], Psp[21], sm[6], Ps[21];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) filt[i] = rec.at(k, kRecFilt + i);
-#pragma unroll
-    for (int i = 0; i < 21; ++i) Pf[i] = rec.at(k, kRecFiltCov + i);
-#pragma unroll
-    for (int i = 0; i < 6; ++i) pp[i] = rec.at(k + 1, kRecPred + i);
-#pragma unroll
-    for (int i = 0; i < 21; ++i) Ppp[i] = rec.at(k + 1, kRecPredCov + i);
-#pragma unroll
-    for (int i = 0; i < 36; ++i) J[i] = rec.at(k + 1, kRecJac + i);
-#pragma unroll
-    for (int i = 0; i < 6; ++i) ps[i] = rec.at(k + 1, kRecFilt + i);
-#pragma unroll
-    for (int i = 0; i < 21; ++i) Psp[i] = rec.at(k + 1, kRecFiltCov + i);
-    if (!smoothStep(filt, Pf, pp, Ppp, J, ps, Psp, sm, Ps)) {
-      fail(fp, CK_TRACK_SMOOTH_FAILED);
-      return;
-    }
-    writeState(fp, slot, k, sm, Ps, k == lastMeas);
-#pragma unroll
-    for (int i = 0; i < 6; ++i) rec.at(k, kRecFilt + i) = sm[i];
-#pragma unroll
-    for (int i = 0; i < 21; ++i) rec.at(k, kRecFiltCov + i) = Ps[i];
-    smoothK = k - 1;
-    if (smoothK < 0) finalize(fp);
-  }
-
-  CK_D void finalize(const FitParams& fp) {
-    const ck_batch_out& out = fp.out;
-    out.status[t] = CK_TRACK_OK;
-    if (out.n_states) out.n_states[t] = tip + 1;
-    if (out.n_measurements) out.n_measurements[t] = nM;
-    if (out.n_holes) out.n_holes[t] = nH;
-    if (out.n_outliers) out.n_outliers[t] = nO;
-    if (out.ndf) out.ndf[t] = ndf;
-    if (out.chi2_sum) out.chi2_sum[t] = chi2sum;
-    phase = PH_FETCH;
   }
 };
 
-// Persistent fit kernel with warp-level phase scheduling (see the header).
+// Persistent forward-filter kernel with warp-level phase scheduling: each
+// warp votes the phase most of its lanes are in (fetch a track, one
+// Runge-Kutta trial, the actor on a reached surface) and runs it for those
+// lanes; fetching lanes take consecutive queue positions with one atomic per
+// warp. Records are indexed by queue position.
 template <typename P, typename CV, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) fitKernel(FitParams fp) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
   Lane<P, CV> L;
   L.phase = PH_FETCH;
   L.t = -1;
+  L.q = -1;
   while (true) {
     const unsigned mFetch = __ballot_sync(FULL, L.phase == PH_FETCH);
     const unsigned mStep = __ballot_sync(FULL, L.phase == PH_STEP);
     const unsigned mSurf = __ballot_sync(FULL, L.phase == PH_SURFACE);
-    const unsigned mSmooth = __ballot_sync(FULL, L.phase == PH_SMOOTH);
-    if ((mFetch | mStep | mSurf | mSmooth) == 0u) break;
+    if ((mFetch | mStep | mSurf) == 0u) break;
     int best = PH_FETCH, bc = __popc(mFetch);
     if (__popc(mStep) > bc) {
       best = PH_STEP;
       bc = __popc(mStep);
     }
-    if (__popc(mSurf) > bc) {
-      best = PH_SURFACE;
-      bc = __popc(mSurf);
-    }
-    if (__popc(mSmooth) > bc) best = PH_SMOOTH;
+    if (__popc(mSurf) > bc) best = PH_SURFACE;
     if (best == PH_FETCH) {
       // warp-aggregated ticket for every fetching lane
       const int leader = __ffs(mFetch) - 1;
@@ -1061,19 +1089,32 @@ __global__ void __launch_bounds__(BLOCK, MINB) fitKernel(FitParams fp) {
       base = __shfl_sync(FULL, base, leader);
       if (L.phase == PH_FETCH) {
         const int q = base + __popc(mFetch & ((1u << lane) - 1u));
-        if (q >= fp.n_queue)
+        if (q >= fp.n_queue) {
           L.phase = PH_DONE;
-        else
-          L.start(fp, slot, fp.perm ? __ldg(&fp.perm[q]) : q);
+        } else {
+          L.q = q;
+          L.start(fp, q, fp.perm ? __ldg(&fp.perm[q]) : q);
+        }
       }
     } else if (L.phase == best) {
       if (best == PH_STEP)
-        L.step(fp, slot);
-      else if (best == PH_SURFACE)
-        L.surface(fp, slot);
+        L.step(fp, L.q);
       else
-        L.smooth(fp, slot);
+        L.surface(fp, L.q);
     }
+  }
+}
+
+// Smoother kernel: one lane per queue position; lanes of a warp hold tracks
+// of similar length (the queue is ordered by sequence length).
+template <typename CV, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) smoothKernel(FitParams fp) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < fp.n_queue;
+       q += gridDim.x * blockDim.x) {
+    const int tip = fp.tip[q];
+    if (tip < 0) continue;
+    Smoother<CV> S;
+    S.run(fp, q, fp.perm ? __ldg(&fp.perm[q]) : q, tip);
   }
 }
 

@@ -53,15 +53,18 @@ struct DevOptions {
   int useOutlierCut, earlyTermination;
 };
 
-// Record of one forward track state kept for the smoother (scratch).
-// Doubles per record: predicted 6, predicted cov 21 (packed upper),
-// filtered 6, filtered cov 21, jacobian 36.
+// Record of one forward track state kept for the smoother (scratch), in two
+// parts: the bound parameters in FP64 (predicted 6, filtered 6) and the
+// matrices in the covariance type of the form (predicted cov 21 and filtered
+// cov 21, packed upper; jacobian 36). The scratch is sized for FP64 matrices.
 constexpr int kRecPred = 0;
-constexpr int kRecPredCov = 6;
-constexpr int kRecFilt = 27;
-constexpr int kRecFiltCov = 33;
-constexpr int kRecJac = 54;
-constexpr int kRecDoubles = 90;
+constexpr int kRecFilt = 6;
+constexpr int kRecParams = 12;
+constexpr int kRecPredCov = 0;
+constexpr int kRecFiltCov = 21;
+constexpr int kRecJac = 42;
+constexpr int kRecMatrix = 78;
+constexpr int kRecDoubles = kRecParams + kRecMatrix;
 
 struct FitParams {
   int n_tracks;
@@ -81,15 +84,20 @@ struct FitParams {
   // queue: slot -> track index (descending sequence length) and ticket
   const int32_t* perm;
   int32_t* ticket;
-  // scratch records of the tracks in flight, indexed by the resident thread
-  // slot (blockIdx.x * blockDim.x + threadIdx.x < n_slots):
-  //   rec        [(k * kRecDoubles + f) * n_slots + slot]
-  //   rec_meta   [(k * 2 + {surface, flags}) * n_slots + slot]
-  //   rec_meta_d [(k * 2 + {pathLength, chi2}) * n_slots + slot]
+  // track-state records of the forward filter, indexed by queue position q
+  // (rec_stride = n_queue), read back by the smoother kernel:
+  //   rec        [(k * kRecParams + f) * rec_stride + q]       (double)
+  //   rec_mat    [(k * kRecMatrix + f) * rec_stride + q]       (CV)
+  //   rec_meta   [(k * 2 + {surface, flags}) * rec_stride + q]
+  //   rec_meta_d [(k * 2 + {pathLength, chi2}) * rec_stride + q]
+  //   tip        [q]: index of the last measurement state, -1 when the
+  //              forward filter failed (its status is then already written)
   double* rec;
+  void* rec_mat;
   int32_t* rec_meta;
   double* rec_meta_d;
-  int n_slots;
+  int32_t* tip;
+  int rec_stride;
   int max_states;
   // outputs (device memory, ck_batch_out layout)
   ck_batch_out out;

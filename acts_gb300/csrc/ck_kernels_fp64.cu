@@ -38,10 +38,15 @@ int occupancyFP64(int variant, int tpb) {
   return n;
 }
 
+cudaError_t launchSmoothFP64(const FitParams& fp, cudaStream_t st) {
+  const int grid = (fp.n_queue + kSmoothBlock - 1) / kSmoothBlock;
+  smoothKernel<double, kSmoothBlock><<<grid, kSmoothBlock, 0, st>>>(fp);
+  return cudaGetLastError();
+}
+
 int occupancyBlocks(int precision, int variant, int tpb) {
   switch (precision) {
     case CK_PRECISION_MIXED: return occupancyMixed(variant, tpb);
-    case CK_PRECISION_MIXED_COV64: return occupancyMixedCov64(variant, tpb);
     default: return occupancyFP64(variant, tpb);
   }
 }

@@ -1,7 +1,8 @@
 // ck_kernels_mixed.cu — instantiations of the mixed-precision fit kernel:
-// stepper, Jacobian transport, field interpolation and covariance transport
-// in FP32; Kalman update (Joseph form when selected), 2x2 inverse, smoother
-// gain inverse and chi2 in FP64.
+// Runge-Kutta stages, Jacobian transport, field interpolation and covariance
+// transport in FP32, with the free parameters accumulated in FP64 from the
+// FP32 stage increments; Kalman update (Joseph form when selected), 2x2
+// inverse, smoother-gain inverse, bound-parameter conversion and chi2 in FP64.
 #include "ck_fitter.cuh"
 #include "ck_launch.h"
 
@@ -20,6 +21,12 @@ cudaError_t launchFitMixed(const FitParams& fp, int variant, int grid, int block
       fitKernel<float, float, 128, 4><<<grid, block, 0, st>>>(fp);
       break;
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launchSmoothMixed(const FitParams& fp, cudaStream_t st) {
+  const int grid = (fp.n_queue + kSmoothBlock - 1) / kSmoothBlock;
+  smoothKernel<float, kSmoothBlock><<<grid, kSmoothBlock, 0, st>>>(fp);
   return cudaGetLastError();
 }
 

@@ -14,11 +14,14 @@ cudaError_t launchFitFP64(const FitParams& fp, int variant, int grid, int block,
                           cudaStream_t st);
 cudaError_t launchFitMixed(const FitParams& fp, int variant, int grid, int block,
                            cudaStream_t st);
-cudaError_t launchFitMixedCov64(const FitParams& fp, int variant, int grid, int block,
-                                cudaStream_t st);
 int occupancyFP64(int variant, int tpb);
 int occupancyMixed(int variant, int tpb);
-int occupancyMixedCov64(int variant, int tpb);
 int occupancyBlocks(int precision, int variant, int tpb);
+cudaError_t launchSmoothFP64(const FitParams& fp, cudaStream_t st);
+cudaError_t launchSmoothMixed(const FitParams& fp, cudaStream_t st);
+inline cudaError_t launchSmooth(const FitParams& fp, int precision, cudaStream_t st) {
+  return precision == CK_PRECISION_MIXED ? launchSmoothMixed(fp, st) : launchSmoothFP64(fp, st);
+}
+constexpr int kSmoothBlock = 128;
 
 }  // namespace ck

@@ -105,7 +105,7 @@ struct ck_server {
     if (spec.fi) out += (size_t)maxStates * 42 * 8;
     if (spec.pr) out += (size_t)maxStates * 42 * 8;
     if (spec.jac) out += (size_t)maxStates * 36 * 8;
-    return in + out;
+    return in + out + recordBytesPerTrack(maxStates, opt.precision);
   }
 };
 
@@ -145,7 +145,7 @@ ck_status slotAlloc(ck_server* s, Slot& sl) {
     return cudaFail(e, "server pinned buffers");
   sl.pinInBytes = pin;
   sl.pinOutBytes = pout;
-  ck_status st = preparePipeline(s->h, sl.ctx, s->capacity, ms, s->tune, s->gridBlocks);
+  ck_status st = preparePipeline(s->h, sl.ctx, s->capacity, ms, s->opt.precision);
   return st;
 }
 
@@ -397,11 +397,8 @@ ck_status ck_server_create(ck_handle* h, const ck_options* opt, const ck_server_
   s->tune = h->tune[opt->precision];
   // each stream gets an equal share of the resident blocks
   s->gridBlocks = std::max(1, gridBlocksFor(h, s->tune) / cfg->n_streams);
-  const size_t scratch = (size_t)s->gridBlocks * s->tune.tpb * cfg->max_states *
-                         (kRecDoubles * 8 + 2 * 4 + 2 * 8);
   const size_t perTrack = s->perTrackBytes(cfg->max_states);
-  const int64_t avail = cfg->memory_budget_bytes - (int64_t)(scratch * cfg->n_streams);
-  if (avail <= 0) return fail(CK_ERR_BUDGET, "budget smaller than the fixed scratch");
+  const int64_t avail = cfg->memory_budget_bytes;
   int64_t cap = avail / (int64_t)(perTrack * cfg->n_streams);
   cap = std::min<int64_t>(cap, cfg->max_batch_tracks);
   if (cap < 1) return fail(CK_ERR_BUDGET, "budget too small for one track per stream");

@@ -217,6 +217,11 @@ def accuracy_report(b, r64, rmx, n):
     ms = r64["max_states"]
     ok = (r64["status"][:n] == 0) & (rmx["status"][:n] == 0)
     agree = float(np.mean(r64["status"][:n] == rmx["status"][:n]))
+    # the bound applies to valid fits (FP64 chi2/ndf < 5); fits broken in
+    # FP64 (the cylinder phi = +-pi seam) are chaotic in any precision
+    good = ok & (r64["chi2_sum"][:n] < 5.0 * np.maximum(r64["ndf"][:n], 1))
+    n_broken = int((ok & ~good).sum())
+    ok = good
     fl = r64["state_flags"].reshape(ms, r64["N"])[:, :n].T
     sm64 = r64["smoothed"].reshape(ms, 6, r64["N"])[:, :, :n].transpose(2, 0, 1)
     smmx = rmx["smoothed"].reshape(ms, 6, rmx["N"])[:, :, :n].transpose(2, 0, 1)
@@ -256,9 +261,15 @@ def accuracy_report(b, r64, rmx, n):
     wmx = [float(np.std(np.clip(p, -10, 10))) for p in pullsmx]
     c64 = float(r64["chi2_sum"][:n][ok].sum() / max(1, r64["ndf"][:n][ok].sum()))
     cmx = float(rmx["chi2_sum"][:n][ok].sum() / max(1, rmx["ndf"][:n][ok].sum()))
-    return {"tracks": int(n), "status_agreement": agree,
+    return {"tracks": int(n), "status_agreement": agree, "valid_fits": int(ok.sum()),
+            "excluded_broken_fits": n_broken,
+            "rel_err_definition": "|x_mixed - x_fp64| / max(|x_fp64|, sigma_fp64), smoothed "
+                                  "parameters at measurement states",
             "max_rel_param_err": float(relm.max()) if relm.size else None,
             "p99_rel_param_err": float(np.quantile(relm, 0.99)) if relm.size else None,
+            "max_rel_err_per_param": dict(zip(["loc0", "loc1", "phi", "theta", "qop", "time"],
+                                              [float("%.3g" % x) for x in relm.max(axis=0)]))
+            if relm.size else None,
             "pull_width_fp64": dict(zip(names, [round(x, 4) for x in w64])),
             "pull_width_mixed": dict(zip(names, [round(x, 4) for x in wmx])),
             "max_pull_width_shift": float(max(abs(a - b2) / a for a, b2 in zip(w64, wmx))),
@@ -340,7 +351,9 @@ def native_arm(args):
     fit = CudaKalman.for_detector(det, device=local, use_graph=True)
     bi, keep_in = device_batch(b, torch, dev)
     bo, keep_out = device_outputs(n, ms, torch, dev)
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated stream: the fit is launched on it and the CUDA events that
+    # time it are recorded on it
+    stream = torch.cuda.Stream(dev)
     sp = C.c_void_p(stream.cuda_stream)
 
     forms = {"mixed": abi.default_options(precision=abi.PRECISION_MIXED),

@@ -151,13 +151,13 @@ typedef struct ck_field {
 /* ------------------------------------------------------------- options */
 
 /* FP64: everything in double (the reference's arithmetic).
- * MIXED: stepper, Jacobian transport, field interpolation and covariance
- *   transport in FP32; Kalman update (Joseph form when selected), 2x2
- *   inverse, smoother-gain inverse and chi2 in FP64.
- * MIXED_COV64: as MIXED, but the covariance is kept and transported in FP64
- *   (the transport Jacobian itself stays FP32). */
-enum { CK_PRECISION_FP64 = 0, CK_PRECISION_MIXED = 1, CK_PRECISION_MIXED_COV64 = 2 };
-#define CK_NUM_PRECISIONS 3
+ * MIXED: Runge-Kutta stages, field interpolation, Jacobian transport and
+ *   covariance transport in FP32; the free parameters (position, direction,
+ *   q/p, time) are accumulated in FP64 from the FP32 stage increments;
+ *   Kalman update (Joseph form when selected), 2x2 inverse, smoother-gain
+ *   inverse, bound-parameter conversion and chi2 in FP64. */
+enum { CK_PRECISION_FP64 = 0, CK_PRECISION_MIXED = 1 };
+#define CK_NUM_PRECISIONS 2
 
 /* Fit options. ck_options_default() fills the reference defaults:
  *   StepperPlainOptions (Core/include/Acts/Propagator/StepperOptions.hpp:36-49)
