@@ -166,6 +166,72 @@ CK_D int intersect(const Surf<P>& s, const P pos[3], const P dir[3], P tol, P pa
   return 2;
 }
 
+// Surface::intersect for the mixed form: position and direction in FP64.
+// The plane distance n.(c - x) and the cylinder's |x_perp|^2 - R^2 (the
+// quantities that cancel near the surface) are formed in FP64; the quadratic
+// is solved in FP32 (root nearest to zero as c/q) and each root is refined
+// by one Newton step on the FP64 quadratic, so the path to the surface is
+// FP64-accurate (the final step lands on the surface as in the plain form).
+CK_D int intersectMixed(const Surf<double>& s, const double pos[3], const double dir[3],
+                        double tol, double path[2], int st[2]) {
+  if (s.type == CK_SURFACE_PLANE) {
+    const double denom = dir[0] * s.R[2] + dir[1] * s.R[5] + dir[2] * s.R[8];
+    if (denom == 0.0) {
+      path[0] = 0.0;
+      st[0] = 0;
+      return 1;
+    }
+    const double num =
+        s.R[2] * (s.c[0] - pos[0]) + s.R[5] * (s.c[1] - pos[1]) + s.R[8] * (s.c[2] - pos[2]);
+    // FP32 quotient refined by one FP64 residual step
+    const double p0 = (double)((float)num / (float)denom);
+    const double pl = p0 + (double)((float)(num - p0 * denom) / (float)denom);
+    path[0] = pl;
+    st[0] = statusOf(pl, tol);
+    return 1;
+  }
+  const double a0 = s.R[2], a1 = s.R[5], a2 = s.R[8];
+  const double pc0 = pos[0] - s.c[0], pc1 = pos[1] - s.c[1], pc2 = pos[2] - s.c[2];
+  const double px0 = pc1 * a2 - pc2 * a1, px1 = pc2 * a0 - pc0 * a2, px2 = pc0 * a1 - pc1 * a0;
+  const double lx0 = dir[1] * a2 - dir[2] * a1, lx1 = dir[2] * a0 - dir[0] * a2,
+               lx2 = dir[0] * a1 - dir[1] * a0;
+  const double ad = lx0 * lx0 + lx1 * lx1 + lx2 * lx2;
+  const double bd = 2.0 * (lx0 * px0 + lx1 * px1 + lx2 * px2);
+  const double ccd = (px0 * px0 + px1 * px1 + px2 * px2) - s.radius * s.radius;
+  const float a = (float)ad, b = (float)bd, cc = (float)ccd;
+  const float disc = b * b - 4.0f * a * cc;
+  if (!(disc >= 0.0f)) {
+    st[0] = st[1] = 0;
+    path[0] = path[1] = 0.0;
+    return 2;
+  }
+  const float sq = sqrtf(disc);
+  const float q = -0.5f * (b + (b > 0.0f ? sq : -sq));
+  auto refine = [&](float t0f) -> double {
+    const double t0 = (double)t0f;
+    const double f = (ad * t0 + bd) * t0 + ccd;
+    const double df = 2.0 * ad * t0 + bd;
+    return df != 0.0 ? t0 - (double)((float)f / (float)df) : t0;
+  };
+  const double first = refine(q / a);
+  if (disc == 0.0f) {
+    path[0] = path[1] = first;
+    st[0] = st[1] = statusOf(first, tol);
+    return 2;
+  }
+  const double second = refine(cc / q);
+  if (first <= second) {
+    path[0] = first;
+    path[1] = second;
+  } else {
+    path[0] = second;
+    path[1] = first;
+  }
+  st[0] = statusOf(path[0], tol);
+  st[1] = statusOf(path[1], tol);
+  return 2;
+}
+
 // Surface::globalToLocal (PlaneSurface.cpp:77-86, CylinderSurface.cpp:125-145)
 template <typename P>
 CK_D bool globalToLocal(const Surf<P>& s, const P pos[3], double tol, P loc[2]) {

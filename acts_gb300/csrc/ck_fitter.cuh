@@ -93,7 +93,7 @@ struct Lane {
   int pdg;
   // ---- pending Runge-Kutta step
   double initialH;
-  P h;
+  double hd;  // step size (FP64 in every form; the stages use it rounded to P)
   unsigned trials;
   bool stepStarted;
   unsigned steps;
@@ -136,7 +136,11 @@ struct Lane {
   CK_NI int intersectSurf(const FitParams& fp, int sid, double path[2], int st[2]) const {
     Surf<double> sf;
     sf.load(fp.surfaces + sid);
-    return intersect(sf, pos, dir, fp.opt.surfaceTolerance, path, st);
+    if constexpr (sizeof(P) == sizeof(float)) {
+      return intersectMixed(sf, pos, dir, fp.opt.surfaceTolerance, path, st);
+    } else {
+      return intersect(sf, pos, dir, fp.opt.surfaceTolerance, path, st);
+    }
   }
 
   // Surface::globalToLocal in double (the bound parameters are outputs)
@@ -687,7 +691,7 @@ struct Lane {
         return;
       }
       initialH = stepValue();
-      h = (P)initialH;
+      hd = initialH;
       trials = 0;
       stepStarted = true;
     }
@@ -705,6 +709,7 @@ struct Lane {
     k1[1] = qop * (dir[2] * B1[0] - dir[0] * B1[2]);
     k1[2] = qop * (dir[0] * B1[1] - dir[1] * B1[0]);
     const P tol = (P)o.stepTolerance;
+    const P h = (P)hd;
     const P h2 = h * h;
     const P hh = h * P(0.5);
     P p1[3], tt[3];
@@ -742,8 +747,8 @@ struct Lane {
     P x = sqrt(sqrt(tol / err));
     x = fmin(fmax(x, P(0.25)), P(4));
     if (!(err <= P(4) * tol)) {
-      h = h * x;
-      if (fabs((double)h) < fabs(o.stepSizeCutOff)) {
+      hd = hd * (double)x;
+      if (fabs(hd) < fabs(o.stepSizeCutOff)) {
         fail(fp, CK_TRACK_STEP_SIZE_STALLED);
         return;
       }
@@ -848,12 +853,20 @@ struct Lane {
       const P h6 = h * P(1.0 / 6.0);
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        pos[i] = pos[i] + ((double)h * this->dir[i] + (double)(hh6 * ((k1[i] + k2[i]) + k3[i])));
+        pos[i] = pos[i] + (hd * this->dir[i] + (double)(hh6 * ((k1[i] + k2[i]) + k3[i])));
         this->dir[i] = this->dir[i] + (double)(h6 * ((k1[i] + P(2) * (k2[i] + k3[i])) + k4[i]));
       }
       double* nd = this->dir;
       const double n2 = nd[0] * nd[0] + nd[1] * nd[1] + nd[2] * nd[2];
-      const double inv = 1.0 / sqrt(n2);
+      double inv;
+      if constexpr (sizeof(P) == sizeof(float)) {
+        // |dir|^2 is within a few 1e-3 of 1: an FP32 reciprocal square root
+        // and one Newton step in FP64 give ~1e-14 relative accuracy
+        const double y0 = (double)rsqrtf((float)n2);
+        inv = y0 * (1.5 - 0.5 * n2 * y0 * y0);
+      } else {
+        inv = 1.0 / sqrt(n2);
+      }
       nd[0] = nd[0] * inv;
       nd[1] = nd[1] * inv;
       nd[2] = nd[2] * inv;
@@ -866,8 +879,8 @@ struct Lane {
       deriv[5] = k4[1];
       deriv[6] = k4[2];
     }
-    pathAcc += (double)h;
-    const double nextAcc = fabs((double)(h * x));
+    pathAcc += hd;
+    const double nextAcc = fabs(hd * (double)x);
     if (nextAcc < fabs(initialH) || nextAcc > fabs(cAcc)) cAcc = nextAcc;
     stepStarted = false;
     ++steps;

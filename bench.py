@@ -465,6 +465,8 @@ def native_arm(args):
     acc = accuracy_report(b, snapshots["fp64"], snapshots["mixed"], min(n, 100000))
     cpu = cpu_baseline(det, b, forms["fp64"], budget_s=10.0)
     fit.close()
+    del keep_in, keep_out, keep_hin, keep_hout
+    serving = serving_report() if args.serving else None
     mixed = results["mixed"]
     line = {"metric": "tracks/s fitted (FP64 vs mixed, same accuracy); p50/p99 event latency",
             "value": round(mixed["tracks_per_s"], 1), "unit": "tracks/s", "n_gpus": world,
@@ -484,7 +486,7 @@ def native_arm(args):
             "e2e": {"value": round(n * world / (e2e_ms / 1e3), 1), "unit": "tracks/s",
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "ms_per_step": round(e2e_ms, 3), "path": "ck_fit_batch, host memory"},
-            "roofline": roofline, "accuracy": acc, "cpu_baseline": cpu,
+            "roofline": roofline, "accuracy": acc, "cpu_baseline": cpu, "serving": serving,
             "clocks": clocks.summary(),
             "gpu_launches": int(mixed["launches_per_step"] * args.steps),
             "kernel": {"mixed": mixed, "fp64": results["fp64"]},
@@ -493,6 +495,84 @@ def native_arm(args):
     if world > 1:
         torch.distributed.barrier()
     return 0
+
+
+def serving_report(precisions=("mixed", "fp64"), event_tracks=10000, pool=12, seed=77):
+    """Continuous-batching serving loop on 10k-track events of the uneven
+    workload (20-cylinder barrel, 4-20 hits, holes, outliers, grid field):
+    capacity measured by saturating the server, then Poisson arrivals at a
+    fraction of that capacity; p50/p99 event latency (submit -> results in
+    host memory) and sustained tracks/s per offered load."""
+    import threading
+
+    from acts_gb300 import abi, generate
+    from acts_gb300.fitter import CudaKalman
+    from acts_gb300.serving import FitServer
+
+    det = generate.Detector(abi.CKG_UNEVEN)
+    events = [generate.generate(det, event_tracks, seed=seed + i, first_track=i * event_tracks)
+              for i in range(pool)]
+    fit = CudaKalman.for_detector(det)
+    rng = np.random.default_rng(seed)
+    report = {"workload": "uneven barrel events of %d tracks (4-20 hits, holes 10 %%, outliers "
+                          "5 %%, grid field), Poisson arrivals" % event_tracks,
+              "memory_budget_gb": 40, "streams": 3}
+    for name in precisions:
+        prec = abi.PRECISION_MIXED if name == "mixed" else abi.PRECISION_FP64
+        opt = abi.default_options(precision=prec, outlier_chi2_cut=15.0)
+        srv = FitServer(fit, opt, memory_budget_bytes=40 << 30, n_streams=3, max_states=24,
+                        max_batch_tracks=8 * event_tracks)
+
+        def run(n_events, rate, first_id):
+            lat = {}
+            done = threading.Event()
+
+            def poller():
+                while len(lat) < n_events:
+                    r = srv.poll(timeout_ms=200)
+                    if r is not None:
+                        lat[r[0]] = r[2]
+                done.set()
+
+            th = threading.Thread(target=poller, daemon=True)
+            th.start()
+            t0 = time.perf_counter()
+            gaps = rng.exponential(1.0 / rate, n_events) if rate else np.zeros(n_events)
+            t_next = t0
+            for i in range(n_events):
+                t_next += gaps[i]
+                while True:
+                    dt = t_next - time.perf_counter()
+                    if dt <= 0:
+                        break
+                    time.sleep(min(dt, 0.002))
+                srv.submit(first_id + i, events[i % pool])
+            done.wait(120)
+            wall = time.perf_counter() - t0
+            v = np.array(list(lat.values()))
+            return v, wall
+
+        # capacity: everything submitted at once
+        run(2 * pool, 0, 0)  # warm-up
+        v, wall = run(8 * pool, 0, 1000)
+        cap_events = 8 * pool / wall
+        res = {"capacity_tracks_per_s": round(cap_events * event_tracks, 1), "loads": []}
+        loads = (0.1, 0.5, 0.8, 1.0, 1.2) if name == "mixed" else (0.5, 1.0)
+        nid = 10000
+        for f in loads:
+            rate = f * cap_events
+            n_ev = int(min(400, max(40, rate * 1.5)))
+            v, wall = run(n_ev, rate, nid)
+            nid += n_ev
+            res["loads"].append({"offered_fraction": f, "events": n_ev,
+                                 "offered_tracks_per_s": round(rate * event_tracks, 1),
+                                 "sustained_tracks_per_s": round(n_ev * event_tracks / wall, 1),
+                                 "p50_ms": round(float(np.percentile(v, 50)), 3),
+                                 "p99_ms": round(float(np.percentile(v, 99)), 3)})
+        srv.close()
+        report[name] = res
+    fit.close()
+    return report
 
 
 class _Null:
@@ -510,6 +590,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--tracks", type=int, default=1000000)
+    ap.add_argument("--no-serving", dest="serving", action="store_false",
+                    help="skip the serving-loop latency measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
