@@ -57,6 +57,11 @@ def lib():
         L.ck_destroy.argtypes = [C.c_void_p]
         L.ck_fit_batch.argtypes = [C.c_void_p, P(abi.ck_options), P(abi.ck_batch_in),
                                    P(abi.ck_batch_out), C.c_void_p]
+        L.ck_fit_batch_static.argtypes = [C.c_void_p, P(abi.ck_options), P(abi.ck_batch_in),
+                                          P(abi.ck_batch_out), C.c_void_p]
+        L.ck_static_scratch_bytes.argtypes = [C.c_int32, C.c_int32, C.c_int32]
+        L.ck_static_scratch_bytes.restype = C.c_int64
+        L.ck_static_scratch_capacity.restype = C.c_int64
         L.ck_sync.argtypes = [C.c_void_p]
         L.ck_last_kernel_ms.argtypes = [C.c_void_p, P(C.c_double)]
         L.ck_last_launch_count.argtypes = [C.c_void_p, P(C.c_int32)]
@@ -245,6 +250,20 @@ class CudaKalman:
     def fit_batch_raw(self, options, batch_in, batch_out, stream=None):
         _check(lib().ck_fit_batch(self._h, C.byref(options), C.byref(batch_in),
                                   C.byref(batch_out), stream))
+
+    def fit_batch_static(self, options, batch_in, batch_out, stream=None):
+        """ck_fit_batch_static: device-resident batch, pipeline scratch in the
+        library's static device array (no allocation)."""
+        _check(lib().ck_fit_batch_static(self._h, C.byref(options), C.byref(batch_in),
+                                         C.byref(batch_out), stream))
+
+    @staticmethod
+    def static_scratch_bytes(n_tracks, max_states, precision):
+        return lib().ck_static_scratch_bytes(int(n_tracks), int(max_states), int(precision))
+
+    @staticmethod
+    def static_scratch_capacity():
+        return lib().ck_static_scratch_capacity()
 
     def sync(self):
         _check(lib().ck_sync(self._h))

@@ -307,6 +307,24 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt,
                        const ck_batch_in* in, ck_batch_out* out, void* stream);
 ck_status ck_sync(ck_handle* h);
 
+/* ck_fit_batch for a device-resident batch (in->memory and out->memory both
+ * CK_MEM_DEVICE) that allocates nothing: the pipeline scratch is one
+ * statically sized device array (ck_static_scratch_capacity() bytes, 32 MiB)
+ * per device, shared by all handles. For callers that must not call the
+ * device allocator once running (cudaMalloc/cudaFree can synchronise the
+ * device; ck_fit_batch grows its buffers on demand). A batch needing more
+ * than the array (ck_static_scratch_bytes) fails with CK_ERR_SCRATCH_LIMIT.
+ * Nothing in the array has to start at zero. Calls whose device work
+ * overlaps (other streams or handles on the same device, unordered) race on
+ * the array. Make the first call before capturing the stream: it resolves
+ * the array's address. No counterpart in the reference. */
+ck_status ck_fit_batch_static(ck_handle* h, const ck_options* opt,
+                              const ck_batch_in* in, ck_batch_out* out, void* stream);
+/* Scratch bytes ck_fit_batch_static needs for a batch (-1 on bad sizes), and
+ * the size of the static array. No counterpart in the reference. */
+int64_t ck_static_scratch_bytes(int32_t n_tracks, int32_t max_states, int32_t precision);
+int64_t ck_static_scratch_capacity(void);
+
 /* Kernel-only timing of the most recent batch (CUDA events recorded on the
  * launching stream around the fit kernel): milliseconds. */
 ck_status ck_last_kernel_ms(ck_handle* h, double* ms);
