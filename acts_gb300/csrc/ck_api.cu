@@ -6,6 +6,7 @@
 // concurrent callers on the same handle are serialised by its mutex.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -187,9 +188,7 @@ void loadTuneCache(ck_handle* h) {
   std::ifstream f(h->cachePath);
   int p, v, tpb, bps;
   while (f >> p >> v >> tpb >> bps) {
-    if (p < 0 || p >= CK_NUM_PRECISIONS || v < 0 || v >= kNumFitVariants || tpb <= 0 ||
-        tpb > kFitMaxBlock ||
-        bps <= 0)
+    if (p < 0 || p >= CK_NUM_PRECISIONS || !validLaunch(v, tpb) || bps <= 0)
       continue;
     h->tune[p] = {v, tpb, bps, true};
   }
@@ -290,6 +289,11 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
   fp.rec_meta_d = (double*)c.recMetaD.p;
   fp.tip = (int32_t*)c.tip.p;
   fp.rec_stride = n;
+  {
+    const long long warps = (long long)grid * (tn.tpb / 32);
+    const long long per = warps > 0 ? (n + warps - 1) / warps : 32;
+    fp.lanes_per_warp = (int)std::min<long long>(32, std::max<long long>(1, per));
+  }
   fp.max_states = maxStates;
   fp.out = dout;
   fp.surfaces = h->dSurfaces;
@@ -423,6 +427,7 @@ ck_status ck_create(const ck_config* cfg, ck_handle** out) {
     if (!f.values_tesla) return fail(CK_ERR_INVALID_ARGUMENT, "field values missing");
   }
   if ((e = cudaSetDevice(cfg->device)) != cudaSuccess) return cudaFail(e, "cudaSetDevice");
+  if ((e = configureFitKernels()) != cudaSuccess) return cudaFail(e, "kernel set-up");
   ck_handle* h = new ck_handle();
   h->device = cfg->device;
   cudaDeviceGetAttribute(&h->smCount, cudaDevAttrMultiProcessorCount, cfg->device);
@@ -477,9 +482,12 @@ ck_status ck_create(const ck_config* cfg, ck_handle** out) {
   h->sortQueue = true;
   if (cfg->autotune_cache) h->cachePath = cfg->autotune_cache;
   for (int p = 0; p < CK_NUM_PRECISIONS; ++p) {
-    h->tune[p].variant = 0;
-    h->tune[p].tpb = cfg->threads_per_block > 0 ? std::min(cfg->threads_per_block, kFitMaxBlock)
-                                                : kFitMaxBlock;
+    // default: the block-compaction kernel with 256 slots per block, unless
+    // the configuration asks for a thread count
+    const bool fixedTpb = cfg->threads_per_block > 0;
+    h->tune[p].variant = fixedTpb ? 0 : kDefaultVariant;
+    h->tune[p].tpb = fixedTpb ? std::min(cfg->threads_per_block, kFitMaxBlock)
+                              : variantBlock(kDefaultVariant);
     h->tune[p].bps = cfg->blocks_per_sm > 0 ? cfg->blocks_per_sm : 0;
     h->tune[p].tuned = false;
   }
@@ -725,8 +733,8 @@ ck_status ck_get_launch_config(ck_handle* h, int32_t precision, int32_t* tpb, in
 
 ck_status ck_set_launch_config(ck_handle* h, int32_t precision, int32_t variant, int32_t tpb,
                                int32_t bps) {
-  if (!h || precision < 0 || precision >= CK_NUM_PRECISIONS || variant < 0 || variant >= kNumFitVariants ||
-      tpb <= 0 || tpb > kFitMaxBlock || (tpb % 32) != 0 || bps <= 0)
+  if (!h || precision < 0 || precision >= CK_NUM_PRECISIONS || !validLaunch(variant, tpb) ||
+      bps <= 0)
     return fail(CK_ERR_INVALID_ARGUMENT, "bad launch configuration");
   std::lock_guard<std::mutex> lock(h->mu);
   int maxB = occupancyBlocks(precision, variant, tpb);
@@ -758,7 +766,8 @@ ck_status ck_autotune(ck_handle* h, const ck_options* opt, const ck_batch_in* in
   double bestMs = 1e30;
   std::string log;
   for (int v = 0; v < kNumFitVariants; ++v)
-    for (int tpb : {32, 64, 128}) {
+    for (int tpb : {32, 64, 128, 256}) {
+      if (!validLaunch(v, tpb)) continue;
       const int maxB = occupancyBlocks(p, v, tpb);
       if (maxB <= 0) continue;
       std::vector<int> cands = {maxB, std::max(1, (maxB * 3) / 4), std::max(1, maxB / 2)};

@@ -62,6 +62,15 @@ CK_D void normalizePhiTheta(double& phi, double& theta) {
 // ------------------------------------------------------------------ float
 // Correctly rounded float logarithm shared with the CPU oracle.
 CK_D float ck_logf(float x) { return (float)log((double)x); }
+// The material physics' logarithm: correctly rounded (plain form, equal to
+// the oracle's) or the FP32 logf (mixed form, within 2 ulp).
+template <bool EXACT>
+CK_D float mlogf(float x) {
+  if constexpr (EXACT)
+    return ck_logf(x);
+  else
+    return logf(x);
+}
 // Un-contracted float arithmetic: the reference evaluates its material
 // physics in float without FMA; these intrinsics keep the device identical.
 CK_D float fm(float a, float b) { return __fmul_rn(a, b); }
@@ -491,24 +500,27 @@ struct RelQ {
 CK_D float computeEpsilon(const MatConst& C, float Ne, float thickness, const RelQ& rq) {
   return fm(fm(fm(fm(0.5f, C.K), Ne), thickness), rq.q2OverBeta2);
 }
+template <bool EXACT>
 CK_D float computeDeltaHalf(const MatConst& C, float I, float Ne, const RelQ& rq) {
   if (rq.betaGamma < 10.0f) return 0.0f;
   const float plasmaEnergy = fm(C.plasmaScale, fsq(fd(Ne, C.invCm3)));
-  return fs(fa(ck_logf(rq.betaGamma), ck_logf(fd(plasmaEnergy, I))), 0.5f);
+  return fs(fa(mlogf<EXACT>(rq.betaGamma), mlogf<EXACT>(fd(plasmaEnergy, I))), 0.5f);
 }
 
+template <bool EXACT = true>
 CK_D float energyLossBethe(const MatConst& C, float I, float Ne, float thickness, float m,
                            float qOverP, float absQ) {
   const RelQ rq(m, qOverP, absQ);
   const float eps = computeEpsilon(C, Ne, thickness, rq);
-  const float dhalf = computeDeltaHalf(C, I, Ne, rq);
+  const float dhalf = computeDeltaHalf<EXACT>(C, I, Ne, rq);
   const float u = fm(fm(fm(2.0f, C.Me), rq.betaGamma), rq.betaGamma);
   const float mfrac = fd(C.Me, m);
   const float nominator = fm(fm(fm(2.0f, C.Me), rq.betaGamma), rq.betaGamma);
   const float denom = fa(fa(1.0f, fm(fm(2.0f, rq.gamma), mfrac)), fm(mfrac, mfrac));
   const float wmax = fd(nominator, denom);
   const float running =
-      fs(fs(fa(ck_logf(fd(u, I)), ck_logf(fd(wmax, I))), fm(2.0f, rq.beta2)), fm(2.0f, dhalf));
+      fs(fs(fa(mlogf<EXACT>(fd(u, I)), mlogf<EXACT>(fd(wmax, I))), fm(2.0f, rq.beta2)),
+         fm(2.0f, dhalf));
   return fm(eps, running);
 }
 
@@ -522,19 +534,20 @@ CK_D float landauSigmaQOverP(const MatConst& C, float Ne, float thickness, float
   return fm(fm(fm(qOverBeta, pInv), pInv), sigmaE);
 }
 
+template <bool EXACT = true>
 CK_D float theta0(const MatConst& C, float tX0, int absPdg, float m, float qOverP, float absQ) {
   const float momentumInv = fabsf(fd(qOverP, absQ));
   const float q2OverBeta2 = RelQ(m, qOverP, absQ).q2OverBeta2;
   const float t = fsq(fm(tX0, q2OverBeta2));
   if (absPdg == 11) {
     // Rossi-Greisen (Interactions.cpp:490-495), log10 = log / log(10)
-    const float lg = fd(ck_logf(fm(10.0f, tX0)), C.log10f);
+    const float lg = fd(mlogf<EXACT>(fm(10.0f, tX0)), C.log10f);
     return (float)dm(dm(dm(C.rossi, (double)momentumInv), (double)t),
                      (double)fa(1.0f, fm(0.125f, lg)));
   }
   // Highland (Interactions.cpp:484-489): double product of the float terms
   return (float)dm(dm(dm(C.highland, (double)momentumInv), (double)t),
-                   (double)fa(1.0f, fm(fm(0.038f, 2.0f), ck_logf(t))));
+                   (double)fa(1.0f, fm(fm(0.038f, 2.0f), mlogf<EXACT>(t))));
 }
 
 struct MatEffects {
@@ -558,15 +571,26 @@ CK_D MatEffects materialEffects(const MatConst& C, const DevSurface* __restrict_
   vacuum = (__ldg(&s->vacuum) != 0) || thick <= 0.0f;
   if (vacuum) return e;
   const float I = __ldg(&s->matI), Ne = __ldg(&s->matNe);
-  if (el) e.eLoss = (double)energyLossBethe(C, I, Ne, thick, mass, qOverP, absQ);
+  // the plain form reproduces the reference's float physics bit for bit; the
+  // mixed form evaluates the same formulas in FP32 throughout
+  constexpr bool EXACT = sizeof(P) == sizeof(double);
+  if (el) e.eLoss = (double)energyLossBethe<EXACT>(C, I, Ne, thick, mass, qOverP, absQ);
   if (ms) {
-    const double th0 = (double)theta0(C, tX0, absPdg, mass, qOverP, absQ);
-    const double d0 = (double)dir[0], d1 = (double)dir[1], d2 = (double)dir[2];
-    const double nrm = sqrt(da(da(dm(d0, d0), dm(d1, d1)), dm(d2, d2)));
-    const double prp = sqrt(da(dm(d0, d0), dm(d1, d1)));
-    const double sigmaPhi = dm(th0, nrm / prp);
-    e.varPhi = dm(sigmaPhi, sigmaPhi);
-    e.varTheta = dm(th0, th0);
+    const float th0f = theta0<EXACT>(C, tX0, absPdg, mass, qOverP, absQ);
+    if constexpr (EXACT) {
+      const double th0 = (double)th0f;
+      const double d0 = (double)dir[0], d1 = (double)dir[1], d2 = (double)dir[2];
+      const double nrm = sqrt(da(da(dm(d0, d0), dm(d1, d1)), dm(d2, d2)));
+      const double prp = sqrt(da(dm(d0, d0), dm(d1, d1)));
+      const double sigmaPhi = dm(th0, nrm / prp);
+      e.varPhi = dm(sigmaPhi, sigmaPhi);
+      e.varTheta = dm(th0, th0);
+    } else {
+      const float d0 = (float)dir[0], d1 = (float)dir[1], d2 = (float)dir[2];
+      const float sigmaPhi = th0f * sqrtf((d0 * d0 + d1 * d1 + d2 * d2) / (d0 * d0 + d1 * d1));
+      e.varPhi = (double)(sigmaPhi * sigmaPhi);
+      e.varTheta = (double)(th0f * th0f);
+    }
   }
   if (el) {
     const double sq = (double)landauSigmaQOverP(C, Ne, thick, mass, qOverP, absQ);

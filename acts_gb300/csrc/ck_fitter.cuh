@@ -143,6 +143,17 @@ struct Lane {
     }
   }
 
+  // Surface::isOnSurface part of globalToLocal: the check alone, without
+  // the local coordinates
+  CK_D bool onSurface(const Surf<double>& sf) const {
+    double l[3];
+    sf.toLocal3(pos, l);
+    if (sf.type == CK_SURFACE_PLANE) return fabs(l[2]) <= kOnSurfaceTolerance;
+    double inttol = sf.radius * 0.0001;
+    if (inttol < 0.01) inttol = 0.01;
+    return fabs(sqrt(l[0] * l[0] + l[1] * l[1]) - sf.radius) <= inttol;
+  }
+
   // Surface::globalToLocal in double (the bound parameters are outputs)
   CK_NI bool toLocal(const Surf<double>& sf, double loc[2]) const {
     double l[3];
@@ -198,6 +209,69 @@ struct Lane {
     sf.toGlobal3(l, pos);
     tim = b[5];
     qop = b[4];
+  }
+
+  // stepper.update with the filtered parameters (EigenStepper.ipp:128-138).
+  // The plain form evaluates transformBoundToFreeParameters; the mixed form
+  // rotates the predicted free state (still held) by the small filtered
+  // changes of phi, theta and the cylinder angle, with FP64 sines and cosines
+  // of those changes from their Taylor series — no FP64 trigonometry.
+  CK_D void updateFree(const Surf<double>& sf, const double pred[6], const double filt[6]) {
+    if constexpr (sizeof(P) == sizeof(double)) {
+      boundToFree(sf, filt);
+    } else {
+      const double dphi = radian_sym(filt[2] - pred[2]);
+      const double dtheta = filt[3] - pred[3];
+      const double dalpha = sf.type == CK_SURFACE_PLANE ? 0.0 : (filt[0] - pred[0]) / sf.radius;
+      const double lim = 0.05;
+      if (!(fabs(dphi) < lim && fabs(dtheta) < lim && fabs(dalpha) < lim)) {
+        boundToFree(sf, filt);
+        return;
+      }
+      auto sc = [](double x, double& sn, double& cs) {
+        const double x2 = x * x;
+        sn = x * (1.0 + x2 * (-1.0 / 6 + x2 * (1.0 / 120 + x2 * (-1.0 / 5040 + x2 * (1.0 / 362880)))));
+        cs = 1.0 + x2 * (-0.5 + x2 * (1.0 / 24 + x2 * (-1.0 / 720 + x2 * (1.0 / 40320))));
+      };
+      // 1/sqrt(v) for v near a known scale: FP32 estimate, one FP64 Newton step
+      auto rsq = [](double v) {
+        const double y = (double)rsqrtf((float)v);
+        return y * (1.5 - 0.5 * v * y * y);
+      };
+      // direction
+      const double s2 = dir[0] * dir[0] + dir[1] * dir[1];
+      const double ist = rsq(s2);
+      const double cphi = dir[0] * ist, sphi = dir[1] * ist;
+      const double stheta = s2 * ist, ctheta = dir[2];
+      double sdp, cdp, sdt, cdt;
+      sc(dphi, sdp, cdp);
+      sc(dtheta, sdt, cdt);
+      const double cp = cphi * cdp - sphi * sdp, sp = sphi * cdp + cphi * sdp;
+      const double st = stheta * cdt + ctheta * sdt, ct = ctheta * cdt - stheta * sdt;
+      dir[0] = cp * st;
+      dir[1] = sp * st;
+      dir[2] = ct;
+      // position
+      double l[3];
+      if (sf.type == CK_SURFACE_PLANE) {
+        l[0] = filt[0];
+        l[1] = filt[1];
+        l[2] = 0.0;
+      } else {
+        double lp[3];
+        sf.toLocal3(pos, lp);
+        const double ir = rsq(lp[0] * lp[0] + lp[1] * lp[1]);
+        const double ca = lp[0] * ir, sa = lp[1] * ir;
+        double sda, cda;
+        sc(dalpha, sda, cda);
+        l[0] = sf.radius * (ca * cda - sa * sda);
+        l[1] = sf.radius * (sa * cda + ca * sda);
+        l[2] = filt[1];
+      }
+      sf.toGlobal3(l, pos);
+      tim = filt[5];
+      qop = filt[4];
+    }
   }
 
   // Surface::boundToFreeJacobian in transport form at the current state
@@ -310,8 +384,7 @@ struct Lane {
       for (int i = 0; i < 3; ++i) ez[i] = (P)sfd.R[i * 3 + 0] * n0 + (P)sfd.R[i * 3 + 1] * n1;
       pc = fabs(P(1) / (ez[0] * d[0] + ez[1] * d[1] + ez[2] * d[2]));
     }
-    double loc[2];
-    if (!toLocal(sfd, loc)) return false;
+    if (!onSurface(sfd)) return false;
     float f1 = 1.0f;
     if (__ldg(&ds->vacuum) == 0) {
       const float split = __ldg(&ds->split);
@@ -325,21 +398,41 @@ struct Lane {
                                             qOverPf, fp.opt.multipleScattering != 0,
                                             fp.opt.energyLoss != 0, vac);
     if (vac) return true;
-    const double massd = (double)mass;
-    const double mom = absMomentum(absQ, qop);
-    const double nextE = sqrt(massd * massd + mom * mom) - e.eLoss;
-    double nextP = 0.0;
-    if (massd < nextE) {
-      const double am = fabs(massd);
-      nextP = sqrt((nextE - am) * (nextE + am));
-    }
-    nextP = fmax(0.01, nextP);
     const float signedQ = (float)copysign((double)absQ, (double)qOverPf);
-    qop = (double)signedQ / nextP;
+    if constexpr (sizeof(P) == sizeof(double)) {
+      // PointwiseMaterialInteraction::updateState (hpp:188-198) in FP64
+      const double massd = (double)mass;
+      const double mom = absMomentum(absQ, qop);
+      const double nextE = sqrt(massd * massd + mom * mom) - e.eLoss;
+      double nextP = 0.0;
+      if (massd < nextE) {
+        const double am = fabs(massd);
+        nextP = sqrt((nextE - am) * (nextE + am));
+      }
+      nextP = fmax(0.01, nextP);
+      qop = (double)signedQ / nextP;
+    } else {
+      // the same update as a relative change of q/p: with u = nextP^2/p^2 - 1
+      // = -eLoss (2E - eLoss) / p^2, q/p scales by 1/sqrt(1 + u); the small
+      // correction is formed in FP32 and applied to the FP64 q/p
+      const float m = mass;
+      const float p = fabsf(signedQ / (float)qop);
+      const float E = sqrtf(m * m + p * p);
+      const float eLoss = (float)e.eLoss;
+      const float nextE = E - eLoss;
+      if (m < nextE && (nextE - m) * (nextE + m) >= 1e-4f) {
+        const float u = -eLoss * (2.0f * E - eLoss) / (p * p);
+        const float r = sqrtf(1.0f + u);
+        const float delta = u / (r * (1.0f + r));  // 1/sqrt(1+u) - 1 = -u/(r(1+r))
+        qop = qop - qop * (double)delta;
+      } else {
+        qop = (double)signedQ / 0.01;  // nextP clamped to 10 MeV
+      }
+    }
     if (!coasting) {
-      cov[sidx(2, 2)] = (CV)fmax(0.0, (double)cov[sidx(2, 2)] + e.varPhi);
-      cov[sidx(3, 3)] = (CV)fmax(0.0, (double)cov[sidx(3, 3)] + e.varTheta);
-      cov[sidx(4, 4)] = (CV)fmax(0.0, (double)cov[sidx(4, 4)] + e.varQoP);
+      cov[sidx(2, 2)] = fmax(CV(0), cov[sidx(2, 2)] + (CV)e.varPhi);
+      cov[sidx(3, 3)] = fmax(CV(0), cov[sidx(3, 3)] + (CV)e.varTheta);
+      cov[sidx(4, 4)] = fmax(CV(0), cov[sidx(4, 4)] + (CV)e.varQoP);
     }
     return true;
   }
@@ -436,8 +529,7 @@ struct Lane {
     for (int i = 0; i < 21; ++i) cov[i] = outc[i];
 #pragma unroll
     for (int i = 0; i < 7; ++i) deriv[i] = P(0);
-    double loc[2];
-    if (toLocal(sfd, loc)) initT(sfd);
+    if (onSurface(sfd)) initT(sfd);
   }
 
   // --------------------------------------------------------------- actor
@@ -499,8 +591,7 @@ struct Lane {
         flags |= CK_FLAG_HAS_MEASUREMENT;
 #pragma unroll
         for (int i = 0; i < 6; ++i) rec.p(k, kRecFilt + i) = filt[i];
-        // stepper.update (EigenStepper.ipp:128-138)
-        boundToFree(sf, filt);
+        updateFree(sf, bp, filt);
 #pragma unroll
         for (int i = 0; i < 21; ++i) {
           cov[i] = (CV)F[i];
@@ -1080,7 +1171,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) fitKernel(FitParams fp) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   Lane<P, CV> L;
-  L.phase = PH_FETCH;
+  L.phase = lane < fp.lanes_per_warp ? PH_FETCH : PH_DONE;
   L.t = -1;
   L.q = -1;
   while (true) {
@@ -1116,6 +1207,95 @@ __global__ void __launch_bounds__(BLOCK, MINB) fitKernel(FitParams fp) {
         L.surface(fp, L.q);
     }
   }
+}
+
+// Persistent forward-filter kernel with block-level phase compaction. The
+// state of every track in flight lives in shared memory (one Lane per slot,
+// S slots per block). Each round the block counts its slots per phase, picks
+// the phase most slots are in, lists those slots contiguously and lets
+// thread i advance slot list[i] by one phase step — so the chosen phase runs
+// on full warps. On GB300 an FP64 warp instruction holds the SM's FP64 unit
+// for 16 clocks however few of its lanes are active, so the lanes a warp
+// carries are the FP64 throughput it gets.
+template <typename P, typename CV, int S>
+__global__ void __launch_bounds__(S, 1) fitKernelCompact(FitParams fp) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  Lane<P, CV>* st = reinterpret_cast<Lane<P, CV>*>(smem);
+  int* items = reinterpret_cast<int*>(smem + sizeof(Lane<P, CV>) * S);
+  __shared__ int warpCnt[S / 32][3];
+  __shared__ int chosen, nItems;
+  const unsigned FULL = 0xffffffffu;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  st[tid].phase = tid < fp.lanes_per_warp * (S / 32) ? PH_FETCH : PH_DONE;
+  st[tid].t = -1;
+  st[tid].q = -1;
+  __syncthreads();
+  while (true) {
+    const int ph = st[tid].phase;
+    const unsigned mF = __ballot_sync(FULL, ph == PH_FETCH);
+    const unsigned mS = __ballot_sync(FULL, ph == PH_STEP);
+    const unsigned mU = __ballot_sync(FULL, ph == PH_SURFACE);
+    if (lane == 0) {
+      warpCnt[warp][0] = __popc(mF);
+      warpCnt[warp][1] = __popc(mS);
+      warpCnt[warp][2] = __popc(mU);
+    }
+    __syncthreads();
+    if (tid == 0) {
+      int tot[3] = {0, 0, 0};
+      for (int w = 0; w < S / 32; ++w)
+        for (int k = 0; k < 3; ++k) tot[k] += warpCnt[w][k];
+      int best = PH_FETCH, bc = tot[0];
+      if (tot[1] > bc) {
+        best = PH_STEP;
+        bc = tot[1];
+      }
+      if (tot[2] > bc) {
+        best = PH_SURFACE;
+        bc = tot[2];
+      }
+      chosen = bc > 0 ? best : -1;
+      nItems = bc;
+    }
+    __syncthreads();
+    const int c = chosen;
+    if (c < 0) break;
+    const unsigned m = c == PH_FETCH ? mF : (c == PH_STEP ? mS : mU);
+    int base = 0;
+    for (int w = 0; w < warp; ++w) base += warpCnt[w][c];
+    if (ph == c) items[base + __popc(m & ((1u << lane) - 1u))] = tid;
+    __syncthreads();
+    if (tid < nItems) {
+      const int slot = items[tid];
+      Lane<P, CV> L = st[slot];
+      if (c == PH_FETCH) {
+        // one ticket per warp for its fetching threads
+        const unsigned act = __activemask();
+        const int leader = __ffs(act) - 1;
+        int qb = 0;
+        if (lane == leader) qb = atomicAdd(fp.ticket, __popc(act));
+        qb = __shfl_sync(act, qb, leader);
+        const int q = qb + __popc(act & ((1u << lane) - 1u));
+        if (q >= fp.n_queue) {
+          L.phase = PH_DONE;
+        } else {
+          L.q = q;
+          L.start(fp, q, fp.perm ? __ldg(&fp.perm[q]) : q);
+        }
+      } else if (c == PH_STEP) {
+        L.step(fp, L.q);
+      } else {
+        L.surface(fp, L.q);
+      }
+      st[slot] = L;
+    }
+    __syncthreads();
+  }
+}
+
+template <typename P, typename CV, int S>
+constexpr size_t compactSmemBytes() {
+  return sizeof(Lane<P, CV>) * S + sizeof(int) * S;
 }
 
 // Smoother kernel: one lane per queue position; lanes of a warp hold tracks

@@ -98,6 +98,9 @@ struct FitParams {
   double* rec_meta_d;
   int32_t* tip;
   int rec_stride;
+  // lanes of each warp that take tracks: all 32 for large batches; fewer
+  // when the batch is small, so that its tracks spread over all warps
+  int lanes_per_warp;
   int max_states;
   // outputs (device memory, ck_batch_out layout)
   ck_batch_out out;

@@ -15,8 +15,14 @@ cudaError_t launchFitFP64(const FitParams& fp, int variant, int grid, int block,
     case 1:
       fitKernel<double, double, 128, 3><<<grid, block, 0, st>>>(fp);
       break;
-    default:
+    case 2:
       fitKernel<double, double, 128, 4><<<grid, block, 0, st>>>(fp);
+      break;
+    case 3:
+      fitKernelCompact<double, double, 256><<<grid, 256, compactSmemBytes<double, double, 256>(), st>>>(fp);
+      break;
+    default:
+      fitKernelCompact<double, double, 128><<<grid, 128, compactSmemBytes<double, double, 128>(), st>>>(fp);
       break;
   }
   return cudaGetLastError();
@@ -31,17 +37,42 @@ int occupancyFP64(int variant, int tpb) {
     case 1:
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernel<double, double, 128, 3>, tpb, 0);
       break;
-    default:
+    case 2:
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernel<double, double, 128, 4>, tpb, 0);
+      break;
+    case 3:
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelCompact<double, double, 256>, 256,
+                                                    compactSmemBytes<double, double, 256>());
+      break;
+    default:
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelCompact<double, double, 128>, 128,
+                                                    compactSmemBytes<double, double, 128>());
       break;
   }
   return n;
+}
+
+cudaError_t configureFP64() {
+  cudaError_t e = cudaFuncSetAttribute(fitKernelCompact<double, double, 256>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)compactSmemBytes<double, double, 256>());
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(fitKernelCompact<double, double, 128>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)compactSmemBytes<double, double, 128>());
 }
 
 cudaError_t launchSmoothFP64(const FitParams& fp, cudaStream_t st) {
   const int grid = (fp.n_queue + kSmoothBlock - 1) / kSmoothBlock;
   smoothKernel<double, kSmoothBlock><<<grid, kSmoothBlock, 0, st>>>(fp);
   return cudaGetLastError();
+}
+
+cudaError_t configureMixed();
+
+cudaError_t configureFitKernels() {
+  cudaError_t e = configureFP64();
+  return e != cudaSuccess ? e : configureMixed();
 }
 
 int occupancyBlocks(int precision, int variant, int tpb) {

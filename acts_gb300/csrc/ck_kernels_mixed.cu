@@ -17,11 +17,27 @@ cudaError_t launchFitMixed(const FitParams& fp, int variant, int grid, int block
     case 1:
       fitKernel<float, float, 128, 3><<<grid, block, 0, st>>>(fp);
       break;
-    default:
+    case 2:
       fitKernel<float, float, 128, 4><<<grid, block, 0, st>>>(fp);
+      break;
+    case 3:
+      fitKernelCompact<float, float, 256><<<grid, 256, compactSmemBytes<float, float, 256>(), st>>>(fp);
+      break;
+    default:
+      fitKernelCompact<float, float, 128><<<grid, 128, compactSmemBytes<float, float, 128>(), st>>>(fp);
       break;
   }
   return cudaGetLastError();
+}
+
+cudaError_t configureMixed() {
+  cudaError_t e = cudaFuncSetAttribute(fitKernelCompact<float, float, 256>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)compactSmemBytes<float, float, 256>());
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(fitKernelCompact<float, float, 128>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)compactSmemBytes<float, float, 128>());
 }
 
 cudaError_t launchSmoothMixed(const FitParams& fp, cudaStream_t st) {
@@ -39,8 +55,16 @@ int occupancyMixed(int variant, int tpb) {
     case 1:
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernel<float, float, 128, 3>, tpb, 0);
       break;
-    default:
+    case 2:
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernel<float, float, 128, 4>, tpb, 0);
+      break;
+    case 3:
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelCompact<float, float, 256>, 256,
+                                                    compactSmemBytes<float, float, 256>());
+      break;
+    default:
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelCompact<float, float, 128>, 128,
+                                                    compactSmemBytes<float, float, 128>());
       break;
   }
   return n;

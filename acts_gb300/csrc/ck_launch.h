@@ -7,8 +7,19 @@
 
 namespace ck {
 
-constexpr int kNumFitVariants = 3;
+// Forward-filter kernel variants: 0-2 per-warp phase scheduling with
+// register caps of 255 / 168 / 128 (1 / 3 / 4 resident 128-thread blocks);
+// 3-4 block-level phase compaction with 256 / 128 slots per block.
+constexpr int kNumFitVariants = 5;
 constexpr int kFitMaxBlock = 128;
+constexpr int kDefaultVariant = 3;
+// block size a variant requires (0: any multiple of 32 up to kFitMaxBlock)
+inline int variantBlock(int variant) { return variant == 3 ? 256 : (variant == 4 ? 128 : 0); }
+inline bool validLaunch(int variant, int tpb) {
+  if (variant < 0 || variant >= kNumFitVariants) return false;
+  const int vb = variantBlock(variant);
+  return vb ? tpb == vb : (tpb > 0 && tpb <= kFitMaxBlock && tpb % 32 == 0);
+}
 
 cudaError_t launchFitFP64(const FitParams& fp, int variant, int grid, int block,
                           cudaStream_t st);
@@ -17,6 +28,8 @@ cudaError_t launchFitMixed(const FitParams& fp, int variant, int grid, int block
 int occupancyFP64(int variant, int tpb);
 int occupancyMixed(int variant, int tpb);
 int occupancyBlocks(int precision, int variant, int tpb);
+// one-time per-device set-up of the kernels (shared-memory limits)
+cudaError_t configureFitKernels();
 cudaError_t launchSmoothFP64(const FitParams& fp, cudaStream_t st);
 cudaError_t launchSmoothMixed(const FitParams& fp, cudaStream_t st);
 inline cudaError_t launchSmooth(const FitParams& fp, int precision, cudaStream_t st) {

@@ -1,21 +1,24 @@
 // ck_server.cu — continuous-batching serving loop of the fitter.
 //
-// Events (one ck_batch_in each) arrive through ck_server_submit from any
-// host thread; their inputs are copied and queued. One request thread runs
-// the loop:
+// Events arrive through ck_server_submit from any host thread, each with its
+// own input arrays (ck_batch_in) and result arrays (ck_batch_out), both
+// owned by the caller and in host (pageable or page-locked) or device
+// memory. Nothing is copied at submission. One request thread runs the loop:
 //   * admission: while a stream slot is free, the pending events (oldest
-//     first) that fit the slot's track capacity are taken together into one
-//     co-batch — events of different sizes share a launch;
-//   * launch: the co-batch's inputs are staged through the slot's pinned
-//     buffer, copied to the slot's device buffers and fitted on the slot's
-//     stream with a share of the GPU (grid = resident blocks / streams), so
-//     batches on different streams overlap on the device;
-//   * completion: finished slots are detected with CUDA events, their
-//     results copied back and split per event, each event's latency is its
-//     submit-to-completion wall time.
-// Device memory: every slot holds input, output and scratch buffers for its
+//     first) that fit the slot's capacity are taken together into one
+//     co-batch — events of different sizes share one launch;
+//   * launch: each event's inputs are copied straight from the caller's
+//     arrays into the slot's device buffers (its CSR offsets shifted on the
+//     device), the co-batch is fitted on the slot's stream over the whole GPU
+//     (a later co-batch on another stream fills the SMs the earlier one
+//     frees as its queue drains); each event's results are copied from the co-batch's
+//     SoA arrays into the caller's arrays with one strided copy per array
+//     (pageable host results go through the slot's page-locked buffer);
+//   * completion: finished slots are found with CUDA events; an event's
+//     latency is its submit-to-results wall time.
+// Device memory: every slot holds input, output and record buffers for its
 // capacity; the capacity is the largest track count for which all slots fit
-// the memory budget. An event larger than a slot's capacity is rejected with
+// the memory budget. An event larger than a slot is rejected with
 // CK_ERR_BUDGET at submission. Track state stays on the device from the
 // input copy to the result copy.
 #include <cuda_runtime.h>
@@ -28,7 +31,6 @@
 #include <memory>
 #include <mutex>
 #include <thread>
-#include <type_traits>
 #include <vector>
 
 #include "ck_api_internal.h"
@@ -40,21 +42,22 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+constexpr int kMaxEventsPerBatch = 1024;
+constexpr int kPlannedSurfacesPerTrack = 20;
+
 struct Event {
   int64_t id = 0;
   int n = 0;
-  std::vector<int32_t> seqOff, seq, measOff, measSurf, pdg;
-  std::vector<double> measVal, measCov, sp, sc, frames;
-  std::vector<float> part;
+  int nSeq = 0, nMeas = 0;
+  ck_batch_in in{};
+  ck_batch_out out{};
+  bool staged = false;  // pageable host results: through the slot's pinned buffer
+  ck_status status = CK_OK;
   Clock::time_point submitted;
-  // results (host)
-  std::vector<int32_t> status, nStates, nMeas, nHoles, nOut, ndf, surf;
-  std::vector<uint32_t> flags;
-  std::vector<double> chi2, path, schi2, sm, smc, fi, fic, pr, prc, jac;
   double latencyMs = 0;
 };
 
-// Output components carried per event.
+// Output components computed by the server.
 struct OutSpec {
   bool sm, fi, pr, jac;
 };
@@ -66,14 +69,51 @@ struct Slot {
   DevBuf din[11];
   size_t inPlanned[11] = {};
   DevBuf dout[18];
-  void* pinIn = nullptr;
-  size_t pinInBytes = 0;
-  void* pinOut = nullptr;
+  DevBuf table;              // per-event {t0, m, seqBase, measBase} on the device
+  int32_t* pinTable = nullptr;
+  void* pinOut = nullptr;    // staging of pageable results
   size_t pinOutBytes = 0;
   std::vector<std::unique_ptr<Event>> events;
-  int nTracks = 0;
+  int nTracks = 0, nSeq = 0, nMeas = 0;
   bool busy = false;
 };
+
+// element size and components per ck_batch_out array, in the order of
+// outFields()
+constexpr size_t kOutElem[18] = {4, 4, 4, 4, 4, 4, 8, 4, 4, 8, 8, 8, 8, 8, 8, 8, 8, 8};
+constexpr int kOutComp[18] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 6, 36, 6, 36, 6, 36, 36};
+constexpr bool kPerState[18] = {false, false, false, false, false, false, false, true, true,
+                                true,  true,  true,  true,  true,  true,  true,  true,  true};
+
+void outFields(ck_batch_out& o, void** f[18]) {
+  void** a[18] = {(void**)&o.status,          (void**)&o.n_states,
+                  (void**)&o.n_measurements,  (void**)&o.n_holes,
+                  (void**)&o.n_outliers,      (void**)&o.ndf,
+                  (void**)&o.chi2_sum,        (void**)&o.state_surface,
+                  (void**)&o.state_flags,     (void**)&o.state_path_length,
+                  (void**)&o.state_chi2,      (void**)&o.predicted,
+                  (void**)&o.predicted_cov,   (void**)&o.filtered,
+                  (void**)&o.filtered_cov,    (void**)&o.smoothed,
+                  (void**)&o.smoothed_cov,    (void**)&o.jacobian};
+  for (int i = 0; i < 18; ++i) f[i] = a[i];
+}
+
+// CSR offsets of a co-batch: each event's offsets were copied unshifted to
+// [t0, t0 + m) (the last event's also to n); add the event's bases.
+__global__ void shiftOffsets(int32_t* __restrict__ seqOff, int32_t* __restrict__ measOff,
+                             const int4* __restrict__ table, int nEvents) {
+  const int e = blockIdx.y;
+  const int4 ev = table[e];
+  const int count = ev.y + (e == nEvents - 1 ? 1 : 0);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    seqOff[ev.x + i] += ev.z;
+    measOff[ev.x + i] += ev.w;
+  }
+}
+
+__global__ void fillInt(int32_t* __restrict__ p, int n, int32_t v) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
+}
 
 }  // namespace
 
@@ -97,15 +137,26 @@ struct ck_server {
   int64_t submitted = 0, completed = 0, tracksDone = 0;
   size_t bytesInUse = 0;
 
+  // device bytes per track of a slot: inputs at the planned surfaces per
+  // track, outputs of the computed components, track-state records
   size_t perTrackBytes(int maxStates) const {
-    // inputs: offsets, 20 sequence surfaces, 20 measurements, start pars
-    const size_t in = 2 * 4 + 20 * 4 + 20 * (4 + 16 + 32) + 48 + 288 + 96 + 8 + 4;
+    const size_t k = kPlannedSurfacesPerTrack;
+    const size_t in = 2 * 4 + k * 4 + k * (4 + 16 + 32) + 48 + 288 + 96 + 8 + 4;
     size_t out = 7 * 8 + (size_t)maxStates * 24;
     if (spec.sm) out += (size_t)maxStates * 42 * 8;
     if (spec.fi) out += (size_t)maxStates * 42 * 8;
     if (spec.pr) out += (size_t)maxStates * 42 * 8;
     if (spec.jac) out += (size_t)maxStates * 36 * 8;
     return in + out + recordBytesPerTrack(maxStates, opt.precision);
+  }
+  bool computes(int field) const {
+    switch (field) {
+      case 11: case 12: return spec.pr;
+      case 13: case 14: return spec.fi;
+      case 15: case 16: return spec.sm;
+      case 17: return spec.jac;
+      default: return true;
+    }
   }
 };
 
@@ -117,80 +168,104 @@ ck_status slotAlloc(ck_server* s, Slot& sl) {
       (e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming)) != cudaSuccess)
     return cudaFail(e, "server stream");
   const size_t cap = (size_t)s->capacity;
+  const size_t k = kPlannedSurfacesPerTrack;
   const int ms = s->cfg.max_states;
-  const size_t inBytes[11] = {4 * (cap + 1), 4 * cap * 20, 4 * (cap + 1), 4 * cap * 20,
-                              16 * cap * 20, 32 * cap * 20, 48 * cap, 288 * cap,
-                              96 * cap, 8 * cap, 4 * cap};
-  size_t pin = 0;
+  const size_t inBytes[11] = {4 * (cap + 1), 4 * cap * k, 4 * (cap + 1), 4 * cap * k,
+                              16 * cap * k,  32 * cap * k, 48 * cap,  288 * cap,
+                              96 * cap,      8 * cap,      4 * cap};
   for (int i = 0; i < 11; ++i) {
     if ((e = sl.din[i].ensure(inBytes[i])) != cudaSuccess) return cudaFail(e, "server input");
     sl.inPlanned[i] = inBytes[i];
-    pin += (inBytes[i] + 255) & ~(size_t)255;
   }
   const size_t S = cap * (size_t)ms;
-  const size_t outBytes[18] = {4 * cap, 4 * cap, 4 * cap, 4 * cap, 4 * cap, 4 * cap, 8 * cap,
-                               4 * S, 4 * S, 8 * S, 8 * S,
-                               s->spec.pr ? 48 * S : 0, s->spec.pr ? 288 * S : 0,
-                               s->spec.fi ? 48 * S : 0, s->spec.fi ? 288 * S : 0,
-                               s->spec.sm ? 48 * S : 0, s->spec.sm ? 288 * S : 0,
-                               s->spec.jac ? 288 * S : 0};
   size_t pout = 0;
   for (int i = 0; i < 18; ++i) {
-    if (outBytes[i] == 0) continue;
-    if ((e = sl.dout[i].ensure(outBytes[i])) != cudaSuccess) return cudaFail(e, "server output");
-    pout += (outBytes[i] + 255) & ~(size_t)255;
+    if (!s->computes(i)) continue;
+    const size_t bytes = kOutElem[i] * kOutComp[i] * (kPerState[i] ? S : cap);
+    if ((e = sl.dout[i].ensure(bytes)) != cudaSuccess) return cudaFail(e, "server output");
+    pout += (bytes + 255) & ~(size_t)255;
   }
-  if ((e = cudaMallocHost(&sl.pinIn, pin)) != cudaSuccess ||
+  if ((e = sl.table.ensure(sizeof(int4) * kMaxEventsPerBatch)) != cudaSuccess)
+    return cudaFail(e, "server table");
+  if ((e = cudaMallocHost((void**)&sl.pinTable, sizeof(int4) * kMaxEventsPerBatch)) !=
+          cudaSuccess ||
       (e = cudaMallocHost(&sl.pinOut, pout)) != cudaSuccess)
     return cudaFail(e, "server pinned buffers");
-  sl.pinInBytes = pin;
   sl.pinOutBytes = pout;
-  ck_status st = preparePipeline(s->h, sl.ctx, s->capacity, ms, s->opt.precision);
-  return st;
+  return preparePipeline(s->h, sl.ctx, s->capacity, ms, s->opt.precision);
 }
 
-// Concatenates the slot's events into its pinned buffer and launches the
-// copies and the fit on the slot's stream.
+// Offsets of the staged result arrays in the slot's pinned buffer.
+void stagedBases(ck_server* s, Slot& sl, size_t base[18]) {
+  const size_t n = (size_t)sl.nTracks, S = n * (size_t)s->cfg.max_states;
+  size_t off = 0;
+  for (int i = 0; i < 18; ++i) {
+    base[i] = off;
+    if (!s->computes(i)) continue;
+    off += (kOutElem[i] * kOutComp[i] * (kPerState[i] ? S : n) + 255) & ~(size_t)255;
+  }
+}
+
+// Copies the co-batch's inputs, launches the fit and the result copies on the
+// slot's stream.
 ck_status launchSlot(ck_server* s, Slot& sl) {
   const int n = sl.nTracks;
-  // host staging: concatenate the events with shifted offsets
-  std::vector<int32_t> so(1, 0), mo(1, 0), seq, msf, pdg;
-  std::vector<double> mv, mc, sp, sc, fr;
-  std::vector<float> pa;
-  for (auto& ev : sl.events) {
-    const int sBase = so.back(), mBase = mo.back();
-    for (int t = 0; t < ev->n; ++t) {
-      so.push_back(sBase + ev->seqOff[t + 1]);
-      mo.push_back(mBase + ev->measOff[t + 1]);
-    }
-    seq.insert(seq.end(), ev->seq.begin(), ev->seq.end());
-    msf.insert(msf.end(), ev->measSurf.begin(), ev->measSurf.end());
-    mv.insert(mv.end(), ev->measVal.begin(), ev->measVal.end());
-    mc.insert(mc.end(), ev->measCov.begin(), ev->measCov.end());
-    sp.insert(sp.end(), ev->sp.begin(), ev->sp.end());
-    sc.insert(sc.end(), ev->sc.begin(), ev->sc.end());
-    fr.insert(fr.end(), ev->frames.begin(), ev->frames.end());
-    pa.insert(pa.end(), ev->part.begin(), ev->part.end());
-    pdg.insert(pdg.end(), ev->pdg.begin(), ev->pdg.end());
-  }
-  const void* srcs[11] = {so.data(), seq.data(), mo.data(), msf.data(), mv.data(), mc.data(),
-                          sp.data(), sc.data(),  fr.data(), pa.data(),  pdg.data()};
-  const size_t bytes[11] = {4 * so.size(), 4 * seq.size(), 4 * mo.size(), 4 * msf.size(),
-                            8 * mv.size(), 8 * mc.size(),  8 * sp.size(), 8 * sc.size(),
-                            8 * fr.size(), 4 * pa.size(),  4 * pdg.size()};
-  // the pinned staging buffer holds exactly the planned sizes
-  for (int i = 0; i < 11; ++i)
-    if (bytes[i] > sl.inPlanned[i]) return fail(CK_ERR_BUDGET, "co-batch exceeds slot buffers");
-  char* pin = (char*)sl.pinIn;
-  size_t off = 0;
+  const int nEv = (int)sl.events.size();
   cudaError_t e;
-  for (int i = 0; i < 11; ++i) {
-    std::memcpy(pin + off, srcs[i], bytes[i]);
-    if (bytes[i] &&
-        (e = cudaMemcpyAsync(sl.din[i].p, pin + off, bytes[i], cudaMemcpyHostToDevice,
-                             sl.stream)) != cudaSuccess)
-      return cudaFail(e, "server input copy");
-    off += (bytes[i] + 255) & ~(size_t)255;
+  // ---- inputs, straight from the callers' arrays
+  int t0 = 0, seqBase = 0, measBase = 0, maxM = 1;
+  for (int i = 0; i < nEv; ++i) {
+    Event& ev = *sl.events[i];
+    const ck_batch_in& in = ev.in;
+    const int m = ev.n;
+    sl.pinTable[4 * i + 0] = t0;
+    sl.pinTable[4 * i + 1] = m;
+    sl.pinTable[4 * i + 2] = seqBase;
+    sl.pinTable[4 * i + 3] = measBase;
+    maxM = std::max(maxM, m + 1);
+    const bool last = (i == nEv - 1);
+    struct Item {
+      int buf;
+      const void* src;
+      size_t dstOff, bytes;
+    } items[] = {
+        {0, in.seq_offsets, 4 * (size_t)t0, 4 * (size_t)(m + (last ? 1 : 0))},
+        {1, in.seq_surfaces, 4 * (size_t)seqBase, 4 * (size_t)ev.nSeq},
+        {2, in.meas_offsets, 4 * (size_t)t0, 4 * (size_t)(m + (last ? 1 : 0))},
+        {3, in.meas_surfaces, 4 * (size_t)measBase, 4 * (size_t)ev.nMeas},
+        {4, in.meas_values, 16 * (size_t)measBase, 16 * (size_t)ev.nMeas},
+        {5, in.meas_cov, 32 * (size_t)measBase, 32 * (size_t)ev.nMeas},
+        {6, in.start_params, 48 * (size_t)t0, 48 * (size_t)m},
+        {7, in.start_cov, 288 * (size_t)t0, 288 * (size_t)m},
+        {8, in.start_frames, 96 * (size_t)t0, 96 * (size_t)m},
+        {9, in.particle, 8 * (size_t)t0, 8 * (size_t)m},
+        {10, in.particle_pdg, 4 * (size_t)t0, 4 * (size_t)m},
+    };
+    for (const Item& it : items) {
+      if (!it.bytes) continue;
+      if (it.dstOff + it.bytes > sl.inPlanned[it.buf])
+        return fail(CK_ERR_BUDGET, "co-batch exceeds slot buffers");
+      char* dst = (char*)sl.din[it.buf].p + it.dstOff;
+      if (it.buf == 10 && !it.src) {
+        fillInt<<<(m + 255) / 256, 256, 0, sl.stream>>>((int32_t*)dst, m, 211);
+        continue;
+      }
+      if ((e = cudaMemcpyAsync(dst, it.src, it.bytes, cudaMemcpyDefault, sl.stream)) !=
+          cudaSuccess)
+        return cudaFail(e, "server input copy");
+    }
+    t0 += m;
+    seqBase += ev.nSeq;
+    measBase += ev.nMeas;
+  }
+  if ((e = cudaMemcpyAsync(sl.table.p, sl.pinTable, sizeof(int4) * nEv, cudaMemcpyHostToDevice,
+                           sl.stream)) != cudaSuccess)
+    return cudaFail(e, "server table copy");
+  {
+    dim3 grid((unsigned)std::min(64, (maxM + 255) / 256), (unsigned)nEv);
+    shiftOffsets<<<grid, 256, 0, sl.stream>>>((int32_t*)sl.din[0].p, (int32_t*)sl.din[2].p,
+                                              (const int4*)sl.table.p, nEv);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cudaFail(e, "offset shift");
   }
   ck_batch_in din{};
   din.n_tracks = n;
@@ -209,15 +284,8 @@ ck_status launchSlot(ck_server* s, Slot& sl) {
   ck_batch_out dout{};
   dout.max_states = s->cfg.max_states;
   dout.memory = CK_MEM_DEVICE;
-  void** f[18] = {(void**)&dout.status,          (void**)&dout.n_states,
-                  (void**)&dout.n_measurements,  (void**)&dout.n_holes,
-                  (void**)&dout.n_outliers,      (void**)&dout.ndf,
-                  (void**)&dout.chi2_sum,        (void**)&dout.state_surface,
-                  (void**)&dout.state_flags,     (void**)&dout.state_path_length,
-                  (void**)&dout.state_chi2,      (void**)&dout.predicted,
-                  (void**)&dout.predicted_cov,   (void**)&dout.filtered,
-                  (void**)&dout.filtered_cov,    (void**)&dout.smoothed,
-                  (void**)&dout.smoothed_cov,    (void**)&dout.jacobian};
+  void** f[18];
+  outFields(dout, f);
   for (int i = 0; i < 18; ++i) *f[i] = sl.dout[i].cap ? sl.dout[i].p : nullptr;
   ck_status st;
   {
@@ -227,85 +295,98 @@ ck_status launchSlot(ck_server* s, Slot& sl) {
                          s->gridBlocks);
   }
   if (st != CK_OK) return st;
-  // results back to the pinned buffer
+  // ---- results
   const int ms = s->cfg.max_states;
-  const size_t S = (size_t)n * ms;
-  const size_t ob[18] = {4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n,
-                         4 * (size_t)n, 8 * (size_t)n, 4 * S, 4 * S, 8 * S, 8 * S, 48 * S, 288 * S,
-                         48 * S, 288 * S, 48 * S, 288 * S, 288 * S};
-  char* po = (char*)sl.pinOut;
-  off = 0;
-  for (int i = 0; i < 18; ++i) {
-    if (!sl.dout[i].cap) continue;
-    if ((e = cudaMemcpyAsync(po + off, sl.dout[i].p, ob[i], cudaMemcpyDeviceToHost,
-                             sl.stream)) != cudaSuccess)
-      return cudaFail(e, "server output copy");
-    off += (ob[i] + 255) & ~(size_t)255;
+  bool anyStaged = false;
+  t0 = 0;
+  for (auto& evp : sl.events) {
+    Event& ev = *evp;
+    const int m = ev.n;
+    if (ev.staged) {
+      anyStaged = true;
+    } else {
+      ck_batch_out o = ev.out;
+      void** g[18];
+      outFields(o, g);
+      for (int i = 0; i < 18; ++i) {
+        if (!*g[i] || !sl.dout[i].cap) continue;
+        const size_t el = kOutElem[i];
+        const char* src = (const char*)sl.dout[i].p + el * t0;
+        if (!kPerState[i])
+          e = cudaMemcpyAsync(*g[i], src, el * m, cudaMemcpyDefault, sl.stream);
+        else
+          e = cudaMemcpy2DAsync(*g[i], el * m, src, el * n, el * m, (size_t)ms * kOutComp[i],
+                                cudaMemcpyDefault, sl.stream);
+        if (e != cudaSuccess) return cudaFail(e, "server result copy");
+      }
+    }
+    t0 += m;
+  }
+  if (anyStaged) {
+    size_t base[18];
+    stagedBases(s, sl, base);
+    const size_t S = (size_t)n * ms;
+    for (int i = 0; i < 18; ++i) {
+      if (!sl.dout[i].cap) continue;
+      const size_t bytes = kOutElem[i] * kOutComp[i] * (kPerState[i] ? S : (size_t)n);
+      if ((e = cudaMemcpyAsync((char*)sl.pinOut + base[i], sl.dout[i].p, bytes,
+                               cudaMemcpyDeviceToHost, sl.stream)) != cudaSuccess)
+        return cudaFail(e, "server staged copy");
+    }
   }
   if ((e = cudaEventRecord(sl.done, sl.stream)) != cudaSuccess) return cudaFail(e, "event");
   return CK_OK;
 }
 
-// Splits a finished slot's results into its events (SoA with the co-batch's
-// track count innermost -> each event's own SoA).
+// Completes a finished slot: host copies of the staged events' results.
 void harvestSlot(ck_server* s, Slot& sl) {
   const int n = sl.nTracks, ms = s->cfg.max_states;
-  const size_t S = (size_t)n * ms;
-  const size_t ob[18] = {4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n,
-                         4 * (size_t)n, 8 * (size_t)n, 4 * S, 4 * S, 8 * S, 8 * S, 48 * S, 288 * S,
-                         48 * S, 288 * S, 48 * S, 288 * S, 288 * S};
-  const char* po = (const char*)sl.pinOut;
-  const char* base[18];
-  size_t off = 0;
-  for (int i = 0; i < 18; ++i) {
-    base[i] = nullptr;
-    if (!sl.dout[i].cap) continue;
-    base[i] = po + off;
-    off += (ob[i] + 255) & ~(size_t)255;
-  }
-  const auto now = Clock::now();
+  size_t base[18];
+  stagedBases(s, sl, base);
   int t0 = 0;
-  for (auto& ev : sl.events) {
-    const int m = ev->n;
-    auto per = [&](int i, auto& v) {
-      using T = typename std::remove_reference<decltype(v)>::type::value_type;
-      v.assign((const T*)base[i] + t0, (const T*)base[i] + t0 + m);
-    };
-    per(0, ev->status);
-    per(1, ev->nStates);
-    per(2, ev->nMeas);
-    per(3, ev->nHoles);
-    per(4, ev->nOut);
-    per(5, ev->ndf);
-    per(6, ev->chi2);
-    auto soa = [&](int i, int C, auto& v) {
-      using T = typename std::remove_reference<decltype(v)>::type::value_type;
-      if (!base[i]) return;
-      const T* src = (const T*)base[i];
-      v.resize((size_t)ms * C * m);
-      for (int k = 0; k < ms; ++k)
-        for (int c = 0; c < C; ++c)
-          std::memcpy(&v[((size_t)k * C + c) * m], src + ((size_t)k * C + c) * n + t0,
-                      sizeof(T) * m);
-    };
-    soa(7, 1, ev->surf);
-    soa(8, 1, ev->flags);
-    soa(9, 1, ev->path);
-    soa(10, 1, ev->schi2);
-    soa(11, 6, ev->pr);
-    soa(12, 36, ev->prc);
-    soa(13, 6, ev->fi);
-    soa(14, 36, ev->fic);
-    soa(15, 6, ev->sm);
-    soa(16, 36, ev->smc);
-    soa(17, 36, ev->jac);
-    ev->latencyMs = std::chrono::duration<double, std::milli>(now - ev->submitted).count();
+  for (auto& evp : sl.events) {
+    Event& ev = *evp;
+    const int m = ev.n;
+    if (ev.staged) {
+      ck_batch_out o = ev.out;
+      void** g[18];
+      outFields(o, g);
+      for (int i = 0; i < 18; ++i) {
+        if (!*g[i] || !sl.dout[i].cap) continue;
+        const size_t el = kOutElem[i];
+        const char* src = (const char*)sl.pinOut + base[i] + el * t0;
+        char* dst = (char*)*g[i];
+        const int rows = kPerState[i] ? ms * kOutComp[i] : 1;
+        for (int r = 0; r < rows; ++r)
+          std::memcpy(dst + el * m * (size_t)r, src + el * n * (size_t)r, el * m);
+      }
+    }
+    ev.latencyMs = std::chrono::duration<double, std::milli>(Clock::now() - ev.submitted).count();
     t0 += m;
   }
 }
 
+void finishSlot(ck_server* s, Slot& sl, ck_status st) {
+  for (auto& ev : sl.events) {
+    if (st != CK_OK) {
+      ev->status = st;
+      ev->latencyMs =
+          std::chrono::duration<double, std::milli>(Clock::now() - ev->submitted).count();
+    }
+    s->tracksDone += ev->n;
+    ++s->completed;
+    s->finished.push_back(std::move(ev));
+  }
+  sl.events.clear();
+  s->bytesInUse -= (size_t)sl.nTracks * s->perTrackBytes(s->cfg.max_states);
+  sl.nTracks = sl.nSeq = sl.nMeas = 0;
+  sl.busy = false;
+  s->cvDone.notify_all();
+}
+
 void workerLoop(ck_server* s) {
   cudaSetDevice(s->h->device);
+  const size_t planned = (size_t)kPlannedSurfacesPerTrack * (size_t)s->capacity;
   std::unique_lock<std::mutex> lock(s->mu);
   while (true) {
     // completion of in-flight slots
@@ -314,35 +395,39 @@ void workerLoop(ck_server* s) {
       if (!sl.busy) continue;
       cudaError_t q = cudaEventQuery(sl.done);
       if (q == cudaErrorNotReady) continue;
+      ck_status st = CK_OK;
       if (q != cudaSuccess) {
-        s->error = cudaFail(q, "server batch");
+        st = cudaFail(q, "server batch");
+        s->error = st;
         s->errorMsg = g_lastError;
       } else {
+        lock.unlock();
         harvestSlot(s, sl);
+        lock.lock();
       }
-      for (auto& ev : sl.events) {
-        s->tracksDone += ev->n;
-        ++s->completed;
-        s->finished.push_back(std::move(ev));
-      }
-      sl.events.clear();
-      s->bytesInUse -= (size_t)sl.nTracks * s->perTrackBytes(s->cfg.max_states);
-      sl.nTracks = 0;
-      sl.busy = false;
-      s->cvDone.notify_all();
+      finishSlot(s, sl, st);
     }
     // admission into free slots: co-batch the oldest pending events
     for (auto& slp : s->slots) {
       Slot& sl = *slp;
       if (sl.busy || s->pending.empty()) continue;
       int n = 0;
-      while (!s->pending.empty() && n + s->pending.front()->n <= s->capacity) {
-        n += s->pending.front()->n;
+      size_t nSeq = 0, nMeas = 0;
+      while (!s->pending.empty() && (int)sl.events.size() < kMaxEventsPerBatch) {
+        const Event& ev = *s->pending.front();
+        if (n + ev.n > s->capacity || nSeq + ev.nSeq > planned || nMeas + ev.nMeas > planned)
+          break;
+        n += ev.n;
+        nSeq += ev.nSeq;
+        nMeas += ev.nMeas;
         sl.events.push_back(std::move(s->pending.front()));
         s->pending.pop_front();
       }
       if (sl.events.empty()) continue;
       sl.nTracks = n;
+      sl.nSeq = (int)nSeq;
+      sl.nMeas = (int)nMeas;
+      sl.busy = true;
       s->bytesInUse += (size_t)n * s->perTrackBytes(s->cfg.max_states);
       lock.unlock();
       ck_status st = launchSlot(s, sl);
@@ -350,18 +435,9 @@ void workerLoop(ck_server* s) {
       if (st != CK_OK) {
         s->error = st;
         s->errorMsg = g_lastError;
-        for (auto& ev : sl.events) {
-          ev->status.assign(ev->n, CK_TRACK_NOT_PROCESSED);
-          ++s->completed;
-          s->finished.push_back(std::move(ev));
-        }
-        sl.events.clear();
-        s->bytesInUse -= (size_t)n * s->perTrackBytes(s->cfg.max_states);
-        sl.nTracks = 0;
-        s->cvDone.notify_all();
-        continue;
+        cudaStreamSynchronize(sl.stream);
+        finishSlot(s, sl, st);
       }
-      sl.busy = true;
     }
     bool anyBusy = false;
     for (auto& slp : s->slots) anyBusy |= slp->busy;
@@ -373,6 +449,15 @@ void workerLoop(ck_server* s) {
       s->cvWork.wait(lock, [&] { return s->stop || !s->pending.empty(); });
     }
   }
+}
+
+ck_status readCount(const int32_t* offsets, int n, int memory, int* out) {
+  if (memory == CK_MEM_HOST) {
+    *out = offsets[n];
+    return CK_OK;
+  }
+  cudaError_t e = cudaMemcpy(out, offsets + n, sizeof(int32_t), cudaMemcpyDefault);
+  return e == cudaSuccess ? CK_OK : cudaFail(e, "event size");
 }
 
 }  // namespace
@@ -395,11 +480,12 @@ ck_status ck_server_create(ck_handle* h, const ck_options* opt, const ck_server_
   s->spec = {(cfg->components & CK_OUT_SMOOTHED) != 0, (cfg->components & CK_OUT_FILTERED) != 0,
              (cfg->components & CK_OUT_PREDICTED) != 0, (cfg->components & CK_OUT_JACOBIAN) != 0};
   s->tune = h->tune[opt->precision];
-  // each stream gets an equal share of the resident blocks
-  s->gridBlocks = std::max(1, gridBlocksFor(h, s->tune) / cfg->n_streams);
+  // every co-batch is launched over the whole GPU: alone it has every SM;
+  // launches on the other streams start their blocks on the SMs that the
+  // running batch's blocks leave as its work queue drains
+  s->gridBlocks = std::max(1, gridBlocksFor(h, s->tune));
   const size_t perTrack = s->perTrackBytes(cfg->max_states);
-  const int64_t avail = cfg->memory_budget_bytes;
-  int64_t cap = avail / (int64_t)(perTrack * cfg->n_streams);
+  int64_t cap = cfg->memory_budget_bytes / (int64_t)(perTrack * cfg->n_streams);
   cap = std::min<int64_t>(cap, cfg->max_batch_tracks);
   if (cap < 1) return fail(CK_ERR_BUDGET, "budget too small for one track per stream");
   s->capacity = (int)cap;
@@ -417,44 +503,68 @@ ck_status ck_server_create(ck_handle* h, const ck_options* opt, const ck_server_
   return CK_OK;
 }
 
-ck_status ck_server_submit(ck_server* s, int64_t event_id, const ck_batch_in* in) {
-  if (!s || !in || in->n_tracks < 0 || in->memory != CK_MEM_HOST)
-    return fail(CK_ERR_INVALID_ARGUMENT, "bad event (host memory required)");
+ck_status ck_server_submit(ck_server* s, int64_t event_id, const ck_batch_in* in,
+                           const ck_batch_out* results) {
+  if (!s || !in || !results || in->n_tracks < 0)
+    return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument or negative track count");
   const int n = in->n_tracks;
   if (n > s->capacity) return fail(CK_ERR_BUDGET, "event larger than a stream's capacity");
+  if (results->max_states != s->cfg.max_states)
+    return fail(CK_ERR_INVALID_ARGUMENT, "results.max_states differs from the server's");
+  if (!results->status) return fail(CK_ERR_INVALID_ARGUMENT, "status array is required");
+  {
+    ck_batch_out o = *results;
+    void** g[18];
+    outFields(o, g);
+    for (int i = 0; i < 18; ++i)
+      if (*g[i] && !s->computes(i))
+        return fail(CK_ERR_INVALID_ARGUMENT, "results ask for a component the server omits");
+  }
+  if (n > 0 && (!in->seq_offsets || !in->seq_surfaces || !in->meas_offsets ||
+                !in->meas_surfaces || !in->meas_values || !in->meas_cov || !in->start_params ||
+                !in->start_cov || !in->start_frames || !in->particle))
+    return fail(CK_ERR_INVALID_ARGUMENT, "input array missing");
   auto ev = std::make_unique<Event>();
   ev->id = event_id;
   ev->n = n;
-  const int nSeq = in->seq_offsets[n], nMeas = in->meas_offsets[n];
-  if (nSeq > 20 * n || nMeas > 20 * n)
-    return fail(CK_ERR_INVALID_ARGUMENT, "more than 20 surfaces per track on average");
-  ev->seqOff.assign(in->seq_offsets, in->seq_offsets + n + 1);
-  ev->seq.assign(in->seq_surfaces, in->seq_surfaces + nSeq);
-  ev->measOff.assign(in->meas_offsets, in->meas_offsets + n + 1);
-  ev->measSurf.assign(in->meas_surfaces, in->meas_surfaces + nMeas);
-  ev->measVal.assign(in->meas_values, in->meas_values + 2 * (size_t)nMeas);
-  ev->measCov.assign(in->meas_cov, in->meas_cov + 4 * (size_t)nMeas);
-  ev->sp.assign(in->start_params, in->start_params + 6 * (size_t)n);
-  ev->sc.assign(in->start_cov, in->start_cov + 36 * (size_t)n);
-  ev->frames.assign(in->start_frames, in->start_frames + 12 * (size_t)n);
-  ev->part.assign(in->particle, in->particle + 2 * (size_t)n);
-  if (in->particle_pdg)
-    ev->pdg.assign(in->particle_pdg, in->particle_pdg + n);
-  else
-    ev->pdg.assign(n, 211);
+  ev->in = *in;
+  ev->out = *results;
+  if (n > 0) {
+    if (in->memory == CK_MEM_HOST && (in->seq_offsets[0] != 0 || in->meas_offsets[0] != 0))
+      return fail(CK_ERR_INVALID_ARGUMENT, "CSR offsets must start at 0");
+    ck_status st;
+    if ((st = readCount(in->seq_offsets, n, in->memory, &ev->nSeq)) != CK_OK ||
+        (st = readCount(in->meas_offsets, n, in->memory, &ev->nMeas)) != CK_OK)
+      return st;
+  }
+  const size_t planned = (size_t)kPlannedSurfacesPerTrack * (size_t)s->capacity;
+  if (ev->nSeq < 0 || ev->nMeas < 0 || (size_t)ev->nSeq > planned || (size_t)ev->nMeas > planned)
+    return fail(CK_ERR_BUDGET, "event exceeds the planned surfaces of a stream");
+  if (results->memory == CK_MEM_HOST) {
+    cudaPointerAttributes a{};
+    ev->staged = cudaPointerGetAttributes(&a, results->status) != cudaSuccess ||
+                 a.type == cudaMemoryTypeUnregistered;
+    cudaGetLastError();
+  }
   ev->submitted = Clock::now();
   {
     std::lock_guard<std::mutex> lock(s->mu);
     if (s->stop) return fail(CK_ERR_INVALID_ARGUMENT, "server stopping");
-    s->pending.push_back(std::move(ev));
     ++s->submitted;
+    if (n == 0) {
+      ++s->completed;
+      s->finished.push_back(std::move(ev));
+      s->cvDone.notify_all();
+      return CK_OK;
+    }
+    s->pending.push_back(std::move(ev));
   }
   s->cvWork.notify_one();
   return CK_OK;
 }
 
-ck_status ck_server_poll(ck_server* s, int64_t* event_id, ck_batch_out* out,
-                         int32_t out_capacity_tracks, double* latency_ms, int32_t timeout_ms) {
+ck_status ck_server_poll(ck_server* s, int64_t* event_id, double* latency_ms,
+                         int32_t timeout_ms) {
   if (!s || !event_id) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
   std::unique_ptr<Event> ev;
   {
@@ -463,39 +573,12 @@ ck_status ck_server_poll(ck_server* s, int64_t* event_id, ck_batch_out* out,
       s->cvDone.wait_for(lock, std::chrono::milliseconds(timeout_ms),
                          [&] { return !s->finished.empty(); });
     if (s->finished.empty()) return fail(CK_ERR_NOT_READY, "no finished event");
-    if (out && s->finished.front()->n > out_capacity_tracks)
-      return fail(CK_ERR_INVALID_ARGUMENT, "output capacity smaller than the event");
     ev = std::move(s->finished.front());
     s->finished.pop_front();
   }
   *event_id = ev->id;
   if (latency_ms) *latency_ms = ev->latencyMs;
-  if (out) {
-    const int m = ev->n, ms = s->cfg.max_states;
-    if (out->max_states != ms) return fail(CK_ERR_INVALID_ARGUMENT, "max_states mismatch");
-    auto cp = [](auto* dst, const auto& v) {
-      if (dst && !v.empty()) std::memcpy(dst, v.data(), v.size() * sizeof(v[0]));
-    };
-    cp(out->status, ev->status);
-    cp(out->n_states, ev->nStates);
-    cp(out->n_measurements, ev->nMeas);
-    cp(out->n_holes, ev->nHoles);
-    cp(out->n_outliers, ev->nOut);
-    cp(out->ndf, ev->ndf);
-    cp(out->chi2_sum, ev->chi2);
-    cp(out->state_surface, ev->surf);
-    cp(out->state_flags, ev->flags);
-    cp(out->state_path_length, ev->path);
-    cp(out->state_chi2, ev->schi2);
-    cp(out->smoothed, ev->sm);
-    cp(out->smoothed_cov, ev->smc);
-    cp(out->filtered, ev->fi);
-    cp(out->filtered_cov, ev->fic);
-    cp(out->predicted, ev->pr);
-    cp(out->predicted_cov, ev->prc);
-    cp(out->jacobian, ev->jac);
-    (void)m;
-  }
+  if (ev->status != CK_OK) return fail(ev->status, "the event's batch failed");
   return CK_OK;
 }
 
@@ -530,8 +613,9 @@ ck_status ck_server_destroy(ck_server* s) {
     if (sl.stream) cudaStreamSynchronize(sl.stream);
     for (auto& b : sl.din) b.release();
     for (auto& b : sl.dout) b.release();
+    sl.table.release();
     sl.ctx.release();
-    if (sl.pinIn) cudaFreeHost(sl.pinIn);
+    if (sl.pinTable) cudaFreeHost(sl.pinTable);
     if (sl.pinOut) cudaFreeHost(sl.pinOut);
     if (sl.done) cudaEventDestroy(sl.done);
     if (sl.stream) cudaStreamDestroy(sl.stream);

@@ -63,3 +63,59 @@ class Results:
         """States 0..n_states-1 of track t for array `name`."""
         v = self.view(name)
         return v[t, : self.n_states[t]]
+
+
+class TorchResults:
+    """Result buffers as torch tensors in device memory (device="cuda:0") or
+    page-locked host memory (device="pinned"), in the ck_batch_out layout;
+    to_host() copies them into a Results."""
+
+    _SPEC = (("status", 1, "int32"), ("n_states", 1, "int32"), ("n_measurements", 1, "int32"),
+             ("n_holes", 1, "int32"), ("n_outliers", 1, "int32"), ("ndf", 1, "int32"),
+             ("chi2_sum", 1, "float64"), ("state_surface", -1, "int32"),
+             ("state_flags", -1, "int32"), ("state_path_length", -1, "float64"),
+             ("state_chi2", -1, "float64"), ("predicted", -6, "float64"),
+             ("predicted_cov", -36, "float64"), ("filtered", -6, "float64"),
+             ("filtered_cov", -36, "float64"), ("smoothed", -6, "float64"),
+             ("smoothed_cov", -36, "float64"), ("jacobian", -36, "float64"))
+    _COMP = {"predicted": abi.OUT_PREDICTED, "predicted_cov": abi.OUT_PREDICTED,
+             "filtered": abi.OUT_FILTERED, "filtered_cov": abi.OUT_FILTERED,
+             "smoothed": abi.OUT_SMOOTHED, "smoothed_cov": abi.OUT_SMOOTHED,
+             "jacobian": abi.OUT_JACOBIAN}
+
+    def __init__(self, n, max_states=24, components=abi.OUT_SMOOTHED, device="cuda:0"):
+        import torch
+
+        self.n = n
+        self.max_states = max_states
+        self.components = components
+        self.pinned = device == "pinned"
+        self.tensors = {}
+        for name, per, dt in self._SPEC:
+            if name in self._COMP and not components & self._COMP[name]:
+                continue
+            size = n * (per if per > 0 else -per * max_states)
+            dtype = getattr(torch, dt)
+            if self.pinned:
+                t = torch.empty(size, dtype=dtype).pin_memory()
+            else:
+                t = torch.empty(size, dtype=dtype, device=device)
+            self.tensors[name] = t
+
+    def as_batch_out(self):
+        o = abi.ck_batch_out()
+        o.max_states = self.max_states
+        o.components = self.components
+        o.memory = abi.MEM_HOST if self.pinned else abi.MEM_DEVICE
+        for name, t in self.tensors.items():
+            ct = C.c_double if t.element_size() == 8 else (
+                C.c_uint32 if name == "state_flags" else C.c_int32)
+            setattr(o, name, C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ct)))
+        return o
+
+    def to_host(self):
+        r = Results(self.n, self.max_states, self.components)
+        for name, t in self.tensors.items():
+            a = t.cpu().numpy()
+            getattr(r, name)[:] = a.view(getattr(r, name).dtype)
+        return r

@@ -466,7 +466,7 @@ def native_arm(args):
     cpu = cpu_baseline(det, b, forms["fp64"], budget_s=10.0)
     fit.close()
     del keep_in, keep_out, keep_hin, keep_hout
-    serving = serving_report() if args.serving else None
+    serving = serving_report(torch) if args.serving else None
     mixed = results["mixed"]
     line = {"metric": "tracks/s fitted (FP64 vs mixed, same accuracy); p50/p99 event latency",
             "value": round(mixed["tracks_per_s"], 1), "unit": "tracks/s", "n_gpus": world,
@@ -497,33 +497,76 @@ def native_arm(args):
     return 0
 
 
-def serving_report(precisions=("mixed", "fp64"), event_tracks=10000, pool=12, seed=77):
+class PinnedBatch:
+    """A Batch's input arrays copied to page-locked host memory."""
+
+    def __init__(self, b, torch):
+        self.n = b.n
+        self._keep = {}
+        self._src = b
+
+    def pin(self, torch):
+        from acts_gb300 import abi
+
+        bi = abi.ck_batch_in()
+        bi.n_tracks = self.n
+        bi.memory = abi.MEM_HOST
+        for name, ct in (("seq_offsets", C.c_int32), ("seq_surfaces", C.c_int32),
+                         ("meas_offsets", C.c_int32), ("meas_surfaces", C.c_int32),
+                         ("meas_values", C.c_double), ("meas_cov", C.c_double),
+                         ("start_params", C.c_double), ("start_cov", C.c_double),
+                         ("start_frames", C.c_double), ("particle", C.c_float),
+                         ("particle_pdg", C.c_int32)):
+            t = torch.from_numpy(getattr(self._src, name)).pin_memory()
+            self._keep[name] = t
+            setattr(bi, name, C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ct)))
+        self._bi = bi
+        return self
+
+    def as_batch_in(self):
+        return self._bi
+
+
+def serving_report(torch, precisions=("mixed", "fp64"), event_tracks=10000, pool=12, seed=77,
+                   max_states=20):
     """Continuous-batching serving loop on 10k-track events of the uneven
     workload (20-cylinder barrel, 4-20 hits, holes, outliers, grid field):
-    capacity measured by saturating the server, then Poisson arrivals at a
-    fraction of that capacity; p50/p99 event latency (submit -> results in
-    host memory) and sustained tracks/s per offered load."""
+    inputs in page-locked host memory, results written into device buffers
+    (and, at one load, into page-locked and into pageable host buffers).
+    Capacity is measured by saturating the server; then Poisson arrivals at
+    fractions of it; p50/p99 event latency (submit -> results in place) and
+    sustained tracks/s per offered load."""
     import threading
 
     from acts_gb300 import abi, generate
     from acts_gb300.fitter import CudaKalman
+    from acts_gb300.results import Results, TorchResults
     from acts_gb300.serving import FitServer
 
     det = generate.Detector(abi.CKG_UNEVEN)
-    events = [generate.generate(det, event_tracks, seed=seed + i, first_track=i * event_tracks)
+    events = [PinnedBatch(generate.generate(det, event_tracks, seed=seed + i,
+                                            first_track=i * event_tracks), torch).pin(torch)
               for i in range(pool)]
     fit = CudaKalman.for_detector(det)
     rng = np.random.default_rng(seed)
+    n_buf = 160
+    dev_results = [TorchResults(event_tracks, max_states, abi.OUT_SMOOTHED, device="cuda:0")
+                   for _ in range(n_buf)]
     report = {"workload": "uneven barrel events of %d tracks (4-20 hits, holes 10 %%, outliers "
-                          "5 %%, grid field), Poisson arrivals" % event_tracks,
-              "memory_budget_gb": 40, "streams": 3}
+                          "5 %%, grid field), Poisson arrivals; inputs in page-locked host "
+                          "memory" % event_tracks,
+              "memory_budget_gb": 40, "streams": 3, "max_states": max_states}
+    # the kernel time of one event alone (whole GPU, device-resident)
+    one = generate.generate(det, event_tracks, seed=seed)
     for name in precisions:
         prec = abi.PRECISION_MIXED if name == "mixed" else abi.PRECISION_FP64
         opt = abi.default_options(precision=prec, outlier_chi2_cut=15.0)
-        srv = FitServer(fit, opt, memory_budget_bytes=40 << 30, n_streams=3, max_states=24,
-                        max_batch_tracks=8 * event_tracks)
+        for _ in range(3):
+            fit.fit_batch(one, opt, max_states=max_states, components=abi.OUT_SMOOTHED)
+        srv = FitServer(fit, opt, memory_budget_bytes=40 << 30, n_streams=3,
+                        max_states=max_states, max_batch_tracks=8 * event_tracks)
 
-        def run(n_events, rate, first_id):
+        def run(n_events, rate, first_id, results_of):
             lat = {}
             done = threading.Event()
 
@@ -545,31 +588,48 @@ def serving_report(precisions=("mixed", "fp64"), event_tracks=10000, pool=12, se
                     dt = t_next - time.perf_counter()
                     if dt <= 0:
                         break
-                    time.sleep(min(dt, 0.002))
-                srv.submit(first_id + i, events[i % pool])
+                    time.sleep(min(dt, 0.001))
+                srv.submit(first_id + i, events[i % pool], results_of(i))
             done.wait(120)
             wall = time.perf_counter() - t0
-            v = np.array(list(lat.values()))
-            return v, wall
+            return np.array(list(lat.values())), wall
 
-        # capacity: everything submitted at once
-        run(2 * pool, 0, 0)  # warm-up
-        v, wall = run(8 * pool, 0, 1000)
-        cap_events = 8 * pool / wall
-        res = {"capacity_tracks_per_s": round(cap_events * event_tracks, 1), "loads": []}
+        on_device = lambda i: dev_results[i % n_buf]
+        run(2 * pool, 0, 0, on_device)  # warm-up
+        n_cap = n_buf
+        v, wall = run(n_cap, 0, 1000, on_device)
+        cap_events = n_cap / wall
+        res = {"capacity_tracks_per_s": round(cap_events * event_tracks, 1),
+               "results": "device memory", "loads": []}
         loads = (0.1, 0.5, 0.8, 1.0, 1.2) if name == "mixed" else (0.5, 1.0)
         nid = 10000
         for f in loads:
             rate = f * cap_events
-            n_ev = int(min(400, max(40, rate * 1.5)))
-            v, wall = run(n_ev, rate, nid)
+            n_ev = int(min(n_buf, max(40, rate * 1.0)))
+            v, wall = run(n_ev, rate, nid, on_device)
             nid += n_ev
             res["loads"].append({"offered_fraction": f, "events": n_ev,
                                  "offered_tracks_per_s": round(rate * event_tracks, 1),
                                  "sustained_tracks_per_s": round(n_ev * event_tracks / wall, 1),
                                  "p50_ms": round(float(np.percentile(v, 50)), 3),
                                  "p99_ms": round(float(np.percentile(v, 99)), 3)})
+        if name == "mixed":
+            # results delivered to host memory at half load
+            pinned = [TorchResults(event_tracks, max_states, abi.OUT_SMOOTHED, device="pinned")
+                      for _ in range(40)]
+            host = [Results(event_tracks, max_states, abi.OUT_SMOOTHED) for _ in range(40)]
+            for label, bufs in (("page-locked host memory", pinned), ("pageable host memory", host)):
+                rate = 0.5 * cap_events
+                v, wall = run(40, rate, nid, lambda i: bufs[i])
+                nid += 40
+                res.setdefault("host_delivery", []).append(
+                    {"results": label, "offered_fraction": 0.5, "events": 40,
+                     "p50_ms": round(float(np.percentile(v, 50)), 3),
+                     "p99_ms": round(float(np.percentile(v, 99)), 3)})
+            del pinned, host
         srv.close()
+        fit.fit_batch(one, opt, max_states=max_states, components=abi.OUT_SMOOTHED)
+        res["kernel_ms_one_event_whole_gpu"] = round(fit.last_kernel_ms(), 3)
         report[name] = res
     fit.close()
     return report

@@ -436,16 +436,21 @@ typedef struct ck_server_config {
 
 ck_status ck_server_create(ck_handle* h, const ck_options* opt,
                            const ck_server_config* cfg, ck_server** out);
-/* Queues one event (host memory; the input is copied before return).
- * Returns CK_ERR_BUDGET when the event alone exceeds the budget. */
+/* Queues one event. `event` (its inputs) and `results` (its output arrays,
+ * laid out as ck_batch_out for event->n_tracks tracks with the server's
+ * max_states; only components the server computes) stay owned by the
+ * caller and must stay valid until ck_server_poll has returned the event;
+ * nothing is copied at submission. Either may be in host memory (pageable
+ * or page-locked) or device memory: results are copied straight into
+ * `results` (pageable host results through a page-locked staging buffer).
+ * Returns CK_ERR_BUDGET when the event alone exceeds a stream's capacity. */
 ck_status ck_server_submit(ck_server* s, int64_t event_id,
-                           const ck_batch_in* event);
-/* Pops one finished event: its id, the per-track outputs copied into `out`
- * (host memory, sized for the event) and its latency in ms (submit to
- * completion). CK_ERR_NOT_READY when none has finished; waits up to
- * timeout_ms. */
-ck_status ck_server_poll(ck_server* s, int64_t* event_id, ck_batch_out* out,
-                         int32_t out_capacity_tracks, double* latency_ms,
+                           const ck_batch_in* event, const ck_batch_out* results);
+/* Pops one finished event: its id and latency in ms (submit until its
+ * results are in place). CK_ERR_NOT_READY when none has finished within
+ * timeout_ms; another status when the event's batch failed (its results are
+ * then not written). */
+ck_status ck_server_poll(ck_server* s, int64_t* event_id, double* latency_ms,
                          int32_t timeout_ms);
 /* Counters: events submitted, completed, tracks completed, bytes in use. */
 ck_status ck_server_stats(ck_server* s, int64_t* submitted, int64_t* completed,

@@ -44,3 +44,31 @@ def test_fp64_parity(fitter_factory, name, preset, n, kw, min_ok):
     print(name, rep)
     assert rep["n_ok"] >= min_ok * n
     assert_parity(rep, RTOL)
+
+
+# every forward-filter kernel variant: per-warp phase scheduling with the
+# three register caps, block-level phase compaction with 256 and 128 slots
+VARIANTS = [(0, 128, 2), (1, 128, 3), (2, 128, 4), (3, 256, 1), (4, 128, 2)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("variant,tpb,bps", VARIANTS, ids=["v%d" % v[0] for v in VARIANTS])
+def test_fp64_parity_every_kernel_variant(variant, tpb, bps):
+    from acts_gb300.fitter import CudaKalman
+
+    preset = abi.CKG_UNEVEN
+    det = detector(preset)
+    n = 1500
+    b = batch(preset, n, seed=19)
+    opt = abi.default_options(outlier_chi2_cut=15.0)
+    ora = Results(n, 24)
+    kforacle.fit_batch(det, b, opt, ora, n_threads=kforacle.hardware_threads())
+    fit = CudaKalman.for_detector(det)
+    try:
+        fit.set_launch_config(abi.PRECISION_FP64, variant, tpb, bps)
+        gpu = fit.fit_batch(b, opt, max_states=24)
+    finally:
+        fit.close()
+    rep = compare(gpu, ora, RTOL)
+    assert rep["n_ok"] >= 0.5 * n
+    assert_parity(rep, RTOL)

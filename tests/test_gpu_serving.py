@@ -64,6 +64,41 @@ def test_same_result_alone_and_in_mix(fitter_factory, precision):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("where", ["cuda:0", "pinned"])
+def test_results_in_device_and_pinned_buffers(fitter_factory, where):
+    """Results written straight into device or page-locked buffers equal the
+    results of ck_fit_batch on the same events."""
+    from acts_gb300.results import TorchResults
+
+    preset = abi.CKG_UNEVEN
+    det = detector(preset)
+    fit = fitter_factory(preset)
+    opt = abi.default_options(precision=abi.PRECISION_MIXED, outlier_chi2_cut=15.0)
+    evs = _events(det, [700, 1500, 300, 2200], seed=57)
+    srv = FitServer(fit, opt, memory_budget_bytes=2 << 30, n_streams=2, max_states=24,
+                    max_batch_tracks=4000)
+    for i, ev in enumerate(evs):
+        srv.submit(i, ev, TorchResults(ev.n, 24, abi.OUT_SMOOTHED, device=where))
+    got = {}
+    t0 = time.time()
+    while len(got) < len(evs) and time.time() - t0 < 60:
+        r = srv.poll(timeout_ms=200)
+        if r is not None:
+            got[r[0]] = r[1]
+    srv.close()
+    assert len(got) == len(evs)
+    for i, ev in enumerate(evs):
+        res = got[i].to_host()
+        alone = fit.fit_batch(ev, opt, max_states=24, components=abi.OUT_SMOOTHED)
+        assert np.array_equal(res.status, alone.status)
+        assert np.array_equal(res.n_states, alone.n_states)
+        ok = alone.status == 0
+        valid = (np.arange(24)[None, :] < alone.n_states[:, None]) & ok[:, None]
+        for name in ("state_flags", "smoothed", "smoothed_cov"):
+            assert np.array_equal(res.view(name)[valid], alone.view(name)[valid]), (i, name)
+
+
+@pytest.mark.gpu
 def test_oversized_event_rejected(fitter_factory):
     preset = abi.CKG_BARREL
     fit = fitter_factory(preset)
