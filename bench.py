@@ -52,10 +52,9 @@ def log(*a):
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    from acts_gb300 import replicas
+
+    return replicas.env()
 
 
 class ClockSampler:
@@ -114,7 +113,10 @@ def make_workload(n, rank):
     from acts_gb300 import abi, generate
 
     det = generate.Detector(abi.CKG_BARREL)
-    b = generate.generate(det, n, seed=SEED + 1000 * rank, cap=12)
+    from acts_gb300 import replicas
+
+    # replicas: every rank fits its own shard (distinct seeded tracks)
+    b = generate.generate(det, n, seed=replicas.rank_seed(SEED, rank), cap=12)
     return det, b
 
 
@@ -356,6 +358,8 @@ def native_arm(args):
     stream = torch.cuda.Stream(dev)
     sp = C.c_void_p(stream.cuda_stream)
 
+    from acts_gb300 import replicas
+
     forms = {"mixed": abi.default_options(precision=abi.PRECISION_MIXED),
              "fp64": abi.default_options(precision=abi.PRECISION_FP64)}
     results = {}
@@ -383,10 +387,7 @@ def native_arm(args):
         fit.fit_batch_raw(opt, bi, bo, sp)
         torch.cuda.synchronize(dev)
         kernel_ms.append(fit.last_kernel_ms())
-        if world > 1:
-            t = torch.tensor([ms_total], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms_total = float(t.item())
+        ms_total = replicas.max_over_ranks(ms_total)
         status = keep_out["status"].cpu().numpy()
         results[name] = {"ms_per_step": ms_total / args.steps,
                          "tracks_per_s": n * world / (ms_total / args.steps / 1e3),
@@ -421,10 +422,7 @@ def native_arm(args):
     e2e_ms = ev0.elapsed_time(ev1) / args.steps
     h2d, d2h = fit.last_transfer_bytes()
     e2e_launches = fit.last_launch_count()
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = replicas.max_over_ranks(e2e_ms)
 
     if rank != 0:
         fit.close()
