@@ -90,6 +90,9 @@ DevSurface toDevSurface(const ck_surface& s) {
   d.tL0 = (eps < s.mat_l0) ? (s.mat_thickness / s.mat_l0) : 0.0f;
   d.split = s.split_factor;
   d.vacuum = (s.mat_ar > 0.0f) ? 0 : 1;
+  for (int i = 0; i < 9; ++i) d.Rf[i] = (float)s.rotation[i];
+  for (int i = 0; i < 3; ++i) d.cf[i] = (float)s.center[i];
+  d.radiusf = (float)s.radius;
   return d;
 }
 
@@ -212,14 +215,12 @@ cudaError_t launchFit(const FitParams& fp, int precision, const Tune& tn, int gr
 
 int gridBlocksFor(ck_handle* h, const Tune& tn) { return h->smCount * tn.bps; }
 
-size_t recordMatrixElem(int precision) {
-  return precision == CK_PRECISION_MIXED ? sizeof(float) : sizeof(double);
+size_t recordStateBytes(int precision) {
+  return precision == CK_PRECISION_MIXED ? sizeof(RecState<float>) : sizeof(RecState<double>);
 }
 
 size_t recordBytesPerTrack(int maxStates, int precision) {
-  return (size_t)maxStates * (kRecParams * sizeof(double) + kRecMatrix * recordMatrixElem(precision) +
-                              2 * sizeof(int32_t) + 2 * sizeof(double)) +
-         2 * sizeof(int32_t);
+  return (size_t)maxStates * recordStateBytes(precision) + 2 * sizeof(int32_t);
 }
 
 // Allocates (grow-only) the scratch of a batch pipeline: the track-state
@@ -228,11 +229,7 @@ size_t recordBytesPerTrack(int maxStates, int precision) {
 ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, int precision) {
   (void)h;
   cudaError_t e;
-  const size_t recBytes = compBytes(n, maxStates, kRecParams, sizeof(double)) +
-                          compBytes(n, maxStates, kRecMatrix, recordMatrixElem(precision));
-  if ((e = c.rec.ensure(recBytes)) ||
-      (e = c.recMeta.ensure(compBytes(n, maxStates, 2, sizeof(int32_t)))) ||
-      (e = c.recMetaD.ensure(compBytes(n, maxStates, 2, sizeof(double)))) ||
+  if ((e = c.rec.ensure(compBytes(n, maxStates, 1, recordStateBytes(precision)))) ||
       (e = c.perm.ensure((size_t)n * sizeof(int32_t) + 16)) ||
       (e = c.tip.ensure((size_t)n * sizeof(int32_t) + 16)) ||
       (e = c.ticket.ensure(sizeof(int32_t) * (kBins + 1))))
@@ -283,12 +280,8 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
   fp.pdg = din.particle_pdg;
   fp.perm = perm;
   fp.ticket = dTicket;
-  fp.rec = (double*)c.rec.p;
-  fp.rec_mat = (void*)((double*)c.rec.p + (size_t)n * maxStates * kRecParams);
-  fp.rec_meta = (int32_t*)c.recMeta.p;
-  fp.rec_meta_d = (double*)c.recMetaD.p;
+  fp.rec = c.rec.p;
   fp.tip = (int32_t*)c.tip.p;
-  fp.rec_stride = n;
   {
     const long long warps = (long long)grid * (tn.tpb / 32);
     const long long per = warps > 0 ? (n + warps - 1) / warps : 32;
@@ -297,6 +290,7 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
   fp.max_states = maxStates;
   fp.out = dout;
   fp.surfaces = h->dSurfaces;
+  fp.trig = h->dTrig;
   fp.n_surfaces = h->nSurfaces;
   fp.field = h->field;
   fp.mc = h->mc;
@@ -449,6 +443,21 @@ ck_status ck_create(const ck_config* cfg, ck_handle** out) {
       return cudaFail(e, "surface upload");
     }
   }
+  {
+    // (cos, sin) of the reference angles k * kTrigStep, evaluated in long
+    // double for the angle exactly as the kernels form it in double
+    std::vector<double2> tab(kTrigEntries);
+    for (int k = -64; k <= 64; ++k) {
+      const long double a = (long double)((double)k * kTrigStep);
+      tab[k + 64] = make_double2((double)std::cos(a), (double)std::sin(a));
+    }
+    if ((e = cudaMalloc(&h->dTrig, sizeof(double2) * kTrigEntries)) != cudaSuccess ||
+        (e = cudaMemcpy(h->dTrig, tab.data(), sizeof(double2) * kTrigEntries,
+                        cudaMemcpyHostToDevice)) != cudaSuccess) {
+      ck_destroy(h);
+      return cudaFail(e, "table upload");
+    }
+  }
   std::memset(&h->field, 0, sizeof(h->field));
   h->field.kind = f.kind;
   for (int i = 0; i < 3; ++i) h->field.b[i] = f.constant_tesla[i] * 0.000299792458;
@@ -513,6 +522,7 @@ ck_status ck_destroy(ck_handle* h) {
   h->ctx.release();
   h->unitBuf.release();
   if (h->dSurfaces) cudaFree(h->dSurfaces);
+  if (h->dTrig) cudaFree(h->dTrig);
   if (h->dNodes) cudaFree(h->dNodes);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -644,8 +654,8 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
     key.tune = tn;
     key.stream = st;
     key.scratch[0] = h->ctx.rec.p;
-    key.scratch[1] = h->ctx.recMeta.p;
-    key.scratch[2] = h->ctx.recMetaD.p;
+    key.scratch[1] = nullptr;
+    key.scratch[2] = nullptr;
     key.scratch[3] = h->ctx.perm.p;
     key.scratch[4] = h->ctx.ticket.p;
     key.scratch[5] = h->ctx.tip.p;

@@ -47,12 +47,10 @@ int occupancyBlocks(int precision, int variant, int tpb);
 // the ordered work queue and its ticket. A handle owns one; the serving loop
 // owns one per stream.
 struct FitContext {
-  DevBuf rec, recMeta, recMetaD, perm, ticket, tip;
+  DevBuf rec, perm, ticket, tip;
   void release() {
     tip.release();
     rec.release();
-    recMeta.release();
-    recMetaD.release();
     perm.release();
     ticket.release();
   }
@@ -65,6 +63,7 @@ ck_status validateOptions(const ck_options* o);
 DevOptions toDevOptions(const ck_options& o);
 MatConst makeMatConst();
 DevSurface toDevSurface(const ck_surface& s);
+size_t recordStateBytes(int precision);
 size_t recordBytesPerTrack(int maxStates, int precision);
 ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, int precision);
 ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
@@ -80,6 +79,7 @@ struct ck_handle {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   ck::DevSurface* dSurfaces = nullptr;
+  double2* dTrig = nullptr;
   int nSurfaces = 0;
   std::vector<ck_surface> hostSurfaces;
   ck_field hostField{};

@@ -89,11 +89,19 @@ struct Surf {
   P radius;
   int type;
   CK_D void load(const DevSurface* __restrict__ s) {
+    if constexpr (sizeof(P) == sizeof(float)) {
 #pragma unroll
-    for (int i = 0; i < 9; ++i) R[i] = (P)__ldg(&s->R[i]);
+      for (int i = 0; i < 9; ++i) R[i] = __ldg(&s->Rf[i]);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) c[i] = (P)__ldg(&s->c[i]);
-    radius = (P)__ldg(&s->radius);
+      for (int i = 0; i < 3; ++i) c[i] = __ldg(&s->cf[i]);
+      radius = __ldg(&s->radiusf);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 9; ++i) R[i] = (P)__ldg(&s->R[i]);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) c[i] = (P)__ldg(&s->c[i]);
+      radius = (P)__ldg(&s->radius);
+    }
     type = __ldg(&s->type);
   }
   CK_D void loadPlane(const double* __restrict__ f12) {
@@ -115,6 +123,41 @@ struct Surf {
     for (int i = 0; i < 3; ++i) g[i] = (R[i * 3 + 0] * l[0] + R[i * 3 + 1] * l[1] + R[i * 3 + 2] * l[2]) + c[i];
   }
 };
+
+// ------------------------------------------- FP64 functions of the mixed form
+// 1/sqrt(v): FP32 estimate refined by one FP64 Newton step (~1e-14 relative).
+CK_D double rsqrtRefined(double v) {
+  const double y = (double)rsqrtf((float)v);
+  return y * (1.5 - 0.5 * v * y * y);
+}
+
+// atan2 in FP64 by table-driven argument reduction: an FP32 atan2 picks the
+// nearest reference angle a_k = k pi/64; the vector (x, y) is rotated by -a_k
+// with the tabulated (cos a_k, sin a_k), so the residual angle d satisfies
+// |d| < pi/128 + 1e-6; d = atan(t), t = y'/x' (FP32 reciprocal refined by
+// FP64 Newton and residual steps), from the odd Taylor series of atan to
+// t^11 (truncation below 1e-19 relative); result a_k + d, wrapped to [-pi, pi].
+// Agrees with a correctly rounded atan2 to a few ulp.
+CK_D double atan2Table(double y, double x, const double2* __restrict__ tab) {
+  const float f = atan2f((float)y, (float)x);
+  int k = __float2int_rn(f * (float)(1.0 / kTrigStep));
+  k = k < -64 ? -64 : (k > 64 ? 64 : k);
+  const double2 cs = __ldg(&tab[k + 64]);
+  const double xr = x * cs.x + y * cs.y;
+  const double yr = y * cs.x - x * cs.y;
+  if (!(xr > 0.0)) return (double)f;  // only for (x, y) = (0, 0)
+  double r = (double)(1.0f / (float)xr);
+  r = r * (2.0 - xr * r);
+  double t = yr * r;
+  t = t + r * (yr - xr * t);
+  const double t2 = t * t;
+  const double d =
+      t * (1.0 + t2 * (-1.0 / 3 + t2 * (1.0 / 5 + t2 * (-1.0 / 7 + t2 * (1.0 / 9 + t2 * (-1.0 / 11))))));
+  double a = (double)k * kTrigStep + d;
+  if (a > kPi) a -= 2 * kPi;
+  if (a < -kPi) a += 2 * kPi;
+  return a;
+}
 
 // intersection status: 0 unreachable, 1 reachable, 2 on surface
 template <typename P>

@@ -58,18 +58,26 @@ CK_D void cupdate(double& slot, double v) {
 }
 
 // scratch record access (one record set per resident lane)
+// the surface in the stepper precision: the FP64 surface itself in the
+// plain form, its FP32 copy in the mixed form
+template <typename P>
+CK_D const Surf<P>& pickSurf(const Surf<double>& d, const Surf<P>& p) {
+  if constexpr (sizeof(P) == sizeof(double))
+    return d;
+  else
+    return p;
+}
+
 template <typename CV>
 struct Rec {
-  double* par;
-  CV* mat;
-  int ns;
-  int slot;
-  CK_D Rec(const FitParams& fp, int s)
-      : par(fp.rec), mat(static_cast<CV*>(fp.rec_mat)), ns(fp.rec_stride), slot(s) {}
+  RecState<CV>* base;  // state 0 of this queue position
+  CK_D Rec(const FitParams& fp, int q)
+      : base(static_cast<RecState<CV>*>(fp.rec) + (size_t)q * (size_t)fp.max_states) {}
   // bound parameters (FP64)
-  CK_D double& p(int k, int f) const { return par[((size_t)k * kRecParams + f) * (size_t)ns + slot]; }
+  CK_D double& p(int k, int f) const { return base[k].par[f]; }
   // covariances and jacobian (CV)
-  CK_D CV& m(int k, int f) const { return mat[((size_t)k * kRecMatrix + f) * (size_t)ns + slot]; }
+  CK_D CV& m(int k, int f) const { return base[k].mat[f]; }
+  CK_D RecState<CV>& s(int k) const { return base[k]; }
 };
 
 template <typename P, typename CV>
@@ -145,19 +153,40 @@ struct Lane {
 
   // Surface::isOnSurface part of globalToLocal: the check alone, without
   // the local coordinates
-  CK_D bool onSurface(const Surf<double>& sf) const {
-    double l[3];
-    sf.toLocal3(pos, l);
+  // sqrt in the form's arithmetic: FP64 sqrt (plain), refined FP32
+  // reciprocal square root (mixed)
+  CK_D static double sqrtF(double v) {
+    if constexpr (sizeof(P) == sizeof(float))
+      return v > 0.0 ? v * rsqrtRefined(v) : 0.0;
+    else
+      return sqrt(v);
+  }
+  CK_D double atan2F(const FitParams& fp, double y, double x) const {
+    if constexpr (sizeof(P) == sizeof(float))
+      return atan2Table(y, x, fp.trig);
+    else
+      return atan2(y, x);
+  }
+
+  // local coordinates R^T (pos - c) of the current position
+  CK_D void local(const Surf<double>& sf, double l[3]) const { sf.toLocal3(pos, l); }
+
+  // Surface::isOnSurface part of globalToLocal, from the local coordinates
+  CK_D static bool onSurfaceLocal(const Surf<double>& sf, const double l[3]) {
     if (sf.type == CK_SURFACE_PLANE) return fabs(l[2]) <= kOnSurfaceTolerance;
     double inttol = sf.radius * 0.0001;
     if (inttol < 0.01) inttol = 0.01;
-    return fabs(sqrt(l[0] * l[0] + l[1] * l[1]) - sf.radius) <= inttol;
+    return fabs(sqrtF(l[0] * l[0] + l[1] * l[1]) - sf.radius) <= inttol;
+  }
+  CK_D bool onSurface(const Surf<double>& sf) const {
+    double l[3];
+    local(sf, l);
+    return onSurfaceLocal(sf, l);
   }
 
   // Surface::globalToLocal in double (the bound parameters are outputs)
-  CK_NI bool toLocal(const Surf<double>& sf, double loc[2]) const {
-    double l[3];
-    sf.toLocal3(pos, l);
+  CK_NI bool toLocal(const FitParams& fp, const Surf<double>& sf, const double l[3],
+                     double loc[2]) const {
     if (sf.type == CK_SURFACE_PLANE) {
       if (fabs(l[2]) > kOnSurfaceTolerance) return false;
       loc[0] = l[0];
@@ -166,22 +195,24 @@ struct Lane {
     }
     double inttol = sf.radius * 0.0001;
     if (inttol < 0.01) inttol = 0.01;
-    const double r = sqrt(l[0] * l[0] + l[1] * l[1]);
+    const double r = sqrtF(l[0] * l[0] + l[1] * l[1]);
     if (fabs(r - sf.radius) > inttol) return false;
-    loc[0] = sf.radius * atan2(l[1], l[0]);
+    loc[0] = sf.radius * atan2F(fp, l[1], l[0]);
     loc[1] = l[2];
     return true;
   }
 
-  // transformFreeToBoundParameters (TransformationHelpers.cpp:41-63)
-  CK_NI bool freeToBound(const Surf<double>& sf, double b[6]) const {
+  // transformFreeToBoundParameters (TransformationHelpers.cpp:41-63), with
+  // the local coordinates of the current position
+  CK_NI bool freeToBound(const FitParams& fp, const Surf<double>& sf, const double l[3],
+                         double b[6]) const {
     double loc[2];
-    if (!toLocal(sf, loc)) return false;
+    if (!toLocal(fp, sf, l, loc)) return false;
     b[0] = loc[0];
     b[1] = loc[1];
     b[5] = tim;
-    b[2] = atan2(dir[1], dir[0]);
-    b[3] = atan2(sqrt(dir[0] * dir[0] + dir[1] * dir[1]), dir[2]);
+    b[2] = atan2F(fp, dir[1], dir[0]);
+    b[3] = atan2F(fp, sqrtF(dir[0] * dir[0] + dir[1] * dir[1]), dir[2]);
     b[4] = qop;
     return true;
   }
@@ -216,7 +247,8 @@ struct Lane {
   // rotates the predicted free state (still held) by the small filtered
   // changes of phi, theta and the cylinder angle, with FP64 sines and cosines
   // of those changes from their Taylor series — no FP64 trigonometry.
-  CK_D void updateFree(const Surf<double>& sf, const double pred[6], const double filt[6]) {
+  CK_D void updateFree(const Surf<double>& sf, const double pred[6], const double filt[6],
+                       const double lp[3]) {
     if constexpr (sizeof(P) == sizeof(double)) {
       boundToFree(sf, filt);
     } else {
@@ -258,8 +290,6 @@ struct Lane {
         l[1] = filt[1];
         l[2] = 0.0;
       } else {
-        double lp[3];
-        sf.toLocal3(pos, lp);
         const double ir = rsq(lp[0] * lp[0] + lp[1] * lp[1]);
         const double ca = lp[0] * ir, sa = lp[1] * ir;
         double sda, cda;
@@ -283,6 +313,9 @@ struct Lane {
     for (int i = 0; i < 3; ++i) sf.c[i] = (P)sfd.c[i];
     sf.radius = (P)sfd.radius;
     sf.type = sfd.type;
+    initTP(sf);
+  }
+  CK_D void initTP(const Surf<P>& sf) {
     const P p[3] = {(P)pos[0], (P)pos[1], (P)pos[2]};
     const P f[8] = {p[0], p[1], p[2], (P)tim, (P)dir[0], (P)dir[1], (P)dir[2], (P)qop};
     initTransport(sf, f, T);
@@ -361,16 +394,15 @@ struct Lane {
 
   // ------------------------------------------------------------ material
   // PointwiseMaterialInteraction: mode 1 pre, 2 post, 3 full.
-  CK_NI bool material(const FitParams& fp, int sid, const Surf<double>& sfd, int mode) {
+  CK_NI bool material(const FitParams& fp, int sid, const Surf<double>& sfd, const Surf<P>& sp,
+                      const double l[3], int mode) {
     const DevSurface* ds = fp.surfaces + sid;
     if (!(__ldg(&ds->flags) & CK_SURF_MATERIAL)) return true;
     const P d[3] = {(P)dir[0], (P)dir[1], (P)dir[2]};
     P pc;
     if (sfd.type == CK_SURFACE_PLANE) {
-      pc = P(1) / fabs((P)sfd.R[2] * d[0] + (P)sfd.R[5] * d[1] + (P)sfd.R[8] * d[2]);
+      pc = P(1) / fabs(sp.R[2] * d[0] + sp.R[5] * d[1] + sp.R[8] * d[2]);
     } else {
-      double l[3];
-      sfd.toLocal3(pos, l);
       const P l0 = (P)l[0], l1 = (P)l[1];
       P n0 = l0, n1 = l1;
       const P n2 = l0 * l0 + l1 * l1;
@@ -381,10 +413,10 @@ struct Lane {
       }
       P ez[3];
 #pragma unroll
-      for (int i = 0; i < 3; ++i) ez[i] = (P)sfd.R[i * 3 + 0] * n0 + (P)sfd.R[i * 3 + 1] * n1;
+      for (int i = 0; i < 3; ++i) ez[i] = sp.R[i * 3 + 0] * n0 + sp.R[i * 3 + 1] * n1;
       pc = fabs(P(1) / (ez[0] * d[0] + ez[1] * d[1] + ez[2] * d[2]));
     }
-    if (!onSurface(sfd)) return false;
+    if (!onSurfaceLocal(sfd, l)) return false;
     float f1 = 1.0f;
     if (__ldg(&ds->vacuum) == 0) {
       const float split = __ldg(&ds->split);
@@ -440,15 +472,9 @@ struct Lane {
   // ------------------------------------------------- covariance transport
   // J = F2B (I + deriv fTP) T, C <- J C J^T, reinitialise T at the surface
   // (CovarianceEngine.cpp:102-165). J is returned for the record.
-  CK_NI void transportToBound(const Surf<double>& sfd, CV Jout[36]) {
+  CK_NI void transportToBound(const Surf<double>& sfd, const Surf<P>& sf, const double l[3],
+                              CV Jout[36]) {
     const P p[3] = {(P)pos[0], (P)pos[1], (P)pos[2]};
-    Surf<P> sf;
-#pragma unroll
-    for (int i = 0; i < 9; ++i) sf.R[i] = (P)sfd.R[i];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) sf.c[i] = (P)sfd.c[i];
-    sf.radius = (P)sfd.radius;
-    sf.type = sfd.type;
     P ex[3], ey[3], ez[3];
     referenceFrame(sf, p, ex, ey, ez);
     const P dir[3] = {(P)this->dir[0], (P)this->dir[1], (P)this->dir[2]};
@@ -529,15 +555,16 @@ struct Lane {
     for (int i = 0; i < 21; ++i) cov[i] = outc[i];
 #pragma unroll
     for (int i = 0; i < 7; ++i) deriv[i] = P(0);
-    if (onSurface(sfd)) initT(sfd);
+    if (onSurfaceLocal(sfd, l)) initTP(sf);
   }
 
   // --------------------------------------------------------------- actor
   CK_D void writeMeta(const FitParams& fp, int slot, int k, int sid, uint32_t flags, double chi2) {
-    fp.rec_meta[((size_t)k * 2 + 0) * (size_t)fp.rec_stride + slot] = sid;
-    fp.rec_meta[((size_t)k * 2 + 1) * (size_t)fp.rec_stride + slot] = (int32_t)flags;
-    fp.rec_meta_d[((size_t)k * 2 + 0) * (size_t)fp.rec_stride + slot] = pathAcc;
-    fp.rec_meta_d[((size_t)k * 2 + 1) * (size_t)fp.rec_stride + slot] = chi2;
+    RecState<CV>& r = Rec<CV>(fp, slot).s(k);
+    r.surface = sid;
+    r.flags = (int32_t)flags;
+    r.pathLength = pathAcc;
+    r.chi2 = chi2;
   }
 
   // KalmanFitter::Actor::filter on surface `sid`
@@ -545,25 +572,32 @@ struct Lane {
     const Rec<CV> rec(fp, slot);
     Surf<double> sf;
     sf.load(fp.surfaces + sid);
+    Surf<P> spv;
+    if constexpr (sizeof(P) == sizeof(float)) spv.load(fp.surfaces + sid);
+    const Surf<P>& sp = pickSurf<P>(sf, spv);
     const int sflags = __ldg(&fp.surfaces[sid].flags);
     const bool sensitive = (sflags & CK_SURF_SENSITIVE) != 0;
     const bool hasMat = (sflags & CK_SURF_MATERIAL) != 0;
     const bool preceding = measurementStates > 0;
+    // local coordinates of the position on arrival (the position changes
+    // only with the update below)
+    double l[3];
+    local(sf, l);
     if (coasting) {
       if ((preceding && sensitive) || hasMat) {
         double bp[6];
-        if (!freeToBound(sf, bp)) return CK_TRACK_NOT_ON_SURFACE;
-        if (!material(fp, sid, sf, 3)) return CK_TRACK_NOT_ON_SURFACE;
+        if (!freeToBound(fp, sf, l, bp)) return CK_TRACK_NOT_ON_SURFACE;
+        if (!material(fp, sid, sf, sp, l, 3)) return CK_TRACK_NOT_ON_SURFACE;
       }
       return CK_TRACK_OK;
     }
     const int mi = findMeas(fp, sid);
     if (mi >= 0) {
       CV J[36];
-      transportToBound(sf, J);
-      if (!material(fp, sid, sf, 1)) return CK_TRACK_NOT_ON_SURFACE;
+      transportToBound(sf, sp, l, J);
+      if (!material(fp, sid, sf, sp, l, 1)) return CK_TRACK_NOT_ON_SURFACE;
       double bp[6];
-      if (!freeToBound(sf, bp)) return CK_TRACK_NOT_ON_SURFACE;
+      if (!freeToBound(fp, sf, l, bp)) return CK_TRACK_NOT_ON_SURFACE;
       if (nStates >= fp.max_states) return CK_TRACK_TOO_MANY_STATES;
       const int k = nStates++;
       double Pp[21];
@@ -591,13 +625,14 @@ struct Lane {
         flags |= CK_FLAG_HAS_MEASUREMENT;
 #pragma unroll
         for (int i = 0; i < 6; ++i) rec.p(k, kRecFilt + i) = filt[i];
-        updateFree(sf, bp, filt);
+        updateFree(sf, bp, filt, l);
 #pragma unroll
         for (int i = 0; i < 21; ++i) {
           cov[i] = (CV)F[i];
           rec.m(k, kRecFiltCov + i) = cov[i];
         }
-        initT(sf);
+        initTP(sp);
+        local(sf, l);  // the updated position
         ++measurementStates;
       } else {
         flags |= CK_FLAG_HAS_MEASUREMENT | CK_FLAG_IS_OUTLIER;
@@ -607,13 +642,13 @@ struct Lane {
         for (int i = 0; i < 21; ++i) rec.m(k, kRecFiltCov + i) = cov[i];
       }
       writeMeta(fp, slot, k, sid, flags, chi2);
-      if (!material(fp, sid, sf, 2)) return CK_TRACK_NOT_ON_SURFACE;
+      if (!material(fp, sid, sf, sp, l, 2)) return CK_TRACK_NOT_ON_SURFACE;
       lastMeasurementIndex = k;
     } else if ((preceding && sensitive) || hasMat) {
       double bp[6];
-      if (!freeToBound(sf, bp)) return CK_TRACK_NOT_ON_SURFACE;
+      if (!freeToBound(fp, sf, l, bp)) return CK_TRACK_NOT_ON_SURFACE;
       CV J[36];
-      transportToBound(sf, J);
+      transportToBound(sf, sp, l, J);
       if (nStates >= fp.max_states) return CK_TRACK_TOO_MANY_STATES;
       const int k = nStates++;
 #pragma unroll
@@ -631,7 +666,7 @@ struct Lane {
       uint32_t flags = CK_FLAG_HAS_PARAMETERS | (hasMat ? CK_FLAG_HAS_MATERIAL : 0u);
       if (sensitive && preceding) flags |= CK_FLAG_IS_HOLE;
       writeMeta(fp, slot, k, sid, flags, 0.0);
-      if (!material(fp, sid, sf, 3)) return CK_TRACK_NOT_ON_SURFACE;
+      if (!material(fp, sid, sf, sp, l, 3)) return CK_TRACK_NOT_ON_SURFACE;
     }
     return CK_TRACK_OK;
   }
@@ -1031,8 +1066,9 @@ struct Smoother {
     t = track;
     q = queuePos;
     lastMeas = tip;
+    const Rec<CV> rec(fp, q);
     for (int k = tip; k >= 0; --k) {
-      const uint32_t fl = (uint32_t)fp.rec_meta[((size_t)k * 2 + 1) * (size_t)fp.rec_stride + q];
+      const uint32_t fl = (uint32_t)rec.s(k).flags;
       if ((fl & CK_FLAG_HAS_MEASUREMENT) && !(fl & CK_FLAG_IS_OUTLIER)) {
         lastMeas = k;
         break;
@@ -1040,20 +1076,18 @@ struct Smoother {
     }
     nM = nH = nO = ndf = 0;
     chi2sum = 0.0;
-    const Rec<CV> rec(fp, q);
-    {
-      double sm[6];
-      CV Ps[21];
+    // the smoothed state of k+1, carried from one step to the next (the tip's
+    // smoothed state is its filtered state)
+    double ps[6];
+    CV Psp[21];
 #pragma unroll
-      for (int i = 0; i < 6; ++i) sm[i] = rec.p(tip, kRecFilt + i);
+    for (int i = 0; i < 6; ++i) ps[i] = rec.p(tip, kRecFilt + i);
 #pragma unroll
-      for (int i = 0; i < 21; ++i) Ps[i] = rec.m(tip, kRecFiltCov + i);
-      writeState(fp, tip, sm, Ps, false);
-    }
+    for (int i = 0; i < 21; ++i) Psp[i] = rec.m(tip, kRecFiltCov + i);
+    writeState(fp, tip, ps, Psp, false);
     for (int k = tip - 1; k >= 0; --k) {
-      // the smoothed state of k+1 sits in the filtered fields of its record
-      double filt[6], pp[6], ps[6], sm[6];
-      CV Pf[21], Ppp[21], J[36], Psp[21], Ps[21];
+      double filt[6], pp[6], sm[6];
+      CV Pf[21], Ppp[21], J[36], Ps[21];
 #pragma unroll
       for (int i = 0; i < 6; ++i) filt[i] = rec.p(k, kRecFilt + i);
 #pragma unroll
@@ -1064,19 +1098,15 @@ struct Smoother {
       for (int i = 0; i < 21; ++i) Ppp[i] = rec.m(k + 1, kRecPredCov + i);
 #pragma unroll
       for (int i = 0; i < 36; ++i) J[i] = rec.m(k + 1, kRecJac + i);
-#pragma unroll
-      for (int i = 0; i < 6; ++i) ps[i] = rec.p(k + 1, kRecFilt + i);
-#pragma unroll
-      for (int i = 0; i < 21; ++i) Psp[i] = rec.m(k + 1, kRecFiltCov + i);
       if (!smoothStep<CV>(filt, Pf, pp, Ppp, J, ps, Psp, sm, Ps)) {
         failSmooth(fp);
         return;
       }
       writeState(fp, k, sm, Ps, k == lastMeas);
 #pragma unroll
-      for (int i = 0; i < 6; ++i) rec.p(k, kRecFilt + i) = sm[i];
+      for (int i = 0; i < 6; ++i) ps[i] = sm[i];
 #pragma unroll
-      for (int i = 0; i < 21; ++i) rec.m(k, kRecFiltCov + i) = Ps[i];
+      for (int i = 0; i < 21; ++i) Psp[i] = Ps[i];
     }
     const ck_batch_out& out = fp.out;
     out.status[t] = CK_TRACK_OK;
@@ -1105,13 +1135,13 @@ struct Smoother {
     const Rec<CV> rec(fp, q);
     const size_t n = (size_t)fp.n_tracks;
     auto at = [&](int C, int c) -> size_t { return ((size_t)k * C + c) * n + t; };
-    const size_t ms = (size_t)fp.rec_stride;
-    const uint32_t fl = (uint32_t)fp.rec_meta[((size_t)k * 2 + 1) * ms + q];
-    const double c2 = fp.rec_meta_d[((size_t)k * 2 + 1) * ms + q];
-    if (out.state_surface) out.state_surface[at(1, 0)] = fp.rec_meta[((size_t)k * 2 + 0) * ms + q];
+    const RecState<CV>& rs = rec.s(k);
+    const uint32_t fl = (uint32_t)rs.flags;
+    const double c2 = rs.chi2;
+    if (out.state_surface) out.state_surface[at(1, 0)] = rs.surface;
     if (out.state_flags) out.state_flags[at(1, 0)] = fl;
     if (out.state_path_length)
-      out.state_path_length[at(1, 0)] = fp.rec_meta_d[((size_t)k * 2 + 0) * ms + q];
+      out.state_path_length[at(1, 0)] = rs.pathLength;
     if (out.state_chi2) out.state_chi2[at(1, 0)] = c2;
     if (fl & CK_FLAG_IS_HOLE) {
       ++nH;

@@ -21,7 +21,14 @@ struct DevSurface {
   float split;                       // split factor
   int vacuum;                        // Material::isVacuum() (Ar <= 0)
   int pad;
+  float Rf[9], cf[3], radiusf;        // FP32 copies for the mixed form
+  int pad2;
 };
+
+// Reference angles of the mixed form's FP64 atan2: entry k + 64 holds
+// (cos, sin) of k * kTrigStep, k = -64..64.
+constexpr int kTrigEntries = 129;
+constexpr double kTrigStep = 3.14159265358979323846 / 64;
 
 // Field as the kernels see it. Grid nodes are float4 (Bx, By, Bz, 0) in
 // Tesla, layout [ix][iy][iz]; the axis arithmetic follows the reference's
@@ -53,10 +60,12 @@ struct DevOptions {
   int useOutlierCut, earlyTermination;
 };
 
-// Record of one forward track state kept for the smoother (scratch), in two
-// parts: the bound parameters in FP64 (predicted 6, filtered 6) and the
-// matrices in the covariance type of the form (predicted cov 21 and filtered
-// cov 21, packed upper; jacobian 36). The scratch is sized for FP64 matrices.
+// Record of one forward track state kept for the smoother (scratch), one
+// contiguous block per (track, state): the bound parameters in FP64
+// (predicted 6, filtered 6), path length, chi2, surface id, type flags and
+// the matrices in the covariance type CV of the form (predicted cov 21 and
+// filtered cov 21, packed upper; jacobian 36). A lane writes its state's
+// block as a whole, so DRAM sees full sectors.
 constexpr int kRecPred = 0;
 constexpr int kRecFilt = 6;
 constexpr int kRecParams = 12;
@@ -64,7 +73,16 @@ constexpr int kRecPredCov = 0;
 constexpr int kRecFiltCov = 21;
 constexpr int kRecJac = 42;
 constexpr int kRecMatrix = 78;
-constexpr int kRecDoubles = kRecParams + kRecMatrix;
+
+template <typename CV>
+struct RecState {
+  double par[kRecParams];
+  double pathLength, chi2;
+  int32_t surface, flags;
+  CV mat[kRecMatrix];
+};
+static_assert(sizeof(RecState<float>) == 432, "record layout");
+static_assert(sizeof(RecState<double>) == 744, "record layout");
 
 struct FitParams {
   int n_tracks;
@@ -84,20 +102,14 @@ struct FitParams {
   // queue: slot -> track index (descending sequence length) and ticket
   const int32_t* perm;
   int32_t* ticket;
-  // track-state records of the forward filter, indexed by queue position q
-  // (rec_stride = n_queue), read back by the smoother kernel:
-  //   rec        [(k * kRecParams + f) * rec_stride + q]       (double)
-  //   rec_mat    [(k * kRecMatrix + f) * rec_stride + q]       (CV)
-  //   rec_meta   [(k * 2 + {surface, flags}) * rec_stride + q]
-  //   rec_meta_d [(k * 2 + {pathLength, chi2}) * rec_stride + q]
-  //   tip        [q]: index of the last measurement state, -1 when the
-  //              forward filter failed (its status is then already written)
-  double* rec;
-  void* rec_mat;
-  int32_t* rec_meta;
-  double* rec_meta_d;
+  // track-state records of the forward filter, read back by the smoother
+  // kernel: RecState<CV> of state k of queue position q at
+  // rec[q * max_states + k];
+  //   tip [q]: index of the last measurement state, -1 when the forward
+  //            filter failed (its status is then already written)
+  void* rec;
   int32_t* tip;
-  int rec_stride;
+  const double2* trig;  // kTrigEntries reference angles (mixed form)
   // lanes of each warp that take tracks: all 32 for large batches; fewer
   // when the batch is small, so that its tracks spread over all warps
   int lanes_per_warp;

@@ -51,20 +51,17 @@ size_t roundUp(size_t b) { return (b + kAlign - 1) & ~(kAlign - 1); }
 
 // Scratch layout for n tracks of up to maxStates states.
 struct Layout {
-  size_t rec, recMeta, recMetaD, perm, tip, ticket, total;
+  size_t rec, perm, tip, ticket, total;
 };
 
 Layout layoutFor(int n, int maxStates, int precision) {
-  const size_t matElem = precision == CK_PRECISION_MIXED ? sizeof(float) : sizeof(double);
   const size_t ns = (size_t)n * (size_t)maxStates;
   Layout l;
-  l.rec = roundUp(ns * kRecParams * sizeof(double) + ns * kRecMatrix * matElem);
-  l.recMeta = roundUp(ns * 2 * sizeof(int32_t));
-  l.recMetaD = roundUp(ns * 2 * sizeof(double));
+  l.rec = roundUp(ns * recordStateBytes(precision));
   l.perm = roundUp((size_t)n * sizeof(int32_t));
   l.tip = roundUp((size_t)n * sizeof(int32_t));
   l.ticket = kTicketBytes;
-  l.total = l.rec + l.recMeta + l.recMetaD + l.perm + l.tip + l.ticket;
+  l.total = l.rec + l.perm + l.tip + l.ticket;
   return l;
 }
 
@@ -129,8 +126,6 @@ ck_status ck_fit_batch_static(ck_handle* h, const ck_options* opt, const ck_batc
     off += bytes;
   };
   view(c.rec, l.rec);
-  view(c.recMeta, l.recMeta);
-  view(c.recMetaD, l.recMetaD);
   view(c.perm, l.perm);
   view(c.tip, l.tip);
   view(c.ticket, l.ticket);

@@ -35,6 +35,12 @@ __global__ void updateKernel(int n, int joseph, const double* __restrict__ pred,
   chi2[i] = c2;
 }
 
+__global__ void atan2Kernel(int n, const double* __restrict__ y, const double* __restrict__ x,
+                            const double2* __restrict__ tab, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = atan2Table(y[i], x[i], tab);
+}
+
 __global__ void smoothKernel(int nTraj, int nStates, const double* __restrict__ pred,
                              const double* __restrict__ predCov, const double* __restrict__ filt,
                              const double* __restrict__ filtCov, const double* __restrict__ jac,
@@ -244,6 +250,29 @@ ck_status ck_material_effects(ck_handle* h, int32_t n, const int32_t* surface,
       multiple_scattering, energy_loss, a.at<double>(tOut));
   cudaMemcpyAsync(effects, a.at<double>(tOut), 32 * n, cudaMemcpyDeviceToHost, st);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cudaFail(e, "material kernel");
+  h->lastLaunches = 1;
+  return CK_OK;
+}
+
+ck_status ck_atan2_mixed(ck_handle* h, int32_t n, const double* y, const double* x,
+                         double* out) {
+  if (!h || n < 0 || !y || !x || !out) return fail(CK_ERR_INVALID_ARGUMENT, "bad argument");
+  if (n == 0) return CK_OK;
+  std::lock_guard<std::mutex> lock(h->mu);
+  cudaSetDevice(h->device);
+  Arena a{h};
+  void* tY = a.add(8 * n);
+  void* tX = a.add(8 * n);
+  void* tO = a.add(8 * n);
+  cudaError_t e = a.commit();
+  if (e != cudaSuccess) return cudaFail(e, "unit buffer");
+  cudaStream_t st = h->stream;
+  cudaMemcpyAsync(a.at<double>(tY), y, 8 * n, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(a.at<double>(tX), x, 8 * n, cudaMemcpyHostToDevice, st);
+  atan2Kernel<<<(n + 127) / 128, 128, 0, st>>>(n, a.at<double>(tY), a.at<double>(tX), h->dTrig,
+                                               a.at<double>(tO));
+  cudaMemcpyAsync(out, a.at<double>(tO), 8 * n, cudaMemcpyDeviceToHost, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cudaFail(e, "atan2 kernel");
   h->lastLaunches = 1;
   return CK_OK;
 }

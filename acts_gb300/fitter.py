@@ -63,6 +63,8 @@ def lib():
         L.ck_static_scratch_bytes.restype = C.c_int64
         L.ck_static_scratch_capacity.restype = C.c_int64
         L.ck_sync.argtypes = [C.c_void_p]
+        L.ck_atan2_mixed.argtypes = [C.c_void_p, C.c_int32, P(C.c_double), P(C.c_double),
+                                     P(C.c_double)]
         L.ck_last_kernel_ms.argtypes = [C.c_void_p, P(C.c_double)]
         L.ck_last_launch_count.argtypes = [C.c_void_p, P(C.c_int32)]
         L.ck_last_transfer_bytes.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64)]
@@ -290,6 +292,15 @@ class CudaKalman:
 
     def set_launch_config(self, precision, variant, tpb, bps):
         _check(lib().ck_set_launch_config(self._h, precision, variant, tpb, bps))
+
+    def atan2_mixed(self, y, x):
+        """The mixed form's FP64 atan2 on the device (numpy arrays in, out)."""
+        y = np.ascontiguousarray(y, np.float64)
+        x = np.ascontiguousarray(x, np.float64)
+        out = np.empty_like(y)
+        _check(lib().ck_atan2_mixed(self._h, y.size, abi.ptr(y, C.c_double), abi.ptr(x, C.c_double),
+                                    abi.ptr(out, C.c_double)))
+        return out
 
     def fp_peak_gflops(self, precision):
         g = C.c_double()

@@ -24,6 +24,10 @@ def main(argv=None):
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--seed", type=int, default=5)
     ap.add_argument("--max-states", type=int, default=0)
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="forward-filter kernel variant (default: the handle's default)")
+    ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--blocks-per-sm", type=int, default=0)
     a = ap.parse_args(argv)
     preset = PRESETS[a.preset]
     det = generate.Detector(preset)
@@ -32,6 +36,8 @@ def main(argv=None):
     fit = CudaKalman.for_detector(det, use_graph=False)
     for name in a.precision.split(","):
         prec = abi.PRECISION_MIXED if name == "mixed" else abi.PRECISION_FP64
+        if a.variant >= 0:
+            fit.set_launch_config(prec, a.variant, a.threads, a.blocks_per_sm)
         opt = abi.default_options(precision=prec,
                                   outlier_chi2_cut=15.0 if preset == abi.CKG_UNEVEN else float("inf"))
         for _ in range(a.repeat):

@@ -278,6 +278,19 @@ def accuracy_report(b, r64, rmx, n):
             "chi2ndf_fp64": c64, "chi2ndf_mixed": cmx}
 
 
+def best_of_tune_log(log):
+    """The fastest entry of an autotuner log ("v3 tpb256 bps1 12.345ms; ...")."""
+    best = None
+    for item in log.split(";"):
+        parts = item.split()
+        if len(parts) == 4 and parts[3].endswith("ms"):
+            ms = float(parts[3][:-2])
+            if best is None or ms < best[1]:
+                best = (" ".join(parts[:3]), ms)
+    return None if best is None else {"config": best[0], "kernel_ms": best[1],
+                                      "configs_tried": len([x for x in log.split(";") if x.strip()])}
+
+
 def cpu_baseline(det, b, opt, budget_s=10.0):
     """The oracle on all host cores over a bounded sample (~budget_s)."""
     from oracle import kforacle
@@ -365,7 +378,12 @@ def native_arm(args):
     results = {}
     snapshots = {}
     clocks = ClockSampler(local)
+    tune_log = {}
     for name, opt in forms.items():
+        # the project's autotuner picks the kernel variant, threads per block
+        # and resident blocks per SM on this very batch (before any timing)
+        if args.autotune:
+            tune_log[name] = fit.autotune(opt, bi, bo)
         for _ in range(max(3, args.warmup)):
             fit.fit_batch_raw(opt, bi, bo, sp)
         torch.cuda.synchronize(dev)
@@ -394,7 +412,8 @@ def native_arm(args):
                          "kernel_ms": float(np.mean(kernel_ms)),
                          "launches_per_step": launches_per_step,
                          "ok_fraction": float(np.mean(status == 0)),
-                         "launch_config": fit.launch_config(opt.precision)}
+                         "launch_config": fit.launch_config(opt.precision),
+                         "autotuned": best_of_tune_log(tune_log.get(name, ""))}
         na = min(n, 100000)
         snapshots[name] = {k: keep_out[k].cpu().numpy() for k in
                            ("status", "state_flags", "state_surface", "smoothed",
@@ -650,6 +669,8 @@ def main():
     ap.add_argument("--tracks", type=int, default=1000000)
     ap.add_argument("--no-serving", dest="serving", action="store_false",
                     help="skip the serving-loop latency measurement")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="keep the default launch configuration")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)

@@ -400,6 +400,14 @@ ck_status ck_gain_matrix_smooth(ck_handle* h, int32_t n_traj, int32_t n_states,
                                 const double* jacobian, double* smoothed,
                                 double* smoothed_cov, int32_t* status);
 
+/* The mixed form's FP64 atan2 (table-driven argument reduction; used for
+ * the bound angles and the cylinder loc0) on a batch: out[i] = atan2(y[i],
+ * x[i]). Host pointers; synchronous. No counterpart in the reference (it
+ * stands for std::atan2 in transformFreeToBoundParameters,
+ * TransformationHelpers.cpp:41-63). */
+ck_status ck_atan2_mixed(ck_handle* h, int32_t n, const double* y, const double* x,
+                         double* out);
+
 /* Pointwise material effects (computeMaterialEffects,
  * Core/src/Propagator/detail/PointwiseMaterialInteraction.cpp:49-90) for a
  * batch of (slab, direction, q/p) inputs on the device: per input the

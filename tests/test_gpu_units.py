@@ -109,3 +109,27 @@ def test_field_lookup_matches_oracle(fitter_factory):
     ok = gs == 0
     assert ok.sum() > 10000 and (~ok).sum() > 1000
     np.testing.assert_allclose(g[ok], o[ok], rtol=1e-12, atol=1e-18)
+
+
+@pytest.mark.gpu
+def test_mixed_form_atan2_matches_correctly_rounded(fitter_factory):
+    """The mixed form's table-driven FP64 atan2 against numpy's arctan2 on
+    random directions of all magnitudes and the edge cases (axes, the +-pi
+    seam, tiny and huge components): within 4 ulp."""
+    fit = fitter_factory(abi.CKG_BARREL)
+    rng = np.random.default_rng(3)
+    n = 200000
+    ang = rng.uniform(-np.pi, np.pi, n)
+    mag = 10.0 ** rng.uniform(-8, 4, n)
+    y, x = mag * np.sin(ang), mag * np.cos(ang)
+    edge_y = np.array([0.0, 0.0, 1.0, -1.0, 1e-300, -1e-300, 1e-12, -1e-12, 1.0, 1.0, 3e3, -2.0])
+    edge_x = np.array([1.0, -1.0, 0.0, 0.0, -1.0, -1.0, -1.0, -1.0, 1e-12, -1e-12, 1e-3, 1e-9])
+    y = np.concatenate([y, edge_y])
+    x = np.concatenate([x, edge_x])
+    got = fit.atan2_mixed(y, x)
+    ref = np.arctan2(y, x)
+    ulp = np.abs(got - ref) / np.spacing(np.abs(ref)).clip(min=np.spacing(1e-300))
+    # +-pi for y = -0 / +0 with x < 0 are the same angle
+    seam = np.isclose(np.abs(ref), np.pi) & np.isclose(np.abs(got), np.pi)
+    ulp[seam] = np.minimum(ulp[seam], np.abs(np.abs(got[seam]) - np.abs(ref[seam])) / np.spacing(np.pi))
+    assert ulp.max() <= 4, (ulp.max(), y[ulp.argmax()], x[ulp.argmax()])
