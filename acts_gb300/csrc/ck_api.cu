@@ -138,43 +138,92 @@ ck_status validateOptions(const ck_options* o) {
 }  // namespace ck
 
 // ------------------------------------------------------------ queue kernels
+// The work queue: the tracks ordered by sequence length, longest first, by a
+// stable counting sort (tracks of equal length keep their input order, so
+// neighbouring queue positions hold neighbouring tracks and the smoother's
+// output writes coalesce). Three launches: per-block histograms, one scan
+// over (length bin, block) in descending length order, rank-preserving
+// scatter.
 namespace {
 
 constexpr int kBins = 64;
 
-__global__ void queueHistogram(const int32_t* __restrict__ off, int n, int32_t* bins) {
+__device__ __forceinline__ int lengthBin(const int32_t* __restrict__ off, int t) {
+  int len = off[t + 1] - off[t];
+  return len < 0 ? 0 : (len >= kBins ? kBins - 1 : len);
+}
+
+// counts[bin * nb + block]
+__global__ void __launch_bounds__(kSortBlock) queueBlockHist(const int32_t* __restrict__ off,
+                                                             int n, int32_t* counts, int nb) {
   __shared__ int32_t h[kBins];
   for (int i = threadIdx.x; i < kBins; i += blockDim.x) h[i] = 0;
   __syncthreads();
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    int len = off[t + 1] - off[t];
-    len = len < 0 ? 0 : (len >= kBins ? kBins - 1 : len);
-    atomicAdd(&h[len], 1);
-  }
+  const int t = blockIdx.x * kSortBlock + threadIdx.x;
+  if (t < n) atomicAdd(&h[lengthBin(off, t)], 1);
   __syncthreads();
-  for (int i = threadIdx.x; i < kBins; i += blockDim.x)
-    if (h[i]) atomicAdd(&bins[i], h[i]);
+  for (int i = threadIdx.x; i < kBins; i += blockDim.x) counts[i * nb + blockIdx.x] = h[i];
 }
 
-// exclusive scan over bins in descending length order -> cursor per bin
-__global__ void queueScan(int32_t* bins) {
+// exclusive scan of the counts in the order (bin 63 .. 0) x (block 0 .. nb-1),
+// one block of kSortBlock threads, each over a contiguous chunk
+__global__ void __launch_bounds__(kSortBlock) queueScanCounts(int32_t* counts, int nb) {
+  __shared__ int32_t part[kSortBlock];
+  const long long total = (long long)kBins * nb;
+  const long long chunk = (total + kSortBlock - 1) / kSortBlock;
+  const long long lo = threadIdx.x * chunk < total ? threadIdx.x * chunk : total;
+  const long long hi = lo + chunk < total ? lo + chunk : total;
+  // entry j of the scan order is counts[(kBins - 1 - j / nb) * nb + j % nb]
+  auto at = [&](long long j) -> int32_t& {
+    return counts[(kBins - 1 - (int)(j / nb)) * (long long)nb + (int)(j % nb)];
+  };
+  int32_t sum = 0;
+  for (long long j = lo; j < hi; ++j) sum += at(j);
+  part[threadIdx.x] = sum;
+  __syncthreads();
   if (threadIdx.x == 0) {
     int32_t acc = 0;
-    for (int b = kBins - 1; b >= 0; --b) {
-      int32_t c = bins[b];
-      bins[b] = acc;
+    for (int i = 0; i < kSortBlock; ++i) {
+      const int32_t c = part[i];
+      part[i] = acc;
       acc += c;
     }
   }
+  __syncthreads();
+  int32_t acc = part[threadIdx.x];
+  for (long long j = lo; j < hi; ++j) {
+    const int32_t c = at(j);
+    at(j) = acc;
+    acc += c;
+  }
 }
 
-__global__ void queueScatter(const int32_t* __restrict__ off, int n, int32_t* cursor,
-                             int32_t* perm) {
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    int len = off[t + 1] - off[t];
-    len = len < 0 ? 0 : (len >= kBins ? kBins - 1 : len);
-    perm[atomicAdd(&cursor[len], 1)] = t;
+__global__ void __launch_bounds__(kSortBlock) queueScatterStable(const int32_t* __restrict__ off,
+                                                                 int n,
+                                                                 const int32_t* __restrict__ counts,
+                                                                 int nb, int32_t* perm) {
+  constexpr int kWarps = kSortBlock / 32;
+  __shared__ int32_t wc[kWarps][kBins];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < kWarps * kBins; i += blockDim.x) wc[i / kBins][i % kBins] = 0;
+  __syncthreads();
+  const int t = blockIdx.x * kSortBlock + threadIdx.x;
+  const int bin = t < n ? lengthBin(off, t) : -1;
+  const unsigned same = __match_any_sync(0xffffffffu, bin);
+  const int rank = __popc(same & ((1u << lane) - 1u));
+  if (bin >= 0 && rank == 0) wc[warp][bin] = __popc(same);
+  __syncthreads();
+  // exclusive prefix over the warps, per bin
+  for (int b = threadIdx.x; b < kBins; b += blockDim.x) {
+    int32_t acc = 0;
+    for (int w = 0; w < kWarps; ++w) {
+      const int32_t c = wc[w][b];
+      wc[w][b] = acc;
+      acc += c;
+    }
   }
+  __syncthreads();
+  if (bin >= 0) perm[counts[bin * nb + blockIdx.x] + wc[warp][bin] + rank] = t;
 }
 
 }  // namespace
@@ -232,7 +281,8 @@ ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, int
   if ((e = c.rec.ensure(compBytes(n, maxStates, 1, recordStateBytes(precision)))) ||
       (e = c.perm.ensure((size_t)n * sizeof(int32_t) + 16)) ||
       (e = c.tip.ensure((size_t)n * sizeof(int32_t) + 16)) ||
-      (e = c.ticket.ensure(sizeof(int32_t) * (kBins + 1))))
+      (e = c.sortCounts.ensure(sortCountsBytes(n))) ||
+      (e = c.ticket.ensure(sizeof(int32_t))))
     return cudaFail(e, "scratch allocation");
   return CK_OK;
 }
@@ -248,18 +298,17 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
   const int maxStates = dout.max_states;
   cudaError_t e;
   int32_t* dTicket = (int32_t*)c.ticket.p;
-  int32_t* dBins = dTicket + 1;
   int launches = 0;
-  cudaMemsetAsync(dTicket, 0, sizeof(int32_t) * (kBins + 1), st);
+  cudaMemsetAsync(dTicket, 0, sizeof(int32_t), st);
   if (n > 0) cudaMemsetAsync(c.tip.p, 0xff, sizeof(int32_t) * (size_t)n, st);
   const int32_t* perm = nullptr;
   if (h->sortQueue && n > 0) {
-    const int tb = 256;
-    int gb = (n + tb - 1) / tb;
-    if (gb > h->smCount * 8) gb = h->smCount * 8;
-    queueHistogram<<<gb, tb, 0, st>>>(din.seq_offsets, n, dBins);
-    queueScan<<<1, 32, 0, st>>>(dBins);
-    queueScatter<<<gb, tb, 0, st>>>(din.seq_offsets, n, dBins, (int32_t*)c.perm.p);
+    const int nb = sortBlocks(n);
+    int32_t* counts = (int32_t*)c.sortCounts.p;
+    queueBlockHist<<<nb, kSortBlock, 0, st>>>(din.seq_offsets, n, counts, nb);
+    queueScanCounts<<<1, kSortBlock, 0, st>>>(counts, nb);
+    queueScatterStable<<<nb, kSortBlock, 0, st>>>(din.seq_offsets, n, counts, nb,
+                                                  (int32_t*)c.perm.p);
     launches += 3;
     perm = (const int32_t*)c.perm.p;
   }
@@ -654,7 +703,7 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
     key.tune = tn;
     key.stream = st;
     key.scratch[0] = h->ctx.rec.p;
-    key.scratch[1] = nullptr;
+    key.scratch[1] = h->ctx.sortCounts.p;
     key.scratch[2] = nullptr;
     key.scratch[3] = h->ctx.perm.p;
     key.scratch[4] = h->ctx.ticket.p;

@@ -47,8 +47,9 @@ int occupancyBlocks(int precision, int variant, int tpb);
 // the ordered work queue and its ticket. A handle owns one; the serving loop
 // owns one per stream.
 struct FitContext {
-  DevBuf rec, perm, ticket, tip;
+  DevBuf rec, perm, ticket, tip, sortCounts;
   void release() {
+    sortCounts.release();
     tip.release();
     rec.release();
     perm.release();
@@ -64,6 +65,10 @@ DevOptions toDevOptions(const ck_options& o);
 MatConst makeMatConst();
 DevSurface toDevSurface(const ck_surface& s);
 size_t recordStateBytes(int precision);
+// the work-queue sort: blocks of kSortBlock tracks, 64 length bins each
+constexpr int kSortBlock = 1024;
+inline int sortBlocks(int n) { return n > 0 ? (n + kSortBlock - 1) / kSortBlock : 1; }
+inline size_t sortCountsBytes(int n) { return sizeof(int32_t) * 64 * (size_t)sortBlocks(n); }
 size_t recordBytesPerTrack(int maxStates, int precision);
 ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, int precision);
 ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,

@@ -16,8 +16,8 @@
 //   - the scratch holds kStaticScratchBytes (32 MiB); a batch that needs more
 //     (see ck_static_scratch_bytes) is rejected with CK_ERR_SCRATCH_LIMIT;
 //   - nothing in the scratch has to start at zero: every call clears the
-//     queue ticket and the length histogram itself and writes each track's
-//     tip and records before reading them;
+//     queue ticket itself and writes the length histograms, each track's tip
+//     and its records before reading them;
 //   - there is one array per device, shared by every handle of this library
 //     on that device: calls whose work overlaps on the device (different
 //     streams, or different handles, without ordering between them) race on
@@ -39,7 +39,7 @@ namespace {
 
 constexpr size_t kStaticScratchBytes = size_t(32) << 20;
 constexpr size_t kAlign = 256;
-constexpr size_t kTicketBytes = 1024;  // queue ticket + 64 length bins
+constexpr size_t kTicketBytes = 256;  // the queue ticket
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_staticScratch[kStaticScratchBytes];
@@ -51,7 +51,7 @@ size_t roundUp(size_t b) { return (b + kAlign - 1) & ~(kAlign - 1); }
 
 // Scratch layout for n tracks of up to maxStates states.
 struct Layout {
-  size_t rec, perm, tip, ticket, total;
+  size_t rec, perm, tip, sortCounts, ticket, total;
 };
 
 Layout layoutFor(int n, int maxStates, int precision) {
@@ -60,8 +60,9 @@ Layout layoutFor(int n, int maxStates, int precision) {
   l.rec = roundUp(ns * recordStateBytes(precision));
   l.perm = roundUp((size_t)n * sizeof(int32_t));
   l.tip = roundUp((size_t)n * sizeof(int32_t));
+  l.sortCounts = roundUp(sortCountsBytes(n));
   l.ticket = kTicketBytes;
-  l.total = l.rec + l.perm + l.tip + l.ticket;
+  l.total = l.rec + l.perm + l.tip + l.sortCounts + l.ticket;
   return l;
 }
 
@@ -128,6 +129,7 @@ ck_status ck_fit_batch_static(ck_handle* h, const ck_options* opt, const ck_batc
   view(c.rec, l.rec);
   view(c.perm, l.perm);
   view(c.tip, l.tip);
+  view(c.sortCounts, l.sortCounts);
   view(c.ticket, l.ticket);
   cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
   const Tune tn = h->tune[opt->precision];
