@@ -357,6 +357,7 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
     e = launchFit(fp, opt.precision, tn, grid, st);
     if (e != cudaSuccess) return cudaFail(e, "fit kernel launch");
     ++launches;
+    if (timed) cudaEventRecordWithFlags(h->evMid, st, recFlags);
     e = launchSmooth(fp, opt.precision, st);
     if (e != cudaSuccess) return cudaFail(e, "smoother kernel launch");
     ++launches;
@@ -476,7 +477,8 @@ ck_status ck_create(const ck_config* cfg, ck_handle** out) {
   cudaDeviceGetAttribute(&h->smCount, cudaDevAttrMultiProcessorCount, cfg->device);
   if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaEventCreate(&h->ev0)) != cudaSuccess ||
-      (e = cudaEventCreate(&h->ev1)) != cudaSuccess) {
+      (e = cudaEventCreate(&h->ev1)) != cudaSuccess ||
+      (e = cudaEventCreate(&h->evMid)) != cudaSuccess) {
     delete h;
     return cudaFail(e, "stream/event creation");
   }
@@ -575,6 +577,7 @@ ck_status ck_destroy(ck_handle* h) {
   if (h->dNodes) cudaFree(h->dNodes);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->evMid) cudaEventDestroy(h->evMid);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return CK_OK;
@@ -766,6 +769,21 @@ ck_status ck_last_kernel_ms(ck_handle* h, double* ms) {
   e = cudaEventElapsedTime(&f, h->ev0, h->ev1);
   if (e != cudaSuccess) return cudaFail(e, "event elapsed");
   *ms = f;
+  return CK_OK;
+}
+
+ck_status ck_last_kernel_split_ms(ck_handle* h, double* filter_ms, double* smoother_ms) {
+  if (!h || !filter_ms || !smoother_ms) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!h->lastTimed) return fail(CK_ERR_NOT_READY, "no timed batch");
+  cudaSetDevice(h->device);
+  cudaError_t e = cudaEventSynchronize(h->ev1);
+  if (e != cudaSuccess) return cudaFail(e, "event synchronize");
+  float a = 0, b = 0;
+  if ((e = cudaEventElapsedTime(&a, h->ev0, h->evMid)) != cudaSuccess ||
+      (e = cudaEventElapsedTime(&b, h->evMid, h->ev1)) != cudaSuccess)
+    return cudaFail(e, "event elapsed");
+  *filter_ms = a;
+  *smoother_ms = b;
   return CK_OK;
 }
 

@@ -82,7 +82,7 @@ struct ck_handle {
   int device = 0;
   int smCount = 1;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evMid = nullptr;
   ck::DevSurface* dSurfaces = nullptr;
   double2* dTrig = nullptr;
   int nSurfaces = 0;

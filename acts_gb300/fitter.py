@@ -63,6 +63,7 @@ def lib():
         L.ck_static_scratch_bytes.restype = C.c_int64
         L.ck_static_scratch_capacity.restype = C.c_int64
         L.ck_sync.argtypes = [C.c_void_p]
+        L.ck_last_kernel_split_ms.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         L.ck_atan2_mixed.argtypes = [C.c_void_p, C.c_int32, P(C.c_double), P(C.c_double),
                                      P(C.c_double)]
         L.ck_last_kernel_ms.argtypes = [C.c_void_p, P(C.c_double)]
@@ -274,6 +275,12 @@ class CudaKalman:
         ms = C.c_double()
         _check(lib().ck_last_kernel_ms(self._h, C.byref(ms)))
         return ms.value
+
+    def last_kernel_split_ms(self):
+        """(forward-filter ms, smoother ms) of the most recent timed batch."""
+        a, b = C.c_double(), C.c_double()
+        _check(lib().ck_last_kernel_split_ms(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def last_launch_count(self):
         n = C.c_int32()

@@ -278,6 +278,16 @@ def accuracy_report(b, r64, rmx, n):
             "chi2ndf_fp64": c64, "chi2ndf_mixed": cmx}
 
 
+# Per-track figures of the ncu capture summarised in
+# profiles/fit_smooth_kernels_barrel200k.md (barrel, 200k tracks, ten states).
+NCU_PER_TRACK = {
+    "mixed_filter_fp64_flops": 8.5e3, "mixed_filter_fp32_flops": 33.7e3,
+    "mixed_filter_dram_bytes": 5.65e3, "mixed_filter_fp64_pipe_busy": 0.556,
+    "fp64_filter_fp64_flops": 44.4e3, "fp64_filter_dram_bytes": 10.14e3,
+    "fp64_filter_fp64_pipe_busy": 0.638,
+}
+
+
 def best_of_tune_log(log):
     """The fastest entry of an autotuner log ("v3 tpb256 bps1 12.345ms; ...")."""
     best = None
@@ -405,11 +415,13 @@ def native_arm(args):
         fit.fit_batch_raw(opt, bi, bo, sp)
         torch.cuda.synchronize(dev)
         kernel_ms.append(fit.last_kernel_ms())
+        split_ms = fit.last_kernel_split_ms()
         ms_total = replicas.max_over_ranks(ms_total)
         status = keep_out["status"].cpu().numpy()
         results[name] = {"ms_per_step": ms_total / args.steps,
                          "tracks_per_s": n * world / (ms_total / args.steps / 1e3),
                          "kernel_ms": float(np.mean(kernel_ms)),
+                         "filter_kernel_ms": split_ms[0], "smoother_kernel_ms": split_ms[1],
                          "launches_per_step": launches_per_step,
                          "ok_fraction": float(np.mean(status == 0)),
                          "launch_config": fit.launch_config(opt.precision),
@@ -449,34 +461,55 @@ def native_arm(args):
             torch.distributed.barrier()
         return 0
 
-    # ---- roofline of the fit kernel (mixed is the headline form)
+    # ---- roofline of the dominant kernel of the mixed step: the forward
+    # filter fitKernel*<float,float>. It is bound by the FP64 pipe. The
+    # algorithmic FP64 work of the mixed formulation per track and its DRAM
+    # bytes per track come from the ncu capture summarised in
+    # profiles/fit_smooth_kernels_barrel200k.md (same kernels, 200k-track
+    # case; both scale with the track count); the duration is measured here.
     from oracle import kforacle
 
     flops = kforacle.count_flops(det, b, forms["fp64"], 0, 300)
-    peak64 = fit.fp_peak_gflops(abi.PRECISION_FP64)
-    peak32 = fit.fp_peak_gflops(abi.PRECISION_MIXED)
-    k64 = results["fp64"]["kernel_ms"]
-    kmx = results["mixed"]["kernel_ms"]
-    ach64 = flops["flops"] * n / (k64 * 1e-3) / 1e12
-    achmx = flops["flops"] * n / (kmx * 1e-3) / 1e12
-    hbm_bytes = 1.2e3 * n  # inputs ~0.9 KB + outputs per track, lower bound
-    roofline = {"bound": "fp64", "kernel": "fitKernel<float,float> (mixed form)",
-                "achieved": round(achmx, 4), "peak": round(peak64 / 1e3, 4), "unit": "TFLOP/s",
-                "frac": round(achmx / (peak64 / 1e3), 4), "traffic": None,
-                "algorithmic_flops_per_track": round(flops["flops"], 1),
-                "flops_definition": "FP64 add/sub/mul/div/sqrt of the reference formulation "
-                                    "(dense products, 8x8 transport), counted by the oracle's "
-                                    "counting scalar over %d tracks" % flops["tracks"],
+    peak64 = fit.fp_peak_gflops(abi.PRECISION_FP64) / 1e3
+    peak32 = fit.fp_peak_gflops(abi.PRECISION_MIXED) / 1e3
+    per_track = NCU_PER_TRACK
+    fwd_mx = results["mixed"]["filter_kernel_ms"] * 1e-3
+    fwd_64 = results["fp64"]["filter_kernel_ms"] * 1e-3
+    ach_mx = per_track["mixed_filter_fp64_flops"] * n / fwd_mx / 1e12
+    ach_64 = per_track["fp64_filter_fp64_flops"] * n / fwd_64 / 1e12
+    roofline = {"bound": "fp64", "kernel": "fitKernelCompact<float,float> (mixed forward filter)",
+                "achieved": round(ach_mx, 4), "peak": round(peak64, 4), "unit": "TFLOP/s",
+                "frac": round(ach_mx / peak64, 4),
+                "traffic": int(per_track["mixed_filter_dram_bytes"] * n),
+                "algorithmic_flops_per_track": per_track["mixed_filter_fp64_flops"],
+                "flops_definition": "FP64 flops of the mixed formulation's forward filter per "
+                                    "track (the FP32 work, %.1f kflop/track, runs on a 63x "
+                                    "faster pipe), counted by ncu" %
+                                    (per_track["mixed_filter_fp32_flops"] / 1e3),
+                "duration_ms": round(fwd_mx * 1e3, 3),
+                "fp64_pipe_busy_ncu": per_track["mixed_filter_fp64_pipe_busy"],
                 "peak_source": "measured live: FP64 FMA loop (ck_fp_peak_gflops); "
                                "MEASURED_PEAKS.json holds no FP64 figure",
-                "fp64_form": {"achieved": round(ach64, 4), "frac": round(ach64 / (peak64 / 1e3), 4),
-                              "kernel_ms": k64},
-                "fp32_peak_tflops": round(peak32 / 1e3, 3),
-                "hbm_achieved_gbs": round(hbm_bytes / (kmx * 1e-3) / 1e9, 1)}
+                "traffic_source": "ncu dram__bytes_read+write per track x tracks",
+                "fp64_form": {"kernel": "fitKernelCompact<double,double>",
+                              "achieved": round(ach_64, 4), "frac": round(ach_64 / peak64, 4),
+                              "duration_ms": round(fwd_64 * 1e3, 3),
+                              "fp64_pipe_busy_ncu": per_track["fp64_filter_fp64_pipe_busy"],
+                              "traffic": int(per_track["fp64_filter_dram_bytes"] * n)},
+                "reference_formulation": {
+                    "flops_per_track": round(flops["flops"], 1),
+                    "definition": "FP64 flops of the reference's dense formulation (8x8 "
+                                  "transport, dense products), counted by the oracle's counting "
+                                  "scalar over %d tracks" % flops["tracks"],
+                    "equivalent_tflops_mixed": round(flops["flops"] * n /
+                                                     (results["mixed"]["kernel_ms"] * 1e-3) / 1e12, 3),
+                    "equivalent_tflops_fp64": round(flops["flops"] * n /
+                                                    (results["fp64"]["kernel_ms"] * 1e-3) / 1e12, 3)},
+                "fp32_peak_tflops": round(peak32, 3)}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        roofline["hbm_frac_of_measured"] = round(roofline["hbm_achieved_gbs"] / peaks["hbm_gbs"], 5)
-    except (OSError, KeyError, ValueError):
+        roofline["hbm_gbs_of_measured"] = round(roofline["traffic"] / fwd_mx / 1e9 / peaks["hbm_gbs"], 5)
+    except (OSError, KeyError, ValueError, ZeroDivisionError):
         pass
 
     acc = accuracy_report(b, snapshots["fp64"], snapshots["mixed"], min(n, 100000))

@@ -329,6 +329,10 @@ int64_t ck_static_scratch_capacity(void);
  * launching stream around the fit kernel): milliseconds. */
 ck_status ck_last_kernel_ms(ck_handle* h, double* ms);
 
+/* The same split into the forward-filter kernel and the smoother kernel
+ * (milliseconds each). */
+ck_status ck_last_kernel_split_ms(ck_handle* h, double* filter_ms, double* smoother_ms);
+
 /* Number of kernels launched by the most recent ck_fit_batch call. */
 ck_status ck_last_launch_count(ck_handle* h, int32_t* n);
 
