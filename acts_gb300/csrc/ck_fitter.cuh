@@ -1247,6 +1247,30 @@ __global__ void __launch_bounds__(BLOCK, MINB) fitKernel(FitParams fp) {
 // on full warps. On GB300 an FP64 warp instruction holds the SM's FP64 unit
 // for 16 clocks however few of its lanes are active, so the lanes a warp
 // carries are the FP64 throughput it gets.
+// One phase step of a slot; fetching threads take one ticket per warp (the
+// threads of the warp that run this call together).
+template <typename P, typename CV>
+__device__ __forceinline__ void advanceSlot(const FitParams& fp, Lane<P, CV>& L, int c, int lane) {
+  if (c == PH_FETCH) {
+    const unsigned act = __activemask();
+    const int leader = __ffs(act) - 1;
+    int qb = 0;
+    if (lane == leader) qb = atomicAdd(fp.ticket, __popc(act));
+    qb = __shfl_sync(act, qb, leader);
+    const int q = qb + __popc(act & ((1u << lane) - 1u));
+    if (q >= fp.n_queue) {
+      L.phase = PH_DONE;
+    } else {
+      L.q = q;
+      L.start(fp, q, fp.perm ? __ldg(&fp.perm[q]) : q);
+    }
+  } else if (c == PH_STEP) {
+    L.step(fp, L.q);
+  } else {
+    L.surface(fp, L.q);
+  }
+}
+
 template <typename P, typename CV, int S>
 __global__ void __launch_bounds__(S, 1) fitKernelCompact(FitParams fp) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1297,26 +1321,9 @@ __global__ void __launch_bounds__(S, 1) fitKernelCompact(FitParams fp) {
     __syncthreads();
     if (tid < nItems) {
       const int slot = items[tid];
+      // the phase step works on a register copy of the slot's state
       Lane<P, CV> L = st[slot];
-      if (c == PH_FETCH) {
-        // one ticket per warp for its fetching threads
-        const unsigned act = __activemask();
-        const int leader = __ffs(act) - 1;
-        int qb = 0;
-        if (lane == leader) qb = atomicAdd(fp.ticket, __popc(act));
-        qb = __shfl_sync(act, qb, leader);
-        const int q = qb + __popc(act & ((1u << lane) - 1u));
-        if (q >= fp.n_queue) {
-          L.phase = PH_DONE;
-        } else {
-          L.q = q;
-          L.start(fp, q, fp.perm ? __ldg(&fp.perm[q]) : q);
-        }
-      } else if (c == PH_STEP) {
-        L.step(fp, L.q);
-      } else {
-        L.surface(fp, L.q);
-      }
+      advanceSlot(fp, L, c, lane);
       st[slot] = L;
     }
     __syncthreads();
