@@ -238,11 +238,12 @@ size_t compBytes(int n, int maxStates, int C, size_t elem) {
 void loadTuneCache(ck_handle* h) {
   if (h->cachePath.empty()) return;
   std::ifstream f(h->cachePath);
-  int p, v, tpb, bps;
-  while (f >> p >> v >> tpb >> bps) {
-    if (p < 0 || p >= CK_NUM_PRECISIONS || !validLaunch(v, tpb) || bps <= 0)
+  int p, v, tpb, bps, spr;
+  while (f >> p >> v >> tpb >> bps >> spr) {
+    if (p < 0 || p >= CK_NUM_PRECISIONS || !validLaunch(v, tpb) || bps <= 0 || spr < 1 ||
+        spr > 64)
       continue;
-    h->tune[p] = {v, tpb, bps, true};
+    h->tune[p] = {v, tpb, bps, spr, 1};
   }
 }
 
@@ -251,7 +252,8 @@ void saveTuneCache(ck_handle* h) {
   std::ofstream f(h->cachePath);
   for (int p = 0; p < CK_NUM_PRECISIONS; ++p)
     if (h->tune[p].tuned)
-      f << p << " " << h->tune[p].variant << " " << h->tune[p].tpb << " " << h->tune[p].bps << "\n";
+      f << p << " " << h->tune[p].variant << " " << h->tune[p].tpb << " " << h->tune[p].bps << " "
+        << h->tune[p].spr << "\n";
 }
 
 cudaError_t launchFit(const FitParams& fp, int precision, const Tune& tn, int grid,
@@ -340,6 +342,7 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
   fp.out = dout;
   fp.surfaces = h->dSurfaces;
   fp.trig = h->dTrig;
+  fp.steps_per_round = tn.spr > 0 ? tn.spr : 1;
   fp.n_surfaces = h->nSurfaces;
   fp.field = h->field;
   fp.mc = h->mc;
@@ -549,7 +552,8 @@ ck_status ck_create(const ck_config* cfg, ck_handle** out) {
     h->tune[p].tpb = fixedTpb ? std::min(cfg->threads_per_block, kFitMaxBlock)
                               : variantBlock(kDefaultVariant);
     h->tune[p].bps = cfg->blocks_per_sm > 0 ? cfg->blocks_per_sm : 0;
-    h->tune[p].tuned = false;
+    h->tune[p].spr = kDefaultStepsPerRound[p];
+    h->tune[p].tuned = 0;
   }
   loadTuneCache(h);
   for (int p = 0; p < CK_NUM_PRECISIONS; ++p) {
@@ -816,7 +820,19 @@ ck_status ck_set_launch_config(ck_handle* h, int32_t precision, int32_t variant,
   std::lock_guard<std::mutex> lock(h->mu);
   int maxB = occupancyBlocks(precision, variant, tpb);
   if (bps > maxB) return fail(CK_ERR_INVALID_ARGUMENT, "more blocks per SM than fit");
-  h->tune[precision] = {variant, tpb, bps, true};
+  h->tune[precision] = {variant, tpb, bps, h->tune[precision].spr, 1};
+  return CK_OK;
+}
+
+ck_status ck_set_steps_per_round(ck_handle* h, int32_t precision, int32_t steps) {
+  if (!h || precision < 0 || precision >= CK_NUM_PRECISIONS || steps < 1 || steps > 64)
+    return fail(CK_ERR_INVALID_ARGUMENT, "bad precision, or steps per round outside [1, 64]");
+  std::lock_guard<std::mutex> lock(h->mu);
+  h->tune[precision].spr = steps;
+  if (h->graphExec) {
+    cudaGraphExecDestroy(h->graphExec);
+    h->graphExec = nullptr;
+  }
   return CK_OK;
 }
 
@@ -842,36 +858,46 @@ ck_status ck_autotune(ck_handle* h, const ck_options* opt, const ck_batch_in* in
   Tune best = h->tune[p];
   double bestMs = 1e30;
   std::string log;
+  // candidates: every variant and block size, resident blocks per SM at the
+  // maximum, 3/4 and 1/2 of it; the compaction variants at the maximum with
+  // 1-4 Runge-Kutta trials per round
+  std::vector<Tune> cands;
   for (int v = 0; v < kNumFitVariants; ++v)
     for (int tpb : {32, 64, 128, 256}) {
       if (!validLaunch(v, tpb)) continue;
       const int maxB = occupancyBlocks(p, v, tpb);
       if (maxB <= 0) continue;
-      std::vector<int> cands = {maxB, std::max(1, (maxB * 3) / 4), std::max(1, maxB / 2)};
-      for (size_t ci = 0; ci < cands.size(); ++ci) {
-        if (ci > 0 && cands[ci] == cands[ci - 1]) continue;
-        {
-          std::lock_guard<std::mutex> lock(h->mu);
-          h->tune[p] = {v, tpb, cands[ci], true};
-        }
-        double tot = 0;
-        for (int rep = 0; rep < 3; ++rep) {
-          ck_status s = ck_fit_batch(h, opt, in, out, nullptr);
-          if (s != CK_OK) return s;
-          double ms = 0;
-          if ((s = ck_last_kernel_ms(h, &ms)) != CK_OK) return s;
-          if (rep > 0) tot += ms;
-        }
-        const double ms = tot / 2;
-        char buf[128];
-        std::snprintf(buf, sizeof(buf), "v%d tpb%d bps%d %.3fms; ", v, tpb, cands[ci], ms);
-        log += buf;
-        if (ms < bestMs) {
-          bestMs = ms;
-          best = {v, tpb, cands[ci], true};
-        }
+      if (variantBlock(v)) {
+        for (int spr = 1; spr <= 4; ++spr) cands.push_back({v, tpb, maxB, spr, 1});
+      } else {
+        const int bs[3] = {maxB, std::max(1, (maxB * 3) / 4), std::max(1, maxB / 2)};
+        for (int i = 0; i < 3; ++i)
+          if (i == 0 || bs[i] != bs[i - 1]) cands.push_back({v, tpb, bs[i], 1, 1});
       }
     }
+  for (const Tune& cand : cands) {
+    {
+      std::lock_guard<std::mutex> lock(h->mu);
+      h->tune[p] = cand;
+    }
+    double tot = 0;
+    for (int rep = 0; rep < 3; ++rep) {
+      ck_status s = ck_fit_batch(h, opt, in, out, nullptr);
+      if (s != CK_OK) return s;
+      double ms = 0;
+      if ((s = ck_last_kernel_ms(h, &ms)) != CK_OK) return s;
+      if (rep > 0) tot += ms;
+    }
+    const double ms = tot / 2;
+    char buf[128];
+    std::snprintf(buf, sizeof(buf), "v%d tpb%d bps%d spr%d %.3fms; ", cand.variant, cand.tpb,
+                  cand.bps, cand.spr, ms);
+    log += buf;
+    if (ms < bestMs) {
+      bestMs = ms;
+      best = cand;
+    }
+  }
   {
     std::lock_guard<std::mutex> lock(h->mu);
     h->tune[p] = best;

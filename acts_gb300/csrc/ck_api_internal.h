@@ -23,10 +23,11 @@ struct DevBuf {
 
 // Launch shape of the fit kernel for one precision.
 struct Tune {
-  int variant;  // register-cap variant (0: 255, 1: 168, 2: 128 registers)
+  int variant;  // kernel variant (ck_launch.h)
   int tpb;      // threads per block
   int bps;      // resident blocks per SM (grid = SMs * bps)
-  bool tuned;
+  int spr;      // Runge-Kutta trials per round (compaction variants)
+  int tuned;
 };
 
 // Identity of a captured batch pipeline.

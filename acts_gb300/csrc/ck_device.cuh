@@ -646,10 +646,24 @@ CK_D MatEffects materialEffects(const MatConst& C, const DevSurface* __restrict_
 struct Inv2 {
   double a00, a01, a10, a11;
 };
-// Eigen's fixed 2x2 inverse (adjugate / determinant)
+// 1/d in FP64 from an FP32 reciprocal and two FP64 Newton steps (correct to
+// about an ulp; no FP64 divide). Falls back to the divide where d is outside
+// the FP32 range.
+CK_D double rcpRefined(double d) {
+  const float f = (float)d;
+  if (!(fabsf(f) > 1e-30f && fabsf(f) < 1e30f)) return 1.0 / d;
+  double y = (double)(1.0f / f);
+  y = fma(y, fma(-d, y, 1.0), y);
+  y = fma(y, fma(-d, y, 1.0), y);
+  return y;
+}
+
+// Eigen's fixed 2x2 inverse (adjugate / determinant); FASTRCP takes the
+// reciprocal of the determinant with rcpRefined (mixed form)
+template <bool FASTRCP = false>
 CK_D Inv2 inverse2(double m00, double m01, double m10, double m11) {
   double det = m00 * m11 - m01 * m10;
-  double invdet = 1.0 / det;
+  double invdet = FASTRCP ? rcpRefined(det) : 1.0 / det;
   Inv2 r;
   r.a00 = m11 * invdet;
   r.a10 = -m10 * invdet;
@@ -661,7 +675,7 @@ CK_D Inv2 inverse2(double m00, double m01, double m10, double m11) {
 // 6x6 inverse of a symmetric matrix given packed, by LU with partial
 // pivoting (the algorithm of Eigen's fixed-size inverse for N > 4). The
 // divisions by the pivots are multiplications by one reciprocal per pivot.
-template <typename T>
+template <typename T, bool FASTRCP = false>
 CK_D void inverse6(const T* __restrict__ Cp, double inv[36]) {
   double lu[36];
 #pragma unroll
@@ -698,7 +712,7 @@ CK_D void inverse6(const T* __restrict__ Cp, double inv[36]) {
         }
       }
     }
-    const double rpiv = 1.0 / lu[k * 6 + k];
+    const double rpiv = FASTRCP ? rcpRefined(lu[k * 6 + k]) : 1.0 / lu[k * 6 + k];
 #pragma unroll
     for (int i = k + 1; i < 6; ++i) {
       double l = lu[i * 6 + k] * rpiv;
@@ -709,7 +723,7 @@ CK_D void inverse6(const T* __restrict__ Cp, double inv[36]) {
   }
   double rdiag[6];
 #pragma unroll
-  for (int i = 0; i < 6; ++i) rdiag[i] = 1.0 / lu[i * 6 + i];
+  for (int i = 0; i < 6; ++i) rdiag[i] = FASTRCP ? rcpRefined(lu[i * 6 + i]) : 1.0 / lu[i * 6 + i];
 #pragma unroll
   for (int c = 0; c < 6; ++c) {
     double y[6];
@@ -733,11 +747,12 @@ CK_D void inverse6(const T* __restrict__ Cp, double inv[36]) {
 // ------------------------------------------------------ Kalman update (N=2)
 // GainMatrixUpdater::visitMeasurementImpl<2>. pred/P packed symmetric;
 // writes filt and F (packed). Returns false on NaN gain (UpdateFailed).
+template <bool FASTRCP = false>
 CK_D bool kalmanUpdate(const double pred[6], const double Pp[21], double m0, double m1,
                        const double V[4], bool joseph, double filt[6], double F[21],
                        double& chi2) {
   // S = H P H^T + V ; K = P H^T S^-1
-  Inv2 Si = inverse2(Pp[sidx(0, 0)] + V[0], Pp[sidx(0, 1)] + V[1], Pp[sidx(1, 0)] + V[2],
+  Inv2 Si = inverse2<FASTRCP>(Pp[sidx(0, 0)] + V[0], Pp[sidx(0, 1)] + V[1], Pp[sidx(1, 0)] + V[2],
                      Pp[sidx(1, 1)] + V[3]);
   double K[6][2];
   bool nan = false;
@@ -782,7 +797,7 @@ CK_D bool kalmanUpdate(const double pred[6], const double Pp[21], double m0, dou
   // chi2 = r^T [(I - H K) V]^-1 r with r = m - H filt
   const double s0 = m0 - filt[0], s1 = m1 - filt[1];
   const double b00 = 1.0 - K[0][0], b01 = -K[0][1], b10 = -K[1][0], b11 = 1.0 - K[1][1];
-  Inv2 Mi = inverse2(b00 * V[0] + b01 * V[2], b00 * V[1] + b01 * V[3], b10 * V[0] + b11 * V[2],
+  Inv2 Mi = inverse2<FASTRCP>(b00 * V[0] + b01 * V[2], b00 * V[1] + b01 * V[3], b10 * V[0] + b11 * V[2],
                      b10 * V[1] + b11 * V[3]);
   const double t0 = s0 * Mi.a00 + s1 * Mi.a10;
   const double t1 = s0 * Mi.a01 + s1 * Mi.a11;
@@ -791,10 +806,11 @@ CK_D bool kalmanUpdate(const double pred[6], const double Pp[21], double m0, dou
 }
 
 // calculatePredictedChi2 (TrackHelpers.hpp:563-694)
+template <bool FASTRCP = false>
 CK_D double predictedChi2(const double pred[6], const double Pp[21], double m0, double m1,
                           const double V[4]) {
   const double r0 = m0 - pred[0], r1 = m1 - pred[1];
-  Inv2 Ri = inverse2(V[0] + Pp[sidx(0, 0)], V[1] + Pp[sidx(0, 1)], V[2] + Pp[sidx(1, 0)],
+  Inv2 Ri = inverse2<FASTRCP>(V[0] + Pp[sidx(0, 0)], V[1] + Pp[sidx(0, 1)], V[2] + Pp[sidx(1, 0)],
                      V[3] + Pp[sidx(1, 1)]);
   const double t0 = r0 * Ri.a00 + r1 * Ri.a10;
   const double t1 = r0 * Ri.a01 + r1 * Ri.a11;
@@ -813,7 +829,7 @@ CK_D bool smoothStep(const double filt[6], const GP Pf[21], const double pp[6], 
                      const GP* J, const double ps[6], const GP Psp[21], double sm[6],
                      GP Ps[21]) {
   double inv[36];
-  inverse6(Ppp, inv);
+  inverse6<GP, sizeof(GP) == sizeof(float)>(Ppp, inv);
   // G = (Pf J^T) Pinv
   GP PJ[36];
 #pragma unroll

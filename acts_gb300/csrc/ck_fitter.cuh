@@ -616,11 +616,13 @@ struct Lane {
 #pragma unroll
       for (int i = 0; i < 4; ++i) V[i] = __ldg(&fp.meas_cov[4 * (size_t)mi + i]);
       bool outlier = false;
-      if (fp.opt.useOutlierCut) outlier = predictedChi2(bp, Pp, mv0, mv1, V) > fp.opt.outlierChi2Cut;
+      constexpr bool kFastRcp = sizeof(P) == sizeof(float);
+      if (fp.opt.useOutlierCut)
+        outlier = predictedChi2<kFastRcp>(bp, Pp, mv0, mv1, V) > fp.opt.outlierChi2Cut;
       double chi2 = 0.0;
       if (!outlier) {
         double filt[6], F[21];
-        if (!kalmanUpdate(bp, Pp, mv0, mv1, V, fp.opt.joseph != 0, filt, F, chi2))
+        if (!kalmanUpdate<kFastRcp>(bp, Pp, mv0, mv1, V, fp.opt.joseph != 0, filt, F, chi2))
           return CK_TRACK_UPDATE_FAILED;
         flags |= CK_FLAG_HAS_MEASUREMENT;
 #pragma unroll
@@ -1265,7 +1267,8 @@ __device__ __forceinline__ void advanceSlot(const FitParams& fp, Lane<P, CV>& L,
       L.start(fp, q, fp.perm ? __ldg(&fp.perm[q]) : q);
     }
   } else if (c == PH_STEP) {
-    L.step(fp, L.q);
+    // up to steps_per_round Runge-Kutta trials while the track stays in STEP
+    for (int k = 0; k < fp.steps_per_round && L.phase == PH_STEP; ++k) L.step(fp, L.q);
   } else {
     L.surface(fp, L.q);
   }

@@ -113,6 +113,9 @@ struct FitParams {
   // lanes of each warp that take tracks: all 32 for large batches; fewer
   // when the batch is small, so that its tracks spread over all warps
   int lanes_per_warp;
+  // Runge-Kutta trials a STEP item of the compaction kernels may take in one
+  // round (>= 1)
+  int steps_per_round;
   int max_states;
   // outputs (device memory, ck_batch_out layout)
   ck_batch_out out;

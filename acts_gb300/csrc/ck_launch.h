@@ -13,6 +13,9 @@ namespace ck {
 constexpr int kNumFitVariants = 5;
 constexpr int kFitMaxBlock = 128;
 constexpr int kDefaultVariant = 3;
+// Runge-Kutta trials per round of the compaction kernels by precision
+// (FP64, mixed): measured best on the barrel and uneven workloads
+constexpr int kDefaultStepsPerRound[2] = {2, 3};
 // block size a variant requires (0: any multiple of 32 up to kFitMaxBlock)
 inline int variantBlock(int variant) { return variant == 3 ? 256 : (variant == 4 ? 128 : 0); }
 inline bool validLaunch(int variant, int tpb) {

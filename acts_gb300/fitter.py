@@ -63,6 +63,7 @@ def lib():
         L.ck_static_scratch_bytes.restype = C.c_int64
         L.ck_static_scratch_capacity.restype = C.c_int64
         L.ck_sync.argtypes = [C.c_void_p]
+        L.ck_set_steps_per_round.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
         L.ck_last_kernel_split_ms.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         L.ck_atan2_mixed.argtypes = [C.c_void_p, C.c_int32, P(C.c_double), P(C.c_double),
                                      P(C.c_double)]
@@ -281,6 +282,9 @@ class CudaKalman:
         a, b = C.c_double(), C.c_double()
         _check(lib().ck_last_kernel_split_ms(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def set_steps_per_round(self, precision, steps):
+        _check(lib().ck_set_steps_per_round(self._h, int(precision), int(steps)))
 
     def last_launch_count(self):
         n = C.c_int32()

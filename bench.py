@@ -289,14 +289,14 @@ NCU_PER_TRACK = {
 
 
 def best_of_tune_log(log):
-    """The fastest entry of an autotuner log ("v3 tpb256 bps1 12.345ms; ...")."""
+    """The fastest entry of an autotuner log ("v3 tpb256 bps1 spr3 12.345ms; ...")."""
     best = None
     for item in log.split(";"):
         parts = item.split()
-        if len(parts) == 4 and parts[3].endswith("ms"):
-            ms = float(parts[3][:-2])
+        if len(parts) >= 2 and parts[-1].endswith("ms"):
+            ms = float(parts[-1][:-2])
             if best is None or ms < best[1]:
-                best = (" ".join(parts[:3]), ms)
+                best = (" ".join(parts[:-1]), ms)
     return None if best is None else {"config": best[0], "kernel_ms": best[1],
                                       "configs_tried": len([x for x in log.split(";") if x.strip()])}
 

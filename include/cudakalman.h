@@ -352,6 +352,12 @@ ck_status ck_get_launch_config(ck_handle* h, int32_t precision,
 ck_status ck_set_launch_config(ck_handle* h, int32_t precision, int32_t variant,
                                int32_t threads_per_block, int32_t blocks_per_sm);
 
+/* Runge-Kutta trials a track may take per scheduling round of the
+ * block-compaction kernels, for one precision (1..64; defaults 2 for FP64,
+ * 3 for mixed; the autotuner also sweeps it). Results do not depend on it.
+ * No counterpart in the reference (a scheduling knob of this implementation). */
+ck_status ck_set_steps_per_round(ck_handle* h, int32_t precision, int32_t steps);
+
 /* Enables (default) or disables ordering the work queue by descending
  * surface-sequence length before the fit. */
 ck_status ck_sort_queue(ck_handle* h, int32_t enable);
