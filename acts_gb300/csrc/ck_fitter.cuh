@@ -110,6 +110,7 @@ struct Lane {
   bool navigationBreak, haveTarget;
   // ---- Kalman fitter actor
   int nStates, lastMeasurementIndex, measurementStates, nDistinct, lastSlSeq;
+  int measHint;  // where the next measurement lookup starts (distinct surfaces only)
   bool finished, coasting;
   double propLimit, kfLimit;
   int seq0, nSeq, m0, nMeas;
@@ -132,6 +133,25 @@ struct Lane {
     if (out.chi2_sum) out.chi2_sum[t] = 0.0;
     fp.tip[q] = -1;
     phase = PH_FETCH;
+  }
+
+  // findMeas when every measurement has its own surface: the search starts
+  // after the last match, where the next surface's measurement usually is
+  // (source links in propagation order); with repeated surfaces the first
+  // match in input order is the one the reference keeps, so the plain search
+  // runs.
+  CK_D int findMeasHinted(const FitParams& fp, int sid) {
+    if (nDistinct != nMeas) return findMeas(fp, sid);
+    int j = measHint;
+    for (int i = 0; i < nMeas; ++i) {
+      if (j >= nMeas) j = 0;
+      if (__ldg(&fp.meas_surf[m0 + j]) == sid) {
+        measHint = j + 1;
+        return m0 + j;
+      }
+      ++j;
+    }
+    return -1;
   }
 
   CK_D int findMeas(const FitParams& fp, int sid) const {
@@ -591,7 +611,7 @@ struct Lane {
       }
       return CK_TRACK_OK;
     }
-    const int mi = findMeas(fp, sid);
+    const int mi = findMeasHinted(fp, sid);
     if (mi >= 0) {
       CV J[36];
       transportToBound(sf, sp, l, J);
@@ -774,9 +794,14 @@ struct Lane {
       for (int j = 0; j < i; ++j) dup |= (__ldg(&fp.meas_surf[m0 + j]) == si);
       nDistinct += dup ? 0 : 1;
     }
+    // the last sequence position that carries a source link
     lastSlSeq = -1;
-    for (int k = 0; k < nSeq; ++k)
-      if (findMeas(fp, __ldg(&fp.seq_surf[seq0 + k])) >= 0) lastSlSeq = k;
+    for (int k = nSeq - 1; k >= 0; --k)
+      if (findMeas(fp, __ldg(&fp.seq_surf[seq0 + k])) >= 0) {
+        lastSlSeq = k;
+        break;
+      }
+    measHint = 0;
     propLimit = loopLimit(fp, fp.opt.pathLimit, false);
     kfLimit = kNotSet;
     surfaceIndex = -1;
