@@ -201,6 +201,8 @@ class ck_server_config(C.Structure):
         ("max_states", C.c_int32),
         ("max_batch_tracks", C.c_int32),
         ("components", C.c_uint32),
+        ("grid_blocks", C.c_int32),
+        ("steps_per_round", C.c_int32),
     ]
 
 

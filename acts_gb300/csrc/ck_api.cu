@@ -264,7 +264,9 @@ cudaError_t launchFit(const FitParams& fp, int precision, const Tune& tn, int gr
   }
 }
 
-int gridBlocksFor(ck_handle* h, const Tune& tn) { return h->smCount * tn.bps; }
+int gridBlocksFor(ck_handle* h, const Tune& tn) {
+  return tn.grid > 0 ? tn.grid : h->smCount * tn.bps;
+}
 
 size_t recordStateBytes(int precision) {
   return precision == CK_PRECISION_MIXED ? sizeof(RecState<float>) : sizeof(RecState<double>);
@@ -820,7 +822,15 @@ ck_status ck_set_launch_config(ck_handle* h, int32_t precision, int32_t variant,
   std::lock_guard<std::mutex> lock(h->mu);
   int maxB = occupancyBlocks(precision, variant, tpb);
   if (bps > maxB) return fail(CK_ERR_INVALID_ARGUMENT, "more blocks per SM than fit");
-  h->tune[precision] = {variant, tpb, bps, h->tune[precision].spr, 1};
+  h->tune[precision] = {variant, tpb, bps, h->tune[precision].spr, 1, h->tune[precision].grid};
+  return CK_OK;
+}
+
+ck_status ck_set_grid_blocks(ck_handle* h, int32_t precision, int32_t blocks) {
+  if (!h || precision < 0 || precision >= CK_NUM_PRECISIONS || blocks < 0)
+    return fail(CK_ERR_INVALID_ARGUMENT, "bad precision, or negative block count");
+  std::lock_guard<std::mutex> lock(h->mu);
+  h->tune[precision].grid = blocks;
   return CK_OK;
 }
 

@@ -28,6 +28,7 @@ struct Tune {
   int bps;      // resident blocks per SM (grid = SMs * bps)
   int spr;      // Runge-Kutta trials per round (compaction variants)
   int tuned;
+  int grid;     // blocks of the fit kernel's grid; 0: SMs * bps
 };
 
 // Identity of a captured batch pipeline.

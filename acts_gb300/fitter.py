@@ -64,6 +64,7 @@ def lib():
         L.ck_static_scratch_capacity.restype = C.c_int64
         L.ck_sync.argtypes = [C.c_void_p]
         L.ck_set_steps_per_round.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+        L.ck_set_grid_blocks.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
         L.ck_last_kernel_split_ms.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         L.ck_atan2_mixed.argtypes = [C.c_void_p, C.c_int32, P(C.c_double), P(C.c_double),
                                      P(C.c_double)]
@@ -285,6 +286,10 @@ class CudaKalman:
 
     def set_steps_per_round(self, precision, steps):
         _check(lib().ck_set_steps_per_round(self._h, int(precision), int(steps)))
+
+    def set_grid_blocks(self, precision, blocks):
+        """Grid of the forward-filter kernel (0: the whole GPU)."""
+        _check(lib().ck_set_grid_blocks(self._h, int(precision), int(blocks)))
 
     def last_launch_count(self):
         n = C.c_int32()

@@ -37,7 +37,8 @@ def _bind():
 
 class FitServer:
     def __init__(self, fitter, options, memory_budget_bytes=40 << 30, n_streams=4, max_states=24,
-                 max_batch_tracks=200000, components=abi.OUT_SMOOTHED):
+                 max_batch_tracks=200000, components=abi.OUT_SMOOTHED, grid_blocks=0,
+                 steps_per_round=0):
         L = _bind()
         cfg = abi.ck_server_config()
         cfg.memory_budget_bytes = int(memory_budget_bytes)
@@ -45,6 +46,8 @@ class FitServer:
         cfg.max_states = max_states
         cfg.max_batch_tracks = max_batch_tracks
         cfg.components = components
+        cfg.grid_blocks = int(grid_blocks)
+        cfg.steps_per_round = int(steps_per_round)
         self.max_states = max_states
         self.components = components
         self._opt = options

@@ -605,7 +605,9 @@ def serving_report(torch, precisions=("mixed", "fp64"), event_tracks=10000, pool
     report = {"workload": "uneven barrel events of %d tracks (4-20 hits, holes 10 %%, outliers "
                           "5 %%, grid field), Poisson arrivals; inputs in page-locked host "
                           "memory" % event_tracks,
-              "memory_budget_gb": 40, "streams": 3, "max_states": max_states}
+              "memory_budget_gb": 40, "streams": 3, "max_states": max_states,
+              "launch": "each co-batch on the SMs / (streams - 1) blocks, 6 Runge-Kutta trials "
+                        "per scheduling round (the server's defaults)"}
     # the kernel time of one event alone (whole GPU, device-resident)
     one = generate.generate(det, event_tracks, seed=seed)
     for name in precisions:
@@ -651,7 +653,7 @@ def serving_report(torch, precisions=("mixed", "fp64"), event_tracks=10000, pool
         cap_events = n_cap / wall
         res = {"capacity_tracks_per_s": round(cap_events * event_tracks, 1),
                "results": "device memory", "loads": []}
-        loads = (0.1, 0.5, 0.8, 1.0, 1.2) if name == "mixed" else (0.5, 1.0)
+        loads = (0.1, 0.3, 0.5, 0.8, 1.0, 1.2) if name == "mixed" else (0.1, 0.5, 1.0)
         nid = 10000
         for f in loads:
             rate = f * cap_events

@@ -346,9 +346,11 @@ ck_status ck_get_launch_config(ck_handle* h, int32_t precision,
                                int32_t* threads_per_block,
                                int32_t* blocks_per_sm);
 
-/* Pins the launch shape: register-cap variant (0: 255, 1: 168, 2: 128
- * registers per thread), threads per block (multiple of 32, <= 128) and
- * resident blocks per SM. */
+/* Pins the launch shape of the forward-filter kernel: variant (0-2
+ * per-warp phase scheduling with register caps of 255 / 168 / 128 per
+ * thread and any multiple of 32 up to 128 threads per block; 3 and 4
+ * block-level phase compaction with 256 and 128 threads per block), threads
+ * per block and resident blocks per SM. */
 ck_status ck_set_launch_config(ck_handle* h, int32_t precision, int32_t variant,
                                int32_t threads_per_block, int32_t blocks_per_sm);
 
@@ -357,6 +359,13 @@ ck_status ck_set_launch_config(ck_handle* h, int32_t precision, int32_t variant,
  * 3 for mixed; the autotuner also sweeps it). Results do not depend on it.
  * No counterpart in the reference (a scheduling knob of this implementation). */
 ck_status ck_set_steps_per_round(ck_handle* h, int32_t precision, int32_t steps);
+
+/* Grid of the forward-filter kernel in blocks for one precision (0, the
+ * default: SMs x resident blocks per SM, the whole GPU). A smaller grid
+ * leaves SMs free for fits launched at the same time on other streams (the
+ * serving loop's concurrent co-batches). Results do not depend on it.
+ * No counterpart in the reference (a scheduling knob of this implementation). */
+ck_status ck_set_grid_blocks(ck_handle* h, int32_t precision, int32_t blocks);
 
 /* Enables (default) or disables ordering the work queue by descending
  * surface-sequence length before the fit. */
@@ -450,6 +459,15 @@ typedef struct ck_server_config {
   int32_t max_states;          /* per-track state capacity                  */
   int32_t max_batch_tracks;    /* largest co-batch                          */
   uint32_t components;         /* CK_OUT_* written back to the host         */
+  /* Launch shape of the co-batches (0: automatic). grid_blocks: blocks of
+   * each co-batch's forward-filter grid; automatic = the whole GPU divided by
+   * (n_streams - 1), so that a co-batch admitted while others run starts on
+   * free SMs at once instead of behind their blocks. steps_per_round:
+   * Runge-Kutta trials per scheduling round; automatic = 6, the measured
+   * best for 10k-track events (latency), where large offline batches prefer
+   * 2-3 (throughput). Neither changes results. */
+  int32_t grid_blocks;
+  int32_t steps_per_round;
 } ck_server_config;
 
 ck_status ck_server_create(ck_handle* h, const ck_options* opt,
