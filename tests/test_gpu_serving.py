@@ -22,8 +22,12 @@ def _events(det, sizes, seed=31):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_MIXED])
-def test_same_result_alone_and_in_mix(fitter_factory, precision):
+@pytest.mark.parametrize("precision,grid_blocks,steps_per_round",
+                         [(abi.PRECISION_FP64, 0, 0), (abi.PRECISION_MIXED, 0, 0),
+                          (abi.PRECISION_MIXED, 7, 1)])
+def test_same_result_alone_and_in_mix(fitter_factory, precision, grid_blocks, steps_per_round):
+    """Also with a launch shape of the co-batches far from the default (7
+    blocks, one Runge-Kutta trial per round): results do not depend on it."""
     preset = abi.CKG_UNEVEN
     det = detector(preset)
     fit = fitter_factory(preset)
@@ -31,7 +35,8 @@ def test_same_result_alone_and_in_mix(fitter_factory, precision):
     sizes = generate.event_sizes(5, 24, lo=100, hi=5000)
     evs = _events(det, sizes)
     srv = FitServer(fit, opt, memory_budget_bytes=4 << 30, n_streams=3, max_states=24,
-                    max_batch_tracks=12000)
+                    max_batch_tracks=12000, grid_blocks=grid_blocks,
+                    steps_per_round=steps_per_round)
     for i, ev in enumerate(evs):
         srv.submit(i, ev)
         if i % 5 == 4:
