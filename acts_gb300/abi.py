@@ -51,6 +51,8 @@ FIELD_GRID_XYZ = 1
 
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
+SMOOTHER_GAIN_MATRIX = 0
+SMOOTHER_MBF = 1
 NUM_PRECISIONS = 2
 
 MEM_HOST = 0
@@ -132,6 +134,7 @@ class ck_options(C.Structure):
         ("free_to_bound_correction", C.c_int32),
         ("reference_surface", C.c_int32),
         ("early_termination", C.c_int32),
+        ("smoother", C.c_int32),
     ]
 
 
@@ -259,6 +262,7 @@ def default_options(**kw):
     o.free_to_bound_correction = 0
     o.reference_surface = -1
     o.early_termination = 0
+    o.smoother = SMOOTHER_GAIN_MATRIX
     for k, v in kw.items():
         setattr(o, k, v)
     return o

@@ -116,6 +116,7 @@ DevOptions toDevOptions(const ck_options& o) {
   d.joseph = o.use_joseph;
   d.useOutlierCut = std::isinf(o.outlier_chi2_cut) ? 0 : 1;
   d.earlyTermination = o.early_termination;
+  d.smoother = o.smoother;
   return d;
 }
 
@@ -129,6 +130,8 @@ ck_status validateOptions(const ck_options* o) {
     return fail(CK_ERR_UNSUPPORTED, "extrapolation to a reference surface is not supported");
   if (o->precision < 0 || o->precision >= CK_NUM_PRECISIONS)
     return fail(CK_ERR_INVALID_ARGUMENT, "unknown precision");
+  if (o->smoother != CK_SMOOTHER_GAIN_MATRIX && o->smoother != CK_SMOOTHER_MBF)
+    return fail(CK_ERR_INVALID_ARGUMENT, "unknown smoother");
   if (!(o->step_tolerance > 0) || !(o->initial_step_size > 0))
     return fail(CK_ERR_INVALID_ARGUMENT, "step tolerance and initial step size must be > 0");
   if (o->max_steps == 0) return fail(CK_ERR_INVALID_ARGUMENT, "max_steps must be > 0");
@@ -409,6 +412,7 @@ void ck_options_default(ck_options* o) {
   o->free_to_bound_correction = 0;
   o->reference_surface = -1;
   o->early_termination = 0;
+  o->smoother = CK_SMOOTHER_GAIN_MATRIX;
 }
 
 int32_t ck_api_version(void) { return CK_API_VERSION; }

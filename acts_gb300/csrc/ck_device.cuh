@@ -890,4 +890,154 @@ CK_D bool smoothStep(const double filt[6], const GP Pf[21], const double pp[6], 
   return true;
 }
 
+// ------------------------------------------------- MbfSmoother (mBF form)
+// Modified Bryson-Frazier smoother (MbfSmoother.hpp:48-90,
+// MbfSmoother.cpp:17-48, MbfSmootherImpl.hpp:17-58): a backward pass that
+// carries Lambda (6x6 symmetric, packed) and lambda (6) from state to state;
+// no 6x6 inverse. Products run in GP (double in the plain form, float in the
+// mixed form); the residual covariance inverse, the gain, the residual and
+// the parameter update are FP64.
+
+// calculateSmoothed: Ps = Pf - Pf Lambda Pf, sm = filt - Pf lambda
+// (normalised). `shared`: the state's smoothed storage is its filtered
+// storage, so the parameter update reads the smoothed covariance.
+template <typename GP>
+CK_D void mbfSmoothed(const double filt[6], const GP Pf[21], const GP L[21], const GP l[6],
+                      bool shared, double sm[6], GP Ps[21]) {
+  GP B[36];  // Lambda Pf
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      GP s = GP(0);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) s += L[sidx(i, k)] * Pf[sidx(k, j)];
+      B[i * 6 + j] = s;
+    }
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = i; j < 6; ++j) {
+      GP s = GP(0);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) s += Pf[sidx(i, k)] * B[k * 6 + j];
+      Ps[sidx(i, j)] = Pf[sidx(i, j)] - s;
+    }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) s += (double)((shared ? Ps : Pf)[sidx(i, k)] * l[k]);
+    sm[i] = filt[i] - s;
+  }
+  normalizePhiTheta(sm[2], sm[3]);
+}
+
+// visitNonMeasurement / the last line of visitMeasurementImpl:
+// Lambda <- F^T Lambda F, lambda <- F^T lambda (F row-major)
+template <typename GP>
+CK_D void mbfTransport(const GP* F, GP L[21], GP l[6]) {
+  GP A[36];  // Lambda F
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      GP s = GP(0);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) s += L[sidx(i, k)] * F[k * 6 + j];
+      A[i * 6 + j] = s;
+    }
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = i; j < 6; ++j) {
+      GP s = GP(0);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) s += F[k * 6 + i] * A[k * 6 + j];
+      L[sidx(i, j)] = s;
+    }
+  GP ln[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    GP s = GP(0);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) s += F[k * 6 + i] * l[k];
+    ln[i] = s;
+  }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) l[i] = ln[i];
+}
+
+// visitMeasurementImpl<2> with the (loc0, loc1) projector H, before the
+// transport: S = H Pp H^T + V, K = Pp H^T S^-1, C = I - K H,
+// Lambda~ = H^T S^-1 H + C^T Lambda C, lambda~ = -H^T S^-1 y + C^T lambda,
+// y = m - H pred. C differs from I in its first two columns only, so
+// Lambda C and C^T (Lambda C) change only those columns / rows.
+template <typename GP>
+CK_D void mbfMeasurement(const double pred[6], const GP Pp[21], double m0, double m1,
+                         const double V[4], GP L[21], GP l[6]) {
+  constexpr bool kFast = sizeof(GP) == sizeof(float);
+  const Inv2 si = inverse2<kFast>((double)Pp[sidx(0, 0)] + V[0], (double)Pp[sidx(0, 1)] + V[1],
+                                  (double)Pp[sidx(1, 0)] + V[2], (double)Pp[sidx(1, 1)] + V[3]);
+  GP K[6][2];
+#pragma unroll
+  for (int r = 0; r < 6; ++r) {
+    const double p0 = (double)Pp[sidx(r, 0)], p1 = (double)Pp[sidx(r, 1)];
+    K[r][0] = (GP)(p0 * si.a00 + p1 * si.a10);
+    K[r][1] = (GP)(p0 * si.a01 + p1 * si.a11);
+  }
+  // A = Lambda C: columns 0 and 1 are Lambda[:,c] - Lambda K[:,c]
+  GP A[6][6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 6; ++j) A[i][j] = L[sidx(i, j)];
+#pragma unroll
+  for (int c = 0; c < 2; ++c)
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      GP s = GP(0);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) s += L[sidx(i, r)] * K[r][c];
+      A[i][c] -= s;
+    }
+  // Lambda~ = C^T A (+ S^-1 on the loc block): rows 0 and 1 are
+  // A[c,:] - K[:,c]^T A
+  GP Lt[21];
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = i; j < 6; ++j) {
+      GP v = A[i][j];
+      if (i < 2) {
+        GP s = GP(0);
+#pragma unroll
+        for (int r = 0; r < 6; ++r) s += K[r][i] * A[r][j];
+        v -= s;
+      }
+      Lt[sidx(i, j)] = v;
+    }
+  Lt[sidx(0, 0)] += (GP)si.a00;
+  Lt[sidx(0, 1)] += (GP)(0.5 * (si.a01 + si.a10));
+  Lt[sidx(1, 1)] += (GP)si.a11;
+  // lambda~ = C^T lambda - H^T S^-1 y
+  const double y0 = m0 - pred[0], y1 = m1 - pred[1];
+  GP lt[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) lt[i] = l[i];
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    GP s = GP(0);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) s += K[r][c] * l[r];
+    lt[c] -= s;
+  }
+  lt[0] -= (GP)(si.a00 * y0 + si.a01 * y1);
+  lt[1] -= (GP)(si.a10 * y0 + si.a11 * y1);
+#pragma unroll
+  for (int i = 0; i < 21; ++i) L[i] = Lt[i];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) l[i] = lt[i];
+}
+
 }  // namespace ck

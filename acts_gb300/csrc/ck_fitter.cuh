@@ -1103,6 +1103,11 @@ struct Smoother {
     }
     nM = nH = nO = ndf = 0;
     chi2sum = 0.0;
+    if (fp.opt.smoother == CK_SMOOTHER_MBF) {
+      runMbf(fp, rec, tip);
+      finish(fp, tip);
+      return;
+    }
     // the smoothed state of k+1, carried from one step to the next (the tip's
     // smoothed state is its filtered state)
     double ps[6];
@@ -1135,6 +1140,62 @@ struct Smoother {
 #pragma unroll
       for (int i = 0; i < 21; ++i) Psp[i] = Ps[i];
     }
+    finish(fp, tip);
+  }
+
+  // MbfSmoother::operator() (MbfSmoother.hpp:48-90): backwards from the tip
+  // with zero lambdas; each state is smoothed from its filtered state and the
+  // lambdas of the states after it, then the lambdas move to the previous
+  // state through its measurement (a non-outlier measurement state) and its
+  // Jacobian. The first state updates no lambdas.
+  CK_D void runMbf(const FitParams& fp, const Rec<CV>& rec, int tip) {
+    const int m0 = __ldg(&fp.meas_off[t]);
+    const int nMeas = __ldg(&fp.meas_off[t + 1]) - m0;
+    CV L[21], l[6];
+#pragma unroll
+    for (int i = 0; i < 21; ++i) L[i] = CV(0);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) l[i] = CV(0);
+    for (int k = tip; k >= 0; --k) {
+      double filt[6], sm[6];
+      CV Pf[21], Ps[21];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) filt[i] = rec.p(k, kRecFilt + i);
+#pragma unroll
+      for (int i = 0; i < 21; ++i) Pf[i] = rec.m(k, kRecFiltCov + i);
+      mbfSmoothed<CV>(filt, Pf, L, l, k == lastMeas, sm, Ps);
+      writeState(fp, k, sm, Ps, k == lastMeas);
+      if (k == 0) break;
+      const RecState<CV>& rs = rec.s(k);
+      const uint32_t fl = (uint32_t)rs.flags;
+      // the source link of a measurement state: the first measurement on its
+      // surface (the one the forward filter used)
+      int mi = -1;
+      if ((fl & CK_FLAG_HAS_MEASUREMENT) && !(fl & CK_FLAG_IS_OUTLIER)) {
+        for (int i = 0; i < nMeas && mi < 0; ++i)
+          if (__ldg(&fp.meas_surf[m0 + i]) == rs.surface) mi = m0 + i;
+      }
+      if ((fl & CK_FLAG_HAS_MEASUREMENT) && !(fl & CK_FLAG_IS_OUTLIER) && mi >= 0) {
+        double pred[6], V[4];
+        CV Pp[21];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) pred[i] = rec.p(k, kRecPred + i);
+#pragma unroll
+        for (int i = 0; i < 21; ++i) Pp[i] = rec.m(k, kRecPredCov + i);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) V[i] = __ldg(&fp.meas_cov[4 * (size_t)mi + i]);
+        mbfMeasurement<CV>(pred, Pp, __ldg(&fp.meas_val[2 * (size_t)mi]),
+                           __ldg(&fp.meas_val[2 * (size_t)mi + 1]), V, L, l);
+      }
+      CV F[36];
+#pragma unroll
+      for (int i = 0; i < 36; ++i) F[i] = rec.m(k, kRecJac + i);
+      mbfTransport<CV>(F, L, l);
+    }
+  }
+
+  // status and calculateTrackQuantities (TrackHelpers.hpp:421-448)
+  CK_D void finish(const FitParams& fp, int tip) {
     const ck_batch_out& out = fp.out;
     out.status[t] = CK_TRACK_OK;
     if (out.n_states) out.n_states[t] = tip + 1;

@@ -58,6 +58,7 @@ struct DevOptions {
   uint32_t maxRkTrials, maxSteps, maxTargetSkipping;
   int loopProtection, multipleScattering, energyLoss, joseph;
   int useOutlierCut, earlyTermination;
+  int smoother;  // CK_SMOOTHER_*
 };
 
 // Record of one forward track state kept for the smoother (scratch), one

@@ -78,6 +78,43 @@ __global__ void smoothKernel(int nTraj, int nStates, const double* __restrict__ 
   }
 }
 
+// MbfSmoother on whole trajectories (FP64): state k's flags select the
+// measurement visit; its Jacobian carries the lambdas to state k-1.
+__global__ void mbfKernel(int nTraj, int nStates, const uint32_t* __restrict__ flags,
+                          const double* __restrict__ pred, const double* __restrict__ predCov,
+                          const double* __restrict__ filt, const double* __restrict__ filtCov,
+                          const double* __restrict__ jac, const double* __restrict__ meas,
+                          const double* __restrict__ measCov, double* smth, double* smthCov) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nTraj) return;
+  const size_t b = (size_t)t * nStates;
+  double L[21], l[6];
+  for (int i = 0; i < 21; ++i) L[i] = 0.0;
+  for (int i = 0; i < 6; ++i) l[i] = 0.0;
+  for (int k = nStates - 1; k >= 0; --k) {
+    const size_t s = b + k;
+    double f[6], Pf[21], sm[6], Ps[21];
+    for (int i = 0; i < 6; ++i) f[i] = filt[6 * s + i];
+    for (int r = 0; r < 6; ++r)
+      for (int c = r; c < 6; ++c) Pf[sidx(r, c)] = filtCov[36 * s + r * 6 + c];
+    mbfSmoothed<double>(f, Pf, L, l, false, sm, Ps);
+    for (int i = 0; i < 6; ++i) smth[6 * s + i] = sm[i];
+    for (int r = 0; r < 6; ++r)
+      for (int c = 0; c < 6; ++c) smthCov[36 * s + r * 6 + c] = Ps[sidx(r, c)];
+    if (k == 0) break;
+    const uint32_t fl = flags[s];
+    if ((fl & CK_FLAG_HAS_MEASUREMENT) && !(fl & CK_FLAG_IS_OUTLIER)) {
+      double p[6], Pp[21], V[4];
+      for (int i = 0; i < 6; ++i) p[i] = pred[6 * s + i];
+      for (int r = 0; r < 6; ++r)
+        for (int c = r; c < 6; ++c) Pp[sidx(r, c)] = predCov[36 * s + r * 6 + c];
+      for (int i = 0; i < 4; ++i) V[i] = measCov[4 * s + i];
+      mbfMeasurement<double>(p, Pp, meas[2 * s], meas[2 * s + 1], V, L, l);
+    }
+    mbfTransport<double>(jac + 36 * s, L, l);
+  }
+}
+
 __global__ void materialKernel(int n, MatConst mc, const DevSurface* __restrict__ surf,
                                const int32_t* __restrict__ sid, const float* __restrict__ scale,
                                const double* __restrict__ dir, const double* __restrict__ qop,
@@ -207,6 +244,52 @@ ck_status ck_gain_matrix_smooth(ck_handle* h, int32_t n_traj, int32_t n_states,
   cudaMemcpyAsync(smoothed_cov, a.at<double>(tSC), 288 * m, cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(status, a.at<int32_t>(tSt), 4 * (size_t)n_traj, cudaMemcpyDeviceToHost, st);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cudaFail(e, "smooth kernel");
+  h->lastLaunches = 1;
+  return CK_OK;
+}
+
+ck_status ck_mbf_smooth(ck_handle* h, int32_t n_traj, int32_t n_states, const uint32_t* flags,
+                        const double* predicted, const double* predicted_cov,
+                        const double* filtered, const double* filtered_cov,
+                        const double* jacobian, const double* measurement,
+                        const double* measurement_cov, double* smoothed, double* smoothed_cov) {
+  if (!h || n_traj < 0 || n_states < 1 || !flags || !predicted || !predicted_cov || !filtered ||
+      !filtered_cov || !jacobian || !measurement || !measurement_cov || !smoothed ||
+      !smoothed_cov)
+    return fail(CK_ERR_INVALID_ARGUMENT, "bad argument");
+  if (n_traj == 0) return CK_OK;
+  std::lock_guard<std::mutex> lock(h->mu);
+  cudaSetDevice(h->device);
+  const size_t m = (size_t)n_traj * n_states;
+  Arena a{h};
+  void* tFl = a.add(4 * m);
+  void* tP = a.add(48 * m);
+  void* tPC = a.add(288 * m);
+  void* tF = a.add(48 * m);
+  void* tFC = a.add(288 * m);
+  void* tJ = a.add(288 * m);
+  void* tM = a.add(16 * m);
+  void* tMC = a.add(32 * m);
+  void* tS = a.add(48 * m);
+  void* tSC = a.add(288 * m);
+  cudaError_t e = a.commit();
+  if (e != cudaSuccess) return cudaFail(e, "unit buffer");
+  cudaStream_t st = h->stream;
+  cudaMemcpyAsync(a.at<uint32_t>(tFl), flags, 4 * m, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(a.at<double>(tP), predicted, 48 * m, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(a.at<double>(tPC), predicted_cov, 288 * m, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(a.at<double>(tF), filtered, 48 * m, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(a.at<double>(tFC), filtered_cov, 288 * m, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(a.at<double>(tJ), jacobian, 288 * m, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(a.at<double>(tM), measurement, 16 * m, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(a.at<double>(tMC), measurement_cov, 32 * m, cudaMemcpyHostToDevice, st);
+  mbfKernel<<<(n_traj + 127) / 128, 128, 0, st>>>(
+      n_traj, n_states, a.at<uint32_t>(tFl), a.at<double>(tP), a.at<double>(tPC),
+      a.at<double>(tF), a.at<double>(tFC), a.at<double>(tJ), a.at<double>(tM),
+      a.at<double>(tMC), a.at<double>(tS), a.at<double>(tSC));
+  cudaMemcpyAsync(smoothed, a.at<double>(tS), 48 * m, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(smoothed_cov, a.at<double>(tSC), 288 * m, cudaMemcpyDeviceToHost, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cudaFail(e, "mbf kernel");
   h->lastLaunches = 1;
   return CK_OK;
 }

@@ -80,6 +80,7 @@ def lib():
         L.ck_autotune_log.argtypes = [C.c_void_p]
         L.ck_gain_matrix_update.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [abi.P_f64] * 7 + [abi.P_i32]
         L.ck_gain_matrix_smooth.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [abi.P_f64] * 7 + [abi.P_i32]
+        L.ck_mbf_smooth.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_uint32)] + [abi.P_f64] * 9
         L.ck_material_effects.argtypes = [C.c_void_p, C.c_int32, abi.P_i32, abi.P_f32, abi.P_f64,
                                           abi.P_f64, abi.P_f32, abi.P_f32, abi.P_i32, C.c_int32,
                                           C.c_int32, abi.P_f64]
@@ -116,6 +117,7 @@ class KalmanFitterOptions:
     loop_protection: bool = True
     loop_fraction: float = 0.5
     early_termination: bool = False
+    smoother: int = abi.SMOOTHER_GAIN_MATRIX  # or abi.SMOOTHER_MBF (MbfSmoother)
     extra: dict = dc_field(default_factory=dict)
 
     def to_ck(self):
@@ -134,6 +136,7 @@ class KalmanFitterOptions:
         o.loop_protection = int(self.loop_protection)
         o.loop_fraction = float(self.loop_fraction)
         o.early_termination = int(self.early_termination)
+        o.smoother = int(self.smoother)
         for k, v in self.extra.items():
             setattr(o, k, v)
         return o
@@ -379,6 +382,19 @@ class CudaKalman:
                                            abi.ptr(s, C.c_double), abi.ptr(sc, C.c_double),
                                            abi.ptr(st, C.c_int32)))
         return s, sc.reshape(nt, ns, 6, 6), st
+
+    def mbf_smooth(self, flags, pred, pred_cov, filt, filt_cov, jac, meas, meas_cov):
+        """MbfSmoother on trajectories (arrays shaped [n_traj, n_states, ...])."""
+        nt, ns = pred.shape[:2]
+        s = np.zeros((nt, ns, 6))
+        sc = np.zeros((nt, ns, 36))
+        fl = np.ascontiguousarray(flags, np.uint32)
+        a = [np.ascontiguousarray(x, np.float64)
+             for x in (pred, pred_cov, filt, filt_cov, jac, meas, meas_cov)]
+        _check(lib().ck_mbf_smooth(self._h, nt, ns, abi.ptr(fl, C.c_uint32),
+                                   *[abi.ptr(x, C.c_double) for x in a],
+                                   abi.ptr(s, C.c_double), abi.ptr(sc, C.c_double)))
+        return s, sc.reshape(nt, ns, 6, 6)
 
     def material_effects(self, surface_ids, scale, directions, qop, mass, absq, pdg, ms=True,
                          el=True):

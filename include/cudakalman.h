@@ -157,6 +157,14 @@ typedef struct ck_field {
  *   Kalman update (Joseph form when selected), 2x2 inverse, smoother-gain
  *   inverse, bound-parameter conversion and chi2 in FP64. */
 enum { CK_PRECISION_FP64 = 0, CK_PRECISION_MIXED = 1 };
+
+/* Smoother extension (KalmanFitterExtensions::smoother):
+ * GAIN_MATRIX: GainMatrixSmoother (Core/src/TrackFitting/GainMatrixSmoother.cpp:18-97),
+ * MBF: MbfSmoother, the modified Bryson-Frazier smoother
+ *   (Core/include/Acts/TrackFitting/MbfSmoother.hpp:48-90, MbfSmoother.cpp:17-48,
+ *    detail/MbfSmootherImpl.hpp:17-58), which the reference's example
+ *   KalmanFitterFunction connects (KalmanFitterFunction.cpp:77,102). */
+enum { CK_SMOOTHER_GAIN_MATRIX = 0, CK_SMOOTHER_MBF = 1 };
 #define CK_NUM_PRECISIONS 2
 
 /* Fit options. ck_options_default() fills the reference defaults:
@@ -198,6 +206,7 @@ typedef struct ck_options {
    * after the last such surface (states beyond it are never part of the
    * track), which turns those failures into successful fits. */
   int32_t early_termination;
+  int32_t smoother;             /* CK_SMOOTHER_*, default GAIN_MATRIX       */
 } ck_options;
 
 /* --------------------------------------------------------------- handle */
@@ -418,6 +427,23 @@ ck_status ck_gain_matrix_smooth(ck_handle* h, int32_t n_traj, int32_t n_states,
                                 const double* filtered_cov,
                                 const double* jacobian, double* smoothed,
                                 double* smoothed_cov, int32_t* status);
+
+/* MbfSmoother::operator() (Core/include/Acts/TrackFitting/MbfSmoother.hpp
+ * :48-90, Core/src/TrackFitting/MbfSmoother.cpp:17-48,
+ * detail/MbfSmootherImpl.hpp:17-58) on n_traj independent trajectories of
+ * n_states each, in forward order, smoothed backwards from the last state:
+ * flags[k] (CK_FLAG_*; a state with a measurement that is not an outlier is
+ * visited as a measurement with the (loc0, loc1) projector), AoS per state:
+ * predicted[6], predicted_cov[36], filtered[6], filtered_cov[36],
+ * jacobian[36] (transport from the previous state), measurement[2],
+ * measurement_cov[4]; outputs smoothed[6], smoothed_cov[36]. FP64. Host
+ * pointers; synchronous. */
+ck_status ck_mbf_smooth(ck_handle* h, int32_t n_traj, int32_t n_states,
+                        const uint32_t* flags, const double* predicted,
+                        const double* predicted_cov, const double* filtered,
+                        const double* filtered_cov, const double* jacobian,
+                        const double* measurement, const double* measurement_cov,
+                        double* smoothed, double* smoothed_cov);
 
 /* The mixed form's FP64 atan2 (table-driven argument reduction; used for
  * the bound angles and the cylinder loc0) on a batch: out[i] = atan2(y[i],

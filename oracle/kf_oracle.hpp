@@ -909,8 +909,10 @@ struct Options {
   bool multipleScattering, energyLoss, josephs;
   double outlierChi2Cut;
   bool coastAfterLastMeasurement;  // faithful reference termination
+  int smoother;                    // CK_SMOOTHER_*
   static Options fromCk(const ck_options& o, bool coast) {
     Options r;
+    r.smoother = o.smoother;
     r.stepTolerance = o.step_tolerance;
     r.stepSizeCutOff = o.step_size_cutoff;
     r.initialStepSize = o.initial_step_size;
@@ -1279,6 +1281,61 @@ bool smoothStep(const Vec<S, 6>& filt, const Mat<S, 6, 6>& Pf, const Vec<S, 6>& 
   return true;
 }
 
+// MbfSmoother (modified Bryson-Frazier): MbfSmoother::calculateSmoothed
+// (MbfSmoother.cpp:17-29) — smoothed covariance P_f - P_f Lambda P_f,
+// smoothed parameters x_f - P_f lambda (normalised). When the state's
+// smoothed storage is shared with its filtered storage (the last measurement
+// state), the covariance is written first and the parameter update then
+// reads the already smoothed covariance through the shared storage.
+template <typename S>
+void mbfSmoothed(const Vec<S, 6>& filt, const Mat<S, 6, 6>& Pf, const Mat<S, 6, 6>& L,
+                 const Vec<S, 6>& l, bool shared, Vec<S, 6>& smth, Mat<S, 6, 6>& Ps) {
+  Ps = sub(Pf, mul(mul(Pf, L), Pf));
+  Vec<S, 6> Pl = mulv(shared ? Ps : Pf, l);
+  for (int i = 0; i < 6; ++i) smth[i] = filt[i] - Pl[i];
+  smth = normalizeBoundParameters(smth);
+}
+
+// MbfSmoother::visitNonMeasurement (MbfSmoother.cpp:31-38): holes, outliers
+// and material states carry the lambdas through their Jacobian only.
+template <typename S>
+void mbfVisitNonMeasurement(const Mat<S, 6, 6>& F, Mat<S, 6, 6>& L, Vec<S, 6>& l) {
+  L = mul(mul(transpose(F), L), F);
+  l = mulv(transpose(F), l);
+}
+
+// MbfSmoother::visitMeasurementImpl<2> (MbfSmootherImpl.hpp:17-58) with the
+// (loc0, loc1) projector.
+template <typename S>
+void mbfVisitMeasurement(const Mat<S, 6, 6>& F, const Vec<S, 6>& pred, const Mat<S, 6, 6>& Pp,
+                         const double meas[2], const double mcov[4], Mat<S, 6, 6>& L,
+                         Vec<S, 6>& l) {
+  Mat<S, 2, 6> H = Mat<S, 2, 6>::zero();
+  H.a[0][0] = S(1.0);
+  H.a[1][1] = S(1.0);
+  Mat<S, 6, 2> Ht = transpose(H);
+  Mat<S, 2, 2> V;
+  V.a[0][0] = S(mcov[0]);
+  V.a[0][1] = S(mcov[1]);
+  V.a[1][0] = S(mcov[2]);
+  V.a[1][1] = S(mcov[3]);
+  Mat<S, 2, 2> Sm = add(mul(mul(H, Pp), Ht), V);
+  Mat<S, 2, 2> Si = inverse2(Sm);
+  Mat<S, 6, 2> K = mul(mul(Pp, Ht), Si);
+  Mat<S, 6, 6> C = sub(Mat<S, 6, 6>::identity(), mul(K, H));
+  Vec<S, 2> Hp = mulv(H, pred);
+  Vec<S, 2> y;
+  y[0] = S(meas[0]) - Hp[0];
+  y[1] = S(meas[1]) - Hp[1];
+  Mat<S, 6, 6> Lt = add(mul(mul(Ht, Si), H), mul(mul(transpose(C), L), C));
+  Vec<S, 6> a = mulv(mul(Ht, Si), y);
+  Vec<S, 6> b = mulv(transpose(C), l);
+  Vec<S, 6> lt;
+  for (int i = 0; i < 6; ++i) lt[i] = -a[i] + b[i];
+  L = mul(mul(transpose(F), Lt), F);
+  l = mulv(transpose(F), lt);
+}
+
 // The whole fit for one track: KalmanFitter::fit_impl / filter_impl
 // (KalmanFitter.hpp:795-984), Actor::act / filter (:337-671), the
 // Propagator stepping loop (Propagator.ipp:25-210) with the DirectNavigator
@@ -1638,9 +1695,35 @@ struct Fitter {
     states[lastMeas].smoothedSharesFiltered = true;
     states[tip].smth = states[tip].filt;
     states[tip].smthCov = states[tip].filtCov;
-    // GainMatrixSmoother::operator() (GainMatrixSmoother.hpp:43-99)
     int status = CK_TRACK_OK;
-    for (int k = tip - 1; k >= 0; --k) {
+    if (o.smoother == CK_SMOOTHER_MBF) {
+      // MbfSmoother::operator() (MbfSmoother.hpp:48-90): backwards from the
+      // tip with zero lambdas; the first state updates no lambdas
+      Mat<S, 6, 6> L = Mat<S, 6, 6>::zero();
+      Vec<S, 6> l;
+      for (int i = 0; i < 6; ++i) l[i] = S(0.0);
+      for (int k = tip; k >= 0; --k) {
+        IState& ts = states[k];
+        Vec<S, 6> sm;
+        Mat<S, 6, 6> Ps;
+        mbfSmoothed(ts.filt, ts.filtCov, L, l, ts.smoothedSharesFiltered, sm, Ps);
+        ts.smth = sm;
+        ts.smthCov = Ps;
+        if (ts.smoothedSharesFiltered) {
+          ts.filt = sm;
+          ts.filtCov = Ps;
+        }
+        if (k == 0) break;
+        if ((ts.flags & CK_FLAG_HAS_MEASUREMENT) && !(ts.flags & CK_FLAG_IS_OUTLIER)) {
+          const MeasRec<S>& m = meas[findMeas(ts.surface)];
+          mbfVisitMeasurement(ts.jac, ts.pred, ts.predCov, m.v, m.cov, L, l);
+        } else {
+          mbfVisitNonMeasurement(ts.jac, L, l);
+        }
+      }
+    }
+    // GainMatrixSmoother::operator() (GainMatrixSmoother.hpp:43-99)
+    for (int k = tip - 1; k >= 0 && o.smoother != CK_SMOOTHER_MBF; --k) {
       IState& ts = states[k];
       const IState& pv = states[k + 1];
       if (!smoothStep(ts.filt, ts.filtCov, pv.pred, pv.predCov, pv.jac, pv.smth, pv.smthCov,

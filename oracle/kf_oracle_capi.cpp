@@ -183,6 +183,35 @@ void kfo_gain_matrix_smooth(int n_traj, int n_states, const double* pred, const 
   }
 }
 
+// MbfSmoother on n_traj trajectories of n_states (forward order), smoothed
+// backwards from the last state; flags select the measurement visit.
+void kfo_mbf_smooth(int n_traj, int n_states, const uint32_t* flags, const double* pred,
+                    const double* predCov, const double* filt, const double* filtCov,
+                    const double* jac, const double* meas, const double* measCov, double* smth,
+                    double* smthCov) {
+  for (int t = 0; t < n_traj; ++t) {
+    size_t b = (size_t)t * n_states;
+    Mat<double, 6, 6> L = Mat<double, 6, 6>::zero();
+    Vec<double, 6> l = Vec<double, 6>::zero();
+    for (int k = n_states - 1; k >= 0; --k) {
+      const size_t s = b + k;
+      Vec<double, 6> sm;
+      Mat<double, 6, 6> Ps;
+      mbfSmoothed(get6<double>(filt + 6 * s), get36<double>(filtCov + 36 * s), L, l, false, sm,
+                  Ps);
+      put6(smth + 6 * s, sm);
+      put36(smthCov + 36 * s, Ps);
+      if (k == 0) break;
+      const Mat<double, 6, 6> F = get36<double>(jac + 36 * s);
+      if ((flags[s] & CK_FLAG_HAS_MEASUREMENT) && !(flags[s] & CK_FLAG_IS_OUTLIER))
+        mbfVisitMeasurement(F, get6<double>(pred + 6 * s), get36<double>(predCov + 36 * s),
+                            meas + 2 * s, measCov + 4 * s, L, l);
+      else
+        mbfVisitNonMeasurement(F, L, l);
+    }
+  }
+}
+
 // Interactions.cpp entry points for the material known-answer tests.
 // slab: thickness, X0, L0, Ar, Z, molarRho (mol/mm^3); which: 0 Bethe,
 // 1 Landau (most probable), 2 Landau sigma(q/p), 3 theta0, 4 Landau FWHM.

@@ -32,6 +32,8 @@ def lib():
         L.kfo_gain_matrix_update.argtypes = [C.c_int, C.c_int] + [abi.P_f64] * 7 + [abi.P_i32]
         L.kfo_gain_matrix_smooth.restype = None
         L.kfo_gain_matrix_smooth.argtypes = [C.c_int, C.c_int] + [abi.P_f64] * 7 + [abi.P_i32]
+        L.kfo_mbf_smooth.restype = None
+        L.kfo_mbf_smooth.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_uint32)] + [abi.P_f64] * 9
         L.kfo_interaction.restype = C.c_float
         L.kfo_interaction.argtypes = [C.c_int] + [C.c_float] * 6 + [C.c_int] + [C.c_float] * 3
         L.kfo_material_effects.restype = None
@@ -82,6 +84,19 @@ def gain_matrix_update(pred, pred_cov, meas, meas_cov, joseph=False):
                                  abi.ptr(f, C.c_double), abi.ptr(fc, C.c_double),
                                  abi.ptr(chi2, C.c_double), abi.ptr(st, C.c_int32))
     return f, fc.reshape(n, 6, 6), chi2, st
+
+
+def mbf_smooth(flags, pred, pred_cov, filt, filt_cov, jac, meas, meas_cov):
+    """MbfSmoother; arrays shaped [n_traj, n_states, ...]."""
+    nt, ns = pred.shape[:2]
+    s = np.zeros((nt, ns, 6))
+    sc = np.zeros((nt, ns, 36))
+    fl = np.ascontiguousarray(flags, np.uint32)
+    args = [np.ascontiguousarray(x, dtype=np.float64)
+            for x in (pred, pred_cov, filt, filt_cov, jac, meas, meas_cov)]
+    lib().kfo_mbf_smooth(nt, ns, abi.ptr(fl, C.c_uint32), *[abi.ptr(a, C.c_double) for a in args],
+                         abi.ptr(s, C.c_double), abi.ptr(sc, C.c_double))
+    return s, sc.reshape(nt, ns, 6, 6)
 
 
 def gain_matrix_smooth(pred, pred_cov, filt, filt_cov, jac):

@@ -6,6 +6,7 @@ default /root/reference). The JSON is committed, so tests never read the
 reference at run time. Sources parsed (paths relative to the acts repo):
   Tests/UnitTests/Core/TrackFitting/GainMatrixUpdaterTests.cpp  (Update, UpdateFailed)
   Tests/UnitTests/Core/TrackFitting/GainMatrixSmootherTests.cpp (Smooth)
+  Tests/UnitTests/Core/TrackFitting/MbfSmootherTests.cpp        (Smooth)
   Tests/UnitTests/Core/Material/InteractionsTests.cpp           (silicon Bethe, Landau)
   Tests/CommonHelpers/include/ActsTests/CommonHelpers/PredefinedMaterials.hpp (makeSilicon)
 """
@@ -81,6 +82,25 @@ def smoother(src):
             "tol": float(tol.group(1))}
 
 
+def mbf_smoother(src):
+    t = open(os.path.join(src, "Tests/UnitTests/Core/TrackFitting/MbfSmootherTests.cpp")).read()
+    cov = values(re.search(r"covTrk\.diagonal\(\) <<[^;]*;", t).group(0))
+    pred = [values(m.group(0)) for m in re.finditer(r"ts\.predicted\(\) <<[^;]*;", t)]
+    filt = [values(m.group(0)) for m in re.finditer(r"ts\.filtered\(\) <<[^;]*;", t)]
+    cal = [values(m.group(0)) for m in re.finditer(r"ts\.calibrated<2>\(\) <<[^;]*;", t)]
+    calc = [values(m.group(0)) for m in re.finditer(r"ts\.calibratedCovariance<2>\(\) <<[^;]*;", t)]
+    paths = [num(m.group(1)) for m in re.finditer(r"pathLength\(\) = ([^;]*);", t)]
+    exp_p = [values(m.group(0)) for m in re.finditer(r"expPars <<[^;]*;", t)]
+    exp_c = values(re.search(r"expCov\.diagonal\(\) <<[^;]*;", t).group(0))
+    tol = re.search(r"double tol = ([0-9.eE+-]+);", t)
+    states = [{"predicted": pred[k], "filtered": filt[k], "calibrated": cal[k],
+               "calibrated_cov": calc[k], "path": paths[k]} for k in range(3)]
+    return {"source": "Tests/UnitTests/Core/TrackFitting/MbfSmootherTests.cpp",
+            "cov_diag": cov, "states": states, "exp_smoothed": exp_p, "exp_cov_diag": exp_c,
+            "tol": float(tol.group(1)), "jacobian": "identity",
+            "projector": ["eBoundLoc0", "eBoundLoc1"], "flags": "measurement"}
+
+
 def interactions(src):
     t = open(os.path.join(src, "Tests/UnitTests/Core/Material/InteractionsTests.cpp")).read()
     mom = re.search(r"static const double momentum\[\] = \{([^}]*)\}", t).group(1)
@@ -123,7 +143,8 @@ def silicon(src):
 
 def main():
     src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    out = {"updater": updater(src), "smoother": smoother(src), "interactions": interactions(src),
+    out = {"updater": updater(src), "smoother": smoother(src), "mbf_smoother": mbf_smoother(src),
+           "interactions": interactions(src),
            "silicon": silicon(src)}
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_known_answers.json")
     with open(path, "w") as f:

@@ -1,7 +1,9 @@
 """Mixed-precision form (Runge-Kutta stages, Jacobian transport, field in
 FP32 with the free parameters accumulated in FP64; update, 2x2 inverse,
 smoother-gain inverse and chi2 in FP64) against the FP64 oracle
-on the same seeded barrel tracks. Bounds: relative parameter error
+on the same seeded barrel tracks, with either smoother (gain matrix; the
+modified Bryson-Frazier smoother with its lambda recursion in FP32 and the
+residual-covariance inverse, gain and parameter update in FP64). Bounds: relative parameter error
 |x_mixed - x_fp64| / max(|x_fp64|, sigma_fp64) <= 1e-4 on the smoothed
 parameters of measurement states of valid fits (FP64 chi2/ndf < 5), and
 pull widths against the generator truth within 1 % of the FP64 widths."""
@@ -38,16 +40,19 @@ def _pulls(res, b):
 
 
 @pytest.mark.gpu
-def test_mixed_precision_accuracy(fitter_factory):
+@pytest.mark.parametrize("smoother", [abi.SMOOTHER_GAIN_MATRIX, abi.SMOOTHER_MBF],
+                         ids=["gain_matrix", "mbf"])
+def test_mixed_precision_accuracy(fitter_factory, smoother):
     precision = abi.PRECISION_MIXED
     preset = abi.CKG_BARREL
     n = 20000
     det = detector(preset)
     b = batch(preset, n, seed=13)
     ora = Results(n, 12)
-    kforacle.fit_batch(det, b, abi.default_options(), ora, n_threads=kforacle.hardware_threads())
-    mix = fitter_factory(preset).fit_batch(b, abi.default_options(precision=precision),
-                                          max_states=12)
+    kforacle.fit_batch(det, b, abi.default_options(smoother=smoother), ora,
+                       n_threads=kforacle.hardware_threads())
+    mix = fitter_factory(preset).fit_batch(
+        b, abi.default_options(precision=precision, smoother=smoother), max_states=12)
     agree = np.mean(mix.status == ora.status)
     assert agree > 0.999, agree
     ok = (mix.status == 0) & (ora.status == 0)

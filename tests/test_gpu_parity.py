@@ -28,6 +28,9 @@ CASES = [
     ("telescope_no_material_options", abi.CKG_TELESCOPE, 500,
      dict(multiple_scattering=0, energy_loss=0), 0.99),
     ("barrel_no_energy_loss", abi.CKG_BARREL, 500, dict(energy_loss=0), 0.99),
+    ("barrel_mbf", abi.CKG_BARREL, 2000, dict(smoother=abi.SMOOTHER_MBF), 0.99),
+    ("uneven_mbf", abi.CKG_UNEVEN, 2000, dict(outlier_chi2_cut=15.0, smoother=abi.SMOOTHER_MBF),
+     0.5),
 ]
 
 

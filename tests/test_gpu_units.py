@@ -74,6 +74,60 @@ def test_smoother_known_answer_on_gpu(fitter_factory):
 
 
 @pytest.mark.gpu
+def test_mbf_smoother_known_answer_on_gpu(fitter_factory):
+    s = KA["mbf_smoother"]
+    cov = _diag(s["cov_diag"])
+    pred = np.array([[st["predicted"] for st in s["states"]]])
+    filt = np.array([[st["filtered"] for st in s["states"]]])
+    meas = np.array([[st["calibrated"] for st in s["states"]]])
+    mcov = np.array([[st["calibrated_cov"] for st in s["states"]]])
+    covs = np.tile(cov, (1, 3, 1))
+    jac = np.tile(np.eye(6).reshape(36), (1, 3, 1))
+    flags = np.full((1, 3), abi.FLAG_HAS_MEASUREMENT | abi.FLAG_HAS_PARAMETERS, np.uint32)
+    fit = fitter_factory(abi.CKG_TELESCOPE)
+    sm, smc = fit.mbf_smooth(flags, pred, covs, filt, covs.copy(), jac, meas, mcov)
+    for k in range(3):
+        np.testing.assert_allclose(sm[0, k], s["exp_smoothed"][k], atol=s["tol"])
+        np.testing.assert_allclose(smc[0, k], np.diag(s["exp_cov_diag"]), atol=s["tol"])
+    assert np.array_equal(sm[0, 2], filt[0, 2])
+
+
+def _spd(rng, n, scale):
+    a = rng.normal(size=(n, 6, 6)) * scale[None, :, None]
+    return a @ a.transpose(0, 2, 1) + np.diag(scale ** 2 * 0.1)[None]
+
+
+@pytest.mark.gpu
+def test_mbf_smoother_random_trajectories(fitter_factory):
+    """Trajectories with measurement, outlier, hole and material states,
+    random covariances and Jacobians: the device MbfSmoother against the
+    oracle's restatement within 1e-9 relative."""
+    rng = np.random.default_rng(11)
+    nt, ns = 200, 12
+    scale = np.array([0.05, 0.05, 1e-3, 1e-3, 1e-3, 1.0])
+    pc = _spd(rng, nt * ns, scale).reshape(nt, ns, 36)
+    fc = (_spd(rng, nt * ns, scale) * 0.5).reshape(nt, ns, 36)
+    pred = rng.normal(size=(nt, ns, 6)) * scale
+    pred[..., 2] = rng.uniform(-3.0, 3.0, (nt, ns))
+    pred[..., 3] = rng.uniform(0.3, 2.8, (nt, ns))
+    filt = pred + rng.normal(size=(nt, ns, 6)) * scale * 0.1
+    jac = (np.eye(6)[None, None] + rng.normal(size=(nt, ns, 6, 6)) * 0.05).reshape(nt, ns, 36)
+    meas = pred[..., :2] + rng.normal(size=(nt, ns, 2)) * 0.02
+    mcov = np.tile(np.array([4e-4, 1e-5, 1e-5, 2.5e-3]), (nt, ns, 1))
+    kinds = rng.choice([abi.FLAG_HAS_MEASUREMENT,
+                        abi.FLAG_HAS_MEASUREMENT | abi.FLAG_IS_OUTLIER,
+                        abi.FLAG_IS_HOLE, abi.FLAG_HAS_MATERIAL], size=(nt, ns),
+                       p=[0.7, 0.1, 0.1, 0.1])
+    flags = (kinds | abi.FLAG_HAS_PARAMETERS).astype(np.uint32)
+    args = (flags, pred, pc, filt, fc, jac, meas, mcov)
+    fit = fitter_factory(abi.CKG_TELESCOPE)
+    g, gc = fit.mbf_smooth(*args)
+    o, oc = kforacle.mbf_smooth(*args)
+    np.testing.assert_allclose(g, o, rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(gc, oc, rtol=1e-9, atol=1e-12 * np.abs(oc).max())
+
+
+@pytest.mark.gpu
 def test_material_effects_bit_exact(fitter_factory):
     """The float Bethe / Landau / Highland physics is reproduced bit for bit
     (un-contracted float arithmetic, shared correctly rounded logf)."""

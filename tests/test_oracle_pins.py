@@ -77,6 +77,53 @@ def test_smoother_known_answer():
     assert not np.array_equal(sm[0, 0], filt[0, 0])
 
 
+# ---------------------------------------------------- MbfSmootherTests.cpp
+def mbf_inputs():
+    s = KA["mbf_smoother"]
+    cov = _diag(s["cov_diag"])
+    pred = np.array([[st["predicted"] for st in s["states"]]])
+    filt = np.array([[st["filtered"] for st in s["states"]]])
+    meas = np.array([[st["calibrated"] for st in s["states"]]])
+    mcov = np.array([[st["calibrated_cov"] for st in s["states"]]])
+    covs = np.tile(cov, (1, 3, 1))
+    jac = np.tile(np.eye(6).reshape(36), (1, 3, 1))
+    flags = np.full((1, 3), abi.FLAG_HAS_MEASUREMENT | abi.FLAG_HAS_PARAMETERS, np.uint32)
+    return flags, pred, covs, filt, covs.copy(), jac, meas, mcov
+
+
+def test_mbf_smoother_known_answer():
+    s = KA["mbf_smoother"]
+    sm, smc = kforacle.mbf_smooth(*mbf_inputs())
+    for k in range(3):
+        np.testing.assert_allclose(sm[0, k], s["exp_smoothed"][k], atol=s["tol"])
+        np.testing.assert_allclose(smc[0, k], np.diag(s["exp_cov_diag"]), atol=s["tol"])
+    # the last state: smoothed == filtered; the earlier ones differ
+    filt = mbf_inputs()[3]
+    assert np.array_equal(sm[0, 2], filt[0, 2])
+    assert not np.array_equal(sm[0, 0], filt[0, 0])
+    assert not np.array_equal(sm[0, 1], filt[0, 1])
+
+
+@pytest.mark.parametrize("preset", [abi.CKG_TELESCOPE, abi.CKG_BARREL])
+def test_mbf_equals_gain_matrix_smoother(preset):
+    """The modified Bryson-Frazier and the Rauch-Tung-Striebel (gain-matrix)
+    smoothers are the same estimator (with or without the material noise the
+    barrel adds between states): whole fits agree to rounding (measured
+    <= 2e-12 relative on the parameters, <= 3e-11 on the covariances)."""
+    b = batch(preset, 50)
+    r1 = _fit(preset, b)
+    r2 = _fit(preset, b, smoother=abi.SMOOTHER_MBF)
+    ok = r1.status == 0
+    assert ok.mean() > 0.9 and np.array_equal(r1.status, r2.status)
+    assert np.array_equal(r1.n_states, r2.n_states)
+    valid = (np.arange(24)[None, :] < r1.n_states[:, None]) & ok[:, None]
+    a, c = r1.view("smoothed")[valid], r2.view("smoothed")[valid]
+    assert not np.array_equal(a, c)  # different arithmetic
+    np.testing.assert_allclose(c, a, rtol=1e-9, atol=1e-12)
+    a, c = r1.view("smoothed_cov")[valid], r2.view("smoothed_cov")[valid]
+    np.testing.assert_allclose(c, a, rtol=1e-8, atol=1e-15)
+
+
 # ------------------------------------------------------ InteractionsTests.cpp
 SI = KA["silicon"]
 
