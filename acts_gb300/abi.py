@@ -53,6 +53,9 @@ PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 SMOOTHER_GAIN_MATRIX = 0
 SMOOTHER_MBF = 1
+MEAS_LOC0 = 1
+MEAS_LOC1 = 2
+MEAS_LOC01 = 3
 NUM_PRECISIONS = 2
 
 MEM_HOST = 0
@@ -69,6 +72,7 @@ CKG_BARREL = 2
 CKG_BARREL_MIXED = 3
 CKG_UNEVEN = 4
 CKG_SERVING = 5
+CKG_STRIPS = 6
 
 P_i32 = C.POINTER(C.c_int32)
 P_u32 = C.POINTER(C.c_uint32)
@@ -167,6 +171,7 @@ class ck_batch_in(C.Structure):
         ("start_frames", P_f64),
         ("particle", P_f32),
         ("particle_pdg", P_i32),
+        ("meas_subspace", P_i32),
     ]
 
 
@@ -226,6 +231,7 @@ class ckg_out(C.Structure):
         ("truth_meas", P_f64),
         ("meas_outlier", P_u8),
         ("truth_start", P_f64),
+        ("meas_subspace", P_i32),
     ]
 
 

@@ -329,6 +329,7 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
   fp.meas_surf = din.meas_surfaces;
   fp.meas_val = din.meas_values;
   fp.meas_cov = din.meas_cov;
+  fp.meas_sub = din.meas_subspace;
   fp.start_params = din.start_params;
   fp.start_cov = din.start_cov;
   fp.start_frames = din.start_frames;
@@ -636,11 +637,12 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
         {in->start_frames, sizeof(double) * 12 * n, (const void**)&din.start_frames},
         {in->particle, sizeof(float) * 2 * n, (const void**)&din.particle},
         {in->particle_pdg, sizeof(int32_t) * n, (const void**)&din.particle_pdg},
+        {in->meas_subspace, sizeof(int32_t) * nMeas, (const void**)&din.meas_subspace},
     };
     size_t h2d = 0;
-    for (int i = 0; i < 11; ++i) {
+    for (int i = 0; i < kInputArrays; ++i) {
       if (!items[i].src) {
-        if (i == 10) {
+        if (i >= 10) {  // optional arrays
           *items[i].dst = nullptr;
           continue;
         }

@@ -68,6 +68,9 @@ MatConst makeMatConst();
 DevSurface toDevSurface(const ck_surface& s);
 size_t recordStateBytes(int precision);
 // the work-queue sort: blocks of kSortBlock tracks, 64 length bins each
+// arrays of ck_batch_in staged for host batches (particle_pdg and
+// meas_subspace optional)
+constexpr int kInputArrays = 12;
 constexpr int kSortBlock = 1024;
 inline int sortBlocks(int n) { return n > 0 ? (n + kSortBlock - 1) / kSortBlock : 1; }
 inline size_t sortCountsBytes(int n) { return sizeof(int32_t) * 64 * (size_t)sortBlocks(n); }
@@ -98,7 +101,7 @@ struct ck_handle {
   std::string tuneLog;
   int useGraph = 1;
   bool sortQueue = true;
-  ck::DevBuf inBufs[11];
+  ck::DevBuf inBufs[ck::kInputArrays];
   ck::DevBuf outBufs[18];
   ck::FitContext ctx;
   ck::DevBuf unitBuf;

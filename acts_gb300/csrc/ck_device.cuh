@@ -817,6 +817,65 @@ CK_D double predictedChi2(const double pred[6], const double Pp[21], double m0, 
   return t0 * r0 + t1 * r1;
 }
 
+// visitMeasurementImpl<1>: a 1D measurement m (variance v) of bound
+// parameter h (0: loc0, 1: loc1), projector row e_h. S, the gain column and
+// the chi2 matrix are scalars (Eigen's 1x1 inverse is the reciprocal).
+template <bool FASTRCP = false>
+CK_D bool kalmanUpdate1(const double pred[6], const double Pp[21], int h, double m, double v,
+                        bool joseph, double filt[6], double F[21], double& chi2) {
+  double q[6];  // row h of Pp
+#pragma unroll
+  for (int j = 0; j < 6; ++j) q[j] = h ? Pp[sidx(1, j)] : Pp[sidx(0, j)];
+  const double S = (h ? q[1] : q[0]) + v;
+  const double iS = FASTRCP ? rcpRefined(S) : 1.0 / S;
+  double K[6];
+  bool nan = false;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    K[i] = q[i] * iS;
+    nan |= isnan(K[i]);
+  }
+  if (nan) return false;
+  const double r = m - (h ? pred[1] : pred[0]);
+#pragma unroll
+  for (int i = 0; i < 6; ++i) filt[i] = pred[i] + K[i] * r;
+  normalizePhiTheta(filt[2], filt[3]);
+  if (!joseph) {
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int j = i; j < 6; ++j) F[sidx(i, j)] = Pp[sidx(i, j)] - K[i] * q[j];
+  } else {
+    double AP[6][6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int j = 0; j < 6; ++j) AP[i][j] = Pp[sidx(i, j)] - K[i] * q[j];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      const double aph = h ? AP[i][1] : AP[i][0];
+      const double kv = K[i] * v;
+#pragma unroll
+      for (int j = i; j < 6; ++j) F[sidx(i, j)] = (AP[i][j] - aph * K[j]) + kv * K[j];
+    }
+  }
+  const double s = m - (h ? filt[1] : filt[0]);
+  const double mm = (1.0 - (h ? K[1] : K[0])) * v;
+  const double im = FASTRCP ? rcpRefined(mm) : 1.0 / mm;
+  chi2 = (s * im) * s;
+  return true;
+}
+
+// calculatePredictedChi2 of a 1D measurement of bound parameter h
+template <bool FASTRCP = false>
+CK_D double predictedChi2_1(const double pred[6], const double Pp[21], int h, double m,
+                            double v) {
+  const double r = m - (h ? pred[1] : pred[0]);
+  const double R = v + (h ? Pp[sidx(1, 1)] : Pp[sidx(0, 0)]);
+  const double iR = FASTRCP ? rcpRefined(R) : 1.0 / R;
+  return (r * iR) * r;
+}
+
 // ---------------------------------------------------------------- smoother
 // GainMatrixSmoother::calculate. Inputs: filtered state k (filt, Pf packed),
 // state k+1 predicted (pp, Ppp packed), its Jacobian J (row-major 36) and its
@@ -891,6 +950,9 @@ CK_D bool smoothStep(const double filt[6], const GP Pf[21], const double pp[6], 
 }
 
 // ------------------------------------------------- MbfSmoother (mBF form)
+template <typename GP>
+CK_D void mbfMeasurement1(const double pred[6], const GP Pp[21], int h, double m, double v,
+                          GP L[21], GP l[6]);
 // Modified Bryson-Frazier smoother (MbfSmoother.hpp:48-90,
 // MbfSmoother.cpp:17-48, MbfSmootherImpl.hpp:17-58): a backward pass that
 // carries Lambda (6x6 symmetric, packed) and lambda (6) from state to state;
@@ -1038,6 +1100,66 @@ CK_D void mbfMeasurement(const double pred[6], const GP Pp[21], double m0, doubl
   for (int i = 0; i < 21; ++i) L[i] = Lt[i];
 #pragma unroll
   for (int i = 0; i < 6; ++i) l[i] = lt[i];
+}
+
+// visitMeasurementImpl<1> before the transport: projector row e_h,
+// S = P_hh + v, K = P[:,h] / S, C = I - K e_h^T differs from I in column h.
+template <typename GP>
+CK_D void mbfMeasurement1(const double pred[6], const GP Pp[21], int h, double m, double v,
+                          GP L[21], GP l[6]) {
+  constexpr bool kFast = sizeof(GP) == sizeof(float);
+  const double S = (double)(h ? Pp[sidx(1, 1)] : Pp[sidx(0, 0)]) + v;
+  const double iS = kFast ? rcpRefined(S) : 1.0 / S;
+  GP K[6];
+#pragma unroll
+  for (int r = 0; r < 6; ++r) K[r] = (GP)((double)(h ? Pp[sidx(r, 1)] : Pp[sidx(r, 0)]) * iS);
+  // A = Lambda C: column h is Lambda[:,h] - Lambda K
+  GP A[6][6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 6; ++j) A[i][j] = L[sidx(i, j)];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    GP s = GP(0);
+#pragma unroll
+    for (int r = 0; r < 6; ++r) s += L[sidx(i, r)] * K[r];
+    if (h)
+      A[i][1] -= s;
+    else
+      A[i][0] -= s;
+  }
+  // Lambda~ = C^T A (+ 1/S at (h, h)): row h is A[h,:] - K^T A
+  GP Lt[21];
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = i; j < 6; ++j) {
+      GP val = A[i][j];
+      if (i == h) {
+        GP s = GP(0);
+#pragma unroll
+        for (int r = 0; r < 6; ++r) s += K[r] * A[r][j];
+        val -= s;
+      }
+      Lt[sidx(i, j)] = val;
+    }
+  if (h)
+    Lt[sidx(1, 1)] += (GP)iS;
+  else
+    Lt[sidx(0, 0)] += (GP)iS;
+  // lambda~ = C^T lambda - e_h (y / S), y = m - pred_h
+  const double y = m - (h ? pred[1] : pred[0]);
+  GP s = GP(0);
+#pragma unroll
+  for (int r = 0; r < 6; ++r) s += K[r] * l[r];
+  const GP upd = s + (GP)(iS * y);
+  if (h)
+    l[1] -= upd;
+  else
+    l[0] -= upd;
+#pragma unroll
+  for (int i = 0; i < 21; ++i) L[i] = Lt[i];
 }
 
 }  // namespace ck

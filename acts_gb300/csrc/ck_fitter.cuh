@@ -635,14 +635,22 @@ struct Lane {
       double V[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) V[i] = __ldg(&fp.meas_cov[4 * (size_t)mi + i]);
+      // (loc0, loc1), or a 1D measurement of loc h (value mv0, variance V[0])
+      const int sub = fp.meas_sub ? __ldg(&fp.meas_sub[mi]) : CK_MEAS_LOC01;
+      const bool twoD = sub == CK_MEAS_LOC01;
+      const int h = sub >> 1;
+      flags |= (uint32_t)sub << kRecSubShift;
       bool outlier = false;
       constexpr bool kFastRcp = sizeof(P) == sizeof(float);
       if (fp.opt.useOutlierCut)
-        outlier = predictedChi2<kFastRcp>(bp, Pp, mv0, mv1, V) > fp.opt.outlierChi2Cut;
+        outlier = (twoD ? predictedChi2<kFastRcp>(bp, Pp, mv0, mv1, V)
+                        : predictedChi2_1<kFastRcp>(bp, Pp, h, mv0, V[0])) > fp.opt.outlierChi2Cut;
       double chi2 = 0.0;
       if (!outlier) {
         double filt[6], F[21];
-        if (!kalmanUpdate<kFastRcp>(bp, Pp, mv0, mv1, V, fp.opt.joseph != 0, filt, F, chi2))
+        const bool joseph = fp.opt.joseph != 0;
+        if (!(twoD ? kalmanUpdate<kFastRcp>(bp, Pp, mv0, mv1, V, joseph, filt, F, chi2)
+                   : kalmanUpdate1<kFastRcp>(bp, Pp, h, mv0, V[0], joseph, filt, F, chi2)))
           return CK_TRACK_UPDATE_FAILED;
         flags |= CK_FLAG_HAS_MEASUREMENT;
 #pragma unroll
@@ -757,6 +765,10 @@ struct Lane {
       for (int i = 0; i < nMeas && !bad; ++i) {
         const int sid = __ldg(&fp.meas_surf[m0 + i]);
         bad |= sid < 0 || sid >= fp.n_surfaces;
+        if (fp.meas_sub) {
+          const int sub = __ldg(&fp.meas_sub[m0 + i]);
+          bad |= sub < CK_MEAS_LOC0 || sub > CK_MEAS_LOC01;
+        }
       }
       if (bad) {
         fail(fp, CK_TRACK_INVALID_INPUT);
@@ -1184,8 +1196,12 @@ struct Smoother {
         for (int i = 0; i < 21; ++i) Pp[i] = rec.m(k, kRecPredCov + i);
 #pragma unroll
         for (int i = 0; i < 4; ++i) V[i] = __ldg(&fp.meas_cov[4 * (size_t)mi + i]);
-        mbfMeasurement<CV>(pred, Pp, __ldg(&fp.meas_val[2 * (size_t)mi]),
-                           __ldg(&fp.meas_val[2 * (size_t)mi + 1]), V, L, l);
+        const int sub = ((uint32_t)rs.flags >> kRecSubShift) & 3u;
+        if (sub == CK_MEAS_LOC01)
+          mbfMeasurement<CV>(pred, Pp, __ldg(&fp.meas_val[2 * (size_t)mi]),
+                             __ldg(&fp.meas_val[2 * (size_t)mi + 1]), V, L, l);
+        else
+          mbfMeasurement1<CV>(pred, Pp, sub >> 1, __ldg(&fp.meas_val[2 * (size_t)mi]), V[0], L, l);
       }
       CV F[36];
 #pragma unroll
@@ -1224,7 +1240,8 @@ struct Smoother {
     const size_t n = (size_t)fp.n_tracks;
     auto at = [&](int C, int c) -> size_t { return ((size_t)k * C + c) * n + t; };
     const RecState<CV>& rs = rec.s(k);
-    const uint32_t fl = (uint32_t)rs.flags;
+    const uint32_t fl = (uint32_t)rs.flags & kRecFlagMask;
+    const int sub = ((uint32_t)rs.flags >> kRecSubShift) & 3u;
     const double c2 = rs.chi2;
     if (out.state_surface) out.state_surface[at(1, 0)] = rs.surface;
     if (out.state_flags) out.state_flags[at(1, 0)] = fl;
@@ -1238,7 +1255,7 @@ struct Smoother {
     } else if (fl & CK_FLAG_HAS_MEASUREMENT) {
       ++nM;
       chi2sum += c2;
-      ndf += 2;
+      ndf += (sub & 1) + (sub >> 1);
     }
     if (out.smoothed) {
 #pragma unroll

@@ -75,6 +75,9 @@ void setSilicon(ck_surface& s, float thickness) {
 
 const double kBarrelRadii[10] = {32, 72, 116, 172, 260, 360, 500, 660, 820, 1020};
 
+// the geometry / field / kinematics preset a preset shares
+int basePreset(int preset) { return preset == CKG_STRIPS ? CKG_BARREL : preset; }
+
 int barrelRadii(int preset, double* r) {
   if (preset == CKG_UNEVEN || preset == CKG_SERVING) {
     // the ten radii plus ten midpoints (the first between the beam line and
@@ -326,6 +329,7 @@ struct TrackRows {
   std::vector<int> seq, measSurf;
   std::vector<double> measVal, measCov, truth;
   std::vector<uint8_t> outlier;
+  std::vector<int32_t> measSub;
   double startParams[6], startCov[36], frame[12], truthStart[6];
   float particle[2];
   int pdg;
@@ -333,6 +337,8 @@ struct TrackRows {
 
 void generateTrack(int preset, uint64_t seed, int64_t id, const std::vector<ck_surface>& surf,
                    const FieldEval& F, TrackRows& out) {
+  const bool stripPreset = preset == CKG_STRIPS;
+  preset = basePreset(preset);
   Preset P = presetOf(preset);
   Rng rng(mix(seed, (uint64_t)id * 0x2545F4914F6CDD1Dull + (uint64_t)preset));
   Particle pa = P.pa;
@@ -471,20 +477,42 @@ void generateTrack(int preset, uint64_t seed, int64_t id, const std::vector<ck_s
     const bool outl = P.outlierProb > 0 && rng.uniform() < P.outlierProb;
     const double sgn0 = rng.uniform() < 0.5 ? -1.0 : 1.0;
     const double sgn1 = rng.uniform() < 0.5 ? -1.0 : 1.0;
-    double m0 = loc[0] + P.sigma0 * rng.gauss();
-    double m1 = loc[1] + P.sigma1 * rng.gauss();
-    if (!hole) {
+    const double g0 = rng.gauss();
+    const double g1 = rng.gauss();
+    // strip layers (CKG_STRIPS, layers 4-9): one local coordinate
+    int sub = CK_MEAS_LOC01;
+    if (stripPreset && sid >= 4) sub = (sid % 2 == 0) ? CK_MEAS_LOC0 : CK_MEAS_LOC1;
+    if (!hole && sub != CK_MEAS_LOC01) {
+      const int h = sub == CK_MEAS_LOC0 ? 0 : 1;
+      const double sg = h == 0 ? 0.100 : 0.150;
+      double m = loc[h] + sg * (h == 0 ? g0 : g1);
+      if (outl) m += (h == 0 ? sgn0 : sgn1) * P.outlierSigma * sg;
+      out.measSurf.push_back(sid);
+      out.measSub.push_back(sub);
+      out.measVal.push_back(m);
+      out.measVal.push_back(0.0);
+      out.measCov.push_back(sg * sg);
+      out.measCov.push_back(0.0);
+      out.measCov.push_back(0.0);
+      out.measCov.push_back(0.0);
+    }
+    double m0 = loc[0] + P.sigma0 * g0;
+    double m1 = loc[1] + P.sigma1 * g1;
+    if (!hole && sub == CK_MEAS_LOC01) {
       if (outl) {
         m0 += sgn0 * P.outlierSigma * P.sigma0;
         m1 += sgn1 * P.outlierSigma * P.sigma1;
       }
       out.measSurf.push_back(sid);
+      out.measSub.push_back(sub);
       out.measVal.push_back(m0);
       out.measVal.push_back(m1);
       out.measCov.push_back(P.sigma0 * P.sigma0);
       out.measCov.push_back(0.0);
       out.measCov.push_back(0.0);
       out.measCov.push_back(P.sigma1 * P.sigma1);
+    }
+    if (!hole) {
       out.truth.push_back(loc[0]);
       out.truth.push_back(loc[1]);
       out.truth.push_back(tphi);
@@ -535,6 +563,7 @@ void generateTrack(int preset, uint64_t seed, int64_t id, const std::vector<ck_s
 extern "C" {
 
 int32_t ckg_geometry(int32_t preset, ck_surface* out, int32_t cap) {
+  preset = basePreset(preset);
   std::vector<ck_surface> v;
   if (preset == CKG_TELESCOPE) {
     for (int i = 0; i < 10; ++i) {
@@ -573,11 +602,13 @@ int32_t ckg_geometry(int32_t preset, ck_surface* out, int32_t cap) {
 }
 
 int64_t ckg_field_values(int32_t preset) {
+  preset = basePreset(preset);
   if (preset == CKG_UNEVEN || preset == CKG_SERVING) return (int64_t)151 * 151 * 301 * 3;
   return 0;
 }
 
 void ckg_field(int32_t preset, float* values, ck_field* out, int32_t n_threads) {
+  preset = basePreset(preset);
   std::memset(out, 0, sizeof(*out));
   if (preset != CKG_UNEVEN && preset != CKG_SERVING) {
     out->kind = CK_FIELD_CONSTANT;
@@ -643,6 +674,7 @@ int64_t ckg_generate(int32_t preset, uint64_t seed, int64_t first_track, int32_t
       if (out->truth_meas)
         for (int c = 0; c < 6; ++c) out->truth_meas[6 * (nm + k) + c] = r.truth[6 * k + c];
       if (out->meas_outlier) out->meas_outlier[nm + k] = r.outlier[k];
+      if (out->meas_subspace) out->meas_subspace[nm + k] = r.measSub[k];
     }
     ns += nseq;
     nm += nmeas;

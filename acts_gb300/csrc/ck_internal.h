@@ -67,6 +67,11 @@ struct DevOptions {
 // the matrices in the covariance type CV of the form (predicted cov 21 and
 // filtered cov 21, packed upper; jacobian 36). A lane writes its state's
 // block as a whole, so DRAM sees full sectors.
+// The record's flags word holds the CK_FLAG_* type flags in its low 16 bits
+// and, for measurement states, the measurement's subspace (CK_MEAS_*) from
+// bit 16.
+constexpr int kRecSubShift = 16;
+constexpr uint32_t kRecFlagMask = 0xffffu;
 constexpr int kRecPred = 0;
 constexpr int kRecFilt = 6;
 constexpr int kRecParams = 12;
@@ -95,6 +100,7 @@ struct FitParams {
   const int32_t* meas_surf;
   const double* meas_val;
   const double* meas_cov;
+  const int32_t* meas_sub;  // CK_MEAS_* per measurement, or NULL (all 2D)
   const double* start_params;
   const double* start_cov;
   const double* start_frames;

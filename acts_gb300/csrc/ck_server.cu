@@ -74,8 +74,8 @@ struct Slot {
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
   FitContext ctx;
-  DevBuf din[11];
-  size_t inPlanned[11] = {};
+  DevBuf din[kInputArrays];
+  size_t inPlanned[kInputArrays] = {};
   DevBuf dout[18];
   DevBuf table;              // per-event {t0, m, seqBase, measBase} on the device
   int32_t* pinTable = nullptr;
@@ -149,7 +149,7 @@ struct ck_server {
   // track, outputs of the computed components, track-state records
   size_t perTrackBytes(int maxStates) const {
     const size_t k = kPlannedSurfacesPerTrack;
-    const size_t in = 2 * 4 + k * 4 + k * (4 + 16 + 32) + 48 + 288 + 96 + 8 + 4;
+    const size_t in = 2 * 4 + k * 4 + k * (4 + 16 + 32 + 4) + 48 + 288 + 96 + 8 + 4;
     size_t out = 7 * 8 + (size_t)maxStates * 24;
     if (spec.sm) out += (size_t)maxStates * 42 * 8;
     if (spec.fi) out += (size_t)maxStates * 42 * 8;
@@ -178,10 +178,10 @@ ck_status slotAlloc(ck_server* s, Slot& sl) {
   const size_t cap = (size_t)s->capacity;
   const size_t k = kPlannedSurfacesPerTrack;
   const int ms = s->cfg.max_states;
-  const size_t inBytes[11] = {4 * (cap + 1), 4 * cap * k, 4 * (cap + 1), 4 * cap * k,
-                              16 * cap * k,  32 * cap * k, 48 * cap,  288 * cap,
-                              96 * cap,      8 * cap,      4 * cap};
-  for (int i = 0; i < 11; ++i) {
+  const size_t inBytes[kInputArrays] = {4 * (cap + 1), 4 * cap * k, 4 * (cap + 1), 4 * cap * k,
+                                        16 * cap * k,  32 * cap * k, 48 * cap,  288 * cap,
+                                        96 * cap,      8 * cap,      4 * cap,   4 * cap * k};
+  for (int i = 0; i < kInputArrays; ++i) {
     if ((e = sl.din[i].ensure(inBytes[i])) != cudaSuccess) return cudaFail(e, "server input");
     sl.inPlanned[i] = inBytes[i];
   }
@@ -248,6 +248,7 @@ ck_status launchSlot(ck_server* s, Slot& sl) {
         {8, in.start_frames, 96 * (size_t)t0, 96 * (size_t)m},
         {9, in.particle, 8 * (size_t)t0, 8 * (size_t)m},
         {10, in.particle_pdg, 4 * (size_t)t0, 4 * (size_t)m},
+        {11, in.meas_subspace, 4 * (size_t)measBase, 4 * (size_t)ev.nMeas},
     };
     for (const Item& it : items) {
       if (!it.bytes) continue;
@@ -256,6 +257,11 @@ ck_status launchSlot(ck_server* s, Slot& sl) {
       char* dst = (char*)sl.din[it.buf].p + it.dstOff;
       if (it.buf == 10 && !it.src) {
         fillInt<<<(m + 255) / 256, 256, 0, sl.stream>>>((int32_t*)dst, m, 211);
+        continue;
+      }
+      if (it.buf == 11 && !it.src) {  // 2D source links
+        const int nm = ev.nMeas;
+        fillInt<<<(nm + 255) / 256, 256, 0, sl.stream>>>((int32_t*)dst, nm, CK_MEAS_LOC01);
         continue;
       }
       if ((e = cudaMemcpyAsync(dst, it.src, it.bytes, cudaMemcpyDefault, sl.stream)) !=
@@ -289,6 +295,7 @@ ck_status launchSlot(ck_server* s, Slot& sl) {
   din.start_frames = (const double*)sl.din[8].p;
   din.particle = (const float*)sl.din[9].p;
   din.particle_pdg = (const int32_t*)sl.din[10].p;
+  din.meas_subspace = (const int32_t*)sl.din[11].p;
   ck_batch_out dout{};
   dout.max_states = s->cfg.max_states;
   dout.memory = CK_MEM_DEVICE;

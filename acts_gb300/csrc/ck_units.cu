@@ -17,7 +17,8 @@ namespace {
 
 __global__ void updateKernel(int n, int joseph, const double* __restrict__ pred,
                              const double* __restrict__ predCov, const double* __restrict__ meas,
-                             const double* __restrict__ measCov, double* filt, double* filtCov,
+                             const double* __restrict__ measCov,
+                             const int32_t* __restrict__ sub, double* filt, double* filtCov,
                              double* chi2, int32_t* status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -26,7 +27,11 @@ __global__ void updateKernel(int n, int joseph, const double* __restrict__ pred,
   for (int r = 0; r < 6; ++r)
     for (int c = r; c < 6; ++c) P[sidx(r, c)] = predCov[36 * i + r * 6 + c];
   for (int k = 0; k < 4; ++k) V[k] = measCov[4 * i + k];
-  const bool ok = kalmanUpdate(p, P, meas[2 * i], meas[2 * i + 1], V, joseph != 0, f, F, c2);
+  const int s = sub ? sub[i] : CK_MEAS_LOC01;
+  const bool ok =
+      s == CK_MEAS_LOC01
+          ? kalmanUpdate(p, P, meas[2 * i], meas[2 * i + 1], V, joseph != 0, f, F, c2)
+          : kalmanUpdate1(p, P, s >> 1, meas[2 * i], V[0], joseph != 0, f, F, c2);
   status[i] = ok ? CK_TRACK_OK : CK_TRACK_UPDATE_FAILED;
   if (!ok) return;
   for (int k = 0; k < 6; ++k) filt[6 * i + k] = f[k];
@@ -172,11 +177,16 @@ extern "C" {
 
 ck_status ck_gain_matrix_update(ck_handle* h, int32_t n, int32_t use_joseph,
                                 const double* predicted, const double* predicted_cov,
-                                const double* meas, const double* meas_cov, double* filtered,
+                                const double* meas, const double* meas_cov,
+                                const int32_t* subspace, double* filtered,
                                 double* filtered_cov, double* chi2, int32_t* status) {
   if (!h || n < 0 || !predicted || !predicted_cov || !meas || !meas_cov || !filtered ||
       !filtered_cov || !chi2 || !status)
     return fail(CK_ERR_INVALID_ARGUMENT, "bad argument");
+  if (subspace)
+    for (int i = 0; i < n; ++i)
+      if (subspace[i] < CK_MEAS_LOC0 || subspace[i] > CK_MEAS_LOC01)
+        return fail(CK_ERR_INVALID_ARGUMENT, "unknown measurement subspace");
   if (n == 0) return CK_OK;
   std::lock_guard<std::mutex> lock(h->mu);
   cudaSetDevice(h->device);
@@ -189,6 +199,7 @@ ck_status ck_gain_matrix_update(ck_handle* h, int32_t n, int32_t use_joseph,
   void* tFC = a.add(288 * n);
   void* tC = a.add(8 * n);
   void* tS = a.add(4 * n);
+  void* tSub = a.add(4 * n);
   cudaError_t e = a.commit();
   if (e != cudaSuccess) return cudaFail(e, "unit buffer");
   cudaStream_t st = h->stream;
@@ -196,9 +207,11 @@ ck_status ck_gain_matrix_update(ck_handle* h, int32_t n, int32_t use_joseph,
   cudaMemcpyAsync(a.at<double>(tPC), predicted_cov, 288 * n, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(a.at<double>(tM), meas, 16 * n, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(a.at<double>(tMC), meas_cov, 32 * n, cudaMemcpyHostToDevice, st);
+  if (subspace) cudaMemcpyAsync(a.at<int32_t>(tSub), subspace, 4 * n, cudaMemcpyHostToDevice, st);
   updateKernel<<<(n + 127) / 128, 128, 0, st>>>(
       n, use_joseph, a.at<double>(tP), a.at<double>(tPC), a.at<double>(tM), a.at<double>(tMC),
-      a.at<double>(tF), a.at<double>(tFC), a.at<double>(tC), a.at<int32_t>(tS));
+      subspace ? a.at<int32_t>(tSub) : nullptr, a.at<double>(tF), a.at<double>(tFC),
+      a.at<double>(tC), a.at<int32_t>(tS));
   cudaMemcpyAsync(filtered, a.at<double>(tF), 48 * n, cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(filtered_cov, a.at<double>(tFC), 288 * n, cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(chi2, a.at<double>(tC), 8 * n, cudaMemcpyDeviceToHost, st);

@@ -78,7 +78,8 @@ def lib():
                                   P(abi.ck_batch_out)]
         L.ck_autotune_log.restype = C.c_char_p
         L.ck_autotune_log.argtypes = [C.c_void_p]
-        L.ck_gain_matrix_update.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [abi.P_f64] * 7 + [abi.P_i32]
+        L.ck_gain_matrix_update.argtypes = ([C.c_void_p, C.c_int32, C.c_int32] + [abi.P_f64] * 4 +
+                                            [abi.P_i32] + [abi.P_f64] * 3 + [abi.P_i32])
         L.ck_gain_matrix_smooth.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [abi.P_f64] * 7 + [abi.P_i32]
         L.ck_mbf_smooth.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_uint32)] + [abi.P_f64] * 9
         L.ck_material_effects.argtypes = [C.c_void_p, C.c_int32, abi.P_i32, abi.P_f32, abi.P_f64,
@@ -359,15 +360,17 @@ class CudaKalman:
         return track_result(res, 0)
 
     # ------------------------------------------------------ unit operators
-    def gain_matrix_update(self, pred, pred_cov, meas, meas_cov, joseph=False):
+    def gain_matrix_update(self, pred, pred_cov, meas, meas_cov, joseph=False, subspace=None):
         n = len(pred)
         f = np.zeros((n, 6))
         fc = np.zeros((n, 36))
         chi2 = np.zeros(n)
         st = np.zeros(n, np.int32)
         a = [np.ascontiguousarray(x, np.float64) for x in (pred, pred_cov, meas, meas_cov)]
+        sub = None if subspace is None else np.ascontiguousarray(subspace, np.int32)
         _check(lib().ck_gain_matrix_update(self._h, n, int(joseph),
                                            *[abi.ptr(x, C.c_double) for x in a],
+                                           abi.ptr(sub, C.c_int32),
                                            abi.ptr(f, C.c_double), abi.ptr(fc, C.c_double),
                                            abi.ptr(chi2, C.c_double), abi.ptr(st, C.c_int32)))
         return f, fc.reshape(n, 6, 6), chi2, st

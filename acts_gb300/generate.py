@@ -77,6 +77,8 @@ class Batch:
         self.truth_meas = np.zeros(n * cap * 6, np.float64)
         self.meas_outlier = np.zeros(n * cap, np.uint8)
         self.truth_start = np.zeros(n * 6, np.float64)
+        # CK_MEAS_* per measurement; None: every source link is 2D
+        self.meas_subspace = None
 
     def trim(self):
         ns = int(self.seq_offsets[-1])
@@ -87,6 +89,8 @@ class Batch:
         self.meas_cov = np.ascontiguousarray(self.meas_cov[: 4 * nm])
         self.truth_meas = np.ascontiguousarray(self.truth_meas[: 6 * nm])
         self.meas_outlier = np.ascontiguousarray(self.meas_outlier[:nm])
+        if self.meas_subspace is not None:
+            self.meas_subspace = np.ascontiguousarray(self.meas_subspace[:nm])
         return self
 
     @property
@@ -108,6 +112,7 @@ class Batch:
         b.start_frames = abi.ptr(self.start_frames, C.c_double)
         b.particle = abi.ptr(self.particle, C.c_float)
         b.particle_pdg = abi.ptr(self.particle_pdg, C.c_int32)
+        b.meas_subspace = abi.ptr(self.meas_subspace, C.c_int32)
         return b
 
     def subset(self, idx):
@@ -115,7 +120,7 @@ class Batch:
         idx = np.asarray(idx, dtype=np.int64)
         so, mo = self.seq_offsets, self.meas_offsets
         out = Batch(len(idx), self.cap)
-        seq, ms, mv, mc, tm, mol = [], [], [], [], [], []
+        seq, ms, mv, mc, tm, mol, msub = [], [], [], [], [], [], []
         for j, t in enumerate(idx):
             a, b = so[t], so[t + 1]
             seq.append(self.seq_surfaces[a:b])
@@ -126,6 +131,8 @@ class Batch:
             mc.append(self.meas_cov[4 * a:4 * b])
             tm.append(self.truth_meas[6 * a:6 * b])
             mol.append(self.meas_outlier[a:b])
+            if self.meas_subspace is not None:
+                msub.append(self.meas_subspace[a:b])
             out.meas_offsets[j + 1] = out.meas_offsets[j] + (b - a)
         cat = lambda xs, dt: np.ascontiguousarray(np.concatenate(xs).astype(dt)) if xs else np.zeros(0, dt)
         out.seq_surfaces = cat(seq, np.int32)
@@ -134,6 +141,7 @@ class Batch:
         out.meas_cov = cat(mc, np.float64)
         out.truth_meas = cat(tm, np.float64)
         out.meas_outlier = cat(mol, np.uint8)
+        out.meas_subspace = cat(msub, np.int32) if self.meas_subspace is not None else None
         for name, k in (("start_params", 6), ("start_cov", 36), ("start_frames", 12),
                         ("particle", 2), ("truth_start", 6)):
             src = getattr(self, name).reshape(self.n, k)
@@ -154,6 +162,9 @@ def generate(detector, n_tracks, seed=1, first_track=0, n_threads=None, cap=24):
         setattr(o, name, abi.ptr(getattr(b, name), C.c_double))
     o.particle = abi.ptr(b.particle, C.c_float)
     o.meas_outlier = abi.ptr(b.meas_outlier, C.c_uint8)
+    if detector.preset == abi.CKG_STRIPS:
+        b.meas_subspace = np.zeros(n_tracks * cap, np.int32)
+        o.meas_subspace = abi.ptr(b.meas_subspace, C.c_int32)
     nm = L.ckg_generate(detector.preset, seed, first_track, n_tracks, detector.surfaces,
                         detector.n_surfaces, C.byref(detector.field),
                         n_threads or os.cpu_count() or 1, C.byref(o))

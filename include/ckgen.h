@@ -31,7 +31,12 @@ enum {
   CKG_BARREL_MIXED = 3,/* geometry and tracks of CKG_BARREL                  */
   CKG_UNEVEN = 4,      /* 20 Si cylinders, grid field, 4-20 hits, holes,
                           outliers                                         */
-  CKG_SERVING = 5      /* tracks of CKG_UNEVEN                               */
+  CKG_SERVING = 5,     /* tracks of CKG_UNEVEN                               */
+  CKG_STRIPS = 6       /* geometry, field and tracks of CKG_BARREL; the outer
+                          six layers are read out by strips: 1D measurements
+                          of loc0 (100 um) and loc1 (150 um) on alternate
+                          layers, as the reference's KF test detector
+                          (FitterTestsCommon.hpp:146-154)                  */
 };
 
 typedef struct ckg_out {
@@ -51,6 +56,7 @@ typedef struct ckg_out {
                               measurement (may be NULL)                    */
   uint8_t* meas_outlier;   /* [n*max_per_track] 1 = displaced (may be NULL) */
   double* truth_start;     /* [n*6] true start parameters (may be NULL)    */
+  int32_t* meas_subspace;  /* [n*max_per_track] CK_MEAS_* (may be NULL)    */
 } ckg_out;
 
 /* Surface table of a preset; returns the number of surfaces written

@@ -243,15 +243,27 @@ typedef struct ck_batch_in {
   const int32_t* seq_surfaces;   /* [seq_offsets[n_tracks]] surface ids     */
   const int32_t* meas_offsets;   /* [n_tracks+1]                            */
   const int32_t* meas_surfaces;  /* [n_meas] surface id of each source link */
-  const double* meas_values;     /* [n_meas*2] (loc0, loc1)                 */
-  const double* meas_cov;        /* [n_meas*4] row-major 2x2                */
+  const double* meas_values;     /* [n_meas*2] (loc0, loc1); 1D: see below  */
+  const double* meas_cov;        /* [n_meas*4] row-major 2x2; 1D: see below */
   const double* start_params;    /* [n_tracks*6] bound parameters           */
   const double* start_cov;       /* [n_tracks*36] row-major                 */
   const double* start_frames;    /* [n_tracks*12] start plane: rotation (9,
                                     row-major, columns = local axes) + center */
   const float* particle;         /* [n_tracks*2] (mass GeV, |q|)            */
   const int32_t* particle_pdg;   /* [n_tracks] absolute PDG id              */
+  /* [n_meas] measured bound parameters of each source link, the projector's
+   * subspace (BoundSubspaceIndices; MeasurementsCreator's eLoc0 / eLoc1 /
+   * eLoc01): CK_MEAS_LOC0 or CK_MEAS_LOC1 for a 1D (strip) measurement,
+   * whose value is meas_values[2m] and variance meas_cov[4m] (the other
+   * slots are ignored), CK_MEAS_LOC01 for a 2D one. NULL: every source link
+   * is 2D. The updater, outlier chi2, ndf and MbfSmoother use the subspace
+   * (GainMatrixUpdaterImpl.hpp:95-104 instantiates N = 1..6; N = 1, 2 with
+   * local-coordinate projectors here). */
+  const int32_t* meas_subspace;
 } ck_batch_in;
+
+/* Measurement subspaces (bit i: bound parameter i is measured). */
+enum { CK_MEAS_LOC0 = 1, CK_MEAS_LOC1 = 2, CK_MEAS_LOC01 = 3 };
 
 /* Which per-state components to write (TrackStatePropMask analogue). */
 enum {
@@ -401,16 +413,18 @@ ck_status ck_autotune(ck_handle* h, const ck_options* opt,
 
 /* ---------------------------------------------- unit operators (batched) */
 
-/* GainMatrixUpdater::operator() for N = 2 (loc0, loc1) on a batch of track
- * states (Core/include/Acts/TrackFitting/detail/GainMatrixUpdaterImpl.hpp
- * :21-91). Arrays are AoS per state: predicted[6], predicted_cov[36],
- * meas[2], meas_cov[4]; outputs filtered[6], filtered_cov[36], chi2[1],
- * status[1] (CK_TRACK_OK or CK_TRACK_UPDATE_FAILED). Host pointers;
- * synchronous. */
+/* GainMatrixUpdater::operator() on a batch of track states
+ * (Core/include/Acts/TrackFitting/detail/GainMatrixUpdaterImpl.hpp:21-91):
+ * N = 2 (loc0, loc1), or N = 1 where subspace[i] (CK_MEAS_*, NULL = all
+ * 2D) selects one local coordinate. Arrays are AoS per state:
+ * predicted[6], predicted_cov[36], meas[2], meas_cov[4] (1D: meas[0],
+ * meas_cov[0]); outputs filtered[6], filtered_cov[36], chi2[1], status[1]
+ * (CK_TRACK_OK or CK_TRACK_UPDATE_FAILED). Host pointers; synchronous. */
 ck_status ck_gain_matrix_update(ck_handle* h, int32_t n, int32_t use_joseph,
                                 const double* predicted,
                                 const double* predicted_cov,
                                 const double* meas, const double* meas_cov,
+                                const int32_t* subspace,
                                 double* filtered, double* filtered_cov,
                                 double* chi2, int32_t* status);
 

@@ -111,6 +111,7 @@ int kfo_count_flops(const ck_options* opt, int n_surfaces, const ck_surface* sur
     for (int m = in->meas_offsets[tr]; m < in->meas_offsets[tr + 1]; ++m) {
       MeasRec<Flop> r;
       r.surface = in->meas_surfaces[m];
+      r.sub = in->meas_subspace ? in->meas_subspace[m] : CK_MEAS_LOC01;
       r.v[0] = in->meas_values[2 * m];
       r.v[1] = in->meas_values[2 * m + 1];
       for (int c = 0; c < 4; ++c) r.cov[c] = in->meas_cov[4 * m + c];

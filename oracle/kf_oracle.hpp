@@ -1174,9 +1174,19 @@ struct TrackOut {
 template <typename S>
 struct MeasRec {
   int surface;
-  double v[2];
-  double cov[4];
+  int sub = CK_MEAS_LOC01;  // measured bound parameters (CK_MEAS_*)
+  double v[2];              // measured values, packed (1D: v[0])
+  double cov[4];            // covariance, packed row-major (1D: cov[0])
 };
+
+// Projector indices of a subspace mask (the measured local coordinates in
+// increasing order) and its dimension.
+inline int subspaceIndices(int sub, int idx[2]) {
+  int n = 0;
+  for (int i = 0; i < 2; ++i)
+    if (sub & (1 << i)) idx[n++] = i;
+  return n;
+}
 
 template <typename S>
 void put6(double* d, const Vec<S, 6>& v) {
@@ -1201,30 +1211,53 @@ Mat<S, 6, 6> get36(const double* d) {
   return m;
 }
 
-// GainMatrixUpdater::visitMeasurementImpl<2> (GainMatrixUpdaterImpl.hpp:21-91)
+// Inverse of a 1x1 / 2x2 matrix as Eigen's fixed-size inverse computes it
+// (reciprocal; adjugate over determinant).
 template <typename S>
-bool gainMatrixUpdate(const Vec<S, 6>& pred, const Mat<S, 6, 6>& P, const double meas[2],
-                      const double mcov[4], bool joseph, Vec<S, 6>& filt, Mat<S, 6, 6>& F,
-                      S& chi2) {
-  Mat<S, 2, 6> H = Mat<S, 2, 6>::zero();
-  H.a[0][0] = S(1.0);
-  H.a[1][1] = S(1.0);
-  Mat<S, 6, 2> Ht = transpose(H);
-  Mat<S, 2, 2> V;
-  V.a[0][0] = S(mcov[0]);
-  V.a[0][1] = S(mcov[1]);
-  V.a[1][0] = S(mcov[2]);
-  V.a[1][1] = S(mcov[3]);
-  Mat<S, 2, 2> Sm = add(mul(mul(H, P), Ht), V);
-  Mat<S, 6, 2> K = mul(mul(P, Ht), inverse2(Sm));
+Mat<S, 1, 1> inverseSmall(const Mat<S, 1, 1>& m) {
+  Mat<S, 1, 1> r;
+  r.a[0][0] = S(1.0) / m.a[0][0];
+  return r;
+}
+template <typename S>
+Mat<S, 2, 2> inverseSmall(const Mat<S, 2, 2>& m) {
+  return inverse2(m);
+}
+
+// Projector H (N x 6) with rows e_idx[k] (FixedBoundSubspaceHelper::projector)
+template <typename S, int N>
+Mat<S, N, 6> projector(const int idx[N]) {
+  Mat<S, N, 6> H = Mat<S, N, 6>::zero();
+  for (int k = 0; k < N; ++k) H.a[k][idx[k]] = S(1.0);
+  return H;
+}
+
+template <typename S, int N>
+Mat<S, N, N> measCovN(const double* mcov) {
+  Mat<S, N, N> V;
+  for (int r = 0; r < N; ++r)
+    for (int c = 0; c < N; ++c) V.a[r][c] = S(mcov[r * N + c]);
+  return V;
+}
+
+// GainMatrixUpdater::visitMeasurementImpl<N> (GainMatrixUpdaterImpl.hpp:21-91)
+// for an N-dimensional measurement of the bound parameters idx[0..N-1];
+// meas / mcov hold the N values and the N x N covariance, packed.
+template <typename S, int N>
+bool gainMatrixUpdateN(const Vec<S, 6>& pred, const Mat<S, 6, 6>& P, const int idx[N],
+                       const double* meas, const double* mcov, bool joseph, Vec<S, 6>& filt,
+                       Mat<S, 6, 6>& F, S& chi2) {
+  const Mat<S, N, 6> H = projector<S, N>(idx);
+  const Mat<S, 6, N> Ht = transpose(H);
+  const Mat<S, N, N> V = measCovN<S, N>(mcov);
+  Mat<S, N, N> Sm = add(mul(mul(H, P), Ht), V);
+  Mat<S, 6, N> K = mul(mul(P, Ht), inverseSmall(Sm));
   if (hasNaN(K)) return false;
-  Vec<S, 2> m;
-  m[0] = S(meas[0]);
-  m[1] = S(meas[1]);
-  Vec<S, 2> Hp = mulv(H, pred);
-  Vec<S, 2> r;
-  r[0] = m[0] - Hp[0];
-  r[1] = m[1] - Hp[1];
+  Vec<S, N> m;
+  for (int k = 0; k < N; ++k) m[k] = S(meas[k]);
+  Vec<S, N> Hp = mulv(H, pred);
+  Vec<S, N> r;
+  for (int k = 0; k < N; ++k) r[k] = m[k] - Hp[k];
   Vec<S, 6> Kr = mulv(K, r);
   for (int i = 0; i < 6; ++i) filt[i] = pred[i] + Kr[i];
   filt = normalizeBoundParameters(filt);
@@ -1234,35 +1267,73 @@ bool gainMatrixUpdate(const Vec<S, 6>& pred, const Mat<S, 6, 6>& P, const double
   } else {
     F = add(mul(mul(tmp, P), transpose(tmp)), mul(mul(K, V), transpose(K)));
   }
-  Vec<S, 2> Hf = mulv(H, filt);
-  Vec<S, 2> res;
-  res[0] = m[0] - Hf[0];
-  res[1] = m[1] - Hf[1];
-  Mat<S, 2, 2> mm = mul(sub(Mat<S, 2, 2>::identity(), mul(H, K)), V);
-  Mat<S, 2, 2> mi = inverse2(mm);
+  Vec<S, N> Hf = mulv(H, filt);
+  Vec<S, N> res;
+  for (int k = 0; k < N; ++k) res[k] = m[k] - Hf[k];
+  Mat<S, N, N> mm = mul(sub(Mat<S, N, N>::identity(), mul(H, K)), V);
+  Mat<S, N, N> mi = inverseSmall(mm);
   // (r^T mi) r
-  S t0 = res[0] * mi.a[0][0] + res[1] * mi.a[1][0];
-  S t1 = res[0] * mi.a[0][1] + res[1] * mi.a[1][1];
-  chi2 = t0 * res[0] + t1 * res[1];
+  chi2 = S(0.0);
+  for (int c = 0; c < N; ++c) {
+    S t = S(0.0);
+    for (int k = 0; k < N; ++k) t = t + res[k] * mi.a[k][c];
+    chi2 = chi2 + t * res[c];
+  }
   return true;
 }
 
-// calculatePredictedChi2 (TrackHelpers.hpp:563-694)
+// the (loc0, loc1) case
+template <typename S>
+bool gainMatrixUpdate(const Vec<S, 6>& pred, const Mat<S, 6, 6>& P, const double meas[2],
+                      const double mcov[4], bool joseph, Vec<S, 6>& filt, Mat<S, 6, 6>& F,
+                      S& chi2) {
+  const int idx[2] = {0, 1};
+  return gainMatrixUpdateN<S, 2>(pred, P, idx, meas, mcov, joseph, filt, F, chi2);
+}
+
+// the update of a source link of any supported subspace
+template <typename S>
+bool gainMatrixUpdateSub(const Vec<S, 6>& pred, const Mat<S, 6, 6>& P, const MeasRec<S>& m,
+                         bool joseph, Vec<S, 6>& filt, Mat<S, 6, 6>& F, S& chi2) {
+  int idx[2] = {0, 1};
+  if (subspaceIndices(m.sub, idx) == 1)
+    return gainMatrixUpdateN<S, 1>(pred, P, idx, m.v, m.cov, joseph, filt, F, chi2);
+  return gainMatrixUpdateN<S, 2>(pred, P, idx, m.v, m.cov, joseph, filt, F, chi2);
+}
+
+// calculatePredictedChi2 (TrackHelpers.hpp:563-694): residual m - H pred,
+// residual covariance V + H P H^T, chi2 = (r^T R^-1) r
+template <typename S, int N>
+S predictedChi2N(const Vec<S, 6>& pred, const Mat<S, 6, 6>& P, const int idx[N],
+                 const double* meas, const double* mcov) {
+  Vec<S, N> r;
+  Mat<S, N, N> Rc;
+  for (int k = 0; k < N; ++k) {
+    r[k] = S(meas[k]) - pred[idx[k]];
+    for (int c = 0; c < N; ++c) Rc.a[k][c] = S(mcov[k * N + c]) + P.a[idx[k]][idx[c]];
+  }
+  Mat<S, N, N> ri = inverseSmall(Rc);
+  S chi2 = S(0.0);
+  for (int c = 0; c < N; ++c) {
+    S t = S(0.0);
+    for (int k = 0; k < N; ++k) t = t + r[k] * ri.a[k][c];
+    chi2 = chi2 + t * r[c];
+  }
+  return chi2;
+}
+
 template <typename S>
 S predictedChi2(const Vec<S, 6>& pred, const Mat<S, 6, 6>& P, const double meas[2],
                 const double mcov[4]) {
-  Vec<S, 2> r;
-  r[0] = S(meas[0]) - pred[0];
-  r[1] = S(meas[1]) - pred[1];
-  Mat<S, 2, 2> Rc;
-  Rc.a[0][0] = S(mcov[0]) + P.a[0][0];
-  Rc.a[0][1] = S(mcov[1]) + P.a[0][1];
-  Rc.a[1][0] = S(mcov[2]) + P.a[1][0];
-  Rc.a[1][1] = S(mcov[3]) + P.a[1][1];
-  Mat<S, 2, 2> ri = inverse2(Rc);
-  S t0 = r[0] * ri.a[0][0] + r[1] * ri.a[1][0];
-  S t1 = r[0] * ri.a[0][1] + r[1] * ri.a[1][1];
-  return t0 * r[0] + t1 * r[1];
+  const int idx[2] = {0, 1};
+  return predictedChi2N<S, 2>(pred, P, idx, meas, mcov);
+}
+
+template <typename S>
+S predictedChi2Sub(const Vec<S, 6>& pred, const Mat<S, 6, 6>& P, const MeasRec<S>& m) {
+  int idx[2] = {0, 1};
+  if (subspaceIndices(m.sub, idx) == 1) return predictedChi2N<S, 1>(pred, P, idx, m.v, m.cov);
+  return predictedChi2N<S, 2>(pred, P, idx, m.v, m.cov);
 }
 
 // GainMatrixSmoother::calculate (GainMatrixSmoother.cpp:18-97)
@@ -1304,29 +1375,22 @@ void mbfVisitNonMeasurement(const Mat<S, 6, 6>& F, Mat<S, 6, 6>& L, Vec<S, 6>& l
   l = mulv(transpose(F), l);
 }
 
-// MbfSmoother::visitMeasurementImpl<2> (MbfSmootherImpl.hpp:17-58) with the
-// (loc0, loc1) projector.
-template <typename S>
-void mbfVisitMeasurement(const Mat<S, 6, 6>& F, const Vec<S, 6>& pred, const Mat<S, 6, 6>& Pp,
-                         const double meas[2], const double mcov[4], Mat<S, 6, 6>& L,
-                         Vec<S, 6>& l) {
-  Mat<S, 2, 6> H = Mat<S, 2, 6>::zero();
-  H.a[0][0] = S(1.0);
-  H.a[1][1] = S(1.0);
-  Mat<S, 6, 2> Ht = transpose(H);
-  Mat<S, 2, 2> V;
-  V.a[0][0] = S(mcov[0]);
-  V.a[0][1] = S(mcov[1]);
-  V.a[1][0] = S(mcov[2]);
-  V.a[1][1] = S(mcov[3]);
-  Mat<S, 2, 2> Sm = add(mul(mul(H, Pp), Ht), V);
-  Mat<S, 2, 2> Si = inverse2(Sm);
-  Mat<S, 6, 2> K = mul(mul(Pp, Ht), Si);
+// MbfSmoother::visitMeasurementImpl<N> (MbfSmootherImpl.hpp:17-58) for an
+// N-dimensional measurement of the bound parameters idx[0..N-1].
+template <typename S, int N>
+void mbfVisitMeasurementN(const Mat<S, 6, 6>& F, const Vec<S, 6>& pred, const Mat<S, 6, 6>& Pp,
+                          const int idx[N], const double* meas, const double* mcov,
+                          Mat<S, 6, 6>& L, Vec<S, 6>& l) {
+  const Mat<S, N, 6> H = projector<S, N>(idx);
+  const Mat<S, 6, N> Ht = transpose(H);
+  const Mat<S, N, N> V = measCovN<S, N>(mcov);
+  Mat<S, N, N> Sm = add(mul(mul(H, Pp), Ht), V);
+  Mat<S, N, N> Si = inverseSmall(Sm);
+  Mat<S, 6, N> K = mul(mul(Pp, Ht), Si);
   Mat<S, 6, 6> C = sub(Mat<S, 6, 6>::identity(), mul(K, H));
-  Vec<S, 2> Hp = mulv(H, pred);
-  Vec<S, 2> y;
-  y[0] = S(meas[0]) - Hp[0];
-  y[1] = S(meas[1]) - Hp[1];
+  Vec<S, N> Hp = mulv(H, pred);
+  Vec<S, N> y;
+  for (int k = 0; k < N; ++k) y[k] = S(meas[k]) - Hp[k];
   Mat<S, 6, 6> Lt = add(mul(mul(Ht, Si), H), mul(mul(transpose(C), L), C));
   Vec<S, 6> a = mulv(mul(Ht, Si), y);
   Vec<S, 6> b = mulv(transpose(C), l);
@@ -1334,6 +1398,26 @@ void mbfVisitMeasurement(const Mat<S, 6, 6>& F, const Vec<S, 6>& pred, const Mat
   for (int i = 0; i < 6; ++i) lt[i] = -a[i] + b[i];
   L = mul(mul(transpose(F), Lt), F);
   l = mulv(transpose(F), lt);
+}
+
+// the (loc0, loc1) case
+template <typename S>
+void mbfVisitMeasurement(const Mat<S, 6, 6>& F, const Vec<S, 6>& pred, const Mat<S, 6, 6>& Pp,
+                         const double meas[2], const double mcov[4], Mat<S, 6, 6>& L,
+                         Vec<S, 6>& l) {
+  const int idx[2] = {0, 1};
+  mbfVisitMeasurementN<S, 2>(F, pred, Pp, idx, meas, mcov, L, l);
+}
+
+template <typename S>
+void mbfVisitMeasurementSub(const Mat<S, 6, 6>& F, const Vec<S, 6>& pred,
+                            const Mat<S, 6, 6>& Pp, const MeasRec<S>& m, Mat<S, 6, 6>& L,
+                            Vec<S, 6>& l) {
+  int idx[2] = {0, 1};
+  if (subspaceIndices(m.sub, idx) == 1)
+    mbfVisitMeasurementN<S, 1>(F, pred, Pp, idx, m.v, m.cov, L, l);
+  else
+    mbfVisitMeasurementN<S, 2>(F, pred, Pp, idx, m.v, m.cov, L, l);
 }
 
 // The whole fit for one track: KalmanFitter::fit_impl / filter_impl
@@ -1357,6 +1441,7 @@ struct Fitter {
     Vec<S, 6> pred, filt, smth;
     Mat<S, 6, 6> predCov, filtCov, smthCov, jac;
     bool smoothedSharesFiltered = false;
+    int measDim = 0;  // dimension of the state's measurement (ndf)
   };
 
   int fit(const Surface<S>& startSurface, const Vec<S, 6>& startPars, const Mat<S, 6, 6>& startCov,
@@ -1503,14 +1588,15 @@ struct Fitter {
         uint32_t flags = CK_FLAG_HAS_PARAMETERS;
         if (s.hasMaterial) flags |= CK_FLAG_HAS_MATERIAL;
         const MeasRec<S>& m = meas[mi];
+        ts.measDim = (m.sub & 1) + ((m.sub >> 1) & 1);
         bool outlier = false;
         if (o.outlierChi2Cut < std::numeric_limits<double>::infinity()) {
-          S c2 = predictedChi2(ts.pred, ts.predCov, m.v, m.cov);
+          S c2 = predictedChi2Sub(ts.pred, ts.predCov, m);
           outlier = c2 > S(o.outlierChi2Cut);
         }
         if (!outlier) {
           S c2;
-          if (!gainMatrixUpdate(ts.pred, ts.predCov, m.v, m.cov, o.josephs, ts.filt, ts.filtCov, c2))
+          if (!gainMatrixUpdateSub(ts.pred, ts.predCov, m, o.josephs, ts.filt, ts.filtCov, c2))
             return CK_TRACK_UPDATE_FAILED;
           ts.chi2 = c2;
           flags |= CK_FLAG_HAS_MEASUREMENT;
@@ -1716,7 +1802,7 @@ struct Fitter {
         if (k == 0) break;
         if ((ts.flags & CK_FLAG_HAS_MEASUREMENT) && !(ts.flags & CK_FLAG_IS_OUTLIER)) {
           const MeasRec<S>& m = meas[findMeas(ts.surface)];
-          mbfVisitMeasurement(ts.jac, ts.pred, ts.predCov, m.v, m.cov, L, l);
+          mbfVisitMeasurementSub(ts.jac, ts.pred, ts.predCov, m, L, l);
         } else {
           mbfVisitNonMeasurement(ts.jac, L, l);
         }
@@ -1764,7 +1850,7 @@ struct Fitter {
       } else if (ts.flags & CK_FLAG_HAS_MEASUREMENT) {
         ++out.nMeasurements;
         out.chi2 += (double)ts.chi2;
-        out.ndf += 2;
+        out.ndf += ts.measDim;
       }
     }
     return CK_TRACK_OK;

@@ -67,7 +67,9 @@ void fitOne(const Ctx& ctx, const ck_batch_in* in, int tr, TrackOut& t) {
       return;
     }
   for (int k = in->meas_offsets[tr]; k < in->meas_offsets[tr + 1]; ++k)
-    if (in->meas_surfaces[k] < 0 || in->meas_surfaces[k] >= ns) {
+    if (in->meas_surfaces[k] < 0 || in->meas_surfaces[k] >= ns ||
+        (in->meas_subspace && (in->meas_subspace[k] < CK_MEAS_LOC0 ||
+                               in->meas_subspace[k] > CK_MEAS_LOC01))) {
       t.status = CK_TRACK_INVALID_INPUT;
       return;
     }
@@ -75,6 +77,7 @@ void fitOne(const Ctx& ctx, const ck_batch_in* in, int tr, TrackOut& t) {
   for (int m = in->meas_offsets[tr]; m < in->meas_offsets[tr + 1]; ++m) {
     MeasRec<double> r;
     r.surface = in->meas_surfaces[m];
+    r.sub = in->meas_subspace ? in->meas_subspace[m] : CK_MEAS_LOC01;
     r.v[0] = in->meas_values[2 * m];
     r.v[1] = in->meas_values[2 * m + 1];
     for (int c = 0; c < 4; ++c) r.cov[c] = in->meas_cov[4 * m + c];
@@ -138,13 +141,18 @@ double kfo_fit_batch(const ck_options* opt, int n_surfaces, const ck_surface* su
 
 // GainMatrixUpdater on n states (AoS), as ck_gain_matrix_update.
 void kfo_gain_matrix_update(int n, int joseph, const double* pred, const double* predCov,
-                            const double* meas, const double* measCov, double* filt,
-                            double* filtCov, double* chi2, int* status) {
+                            const double* meas, const double* measCov, const int* subspace,
+                            double* filt, double* filtCov, double* chi2, int* status) {
   for (int i = 0; i < n; ++i) {
     Vec<double, 6> p = get6<double>(pred + 6 * i), f;
     Mat<double, 6, 6> P = get36<double>(predCov + 36 * i), F;
     double c2 = 0;
-    bool ok = gainMatrixUpdate(p, P, meas + 2 * i, measCov + 4 * i, joseph != 0, f, F, c2);
+    MeasRec<double> m;
+    m.surface = 0;
+    m.sub = subspace ? subspace[i] : CK_MEAS_LOC01;
+    for (int c = 0; c < 2; ++c) m.v[c] = meas[2 * i + c];
+    for (int c = 0; c < 4; ++c) m.cov[c] = measCov[4 * i + c];
+    bool ok = gainMatrixUpdateSub(p, P, m, joseph != 0, f, F, c2);
     status[i] = ok ? CK_TRACK_OK : CK_TRACK_UPDATE_FAILED;
     if (ok) {
       put6(filt + 6 * i, f);

@@ -29,7 +29,8 @@ def lib():
                                     C.POINTER(abi.ck_batch_out), C.c_int, C.c_int, C.c_int,
                                     C.c_int]
         L.kfo_gain_matrix_update.restype = None
-        L.kfo_gain_matrix_update.argtypes = [C.c_int, C.c_int] + [abi.P_f64] * 7 + [abi.P_i32]
+        L.kfo_gain_matrix_update.argtypes = ([C.c_int, C.c_int] + [abi.P_f64] * 4 + [abi.P_i32] +
+                                             [abi.P_f64] * 3 + [abi.P_i32])
         L.kfo_gain_matrix_smooth.restype = None
         L.kfo_gain_matrix_smooth.argtypes = [C.c_int, C.c_int] + [abi.P_f64] * 7 + [abi.P_i32]
         L.kfo_mbf_smooth.restype = None
@@ -73,14 +74,16 @@ def time_batch(detector, batch, options, n_threads, first=0, count=-1):
                                count)
 
 
-def gain_matrix_update(pred, pred_cov, meas, meas_cov, joseph=False):
+def gain_matrix_update(pred, pred_cov, meas, meas_cov, joseph=False, subspace=None):
     n = pred.shape[0]
     f = np.zeros((n, 6))
     fc = np.zeros((n, 36))
     chi2 = np.zeros(n)
     st = np.zeros(n, np.int32)
     args = [np.ascontiguousarray(x, dtype=np.float64) for x in (pred, pred_cov, meas, meas_cov)]
+    sub = None if subspace is None else np.ascontiguousarray(subspace, np.int32)
     lib().kfo_gain_matrix_update(n, int(joseph), *[abi.ptr(a, C.c_double) for a in args],
+                                 abi.ptr(sub, C.c_int32),
                                  abi.ptr(f, C.c_double), abi.ptr(fc, C.c_double),
                                  abi.ptr(chi2, C.c_double), abi.ptr(st, C.c_int32))
     return f, fc.reshape(n, 6, 6), chi2, st

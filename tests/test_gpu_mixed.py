@@ -40,11 +40,12 @@ def _pulls(res, b):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("smoother", [abi.SMOOTHER_GAIN_MATRIX, abi.SMOOTHER_MBF],
-                         ids=["gain_matrix", "mbf"])
-def test_mixed_precision_accuracy(fitter_factory, smoother):
+@pytest.mark.parametrize("preset,smoother", [(abi.CKG_BARREL, abi.SMOOTHER_GAIN_MATRIX),
+                                             (abi.CKG_BARREL, abi.SMOOTHER_MBF),
+                                             (abi.CKG_STRIPS, abi.SMOOTHER_GAIN_MATRIX)],
+                         ids=["gain_matrix", "mbf", "strips"])
+def test_mixed_precision_accuracy(fitter_factory, preset, smoother):
     precision = abi.PRECISION_MIXED
-    preset = abi.CKG_BARREL
     n = 20000
     det = detector(preset)
     b = batch(preset, n, seed=13)

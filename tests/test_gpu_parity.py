@@ -31,6 +31,10 @@ CASES = [
     ("barrel_mbf", abi.CKG_BARREL, 2000, dict(smoother=abi.SMOOTHER_MBF), 0.99),
     ("uneven_mbf", abi.CKG_UNEVEN, 2000, dict(outlier_chi2_cut=15.0, smoother=abi.SMOOTHER_MBF),
      0.5),
+    ("strips", abi.CKG_STRIPS, 2000, dict(), 0.99),
+    ("strips_joseph_outliers", abi.CKG_STRIPS, 1000, dict(use_joseph=1, outlier_chi2_cut=15.0),
+     0.99),
+    ("strips_mbf", abi.CKG_STRIPS, 1000, dict(smoother=abi.SMOOTHER_MBF), 0.99),
 ]
 
 

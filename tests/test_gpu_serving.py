@@ -22,13 +22,17 @@ def _events(det, sizes, seed=31):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision,grid_blocks,steps_per_round",
-                         [(abi.PRECISION_FP64, 0, 0), (abi.PRECISION_MIXED, 0, 0),
-                          (abi.PRECISION_MIXED, 7, 1)])
-def test_same_result_alone_and_in_mix(fitter_factory, precision, grid_blocks, steps_per_round):
+@pytest.mark.parametrize("precision,grid_blocks,steps_per_round,preset",
+                         [(abi.PRECISION_FP64, 0, 0, abi.CKG_UNEVEN),
+                          (abi.PRECISION_MIXED, 0, 0, abi.CKG_UNEVEN),
+                          (abi.PRECISION_MIXED, 7, 1, abi.CKG_UNEVEN),
+                          (abi.PRECISION_MIXED, 0, 0, abi.CKG_STRIPS)])
+def test_same_result_alone_and_in_mix(fitter_factory, precision, grid_blocks, steps_per_round,
+                                      preset):
     """Also with a launch shape of the co-batches far from the default (7
-    blocks, one Runge-Kutta trial per round): results do not depend on it."""
-    preset = abi.CKG_UNEVEN
+    blocks, one Runge-Kutta trial per round): results do not depend on it;
+    and with 1D strip measurements (per-measurement subspaces staged with
+    the events)."""
     det = detector(preset)
     fit = fitter_factory(preset)
     opt = abi.default_options(precision=precision, outlier_chi2_cut=15.0)

@@ -74,6 +74,32 @@ def test_smoother_known_answer_on_gpu(fitter_factory):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("joseph", [False, True])
+def test_updater_1d_against_oracle(fitter_factory, joseph):
+    """visitMeasurementImpl<1> (loc0 or loc1) on random states: device
+    against the oracle's restatement."""
+    rng = np.random.default_rng(21)
+    n = 400
+    scale = np.array([0.05, 0.05, 1e-3, 1e-3, 1e-3, 1.0])
+    a = rng.normal(size=(n, 6, 6)) * scale[None, :, None]
+    cov = (a @ a.transpose(0, 2, 1) + np.diag(scale ** 2 * 0.1)[None]).reshape(n, 36)
+    pred = rng.normal(size=(n, 6)) * scale
+    pred[:, 2] = rng.uniform(-3.0, 3.0, n)
+    pred[:, 3] = rng.uniform(0.3, 2.8, n)
+    meas = pred[:, :2] + rng.normal(size=(n, 2)) * 0.03
+    mcov = np.zeros((n, 4))
+    mcov[:, 0] = 0.1 ** 2
+    sub = rng.choice([abi.MEAS_LOC0, abi.MEAS_LOC1], n).astype(np.int32)
+    fit = fitter_factory(abi.CKG_TELESCOPE)
+    g = fit.gain_matrix_update(pred, cov, meas, mcov, joseph=joseph, subspace=sub)
+    o = kforacle.gain_matrix_update(pred, cov, meas, mcov, joseph=joseph, subspace=sub)
+    assert (g[3] == 0).all() and (o[3] == 0).all()
+    np.testing.assert_allclose(g[0], o[0], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(g[1], o[1], rtol=1e-9, atol=1e-15)
+    np.testing.assert_allclose(g[2], o[2], rtol=1e-9)
+
+
+@pytest.mark.gpu
 def test_mbf_smoother_known_answer_on_gpu(fitter_factory):
     s = KA["mbf_smoother"]
     cov = _diag(s["cov_diag"])

@@ -77,6 +77,94 @@ def test_smoother_known_answer():
     assert not np.array_equal(sm[0, 0], filt[0, 0])
 
 
+def _random_states(n, seed):
+    rng = np.random.default_rng(seed)
+    scale = np.array([0.05, 0.05, 1e-3, 1e-3, 1e-3, 1.0])
+    a = rng.normal(size=(n, 6, 6)) * scale[None, :, None]
+    cov = (a @ a.transpose(0, 2, 1) + np.diag(scale ** 2 * 0.1)[None]).reshape(n, 36)
+    pred = rng.normal(size=(n, 6)) * scale
+    pred[:, 2] = rng.uniform(-3.0, 3.0, n)
+    pred[:, 3] = rng.uniform(0.3, 2.8, n)
+    meas = pred[:, :2] + rng.normal(size=(n, 2)) * 0.03
+    return pred, cov, meas
+
+
+@pytest.mark.parametrize("h", [0, 1])
+@pytest.mark.parametrize("joseph", [False, True])
+def test_updater_1d_is_the_2d_limit(h, joseph):
+    """visitMeasurementImpl<1> of loc h equals the 2D update in the limit of
+    an unmeasured other coordinate (variance 1e16): same filtered state and
+    covariance, and the chi2 of the measured coordinate."""
+    n = 50
+    pred, cov, meas = _random_states(n, 3 + h)
+    var = 0.03 ** 2
+    m1 = np.zeros((n, 2))
+    m1[:, 0] = meas[:, h]
+    c1 = np.zeros((n, 4))
+    c1[:, 0] = var
+    f1, fc1, chi1, st1 = kforacle.gain_matrix_update(pred, cov, m1, c1, joseph=joseph,
+                                                     subspace=np.full(n, 1 << h))
+    c2 = np.zeros((n, 4))
+    c2[:, 3 * h] = var
+    c2[:, 3 * (1 - h)] = 1e16
+    f2, fc2, chi2, st2 = kforacle.gain_matrix_update(pred, cov, meas, c2, joseph=joseph)
+    assert (st1 == 0).all() and (st2 == 0).all()
+    np.testing.assert_allclose(f1, f2, rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(fc1, fc2, rtol=1e-7, atol=1e-14)
+    np.testing.assert_allclose(chi1, chi2, rtol=1e-7)
+
+
+def test_kf_strip_measurements():
+    """Barrel tracks whose outer six layers measure one local coordinate
+    (loc0 / loc1 alternating, as the reference's KF test detector): the fits
+    succeed where the all-2D barrel fits of the same tracks do, ndf is the
+    sum of the measurement dimensions, chi2/ndf ~ 1, and both smoothers
+    agree."""
+    b = batch(abi.CKG_STRIPS, 300)
+    dims = np.where(b.meas_subspace == abi.MEAS_LOC01, 2, 1)
+    exp_ndf = np.add.reduceat(dims, b.meas_offsets[:-1])
+    r = _fit(abi.CKG_STRIPS, b)
+    ok = r.status == 0
+    assert ok.mean() > 0.99
+    assert np.array_equal(r.status, _fit(abi.CKG_BARREL, batch(abi.CKG_BARREL, 300)).status)
+    assert np.array_equal(r.ndf[ok], exp_ndf[ok])
+    assert (b.meas_subspace != abi.MEAS_LOC01).sum() > 0.4 * b.meas_subspace.size
+    assert 0.9 < r.chi2_sum[ok].sum() / r.ndf[ok].sum() < 1.1
+    r2 = _fit(abi.CKG_STRIPS, b, smoother=abi.SMOOTHER_MBF)
+    valid = (np.arange(24)[None, :] < r.n_states[:, None]) & ok[:, None]
+    np.testing.assert_allclose(r2.view("smoothed")[valid], r.view("smoothed")[valid],
+                               rtol=1e-9, atol=1e-12)
+
+
+def test_kf_strip_outlier_flagged():
+    """A 1D measurement displaced by 10 mm is flagged as an outlier by the
+    predicted-chi2 cut (outlier finder with a 1D residual)."""
+    b = batch(abi.CKG_STRIPS, 100)
+    nb = b.subset(np.arange(b.n))
+    hit = 0
+    for t in range(nb.n):
+        for m in range(nb.meas_offsets[t], nb.meas_offsets[t + 1]):
+            if nb.meas_subspace[m] != abi.MEAS_LOC01:
+                nb.meas_values[2 * m] += 10.0
+                hit += 1
+                break
+    assert hit > 80
+    r = _fit(abi.CKG_STRIPS, nb, outlier_chi2_cut=15.0)
+    moved = np.array([(nb.meas_subspace[nb.meas_offsets[t]:nb.meas_offsets[t + 1]]
+                       != abi.MEAS_LOC01).any() for t in range(nb.n)])
+    sel = moved & (r.status == 0)
+    assert sel.sum() >= 0.98 * moved.sum()
+    assert (r.n_outliers[sel] == 1).all()
+
+
+def test_invalid_subspace_rejected():
+    b = batch(abi.CKG_STRIPS, 10).subset(np.arange(10))
+    b.meas_subspace[b.meas_offsets[3]] = 0
+    r = _fit(abi.CKG_STRIPS, b)
+    assert r.status[3] == 12  # InvalidInput
+    assert (np.delete(r.status, 3) != 12).all()
+
+
 # ---------------------------------------------------- MbfSmootherTests.cpp
 def mbf_inputs():
     s = KA["mbf_smoother"]
