@@ -111,8 +111,11 @@ struct BoundTrackParameters {
 // (loc0, loc1) of a surface (TestSourceLink + testSourceLinkCalibrator).
 struct SourceLink {
   int surface = -1;
-  std::array<double, 2> value{};
-  std::array<double, 4> covariance{};  // row-major 2x2
+  std::array<double, 2> value{};       // 1D: value[0]
+  std::array<double, 4> covariance{};  // row-major 2x2; 1D: covariance[0]
+  // measured local coordinates (the calibrator's projector subspace):
+  // CK_MEAS_LOC01 (pixel), CK_MEAS_LOC0 or CK_MEAS_LOC1 (strip)
+  int32_t subspace = CK_MEAS_LOC01;
 };
 
 // KalmanFitterOptions + plain stepper / propagator options.
@@ -207,7 +210,7 @@ class CudaKalman {
   std::vector<Result<size_t>> fitBatch(const TrackInput* tracks, size_t n,
                                        const KalmanFitterOptions& options,
                                        TrackContainer& container) const {
-    std::vector<int32_t> seqOff(n + 1, 0), measOff(n + 1, 0), seq, measSurf, pdg(n);
+    std::vector<int32_t> seqOff(n + 1, 0), measOff(n + 1, 0), seq, measSurf, measSub, pdg(n);
     std::vector<double> measVal, measCov, sp(6 * n), sc(36 * n), frames(12 * n);
     std::vector<float> part(2 * n);
     for (size_t t = 0; t < n; ++t) {
@@ -217,6 +220,7 @@ class CudaKalman {
       for (size_t k = 0; k < ti.nSourceLinks; ++k) {
         const SourceLink& sl = ti.sourceLinks[k];
         measSurf.push_back(sl.surface);
+        measSub.push_back(sl.subspace);
         measVal.insert(measVal.end(), sl.value.begin(), sl.value.end());
         measCov.insert(measCov.end(), sl.covariance.begin(), sl.covariance.end());
       }
@@ -243,6 +247,7 @@ class CudaKalman {
     in.start_frames = frames.data();
     in.particle = part.data();
     in.particle_pdg = pdg.data();
+    in.meas_subspace = measSub.data();
 
     const int ms = m_cfg.maxStates;
     const size_t S = static_cast<size_t>(ms) * n;
