@@ -33,6 +33,8 @@ TRACK_STATUS = {
     10: "TooManyStates",
     11: "NotProcessed",
     12: "InvalidInput",
+    13: "CompatibleTrackStateNotFound",
+    14: "ReferenceSurfaceUnreachable",
 }
 
 FLAG_HAS_MEASUREMENT = 1 << 0
@@ -43,6 +45,7 @@ FLAG_HAS_MATERIAL = 1 << 4
 
 SURFACE_PLANE = 0
 SURFACE_CYLINDER = 1
+SURFACE_LINE = 2
 SURF_SENSITIVE = 1
 SURF_MATERIAL = 2
 
@@ -65,6 +68,10 @@ OUT_PREDICTED = 1 << 0
 OUT_FILTERED = 1 << 1
 OUT_SMOOTHED = 1 << 2
 OUT_JACOBIAN = 1 << 3
+OUT_REFERENCE = 1 << 4
+EXTRAPOLATE_FIRST = 0
+EXTRAPOLATE_LAST = 1
+EXTRAPOLATE_FIRST_OR_LAST = 2
 OUT_ALL = OUT_PREDICTED | OUT_FILTERED | OUT_SMOOTHED | OUT_JACOBIAN
 
 CKG_TELESCOPE = 1
@@ -139,6 +146,7 @@ class ck_options(C.Structure):
         ("reference_surface", C.c_int32),
         ("early_termination", C.c_int32),
         ("smoother", C.c_int32),
+        ("reference_strategy", C.c_int32),
     ]
 
 
@@ -199,6 +207,8 @@ class ck_batch_out(C.Structure):
         ("smoothed", P_f64),
         ("smoothed_cov", P_f64),
         ("jacobian", P_f64),
+        ("track_params", P_f64),
+        ("track_cov", P_f64),
     ]
 
 
@@ -269,6 +279,7 @@ def default_options(**kw):
     o.reference_surface = -1
     o.early_termination = 0
     o.smoother = SMOOTHER_GAIN_MATRIX
+    o.reference_strategy = EXTRAPOLATE_FIRST_OR_LAST
     for k, v in kw.items():
         setattr(o, k, v)
     return o

@@ -126,8 +126,11 @@ ck_status validateOptions(const ck_options* o) {
     return fail(CK_ERR_UNSUPPORTED, "reverse filtering is not in the declared extension set");
   if (o->free_to_bound_correction)
     return fail(CK_ERR_UNSUPPORTED, "free-to-bound correction is not supported");
-  if (o->reference_surface != -1)
-    return fail(CK_ERR_UNSUPPORTED, "extrapolation to a reference surface is not supported");
+  if (o->reference_surface < -1)
+    return fail(CK_ERR_INVALID_ARGUMENT, "reference_surface must be -1 or a surface index");
+  if (o->reference_strategy < CK_EXTRAPOLATE_FIRST ||
+      o->reference_strategy > CK_EXTRAPOLATE_FIRST_OR_LAST)
+    return fail(CK_ERR_INVALID_ARGUMENT, "unknown reference_strategy");
   if (o->precision < 0 || o->precision >= CK_NUM_PRECISIONS)
     return fail(CK_ERR_INVALID_ARGUMENT, "unknown precision");
   if (o->smoother != CK_SMOOTHER_GAIN_MATRIX && o->smoother != CK_SMOOTHER_MBF)
@@ -282,9 +285,21 @@ size_t recordBytesPerTrack(int maxStates, int precision) {
 // Allocates (grow-only) the scratch of a batch pipeline: the track-state
 // records of n tracks, the queue permutation and the tips. Never called
 // while a stream is being captured.
-ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, int precision) {
+ck_status validateReference(const ck_handle* h, const ck_options* o) {
+  if (o->reference_surface < 0) return CK_OK;
+  if (o->reference_surface >= h->nSurfaces)
+    return fail(CK_ERR_INVALID_ARGUMENT, "reference_surface outside the surface table");
+  if (h->hostSurfaces[o->reference_surface].type != CK_SURFACE_LINE)
+    return fail(CK_ERR_UNSUPPORTED, "the reference surface must be a line (perigee) surface");
+  return CK_OK;
+}
+
+ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, int precision,
+                          bool extrapolate) {
   (void)h;
   cudaError_t e;
+  if (extrapolate && (e = c.ext.ensure((size_t)n * 2 * sizeof(ExtStart) + 16)))
+    return cudaFail(e, "extrapolation scratch");
   if ((e = c.rec.ensure(compBytes(n, maxStates, 1, recordStateBytes(precision)))) ||
       (e = c.perm.ensure((size_t)n * sizeof(int32_t) + 16)) ||
       (e = c.tip.ensure((size_t)n * sizeof(int32_t) + 16)) ||
@@ -353,6 +368,16 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
   fp.field = h->field;
   fp.mc = h->mc;
   fp.opt = toDevOptions(opt);
+  fp.ref_surface = opt.reference_surface;
+  fp.ref_strategy = opt.reference_strategy;
+  fp.ext = opt.reference_surface >= 0 ? (ExtStart*)c.ext.p : nullptr;
+  {
+    // the extrapolation's propagator options: the reference's defaults
+    // (KalmanFitter.hpp:960-961 constructs them without the fit's options)
+    ck_options d;
+    ck_options_default(&d);
+    fp.extOpt = toDevOptions(d);
+  }
   // inside a stream capture the timing events become event-record nodes of
   // the graph (cudaEventRecordExternal), so they time every replay
   unsigned recFlags = cudaEventRecordDefault;
@@ -370,6 +395,11 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
     e = launchSmooth(fp, opt.precision, st);
     if (e != cudaSuccess) return cudaFail(e, "smoother kernel launch");
     ++launches;
+    if (fp.ext) {
+      e = launchExtrapolate(fp, st);
+      if (e != cudaSuccess) return cudaFail(e, "extrapolation kernel launch");
+      ++launches;
+    }
   }
   if (timed) cudaEventRecordWithFlags(h->ev1, st, recFlags);
   h->lastLaunches = launches;
@@ -378,9 +408,9 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
 }
 
 struct OutArrays {
-  void* host[18];
-  void* dev[18];
-  size_t bytes[18];
+  void* host[kOutArrays];
+  void* dev[kOutArrays];
+  size_t bytes[kOutArrays];
   int count = 0;
 };
 
@@ -414,6 +444,7 @@ void ck_options_default(ck_options* o) {
   o->reference_surface = -1;
   o->early_termination = 0;
   o->smoother = CK_SMOOTHER_GAIN_MATRIX;
+  o->reference_strategy = CK_EXTRAPOLATE_FIRST_OR_LAST;
 }
 
 int32_t ck_api_version(void) { return CK_API_VERSION; }
@@ -466,7 +497,7 @@ ck_status ck_create(const ck_config* cfg, ck_handle** out) {
     return fail(CK_ERR_INVALID_ARGUMENT, "bad surface table");
   for (int i = 0; i < cfg->n_surfaces; ++i) {
     const ck_surface& s = cfg->surfaces[i];
-    if (s.type != CK_SURFACE_PLANE && s.type != CK_SURFACE_CYLINDER)
+    if (s.type != CK_SURFACE_PLANE && s.type != CK_SURFACE_CYLINDER && s.type != CK_SURFACE_LINE)
       return fail(CK_ERR_UNSUPPORTED, "surface " + std::to_string(i) + ": unsupported type");
     if (s.type == CK_SURFACE_CYLINDER && !(s.radius > 0))
       return fail(CK_ERR_INVALID_ARGUMENT, "surface " + std::to_string(i) + ": radius <= 0");
@@ -599,6 +630,7 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
   if (!h || !in || !out) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
   ck_status vs = validateOptions(opt);
   if (vs != CK_OK) return vs;
+  if ((vs = validateReference(h, opt)) != CK_OK) return vs;
   if (in->n_tracks < 0) return fail(CK_ERR_INVALID_ARGUMENT, "n_tracks < 0");
   if (out->max_states <= 0) return fail(CK_ERR_INVALID_ARGUMENT, "max_states <= 0");
   if (!out->status) return fail(CK_ERR_INVALID_ARGUMENT, "status array is required");
@@ -690,8 +722,10 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
         {(void**)&dout.smoothed, compBytes(n, ms, 6, 8)},
         {(void**)&dout.smoothed_cov, compBytes(n, ms, 36, 8)},
         {(void**)&dout.jacobian, compBytes(n, ms, 36, 8)},
+        {(void**)&dout.track_params, sizeof(double) * 6 * (size_t)n},
+        {(void**)&dout.track_cov, sizeof(double) * 36 * (size_t)n},
     };
-    for (int i = 0; i < 18; ++i) {
+    for (int i = 0; i < kOutArrays; ++i) {
       void* hostPtr = *items[i].field;
       if (!hostPtr) continue;
       if ((e = h->outBufs[i].ensure(items[i].bytes)) != cudaSuccess)
@@ -707,7 +741,8 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
 
   // ---- pipeline (graph-captured for device-resident batches)
   const int gridBlocks = gridBlocksFor(h, tn);
-  ck_status s = preparePipeline(h, h->ctx, n, out->max_states, opt->precision);
+  ck_status s = preparePipeline(h, h->ctx, n, out->max_states, opt->precision,
+                                opt->reference_surface >= 0);
   if (s != CK_OK) return s;
   const bool deviceOnly = in->memory == CK_MEM_DEVICE && out->memory == CK_MEM_DEVICE;
   if (deviceOnly && h->useGraph && n > 0) {
@@ -719,7 +754,7 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
     key.stream = st;
     key.scratch[0] = h->ctx.rec.p;
     key.scratch[1] = h->ctx.sortCounts.p;
-    key.scratch[2] = nullptr;
+    key.scratch[2] = h->ctx.ext.p;
     key.scratch[3] = h->ctx.perm.p;
     key.scratch[4] = h->ctx.ticket.p;
     key.scratch[5] = h->ctx.tip.p;
@@ -868,6 +903,7 @@ ck_status ck_autotune(ck_handle* h, const ck_options* opt, const ck_batch_in* in
   if (!h || !in || !out) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
   ck_status vs = validateOptions(opt);
   if (vs != CK_OK) return vs;
+  if ((vs = validateReference(h, opt)) != CK_OK) return vs;
   if (in->memory != CK_MEM_DEVICE || out->memory != CK_MEM_DEVICE)
     return fail(CK_ERR_INVALID_ARGUMENT, "autotuning needs a device-resident batch");
   const int p = opt->precision;

@@ -50,7 +50,9 @@ int occupancyBlocks(int precision, int variant, int tpb);
 // owns one per stream.
 struct FitContext {
   DevBuf rec, perm, ticket, tip, sortCounts;
+  DevBuf ext;  // extrapolation start states (reference surface set)
   void release() {
+    ext.release();
     sortCounts.release();
     tip.release();
     rec.release();
@@ -63,6 +65,9 @@ extern thread_local std::string g_lastError;
 ck_status fail(ck_status s, const std::string& msg);
 ck_status cudaFail(cudaError_t e, const char* what);
 ck_status validateOptions(const ck_options* o);
+// the reference surface of the options against the handle's table (a line
+// surface) and the strategy
+ck_status validateReference(const ck_handle* h, const ck_options* o);
 DevOptions toDevOptions(const ck_options& o);
 MatConst makeMatConst();
 DevSurface toDevSurface(const ck_surface& s);
@@ -71,11 +76,14 @@ size_t recordStateBytes(int precision);
 // arrays of ck_batch_in staged for host batches (particle_pdg and
 // meas_subspace optional)
 constexpr int kInputArrays = 12;
+// arrays of ck_batch_out (status ... jacobian, track_params, track_cov)
+constexpr int kOutArrays = 20;
 constexpr int kSortBlock = 1024;
 inline int sortBlocks(int n) { return n > 0 ? (n + kSortBlock - 1) / kSortBlock : 1; }
 inline size_t sortCountsBytes(int n) { return sizeof(int32_t) * 64 * (size_t)sortBlocks(n); }
 size_t recordBytesPerTrack(int maxStates, int precision);
-ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, int precision);
+ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, int precision,
+                          bool extrapolate);
 ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
                           const ck_batch_in& din, const ck_batch_out& dout, const Tune& tn,
                           cudaStream_t st, bool timed, int gridBlocks);
@@ -102,7 +110,7 @@ struct ck_handle {
   int useGraph = 1;
   bool sortQueue = true;
   ck::DevBuf inBufs[ck::kInputArrays];
-  ck::DevBuf outBufs[18];
+  ck::DevBuf outBufs[ck::kOutArrays];
   ck::FitContext ctx;
   ck::DevBuf unitBuf;
   int lastLaunches = 0;

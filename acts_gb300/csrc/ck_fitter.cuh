@@ -108,6 +108,10 @@ struct Lane {
   // ---- navigation
   int surfaceIndex, currentSurface, targetSurf, targetIdx;
   bool navigationBreak, haveTarget;
+  // ---- propagation direction (+1; -1 for a backward extrapolation) and the
+  // mode of the lane: the fit, or the extrapolation to the reference surface
+  double dirSign;
+  bool extrapolating;
   // ---- Kalman fitter actor
   int nStates, lastMeasurementIndex, measurementStates, nDistinct, lastSlSeq;
   int measHint;  // where the next measurement lookup starts (distinct surfaces only)
@@ -758,13 +762,15 @@ struct Lane {
     nMeas = __ldg(&fp.meas_off[t + 1]) - m0;
     {
       bool bad = nSeq < 0 || nMeas < 0;
+      // (a line surface is only a reference surface: not in a sequence, no
+      // measurement on it)
       for (int i = 0; i < nSeq && !bad; ++i) {
         const int sid = __ldg(&fp.seq_surf[seq0 + i]);
-        bad |= sid < 0 || sid >= fp.n_surfaces;
+        bad |= sid < 0 || sid >= fp.n_surfaces || __ldg(&fp.surfaces[sid].type) == CK_SURFACE_LINE;
       }
       for (int i = 0; i < nMeas && !bad; ++i) {
         const int sid = __ldg(&fp.meas_surf[m0 + i]);
-        bad |= sid < 0 || sid >= fp.n_surfaces;
+        bad |= sid < 0 || sid >= fp.n_surfaces || __ldg(&fp.surfaces[sid].type) == CK_SURFACE_LINE;
         if (fp.meas_sub) {
           const int sub = __ldg(&fp.meas_sub[m0 + i]);
           bad |= sub < CK_MEAS_LOC0 || sub > CK_MEAS_LOC01;
@@ -814,6 +820,8 @@ struct Lane {
         break;
       }
     measHint = 0;
+    dirSign = 1.0;
+    extrapolating = false;
     propLimit = loopLimit(fp, fp.opt.pathLimit, false);
     kfLimit = kNotSet;
     surfaceIndex = -1;
@@ -855,7 +863,7 @@ struct Lane {
         fail(fp, CK_TRACK_STEP_COUNT_LIMIT);
         return;
       }
-      initialH = stepValue();
+      initialH = stepValue() * dirSign;  // EigenStepper.ipp:272
       hd = initialH;
       trials = 0;
       stepStarted = true;
@@ -1052,6 +1060,11 @@ struct Lane {
     // post-step navigation (Propagator.ipp:113-141)
     cNav = kNotSet;
     cActor = kNotSet;
+    if (extrapolating) {
+      // no navigation target and no actors; the aborters decide
+      if (extrapolationAbort(fp)) finishExtrapolation(fp);
+      return;
+    }
     if (haveTarget) {
       const int post = surfaceStatus(fp, targetSurf, targetIdx);
       if (post == 2 && !navigationBreak) currentSurface = __ldg(&fp.seq_surf[seq0 + surfaceIndex]);
@@ -1067,6 +1080,176 @@ struct Lane {
       return;
     }
     afterAct(fp, slot);
+  }
+
+  // ------------------------------------ extrapolation to the reference surface
+  // extrapolateTrackToReferenceSurface (TrackHelpers.hpp:339-381): a plain
+  // propagation (no actors; DirectNavigator without surfaces) from a smoothed
+  // track state to the reference line surface with the ForcedSurfaceReached
+  // and PathLimitReached aborters (StandardAborters.hpp:66-164), in the
+  // direction of the straight-line distance to it; fp.opt holds the
+  // reference's default propagator options here.
+
+  // LineSurface::intersect (LineSurface.cpp:141-185): false when the track
+  // is parallel to the line (invalid intersection)
+  CK_D static bool lineIntersect(const Surf<double>& s, const double p[3], const double d[3],
+                                 double tol, double& u) {
+    const double eb[3] = {s.R[2], s.R[5], s.R[8]};
+    const double mab[3] = {s.c[0] - p[0], s.c[1] - p[1], s.c[2] - p[2]};
+    const double eaTeb = d[0] * eb[0] + d[1] * eb[1] + d[2] * eb[2];
+    const double denom = 1.0 - eaTeb * eaTeb;
+    if (fabs(denom) < fabs(tol)) return false;
+    const double ma = mab[0] * d[0] + mab[1] * d[1] + mab[2] * d[2];
+    const double mb = mab[0] * eb[0] + mab[1] * eb[1] + mab[2] * eb[2];
+    u = (ma - mb * eaTeb) / denom;
+    return true;
+  }
+
+  CK_D void startExtrapolation(const FitParams& fp, int queuePos, int track, const ExtStart& es,
+                               double distance) {
+    t = track;
+    q = queuePos;
+    extrapolating = true;
+    dirSign = distance >= 0.0 ? 1.0 : -1.0;  // Direction::fromScalarZeroAsPositive
+    Surf<double> sf;
+    sf.load(fp.surfaces + es.surface);
+    boundToFree(sf, es.par);
+    initT(sf);
+#pragma unroll
+    for (int i = 0; i < 21; ++i) cov[i] = (CV)es.cov[i];
+#pragma unroll
+    for (int i = 0; i < 7; ++i) deriv[i] = P(0);
+    pathAcc = 0.0;
+    cNav = kNotSet;
+    cActor = kNotSet;
+    cUser = fp.opt.maxStepSize;
+    cAcc = fp.opt.initialStepSize;
+    mass = __ldg(&fp.particle[2 * (size_t)t]);
+    absQ = __ldg(&fp.particle[2 * (size_t)t + 1]);
+    pdg = fp.pdg ? __ldg(&fp.pdg[t]) : 211;
+    coasting = false;
+    finished = false;
+    stepStarted = false;
+    steps = 0;
+    haveTarget = false;
+    navigationBreak = true;
+    currentSurface = -1;
+    propLimit = loopLimit(fp, fp.opt.pathLimit, false);
+    phase = PH_STEP;
+    if (extrapolationAbort(fp)) finishExtrapolation(fp);  // pre-propagation check
+  }
+
+  // the aborters in list order, the first that fires ends the propagation:
+  // the target (its distance becomes the actor step constraint), then the
+  // path limit
+  CK_D bool extrapolationAbort(const FitParams& fp) {
+    Surf<double> ts;
+    ts.load(fp.surfaces + fp.ref_surface);
+    const double d[3] = {dirSign * dir[0], dirSign * dir[1], dirSign * dir[2]};
+    const double tol = fp.opt.surfaceTolerance;
+    double u = 0.0;
+    const bool valid = lineIntersect(ts, pos, d, tol, u);
+    if (valid) {
+      cActor = kNotSet;  // updateSingleSurfaceStatus: release, then update
+      cupdate(cActor, u);
+      if (!(fabs(u) > fabs(tol))) return true;  // on surface
+    }
+    return pathLimitReached(fp, propLimit);
+  }
+
+  // Propagator::makeResult -> EigenStepper::boundState on the target:
+  // J = F2B (I + derivative x freeToPath) T with the line surface's frame and
+  // path derivative (LineSurface.cpp:102-115,224-251), C <- J C J^T, and the
+  // bound parameters (LineSurface::globalToLocal, LineSurface.cpp:70-96)
+  CK_D void finishExtrapolation(const FitParams& fp) {
+    Surf<double> ts;
+    ts.load(fp.surfaces + fp.ref_surface);
+    const double z0[3] = {ts.R[2], ts.R[5], ts.R[8]};
+    double d0[3] = {z0[1] * dir[2] - z0[2] * dir[1], z0[2] * dir[0] - z0[0] * dir[2],
+                    z0[0] * dir[1] - z0[1] * dir[0]};
+    const double dn = 1.0 / sqrt(d0[0] * d0[0] + d0[1] * d0[1] + d0[2] * d0[2]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) d0[i] *= dn;
+    const double dist[3] = {d0[1] * z0[2] - d0[2] * z0[1], d0[2] * z0[0] - d0[0] * z0[2],
+                            d0[0] * z0[1] - d0[1] * z0[0]};
+    const double pc[3] = {pos[0] - ts.c[0], pos[1] - ts.c[1], pos[2] - ts.c[2]};
+    if (fabs(dist[0] * pc[0] + dist[1] * pc[1] + dist[2] * pc[2]) > fabs(kOnSurfaceTolerance)) {
+      fail(fp, CK_TRACK_NOT_ON_SURFACE);
+      return;
+    }
+    // path derivative of the line surface
+    const double pz = pc[0] * z0[0] + pc[1] * z0[1] + pc[2] * z0[2];
+    const double dz = z0[0] * dir[0] + z0[1] * dir[1] + z0[2] * dir[2];
+    const double nrm = 1.0 / (1.0 - dz * dz);
+    double fpos[3], fdir[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      fpos[i] = nrm * (dz * z0[i] - dir[i]);
+      fdir[i] = nrm * (pz * z0[i] - pc[i]);
+    }
+    const double dd[3] = {dir[0], dir[1], dir[2]};
+    const Trig<double> tg = trig(dd);
+    const double a0 = -tg.sinPhi * tg.invSinTheta, a1 = tg.cosPhi * tg.invSinTheta;
+    const double b0 = tg.cosPhi * tg.cosTheta, b1 = tg.sinPhi * tg.cosTheta, b2 = -tg.sinTheta;
+    double J[6][6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      // free column c of T = jacTransport * jacToGlobal
+      double v[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) v[r] = 0.0;
+      if (c < 2) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r) v[r] = (double)T.loc[r][c];
+      } else if (c < 5) {
+#pragma unroll
+        for (int r = 0; r < 7; ++r) v[r] = (double)T.dyn[r][c - 2];
+        v[7] = c == 4 ? 1.0 : 0.0;
+      } else {
+        v[3] = 1.0;
+      }
+      const double sc = (fpos[0] * v[0] + fpos[1] * v[1] + fpos[2] * v[2]) +
+                        (fdir[0] * v[4] + fdir[1] * v[5] + fdir[2] * v[6]);
+#pragma unroll
+      for (int r = 0; r < 7; ++r) v[r] += (double)deriv[r] * sc;
+      J[0][c] = d0[0] * v[0] + d0[1] * v[1] + d0[2] * v[2];
+      J[1][c] = z0[0] * v[0] + z0[1] * v[1] + z0[2] * v[2];
+      J[2][c] = a0 * v[4] + a1 * v[5];
+      J[3][c] = b0 * v[4] + b1 * v[5] + b2 * v[6];
+      J[4][c] = v[7];
+      J[5][c] = v[3];
+    }
+    double JC[6][6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) s += J[i][k] * (double)cov[sidx(k, j)];
+        JC[i][j] = s;
+      }
+    const ck_batch_out& out = fp.out;
+    const size_t n = (size_t)fp.n_tracks;
+    if (out.track_cov) {
+#pragma unroll
+      for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+          double s = 0.0;
+#pragma unroll
+          for (int k = 0; k < 6; ++k) s += JC[i][k] * J[j][k];
+          out.track_cov[(size_t)(i * 6 + j) * n + t] = s;
+        }
+    }
+    if (out.track_params) {
+      const double b[6] = {d0[0] * pc[0] + d0[1] * pc[1] + d0[2] * pc[2], pz,
+                           atan2(dir[1], dir[0]),
+                           atan2(sqrt(dir[0] * dir[0] + dir[1] * dir[1]), dir[2]), qop, tim};
+#pragma unroll
+      for (int i = 0; i < 6; ++i) out.track_params[(size_t)i * n + t] = b[i];
+    }
+    phase = PH_DONE;
   }
 
   // SURFACE: the actor on the reached surface
@@ -1097,7 +1280,7 @@ struct Lane {
 template <typename CV>
 struct Smoother {
   int t, q;
-  int lastMeas;
+  int lastMeas, firstMeas;
   int nM, nH, nO, ndf;
   double chi2sum;
 
@@ -1105,7 +1288,22 @@ struct Smoother {
     t = track;
     q = queuePos;
     lastMeas = tip;
+    firstMeas = -1;
     const Rec<CV> rec(fp, q);
+    if (fp.ext) {
+      // the extrapolation's candidate start states: the first and the last
+      // state with a non-outlier measurement (findFirst/LastMeasurementState,
+      // TrackHelpers.hpp:64-102); none yet
+      fp.ext[2 * (size_t)q].surface = -1;
+      fp.ext[2 * (size_t)q + 1].surface = -1;
+      for (int k = 0; k <= tip; ++k) {
+        const uint32_t fl = (uint32_t)rec.s(k).flags;
+        if ((fl & CK_FLAG_HAS_MEASUREMENT) && !(fl & CK_FLAG_IS_OUTLIER)) {
+          firstMeas = k;
+          break;
+        }
+      }
+    }
     for (int k = tip; k >= 0; --k) {
       const uint32_t fl = (uint32_t)rec.s(k).flags;
       if ((fl & CK_FLAG_HAS_MEASUREMENT) && !(fl & CK_FLAG_IS_OUTLIER)) {
@@ -1237,6 +1435,19 @@ struct Smoother {
                        bool filtOverride) {
     const ck_batch_out& out = fp.out;
     const Rec<CV> rec(fp, q);
+    if (fp.ext && (k == firstMeas || k == lastMeas)) {
+      // its smoothed parameters (TrackStateProxy::parameters) for the
+      // extrapolation; slot 0 first, slot 1 last
+      for (int slot = 0; slot < 2; ++slot) {
+        if (k != (slot == 0 ? firstMeas : lastMeas)) continue;
+        ExtStart& es = fp.ext[2 * (size_t)q + slot];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) es.par[i] = sm[i];
+#pragma unroll
+        for (int i = 0; i < 21; ++i) es.cov[i] = (double)Ps[i];
+        es.surface = rec.s(k).surface;
+      }
+    }
     const size_t n = (size_t)fp.n_tracks;
     auto at = [&](int C, int c) -> size_t { return ((size_t)k * C + c) * n + t; };
     const RecState<CV>& rs = rec.s(k);

@@ -90,6 +90,18 @@ struct RecState {
 static_assert(sizeof(RecState<float>) == 432, "record layout");
 static_assert(sizeof(RecState<double>) == 744, "record layout");
 
+// A track state the extrapolation to the reference surface may start from
+// (the first and the last state with a non-outlier measurement, slots 0 and
+// 1 of each queue position): its surface and smoothed parameters and
+// covariance (packed upper) in FP64. Written by the smoother.
+struct ExtStart {
+  double par[6];
+  double cov[21];
+  int32_t surface;  // -1: no such state
+  int32_t pad;
+};
+static_assert(sizeof(ExtStart) == 224, "extrapolation start layout");
+
 struct FitParams {
   int n_tracks;
   int n_queue;  // number of slots in the work queue (= n_tracks)
@@ -132,6 +144,13 @@ struct FitParams {
   DevField field;
   MatConst mc;
   DevOptions opt;
+  // extrapolation to the reference surface: its table index (-1: none), the
+  // strategy (CK_EXTRAPOLATE_*), two start states per queue position, and
+  // the propagator options it runs with (the reference's defaults)
+  int ref_surface;
+  int ref_strategy;
+  ExtStart* ext;
+  DevOptions extOpt;
 };
 
 }  // namespace ck

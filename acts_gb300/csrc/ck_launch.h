@@ -39,5 +39,9 @@ inline cudaError_t launchSmooth(const FitParams& fp, int precision, cudaStream_t
   return precision == CK_PRECISION_MIXED ? launchSmoothMixed(fp, st) : launchSmoothFP64(fp, st);
 }
 constexpr int kSmoothBlock = 128;
+// extrapolation of every successfully smoothed track to the reference
+// surface (FP64 in both forms; ck_extrapolate.cu)
+cudaError_t launchExtrapolate(const FitParams& fp, cudaStream_t st);
+constexpr int kExtrapolateBlock = 64;
 
 }  // namespace ck

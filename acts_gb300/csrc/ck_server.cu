@@ -76,7 +76,7 @@ struct Slot {
   FitContext ctx;
   DevBuf din[kInputArrays];
   size_t inPlanned[kInputArrays] = {};
-  DevBuf dout[18];
+  DevBuf dout[kOutArrays];
   DevBuf table;              // per-event {t0, m, seqBase, measBase} on the device
   int32_t* pinTable = nullptr;
   void* pinOut = nullptr;    // staging of pageable results
@@ -88,13 +88,16 @@ struct Slot {
 
 // element size and components per ck_batch_out array, in the order of
 // outFields()
-constexpr size_t kOutElem[18] = {4, 4, 4, 4, 4, 4, 8, 4, 4, 8, 8, 8, 8, 8, 8, 8, 8, 8};
-constexpr int kOutComp[18] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 6, 36, 6, 36, 6, 36, 36};
-constexpr bool kPerState[18] = {false, false, false, false, false, false, false, true, true,
-                                true,  true,  true,  true,  true,  true,  true,  true,  true};
+constexpr size_t kOutElem[kOutArrays] = {4, 4, 4, 4, 4, 4, 8, 4, 4, 8,
+                                         8, 8, 8, 8, 8, 8, 8, 8, 8, 8};
+constexpr int kOutComp[kOutArrays] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1,
+                                      1, 6, 36, 6, 36, 6, 36, 36, 6, 36};
+constexpr bool kPerState[kOutArrays] = {false, false, false, false, false, false, false,
+                                        true,  true,  true,  true,  true,  true,  true,
+                                        true,  true,  true,  true,  false, false};
 
-void outFields(ck_batch_out& o, void** f[18]) {
-  void** a[18] = {(void**)&o.status,          (void**)&o.n_states,
+void outFields(ck_batch_out& o, void** f[kOutArrays]) {
+  void** a[kOutArrays] = {(void**)&o.status,          (void**)&o.n_states,
                   (void**)&o.n_measurements,  (void**)&o.n_holes,
                   (void**)&o.n_outliers,      (void**)&o.ndf,
                   (void**)&o.chi2_sum,        (void**)&o.state_surface,
@@ -102,8 +105,9 @@ void outFields(ck_batch_out& o, void** f[18]) {
                   (void**)&o.state_chi2,      (void**)&o.predicted,
                   (void**)&o.predicted_cov,   (void**)&o.filtered,
                   (void**)&o.filtered_cov,    (void**)&o.smoothed,
-                  (void**)&o.smoothed_cov,    (void**)&o.jacobian};
-  for (int i = 0; i < 18; ++i) f[i] = a[i];
+                  (void**)&o.smoothed_cov,    (void**)&o.jacobian,
+                  (void**)&o.track_params,    (void**)&o.track_cov};
+  for (int i = 0; i < kOutArrays; ++i) f[i] = a[i];
 }
 
 // CSR offsets of a co-batch: each event's offsets were copied unshifted to
@@ -155,6 +159,7 @@ struct ck_server {
     if (spec.fi) out += (size_t)maxStates * 42 * 8;
     if (spec.pr) out += (size_t)maxStates * 42 * 8;
     if (spec.jac) out += (size_t)maxStates * 36 * 8;
+    if (opt.reference_surface >= 0) out += 42 * 8 + 2 * sizeof(ExtStart);
     return in + out + recordBytesPerTrack(maxStates, opt.precision);
   }
   bool computes(int field) const {
@@ -163,6 +168,7 @@ struct ck_server {
       case 13: case 14: return spec.fi;
       case 15: case 16: return spec.sm;
       case 17: return spec.jac;
+      case 18: case 19: return opt.reference_surface >= 0;
       default: return true;
     }
   }
@@ -187,7 +193,7 @@ ck_status slotAlloc(ck_server* s, Slot& sl) {
   }
   const size_t S = cap * (size_t)ms;
   size_t pout = 0;
-  for (int i = 0; i < 18; ++i) {
+  for (int i = 0; i < kOutArrays; ++i) {
     if (!s->computes(i)) continue;
     const size_t bytes = kOutElem[i] * kOutComp[i] * (kPerState[i] ? S : cap);
     if ((e = sl.dout[i].ensure(bytes)) != cudaSuccess) return cudaFail(e, "server output");
@@ -200,14 +206,15 @@ ck_status slotAlloc(ck_server* s, Slot& sl) {
       (e = cudaMallocHost(&sl.pinOut, pout)) != cudaSuccess)
     return cudaFail(e, "server pinned buffers");
   sl.pinOutBytes = pout;
-  return preparePipeline(s->h, sl.ctx, s->capacity, ms, s->opt.precision);
+  return preparePipeline(s->h, sl.ctx, s->capacity, ms, s->opt.precision,
+                         s->opt.reference_surface >= 0);
 }
 
 // Offsets of the staged result arrays in the slot's pinned buffer.
-void stagedBases(ck_server* s, Slot& sl, size_t base[18]) {
+void stagedBases(ck_server* s, Slot& sl, size_t base[kOutArrays]) {
   const size_t n = (size_t)sl.nTracks, S = n * (size_t)s->cfg.max_states;
   size_t off = 0;
-  for (int i = 0; i < 18; ++i) {
+  for (int i = 0; i < kOutArrays; ++i) {
     base[i] = off;
     if (!s->computes(i)) continue;
     off += (kOutElem[i] * kOutComp[i] * (kPerState[i] ? S : n) + 255) & ~(size_t)255;
@@ -299,9 +306,9 @@ ck_status launchSlot(ck_server* s, Slot& sl) {
   ck_batch_out dout{};
   dout.max_states = s->cfg.max_states;
   dout.memory = CK_MEM_DEVICE;
-  void** f[18];
+  void** f[kOutArrays];
   outFields(dout, f);
-  for (int i = 0; i < 18; ++i) *f[i] = sl.dout[i].cap ? sl.dout[i].p : nullptr;
+  for (int i = 0; i < kOutArrays; ++i) *f[i] = sl.dout[i].cap ? sl.dout[i].p : nullptr;
   ck_status st;
   {
     std::lock_guard<std::mutex> lock(s->h->mu);
@@ -321,27 +328,29 @@ ck_status launchSlot(ck_server* s, Slot& sl) {
       anyStaged = true;
     } else {
       ck_batch_out o = ev.out;
-      void** g[18];
+      void** g[kOutArrays];
       outFields(o, g);
-      for (int i = 0; i < 18; ++i) {
+      for (int i = 0; i < kOutArrays; ++i) {
         if (!*g[i] || !sl.dout[i].cap) continue;
         const size_t el = kOutElem[i];
         const char* src = (const char*)sl.dout[i].p + el * t0;
-        if (!kPerState[i])
+        // rows of the SoA array: components (x states)
+        const size_t rows = (kPerState[i] ? (size_t)ms : 1) * (size_t)kOutComp[i];
+        if (rows == 1)
           e = cudaMemcpyAsync(*g[i], src, el * m, cudaMemcpyDefault, sl.stream);
         else
-          e = cudaMemcpy2DAsync(*g[i], el * m, src, el * n, el * m, (size_t)ms * kOutComp[i],
-                                cudaMemcpyDefault, sl.stream);
+          e = cudaMemcpy2DAsync(*g[i], el * m, src, el * n, el * m, rows, cudaMemcpyDefault,
+                                sl.stream);
         if (e != cudaSuccess) return cudaFail(e, "server result copy");
       }
     }
     t0 += m;
   }
   if (anyStaged) {
-    size_t base[18];
+    size_t base[kOutArrays];
     stagedBases(s, sl, base);
     const size_t S = (size_t)n * ms;
-    for (int i = 0; i < 18; ++i) {
+    for (int i = 0; i < kOutArrays; ++i) {
       if (!sl.dout[i].cap) continue;
       const size_t bytes = kOutElem[i] * kOutComp[i] * (kPerState[i] ? S : (size_t)n);
       if ((e = cudaMemcpyAsync((char*)sl.pinOut + base[i], sl.dout[i].p, bytes,
@@ -356,7 +365,7 @@ ck_status launchSlot(ck_server* s, Slot& sl) {
 // Completes a finished slot: host copies of the staged events' results.
 void harvestSlot(ck_server* s, Slot& sl) {
   const int n = sl.nTracks, ms = s->cfg.max_states;
-  size_t base[18];
+  size_t base[kOutArrays];
   stagedBases(s, sl, base);
   int t0 = 0;
   for (auto& evp : sl.events) {
@@ -364,14 +373,14 @@ void harvestSlot(ck_server* s, Slot& sl) {
     const int m = ev.n;
     if (ev.staged) {
       ck_batch_out o = ev.out;
-      void** g[18];
+      void** g[kOutArrays];
       outFields(o, g);
-      for (int i = 0; i < 18; ++i) {
+      for (int i = 0; i < kOutArrays; ++i) {
         if (!*g[i] || !sl.dout[i].cap) continue;
         const size_t el = kOutElem[i];
         const char* src = (const char*)sl.pinOut + base[i] + el * t0;
         char* dst = (char*)*g[i];
-        const int rows = kPerState[i] ? ms * kOutComp[i] : 1;
+        const int rows = (kPerState[i] ? ms : 1) * kOutComp[i];
         for (int r = 0; r < rows; ++r)
           std::memcpy(dst + el * m * (size_t)r, src + el * n * (size_t)r, el * m);
       }
@@ -484,6 +493,7 @@ ck_status ck_server_create(ck_handle* h, const ck_options* opt, const ck_server_
   if (!h || !cfg || !out) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
   ck_status vs = validateOptions(opt);
   if (vs != CK_OK) return vs;
+  if ((vs = validateReference(h, opt)) != CK_OK) return vs;
   if (cfg->n_streams < 1 || cfg->n_streams > 16 || cfg->max_states < 1 ||
       cfg->memory_budget_bytes <= 0 || cfg->max_batch_tracks < 1 || cfg->grid_blocks < 0 ||
       cfg->steps_per_round < 0 || cfg->steps_per_round > 64)
@@ -533,9 +543,9 @@ ck_status ck_server_submit(ck_server* s, int64_t event_id, const ck_batch_in* in
   if (!results->status) return fail(CK_ERR_INVALID_ARGUMENT, "status array is required");
   {
     ck_batch_out o = *results;
-    void** g[18];
+    void** g[kOutArrays];
     outFields(o, g);
-    for (int i = 0; i < 18; ++i)
+    for (int i = 0; i < kOutArrays; ++i)
       if (*g[i] && !s->computes(i))
         return fail(CK_ERR_INVALID_ARGUMENT, "results ask for a component the server omits");
   }

@@ -51,10 +51,11 @@ size_t roundUp(size_t b) { return (b + kAlign - 1) & ~(kAlign - 1); }
 
 // Scratch layout for n tracks of up to maxStates states.
 struct Layout {
-  size_t rec, perm, tip, sortCounts, ticket, total;
+  size_t rec, perm, tip, sortCounts, ticket, ext, total;
 };
 
-Layout layoutFor(int n, int maxStates, int precision) {
+// ext: the extrapolation start states (only with a reference surface)
+Layout layoutFor(int n, int maxStates, int precision, bool ext) {
   const size_t ns = (size_t)n * (size_t)maxStates;
   Layout l;
   l.rec = roundUp(ns * recordStateBytes(precision));
@@ -62,7 +63,8 @@ Layout layoutFor(int n, int maxStates, int precision) {
   l.tip = roundUp((size_t)n * sizeof(int32_t));
   l.sortCounts = roundUp(sortCountsBytes(n));
   l.ticket = kTicketBytes;
-  l.total = l.rec + l.perm + l.tip + l.sortCounts + l.ticket;
+  l.ext = ext ? roundUp((size_t)n * 2 * sizeof(ExtStart)) : 0;
+  l.total = l.rec + l.perm + l.tip + l.sortCounts + l.ticket + l.ext;
   return l;
 }
 
@@ -87,7 +89,7 @@ extern "C" {
 
 int64_t ck_static_scratch_bytes(int32_t n_tracks, int32_t max_states, int32_t precision) {
   if (n_tracks < 0 || max_states <= 0) return -1;
-  return (int64_t)layoutFor(n_tracks, max_states, precision).total;
+  return (int64_t)layoutFor(n_tracks, max_states, precision, false).total;
 }
 
 int64_t ck_static_scratch_capacity(void) { return (int64_t)kStaticScratchBytes; }
@@ -97,6 +99,7 @@ ck_status ck_fit_batch_static(ck_handle* h, const ck_options* opt, const ck_batc
   if (!h || !in || !out) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
   ck_status vs = validateOptions(opt);
   if (vs != CK_OK) return vs;
+  if ((vs = validateReference(h, opt)) != CK_OK) return vs;
   if (in->memory != CK_MEM_DEVICE || out->memory != CK_MEM_DEVICE)
     return fail(CK_ERR_INVALID_ARGUMENT,
                 "ck_fit_batch_static takes device-resident inputs and outputs only");
@@ -107,7 +110,7 @@ ck_status ck_fit_batch_static(ck_handle* h, const ck_options* opt, const ck_batc
       (out->smoothed && !out->smoothed_cov))
     return fail(CK_ERR_INVALID_ARGUMENT, "parameter arrays need their covariance arrays");
   const int n = in->n_tracks;
-  const Layout l = layoutFor(n, out->max_states, opt->precision);
+  const Layout l = layoutFor(n, out->max_states, opt->precision, opt->reference_surface >= 0);
   if (l.total > kStaticScratchBytes)
     return fail(CK_ERR_SCRATCH_LIMIT,
                 "batch needs " + std::to_string(l.total) + " bytes of scratch; the static scratch "
@@ -131,6 +134,7 @@ ck_status ck_fit_batch_static(ck_handle* h, const ck_options* opt, const ck_batc
   view(c.tip, l.tip);
   view(c.sortCounts, l.sortCounts);
   view(c.ticket, l.ticket);
+  if (l.ext) view(c.ext, l.ext);
   cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
   const Tune tn = h->tune[opt->precision];
   h->lastH2D = 0;

@@ -41,13 +41,26 @@ def lib():
 class Detector:
     """Surface table and field of a preset (owns the field value buffer)."""
 
-    def __init__(self, preset, n_threads=None):
+    def __init__(self, preset, n_threads=None, perigee=False):
+        """perigee: append a PerigeeSurface (a line along global z through the
+        origin) to the table, as the reference surface of the extrapolation;
+        its index is `self.perigee`."""
         L = lib()
         self.preset = preset
         arr = (abi.ck_surface * 64)()
         n = L.ckg_geometry(preset, arr, 64)
         if n < 0:
             raise ValueError("unknown preset %r" % preset)
+        self.perigee = -1
+        if perigee:
+            p = abi.ck_surface()
+            p.type = abi.SURFACE_LINE
+            for i in range(3):
+                p.rotation[4 * i] = 1.0
+            p.split_factor = 1.0
+            arr[n] = p
+            self.perigee = n
+            n += 1
         self.surfaces = (abi.ck_surface * n)(*arr[:n])
         self.n_surfaces = n
         nv = L.ckg_field_values(preset)

@@ -35,6 +35,9 @@ class Results:
         self.smoothed = z(6, np.float64) if components & abi.OUT_SMOOTHED else None
         self.smoothed_cov = z(36, np.float64) if components & abi.OUT_SMOOTHED else None
         self.jacobian = z(36, np.float64) if components & abi.OUT_JACOBIAN else None
+        ref = components & abi.OUT_REFERENCE
+        self.track_params = np.zeros(6 * n, np.float64) if ref else None
+        self.track_cov = np.zeros(36 * n, np.float64) if ref else None
 
     def as_batch_out(self):
         o = abi.ck_batch_out()
@@ -46,9 +49,15 @@ class Results:
             setattr(o, name, abi.ptr(getattr(self, name), C.c_int32))
         o.state_flags = abi.ptr(self.state_flags, C.c_uint32)
         for name in ("chi2_sum", "state_path_length", "state_chi2", "predicted", "predicted_cov",
-                     "filtered", "filtered_cov", "smoothed", "smoothed_cov", "jacobian"):
+                     "filtered", "filtered_cov", "smoothed", "smoothed_cov", "jacobian",
+                     "track_params", "track_cov"):
             setattr(o, name, abi.ptr(getattr(self, name), C.c_double))
         return o
+
+    def track(self, name):
+        """Per-track array `name` (track_params / track_cov) as [n, C]."""
+        a = getattr(self, name)
+        return None if a is None else a.reshape(-1, self.n).T
 
     def view(self, name, k=None):
         """Array `name` as [n, max_states, C] (or [n, max_states] for scalars)."""

@@ -80,7 +80,11 @@ enum {
   CK_TRACK_FIELD_OUT_OF_BOUNDS = 9,   /* grid field lookup outside the map */
   CK_TRACK_TOO_MANY_STATES = 10,      /* more states than out->max_states  */
   CK_TRACK_NOT_PROCESSED = 11,        /* the kernel did not reach the track */
-  CK_TRACK_INVALID_INPUT = 12         /* a surface id outside the table    */
+  CK_TRACK_INVALID_INPUT = 12,        /* a surface id outside the table    */
+  /* extrapolation to the reference surface (TrackExtrapolationError,
+   * Core/include/Acts/Utilities/TrackHelpers.hpp:48-53) */
+  CK_TRACK_NO_COMPATIBLE_STATE = 13,  /* CompatibleTrackStateNotFound      */
+  CK_TRACK_REFERENCE_UNREACHABLE = 14 /* ReferenceSurfaceUnreachable       */
 };
 
 /* Track-state type flags, bit positions of Acts::TrackStateFlag
@@ -95,7 +99,7 @@ enum {
 
 /* ------------------------------------------------------------- geometry */
 
-enum { CK_SURFACE_PLANE = 0, CK_SURFACE_CYLINDER = 1 };
+enum { CK_SURFACE_PLANE = 0, CK_SURFACE_CYLINDER = 1, CK_SURFACE_LINE = 2 };
 enum { CK_SURF_SENSITIVE = 1, CK_SURF_MATERIAL = 2 };
 
 /* A surface of the flat surface table (the DirectNavigator sequence refers to
@@ -104,11 +108,17 @@ enum { CK_SURF_SENSITIVE = 1, CK_SURF_MATERIAL = 2 };
  *             local frame = rotation columns, normal = column 2.
  *   Cylinder: CylinderSurface (Core/src/Surfaces/CylinderSurface.cpp:90-277),
  *             symmetry axis = rotation column 2, radius `radius`.
+ *   Line    : LineSurface without bounds (Core/src/Surfaces/LineSurface.cpp
+ *             :57-251), line = rotation column 2 through `center`; a
+ *             PerigeeSurface (PerigeeSurface.cpp) is the line along global z
+ *             (identity rotation). Only as the reference surface of the
+ *             extrapolation (ck_options.reference_surface); a sequence or a
+ *             measurement on a line surface is invalid input.
  * Material is a homogeneous slab (HomogeneousSurfaceMaterial) with the
  * reference's float Material fields (Core/include/Acts/Material/Material.hpp
  * :135-145) and split factor (Core/src/Material/ISurfaceMaterial.cpp:18-46). */
 typedef struct ck_surface {
-  int32_t type;          /* CK_SURFACE_PLANE / CK_SURFACE_CYLINDER          */
+  int32_t type;          /* CK_SURFACE_PLANE / _CYLINDER / _LINE             */
   int32_t flags;         /* CK_SURF_SENSITIVE | CK_SURF_MATERIAL            */
   double rotation[9];    /* row-major 3x3, columns = local x, y, z axes     */
   double center[3];
@@ -193,12 +203,17 @@ typedef struct ck_options {
   int32_t use_joseph;           /* 0 (GainMatrixUpdater default)           */
   int32_t precision;            /* CK_PRECISION_*                          */
   double outlier_chi2_cut;      /* +inf                                    */
-  /* Extensions outside the reference's declared set are rejected with
-   * CK_ERR_UNSUPPORTED: reverse filtering, free-to-bound correction and
-   * extrapolation to a reference surface. */
+  /* Extensions outside the declared set are rejected with
+   * CK_ERR_UNSUPPORTED: reverse filtering and free-to-bound correction. */
   int32_t reverse_filtering;    /* must be 0                               */
   int32_t free_to_bound_correction; /* must be 0                           */
-  int32_t reference_surface;    /* must be -1 (none)                       */
+  /* KalmanFitterOptions::referenceSurface: -1 (none) or the index of a
+   * CK_SURFACE_LINE surface of the table. After smoothing, each track is
+   * extrapolated to it (extrapolateTrackToReferenceSurface,
+   * Core/include/Acts/Utilities/TrackHelpers.hpp:175-381) with the
+   * reference's default propagator options, and its parameters and
+   * covariance there are written to ck_batch_out.track_params/track_cov. */
+  int32_t reference_surface;
   /* 0 (default, the reference's behaviour): when outliers keep the track
    * incomplete, propagation continues after the last surface that carries a
    * source link until the loop-protection path limit, and any propagation
@@ -207,7 +222,12 @@ typedef struct ck_options {
    * track), which turns those failures into successful fits. */
   int32_t early_termination;
   int32_t smoother;             /* CK_SMOOTHER_*, default GAIN_MATRIX       */
+  /* KalmanFitterOptions::referenceSurfaceStrategy (TrackExtrapolationStrategy):
+   * the track state the extrapolation starts from; default FIRST_OR_LAST. */
+  int32_t reference_strategy;
 } ck_options;
+
+enum { CK_EXTRAPOLATE_FIRST = 0, CK_EXTRAPOLATE_LAST = 1, CK_EXTRAPOLATE_FIRST_OR_LAST = 2 };
 
 /* --------------------------------------------------------------- handle */
 
@@ -270,7 +290,8 @@ enum {
   CK_OUT_PREDICTED = 1u << 0,
   CK_OUT_FILTERED = 1u << 1,
   CK_OUT_SMOOTHED = 1u << 2,
-  CK_OUT_JACOBIAN = 1u << 3
+  CK_OUT_JACOBIAN = 1u << 3,
+  CK_OUT_REFERENCE = 1u << 4   /* track parameters at the reference surface */
 };
 
 /* Results of a batch. Arrays the component mask does not select may be NULL.
@@ -300,6 +321,12 @@ typedef struct ck_batch_out {
   double* smoothed;          /* C = 6  */
   double* smoothed_cov;      /* C = 36 */
   double* jacobian;          /* C = 36, transport from the previous state   */
+  /* per track [C * n_tracks], element c of track t at [c * n_tracks + t]:
+   * the track's parameters and covariance at the reference surface
+   * (TrackProxy::parameters / covariance after the extrapolation); written
+   * when options.reference_surface >= 0 */
+  double* track_params;      /* C = 6  */
+  double* track_cov;         /* C = 36 */
 } ck_batch_out;
 
 /* Fills the reference defaults (see ck_options). Replaces the default member
@@ -342,7 +369,9 @@ ck_status ck_sync(ck_handle* h);
 ck_status ck_fit_batch_static(ck_handle* h, const ck_options* opt,
                               const ck_batch_in* in, ck_batch_out* out, void* stream);
 /* Scratch bytes ck_fit_batch_static needs for a batch (-1 on bad sizes), and
- * the size of the static array. No counterpart in the reference. */
+ * the size of the static array. No counterpart in the reference. With a
+ * reference surface (options.reference_surface >= 0) a batch needs 448 bytes
+ * per track more (two extrapolation start states). */
 int64_t ck_static_scratch_bytes(int32_t n_tracks, int32_t max_states, int32_t precision);
 int64_t ck_static_scratch_capacity(void);
 

@@ -434,6 +434,22 @@ struct Surface {
   int intersect(const V3<S>& pos, const V3<S>& dir, S tol, Intersection<S> out[2]) const {
     using std::abs;
     using std::sqrt;
+    if (type == CK_SURFACE_LINE) {
+      // LineSurface::intersect (LineSurface.cpp:141-185): closest approach of
+      // the straight track to the line; no bounds (a PerigeeSurface)
+      V3<S> eb = col(2);
+      V3<S> mab;
+      for (int i = 0; i < 3; ++i) mab[i] = c[i] - pos[i];
+      S eaTeb = dot(dir, eb);
+      S denom = S(1.0) - eaTeb * eaTeb;
+      if (abs(denom) < abs(tol)) {
+        out[0] = Intersection<S>{S(std::numeric_limits<double>::infinity()), IStatus::unreachable};
+        return 0;
+      }
+      S u = (dot(mab, dir) - dot(mab, eb) * eaTeb) / denom;
+      out[0] = Intersection<S>{u, abs(u) > abs(tol) ? IStatus::reachable : IStatus::onSurface};
+      return 1;
+    }
     if (type == CK_SURFACE_PLANE) {
       V3<S> n = col(2);
       S denom = dot(dir, n);
@@ -483,10 +499,21 @@ struct Surface {
     return 2;
   }
 
-  // PlaneSurface.cpp:77-86 ; CylinderSurface.cpp:125-145
-  bool globalToLocal(const V3<S>& pos, S tol, S loc[2]) const {
+  // PlaneSurface.cpp:77-86 ; CylinderSurface.cpp:125-145 ;
+  // LineSurface.cpp:70-96 (the line frame depends on the direction)
+  bool globalToLocal(const V3<S>& pos, const V3<S>& dir, S tol, S loc[2]) const {
     using std::abs;
     using std::atan2;
+    if (type == CK_SURFACE_LINE) {
+      Mat<S, 3, 3> f = referenceFrame(pos, dir);
+      V3<S> d;
+      for (int i = 0; i < 3; ++i) d[i] = pos[i] - c[i];
+      S lz = f.a[0][2] * d[0] + f.a[1][2] * d[1] + f.a[2][2] * d[2];
+      if (abs(lz) > abs(tol)) return false;
+      loc[0] = f.a[0][0] * d[0] + f.a[1][0] * d[1] + f.a[2][0] * d[2];
+      loc[1] = f.a[0][1] * d[0] + f.a[1][1] * d[1] + f.a[2][1] * d[2];
+      return true;
+    }
     V3<S> l = toLocal3(pos);
     if (type == CK_SURFACE_PLANE) {
       if (abs(l[2]) > abs(tol)) return false;
@@ -503,11 +530,19 @@ struct Surface {
     return true;
   }
 
-  // PlaneSurface.cpp:72-75 ; CylinderSurface.cpp:116-123
-  V3<S> localToGlobal(const S loc[2]) const {
+  // PlaneSurface.cpp:72-75 ; CylinderSurface.cpp:116-123 ; LineSurface.cpp:57-68
+  V3<S> localToGlobal(const S loc[2], const V3<S>& dir) const {
     using std::cos;
     using std::sin;
     V3<S> l;
+    if (type == CK_SURFACE_LINE) {
+      V3<S> r = normalized(cross(col(2), dir));
+      V3<S> z;
+      for (int i = 0; i < 3; ++i) z[i] = R[i][2] * loc[1] + c[i];
+      V3<S> g;
+      for (int i = 0; i < 3; ++i) g[i] = z[i] + loc[0] * r[i];
+      return g;
+    }
     if (type == CK_SURFACE_PLANE) {
       l[0] = loc[0];
       l[1] = loc[1];
@@ -532,9 +567,20 @@ struct Surface {
     return g;
   }
 
-  // PlaneSurface.cpp:63-66 ; CylinderSurface.cpp:93-110
-  Mat<S, 3, 3> referenceFrame(const V3<S>& pos) const {
+  // PlaneSurface.cpp:63-66 ; CylinderSurface.cpp:93-110 ; LineSurface.cpp:102-115
+  Mat<S, 3, 3> referenceFrame(const V3<S>& pos, const V3<S>& dir) const {
     Mat<S, 3, 3> f;
+    if (type == CK_SURFACE_LINE) {
+      V3<S> z0 = col(2);
+      V3<S> d0 = normalized(cross(z0, dir));
+      V3<S> dist = cross(d0, z0);
+      for (int i = 0; i < 3; ++i) {
+        f.a[i][0] = d0[i];
+        f.a[i][1] = z0[i];
+        f.a[i][2] = dist[i];
+      }
+      return f;
+    }
     if (type == CK_SURFACE_PLANE) {
       for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) f.a[i][j] = R[i][j];
@@ -562,7 +608,7 @@ struct Surface {
 
   // Surface.cpp:249-268
   Mat<S, 8, 6> boundToFreeJacobian(const V3<S>& pos, const V3<S>& dir) const {
-    Mat<S, 3, 3> rf = referenceFrame(pos);
+    Mat<S, 3, 3> rf = referenceFrame(pos, dir);
     Mat<S, 8, 6> j = Mat<S, 8, 6>::zero();
     for (int i = 0; i < 3; ++i) {
       j.a[i][0] = rf.a[i][0];
@@ -580,7 +626,7 @@ struct Surface {
 
   // Surface.cpp:270-291
   Mat<S, 6, 8> freeToBoundJacobian(const V3<S>& pos, const V3<S>& dir) const {
-    Mat<S, 3, 3> rf = referenceFrame(pos);
+    Mat<S, 3, 3> rf = referenceFrame(pos, dir);
     Mat<S, 6, 8> j = Mat<S, 6, 8>::zero();
     for (int k = 0; k < 3; ++k) {
       j.a[0][k] = rf.a[k][0];
@@ -596,9 +642,22 @@ struct Surface {
     return j;
   }
 
-  // Surface.cpp:293-306
+  // Surface.cpp:293-306 ; LineSurface.cpp:224-251
   Vec<S, 8> freeToPathDerivative(const V3<S>& pos, const V3<S>& dir) const {
-    Mat<S, 3, 3> rf = referenceFrame(pos);
+    if (type == CK_SURFACE_LINE) {
+      V3<S> pc, z = col(2);
+      for (int i = 0; i < 3; ++i) pc[i] = pos[i] - c[i];
+      S pz = dot(pc, z);
+      S dz = dot(z, dir);
+      S nrm = S(1.0) / (S(1.0) - dz * dz);
+      Vec<S, 8> f = Vec<S, 8>::zero();
+      for (int i = 0; i < 3; ++i) {
+        f[i] = nrm * (dz * z[i] - dir[i]);
+        f[4 + i] = nrm * (pz * z[i] - pc[i]);
+      }
+      return f;
+    }
+    Mat<S, 3, 3> rf = referenceFrame(pos, dir);
     V3<S> z;
     for (int i = 0; i < 3; ++i) z[i] = rf.a[i][2];
     S dz = dot(z, dir);
@@ -620,7 +679,7 @@ Vec<S, 8> boundToFree(const Surface<S>& s, const Vec<S, 6>& b) {
   dir[1] = sin(b[2]) * sinTheta;
   dir[2] = cos(b[3]);
   S loc[2] = {b[0], b[1]};
-  V3<S> pos = s.localToGlobal(loc);
+  V3<S> pos = s.localToGlobal(loc, dir);
   Vec<S, 8> f;
   f[0] = pos[0];
   f[1] = pos[1];
@@ -639,7 +698,7 @@ bool freeToBound(const Vec<S, 8>& f, const Surface<S>& s, Vec<S, 6>& b) {
   V3<S> pos{{f[0], f[1], f[2]}};
   V3<S> dir{{f[4], f[5], f[6]}};
   S loc[2];
-  if (!s.globalToLocal(pos, S(kOnSurfaceTolerance), loc)) return false;
+  if (!s.globalToLocal(pos, dir, S(kOnSurfaceTolerance), loc)) return false;
   b[0] = loc[0];
   b[1] = loc[1];
   b[5] = f[3];
@@ -910,9 +969,13 @@ struct Options {
   double outlierChi2Cut;
   bool coastAfterLastMeasurement;  // faithful reference termination
   int smoother;                    // CK_SMOOTHER_*
+  int referenceSurface;            // -1 or a table index
+  int referenceStrategy;           // CK_EXTRAPOLATE_*
   static Options fromCk(const ck_options& o, bool coast) {
     Options r;
     r.smoother = o.smoother;
+    r.referenceSurface = o.reference_surface;
+    r.referenceStrategy = o.reference_strategy;
     r.stepTolerance = o.step_tolerance;
     r.stepSizeCutOff = o.step_size_cutoff;
     r.initialStepSize = o.initial_step_size;
@@ -939,7 +1002,8 @@ struct Options {
 enum StepErr { kStepOk = 0, kStepField = 1, kStepStalled = 2, kStepAdjust = 3 };
 
 template <typename S>
-int eigenStep(Stepper<S>& st, const Field<S>& field, const Options& o, S& hOut) {
+int eigenStep(Stepper<S>& st, const Field<S>& field, const Options& o, S& hOut,
+              int propDir = 1) {
   using std::abs;
   using std::sqrt;
   V3<S> pos = st.pos();
@@ -984,7 +1048,7 @@ int eigenStep(Stepper<S>& st, const Field<S>& field, const Options& o, S& hOut) 
     ok = errorEstimate <= S(4.0) * S(o.stepTolerance);
     return true;
   };
-  const S initialH = S(st.stepSize.value());  // propDir = +1
+  const S initialH = S(st.stepSize.value() * propDir);  // EigenStepper.ipp:272
   S h = initialH;
   unsigned nStepTrials = 0;
   while (true) {
@@ -1154,7 +1218,10 @@ void transportCovarianceToBound(Stepper<S>& st, const Surface<S>& s) {
   st.jacTransport = Mat<S, 8, 8>::identity();
   st.derivative = Vec<S, 8>::zero();
   S loc[2];
-  if (s.globalToLocal(pos, S(kOnSurfaceTolerance), loc)) st.jacToGlobal = s.boundToFreeJacobian(pos, dir);
+  // (after the extrapolation to a line surface nothing steps on, so its
+  // bound-to-free Jacobian, LineSurface.cpp:187-222, is not needed)
+  if (s.type != CK_SURFACE_LINE && s.globalToLocal(pos, dir, S(kOnSurfaceTolerance), loc))
+    st.jacToGlobal = s.boundToFreeJacobian(pos, dir);
 }
 
 // -------------------------------------------------------------- KF output
@@ -1162,6 +1229,8 @@ struct TrackOut {
   int status = CK_TRACK_NOT_PROCESSED;
   int nStates = 0, nMeasurements = 0, nHoles = 0, nOutliers = 0, ndf = 0;
   double chi2 = 0;
+  bool hasTrackParams = false;  // parameters at the reference surface
+  double trackParams[6], trackCov[36];
   struct St {
     int surface;
     uint32_t flags;
@@ -1444,6 +1513,148 @@ struct Fitter {
     int measDim = 0;  // dimension of the state's measurement (ndf)
   };
 
+  // PropagatorPlainOptions / StepperPlainOptions defaults
+  // (PropagatorOptions.hpp:28-51, StepperOptions.hpp:36-49): the options of
+  // the extrapolation (KalmanFitter.hpp:960-961 builds them afresh)
+  static Options defaultPropagation() {
+    Options d{};
+    d.stepTolerance = 1e-4;
+    d.stepSizeCutOff = 0.0;
+    d.initialStepSize = 10000.0;
+    d.maxStepSize = std::numeric_limits<double>::max();
+    d.maxRungeKuttaStepTrials = 10000;
+    d.maxSteps = 1000;
+    d.maxTargetSkipping = 100;
+    d.loopProtection = true;
+    d.pathLimit = std::numeric_limits<double>::max();
+    d.loopFraction = 0.5;
+    d.surfaceTolerance = kOnSurfaceTolerance;
+    d.nearLimit = -0.1;
+    return d;
+  }
+
+  // extrapolateTrackToReferenceSurface (TrackHelpers.hpp:339-381): the start
+  // state by the strategy (findTrackStateForExtrapolation, :175-300; first /
+  // last state with a non-outlier measurement, its smoothed parameters), then
+  // Propagator::propagate with ForcedSurfaceReached and PathLimitReached
+  // (Propagator.ipp:25-210, StandardAborters.hpp:66-164) in the direction of
+  // the straight-line distance, and the bound state on the target with the
+  // transported covariance (Propagator.ipp:342-380).
+  int extrapolate(const std::vector<IState>& states, int tip, float mass, float absQ, int absPdg,
+                  TrackOut& out) const {
+    using std::abs;
+    const std::vector<Surface<S>>& sf = *surfaces;
+    const Surface<S>& target = sf[o.referenceSurface];
+    int first = -1, last = -1;
+    for (int k = 0; k <= tip; ++k)
+      if ((states[k].flags & CK_FLAG_HAS_MEASUREMENT) && !(states[k].flags & CK_FLAG_IS_OUTLIER)) {
+        if (first < 0) first = k;
+        last = k;
+      }
+    if (first < 0) return CK_TRACK_NO_COMPATIBLE_STATE;
+    auto intersectFrom = [&](int k, S& path) -> bool {
+      Vec<S, 8> f = boundToFree(sf[states[k].surface], states[k].smth);
+      V3<S> pos{{f[0], f[1], f[2]}}, dir{{f[4], f[5], f[6]}};
+      Intersection<S> is[2];
+      const int n = target.intersect(pos, dir, S(kOnSurfaceTolerance), is);
+      path = is[0].pathLength;
+      return n > 0 && is[0].status != IStatus::unreachable;
+    };
+    int k = -1;
+    S distance = S(0.0);
+    if (o.referenceStrategy == CK_EXTRAPOLATE_FIRST || o.referenceStrategy == CK_EXTRAPOLATE_LAST) {
+      k = o.referenceStrategy == CK_EXTRAPOLATE_FIRST ? first : last;
+      if (!intersectFrom(k, distance)) return CK_TRACK_REFERENCE_UNREACHABLE;
+    } else {
+      S pf, pl;
+      const bool vf = intersectFrom(first, pf), vl = intersectFrom(last, pl);
+      const S inf = S(std::numeric_limits<double>::infinity());
+      const S df = vf ? abs(pf) : inf, dl = vl ? abs(pl) : inf;
+      if (vf && df <= dl) {
+        k = first;
+        distance = pf;
+      } else if (vl && dl <= df) {
+        k = last;
+        distance = pl;
+      } else {
+        return CK_TRACK_REFERENCE_UNREACHABLE;
+      }
+    }
+    const int propDir = distance >= S(0.0) ? 1 : -1;  // Direction::fromScalarZeroAsPositive
+    const Options eo = defaultPropagation();
+    const Surface<S>& from = sf[states[k].surface];
+    Stepper<S> st;
+    st.mass = mass;
+    st.absQ = absQ;
+    st.absPdg = absPdg;
+    st.pars = boundToFree(from, states[k].smth);
+    st.pathAccumulated = S(0.0);
+    st.nSteps = 0;
+    st.stepSize = ConstrainedStep();
+    st.stepSize.accuracy = eo.initialStepSize;
+    st.stepSize.values[kUser] = eo.maxStepSize;
+    st.cov = states[k].smthCov;
+    st.jacToGlobal = from.boundToFreeJacobian(st.pos(), st.dir());
+    st.jacobian = Mat<S, 6, 6>::identity();
+    st.jacTransport = Mat<S, 8, 8>::identity();
+    st.derivative = Vec<S, 8>::zero();
+    // loop protection of the path aborter (LoopProtection.hpp:19-72)
+    double pathLimit = eo.pathLimit;
+    {
+      V3<S> B;
+      if (field.get(st.pos(), B)) {
+        const double Bn = (double)norm(B);
+        if (Bn != 0) {
+          const double ll = eo.loopFraction * (2 * kPi * (double)st.absoluteMomentum() / Bn);
+          if (std::abs(ll) < std::abs(pathLimit)) pathLimit = ll;
+        }
+      }
+    }
+    // the aborters in list order; the first that fires ends the propagation
+    auto checkAbort = [&]() -> bool {
+      V3<S> d = st.dir();
+      for (int i = 0; i < 3; ++i) d[i] = S(double(propDir)) * d[i];
+      Intersection<S> is[2];
+      const int n = target.intersect(st.pos(), d, S(eo.surfaceTolerance), is);
+      const bool reached = n > 0 && is[0].status == IStatus::onSurface;
+      if (n > 0 && is[0].status != IStatus::unreachable) {
+        // updateSingleSurfaceStatus (SteppingHelper.hpp:41-78), Actor type
+        st.stepSize.release(kActor);
+        st.stepSize.update((double)is[0].pathLength, kActor);
+      }
+      if (reached) return true;
+      const double dist = std::abs(pathLimit) - std::abs((double)st.pathAccumulated);
+      if (std::abs(dist) < std::abs(eo.surfaceTolerance)) return true;
+      st.stepSize.update(dist, kActor);
+      return false;
+    };
+    if (!checkAbort()) {
+      bool terminated = false;
+      for (unsigned s = 0; s < eo.maxSteps; ++s) {
+        S h;
+        const int se = eigenStep(st, field, eo, h, propDir);
+        if (se != kStepOk)
+          return se == kStepField ? CK_TRACK_FIELD_OUT_OF_BOUNDS
+                                  : (se == kStepStalled ? CK_TRACK_STEP_SIZE_STALLED
+                                                        : CK_TRACK_STEP_ADJUST_FAILED);
+        st.stepSize.release(kNav);
+        st.stepSize.release(kActor);
+        if (checkAbort()) {
+          terminated = true;
+          break;
+        }
+      }
+      if (!terminated) return CK_TRACK_STEP_COUNT_LIMIT;
+    }
+    transportCovarianceToBound(st, target);
+    Vec<S, 6> bp;
+    if (!freeToBound(st.pars, target, bp)) return CK_TRACK_NOT_ON_SURFACE;
+    put6(out.trackParams, bp);
+    put36(out.trackCov, st.cov);
+    out.hasTrackParams = true;
+    return CK_TRACK_OK;
+  }
+
   int fit(const Surface<S>& startSurface, const Vec<S, 6>& startPars, const Mat<S, 6, 6>& startCov,
           float mass, float absQ, int absPdg, const int* seq, int nSeq,
           const std::vector<MeasRec<S>>& meas, TrackOut& out) const {
@@ -1537,7 +1748,7 @@ struct Fitter {
       V3<S> pos = st.pos(), dir = st.dir();
       S pc = s.pathCorrection(pos, dir);
       S loc[2];
-      if (!s.globalToLocal(pos, S(kOnSurfaceTolerance), loc)) return false;
+      if (!s.globalToLocal(pos, st.dir(), S(kOnSurfaceTolerance), loc)) return false;
       Slab slab = s.slab;
       if (!slab.isVacuum()) {
         double factor = (mode == 3) ? 1.0 : (mode == 1 ? 1.0 - s.splitFactor : (double)s.splitFactor);
@@ -1851,6 +2062,17 @@ struct Fitter {
         ++out.nMeasurements;
         out.chi2 += (double)ts.chi2;
         out.ndf += ts.measDim;
+      }
+    }
+    if (o.referenceSurface >= 0) {
+      // KalmanFitter.hpp:959-972: the fit fails when the extrapolation does
+      const int e = extrapolate(states, tip, mass, absQ, absPdg, out);
+      if (e != CK_TRACK_OK) {
+        out.status = e;
+        out.states.clear();
+        out.nStates = out.nMeasurements = out.nHoles = out.nOutliers = out.ndf = 0;
+        out.chi2 = 0;
+        return e;
       }
     }
     return CK_TRACK_OK;

@@ -38,6 +38,12 @@ void writeTrack(const TrackOut& t, int tr, int n, const ck_batch_out* out) {
     if (out->n_states) out->n_states[tr] = 0;
     return;
   }
+  if (t.hasTrackParams) {
+    for (int c = 0; c < 6; ++c)
+      if (out->track_params) out->track_params[(size_t)c * n + tr] = t.trackParams[c];
+    for (int c = 0; c < 36; ++c)
+      if (out->track_cov) out->track_cov[(size_t)c * n + tr] = t.trackCov[c];
+  }
   auto at = [&](int k, int C, int c) -> size_t { return ((size_t)k * C + c) * n + tr; };
   for (int k = 0; k < ns; ++k) {
     const TrackOut::St& s = t.states[k];
@@ -61,13 +67,16 @@ void writeTrack(const TrackOut& t, int tr, int n, const ck_batch_out* out) {
 
 void fitOne(const Ctx& ctx, const ck_batch_in* in, int tr, TrackOut& t) {
   const int ns = (int)ctx.surfaces.size();
+  // (a line surface is only a reference surface: not in a sequence, no
+  // measurement on it)
+  auto bad = [&](int sid) { return sid < 0 || sid >= ns || ctx.surfaces[sid].type == CK_SURFACE_LINE; };
   for (int k = in->seq_offsets[tr]; k < in->seq_offsets[tr + 1]; ++k)
-    if (in->seq_surfaces[k] < 0 || in->seq_surfaces[k] >= ns) {
+    if (bad(in->seq_surfaces[k])) {
       t.status = CK_TRACK_INVALID_INPUT;
       return;
     }
   for (int k = in->meas_offsets[tr]; k < in->meas_offsets[tr + 1]; ++k)
-    if (in->meas_surfaces[k] < 0 || in->meas_surfaces[k] >= ns ||
+    if (bad(in->meas_surfaces[k]) ||
         (in->meas_subspace && (in->meas_subspace[k] < CK_MEAS_LOC0 ||
                                in->meas_subspace[k] > CK_MEAS_LOC01))) {
       t.status = CK_TRACK_INVALID_INPUT;
@@ -218,6 +227,37 @@ void kfo_mbf_smooth(int n_traj, int n_states, const uint32_t* flags, const doubl
         mbfVisitNonMeasurement(F, L, l);
     }
   }
+}
+
+// LineSurface::globalToLocal / intersect (LineSurface.cpp:70-96,141-185) of
+// a line surface with rotation rot (row-major, line = column 2) through
+// center, for the known-answer tests. globalToLocal: 1 on success (the
+// tolerance is infinite, as the reference test calls it); intersect: the
+// status 0 unreachable, 1 reachable, 2 on surface, and the path length.
+int kfo_line_global_to_local(const double* center, const double* rot, const double* pos,
+                             const double* dir, double* loc) {
+  ck_surface cs{};
+  cs.type = CK_SURFACE_LINE;
+  for (int i = 0; i < 9; ++i) cs.rotation[i] = rot[i];
+  for (int i = 0; i < 3; ++i) cs.center[i] = center[i];
+  Surface<double> s = Surface<double>::fromCk(cs);
+  V3<double> p{{pos[0], pos[1], pos[2]}}, d{{dir[0], dir[1], dir[2]}};
+  return s.globalToLocal(p, d, std::numeric_limits<double>::max(), loc) ? 1 : 0;
+}
+
+int kfo_line_intersect(const double* center, const double* rot, const double* pos,
+                       const double* dir, double* path) {
+  ck_surface cs{};
+  cs.type = CK_SURFACE_LINE;
+  for (int i = 0; i < 9; ++i) cs.rotation[i] = rot[i];
+  for (int i = 0; i < 3; ++i) cs.center[i] = center[i];
+  Surface<double> s = Surface<double>::fromCk(cs);
+  V3<double> p{{pos[0], pos[1], pos[2]}}, d{{dir[0], dir[1], dir[2]}};
+  Intersection<double> is[2];
+  const int n = s.intersect(p, d, kOnSurfaceTolerance, is);
+  *path = is[0].pathLength;
+  if (n == 0) return 0;
+  return is[0].status == IStatus::onSurface ? 2 : 1;
 }
 
 // Interactions.cpp entry points for the material known-answer tests.

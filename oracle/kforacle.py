@@ -35,6 +35,10 @@ def lib():
         L.kfo_gain_matrix_smooth.argtypes = [C.c_int, C.c_int] + [abi.P_f64] * 7 + [abi.P_i32]
         L.kfo_mbf_smooth.restype = None
         L.kfo_mbf_smooth.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_uint32)] + [abi.P_f64] * 9
+        L.kfo_line_global_to_local.restype = C.c_int
+        L.kfo_line_global_to_local.argtypes = [abi.P_f64] * 5
+        L.kfo_line_intersect.restype = C.c_int
+        L.kfo_line_intersect.argtypes = [abi.P_f64] * 4 + [C.POINTER(C.c_double)]
         L.kfo_interaction.restype = C.c_float
         L.kfo_interaction.argtypes = [C.c_int] + [C.c_float] * 6 + [C.c_int] + [C.c_float] * 3
         L.kfo_material_effects.restype = None
@@ -72,6 +76,27 @@ def time_batch(detector, batch, options, n_threads, first=0, count=-1):
     return lib().kfo_fit_batch(C.byref(options), detector.n_surfaces, detector.surfaces,
                                C.byref(detector.field), C.byref(bi), None, n_threads, -1, first,
                                count)
+
+
+def _v(x):
+    return np.ascontiguousarray(x, np.float64)
+
+
+def line_global_to_local(center, rotation, pos, direction):
+    """LineSurface::globalToLocal: (ok, loc[2])."""
+    loc = np.zeros(2)
+    a = [_v(center), _v(rotation), _v(pos), _v(direction)]
+    ok = lib().kfo_line_global_to_local(*[abi.ptr(x, C.c_double) for x in a],
+                                        abi.ptr(loc, C.c_double))
+    return bool(ok), loc
+
+
+def line_intersect(center, rotation, pos, direction):
+    """LineSurface::intersect: (status 0/1/2, path length)."""
+    path = C.c_double()
+    a = [_v(center), _v(rotation), _v(pos), _v(direction)]
+    st = lib().kfo_line_intersect(*[abi.ptr(x, C.c_double) for x in a], C.byref(path))
+    return st, path.value
 
 
 def gain_matrix_update(pred, pred_cov, meas, meas_cov, joseph=False, subspace=None):

@@ -7,6 +7,7 @@ reference at run time. Sources parsed (paths relative to the acts repo):
   Tests/UnitTests/Core/TrackFitting/GainMatrixUpdaterTests.cpp  (Update, UpdateFailed)
   Tests/UnitTests/Core/TrackFitting/GainMatrixSmootherTests.cpp (Smooth)
   Tests/UnitTests/Core/TrackFitting/MbfSmootherTests.cpp        (Smooth)
+  Tests/UnitTests/Core/Surfaces/LineSurfaceTests.cpp            (globalToLocal, intersect)
   Tests/UnitTests/Core/Material/InteractionsTests.cpp           (silicon Bethe, Landau)
   Tests/CommonHelpers/include/ActsTests/CommonHelpers/PredefinedMaterials.hpp (makeSilicon)
 """
@@ -101,6 +102,19 @@ def mbf_smoother(src):
             "projector": ["eBoundLoc0", "eBoundLoc1"], "flags": "measurement"}
 
 
+def line_surface(src):
+    t = open(os.path.join(src, "Tests/UnitTests/Core/Surfaces/LineSurfaceTests.cpp")).read()
+    case = t[t.index("BOOST_AUTO_TEST_CASE(LineSurface_allNamedMethods_test)"):]
+    vec = lambda pat: [num(x) for x in re.search(pat, case).group(1).split(",")]
+    return {"source": "Tests/UnitTests/Core/Surfaces/LineSurfaceTests.cpp",
+            "center": vec(r"Translation3 translation\{([^}]*)\}"),
+            "g2l_position": vec(r"Vector3 gpos\{([^}]*)\}"),
+            "g2l_momentum": vec(r"const Vector3 mom\{([^}]*)\}"),
+            "g2l_expected": vec(r"const Vector2 expectedResult\{([^}]*)\}"),
+            "intersect_direction": vec(r"const Vector3 direction\{([^}]*)\}"),
+            "intersect_expected": vec(r"Vector3 expectedIntersection\(([^)]*)\)")}
+
+
 def interactions(src):
     t = open(os.path.join(src, "Tests/UnitTests/Core/Material/InteractionsTests.cpp")).read()
     mom = re.search(r"static const double momentum\[\] = \{([^}]*)\}", t).group(1)
@@ -144,6 +158,7 @@ def silicon(src):
 def main():
     src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     out = {"updater": updater(src), "smoother": smoother(src), "mbf_smoother": mbf_smoother(src),
+           "line_surface": line_surface(src),
            "interactions": interactions(src),
            "silicon": silicon(src)}
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_known_answers.json")

@@ -55,6 +55,15 @@ def compare(gpu, ora, rtol=1e-9, fields=("predicted", "filtered", "smoothed")):
         floor = np.broadcast_to(rowmax, jr.shape).reshape(jb.shape)
         r = rel(ja, jb, floor)[m]
         rep["jacobian"] = float(r.max()) if r.size else 0.0
+    ta, tb = getattr(gpu, "track_params", None), getattr(ora, "track_params", None)
+    if ta is not None and tb is not None and ok.any():
+        # parameters and covariance at the reference surface
+        pa, pb = gpu.track("track_params")[ok], ora.track("track_params")[ok]
+        ca, cb = gpu.track("track_cov")[ok], ora.track("track_cov")[ok]
+        sig = _sig(cb)
+        rep["track_params"] = float(rel(pa, pb, sig).max())
+        floor = (sig[:, :, None] * sig[:, None, :]).reshape(-1, 36)
+        rep["track_cov"] = float(rel(ca, cb, floor).max())
     return rep
 
 
@@ -63,6 +72,7 @@ def assert_parity(rep, rtol=1e-9):
         if k.endswith("_mismatch"):
             assert v == 0, (k, rep)
     for k in ("state_path_length", "state_chi2", "chi2_sum", "predicted", "predicted_cov",
-              "filtered", "filtered_cov", "smoothed", "smoothed_cov", "jacobian"):
+              "filtered", "filtered_cov", "smoothed", "smoothed_cov", "jacobian", "track_params",
+              "track_cov"):
         if k in rep:
             assert rep[k] <= rtol, (k, rep[k], rep)

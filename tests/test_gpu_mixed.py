@@ -84,3 +84,37 @@ def test_mixed_precision_accuracy(fitter_factory, preset, smoother):
     c64 = ora.chi2_sum[ok].sum() / ora.ndf[ok].sum()
     cmx = mix.chi2_sum[ok].sum() / mix.ndf[ok].sum()
     assert abs(c64 - cmx) / c64 < 1e-3
+
+
+@pytest.mark.gpu
+def test_mixed_precision_perigee_parameters():
+    """The perigee parameters of the mixed form (extrapolated in FP64 from the
+    mixed smoothed first measurement state) against the FP64 oracle's, with
+    the same relative bound as the smoothed parameters."""
+    from acts_gb300 import generate
+    from acts_gb300.fitter import CudaKalman
+
+    det = generate.Detector(abi.CKG_BARREL, perigee=True)
+    n = 20000
+    b = generate.generate(det, n, seed=13)
+    kw = dict(reference_surface=det.perigee, reference_strategy=abi.EXTRAPOLATE_FIRST)
+    comps = abi.OUT_SMOOTHED | abi.OUT_REFERENCE
+    ora = Results(n, 12, comps)
+    kforacle.fit_batch(det, b, abi.default_options(**kw), ora,
+                       n_threads=kforacle.hardware_threads())
+    fit = CudaKalman.for_detector(det)
+    try:
+        mix = fit.fit_batch(b, abi.default_options(precision=abi.PRECISION_MIXED, **kw),
+                            max_states=12, components=comps)
+    finally:
+        fit.close()
+    ok = (mix.status == 0) & (ora.status == 0)
+    ok &= ora.chi2_sum < GOOD_CHI2NDF * np.maximum(ora.ndf, 1)
+    assert ok.mean() > 0.99
+    a, o = mix.track("track_params")[ok], ora.track("track_params")[ok]
+    sig = np.sqrt(ora.track("track_cov")[ok][:, [0, 7, 14, 21, 28, 35]])
+    d = np.abs(a - o)
+    d[:, 2] = np.abs((a[:, 2] - o[:, 2] + np.pi) % (2 * np.pi) - np.pi)
+    rel = d / np.maximum(np.abs(o), sig)
+    print("perigee max rel %.3g" % rel.max())
+    assert rel.max() <= REL_BOUND

@@ -53,6 +53,44 @@ def test_fp64_parity(fitter_factory, name, preset, n, kw, min_ok):
     assert_parity(rep, RTOL)
 
 
+# extrapolation to a PerigeeSurface at the origin (the reference surface of
+# the reference's TrackFittingAlgorithm) with each strategy
+REF_CASES = [
+    ("barrel_perigee_first", abi.CKG_BARREL, 2000, dict(reference_strategy=abi.EXTRAPOLATE_FIRST)),
+    ("barrel_perigee_last", abi.CKG_BARREL, 1000, dict(reference_strategy=abi.EXTRAPOLATE_LAST)),
+    ("uneven_perigee_first_or_last", abi.CKG_UNEVEN, 2000,
+     dict(outlier_chi2_cut=15.0, early_termination=1,
+          reference_strategy=abi.EXTRAPOLATE_FIRST_OR_LAST)),
+    ("strips_perigee_mbf", abi.CKG_STRIPS, 1000,
+     dict(smoother=abi.SMOOTHER_MBF, reference_strategy=abi.EXTRAPOLATE_FIRST)),
+    ("telescope_perigee", abi.CKG_TELESCOPE, 500, dict()),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,preset,n,kw", REF_CASES, ids=[c[0] for c in REF_CASES])
+def test_fp64_parity_reference_surface(name, preset, n, kw):
+    from acts_gb300 import generate
+    from acts_gb300.fitter import CudaKalman
+
+    det = generate.Detector(preset, perigee=True)
+    b = generate.generate(det, n, seed=11)
+    opt = abi.default_options(reference_surface=det.perigee, **kw)
+    comps = abi.OUT_SMOOTHED | abi.OUT_REFERENCE
+    ora = Results(n, 24, comps)
+    kforacle.fit_batch(det, b, opt, ora, n_threads=kforacle.hardware_threads())
+    fit = CudaKalman.for_detector(det)
+    try:
+        gpu = fit.fit_batch(b, opt, max_states=24, components=comps)
+    finally:
+        fit.close()
+    rep = compare(gpu, ora, RTOL)
+    print(name, rep)
+    assert rep["n_ok"] >= 0.99 * n
+    assert "track_params" in rep
+    assert_parity(rep, RTOL)
+
+
 # every forward-filter kernel variant: per-warp phase scheduling with the
 # three register caps, block-level phase compaction with 256 and 128 slots
 VARIANTS = [(0, 128, 2), (1, 128, 3), (2, 128, 4), (3, 256, 1), (4, 128, 2)]

@@ -126,3 +126,44 @@ def test_oversized_event_rejected(fitter_factory):
         r = srv.poll(timeout_ms=200)
     srv.close()
     assert r is not None and r[0] == 2 and (r[1].status == 0).mean() > 0.99
+
+
+@pytest.mark.gpu
+def test_serving_with_reference_surface():
+    """Events fitted through the serving loop with extrapolation to a
+    perigee surface: every event's perigee parameters (and states) equal its
+    fit alone."""
+    from acts_gb300.fitter import CudaKalman
+
+    det = generate.Detector(abi.CKG_UNEVEN, perigee=True)
+    fit = CudaKalman.for_detector(det)
+    comps = abi.OUT_SMOOTHED | abi.OUT_REFERENCE
+    opt = abi.default_options(precision=abi.PRECISION_MIXED, outlier_chi2_cut=15.0,
+                              reference_surface=det.perigee)
+    sizes = generate.event_sizes(9, 10, lo=100, hi=3000)
+    evs = _events(det, sizes, seed=41)
+    srv = FitServer(fit, opt, memory_budget_bytes=2 << 30, n_streams=2, max_states=24,
+                    max_batch_tracks=8000, components=comps)
+    try:
+        for i, ev in enumerate(evs):
+            srv.submit(i, ev)
+        got = {}
+        t0 = time.time()
+        while len(got) < len(evs) and time.time() - t0 < 120:
+            r = srv.poll(timeout_ms=200)
+            if r is not None:
+                got[r[0]] = r[1]
+    finally:
+        srv.close()
+    assert len(got) == len(evs)
+    try:
+        for i, ev in enumerate(evs):
+            res = got[i]
+            alone = fit.fit_batch(ev, opt, max_states=24, components=comps)
+            assert np.array_equal(res.status, alone.status), i
+            ok = alone.status == 0
+            assert ok.mean() > 0.3
+            for name in ("track_params", "track_cov"):
+                assert np.array_equal(res.track(name)[ok], alone.track(name)[ok]), (i, name)
+    finally:
+        fit.close()

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from acts_gb300 import abi
-from conftest import detector
+from conftest import batch, detector
 from oracle import kforacle
 
 KA = json.load(open(os.path.join(os.path.dirname(__file__), "golden",
@@ -213,3 +213,20 @@ def test_mixed_form_atan2_matches_correctly_rounded(fitter_factory):
     seam = np.isclose(np.abs(ref), np.pi) & np.isclose(np.abs(got), np.pi)
     ulp[seam] = np.minimum(ulp[seam], np.abs(np.abs(got[seam]) - np.abs(ref[seam])) / np.spacing(np.pi))
     assert ulp.max() <= 4, (ulp.max(), y[ulp.argmax()], x[ulp.argmax()])
+
+
+@pytest.mark.gpu
+def test_reference_surface_must_be_a_line(fitter_factory):
+    """A reference surface that is not a line (perigee) surface is rejected
+    with CK_ERR_UNSUPPORTED; an index outside the table with
+    CK_ERR_INVALID_ARGUMENT."""
+    from acts_gb300.fitter import CudaKalmanError
+
+    fit = fitter_factory(abi.CKG_BARREL)
+    b = batch(abi.CKG_BARREL, 10)
+    with pytest.raises(CudaKalmanError) as e:
+        fit.fit_batch(b, abi.default_options(reference_surface=0))
+    assert e.value.status == abi.CK_ERR_UNSUPPORTED
+    with pytest.raises(CudaKalmanError) as e:
+        fit.fit_batch(b, abi.default_options(reference_surface=10 ** 6))
+    assert e.value.status == abi.CK_ERR_INVALID_ARGUMENT

@@ -165,6 +165,82 @@ def test_invalid_subspace_rejected():
     assert (np.delete(r.status, 3) != 12).all()
 
 
+# ------------------------------------------------------ LineSurfaceTests.cpp
+def test_line_surface_known_answers():
+    ls = KA["line_surface"]
+    rot = np.eye(3).reshape(9)
+    mom = np.array(ls["g2l_momentum"])
+    ok, loc = kforacle.line_global_to_local(ls["center"], rot, ls["g2l_position"],
+                                            mom / np.linalg.norm(mom))
+    assert ok
+    np.testing.assert_allclose(loc, ls["g2l_expected"], atol=1e-6)
+    d = np.array(ls["intersect_direction"])
+    d = d / np.linalg.norm(d)
+    st, path = kforacle.line_intersect(ls["center"], rot, [0.0, 0.0, 0.0], d)
+    assert st == 1  # reachable
+    np.testing.assert_allclose(path * d, ls["intersect_expected"], atol=1e-6)
+
+
+def _perigee_fit(preset, n, **kw):
+    from acts_gb300 import generate
+
+    det = generate.Detector(preset, perigee=True)
+    b = generate.generate(det, n, seed=3)
+    res = Results(b.n, 24, abi.OUT_SMOOTHED | abi.OUT_REFERENCE)
+    kforacle.fit_batch(det, b, abi.default_options(reference_surface=det.perigee, **kw), res,
+                       n_threads=4)
+    return det, b, res
+
+
+@pytest.mark.parametrize("strategy", [abi.EXTRAPOLATE_FIRST, abi.EXTRAPOLATE_FIRST_OR_LAST])
+def test_extrapolation_to_perigee_pulls(strategy):
+    """extrapolateTrackToReferenceSurface to a PerigeeSurface at the origin
+    from the first measurement state (firstOrLast picks it: it is nearer):
+    the perigee parameters against the generator truth (d0 = 0, z0 = vertex
+    z, and the momentum at the vertex) have pulls of mean 0, width 1."""
+    det, b, r = _perigee_fit(abi.CKG_BARREL, 3000, reference_strategy=strategy)
+    ok = r.status == 0
+    assert ok.mean() > 0.99
+    tp, tc = r.track("track_params"), r.track("track_cov")
+    ts = b.truth_start.reshape(-1, 6)
+    truth = [np.zeros(b.n), b.start_frames.reshape(-1, 12)[:, 11], ts[:, 2], ts[:, 3], ts[:, 4]]
+    for i in range(5):
+        d = tp[ok, i] - truth[i][ok]
+        if i == 2:
+            d = (d + np.pi) % (2 * np.pi) - np.pi
+        pull = d / np.sqrt(tc[ok, 7 * i])
+        assert abs(pull.mean()) < 0.08, (i, pull.mean())
+        assert 0.93 < pull.std() < 1.07, (i, pull.std())
+
+
+def test_extrapolation_strategies_agree_without_material():
+    """Without process noise every smoothed state estimates the same
+    trajectory: the first, the last and the nearer state give the same
+    perigee parameters (telescope), up to the linearisation and the
+    Runge-Kutta error of the longer extrapolation (a few % of a sigma)."""
+    res = [_perigee_fit(abi.CKG_TELESCOPE, 200, reference_strategy=s)[2]
+           for s in (abi.EXTRAPOLATE_FIRST, abi.EXTRAPOLATE_LAST, abi.EXTRAPOLATE_FIRST_OR_LAST)]
+    assert all((r.status == 0).all() for r in res)
+    sig = np.sqrt(res[0].track("track_cov")[:, [0, 7, 14, 21, 28, 35]])
+    for r in res[1:]:
+        d = np.abs(r.track("track_params") - res[0].track("track_params")) / sig
+        assert d.max() < 0.05, d.max(axis=0)
+    np.testing.assert_array_equal(res[2].track("track_params"), res[0].track("track_params"))
+
+
+def test_line_surface_only_as_reference():
+    """A sequence that contains the line surface is invalid input."""
+    from acts_gb300 import generate
+
+    det = generate.Detector(abi.CKG_BARREL, perigee=True)
+    b = generate.generate(det, 5, seed=3)
+    b.seq_surfaces[b.seq_offsets[2]] = det.perigee
+    res = Results(b.n, 24)
+    kforacle.fit_batch(det, b, abi.default_options(), res, n_threads=1)
+    assert res.status[2] == 12
+    assert (np.delete(res.status, 2) == 0).all()
+
+
 # ---------------------------------------------------- MbfSmootherTests.cpp
 def mbf_inputs():
     s = KA["mbf_smoother"]

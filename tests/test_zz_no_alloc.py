@@ -123,3 +123,35 @@ def test_static_scratch_rejects_oversized_batch(fitter_factory):
         fit.fit_batch_static(abi.default_options(), bi, bo)
     assert e.value.status == abi.CK_ERR_SCRATCH_LIMIT
     assert "static scratch" in str(e.value)
+
+
+@pytest.mark.gpu
+def test_static_scratch_with_reference_surface():
+    """ck_fit_batch_static with extrapolation to a perigee surface (its start
+    states in the static array too) gives ck_fit_batch's perigee parameters."""
+    from acts_gb300 import generate
+    from acts_gb300.fitter import CudaKalman
+
+    det = generate.Detector(abi.CKG_BARREL, perigee=True)
+    b = generate.generate(det, N_TRACKS, seed=29)
+    dev = torch.device("cuda", 0)
+    opt = abi.default_options(precision=abi.PRECISION_MIXED, reference_surface=det.perigee)
+    fit = CudaKalman.for_detector(det)
+    try:
+        bi, keep_in = _device_in(b, dev)
+        outs = []
+        for call in (fit.fit_batch_raw, fit.fit_batch_static):
+            bo, keep = _device_out(N_TRACKS, dev)
+            tp = torch.zeros(6 * N_TRACKS, dtype=torch.float64, device=dev)
+            tc = torch.zeros(36 * N_TRACKS, dtype=torch.float64, device=dev)
+            bo.track_params = C.cast(C.c_void_p(tp.data_ptr()), C.POINTER(C.c_double))
+            bo.track_cov = C.cast(C.c_void_p(tc.data_ptr()), C.POINTER(C.c_double))
+            call(opt, bi, bo)
+            fit.sync()
+            outs.append((keep["status"].cpu().numpy(), tp.cpu().numpy(), tc.cpu().numpy()))
+    finally:
+        fit.close()
+    (s0, p0, c0), (s1, p1, c1) = outs
+    assert np.array_equal(s0, s1)
+    assert (s0 == 0).mean() > 0.99
+    assert np.array_equal(p0, p1) and np.array_equal(c0, c1)
