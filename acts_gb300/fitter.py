@@ -108,7 +108,8 @@ class KalmanFitterOptions:
     energy_loss: bool = True
     reverse_filtering: bool = False
     free_to_bound_correction: bool = False
-    reference_surface: int = -1
+    reference_surface: int = -1  # a line (perigee) surface of the table, or -1
+    reference_strategy: int = abi.EXTRAPOLATE_FIRST_OR_LAST
     use_joseph: bool = False
     outlier_chi2_cut: float = float("inf")
     precision: int = abi.PRECISION_FP64
@@ -128,6 +129,7 @@ class KalmanFitterOptions:
         o.reverse_filtering = int(self.reverse_filtering)
         o.free_to_bound_correction = int(self.free_to_bound_correction)
         o.reference_surface = int(self.reference_surface)
+        o.reference_strategy = int(self.reference_strategy)
         o.use_joseph = int(self.use_joseph)
         o.outlier_chi2_cut = float(self.outlier_chi2_cut)
         o.precision = int(self.precision)

@@ -147,6 +147,11 @@ struct Track {
   size_t nStates = 0;
   size_t nMeasurements = 0, nHoles = 0, nOutliers = 0, nDoF = 0;
   double chi2 = 0;
+  // TrackProxy::referenceSurface / parameters / covariance: set when the
+  // options name a reference surface (the track extrapolated to it)
+  int referenceSurface = -1;
+  std::array<double, 6> parameters{};
+  std::array<double, 36> covariance{};  // row-major
 };
 
 struct TrackContainer {
@@ -254,10 +259,16 @@ class CudaKalman {
     std::vector<int32_t> status(n), nStates(n), nMeas(n), nHoles(n), nOut(n), ndf(n), surf(S);
     std::vector<uint32_t> flags(S);
     std::vector<double> chi2(n), path(S), schi2(S), pr(6 * S), prc(36 * S), fi(6 * S), fic(36 * S),
-        sm(6 * S), smc(36 * S), jac(36 * S);
+        sm(6 * S), smc(36 * S), jac(36 * S), tp(6 * n), tc(36 * n);
+    const bool ref = options.options.reference_surface >= 0;
     ck_batch_out out{};
     out.max_states = ms;
-    out.components = CK_OUT_PREDICTED | CK_OUT_FILTERED | CK_OUT_SMOOTHED | CK_OUT_JACOBIAN;
+    out.components = CK_OUT_PREDICTED | CK_OUT_FILTERED | CK_OUT_SMOOTHED | CK_OUT_JACOBIAN |
+                     (ref ? CK_OUT_REFERENCE : 0u);
+    if (ref) {
+      out.track_params = tp.data();
+      out.track_cov = tc.data();
+    }
     out.memory = CK_MEM_HOST;
     out.status = status.data();
     out.n_states = nStates.data();
@@ -297,6 +308,11 @@ class CudaKalman {
       tr.nOutliers = static_cast<size_t>(nOut[t]);
       tr.nDoF = static_cast<size_t>(ndf[t]);
       tr.chi2 = chi2[t];
+      if (ref) {
+        tr.referenceSurface = options.options.reference_surface;
+        for (size_t c = 0; c < 6; ++c) tr.parameters[c] = tp[c * n + t];
+        for (size_t c = 0; c < 36; ++c) tr.covariance[c] = tc[c * n + t];
+      }
       for (size_t k = 0; k < tr.nStates; ++k) {
         TrackState st;
         st.surface = surf[at(k, 1, 0, t)];
