@@ -578,6 +578,12 @@ ck_status ck_create(const ck_config* cfg, ck_handle** out) {
     }
     h->field.nodes = h->dNodes;
   }
+  for (int i = 0; i < 3; ++i) {
+    h->field.bf[i] = (float)h->field.b[i];
+    h->field.mnf[i] = (float)h->field.mn[i];
+    h->field.widthf[i] = (float)h->field.width[i];
+    h->field.upperf[i] = (float)h->field.upper[i];
+  }
   h->mc = makeMatConst();
   h->useGraph = cfg->use_graph;
   h->sortQueue = true;

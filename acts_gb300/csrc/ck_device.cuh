@@ -124,10 +124,67 @@ struct Surf {
   }
 };
 
+// ------------------------------------ FP64 <-> FP32 on the integer pipes
+// On GB300 a conversion between double and float issues to the FP64 unit
+// (one warp instruction holds it ~16 clocks, like an FP64 FMA), and the
+// mixed form converts a few thousand values per track between its FP64 free
+// state and its FP32 stages. d2f / f2d do the conversions with integer
+// instructions on the bit patterns: they give cvt.rn.f32.f64 /
+// cvt.f64.f32 results bit for bit for normal values and signed zero; other
+// inputs (subnormal results, overflow to inf, inf, nan) take the hardware
+// conversion.
+CK_D float d2f(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  if (e - 897u > 253u) {  // float exponent e - 896 outside [1, 254]
+    if (e == 0u && ((hi & 0xfffffu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
+    return __double2float_rn(x);
+  }
+  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // 23 mantissa bits
+  const unsigned r = lo & 0x1fffffffu;                      // 29 bits rounded off
+  unsigned f = (hi & 0x80000000u) | ((e - 896u) << 23) | m;
+  // to nearest, ties to even; a carry out of the mantissa is the correct
+  // next binade (or inf above the largest float)
+  f += (r > 0x10000000u || (r == 0x10000000u && (m & 1u))) ? 1u : 0u;
+  return __uint_as_float(f);
+}
+CK_D double f2d(float y) {
+  const unsigned u = __float_as_uint(y);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e - 1u > 253u) {  // zero, subnormal, inf or nan
+    if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    return (double)y;
+  }
+  const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+  return __hiloint2double((int)hi, (int)(u << 29));
+}
+// double -> P (the form's stage type) and P -> double. toP / toD are the
+// hardware conversions: in the forward filter the integer sequences (with
+// their branch for the rare operands) cost more than they save (measured:
+// the uneven workload's mixed filter 19.4 -> 23.6 ms), because they split the
+// straight-line code the scheduler interleaves. The smoother, whose
+// conversions sit between long FP64 sequences, uses the integer ones
+// (toPi / toDi; its kernel 4.17 -> 3.75 ms on 500k barrel tracks).
+template <typename P>
+CK_D P toP(double x) {
+  return (P)x;
+}
+CK_D double toD(float y) { return (double)y; }
+CK_D double toD(double y) { return y; }
+template <typename P>
+CK_D P toPi(double x) {
+  if constexpr (sizeof(P) == sizeof(float))
+    return d2f(x);
+  else
+    return x;
+}
+CK_D double toDi(float y) { return f2d(y); }
+CK_D double toDi(double y) { return y; }
+
 // ------------------------------------------- FP64 functions of the mixed form
 // 1/sqrt(v): FP32 estimate refined by one FP64 Newton step (~1e-14 relative).
 CK_D double rsqrtRefined(double v) {
-  const double y = (double)rsqrtf((float)v);
+  const double y = toD(rsqrtf(d2f(v)));
   return y * (1.5 - 0.5 * v * y * y);
 }
 
@@ -139,14 +196,14 @@ CK_D double rsqrtRefined(double v) {
 // t^11 (truncation below 1e-19 relative); result a_k + d, wrapped to [-pi, pi].
 // Agrees with a correctly rounded atan2 to a few ulp.
 CK_D double atan2Table(double y, double x, const double2* __restrict__ tab) {
-  const float f = atan2f((float)y, (float)x);
+  const float f = atan2f(d2f(y), d2f(x));
   int k = __float2int_rn(f * (float)(1.0 / kTrigStep));
   k = k < -64 ? -64 : (k > 64 ? 64 : k);
   const double2 cs = __ldg(&tab[k + 64]);
   const double xr = x * cs.x + y * cs.y;
   const double yr = y * cs.x - x * cs.y;
   if (!(xr > 0.0)) return (double)f;  // only for (x, y) = (0, 0)
-  double r = (double)(1.0f / (float)xr);
+  double r = toD(1.0f / d2f(xr));
   r = r * (2.0 - xr * r);
   double t = yr * r;
   t = t + r * (yr - xr * t);
@@ -236,8 +293,9 @@ CK_D int intersectMixed(const Surf<double>& s, const double pos[3], const double
     const double num =
         s.R[2] * (s.c[0] - pos[0]) + s.R[5] * (s.c[1] - pos[1]) + s.R[8] * (s.c[2] - pos[2]);
     // FP32 quotient refined by one FP64 residual step
-    const double p0 = (double)((float)num / (float)denom);
-    const double pl = p0 + (double)((float)(num - p0 * denom) / (float)denom);
+    const float denomf = d2f(denom);
+    const double p0 = toD(d2f(num) / denomf);
+    const double pl = p0 + toD(d2f(num - p0 * denom) / denomf);
     path[0] = pl;
     st[0] = statusOf(pl, tol);
     return 1;
@@ -250,7 +308,7 @@ CK_D int intersectMixed(const Surf<double>& s, const double pos[3], const double
   const double ad = lx0 * lx0 + lx1 * lx1 + lx2 * lx2;
   const double bd = 2.0 * (lx0 * px0 + lx1 * px1 + lx2 * px2);
   const double ccd = (px0 * px0 + px1 * px1 + px2 * px2) - s.radius * s.radius;
-  const float a = (float)ad, b = (float)bd, cc = (float)ccd;
+  const float a = d2f(ad), b = d2f(bd), cc = d2f(ccd);
   const float disc = b * b - 4.0f * a * cc;
   if (!(disc >= 0.0f)) {
     st[0] = st[1] = 0;
@@ -260,10 +318,10 @@ CK_D int intersectMixed(const Surf<double>& s, const double pos[3], const double
   const float sq = sqrtf(disc);
   const float q = -0.5f * (b + (b > 0.0f ? sq : -sq));
   auto refine = [&](float t0f) -> double {
-    const double t0 = (double)t0f;
+    const double t0 = toD(t0f);
     const double f = (ad * t0 + bd) * t0 + ccd;
     const double df = 2.0 * ad * t0 + bd;
-    return df != 0.0 ? t0 - (double)((float)f / (float)df) : t0;
+    return df != 0.0 ? t0 - toD(d2f(f) / d2f(df)) : t0;
   };
   const double first = refine(q / a);
   if (disc == 0.0f) {
@@ -472,12 +530,30 @@ CK_D bool getGridField(const DevField& F, const P p[3], P B[3]);
 template <typename P>
 CK_D bool getField(const DevField& F, const P p[3], P B[3]) {
   if (F.kind == CK_FIELD_CONSTANT) {
-    B[0] = (P)F.b[0];
-    B[1] = (P)F.b[1];
-    B[2] = (P)F.b[2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      if constexpr (sizeof(P) == sizeof(float))
+        B[i] = F.bf[i];
+      else
+        B[i] = F.b[i];
+    }
     return true;
   }
   return getGridField(F, p, B);
+}
+
+// the grid constants of the form's type (float copies for the FP32 form)
+template <typename P>
+CK_D void gridConstants(const DevField& F, int i, P& mn, P& width, P& upper) {
+  if constexpr (sizeof(P) == sizeof(float)) {
+    mn = F.mnf[i];
+    width = F.widthf[i];
+    upper = F.upperf[i];
+  } else {
+    mn = F.mn[i];
+    width = F.width[i];
+    upper = F.upper[i];
+  }
 }
 
 template <typename P>
@@ -488,13 +564,15 @@ CK_D bool getGridField(const DevField& F, const P p[3], P B[3]) {
   P f[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    if (p[i] < (P)F.mn[i] || p[i] >= (P)F.upper[i]) return false;
-    P u = (p[i] - (P)F.mn[i]) / (P)F.width[i];
+    P mn, width, upper;
+    gridConstants(F, i, mn, width, upper);
+    if (p[i] < mn || p[i] >= upper) return false;
+    P u = (p[i] - mn) / width;
     int bb = (int)floor(u);  // 0-based lower node
     bb = max(0, min(bb, F.n[i] - 2));
     bin[i] = bb;
-    P ll = (P)F.mn[i] + (P)bb * (P)F.width[i];
-    P ur = (P)F.mn[i] + (P)(bb + 1) * (P)F.width[i];
+    P ll = mn + (P)bb * width;
+    P ur = mn + (P)(bb + 1) * width;
     f[i] = (p[i] - ll) / (ur - ll);
   }
   const size_t nz = F.n[2], nyz = (size_t)F.n[1] * F.n[2];
@@ -650,9 +728,9 @@ struct Inv2 {
 // about an ulp; no FP64 divide). Falls back to the divide where d is outside
 // the FP32 range.
 CK_D double rcpRefined(double d) {
-  const float f = (float)d;
+  const float f = d2f(d);
   if (!(fabsf(f) > 1e-30f && fabsf(f) < 1e30f)) return 1.0 / d;
-  double y = (double)(1.0f / f);
+  double y = toD(1.0f / f);
   y = fma(y, fma(-d, y, 1.0), y);
   y = fma(y, fma(-d, y, 1.0), y);
   return y;
@@ -681,7 +759,7 @@ CK_D void inverse6(const T* __restrict__ Cp, double inv[36]) {
 #pragma unroll
   for (int i = 0; i < 6; ++i)
 #pragma unroll
-    for (int j = 0; j < 6; ++j) lu[i * 6 + j] = (double)Cp[sidx(i, j)];
+    for (int j = 0; j < 6; ++j) lu[i * 6 + j] = toDi(Cp[sidx(i, j)]);
   int perm[6] = {0, 1, 2, 3, 4, 5};
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
@@ -820,9 +898,12 @@ CK_D double predictedChi2(const double pred[6], const double Pp[21], double m0, 
 // visitMeasurementImpl<1>: a 1D measurement m (variance v) of bound
 // parameter h (0: loc0, 1: loc1), projector row e_h. S, the gain column and
 // the chi2 matrix are scalars (Eigen's 1x1 inverse is the reciprocal).
+// (out of line: strip measurements share a kernel with the 2D path, whose
+// register allocation they would otherwise raise)
 template <bool FASTRCP = false>
-CK_D bool kalmanUpdate1(const double pred[6], const double Pp[21], int h, double m, double v,
-                        bool joseph, double filt[6], double F[21], double& chi2) {
+__device__ __noinline__ bool kalmanUpdate1(const double pred[6], const double Pp[21], int h,
+                                           double m, double v, bool joseph, double filt[6],
+                                           double F[21], double& chi2) {
   double q[6];  // row h of Pp
 #pragma unroll
   for (int j = 0; j < 6; ++j) q[j] = h ? Pp[sidx(1, j)] : Pp[sidx(0, j)];
@@ -900,6 +981,9 @@ CK_D bool smoothStep(const double filt[6], const GP Pf[21], const double pp[6], 
       for (int k = 0; k < 6; ++k) s += Pf[sidx(i, k)] * J[j * 6 + k];
       PJ[i * 6 + j] = s;
     }
+  GP invg[36];
+#pragma unroll
+  for (int i = 0; i < 36; ++i) invg[i] = toPi<GP>(inv[i]);
   GP G[36];
   bool nan = false;
 #pragma unroll
@@ -908,7 +992,7 @@ CK_D bool smoothStep(const double filt[6], const GP Pf[21], const double pp[6], 
     for (int j = 0; j < 6; ++j) {
       GP s = GP(0);
 #pragma unroll
-      for (int k = 0; k < 6; ++k) s += PJ[i * 6 + k] * (GP)inv[k * 6 + j];
+      for (int k = 0; k < 6; ++k) s += PJ[i * 6 + k] * invg[k * 6 + j];
       G[i * 6 + j] = s;
       nan |= isnan(s);
     }
@@ -919,11 +1003,15 @@ CK_D bool smoothStep(const double filt[6], const GP Pf[21], const double pp[6], 
   d[2] = radian_sym(d[2]);
   d[3] = radian_sym(d[3]);
 #pragma unroll
+  GP dg[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) dg[k] = toPi<GP>(d[k]);
+#pragma unroll
   for (int i = 0; i < 6; ++i) {
     GP s = GP(0);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) s += G[i * 6 + k] * (GP)d[k];
-    sm[i] = filt[i] + (double)s;
+    for (int k = 0; k < 6; ++k) s += G[i * 6 + k] * dg[k];
+    sm[i] = filt[i] + toDi(s);
   }
   normalizePhiTheta(sm[2], sm[3]);
   // Ps = Pf + G (Psp - Ppp) G^T
@@ -989,7 +1077,7 @@ CK_D void mbfSmoothed(const double filt[6], const GP Pf[21], const GP L[21], con
   for (int i = 0; i < 6; ++i) {
     double s = 0.0;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) s += (double)((shared ? Ps : Pf)[sidx(i, k)] * l[k]);
+    for (int k = 0; k < 6; ++k) s += toDi((shared ? Ps : Pf)[sidx(i, k)] * l[k]);
     sm[i] = filt[i] - s;
   }
   normalizePhiTheta(sm[2], sm[3]);
@@ -1039,14 +1127,14 @@ template <typename GP>
 CK_D void mbfMeasurement(const double pred[6], const GP Pp[21], double m0, double m1,
                          const double V[4], GP L[21], GP l[6]) {
   constexpr bool kFast = sizeof(GP) == sizeof(float);
-  const Inv2 si = inverse2<kFast>((double)Pp[sidx(0, 0)] + V[0], (double)Pp[sidx(0, 1)] + V[1],
-                                  (double)Pp[sidx(1, 0)] + V[2], (double)Pp[sidx(1, 1)] + V[3]);
+  const Inv2 si = inverse2<kFast>(toDi(Pp[sidx(0, 0)]) + V[0], toDi(Pp[sidx(0, 1)]) + V[1],
+                                  toDi(Pp[sidx(1, 0)]) + V[2], toDi(Pp[sidx(1, 1)]) + V[3]);
   GP K[6][2];
 #pragma unroll
   for (int r = 0; r < 6; ++r) {
-    const double p0 = (double)Pp[sidx(r, 0)], p1 = (double)Pp[sidx(r, 1)];
-    K[r][0] = (GP)(p0 * si.a00 + p1 * si.a10);
-    K[r][1] = (GP)(p0 * si.a01 + p1 * si.a11);
+    const double p0 = toDi(Pp[sidx(r, 0)]), p1 = toDi(Pp[sidx(r, 1)]);
+    K[r][0] = toPi<GP>(p0 * si.a00 + p1 * si.a10);
+    K[r][1] = toPi<GP>(p0 * si.a01 + p1 * si.a11);
   }
   // A = Lambda C: columns 0 and 1 are Lambda[:,c] - Lambda K[:,c]
   GP A[6][6];
@@ -1079,9 +1167,9 @@ CK_D void mbfMeasurement(const double pred[6], const GP Pp[21], double m0, doubl
       }
       Lt[sidx(i, j)] = v;
     }
-  Lt[sidx(0, 0)] += (GP)si.a00;
-  Lt[sidx(0, 1)] += (GP)(0.5 * (si.a01 + si.a10));
-  Lt[sidx(1, 1)] += (GP)si.a11;
+  Lt[sidx(0, 0)] += toPi<GP>(si.a00);
+  Lt[sidx(0, 1)] += toPi<GP>(0.5 * (si.a01 + si.a10));
+  Lt[sidx(1, 1)] += toPi<GP>(si.a11);
   // lambda~ = C^T lambda - H^T S^-1 y
   const double y0 = m0 - pred[0], y1 = m1 - pred[1];
   GP lt[6];
@@ -1094,8 +1182,8 @@ CK_D void mbfMeasurement(const double pred[6], const GP Pp[21], double m0, doubl
     for (int r = 0; r < 6; ++r) s += K[r][c] * l[r];
     lt[c] -= s;
   }
-  lt[0] -= (GP)(si.a00 * y0 + si.a01 * y1);
-  lt[1] -= (GP)(si.a10 * y0 + si.a11 * y1);
+  lt[0] -= toPi<GP>(si.a00 * y0 + si.a01 * y1);
+  lt[1] -= toPi<GP>(si.a10 * y0 + si.a11 * y1);
 #pragma unroll
   for (int i = 0; i < 21; ++i) L[i] = Lt[i];
 #pragma unroll
@@ -1108,11 +1196,11 @@ template <typename GP>
 CK_D void mbfMeasurement1(const double pred[6], const GP Pp[21], int h, double m, double v,
                           GP L[21], GP l[6]) {
   constexpr bool kFast = sizeof(GP) == sizeof(float);
-  const double S = (double)(h ? Pp[sidx(1, 1)] : Pp[sidx(0, 0)]) + v;
+  const double S = toDi(h ? Pp[sidx(1, 1)] : Pp[sidx(0, 0)]) + v;
   const double iS = kFast ? rcpRefined(S) : 1.0 / S;
   GP K[6];
 #pragma unroll
-  for (int r = 0; r < 6; ++r) K[r] = (GP)((double)(h ? Pp[sidx(r, 1)] : Pp[sidx(r, 0)]) * iS);
+  for (int r = 0; r < 6; ++r) K[r] = toPi<GP>(toDi(h ? Pp[sidx(r, 1)] : Pp[sidx(r, 0)]) * iS);
   // A = Lambda C: column h is Lambda[:,h] - Lambda K
   GP A[6][6];
 #pragma unroll
@@ -1145,15 +1233,15 @@ CK_D void mbfMeasurement1(const double pred[6], const GP Pp[21], int h, double m
       Lt[sidx(i, j)] = val;
     }
   if (h)
-    Lt[sidx(1, 1)] += (GP)iS;
+    Lt[sidx(1, 1)] += toPi<GP>(iS);
   else
-    Lt[sidx(0, 0)] += (GP)iS;
+    Lt[sidx(0, 0)] += toPi<GP>(iS);
   // lambda~ = C^T lambda - e_h (y / S), y = m - pred_h
   const double y = m - (h ? pred[1] : pred[0]);
   GP s = GP(0);
 #pragma unroll
   for (int r = 0; r < 6; ++r) s += K[r] * l[r];
-  const GP upd = s + (GP)(iS * y);
+  const GP upd = s + toPi<GP>(iS * y);
   if (h)
     l[1] -= upd;
   else

@@ -49,7 +49,11 @@ enum Phase { PH_FETCH = 0, PH_STEP = 1, PH_SURFACE = 2, PH_DONE = 3 };
 // ChargeHypothesis::extractMomentum (ChargeHypothesis.hpp:70-90)
 template <typename P>
 CK_D P absMomentum(float absQ, P qop) {
-  float q = (float)copysign((double)absQ, (double)qop);
+  float q;
+  if constexpr (sizeof(P) == sizeof(float))
+    q = copysignf(absQ, qop);  // the same value without a double round trip
+  else
+    q = (float)copysign((double)absQ, (double)qop);
   return (P)q / qop;
 }
 
@@ -291,7 +295,7 @@ struct Lane {
       };
       // 1/sqrt(v) for v near a known scale: FP32 estimate, one FP64 Newton step
       auto rsq = [](double v) {
-        const double y = (double)rsqrtf((float)v);
+        const double y = toD(rsqrtf(d2f(v)));
         return y * (1.5 - 0.5 * v * y * y);
       };
       // direction
@@ -340,8 +344,9 @@ struct Lane {
     initTP(sf);
   }
   CK_D void initTP(const Surf<P>& sf) {
-    const P p[3] = {(P)pos[0], (P)pos[1], (P)pos[2]};
-    const P f[8] = {p[0], p[1], p[2], (P)tim, (P)dir[0], (P)dir[1], (P)dir[2], (P)qop};
+    const P p[3] = {toP<P>(pos[0]), toP<P>(pos[1]), toP<P>(pos[2])};
+    const P f[8] = {p[0],           p[1],           p[2],           toP<P>(tim),
+                    toP<P>(dir[0]), toP<P>(dir[1]), toP<P>(dir[2]), toP<P>(qop)};
     initTransport(sf, f, T);
   }
 
@@ -422,12 +427,12 @@ struct Lane {
                       const double l[3], int mode) {
     const DevSurface* ds = fp.surfaces + sid;
     if (!(__ldg(&ds->flags) & CK_SURF_MATERIAL)) return true;
-    const P d[3] = {(P)dir[0], (P)dir[1], (P)dir[2]};
+    const P d[3] = {toP<P>(dir[0]), toP<P>(dir[1]), toP<P>(dir[2])};
     P pc;
     if (sfd.type == CK_SURFACE_PLANE) {
       pc = P(1) / fabs(sp.R[2] * d[0] + sp.R[5] * d[1] + sp.R[8] * d[2]);
     } else {
-      const P l0 = (P)l[0], l1 = (P)l[1];
+      const P l0 = toP<P>(l[0]), l1 = toP<P>(l[1]);
       P n0 = l0, n1 = l1;
       const P n2 = l0 * l0 + l1 * l1;
       if (n2 > P(0)) {
@@ -449,12 +454,12 @@ struct Lane {
       f1 = (float)factor;
     }
     bool vac = false;
-    const float qOverPf = (float)qop;
+    const float qOverPf = d2f(qop);
     const MatEffects e = materialEffects<P>(fp.mc, ds, f1, (float)pc, pdg, mass, absQ, d,
                                             qOverPf, fp.opt.multipleScattering != 0,
                                             fp.opt.energyLoss != 0, vac);
     if (vac) return true;
-    const float signedQ = (float)copysign((double)absQ, (double)qOverPf);
+    const float signedQ = copysignf(absQ, qOverPf);
     if constexpr (sizeof(P) == sizeof(double)) {
       // PointwiseMaterialInteraction::updateState (hpp:188-198) in FP64
       const double massd = (double)mass;
@@ -472,7 +477,7 @@ struct Lane {
       // = -eLoss (2E - eLoss) / p^2, q/p scales by 1/sqrt(1 + u); the small
       // correction is formed in FP32 and applied to the FP64 q/p
       const float m = mass;
-      const float p = fabsf(signedQ / (float)qop);
+      const float p = fabsf(signedQ / d2f(qop));
       const float E = sqrtf(m * m + p * p);
       const float eLoss = (float)e.eLoss;
       const float nextE = E - eLoss;
@@ -480,7 +485,7 @@ struct Lane {
         const float u = -eLoss * (2.0f * E - eLoss) / (p * p);
         const float r = sqrtf(1.0f + u);
         const float delta = u / (r * (1.0f + r));  // 1/sqrt(1+u) - 1 = -u/(r(1+r))
-        qop = qop - qop * (double)delta;
+        qop = qop - qop * toD(delta);
       } else {
         qop = (double)signedQ / 0.01;  // nextP clamped to 10 MeV
       }
@@ -498,10 +503,10 @@ struct Lane {
   // (CovarianceEngine.cpp:102-165). J is returned for the record.
   CK_NI void transportToBound(const Surf<double>& sfd, const Surf<P>& sf, const double l[3],
                               CV Jout[36]) {
-    const P p[3] = {(P)pos[0], (P)pos[1], (P)pos[2]};
+    const P p[3] = {toP<P>(pos[0]), toP<P>(pos[1]), toP<P>(pos[2])};
     P ex[3], ey[3], ez[3];
     referenceFrame(sf, p, ex, ey, ez);
-    const P dir[3] = {(P)this->dir[0], (P)this->dir[1], (P)this->dir[2]};
+    const P dir[3] = {toP<P>(this->dir[0]), toP<P>(this->dir[1]), toP<P>(this->dir[2])};
     const P dz = ez[0] * dir[0] + ez[1] * dir[1] + ez[2] * dir[2];
     const P idz = P(-1) / dz;
     const P f0 = ez[0] * idz, f1 = ez[1] * idz, f2 = ez[2] * idz;
@@ -626,7 +631,7 @@ struct Lane {
       const int k = nStates++;
       double Pp[21];
 #pragma unroll
-      for (int i = 0; i < 21; ++i) Pp[i] = (double)cov[i];
+      for (int i = 0; i < 21; ++i) Pp[i] = toD(cov[i]);
 #pragma unroll
       for (int i = 0; i < 6; ++i) rec.p(k, kRecPred + i) = bp[i];
 #pragma unroll
@@ -662,7 +667,7 @@ struct Lane {
         updateFree(sf, bp, filt, l);
 #pragma unroll
         for (int i = 0; i < 21; ++i) {
-          cov[i] = (CV)F[i];
+          cov[i] = toP<CV>(F[i]);
           rec.m(k, kRecFiltCov + i) = cov[i];
         }
         initTP(sp);
@@ -793,7 +798,7 @@ struct Lane {
 #pragma unroll
       for (int i = 0; i < 6; ++i)
 #pragma unroll
-        for (int j = i; j < 6; ++j) cov[sidx(i, j)] = (CV)__ldg(&sc[i * 6 + j]);
+        for (int j = i; j < 6; ++j) cov[sidx(i, j)] = toP<CV>(__ldg(&sc[i * 6 + j]));
     }
 #pragma unroll
     for (int i = 0; i < 7; ++i) deriv[i] = P(0);
@@ -856,6 +861,10 @@ struct Lane {
   }
 
   // STEP: one Runge-Kutta trial (EigenStepper::step, EigenStepper.ipp:168-388)
+  // EXTRAP: the lane extrapolates to the reference surface (signed step
+  // direction, the aborters after each step); the fit kernels instantiate
+  // the forward-only step without that code
+  template <bool EXTRAP = false>
   CK_D void step(const FitParams& fp, int slot) {
     const DevOptions& o = fp.opt;
     if (!stepStarted) {
@@ -863,15 +872,16 @@ struct Lane {
         fail(fp, CK_TRACK_STEP_COUNT_LIMIT);
         return;
       }
-      initialH = stepValue() * dirSign;  // EigenStepper.ipp:272
+      initialH = stepValue();
+      if constexpr (EXTRAP) initialH *= dirSign;  // EigenStepper.ipp:272
       hd = initialH;
       trials = 0;
       stepStarted = true;
     }
     ++trials;
-    const P pp[3] = {(P)pos[0], (P)pos[1], (P)pos[2]};
-    const P dir[3] = {(P)this->dir[0], (P)this->dir[1], (P)this->dir[2]};
-    const P qop = (P)this->qop;
+    const P pp[3] = {toP<P>(pos[0]), toP<P>(pos[1]), toP<P>(pos[2])};
+    const P dir[3] = {toP<P>(this->dir[0]), toP<P>(this->dir[1]), toP<P>(this->dir[2])};
+    const P qop = toP<P>(this->qop);
     P B1[3], B2[3], B3[3];
     if (!getField(fp.field, pp, B1)) {
       fail(fp, CK_TRACK_FIELD_OUT_OF_BOUNDS);
@@ -881,8 +891,8 @@ struct Lane {
     k1[0] = qop * (dir[1] * B1[2] - dir[2] * B1[1]);
     k1[1] = qop * (dir[2] * B1[0] - dir[0] * B1[2]);
     k1[2] = qop * (dir[0] * B1[1] - dir[1] * B1[0]);
-    const P tol = (P)o.stepTolerance;
-    const P h = (P)hd;
+    const P tol = toP<P>(o.stepTolerance);
+    const P h = toP<P>(hd);
     const P h2 = h * h;
     const P hh = h * P(0.5);
     P p1[3], tt[3];
@@ -920,7 +930,7 @@ struct Lane {
     P x = sqrt(sqrt(tol / err));
     x = fmin(fmax(x, P(0.25)), P(4));
     if (!(err <= P(4) * tol)) {
-      hd = hd * (double)x;
+      hd = hd * toD(x);
       if (fabs(hd) < fabs(o.stepSizeCutOff)) {
         fail(fp, CK_TRACK_STEP_SIZE_STALLED);
         return;
@@ -933,7 +943,7 @@ struct Lane {
     const P pm = absMomentum(absQ, qop);
     const P mp = m / pm;
     const P dtds = sqrt(P(1) + mp * mp);
-    tim = tim + (double)(h * dtds);
+    tim = tim + toD(h * dtds);
     if (!coasting) {
       deriv[3] = dtds;
       P dk1dL[3], dk2dL[3], dk3dL[3], dk4dL[3];
@@ -1026,8 +1036,8 @@ struct Lane {
       const P h6 = h * P(1.0 / 6.0);
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
-        pos[i] = pos[i] + (hd * this->dir[i] + (double)(hh6 * ((k1[i] + k2[i]) + k3[i])));
-        this->dir[i] = this->dir[i] + (double)(h6 * ((k1[i] + P(2) * (k2[i] + k3[i])) + k4[i]));
+        pos[i] = pos[i] + (hd * this->dir[i] + toD(hh6 * ((k1[i] + k2[i]) + k3[i])));
+        this->dir[i] = this->dir[i] + toD(h6 * ((k1[i] + P(2) * (k2[i] + k3[i])) + k4[i]));
       }
       double* nd = this->dir;
       const double n2 = nd[0] * nd[0] + nd[1] * nd[1] + nd[2] * nd[2];
@@ -1035,7 +1045,7 @@ struct Lane {
       if constexpr (sizeof(P) == sizeof(float)) {
         // |dir|^2 is within a few 1e-3 of 1: an FP32 reciprocal square root
         // and one Newton step in FP64 give ~1e-14 relative accuracy
-        const double y0 = (double)rsqrtf((float)n2);
+        const double y0 = toD(rsqrtf(d2f(n2)));
         inv = y0 * (1.5 - 0.5 * n2 * y0 * y0);
       } else {
         inv = 1.0 / sqrt(n2);
@@ -1045,22 +1055,22 @@ struct Lane {
       nd[2] = nd[2] * inv;
     }
     if (!coasting) {
-      deriv[0] = (P)this->dir[0];
-      deriv[1] = (P)this->dir[1];
-      deriv[2] = (P)this->dir[2];
+      deriv[0] = toP<P>(this->dir[0]);
+      deriv[1] = toP<P>(this->dir[1]);
+      deriv[2] = toP<P>(this->dir[2]);
       deriv[4] = k4[0];
       deriv[5] = k4[1];
       deriv[6] = k4[2];
     }
     pathAcc += hd;
-    const double nextAcc = fabs(hd * (double)x);
+    const double nextAcc = fabs(hd * toD(x));
     if (nextAcc < fabs(initialH) || nextAcc > fabs(cAcc)) cAcc = nextAcc;
     stepStarted = false;
     ++steps;
     // post-step navigation (Propagator.ipp:113-141)
     cNav = kNotSet;
     cActor = kNotSet;
-    if (extrapolating) {
+    if constexpr (EXTRAP) {
       // no navigation target and no actors; the aborters decide
       if (extrapolationAbort(fp)) finishExtrapolation(fp);
       return;
@@ -1475,7 +1485,7 @@ struct Smoother {
       for (int i = 0; i < 6; ++i)
 #pragma unroll
         for (int j = i; j < 6; ++j) {
-          const double v = (double)Ps[sidx(i, j)];
+          const double v = toDi(Ps[sidx(i, j)]);
           out.smoothed_cov[at(36, i * 6 + j)] = v;
           if (j != i) out.smoothed_cov[at(36, j * 6 + i)] = v;
         }

@@ -40,6 +40,9 @@ struct DevField {
   double mn[3];     // first grid point
   double width[3];  // bin width of the reference axis
   double upper[3];  // lower edge of the last bin (end of the valid range)
+  // the same constants rounded to float (host conversion, round to
+  // nearest) for the mixed form's FP32 lookups
+  float bf[3], mnf[3], widthf[3], upperf[3];
   const float4* nodes;
 };
 
