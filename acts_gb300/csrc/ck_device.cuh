@@ -895,66 +895,100 @@ CK_D double predictedChi2(const double pred[6], const double Pp[21], double m0, 
   return t0 * r0 + t1 * r1;
 }
 
-// visitMeasurementImpl<1>: a 1D measurement m (variance v) of bound
-// parameter h (0: loc0, 1: loc1), projector row e_h. S, the gain column and
-// the chi2 matrix are scalars (Eigen's 1x1 inverse is the reciprocal).
-// (out of line: strip measurements share a kernel with the 2D path, whose
-// register allocation they would otherwise raise)
+// visitMeasurementImpl<N> for N = 2 (sub = CK_MEAS_LOC01: values m0, m1,
+// covariance V) and N = 1 (sub = CK_MEAS_LOC0 / LOC1: value m0, variance
+// V[0] of bound parameter a = sub >> 1) in one code path: the 1D case runs
+// the 2x2 algebra with its second row switched off (S = diag(S_aa, 1), the
+// second gain column and residual zero), which reduces exactly to the scalar
+// formulas, so strip and pixel measurements share the kernel's registers.
+// The 2D case evaluates the same expressions as kalmanUpdate.
 template <bool FASTRCP = false>
-__device__ __noinline__ bool kalmanUpdate1(const double pred[6], const double Pp[21], int h,
-                                           double m, double v, bool joseph, double filt[6],
-                                           double F[21], double& chi2) {
-  double q[6];  // row h of Pp
+CK_D bool kalmanUpdateSub(const double pred[6], const double Pp[21], int sub, double m0, double m1,
+                          const double Vin[4], bool joseph, double filt[6], double F[21],
+                          double& chi2) {
+  const bool two = sub == CK_MEAS_LOC01;
+  const bool a1 = sub == CK_MEAS_LOC1;  // the (first) measured parameter is loc1
+  const double V0 = Vin[0], V1 = two ? Vin[1] : 0.0, V2 = two ? Vin[2] : 0.0,
+               V3 = two ? Vin[3] : 0.0;
+  double ra[6], r1[6];  // row a and row 1 of Pp
 #pragma unroll
-  for (int j = 0; j < 6; ++j) q[j] = h ? Pp[sidx(1, j)] : Pp[sidx(0, j)];
-  const double S = (h ? q[1] : q[0]) + v;
-  const double iS = FASTRCP ? rcpRefined(S) : 1.0 / S;
-  double K[6];
+  for (int j = 0; j < 6; ++j) {
+    r1[j] = Pp[sidx(1, j)];
+    ra[j] = a1 ? r1[j] : Pp[sidx(0, j)];
+  }
+  const double saa = (a1 ? ra[1] : ra[0]) + V0;
+  Inv2 Si = inverse2<FASTRCP>(saa, two ? ra[1] + V1 : 0.0, two ? r1[0] + V2 : 0.0,
+                              two ? r1[1] + V3 : 1.0);
+  double K[6][2];
   bool nan = false;
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
-    K[i] = q[i] * iS;
-    nan |= isnan(K[i]);
+    const double pa = a1 ? Pp[sidx(i, 1)] : Pp[sidx(i, 0)], p1 = Pp[sidx(i, 1)];
+    K[i][0] = pa * Si.a00 + p1 * Si.a10;
+    K[i][1] = two ? pa * Si.a01 + p1 * Si.a11 : 0.0;
+    nan |= isnan(K[i][0]) || isnan(K[i][1]);
   }
   if (nan) return false;
-  const double r = m - (h ? pred[1] : pred[0]);
+  const double r0 = m0 - (a1 ? pred[1] : pred[0]);
+  const double rr1 = two ? m1 - pred[1] : 0.0;
 #pragma unroll
-  for (int i = 0; i < 6; ++i) filt[i] = pred[i] + K[i] * r;
+  for (int i = 0; i < 6; ++i) filt[i] = pred[i] + (K[i][0] * r0 + K[i][1] * rr1);
   normalizePhiTheta(filt[2], filt[3]);
+  // A P with A = I - K H : (AP)_ij = P_ij - K_i0 P_aj - K_i1 P_1j
   if (!joseph) {
 #pragma unroll
     for (int i = 0; i < 6; ++i)
 #pragma unroll
-      for (int j = i; j < 6; ++j) F[sidx(i, j)] = Pp[sidx(i, j)] - K[i] * q[j];
+      for (int j = i; j < 6; ++j)
+        F[sidx(i, j)] = Pp[sidx(i, j)] - (K[i][0] * ra[j] + K[i][1] * r1[j]);
   } else {
     double AP[6][6];
 #pragma unroll
     for (int i = 0; i < 6; ++i)
 #pragma unroll
-      for (int j = 0; j < 6; ++j) AP[i][j] = Pp[sidx(i, j)] - K[i] * q[j];
+      for (int j = 0; j < 6; ++j)
+        AP[i][j] = Pp[sidx(i, j)] - (K[i][0] * ra[j] + K[i][1] * r1[j]);
+    // (AP) A^T + K V K^T
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
-      const double aph = h ? AP[i][1] : AP[i][0];
-      const double kv = K[i] * v;
+      const double kv0 = K[i][0] * V0 + K[i][1] * V2;
+      const double kv1 = K[i][0] * V1 + K[i][1] * V3;
+      const double apa = a1 ? AP[i][1] : AP[i][0];
 #pragma unroll
-      for (int j = i; j < 6; ++j) F[sidx(i, j)] = (AP[i][j] - aph * K[j]) + kv * K[j];
+      for (int j = i; j < 6; ++j) {
+        const double apat = AP[i][j] - (apa * K[j][0] + AP[i][1] * K[j][1]);
+        F[sidx(i, j)] = apat + (kv0 * K[j][0] + kv1 * K[j][1]);
+      }
     }
   }
-  const double s = m - (h ? filt[1] : filt[0]);
-  const double mm = (1.0 - (h ? K[1] : K[0])) * v;
-  const double im = FASTRCP ? rcpRefined(mm) : 1.0 / mm;
-  chi2 = (s * im) * s;
+  // chi2 = r^T [(I - H K) V]^-1 r with r = m - H filt
+  const double s0 = m0 - (a1 ? filt[1] : filt[0]);
+  const double s1 = two ? m1 - filt[1] : 0.0;
+  const double ka0 = a1 ? K[1][0] : K[0][0], ka1 = a1 ? K[1][1] : K[0][1];
+  const double b00 = 1.0 - ka0, b01 = -ka1, b10 = -K[1][0], b11 = 1.0 - K[1][1];
+  Inv2 Mi = inverse2<FASTRCP>(b00 * V0 + b01 * V2, two ? b00 * V1 + b01 * V3 : 0.0,
+                              two ? b10 * V0 + b11 * V2 : 0.0, two ? b10 * V1 + b11 * V3 : 1.0);
+  const double t0 = s0 * Mi.a00 + s1 * Mi.a10;
+  const double t1 = s0 * Mi.a01 + s1 * Mi.a11;
+  chi2 = t0 * s0 + t1 * s1;
   return true;
 }
 
-// calculatePredictedChi2 of a 1D measurement of bound parameter h
+// calculatePredictedChi2 for either subspace (as kalmanUpdateSub)
 template <bool FASTRCP = false>
-CK_D double predictedChi2_1(const double pred[6], const double Pp[21], int h, double m,
-                            double v) {
-  const double r = m - (h ? pred[1] : pred[0]);
-  const double R = v + (h ? Pp[sidx(1, 1)] : Pp[sidx(0, 0)]);
-  const double iR = FASTRCP ? rcpRefined(R) : 1.0 / R;
-  return (r * iR) * r;
+CK_D double predictedChi2Sub(const double pred[6], const double Pp[21], int sub, double m0,
+                             double m1, const double Vin[4]) {
+  const bool two = sub == CK_MEAS_LOC01;
+  const bool a1 = sub == CK_MEAS_LOC1;
+  const double r0 = m0 - (a1 ? pred[1] : pred[0]);
+  const double r1 = two ? m1 - pred[1] : 0.0;
+  Inv2 Ri = inverse2<FASTRCP>(Vin[0] + (a1 ? Pp[sidx(1, 1)] : Pp[sidx(0, 0)]),
+                              two ? Vin[1] + Pp[sidx(0, 1)] : 0.0,
+                              two ? Vin[2] + Pp[sidx(1, 0)] : 0.0,
+                              two ? Vin[3] + Pp[sidx(1, 1)] : 1.0);
+  const double t0 = r0 * Ri.a00 + r1 * Ri.a10;
+  const double t1 = r0 * Ri.a01 + r1 * Ri.a11;
+  return t0 * r0 + t1 * r1;
 }
 
 // ---------------------------------------------------------------- smoother

@@ -646,20 +646,16 @@ struct Lane {
       for (int i = 0; i < 4; ++i) V[i] = __ldg(&fp.meas_cov[4 * (size_t)mi + i]);
       // (loc0, loc1), or a 1D measurement of loc h (value mv0, variance V[0])
       const int sub = fp.meas_sub ? __ldg(&fp.meas_sub[mi]) : CK_MEAS_LOC01;
-      const bool twoD = sub == CK_MEAS_LOC01;
-      const int h = sub >> 1;
       flags |= (uint32_t)sub << kRecSubShift;
       bool outlier = false;
       constexpr bool kFastRcp = sizeof(P) == sizeof(float);
       if (fp.opt.useOutlierCut)
-        outlier = (twoD ? predictedChi2<kFastRcp>(bp, Pp, mv0, mv1, V)
-                        : predictedChi2_1<kFastRcp>(bp, Pp, h, mv0, V[0])) > fp.opt.outlierChi2Cut;
+        outlier = predictedChi2Sub<kFastRcp>(bp, Pp, sub, mv0, mv1, V) > fp.opt.outlierChi2Cut;
       double chi2 = 0.0;
       if (!outlier) {
         double filt[6], F[21];
         const bool joseph = fp.opt.joseph != 0;
-        if (!(twoD ? kalmanUpdate<kFastRcp>(bp, Pp, mv0, mv1, V, joseph, filt, F, chi2)
-                   : kalmanUpdate1<kFastRcp>(bp, Pp, h, mv0, V[0], joseph, filt, F, chi2)))
+        if (!kalmanUpdateSub<kFastRcp>(bp, Pp, sub, mv0, mv1, V, joseph, filt, F, chi2))
           return CK_TRACK_UPDATE_FAILED;
         flags |= CK_FLAG_HAS_MEASUREMENT;
 #pragma unroll

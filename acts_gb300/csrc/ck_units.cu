@@ -29,9 +29,7 @@ __global__ void updateKernel(int n, int joseph, const double* __restrict__ pred,
   for (int k = 0; k < 4; ++k) V[k] = measCov[4 * i + k];
   const int s = sub ? sub[i] : CK_MEAS_LOC01;
   const bool ok =
-      s == CK_MEAS_LOC01
-          ? kalmanUpdate(p, P, meas[2 * i], meas[2 * i + 1], V, joseph != 0, f, F, c2)
-          : kalmanUpdate1(p, P, s >> 1, meas[2 * i], V[0], joseph != 0, f, F, c2);
+      kalmanUpdateSub(p, P, s, meas[2 * i], meas[2 * i + 1], V, joseph != 0, f, F, c2);
   status[i] = ok ? CK_TRACK_OK : CK_TRACK_UPDATE_FAILED;
   if (!ok) return;
   for (int k = 0; k < 6; ++k) filt[6 * i + k] = f[k];
