@@ -117,6 +117,7 @@ DevOptions toDevOptions(const ck_options& o) {
   d.useOutlierCut = std::isinf(o.outlier_chi2_cut) ? 0 : 1;
   d.earlyTermination = o.early_termination;
   d.smoother = o.smoother;
+  d.freeToBoundCorrection = o.free_to_bound_correction;
   return d;
 }
 
@@ -124,8 +125,6 @@ ck_status validateOptions(const ck_options* o) {
   if (!o) return fail(CK_ERR_INVALID_ARGUMENT, "options is NULL");
   if (o->reverse_filtering)
     return fail(CK_ERR_UNSUPPORTED, "reverse filtering is not in the declared extension set");
-  if (o->free_to_bound_correction)
-    return fail(CK_ERR_UNSUPPORTED, "free-to-bound correction is not supported");
   if (o->reference_surface < -1)
     return fail(CK_ERR_INVALID_ARGUMENT, "reference_surface must be -1 or a surface index");
   if (o->reference_strategy < CK_EXTRAPOLATE_FIRST ||
@@ -354,8 +353,12 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
   fp.ticket = dTicket;
   fp.rec = c.rec.p;
   fp.tip = (int32_t*)c.tip.p;
+  // the free-to-bound correction's kernel: 256 slots, one block per SM
+  const bool f2b = opt.free_to_bound_correction != 0;
+  const int fitGrid = f2b ? h->smCount : grid;
+  const int fitTpb = f2b ? 256 : tn.tpb;
   {
-    const long long warps = (long long)grid * (tn.tpb / 32);
+    const long long warps = (long long)fitGrid * (fitTpb / 32);
     const long long per = warps > 0 ? (n + warps - 1) / warps : 32;
     fp.lanes_per_warp = (int)std::min<long long>(32, std::max<long long>(1, per));
   }
@@ -388,7 +391,7 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
     cudaEventRecordWithFlags(h->ev0, st, recFlags);
   }
   if (n > 0) {
-    e = launchFit(fp, opt.precision, tn, grid, st);
+    e = launchFit(fp, opt.precision, tn, fitGrid, st);
     if (e != cudaSuccess) return cudaFail(e, "fit kernel launch");
     ++launches;
     if (timed) cudaEventRecordWithFlags(h->evMid, st, recFlags);

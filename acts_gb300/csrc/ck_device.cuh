@@ -991,6 +991,143 @@ CK_D double predictedChi2Sub(const double pred[6], const double Pp[21], int sub,
   return t0 * r0 + t1 * r1;
 }
 
+// ------------------------------------------------ free-to-bound correction
+// Eigen decomposition of a symmetric 8x8 matrix (row-major A) by cyclic
+// Jacobi rotations: A ends with the eigenvalues on its diagonal, V holds the
+// eigenvectors in its columns. For the positive semi-definite free
+// covariance this is the SVD U S U^T the reference takes (JacobiSVD).
+static __device__ __noinline__ void jacobiEigen8(double* A, double* V) {
+  for (int i = 0; i < 64; ++i) V[i] = (i % 9 == 0) ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0, diag = 0.0;
+    for (int p = 0; p < 8; ++p) {
+      diag += A[p * 9] * A[p * 9];
+      for (int q = p + 1; q < 8; ++q) off += A[p * 8 + q] * A[p * 8 + q];
+    }
+    if (!(off > 1e-60 * diag)) break;
+    for (int p = 0; p < 7; ++p)
+      for (int q = p + 1; q < 8; ++q) {
+        const double apq = A[p * 8 + q];
+        if (apq == 0.0) continue;
+        const double theta = (A[q * 9] - A[p * 9]) / (2.0 * apq);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < 8; ++k) {
+          const double akp = A[k * 8 + p], akq = A[k * 8 + q];
+          A[k * 8 + p] = c * akp - sn * akq;
+          A[k * 8 + q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < 8; ++k) {
+          const double apk = A[p * 8 + k], aqk = A[q * 8 + k];
+          A[p * 8 + k] = c * apk - sn * aqk;
+          A[q * 8 + k] = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < 8; ++k) {
+          const double vkp = V[k * 8 + p], vkq = V[k * 8 + q];
+          V[k * 8 + p] = c * vkp - sn * vkq;
+          V[k * 8 + q] = sn * vkp + c * vkq;
+        }
+      }
+  }
+}
+
+// detail::CorrectedFreeToBoundTransformer::operator()
+// (Core/src/EventData/CorrectedTransformationFreeToBound.cpp:51-183) with the
+// FreeToBoundCorrection defaults (alpha 0.1, beta 2, incidence window
+// [1e-5, 0.99500417]): the unscented transform of the free covariance C
+// (row-major 8x8, destroyed) through free-to-bound, each shifted sigma point
+// re-intersected with the surface along its direction. False when no
+// correction applies. FP64 in both forms; out of line (it runs only with the
+// option on, and is heavy).
+static __device__ __noinline__ bool correctedFreeToBound(const Surf<double>& s, const double* f,
+                                                         double* C, double* mean, double* cov) {
+  const double alpha = 0.1, beta = 2.0;
+  const double pos[3] = {f[0], f[1], f[2]}, dir[3] = {f[4], f[5], f[6]};
+  double ex[3], ey[3], ez[3];
+  referenceFrame(s, pos, ex, ey, ez);
+  const double absCos = fabs(dir[0] * ez[0] + dir[1] * ez[1] + dir[2] * ez[2]);
+  if (absCos < 1e-5 || absCos > 0.99500417) return false;
+  double U[64];
+  jacobiEigen8(C, U);
+  const double kappa = alpha * alpha * 8.0, lambda = kappa - 8.0, gamma = sqrt(kappa);
+  double b0[6];
+  if (!freeToBound(f, s, b0)) return false;
+  double b[17][6];
+  for (int r = 0; r < 6; ++r) b[0][r] = b0[r];
+  for (int i = 0; i < 8; ++i) {
+    const double sq = C[i * 9] > 0.0 ? sqrt(C[i * 9]) : 0.0;  // covSqrt = U sqrt(S)
+    for (int sg = 0; sg < 2; ++sg) {
+      double p[8];
+      for (int r = 0; r < 8; ++r) {
+        const double dlt = (U[r * 8 + i] * sq) * gamma;
+        p[r] = sg == 0 ? f[r] + dlt : f[r] - dlt;
+      }
+      const double pp[3] = {p[0], p[1], p[2]}, pd[3] = {p[4], p[5], p[6]};
+      double path[2];
+      int st[2];
+      const int n = intersect(s, pp, pd, kOnSurfaceTolerance, path, st);
+      int best = -1;
+      for (int j = 0; j < n; ++j) {
+        if (st[j] == 0) continue;
+        if (best < 0 || fabs(path[j]) < fabs(path[best])) best = j;
+      }
+      if (best < 0) return false;
+      for (int r = 0; r < 3; ++r) p[r] = pp[r] + path[best] * pd[r];
+      if (!freeToBound(p, s, b[1 + 2 * i + sg])) return false;
+    }
+  }
+  const double wm0 = lambda / kappa, wc0 = lambda / kappa + (1.0 - alpha * alpha + beta);
+  const double w = 0.5 / kappa;
+  for (int r = 0; r < 6; ++r) {
+    double m = 0.0;
+    for (int k = 0; k < 17; ++k) m += (k == 0 ? wm0 : w) * b[k][r];
+    mean[r] = m;
+  }
+  for (int r = 0; r < 6; ++r)
+    for (int c = r; c < 6; ++c) {
+      double v = 0.0;
+      for (int k = 0; k < 17; ++k) v += (k == 0 ? wc0 : w) * (b[k][r] - mean[r]) * (b[k][c] - mean[c]);
+      cov[sidx(r, c)] = v;
+    }
+  return true;
+}
+
+// CovarianceEngine.cpp:120-144: the free covariance T C T^T (T = transport
+// x bound-to-free Jacobian, here its reduced form: tloc = T.loc (3x2),
+// tdyn = T.dyn (7x3); C = the bound covariance at the previous surface,
+// packed) through correctedFreeToBound at the free state fr. Out of line,
+// with its operands copied, so that the fit kernels' registers are not
+// sized for it.
+template <typename P, typename CV>
+__device__ __noinline__ bool correctedTransport(const Surf<double>& sfd, const P* tloc,
+                                                const P* tdyn, const CV* cov, const double* fr,
+                                                double* mean, double* bc) {
+  double T8[8][6];
+  for (int r = 0; r < 8; ++r)
+    for (int c = 0; c < 6; ++c) T8[r][c] = 0.0;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 2; ++c) T8[r][c] = (double)tloc[r * 2 + c];
+  for (int r = 0; r < 7; ++r)
+    for (int c = 0; c < 3; ++c) T8[r][2 + c] = (double)tdyn[r * 3 + c];
+  T8[7][4] = 1.0;
+  T8[3][5] = 1.0;
+  double TC[8][6];
+  for (int r = 0; r < 8; ++r)
+    for (int c = 0; c < 6; ++c) {
+      double s = 0.0;
+      for (int k = 0; k < 6; ++k) s += T8[r][k] * (double)cov[sidx(k, c)];
+      TC[r][c] = s;
+    }
+  double C[64];
+  for (int r = 0; r < 8; ++r)
+    for (int c = 0; c < 8; ++c) {
+      double s = 0.0;
+      for (int k = 0; k < 6; ++k) s += TC[r][k] * T8[c][k];
+      C[r * 8 + c] = s;
+    }
+  return correctedFreeToBound(sfd, fr, C, mean, bc);
+}
+
 // ---------------------------------------------------------------- smoother
 // GainMatrixSmoother::calculate. Inputs: filtered state k (filt, Pf packed),
 // state k+1 predicted (pp, Ppp packed), its Jacobian J (row-major 36) and its

@@ -84,7 +84,10 @@ struct Rec {
   CK_D RecState<CV>& s(int k) const { return base[k]; }
 };
 
-template <typename P, typename CV>
+// F2B: the lane applies the free-to-bound correction in its covariance
+// transport when the options ask for it (instantiated separately, so that
+// the default kernels carry none of its code)
+template <typename P, typename CV, bool F2B = false>
 struct Lane {
   // ---- identity: track index and queue position (which indexes the records)
   int phase;
@@ -501,8 +504,11 @@ struct Lane {
   // ------------------------------------------------- covariance transport
   // J = F2B (I + deriv fTP) T, C <- J C J^T, reinitialise T at the surface
   // (CovarianceEngine.cpp:102-165). J is returned for the record.
-  CK_NI void transportToBound(const Surf<double>& sfd, const Surf<P>& sf, const double l[3],
-                              CV Jout[36]) {
+  // correct: KalmanFitterOptions::freeToBoundCorrection (the covariance, and
+  // the free state, through the unscented transform when it applies; l is
+  // then updated to the new position)
+  CK_NI void transportToBound(const Surf<double>& sfd, const Surf<P>& sf, double l[3],
+                              CV Jout[36], bool correct) {
     const P p[3] = {toP<P>(pos[0]), toP<P>(pos[1]), toP<P>(pos[2])};
     P ex[3], ey[3], ez[3];
     referenceFrame(sf, p, ex, ey, ez);
@@ -547,6 +553,14 @@ struct Lane {
     for (int r = 0; r < 6; ++r)
 #pragma unroll
       for (int c = 0; c < 6; ++c) Jout[r * 6 + c] = (CV)J[r][c];
+    if constexpr (F2B) {
+      if (correct && correctTransport(sfd, l)) {
+#pragma unroll
+        for (int i = 0; i < 7; ++i) deriv[i] = P(0);
+        if (onSurfaceLocal(sfd, l)) initTP(sf);
+        return;
+      }
+    }
     // C <- J C J^T (packed); J row 4 is e4 and column 5 is e5
     CV JC[6][6];
 #pragma unroll
@@ -587,6 +601,34 @@ struct Lane {
     if (onSurfaceLocal(sfd, l)) initTP(sf);
   }
 
+  // CovarianceEngine.cpp:120-144 with CorrectedFreeToBoundTransformer: the
+  // free covariance T C T^T goes through the unscented transform; when it
+  // applies, the bound covariance is its result and the free state moves to
+  // the corrected mean. The operands are copied to local arrays for the
+  // out-of-line transformer (the option is off in the common case).
+  CK_D bool correctTransport(const Surf<double>& sfd, double l[3]) {
+    P tl[6], td[21];
+    CV c[21];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int k = 0; k < 2; ++k) tl[r * 2 + k] = T.loc[r][k];
+#pragma unroll
+    for (int r = 0; r < 7; ++r)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) td[r * 3 + k] = T.dyn[r][k];
+#pragma unroll
+    for (int i = 0; i < 21; ++i) c[i] = cov[i];
+    const double fr[8] = {pos[0], pos[1], pos[2], tim, dir[0], dir[1], dir[2], qop};
+    double mean[6], bc[21];
+    if (!correctedTransport<P, CV>(sfd, tl, td, c, fr, mean, bc)) return false;
+    boundToFree(sfd, mean);
+#pragma unroll
+    for (int i = 0; i < 21; ++i) cov[i] = (CV)bc[i];
+    local(sfd, l);
+    return true;
+  }
+
   // --------------------------------------------------------------- actor
   CK_D void writeMeta(const FitParams& fp, int slot, int k, int sid, uint32_t flags, double chi2) {
     RecState<CV>& r = Rec<CV>(fp, slot).s(k);
@@ -623,7 +665,7 @@ struct Lane {
     const int mi = findMeasHinted(fp, sid);
     if (mi >= 0) {
       CV J[36];
-      transportToBound(sf, sp, l, J);
+      transportToBound(sf, sp, l, J, fp.opt.freeToBoundCorrection != 0);
       if (!material(fp, sid, sf, sp, l, 1)) return CK_TRACK_NOT_ON_SURFACE;
       double bp[6];
       if (!freeToBound(fp, sf, l, bp)) return CK_TRACK_NOT_ON_SURFACE;
@@ -683,7 +725,7 @@ struct Lane {
       double bp[6];
       if (!freeToBound(fp, sf, l, bp)) return CK_TRACK_NOT_ON_SURFACE;
       CV J[36];
-      transportToBound(sf, sp, l, J);
+      transportToBound(sf, sp, l, J, fp.opt.freeToBoundCorrection != 0);
       if (nStates >= fp.max_states) return CK_TRACK_TOO_MANY_STATES;
       const int k = nStates++;
 #pragma unroll
@@ -1571,8 +1613,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) fitKernel(FitParams fp) {
 // carries are the FP64 throughput it gets.
 // One phase step of a slot; fetching threads take one ticket per warp (the
 // threads of the warp that run this call together).
-template <typename P, typename CV>
-__device__ __forceinline__ void advanceSlot(const FitParams& fp, Lane<P, CV>& L, int c, int lane) {
+template <typename P, typename CV, bool F2B>
+__device__ __forceinline__ void advanceSlot(const FitParams& fp, Lane<P, CV, F2B>& L, int c,
+                                            int lane) {
   if (c == PH_FETCH) {
     const unsigned act = __activemask();
     const int leader = __ffs(act) - 1;
@@ -1594,11 +1637,11 @@ __device__ __forceinline__ void advanceSlot(const FitParams& fp, Lane<P, CV>& L,
   }
 }
 
-template <typename P, typename CV, int S>
+template <typename P, typename CV, int S, bool F2B = false>
 __global__ void __launch_bounds__(S, 1) fitKernelCompact(FitParams fp) {
   extern __shared__ __align__(16) unsigned char smem[];
-  Lane<P, CV>* st = reinterpret_cast<Lane<P, CV>*>(smem);
-  int* items = reinterpret_cast<int*>(smem + sizeof(Lane<P, CV>) * S);
+  Lane<P, CV, F2B>* st = reinterpret_cast<Lane<P, CV, F2B>*>(smem);
+  int* items = reinterpret_cast<int*>(smem + sizeof(Lane<P, CV, F2B>) * S);
   __shared__ int warpCnt[S / 32][3];
   __shared__ int chosen, nItems;
   const unsigned FULL = 0xffffffffu;
@@ -1645,7 +1688,7 @@ __global__ void __launch_bounds__(S, 1) fitKernelCompact(FitParams fp) {
     if (tid < nItems) {
       const int slot = items[tid];
       // the phase step works on a register copy of the slot's state
-      Lane<P, CV> L = st[slot];
+      Lane<P, CV, F2B> L = st[slot];
       advanceSlot(fp, L, c, lane);
       st[slot] = L;
     }

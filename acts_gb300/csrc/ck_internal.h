@@ -62,6 +62,7 @@ struct DevOptions {
   int loopProtection, multipleScattering, energyLoss, joseph;
   int useOutlierCut, earlyTermination;
   int smoother;  // CK_SMOOTHER_*
+  int freeToBoundCorrection;
 };
 
 // Record of one forward track state kept for the smoother (scratch), one

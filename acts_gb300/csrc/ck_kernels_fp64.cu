@@ -8,6 +8,13 @@ namespace ck {
 // 1 / 3 / 4 resident blocks per SM -> 255 / 168 / 128 registers per thread).
 cudaError_t launchFitFP64(const FitParams& fp, int variant, int grid, int block,
                           cudaStream_t st) {
+  if (fp.opt.freeToBoundCorrection) {
+    // the free-to-bound correction runs in its own instantiation of the
+    // 256-slot compaction kernel (the caller sizes the grid for it)
+    fitKernelCompact<double, double, 256, true>
+        <<<grid, 256, compactSmemBytes<double, double, 256>(), st>>>(fp);
+    return cudaGetLastError();
+  }
   switch (variant) {
     case 0:
       fitKernel<double, double, 128, 1><<<grid, block, 0, st>>>(fp);
@@ -53,7 +60,11 @@ int occupancyFP64(int variant, int tpb) {
 }
 
 cudaError_t configureFP64() {
-  cudaError_t e = cudaFuncSetAttribute(fitKernelCompact<double, double, 256>,
+  cudaError_t e = cudaFuncSetAttribute(fitKernelCompact<double, double, 256, true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)compactSmemBytes<double, double, 256>());
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(fitKernelCompact<double, double, 256>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)compactSmemBytes<double, double, 256>());
   if (e != cudaSuccess) return e;

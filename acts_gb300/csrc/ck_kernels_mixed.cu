@@ -10,6 +10,13 @@ namespace ck {
 
 cudaError_t launchFitMixed(const FitParams& fp, int variant, int grid, int block,
                            cudaStream_t st) {
+  if (fp.opt.freeToBoundCorrection) {
+    // the free-to-bound correction runs in its own instantiation of the
+    // 256-slot compaction kernel (the caller sizes the grid for it)
+    fitKernelCompact<float, float, 256, true>
+        <<<grid, 256, compactSmemBytes<float, float, 256>(), st>>>(fp);
+    return cudaGetLastError();
+  }
   switch (variant) {
     case 0:
       fitKernel<float, float, 128, 1><<<grid, block, 0, st>>>(fp);
@@ -31,7 +38,11 @@ cudaError_t launchFitMixed(const FitParams& fp, int variant, int grid, int block
 }
 
 cudaError_t configureMixed() {
-  cudaError_t e = cudaFuncSetAttribute(fitKernelCompact<float, float, 256>,
+  cudaError_t e = cudaFuncSetAttribute(fitKernelCompact<float, float, 256, true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)compactSmemBytes<float, float, 256>());
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(fitKernelCompact<float, float, 256>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)compactSmemBytes<float, float, 256>());
   if (e != cudaSuccess) return e;

@@ -203,10 +203,17 @@ typedef struct ck_options {
   int32_t use_joseph;           /* 0 (GainMatrixUpdater default)           */
   int32_t precision;            /* CK_PRECISION_*                          */
   double outlier_chi2_cut;      /* +inf                                    */
-  /* Extensions outside the declared set are rejected with
-   * CK_ERR_UNSUPPORTED: reverse filtering and free-to-bound correction. */
+  /* Reverse filtering is outside the declared set and rejected with
+   * CK_ERR_UNSUPPORTED. */
   int32_t reverse_filtering;    /* must be 0                               */
-  int32_t free_to_bound_correction; /* must be 0                           */
+  /* KalmanFitterOptions::freeToBoundCorrection (FreeToBoundCorrection with
+   * its defaults: alpha 0.1, beta 2, incidence window [1e-5, 0.99500417]):
+   * the covariance transport to each state's surface goes through the
+   * unscented transform of CorrectedFreeToBoundTransformer
+   * (Core/src/EventData/CorrectedTransformationFreeToBound.cpp:51-183,
+   * Core/src/Propagator/detail/CovarianceEngine.cpp:120-144). 0 (default)
+   * or 1. Computed in FP64 in both forms. */
+  int32_t free_to_bound_correction;
   /* KalmanFitterOptions::referenceSurface: -1 (none) or the index of a
    * CK_SURFACE_LINE surface of the table. After smoothing, each track is
    * extrapolated to it (extrapolateTrackToReferenceSurface,

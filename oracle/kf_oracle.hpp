@@ -971,8 +971,10 @@ struct Options {
   int smoother;                    // CK_SMOOTHER_*
   int referenceSurface;            // -1 or a table index
   int referenceStrategy;           // CK_EXTRAPOLATE_*
+  bool freeToBoundCorrection;      // KalmanFitterOptions::freeToBoundCorrection
   static Options fromCk(const ck_options& o, bool coast) {
     Options r;
+    r.freeToBoundCorrection = o.free_to_bound_correction != 0;
     r.smoother = o.smoother;
     r.referenceSurface = o.reference_surface;
     r.referenceStrategy = o.reference_strategy;
@@ -1200,9 +1202,115 @@ int eigenStep(Stepper<S>& st, const Field<S>& field, const Options& o, S& hOut,
   return kStepOk;
 }
 
+// Eigen decomposition of a symmetric 8x8 matrix by cyclic Jacobi rotations
+// (the free covariance is symmetric positive semi-definite, so its SVD
+// U S U^T is this decomposition; Eigen::JacobiSVD is not available here).
+// On return A holds the eigenvalues on its diagonal, V the eigenvectors in
+// its columns.
+template <typename S>
+void jacobiEigen8(Mat<S, 8, 8>& A, Mat<S, 8, 8>& V) {
+  using std::abs;
+  using std::sqrt;
+  V = Mat<S, 8, 8>::identity();
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    S off = S(0.0), diag = S(0.0);
+    for (int p = 0; p < 8; ++p) {
+      diag = diag + A.a[p][p] * A.a[p][p];
+      for (int q = p + 1; q < 8; ++q) off = off + A.a[p][q] * A.a[p][q];
+    }
+    if (!(off > S(1e-60) * diag)) break;
+    for (int p = 0; p < 7; ++p)
+      for (int q = p + 1; q < 8; ++q) {
+        const S apq = A.a[p][q];
+        if (apq == S(0.0)) continue;
+        const S theta = (A.a[q][q] - A.a[p][p]) / (S(2.0) * apq);
+        const S t = (theta >= S(0.0) ? S(1.0) : S(-1.0)) /
+                    (abs(theta) + sqrt(theta * theta + S(1.0)));
+        const S c = S(1.0) / sqrt(t * t + S(1.0)), sn = t * c;
+        for (int k = 0; k < 8; ++k) {  // A <- A R (columns p, q)
+          const S akp = A.a[k][p], akq = A.a[k][q];
+          A.a[k][p] = c * akp - sn * akq;
+          A.a[k][q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < 8; ++k) {  // A <- R^T A (rows p, q)
+          const S apk = A.a[p][k], aqk = A.a[q][k];
+          A.a[p][k] = c * apk - sn * aqk;
+          A.a[q][k] = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < 8; ++k) {
+          const S vkp = V.a[k][p], vkq = V.a[k][q];
+          V.a[k][p] = c * vkp - sn * vkq;
+          V.a[k][q] = sn * vkp + c * vkq;
+        }
+      }
+  }
+}
+
+// detail::CorrectedFreeToBoundTransformer::operator()
+// (Core/src/EventData/CorrectedTransformationFreeToBound.cpp:51-183) with the
+// FreeToBoundCorrection defaults (alpha 0.1, beta 2, incidence cut-offs
+// 1e-5 / 0.99500417; CorrectedTransformationFreeToBound.hpp:22-35): an
+// unscented transform of the free covariance through free-to-bound, each
+// shifted sigma point put back on the surface along its direction. False
+// (no correction) outside the incidence window or when a transformation
+// fails.
+template <typename S>
+bool correctedFreeToBound(const Vec<S, 8>& fp, const Mat<S, 8, 8>& freeCov, const Surface<S>& s,
+                          Vec<S, 6>& mean, Mat<S, 6, 6>& cov) {
+  using std::abs;
+  using std::sqrt;
+  const double alpha = 0.1, beta = 2.0, cosMin = 1e-5, cosMax = 0.99500417;
+  V3<S> pos{{fp[0], fp[1], fp[2]}}, dir{{fp[4], fp[5], fp[6]}};
+  const S absCos = abs(dot(dir, s.normal(pos)));
+  if (absCos < S(cosMin) || absCos > S(cosMax)) return false;
+  Mat<S, 8, 8> A = freeCov, U;
+  jacobiEigen8(A, U);
+  Mat<S, 8, 8> covSqrt;
+  for (int i = 0; i < 8; ++i)
+    for (int j = 0; j < 8; ++j) covSqrt.a[i][j] = A.a[j][j] > S(0.0) ? U.a[i][j] * sqrt(A.a[j][j]) : S(0.0);
+  const double kappa = alpha * alpha * 8.0, lambda = kappa - 8.0, gamma = std::sqrt(kappa);
+  Vec<S, 6> b[17];
+  double wm[17], wc[17];
+  if (!freeToBound(fp, s, b[0])) return false;
+  wm[0] = lambda / kappa;
+  wc[0] = lambda / kappa + (1.0 - alpha * alpha + beta);
+  for (int i = 0; i < 8; ++i)
+    for (int sg = 0; sg < 2; ++sg) {
+      const int k = 1 + 2 * i + sg;
+      Vec<S, 8> p = fp;
+      for (int r = 0; r < 8; ++r)
+        p[r] = sg == 0 ? p[r] + covSqrt.a[r][i] * S(gamma) : p[r] - covSqrt.a[r][i] * S(gamma);
+      // re-intersect along the sample's direction (forward), no bounds
+      V3<S> pp{{p[0], p[1], p[2]}}, pd{{p[4], p[5], p[6]}};
+      Intersection<S> is[2];
+      const int n = s.intersect(pp, pd, S(kOnSurfaceTolerance), is);
+      int best = -1;
+      for (int j = 0; j < n; ++j) {
+        if (is[j].status == IStatus::unreachable) continue;
+        if (best < 0 || abs(is[j].pathLength) < abs(is[best].pathLength)) best = j;
+      }
+      if (best < 0) return false;
+      for (int r = 0; r < 3; ++r) p[r] = pp[r] + is[best].pathLength * pd[r];
+      if (!freeToBound(p, s, b[k])) return false;
+      wm[k] = 0.5 / kappa;
+      wc[k] = 0.5 / kappa;
+    }
+  for (int r = 0; r < 6; ++r) mean[r] = S(0.0);
+  for (int k = 0; k < 17; ++k)
+    for (int r = 0; r < 6; ++r) mean[r] = mean[r] + S(wm[k]) * b[k][r];
+  cov = Mat<S, 6, 6>::zero();
+  for (int k = 0; k < 17; ++k) {
+    Vec<S, 6> d;
+    for (int r = 0; r < 6; ++r) d[r] = b[k][r] - mean[r];
+    for (int r = 0; r < 6; ++r)
+      for (int c = 0; c < 6; ++c) cov.a[r][c] = cov.a[r][c] + S(wc[k]) * d[r] * d[c];
+  }
+  return true;
+}
+
 // CovarianceEngine.cpp:102-165 + JacobianEngine.cpp:19-45,122-141
 template <typename S>
-void transportCovarianceToBound(Stepper<S>& st, const Surface<S>& s) {
+void transportCovarianceToBound(Stepper<S>& st, const Surface<S>& s, bool correction = false) {
   V3<S> pos = st.pos(), dir = st.dir();
   Vec<S, 8> fTP = s.freeToPathDerivative(pos, dir);
   Mat<S, 6, 8> F2B = s.freeToBoundJacobian(pos, dir);
@@ -1212,7 +1320,23 @@ void transportCovarianceToBound(Stepper<S>& st, const Surface<S>& s) {
   Mat<S, 6, 8> A = mul(F2B, M);
   Mat<S, 6, 8> B = mul(A, st.jacTransport);
   st.jacobian = mul(B, st.jacToGlobal);
-  st.cov = mul(mul(st.jacobian, st.cov), transpose(st.jacobian));
+  bool corrected = false;
+  if (correction) {
+    // CovarianceEngine.cpp:120-144: the free covariance through the
+    // unscented transform; the free parameters move to the corrected mean
+    Mat<S, 8, 6> T = mul(st.jacTransport, st.jacToGlobal);
+    Mat<S, 8, 8> freeCov = mul(mul(T, st.cov), transpose(T));
+    Vec<S, 6> mean;
+    Mat<S, 6, 6> bc;
+    if (correctedFreeToBound(st.pars, freeCov, s, mean, bc)) {
+      st.pars = boundToFree(s, mean);
+      st.cov = bc;
+      corrected = true;
+      pos = st.pos();
+      dir = st.dir();
+    }
+  }
+  if (!corrected) st.cov = mul(mul(st.jacobian, st.cov), transpose(st.jacobian));
   // reinitializeJacobians: identity, zero, and the new boundToFree (only if
   // the position is on the surface; the result is ignored otherwise)
   st.jacTransport = Mat<S, 8, 8>::identity();
@@ -1736,7 +1860,7 @@ struct Fitter {
     // boundState (CovarianceEngine.cpp:29-63)
     auto boundState = [&](const Surface<S>& s, bool transportCov, Vec<S, 6>& bp) -> bool {
       if (!freeToBound(st.pars, s, bp)) return false;
-      if (transportCov) transportCovarianceToBound(st, s);
+      if (transportCov) transportCovarianceToBound(st, s, o.freeToBoundCorrection);
       return true;
     };
 
@@ -1785,7 +1909,7 @@ struct Fitter {
       const bool precedingMeasurementExists = measurementStates > 0;
       const int mi = findMeas(sid);
       if (mi >= 0) {
-        transportCovarianceToBound(st, s);
+        transportCovarianceToBound(st, s, o.freeToBoundCorrection);
         if (!material(s, 1)) return CK_TRACK_NOT_ON_SURFACE;
         IState ts;
         ts.surface = sid;

@@ -260,6 +260,25 @@ int kfo_line_intersect(const double* center, const double* rot, const double* po
   return is[0].status == IStatus::onSurface ? 2 : 1;
 }
 
+// detail::CorrectedFreeToBoundTransformer on one free state and covariance
+// (8, 64 row-major) and a surface: 1 with the corrected bound mean (6) and
+// covariance (36), 0 when no correction applies.
+int kfo_corrected_free_to_bound(const ck_surface* cs, const double* freePars,
+                                const double* freeCov, double* mean, double* cov) {
+  Surface<double> s = Surface<double>::fromCk(*cs);
+  Vec<double, 8> f;
+  for (int i = 0; i < 8; ++i) f[i] = freePars[i];
+  Mat<double, 8, 8> C;
+  for (int i = 0; i < 8; ++i)
+    for (int j = 0; j < 8; ++j) C.a[i][j] = freeCov[i * 8 + j];
+  Vec<double, 6> m;
+  Mat<double, 6, 6> bc;
+  if (!correctedFreeToBound(f, C, s, m, bc)) return 0;
+  put6(mean, m);
+  put36(cov, bc);
+  return 1;
+}
+
 // Interactions.cpp entry points for the material known-answer tests.
 // slab: thickness, X0, L0, Ar, Z, molarRho (mol/mm^3); which: 0 Bethe,
 // 1 Landau (most probable), 2 Landau sigma(q/p), 3 theta0, 4 Landau FWHM.

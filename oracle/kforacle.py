@@ -39,6 +39,8 @@ def lib():
         L.kfo_line_global_to_local.argtypes = [abi.P_f64] * 5
         L.kfo_line_intersect.restype = C.c_int
         L.kfo_line_intersect.argtypes = [abi.P_f64] * 4 + [C.POINTER(C.c_double)]
+        L.kfo_corrected_free_to_bound.restype = C.c_int
+        L.kfo_corrected_free_to_bound.argtypes = [C.POINTER(abi.ck_surface)] + [abi.P_f64] * 4
         L.kfo_interaction.restype = C.c_float
         L.kfo_interaction.argtypes = [C.c_int] + [C.c_float] * 6 + [C.c_int] + [C.c_float] * 3
         L.kfo_material_effects.restype = None
@@ -89,6 +91,16 @@ def line_global_to_local(center, rotation, pos, direction):
     ok = lib().kfo_line_global_to_local(*[abi.ptr(x, C.c_double) for x in a],
                                         abi.ptr(loc, C.c_double))
     return bool(ok), loc
+
+
+def corrected_free_to_bound(surface, free_params, free_cov):
+    """CorrectedFreeToBoundTransformer: (ok, mean[6], cov[6, 6])."""
+    mean = np.zeros(6)
+    cov = np.zeros(36)
+    ok = lib().kfo_corrected_free_to_bound(C.byref(surface), abi.ptr(_v(free_params), C.c_double),
+                                           abi.ptr(_v(np.reshape(free_cov, 64)), C.c_double),
+                                           abi.ptr(mean, C.c_double), abi.ptr(cov, C.c_double))
+    return bool(ok), mean, cov.reshape(6, 6)
 
 
 def line_intersect(center, rotation, pos, direction):

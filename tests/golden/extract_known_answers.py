@@ -8,6 +8,7 @@ reference at run time. Sources parsed (paths relative to the acts repo):
   Tests/UnitTests/Core/TrackFitting/GainMatrixSmootherTests.cpp (Smooth)
   Tests/UnitTests/Core/TrackFitting/MbfSmootherTests.cpp        (Smooth)
   Tests/UnitTests/Core/Surfaces/LineSurfaceTests.cpp            (globalToLocal, intersect)
+  Tests/UnitTests/Core/EventData/CorrectedTransformFreeToBoundTests.cpp
   Tests/UnitTests/Core/Material/InteractionsTests.cpp           (silicon Bethe, Landau)
   Tests/CommonHelpers/include/ActsTests/CommonHelpers/PredefinedMaterials.hpp (makeSilicon)
 """
@@ -19,7 +20,8 @@ import sys
 
 UNITS = {"_GeV": 1.0, "_MeV": 1e-3, "_keV": 1e-6, "_eV": 1e-9, "_TeV": 1e3, "_mm": 1.0,
          "_cm": 10.0, "_um": 1e-3, "_m": 1e3, "_e": 1.0, "_mol": 1.0, "_cm3": 1000.0,
-         "_mm2": 1.0, "_g": 1.0 / 1.782662e-24, "_cm2": 100.0}
+         "_mm2": 1.0, "_g": 1.0 / 1.782662e-24, "_cm2": 100.0,
+         "_ns": 299.792458}  # ACTS time unit: mm (1 s = c * 1 s in mm)
 
 
 def num(expr):
@@ -115,6 +117,23 @@ def line_surface(src):
             "intersect_expected": vec(r"Vector3 expectedIntersection\(([^)]*)\)")}
 
 
+def corrected_free_to_bound(src):
+    t = open(os.path.join(src, "Tests/UnitTests/Core/EventData/CorrectedTransformFreeToBoundTests.cpp")).read()
+    v = {}
+    for name in ("loc0", "loc1", "phi", "theta", "qOverP", "t", "resLoc0", "resLoc1", "resPhi",
+                 "resTheta", "resQOverP", "resTime"):
+        v[name] = num(re.search(r"const auto %s = ([^;]*);" % name, t).group(1))
+    v["distance"] = num(re.search(r"double distance = ([^;]*);", t).group(1))
+    m = re.search(r"CHECK_CLOSE_REL\(eCorrectedBoundParams\[eBoundLoc1\], ([0-9.eE+-]+), eps\)", t)
+    v["exp_loc1"] = float(m.group(1))
+    m = re.search(r"std::pow\(([0-9.eE+-]+), 2\)", t)
+    v["exp_loc0_sigma"] = float(m.group(1))
+    v["eps"] = num(re.search(r"constexpr double eps = ([^;]*);", t).group(1))
+    v["source"] = "Tests/UnitTests/Core/EventData/CorrectedTransformFreeToBoundTests.cpp"
+    v["surface"] = "curvilinear plane at (distance, 0, 0), normal x"
+    return v
+
+
 def interactions(src):
     t = open(os.path.join(src, "Tests/UnitTests/Core/Material/InteractionsTests.cpp")).read()
     mom = re.search(r"static const double momentum\[\] = \{([^}]*)\}", t).group(1)
@@ -159,6 +178,7 @@ def main():
     src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     out = {"updater": updater(src), "smoother": smoother(src), "mbf_smoother": mbf_smoother(src),
            "line_surface": line_surface(src),
+           "corrected_free_to_bound": corrected_free_to_bound(src),
            "interactions": interactions(src),
            "silicon": silicon(src)}
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_known_answers.json")

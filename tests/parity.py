@@ -12,12 +12,16 @@ def _sig(cov):
     return np.sqrt(np.abs(d))
 
 
-def compare(gpu, ora, rtol=1e-9, fields=("predicted", "filtered", "smoothed")):
-    """Returns a dict of max normalised errors and mismatch counts."""
+def compare(gpu, ora, rtol=1e-9, fields=("predicted", "filtered", "smoothed"), exclude=None):
+    """Returns a dict of max normalised errors and mismatch counts. `exclude`:
+    tracks left out of the floating-point comparison (statuses still
+    compared)."""
     rep = {}
     st_g, st_o = gpu.status, ora.status
     rep["status_mismatch"] = int(np.sum(st_g != st_o))
     ok = (st_g == 0) & (st_o == 0)
+    if exclude is not None:
+        ok &= ~exclude
     rep["n_ok"] = int(ok.sum())
     for name in ("n_states", "n_measurements", "n_holes", "n_outliers", "ndf"):
         rep[name + "_mismatch"] = int(np.sum(getattr(gpu, name)[ok] != getattr(ora, name)[ok]))

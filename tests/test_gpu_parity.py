@@ -35,6 +35,10 @@ CASES = [
     ("strips_joseph_outliers", abi.CKG_STRIPS, 1000, dict(use_joseph=1, outlier_chi2_cut=15.0),
      0.99),
     ("strips_mbf", abi.CKG_STRIPS, 1000, dict(smoother=abi.SMOOTHER_MBF), 0.99),
+    ("barrel_free_to_bound_correction", abi.CKG_BARREL, 1000, dict(free_to_bound_correction=1),
+     0.99),
+    ("uneven_free_to_bound_correction", abi.CKG_UNEVEN, 1000,
+     dict(outlier_chi2_cut=15.0, free_to_bound_correction=1), 0.5),
 ]
 
 
@@ -47,9 +51,17 @@ def test_fp64_parity(fitter_factory, name, preset, n, kw, min_ok):
     ora = Results(n, 24)
     kforacle.fit_batch(det, b, opt, ora, n_threads=kforacle.hardware_threads())
     gpu = fitter_factory(preset).fit_batch(b, opt, max_states=24)
-    rep = compare(gpu, ora, RTOL)
+    exclude = None
+    if kw.get("free_to_bound_correction"):
+        # the correction's unscented transform averages bound vectors without
+        # unwrapping phi (as the reference): sigma points straddling the
+        # cylinder seam break a fit (chi2/ndf ~ 1e4), and the broken fit is
+        # chaotic in the last bits; such fits are compared by status only
+        exclude = ora.chi2_sum > 100.0 * np.maximum(ora.ndf, 1)
+        assert exclude.sum() <= 0.003 * n
+    rep = compare(gpu, ora, RTOL, exclude=exclude)
     print(name, rep)
-    assert rep["n_ok"] >= min_ok * n
+    assert rep["n_ok"] >= min_ok * n - (0 if exclude is None else exclude.sum())
     assert_parity(rep, RTOL)
 
 

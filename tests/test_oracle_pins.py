@@ -241,6 +241,69 @@ def test_line_surface_only_as_reference():
     assert (np.delete(res.status, 2) == 0).all()
 
 
+# ------------------------------------- CorrectedTransformFreeToBoundTests.cpp
+def test_corrected_free_to_bound_known_answer():
+    """The unscented free-to-bound correction on the reference's setup: a
+    track from the origin (phi 0, theta pi/4, sigma(phi) = sigma(theta) =
+    0.25) to a plane at x = 10 mm: loc0 and phi unchanged, loc1 shifted to
+    11.2563, sigma(loc0) = 2.5 mm."""
+    ka = KA["corrected_free_to_bound"]
+    d = ka["distance"]
+    # the plane: curvilinear frame of direction x (local x = y, local y = z)
+    s = abi.ck_surface()
+    s.type = abi.SURFACE_PLANE
+    for i, v in enumerate([0, 0, 1, 1, 0, 0, 0, 1, 0]):
+        s.rotation[i] = float(v)
+    s.center[0] = d
+    ph, th = ka["phi"], ka["theta"]
+    direction = np.array([np.cos(ph) * np.sin(th), np.sin(ph) * np.sin(th), np.cos(th)])
+    path = d / direction[0]
+    assert path == pytest.approx(d * np.sqrt(2.0))
+    free = np.concatenate([path * direction, [ka["t"]], direction, [ka["qOverP"]]])
+    # bound-to-free Jacobian of the plane at the end point (as the test
+    # builds it), the bound covariance, the straight-line transport
+    j = np.zeros((8, 6))
+    j[0:3, 0] = [0, 1, 0]
+    j[0:3, 1] = [0, 0, 1]
+    j[3, 5] = 1.0
+    j[4:7, 2] = [-np.sin(th) * np.sin(ph), np.sin(th) * np.cos(ph), 0.0]
+    j[4:7, 3] = [np.cos(th) * np.cos(ph), np.cos(th) * np.sin(ph), -np.sin(th)]
+    j[7, 4] = 1.0
+    res = [ka["resLoc0"], ka["resLoc1"], ka["resPhi"], ka["resTheta"], ka["resQOverP"],
+           ka["resTime"]]
+    sfree = j @ np.diag(np.square(res)) @ j.T
+    tj = np.eye(8)
+    for i in range(3):
+        tj[i, 4 + i] = path
+    efree = tj @ sfree @ tj.T
+    ok, mean, cov = kforacle.corrected_free_to_bound(s, free, efree)
+    assert ok
+    assert mean[0] == pytest.approx(ka["loc0"], abs=1e-9)
+    assert mean[2] == pytest.approx(ka["phi"], abs=1e-9)
+    assert mean[1] == pytest.approx(ka["exp_loc1"], rel=ka["eps"])
+    assert cov[0, 0] == pytest.approx(ka["exp_loc0_sigma"] ** 2, rel=ka["eps"])
+
+
+def test_free_to_bound_correction_in_fits():
+    """With the correction the fits move by a small fraction of a sigma
+    (median < 0.1), except where the sigma points straddle phi = +-pi: the
+    reference's unscented transform averages the bound vectors without
+    unwrapping, which breaks such a fit (~1 in 2000 barrel tracks)."""
+    b = batch(abi.CKG_BARREL, 2000)
+    r0 = _fit(abi.CKG_BARREL, b)
+    r1 = _fit(abi.CKG_BARREL, b, free_to_bound_correction=1)
+    ok = (r0.status == 0) & (r1.status == 0)
+    assert ok.mean() > 0.98
+    a, c = r0.view("smoothed")[ok, 0], r1.view("smoothed")[ok, 0]
+    assert not np.array_equal(a, c)
+    sig = np.sqrt(r0.view("smoothed_cov")[ok, 0][:, [0, 7, 14, 21, 28]])
+    d = (np.abs(c[:, :5] - a[:, :5]) / sig).max(axis=1)
+    assert np.median(d) < 0.1
+    broken = d > 1.0
+    assert broken.sum() <= 0.002 * ok.sum()
+    assert (np.abs(np.abs(a[broken, 2]) - np.pi) < 0.1).all()  # at the seam
+
+
 # ---------------------------------------------------- MbfSmootherTests.cpp
 def mbf_inputs():
     s = KA["mbf_smoother"]
