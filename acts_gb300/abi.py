@@ -35,7 +35,10 @@ TRACK_STATUS = {
     12: "InvalidInput",
     13: "CompatibleTrackStateNotFound",
     14: "ReferenceSurfaceUnreachable",
+    15: "InconsistentTrackStates",
 }
+
+TRACK_INCONSISTENT_STATES = 15
 
 FLAG_HAS_MEASUREMENT = 1 << 0
 FLAG_HAS_PARAMETERS = 1 << 1
@@ -147,6 +150,8 @@ class ck_options(C.Structure):
         ("early_termination", C.c_int32),
         ("smoother", C.c_int32),
         ("reference_strategy", C.c_int32),
+        ("reverse_filtering_cov_scaling", C.c_double),
+        ("reverse_filtering_mom_threshold", C.c_double),
     ]
 
 
@@ -280,6 +285,8 @@ def default_options(**kw):
     o.early_termination = 0
     o.smoother = SMOOTHER_GAIN_MATRIX
     o.reference_strategy = EXTRAPOLATE_FIRST_OR_LAST
+    o.reverse_filtering_cov_scaling = 100.0
+    o.reverse_filtering_mom_threshold = 0.0
     for k, v in kw.items():
         setattr(o, k, v)
     return o

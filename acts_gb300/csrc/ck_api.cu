@@ -118,13 +118,14 @@ DevOptions toDevOptions(const ck_options& o) {
   d.earlyTermination = o.early_termination;
   d.smoother = o.smoother;
   d.freeToBoundCorrection = o.free_to_bound_correction;
+  d.reverseFiltering = o.reverse_filtering;
+  d.reverseCovScaling = o.reverse_filtering_cov_scaling;
+  d.reverseMomThreshold = o.reverse_filtering_mom_threshold;
   return d;
 }
 
 ck_status validateOptions(const ck_options* o) {
   if (!o) return fail(CK_ERR_INVALID_ARGUMENT, "options is NULL");
-  if (o->reverse_filtering)
-    return fail(CK_ERR_UNSUPPORTED, "reverse filtering is not in the declared extension set");
   if (o->reference_surface < -1)
     return fail(CK_ERR_INVALID_ARGUMENT, "reference_surface must be -1 or a surface index");
   if (o->reference_strategy < CK_EXTRAPOLATE_FIRST ||
@@ -373,7 +374,7 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
   fp.opt = toDevOptions(opt);
   fp.ref_surface = opt.reference_surface;
   fp.ref_strategy = opt.reference_strategy;
-  fp.ext = opt.reference_surface >= 0 ? (ExtStart*)c.ext.p : nullptr;
+  fp.ext = needsExtStart(opt) ? (ExtStart*)c.ext.p : nullptr;
   {
     // the extrapolation's propagator options: the reference's defaults
     // (KalmanFitter.hpp:960-961 constructs them without the fit's options)
@@ -395,10 +396,26 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
     if (e != cudaSuccess) return cudaFail(e, "fit kernel launch");
     ++launches;
     if (timed) cudaEventRecordWithFlags(h->evMid, st, recFlags);
-    e = launchSmooth(fp, opt.precision, st);
-    if (e != cudaSuccess) return cudaFail(e, "smoother kernel launch");
-    ++launches;
-    if (fp.ext) {
+    if (anyReverse(opt)) {
+      // the reversed pass: the 256-slot compaction kernel, one block per SM,
+      // over the same queue (the tracks the reverse-filtering logic selects)
+      FitParams rp = fp;
+      const long long warps = (long long)h->smCount * (256 / 32);
+      rp.lanes_per_warp = (int)std::min<long long>(32, std::max<long long>(1, (n + warps - 1) / warps));
+      cudaMemsetAsync(dTicket, 0, sizeof(int32_t), st);
+      e = launchReverse(rp, opt.precision, h->smCount, st);
+      if (e != cudaSuccess) return cudaFail(e, "reversed filter kernel launch");
+      ++launches;
+      e = launchReverseOutput(fp, opt.precision, st);
+      if (e != cudaSuccess) return cudaFail(e, "reverse filtering output kernel launch");
+      ++launches;
+    }
+    if (!opt.reverse_filtering) {
+      e = launchSmooth(fp, opt.precision, st);
+      if (e != cudaSuccess) return cudaFail(e, "smoother kernel launch");
+      ++launches;
+    }
+    if (opt.reference_surface >= 0) {
       e = launchExtrapolate(fp, st);
       if (e != cudaSuccess) return cudaFail(e, "extrapolation kernel launch");
       ++launches;
@@ -448,6 +465,8 @@ void ck_options_default(ck_options* o) {
   o->early_termination = 0;
   o->smoother = CK_SMOOTHER_GAIN_MATRIX;
   o->reference_strategy = CK_EXTRAPOLATE_FIRST_OR_LAST;
+  o->reverse_filtering_cov_scaling = 100.0;
+  o->reverse_filtering_mom_threshold = 0.0;
 }
 
 int32_t ck_api_version(void) { return CK_API_VERSION; }
@@ -751,7 +770,7 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
   // ---- pipeline (graph-captured for device-resident batches)
   const int gridBlocks = gridBlocksFor(h, tn);
   ck_status s = preparePipeline(h, h->ctx, n, out->max_states, opt->precision,
-                                opt->reference_surface >= 0);
+                                needsExtStart(*opt));
   if (s != CK_OK) return s;
   const bool deviceOnly = in->memory == CK_MEM_DEVICE && out->memory == CK_MEM_DEVICE;
   if (deviceOnly && h->useGraph && n > 0) {

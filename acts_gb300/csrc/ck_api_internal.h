@@ -68,6 +68,12 @@ ck_status validateOptions(const ck_options* o);
 // the reference surface of the options against the handle's table (a line
 // surface) and the strategy
 ck_status validateReference(const ck_handle* h, const ck_options* o);
+// the extrapolation start slots are needed for the extrapolation to the
+// reference surface and for reverse filtering
+inline bool anyReverse(const ck_options& o) {
+  return o.reverse_filtering != 0 || o.reverse_filtering_mom_threshold > 0.0;
+}
+inline bool needsExtStart(const ck_options& o) { return o.reference_surface >= 0 || anyReverse(o); }
 DevOptions toDevOptions(const ck_options& o);
 MatConst makeMatConst();
 DevSurface toDevSurface(const ck_surface& s);

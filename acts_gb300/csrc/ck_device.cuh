@@ -1173,7 +1173,6 @@ CK_D bool smoothStep(const double filt[6], const GP Pf[21], const double pp[6], 
   for (int i = 0; i < 6; ++i) d[i] = ps[i] - pp[i];
   d[2] = radian_sym(d[2]);
   d[3] = radian_sym(d[3]);
-#pragma unroll
   GP dg[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) dg[k] = toPi<GP>(d[k]);

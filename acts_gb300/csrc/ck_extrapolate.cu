@@ -36,6 +36,9 @@ __global__ void __launch_bounds__(kExtrapolateBlock) extrapolateKernel(FitParams
     if (fp.out.status[t] != CK_TRACK_OK) continue;  // the smoother failed
     const ExtStart& first = fp.ext[2 * (size_t)q];
     const ExtStart& last = fp.ext[2 * (size_t)q + 1];
+    // the reversed pass reached the reference surface: the track has its
+    // parameters (KalmanFitter.hpp:938-943, :949)
+    if (first.fitted) continue;
     Lane<double, double> L;
     L.t = t;
     L.q = q;

@@ -84,10 +84,33 @@ struct Rec {
   CK_D RecState<CV>& s(int k) const { return base[k]; }
 };
 
+// KalmanFitter.hpp:897-900: every track with reverseFiltering, else the
+// tracks whose last measurement state's filtered momentum 1/|q/p| is at most
+// the threshold (SimpleReverseFilteringLogic, Examples/Algorithms/
+// TrackFitting/src/KalmanFitterFunction.cpp:50-58)
+template <typename CV>
+CK_D bool reverseSelected(const FitParams& fp, int q, int tip) {
+  if (fp.opt.reverseFiltering) return true;
+  if (!(fp.opt.reverseMomThreshold > 0.0)) return false;
+  const Rec<CV> rec(fp, q);
+  for (int k = tip; k >= 0; --k) {
+    const uint32_t fl = (uint32_t)rec.s(k).flags;
+    if ((fl & CK_FLAG_HAS_MEASUREMENT) && !(fl & CK_FLAG_IS_OUTLIER))
+      return fabs(1.0 / rec.p(k, kRecFilt + 4)) <= fp.opt.reverseMomThreshold;
+  }
+  return false;
+}
+
 // F2B: the lane applies the free-to-bound correction in its covariance
 // transport when the options ask for it (instantiated separately, so that
-// the default kernels carry none of its code)
-template <typename P, typename CV, bool F2B = false>
+// the default kernels carry none of its code).
+// REV: the lane runs the reversed filter pass of reverse filtering
+// (KalmanFitter.hpp:897-945): backwards along the sequence from the forward
+// pass's last measurement state, which it reads from that pass's records;
+// it writes no records, only its latest filtered measurement state (the
+// extrapolation start slot 0) and, when it reaches the reference surface,
+// the track parameters there.
+template <typename P, typename CV, bool F2B = false, bool REV = false>
 struct Lane {
   // ---- identity: track index and queue position (which indexes the records)
   int phase;
@@ -119,8 +142,16 @@ struct Lane {
   // mode of the lane: the fit, or the extrapolation to the reference surface
   double dirSign;
   bool extrapolating;
-  // ---- Kalman fitter actor
-  int nStates, lastMeasurementIndex, measurementStates, nDistinct, lastSlSeq;
+  // ---- Kalman fitter actor; lastSlSeq is the last sequence position in the
+  // direction of travel that carries a source link. The reversed pass keeps
+  // no track (no tip) and holds its start surface in the tip's place (an
+  // extra field costs the FP64 kernel spills).
+  int nStates;
+  union {
+    int lastMeasurementIndex;  // forward: the tip
+    int startSid;              // reversed: the start surface (a table id)
+  };
+  int measurementStates, nDistinct, lastSlSeq;
   int measHint;  // where the next measurement lookup starts (distinct surfaces only)
   bool finished, coasting;
   double propLimit, kfLimit;
@@ -171,14 +202,21 @@ struct Lane {
     return -1;
   }
 
-  // Surface::intersect in double (BoundaryTolerance::Infinite)
+  // Surface::intersect in double (BoundaryTolerance::Infinite), along the
+  // direction of travel (the navigator's direction times the momentum's)
   CK_NI int intersectSurf(const FitParams& fp, int sid, double path[2], int st[2]) const {
     Surf<double> sf;
     sf.load(fp.surfaces + sid);
+    double nd[3] = {dir[0], dir[1], dir[2]};
+    if constexpr (REV) {
+      nd[0] = -dir[0];
+      nd[1] = -dir[1];
+      nd[2] = -dir[2];
+    }
     if constexpr (sizeof(P) == sizeof(float)) {
-      return intersectMixed(sf, pos, dir, fp.opt.surfaceTolerance, path, st);
+      return intersectMixed(sf, pos, nd, fp.opt.surfaceTolerance, path, st);
     } else {
-      return intersect(sf, pos, dir, fp.opt.surfaceTolerance, path, st);
+      return intersect(sf, pos, nd, fp.opt.surfaceTolerance, path, st);
     }
   }
 
@@ -391,10 +429,11 @@ struct Lane {
   }
 
   CK_D bool nextTargetNav(const FitParams& fp) {
+    constexpr int inc = REV ? -1 : 1;  // DirectNavigator::State::nextSurface
     currentSurface = -1;
     if (navigationBreak) return false;
-    ++surfaceIndex;
-    while (surfaceIndex < nSeq) {
+    surfaceIndex += inc;
+    while (surfaceIndex >= 0 && surfaceIndex < nSeq) {
       const int sid = __ldg(&fp.seq_surf[seq0 + surfaceIndex]);
       double path[2];
       int st[2];
@@ -406,7 +445,7 @@ struct Lane {
           return true;
         }
       }
-      ++surfaceIndex;
+      surfaceIndex += inc;
     }
     navigationBreak = true;
     return false;
@@ -425,11 +464,17 @@ struct Lane {
   }
 
   // ------------------------------------------------------------ material
-  // PointwiseMaterialInteraction: mode 1 pre, 2 post, 3 full.
+  // PointwiseMaterialInteraction: mode 1 pre, 2 post, 3 full; on the start
+  // surface only the post-update part applies (determineMaterialUpdateMode,
+  // PointwiseMaterialInteraction.cpp:16-29), and the pre/post split factors
+  // follow the direction of travel (ISurfaceMaterial.cpp:18-31).
   CK_NI bool material(const FitParams& fp, int sid, const Surf<double>& sfd, const Surf<P>& sp,
                       const double l[3], int mode) {
     const DevSurface* ds = fp.surfaces + sid;
     if (!(__ldg(&ds->flags) & CK_SURF_MATERIAL)) return true;
+    if constexpr (REV) {
+      if (sid == startSid) mode &= 2;
+    }
     const P d[3] = {toP<P>(dir[0]), toP<P>(dir[1]), toP<P>(dir[2])};
     P pc;
     if (sfd.type == CK_SURFACE_PLANE) {
@@ -452,7 +497,10 @@ struct Lane {
     float f1 = 1.0f;
     if (__ldg(&ds->vacuum) == 0) {
       const float split = __ldg(&ds->split);
-      const double factor = (mode == 3) ? 1.0 : (mode == 1 ? 1.0 - (double)split : (double)split);
+      // forward: pre 1 - split, post split; backward the other way round
+      const bool firstPart = (mode == 1) != REV;
+      const double factor =
+          mode == 0 ? 0.0 : (mode == 3 ? 1.0 : (firstPart ? 1.0 - (double)split : (double)split));
       if (factor == 0.0) return true;
       f1 = (float)factor;
     }
@@ -463,11 +511,13 @@ struct Lane {
                                             fp.opt.energyLoss != 0, vac);
     if (vac) return true;
     const float signedQ = copysignf(absQ, qOverPf);
+    // the energy decreases forward and increases backward (hpp:185-190)
+    const double eLoss = REV ? -e.eLoss : e.eLoss;
     if constexpr (sizeof(P) == sizeof(double)) {
       // PointwiseMaterialInteraction::updateState (hpp:188-198) in FP64
       const double massd = (double)mass;
       const double mom = absMomentum(absQ, qop);
-      const double nextE = sqrt(massd * massd + mom * mom) - e.eLoss;
+      const double nextE = sqrt(massd * massd + mom * mom) - eLoss;
       double nextP = 0.0;
       if (massd < nextE) {
         const double am = fabs(massd);
@@ -482,10 +532,10 @@ struct Lane {
       const float m = mass;
       const float p = fabsf(signedQ / d2f(qop));
       const float E = sqrtf(m * m + p * p);
-      const float eLoss = (float)e.eLoss;
-      const float nextE = E - eLoss;
+      const float eLossF = (float)eLoss;
+      const float nextE = E - eLossF;
       if (m < nextE && (nextE - m) * (nextE + m) >= 1e-4f) {
-        const float u = -eLoss * (2.0f * E - eLoss) / (p * p);
+        const float u = -eLossF * (2.0f * E - eLossF) / (p * p);
         const float r = sqrtf(1.0f + u);
         const float delta = u / (r * (1.0f + r));  // 1/sqrt(1+u) - 1 = -u/(r(1+r))
         qop = qop - qop * toD(delta);
@@ -669,17 +719,20 @@ struct Lane {
       if (!material(fp, sid, sf, sp, l, 1)) return CK_TRACK_NOT_ON_SURFACE;
       double bp[6];
       if (!freeToBound(fp, sf, l, bp)) return CK_TRACK_NOT_ON_SURFACE;
-      if (nStates >= fp.max_states) return CK_TRACK_TOO_MANY_STATES;
+      // (the reversed pass's states are not part of the track: no records)
+      if (!REV && nStates >= fp.max_states) return CK_TRACK_TOO_MANY_STATES;
       const int k = nStates++;
       double Pp[21];
 #pragma unroll
       for (int i = 0; i < 21; ++i) Pp[i] = toD(cov[i]);
+      if constexpr (!REV) {
 #pragma unroll
-      for (int i = 0; i < 6; ++i) rec.p(k, kRecPred + i) = bp[i];
+        for (int i = 0; i < 6; ++i) rec.p(k, kRecPred + i) = bp[i];
 #pragma unroll
-      for (int i = 0; i < 21; ++i) rec.m(k, kRecPredCov + i) = cov[i];
+        for (int i = 0; i < 21; ++i) rec.m(k, kRecPredCov + i) = cov[i];
 #pragma unroll
-      for (int i = 0; i < 36; ++i) rec.m(k, kRecJac + i) = J[i];
+        for (int i = 0; i < 36; ++i) rec.m(k, kRecJac + i) = J[i];
+      }
       uint32_t flags = CK_FLAG_HAS_PARAMETERS | (hasMat ? CK_FLAG_HAS_MATERIAL : 0u);
       const double mv0 = __ldg(&fp.meas_val[2 * (size_t)mi]);
       const double mv1 = __ldg(&fp.meas_val[2 * (size_t)mi + 1]);
@@ -700,49 +753,62 @@ struct Lane {
         if (!kalmanUpdateSub<kFastRcp>(bp, Pp, sub, mv0, mv1, V, joseph, filt, F, chi2))
           return CK_TRACK_UPDATE_FAILED;
         flags |= CK_FLAG_HAS_MEASUREMENT;
+        if constexpr (REV) {
+          // the latest filtered measurement state of the reversed pass
+          // (findLastMeasurementState of the reversed track)
+          ExtStart& es = fp.ext[2 * (size_t)slot];
 #pragma unroll
-        for (int i = 0; i < 6; ++i) rec.p(k, kRecFilt + i) = filt[i];
+          for (int i = 0; i < 6; ++i) es.par[i] = filt[i];
+#pragma unroll
+          for (int i = 0; i < 21; ++i) es.cov[i] = (double)toP<CV>(F[i]);
+          es.surface = sid;
+        } else {
+#pragma unroll
+          for (int i = 0; i < 6; ++i) rec.p(k, kRecFilt + i) = filt[i];
+        }
         updateFree(sf, bp, filt, l);
 #pragma unroll
         for (int i = 0; i < 21; ++i) {
           cov[i] = toP<CV>(F[i]);
-          rec.m(k, kRecFiltCov + i) = cov[i];
+          if constexpr (!REV) rec.m(k, kRecFiltCov + i) = cov[i];
         }
         initTP(sp);
         local(sf, l);  // the updated position
         ++measurementStates;
-      } else {
+      } else if constexpr (!REV) {
         flags |= CK_FLAG_HAS_MEASUREMENT | CK_FLAG_IS_OUTLIER;
 #pragma unroll
         for (int i = 0; i < 6; ++i) rec.p(k, kRecFilt + i) = bp[i];
 #pragma unroll
         for (int i = 0; i < 21; ++i) rec.m(k, kRecFiltCov + i) = cov[i];
       }
-      writeMeta(fp, slot, k, sid, flags, chi2);
+      if constexpr (!REV) writeMeta(fp, slot, k, sid, flags, chi2);
       if (!material(fp, sid, sf, sp, l, 2)) return CK_TRACK_NOT_ON_SURFACE;
-      lastMeasurementIndex = k;
+      if constexpr (!REV) lastMeasurementIndex = k;
     } else if ((preceding && sensitive) || hasMat) {
       double bp[6];
       if (!freeToBound(fp, sf, l, bp)) return CK_TRACK_NOT_ON_SURFACE;
       CV J[36];
       transportToBound(sf, sp, l, J, fp.opt.freeToBoundCorrection != 0);
-      if (nStates >= fp.max_states) return CK_TRACK_TOO_MANY_STATES;
-      const int k = nStates++;
+      if constexpr (!REV) {
+        if (nStates >= fp.max_states) return CK_TRACK_TOO_MANY_STATES;
+        const int k = nStates++;
 #pragma unroll
-      for (int i = 0; i < 6; ++i) {
-        rec.p(k, kRecPred + i) = bp[i];
-        rec.p(k, kRecFilt + i) = bp[i];
+        for (int i = 0; i < 6; ++i) {
+          rec.p(k, kRecPred + i) = bp[i];
+          rec.p(k, kRecFilt + i) = bp[i];
+        }
+#pragma unroll
+        for (int i = 0; i < 21; ++i) {
+          rec.m(k, kRecPredCov + i) = cov[i];
+          rec.m(k, kRecFiltCov + i) = cov[i];
+        }
+#pragma unroll
+        for (int i = 0; i < 36; ++i) rec.m(k, kRecJac + i) = J[i];
+        uint32_t flags = CK_FLAG_HAS_PARAMETERS | (hasMat ? CK_FLAG_HAS_MATERIAL : 0u);
+        if (sensitive && preceding) flags |= CK_FLAG_IS_HOLE;
+        writeMeta(fp, slot, k, sid, flags, 0.0);
       }
-#pragma unroll
-      for (int i = 0; i < 21; ++i) {
-        rec.m(k, kRecPredCov + i) = cov[i];
-        rec.m(k, kRecFiltCov + i) = cov[i];
-      }
-#pragma unroll
-      for (int i = 0; i < 36; ++i) rec.m(k, kRecJac + i) = J[i];
-      uint32_t flags = CK_FLAG_HAS_PARAMETERS | (hasMat ? CK_FLAG_HAS_MATERIAL : 0u);
-      if (sensitive && preceding) flags |= CK_FLAG_IS_HOLE;
-      writeMeta(fp, slot, k, sid, flags, 0.0);
       if (!material(fp, sid, sf, sp, l, 3)) return CK_TRACK_NOT_ON_SURFACE;
     }
     return CK_TRACK_OK;
@@ -758,15 +824,40 @@ struct Lane {
       if (r != CK_TRACK_OK) return r;
     }
     bool complete = measurementStates == nDistinct;
-    if (!complete && lastSlSeq >= 0 && currentSurface >= 0 && surfaceIndex >= lastSlSeq) {
+    if (!complete && lastSlSeq >= 0 && currentSurface >= 0 &&
+        (REV ? surfaceIndex <= lastSlSeq : surfaceIndex >= lastSlSeq)) {
       // every later state would lie beyond the track's tip
       if (fp.opt.earlyTermination)
         complete = true;
-      else
-        coasting = true;
+      else if (!REV || fp.ref_surface < 0)
+        coasting = true;  // (a reversed pass that may reach its target keeps its covariance)
     }
     const bool pathReached = pathLimitReached(fp, kfLimit);
-    if (complete || pathReached) finished = true;
+    bool targetReached = false;
+    if constexpr (REV) {
+      if (fp.ref_surface >= 0) {
+        // Actor::targetReached, a SurfaceReached on the reference surface
+        // with an unlimited near limit (StandardAborters.hpp:94-155): its
+        // distance becomes the actor step constraint
+        Surf<double> ts;
+        ts.load(fp.surfaces + fp.ref_surface);
+        const double nd[3] = {-dir[0], -dir[1], -dir[2]};
+        const double tol = fp.opt.surfaceTolerance;
+        double u = 0.0;
+        if (lineIntersect(ts, pos, nd, tol, u)) {
+          cActor = kNotSet;
+          cupdate(cActor, u);
+          targetReached = !(fabs(u) > fabs(tol));
+        }
+        if (targetReached) {
+          // the fitted parameters: the bound state on the target
+          // (KalmanFitter.hpp:398-412)
+          if (!writeReferenceState(fp)) return CK_TRACK_NOT_ON_SURFACE;
+          fp.ext[2 * (size_t)slot].fitted = 1;
+        }
+      }
+    }
+    if (complete || pathReached || targetReached) finished = true;
     return CK_TRACK_OK;
   }
 
@@ -870,11 +961,17 @@ struct Lane {
     surfaceIndex = -1;
     navigationBreak = false;
     currentSurface = -1;
+    prePropagation(fp, slot);
+  }
+
+  // the common tail of both passes' initialisation: the actor's first call,
+  // the abort check and the first navigation target
+  CK_D void prePropagation(const FitParams& fp, int slot) {
     targetSurf = -1;
     targetIdx = 0;
     haveTarget = false;
     nStates = 0;
-    lastMeasurementIndex = -1;
+    if constexpr (!REV) lastMeasurementIndex = -1;
     measurementStates = 0;
     finished = false;
     coasting = false;
@@ -898,6 +995,90 @@ struct Lane {
     phase = PH_STEP;
   }
 
+  // FETCH of the reversed pass (KalmanFitter.hpp:901-911): the start
+  // parameters are the forward pass's last measurement state's filtered ones
+  // (its smoothed parameters share them), the covariance scaled by
+  // reverseFilteringCovarianceScaling; the DirectNavigator starts on that
+  // surface (DirectNavigator.hpp:238-262) and the first actor call filters
+  // it. Tracks the forward pass failed are skipped.
+  CK_D void startReverse(const FitParams& fp, int slot, int track) {
+    t = track;
+    const int tip = fp.tip[slot];
+    if (tip < 0 || !reverseSelected<CV>(fp, slot, tip)) {
+      phase = PH_FETCH;
+      return;
+    }
+    seq0 = __ldg(&fp.seq_off[t]);
+    nSeq = __ldg(&fp.seq_off[t + 1]) - seq0;
+    m0 = __ldg(&fp.meas_off[t]);
+    nMeas = __ldg(&fp.meas_off[t + 1]) - m0;
+    const Rec<CV> rec(fp, slot);
+    int last = tip;
+    for (int k = tip; k >= 0; --k) {
+      const uint32_t fl = (uint32_t)rec.s(k).flags;
+      if ((fl & CK_FLAG_HAS_MEASUREMENT) && !(fl & CK_FLAG_IS_OUTLIER)) {
+        last = k;
+        break;
+      }
+    }
+    const int sid = rec.s(last).surface;
+    {
+      Surf<double> sf;
+      sf.load(fp.surfaces + sid);
+      double b[6];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) b[i] = rec.p(last, kRecFilt + i);
+      boundToFree(sf, b);
+      initT(sf);
+      const CV scale = (CV)fp.opt.reverseCovScaling;
+#pragma unroll
+      for (int i = 0; i < 21; ++i) cov[i] = rec.m(last, kRecFiltCov + i) * scale;
+    }
+    ExtStart& es = fp.ext[2 * (size_t)slot];
+    es.surface = -1;
+    es.fitted = 0;
+#pragma unroll
+    for (int i = 0; i < 7; ++i) deriv[i] = P(0);
+    pathAcc = 0.0;
+    cNav = kNotSet;
+    cActor = kNotSet;
+    cUser = fp.opt.maxStepSize;
+    cAcc = fp.opt.initialStepSize;
+    mass = __ldg(&fp.particle[2 * (size_t)t]);
+    absQ = __ldg(&fp.particle[2 * (size_t)t + 1]);
+    pdg = fp.pdg ? __ldg(&fp.pdg[t]) : 211;
+    nDistinct = 0;
+    for (int i = 0; i < nMeas; ++i) {
+      const int si = __ldg(&fp.meas_surf[m0 + i]);
+      bool dup = false;
+      for (int j = 0; j < i; ++j) dup |= (__ldg(&fp.meas_surf[m0 + j]) == si);
+      nDistinct += dup ? 0 : 1;
+    }
+    // the first sequence position that carries a source link
+    lastSlSeq = -1;
+    for (int k = 0; k < nSeq; ++k)
+      if (findMeas(fp, __ldg(&fp.seq_surf[seq0 + k])) >= 0) {
+        lastSlSeq = k;
+        break;
+      }
+    measHint = 0;
+    dirSign = -1.0;
+    extrapolating = false;
+    propLimit = loopLimit(fp, fp.opt.pathLimit, false);
+    kfLimit = kNotSet;
+    // the position after the start surface's first occurrence, or the end
+    surfaceIndex = nSeq;
+    for (int k = 0; k < nSeq; ++k)
+      if (__ldg(&fp.seq_surf[seq0 + k]) == sid) {
+        surfaceIndex = k + 1;
+        break;
+      }
+    navigationBreak = false;
+    currentSurface = sid;
+    startSid = sid;
+    prePropagation(fp, slot);
+  }
+
   // STEP: one Runge-Kutta trial (EigenStepper::step, EigenStepper.ipp:168-388)
   // EXTRAP: the lane extrapolates to the reference surface (signed step
   // direction, the aborters after each step); the fit kernels instantiate
@@ -911,7 +1092,7 @@ struct Lane {
         return;
       }
       initialH = stepValue();
-      if constexpr (EXTRAP) initialH *= dirSign;  // EigenStepper.ipp:272
+      if constexpr (EXTRAP || REV) initialH *= dirSign;  // EigenStepper.ipp:272
       hd = initialH;
       trials = 0;
       stepStarted = true;
@@ -1205,11 +1386,21 @@ struct Lane {
     return pathLimitReached(fp, propLimit);
   }
 
-  // Propagator::makeResult -> EigenStepper::boundState on the target:
+  CK_D void finishExtrapolation(const FitParams& fp) {
+    if (!writeReferenceState(fp)) {
+      fail(fp, CK_TRACK_NOT_ON_SURFACE);
+      return;
+    }
+    phase = PH_DONE;
+  }
+
+  // EigenStepper::boundState on the reference surface, written as the
+  // track's parameters and covariance:
   // J = F2B (I + derivative x freeToPath) T with the line surface's frame and
   // path derivative (LineSurface.cpp:102-115,224-251), C <- J C J^T, and the
-  // bound parameters (LineSurface::globalToLocal, LineSurface.cpp:70-96)
-  CK_D void finishExtrapolation(const FitParams& fp) {
+  // bound parameters (LineSurface::globalToLocal, LineSurface.cpp:70-96);
+  // false when the position is not on the line
+  CK_D bool writeReferenceState(const FitParams& fp) {
     Surf<double> ts;
     ts.load(fp.surfaces + fp.ref_surface);
     const double z0[3] = {ts.R[2], ts.R[5], ts.R[8]};
@@ -1221,10 +1412,8 @@ struct Lane {
     const double dist[3] = {d0[1] * z0[2] - d0[2] * z0[1], d0[2] * z0[0] - d0[0] * z0[2],
                             d0[0] * z0[1] - d0[1] * z0[0]};
     const double pc[3] = {pos[0] - ts.c[0], pos[1] - ts.c[1], pos[2] - ts.c[2]};
-    if (fabs(dist[0] * pc[0] + dist[1] * pc[1] + dist[2] * pc[2]) > fabs(kOnSurfaceTolerance)) {
-      fail(fp, CK_TRACK_NOT_ON_SURFACE);
-      return;
-    }
+    if (fabs(dist[0] * pc[0] + dist[1] * pc[1] + dist[2] * pc[2]) > fabs(kOnSurfaceTolerance))
+      return false;
     // path derivative of the line surface
     const double pz = pc[0] * z0[0] + pc[1] * z0[1] + pc[2] * z0[2];
     const double dz = z0[0] * dir[0] + z0[1] * dir[1] + z0[2] * dir[2];
@@ -1297,7 +1486,7 @@ struct Lane {
 #pragma unroll
       for (int i = 0; i < 6; ++i) out.track_params[(size_t)i * n + t] = b[i];
     }
-    phase = PH_DONE;
+    return true;
   }
 
   // SURFACE: the actor on the reached surface
@@ -1311,13 +1500,29 @@ struct Lane {
   }
 
   // end of propagation: NoMeasurementFound, or the track's tip is handed to
-  // the smoother kernel
+  // the smoother kernel. The reversed pass instead checks that its last
+  // measurement state lies on the forward pass's first one's surface
+  // (KalmanFitter.hpp:920-932); the output kernel then takes the track.
   CK_D void endPropagation(const FitParams& fp, int slot) {
     if (measurementStates == 0) {
       fail(fp, CK_TRACK_NO_MEASUREMENT_FOUND);
       return;
     }
-    fp.tip[slot] = lastMeasurementIndex;
+    if constexpr (REV) {
+      const Rec<CV> rec(fp, slot);
+      const int tip = fp.tip[slot];
+      int firstSurf = -1;
+      for (int k = 0; k <= tip && firstSurf < 0; ++k) {
+        const uint32_t fl = (uint32_t)rec.s(k).flags;
+        if ((fl & CK_FLAG_HAS_MEASUREMENT) && !(fl & CK_FLAG_IS_OUTLIER)) firstSurf = rec.s(k).surface;
+      }
+      if (fp.ext[2 * (size_t)slot].surface != firstSurf) {
+        fail(fp, CK_TRACK_INCONSISTENT_STATES);
+        return;
+      }
+    } else {
+      fp.tip[slot] = lastMeasurementIndex;
+    }
     phase = PH_FETCH;
   }
 };
@@ -1343,6 +1548,7 @@ struct Smoother {
       // state with a non-outlier measurement (findFirst/LastMeasurementState,
       // TrackHelpers.hpp:64-102); none yet
       fp.ext[2 * (size_t)q].surface = -1;
+      fp.ext[2 * (size_t)q].fitted = 0;
       fp.ext[2 * (size_t)q + 1].surface = -1;
       for (int k = 0; k <= tip; ++k) {
         const uint32_t fl = (uint32_t)rec.s(k).flags;
@@ -1454,6 +1660,57 @@ struct Smoother {
       for (int i = 0; i < 36; ++i) F[i] = rec.m(k, kRecJac + i);
       mbfTransport<CV>(F, L, l);
     }
+  }
+
+  // The output of a reverse-filtered track (KalmanFitter.hpp:889-945): every
+  // state's predicted and filtered parameters and Jacobian as the forward
+  // pass recorded them; smoothed parameters only on the last measurement
+  // state (its filtered ones, shared) and on the first (the reversed pass's
+  // last filtered state, extrapolation slot 0, which wins when the two are
+  // one state); every other state's smoothed parameters are NaN.
+  CK_D void runReverse(const FitParams& fp, int queuePos, int track, int tip) {
+    t = track;
+    q = queuePos;
+    const Rec<CV> rec(fp, q);
+    firstMeas = -1;
+    lastMeas = tip;
+    for (int k = 0; k <= tip && firstMeas < 0; ++k) {
+      const uint32_t fl = (uint32_t)rec.s(k).flags;
+      if ((fl & CK_FLAG_HAS_MEASUREMENT) && !(fl & CK_FLAG_IS_OUTLIER)) firstMeas = k;
+    }
+    for (int k = tip; k >= 0; --k) {
+      const uint32_t fl = (uint32_t)rec.s(k).flags;
+      if ((fl & CK_FLAG_HAS_MEASUREMENT) && !(fl & CK_FLAG_IS_OUTLIER)) {
+        lastMeas = k;
+        break;
+      }
+    }
+    fp.ext[2 * (size_t)q + 1].surface = -1;
+    nM = nH = nO = ndf = 0;
+    chi2sum = 0.0;
+    const ExtStart& rv = fp.ext[2 * (size_t)q];
+    for (int k = 0; k <= tip; ++k) {
+      double sm[6];
+      CV Ps[21];
+      if (k == firstMeas) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) sm[i] = rv.par[i];
+#pragma unroll
+        for (int i = 0; i < 21; ++i) Ps[i] = (CV)rv.cov[i];
+      } else if (k == lastMeas) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) sm[i] = rec.p(k, kRecFilt + i);
+#pragma unroll
+        for (int i = 0; i < 21; ++i) Ps[i] = rec.m(k, kRecFiltCov + i);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) sm[i] = CUDART_NAN;
+#pragma unroll
+        for (int i = 0; i < 21; ++i) Ps[i] = (CV)CUDART_NAN;
+      }
+      writeState(fp, k, sm, Ps, false);
+    }
+    finish(fp, tip);
   }
 
   // status and calculateTrackQuantities (TrackHelpers.hpp:421-448)
@@ -1613,8 +1870,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) fitKernel(FitParams fp) {
 // carries are the FP64 throughput it gets.
 // One phase step of a slot; fetching threads take one ticket per warp (the
 // threads of the warp that run this call together).
-template <typename P, typename CV, bool F2B>
-__device__ __forceinline__ void advanceSlot(const FitParams& fp, Lane<P, CV, F2B>& L, int c,
+template <typename P, typename CV, bool F2B, bool REV>
+__device__ __forceinline__ void advanceSlot(const FitParams& fp, Lane<P, CV, F2B, REV>& L, int c,
                                             int lane) {
   if (c == PH_FETCH) {
     const unsigned act = __activemask();
@@ -1627,7 +1884,10 @@ __device__ __forceinline__ void advanceSlot(const FitParams& fp, Lane<P, CV, F2B
       L.phase = PH_DONE;
     } else {
       L.q = q;
-      L.start(fp, q, fp.perm ? __ldg(&fp.perm[q]) : q);
+      if constexpr (REV)
+        L.startReverse(fp, q, fp.perm ? __ldg(&fp.perm[q]) : q);
+      else
+        L.start(fp, q, fp.perm ? __ldg(&fp.perm[q]) : q);
     }
   } else if (c == PH_STEP) {
     // up to steps_per_round Runge-Kutta trials while the track stays in STEP
@@ -1637,11 +1897,12 @@ __device__ __forceinline__ void advanceSlot(const FitParams& fp, Lane<P, CV, F2B
   }
 }
 
-template <typename P, typename CV, int S, bool F2B = false>
+template <typename P, typename CV, int S, bool F2B = false, bool REV = false>
 __global__ void __launch_bounds__(S, 1) fitKernelCompact(FitParams fp) {
   extern __shared__ __align__(16) unsigned char smem[];
-  Lane<P, CV, F2B>* st = reinterpret_cast<Lane<P, CV, F2B>*>(smem);
-  int* items = reinterpret_cast<int*>(smem + sizeof(Lane<P, CV, F2B>) * S);
+  using LaneT = Lane<P, CV, F2B, REV>;
+  LaneT* st = reinterpret_cast<LaneT*>(smem);
+  int* items = reinterpret_cast<int*>(smem + sizeof(LaneT) * S);
   __shared__ int warpCnt[S / 32][3];
   __shared__ int chosen, nItems;
   const unsigned FULL = 0xffffffffu;
@@ -1688,7 +1949,7 @@ __global__ void __launch_bounds__(S, 1) fitKernelCompact(FitParams fp) {
     if (tid < nItems) {
       const int slot = items[tid];
       // the phase step works on a register copy of the slot's state
-      Lane<P, CV, F2B> L = st[slot];
+      LaneT L = st[slot];
       advanceSlot(fp, L, c, lane);
       st[slot] = L;
     }
@@ -1703,12 +1964,27 @@ constexpr size_t compactSmemBytes() {
 
 // Smoother kernel: one lane per queue position; lanes of a warp hold tracks
 // of similar length (the queue is ordered by sequence length).
+// Output kernel of reverse filtering, after the reversed pass: one lane per
+// queue position, for the tracks both passes fitted.
+template <typename CV, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) reverseOutputKernel(FitParams fp) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < fp.n_queue;
+       q += gridDim.x * blockDim.x) {
+    const int tip = fp.tip[q];
+    if (tip < 0 || !reverseSelected<CV>(fp, q, tip)) continue;
+    Smoother<CV> S;
+    S.runReverse(fp, q, fp.perm ? __ldg(&fp.perm[q]) : q, tip);
+  }
+}
+
 template <typename CV, int BLOCK>
 __global__ void __launch_bounds__(BLOCK) smoothKernel(FitParams fp) {
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < fp.n_queue;
        q += gridDim.x * blockDim.x) {
     const int tip = fp.tip[q];
     if (tip < 0) continue;
+    // (tracks the reverse-filtering logic selects take the reversed pass)
+    if (fp.opt.reverseMomThreshold > 0.0 && reverseSelected<CV>(fp, q, tip)) continue;
     Smoother<CV> S;
     S.run(fp, q, fp.perm ? __ldg(&fp.perm[q]) : q, tip);
   }

@@ -63,6 +63,8 @@ struct DevOptions {
   int useOutlierCut, earlyTermination;
   int smoother;  // CK_SMOOTHER_*
   int freeToBoundCorrection;
+  int reverseFiltering;
+  double reverseCovScaling, reverseMomThreshold;
 };
 
 // Record of one forward track state kept for the smoother (scratch), one
@@ -97,12 +99,16 @@ static_assert(sizeof(RecState<double>) == 744, "record layout");
 // A track state the extrapolation to the reference surface may start from
 // (the first and the last state with a non-outlier measurement, slots 0 and
 // 1 of each queue position): its surface and smoothed parameters and
-// covariance (packed upper) in FP64. Written by the smoother.
+// covariance (packed upper) in FP64. Written by the smoother; with reverse
+// filtering, slot 0 holds the reversed pass's last filtered state (written by
+// that pass) and is also the first measurement state's smoothed output.
 struct ExtStart {
   double par[6];
   double cov[21];
   int32_t surface;  // -1: no such state
-  int32_t pad;
+  // slot 0 with reverse filtering: 1 when the reversed pass reached the
+  // reference surface and wrote the track parameters itself
+  int32_t fitted;
 };
 static_assert(sizeof(ExtStart) == 224, "extrapolation start layout");
 

@@ -83,7 +83,9 @@ cudaError_t configureMixed();
 
 cudaError_t configureFitKernels() {
   cudaError_t e = configureFP64();
-  return e != cudaSuccess ? e : configureMixed();
+  if (e == cudaSuccess) e = configureMixed();
+  if (e == cudaSuccess) e = configureReverseFP64();
+  return e != cudaSuccess ? e : configureReverseMixed();
 }
 
 int occupancyBlocks(int precision, int variant, int tpb) {

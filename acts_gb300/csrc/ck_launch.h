@@ -39,6 +39,23 @@ inline cudaError_t launchSmooth(const FitParams& fp, int precision, cudaStream_t
   return precision == CK_PRECISION_MIXED ? launchSmoothMixed(fp, st) : launchSmoothFP64(fp, st);
 }
 constexpr int kSmoothBlock = 128;
+// reverse filtering (ck_reverse_*.cu): the reversed filter pass, then the
+// output kernel in place of the smoother; the pass needs the queue ticket
+// cleared and the extrapolation start slots
+cudaError_t launchReverseFP64(const FitParams& fp, int grid, cudaStream_t st);
+cudaError_t launchReverseMixed(const FitParams& fp, int grid, cudaStream_t st);
+cudaError_t launchReverseOutputFP64(const FitParams& fp, cudaStream_t st);
+cudaError_t launchReverseOutputMixed(const FitParams& fp, cudaStream_t st);
+cudaError_t configureReverseFP64();
+cudaError_t configureReverseMixed();
+inline cudaError_t launchReverse(const FitParams& fp, int precision, int grid, cudaStream_t st) {
+  return precision == CK_PRECISION_MIXED ? launchReverseMixed(fp, grid, st)
+                                         : launchReverseFP64(fp, grid, st);
+}
+inline cudaError_t launchReverseOutput(const FitParams& fp, int precision, cudaStream_t st) {
+  return precision == CK_PRECISION_MIXED ? launchReverseOutputMixed(fp, st)
+                                         : launchReverseOutputFP64(fp, st);
+}
 // extrapolation of every successfully smoothed track to the reference
 // surface (FP64 in both forms; ck_extrapolate.cu)
 cudaError_t launchExtrapolate(const FitParams& fp, cudaStream_t st);

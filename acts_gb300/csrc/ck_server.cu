@@ -159,7 +159,8 @@ struct ck_server {
     if (spec.fi) out += (size_t)maxStates * 42 * 8;
     if (spec.pr) out += (size_t)maxStates * 42 * 8;
     if (spec.jac) out += (size_t)maxStates * 36 * 8;
-    if (opt.reference_surface >= 0) out += 42 * 8 + 2 * sizeof(ExtStart);
+    if (opt.reference_surface >= 0) out += 42 * 8;
+    if (needsExtStart(opt)) out += 2 * sizeof(ExtStart);
     return in + out + recordBytesPerTrack(maxStates, opt.precision);
   }
   bool computes(int field) const {
@@ -207,7 +208,7 @@ ck_status slotAlloc(ck_server* s, Slot& sl) {
     return cudaFail(e, "server pinned buffers");
   sl.pinOutBytes = pout;
   return preparePipeline(s->h, sl.ctx, s->capacity, ms, s->opt.precision,
-                         s->opt.reference_surface >= 0);
+                         needsExtStart(s->opt));
 }
 
 // Offsets of the staged result arrays in the slot's pinned buffer.

@@ -110,7 +110,7 @@ ck_status ck_fit_batch_static(ck_handle* h, const ck_options* opt, const ck_batc
       (out->smoothed && !out->smoothed_cov))
     return fail(CK_ERR_INVALID_ARGUMENT, "parameter arrays need their covariance arrays");
   const int n = in->n_tracks;
-  const Layout l = layoutFor(n, out->max_states, opt->precision, opt->reference_surface >= 0);
+  const Layout l = layoutFor(n, out->max_states, opt->precision, needsExtStart(*opt));
   if (l.total > kStaticScratchBytes)
     return fail(CK_ERR_SCRATCH_LIMIT,
                 "batch needs " + std::to_string(l.total) + " bytes of scratch; the static scratch "

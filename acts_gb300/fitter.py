@@ -107,6 +107,8 @@ class KalmanFitterOptions:
     multiple_scattering: bool = True
     energy_loss: bool = True
     reverse_filtering: bool = False
+    reverse_filtering_cov_scaling: float = 100.0
+    reverse_filtering_mom_threshold: float = 0.0  # GeV (the examples' reverseFilteringMomThreshold)
     free_to_bound_correction: bool = False
     reference_surface: int = -1  # a line (perigee) surface of the table, or -1
     reference_strategy: int = abi.EXTRAPOLATE_FIRST_OR_LAST
@@ -127,6 +129,8 @@ class KalmanFitterOptions:
         o.multiple_scattering = int(self.multiple_scattering)
         o.energy_loss = int(self.energy_loss)
         o.reverse_filtering = int(self.reverse_filtering)
+        o.reverse_filtering_cov_scaling = float(self.reverse_filtering_cov_scaling)
+        o.reverse_filtering_mom_threshold = float(self.reverse_filtering_mom_threshold)
         o.free_to_bound_correction = int(self.free_to_bound_correction)
         o.reference_surface = int(self.reference_surface)
         o.reference_strategy = int(self.reference_strategy)

@@ -67,6 +67,9 @@ inline const char* errorName(int code) {
     case CK_TRACK_TOO_MANY_STATES: return "TooManyStates";
     case CK_TRACK_NOT_PROCESSED: return "NotProcessed";
     case CK_TRACK_INVALID_INPUT: return "InvalidInput";
+    case CK_TRACK_NO_COMPATIBLE_STATE: return "CompatibleTrackStateNotFound";
+    case CK_TRACK_REFERENCE_UNREACHABLE: return "ReferenceSurfaceUnreachable";
+    case CK_TRACK_INCONSISTENT_STATES: return "InconsistentTrackStates";
     default: return "ok";
   }
 }

@@ -84,7 +84,10 @@ enum {
   /* extrapolation to the reference surface (TrackExtrapolationError,
    * Core/include/Acts/Utilities/TrackHelpers.hpp:48-53) */
   CK_TRACK_NO_COMPATIBLE_STATE = 13,  /* CompatibleTrackStateNotFound      */
-  CK_TRACK_REFERENCE_UNREACHABLE = 14 /* ReferenceSurfaceUnreachable       */
+  CK_TRACK_REFERENCE_UNREACHABLE = 14, /* ReferenceSurfaceUnreachable      */
+  /* KalmanFitterError::InconsistentTrackStates: the reversed filter's last
+   * measurement state is not on the forward filter's first one's surface */
+  CK_TRACK_INCONSISTENT_STATES = 15
 };
 
 /* Track-state type flags, bit positions of Acts::TrackStateFlag
@@ -203,9 +206,17 @@ typedef struct ck_options {
   int32_t use_joseph;           /* 0 (GainMatrixUpdater default)           */
   int32_t precision;            /* CK_PRECISION_*                          */
   double outlier_chi2_cut;      /* +inf                                    */
-  /* Reverse filtering is outside the declared set and rejected with
-   * CK_ERR_UNSUPPORTED. */
-  int32_t reverse_filtering;    /* must be 0                               */
+  /* KalmanFitterOptions::reverseFiltering (KalmanFitter.hpp:897-945): 1
+   * (for every track; see also reverse_filtering_mom_threshold) replaces the
+   * smoother by a second filter pass backwards along the
+   * sequence, started from the last measurement state with its covariance
+   * scaled by reverse_filtering_cov_scaling and aimed at reference_surface.
+   * Only the first measurement state receives smoothed parameters (the
+   * reversed pass's last filtered ones) and the last one its own filtered
+   * parameters; every other state's smoothed parameters are NaN. The track
+   * parameters come from the reversed pass when it reached the reference
+   * surface, else from the extrapolation. Default 0. */
+  int32_t reverse_filtering;
   /* KalmanFitterOptions::freeToBoundCorrection (FreeToBoundCorrection with
    * its defaults: alpha 0.1, beta 2, incidence window [1e-5, 0.99500417]):
    * the covariance transport to each state's surface goes through the
@@ -232,6 +243,15 @@ typedef struct ck_options {
   /* KalmanFitterOptions::referenceSurfaceStrategy (TrackExtrapolationStrategy):
    * the track state the extrapolation starts from; default FIRST_OR_LAST. */
   int32_t reference_strategy;
+  /* KalmanFitterOptions::reverseFilteringCovarianceScaling: 100 */
+  double reverse_filtering_cov_scaling;
+  /* KalmanFitterExtensions::reverseFilteringLogic as the examples' fitter
+   * function connects it (SimpleReverseFilteringLogic,
+   * Examples/Algorithms/TrackFitting/src/KalmanFitterFunction.cpp:50-58):
+   * with reverse_filtering 0, a track is reverse-filtered when its last
+   * measurement state's filtered momentum 1/|q/p| is at most this threshold
+   * (GeV). Default 0: no track. */
+  double reverse_filtering_mom_threshold;
 } ck_options;
 
 enum { CK_EXTRAPOLATE_FIRST = 0, CK_EXTRAPOLATE_LAST = 1, CK_EXTRAPOLATE_FIRST_OR_LAST = 2 };

@@ -972,8 +972,14 @@ struct Options {
   int referenceSurface;            // -1 or a table index
   int referenceStrategy;           // CK_EXTRAPOLATE_*
   bool freeToBoundCorrection;      // KalmanFitterOptions::freeToBoundCorrection
+  bool reverseFiltering;           // KalmanFitterOptions::reverseFiltering
+  double reverseCovScaling;        // reverseFilteringCovarianceScaling
+  double reverseMomThreshold;      // the examples' reverseFilteringLogic threshold
   static Options fromCk(const ck_options& o, bool coast) {
     Options r;
+    r.reverseFiltering = o.reverse_filtering != 0;
+    r.reverseCovScaling = o.reverse_filtering_cov_scaling;
+    r.reverseMomThreshold = o.reverse_filtering_mom_threshold;
     r.freeToBoundCorrection = o.free_to_bound_correction != 0;
     r.smoother = o.smoother;
     r.referenceSurface = o.reference_surface;
@@ -1779,9 +1785,31 @@ struct Fitter {
     return CK_TRACK_OK;
   }
 
-  int fit(const Surface<S>& startSurface, const Vec<S, 6>& startPars, const Mat<S, 6, 6>& startCov,
-          float mass, float absQ, int absPdg, const int* seq, int nSeq,
-          const std::vector<MeasRec<S>>& meas, TrackOut& out) const {
+  // The outcome of one filter pass (KalmanFitter::filter_impl,
+  // KalmanFitter.hpp:794-848): its track states, the index of the last state
+  // with a measurement, the number of non-outlier measurement states, and the
+  // bound state on the target surface when the pass reached it
+  // (KalmanFitter.hpp:398-412).
+  struct Pass {
+    std::vector<IState> states;
+    int lastMeasurementIndex = -1;
+    int measurementStates = 0;
+    bool fitted = false;
+    Vec<S, 6> fittedPars;
+    Mat<S, 6, 6> fittedCov;
+  };
+
+  // One propagation of the Kalman actor along the surface sequence: forward
+  // (propDir +1) from a start surface outside the sequence (startSid -2), or
+  // backward (propDir -1) from the sequence surface startSid, which the
+  // first actor call filters with its own measurement (the DirectNavigator
+  // starts on it, DirectNavigator.hpp:238-262). `target` >= 0 is the
+  // reversed pass's target surface (Actor::targetReached, a SurfaceReached
+  // with an unlimited near limit, KalmanFitter.hpp:292, :384-412).
+  int filterPass(const Surface<S>& startSurface, int startSid, const Vec<S, 6>& startPars,
+                 const Mat<S, 6, 6>& startCov, float mass, float absQ, int absPdg,
+                 const int* seq, int nSeq, const std::vector<MeasRec<S>>& meas, int propDir,
+                 int target, Pass& p) const {
     using std::abs;
     const std::vector<Surface<S>>& sf = *surfaces;
     // measurement map (first source link per surface wins, :750-755)
@@ -1797,10 +1825,13 @@ struct Fitter {
       nDistinct += dup ? 0 : 1;
     }
     // surfaces of the sequence that carry a source link: the early
-    // termination point used when not coasting
-    int lastSlSeq = -1;
+    // termination points used when not coasting
+    int lastSlSeq = -1, firstSlSeq = -1;
     for (int k = 0; k < nSeq; ++k)
-      if (findMeas(seq[k]) >= 0) lastSlSeq = k;
+      if (findMeas(seq[k]) >= 0) {
+        lastSlSeq = k;
+        if (firstSlSeq < 0) firstSlSeq = k;
+      }
 
     Stepper<S> st;
     st.mass = mass;
@@ -1836,14 +1867,28 @@ struct Fitter {
     double propPathLimit = loopLimit(o.pathLimit, false);
     double kfPathLimit = std::numeric_limits<double>::max();
 
-    // navigator state
-    int surfaceIndex = -1;  // start surface is not part of the sequence
+    // navigator state (DirectNavigator::initialize, DirectNavigator.hpp:
+    // 238-262): the index before the start surface in the direction of
+    // travel, or one end of the sequence when the start surface is not in it
+    int surfaceIndex = propDir > 0 ? -1 : nSeq;
+    for (int k = 0; startSid >= 0 && k < nSeq; ++k)
+      if (seq[k] == startSid) {
+        surfaceIndex = k - propDir;
+        break;
+      }
     bool navigationBreak = false;
-    int currentSurface = -2;  // -2: start surface, -1: none, >= 0: table id
+    int currentSurface = startSid;  // -2: start surface, -1: none, >= 0: table id
     int targetSurf = -1, targetIdx = 0;
     bool haveTarget = false;
+    // the direction the navigator and the aborters intersect along
+    auto navDir = [&]() -> V3<S> {
+      V3<S> d = st.dir();
+      if (propDir < 0)
+        for (int i = 0; i < 3; ++i) d[i] = -d[i];
+      return d;
+    };
 
-    std::vector<IState> states;
+    std::vector<IState>& states = p.states;
     int lastTrackIndex = -1, lastMeasurementIndex = -1;
     int measurementStates = 0;
     int missedActive = 0;
@@ -1865,9 +1910,12 @@ struct Fitter {
     };
 
     // PointwiseMaterialInteraction.hpp:162-274 ; mode factors from
-    // ISurfaceMaterial.cpp:18-27 (forward propagation)
-    auto material = [&](const Surface<S>& s, int mode) -> bool {
-      // mode: 1 pre, 2 post, 3 full
+    // ISurfaceMaterial.cpp:18-27 by the direction of travel; on the start
+    // surface only the post-update part applies
+    // (PointwiseMaterialInteraction.cpp:16-29)
+    auto material = [&](int sid, const Surface<S>& s, int mode) -> bool {
+      // mode: 0 none, 1 pre, 2 post, 3 full
+      if (sid == startSid) mode &= 2;
       if (!s.hasMaterial) return true;
       V3<S> pos = st.pos(), dir = st.dir();
       S pc = s.pathCorrection(pos, dir);
@@ -1875,7 +1923,11 @@ struct Fitter {
       if (!s.globalToLocal(pos, st.dir(), S(kOnSurfaceTolerance), loc)) return false;
       Slab slab = s.slab;
       if (!slab.isVacuum()) {
-        double factor = (mode == 3) ? 1.0 : (mode == 1 ? 1.0 - s.splitFactor : (double)s.splitFactor);
+        const double split = (double)s.splitFactor;
+        const bool pre = mode == 1;
+        double factor = mode == 0   ? 0.0
+                        : mode == 3 ? 1.0
+                                    : ((pre == (propDir > 0)) ? 1.0 - split : split);
         if (factor == 0.0) return true;  // MaterialSlab::Nothing()
         slab.scaleThickness((float)factor);
       }
@@ -1888,7 +1940,7 @@ struct Fitter {
       const double massd = (double)st.mass;
       const double absQd = (double)st.absQ;
       const double momentum = (double)st.absoluteMomentum();
-      const double nextE = std::sqrt(massd * massd + momentum * momentum) - e.eLoss * 1.0;
+      const double nextE = std::sqrt(massd * massd + momentum * momentum) - e.eLoss * double(propDir);
       double nextP = 0.0;
       if (massd < nextE) {
         double am = std::abs(massd);
@@ -1910,7 +1962,7 @@ struct Fitter {
       const int mi = findMeas(sid);
       if (mi >= 0) {
         transportCovarianceToBound(st, s, o.freeToBoundCorrection);
-        if (!material(s, 1)) return CK_TRACK_NOT_ON_SURFACE;
+        if (!material(sid, s, 1)) return CK_TRACK_NOT_ON_SURFACE;
         IState ts;
         ts.surface = sid;
         Vec<S, 6> bp;
@@ -1950,7 +2002,7 @@ struct Fitter {
           st.jacToGlobal = s.boundToFreeJacobian(st.pos(), st.dir());
           ++measurementStates;
         }
-        if (!material(s, 2)) return CK_TRACK_NOT_ON_SURFACE;
+        if (!material(sid, s, 2)) return CK_TRACK_NOT_ON_SURFACE;
         lastMeasurementIndex = lastTrackIndex;
       } else if ((precedingMeasurementExists && s.sensitive) || s.hasMaterial) {
         IState ts;
@@ -1973,7 +2025,7 @@ struct Fitter {
         ts.flags = flags;
         states.push_back(ts);
         lastTrackIndex = (int)states.size() - 1;
-        if (!material(s, 3)) return CK_TRACK_NOT_ON_SURFACE;
+        if (!material(sid, s, 3)) return CK_TRACK_NOT_ON_SURFACE;
       }
       return CK_TRACK_OK;
     };
@@ -1987,11 +2039,48 @@ struct Fitter {
         if (r != CK_TRACK_OK) return r;
       }
       bool complete = measurementStates == nDistinct;
-      if (!o.coastAfterLastMeasurement && !complete && lastSlSeq >= 0 &&
-          currentSurface >= 0 && surfaceIndex >= lastSlSeq)
+      if (!o.coastAfterLastMeasurement && !complete && lastSlSeq >= 0 && currentSurface >= 0 &&
+          (propDir > 0 ? surfaceIndex >= lastSlSeq : surfaceIndex <= firstSlSeq))
         complete = true;  // early termination: later states cannot join the track
       bool pathReached = pathLimitCheck(kfPathLimit);
-      if (complete || pathReached) finished = true;
+      bool targetReached = false;
+      if (target >= 0) {
+        // SurfaceReached::checkAbort (StandardAborters.hpp:94-155): the
+        // closest intersection decides; the first valid one in the (unlimited)
+        // path window steers the actor step size
+        const Surface<S>& ts = sf[target];
+        Intersection<S> is[2];
+        const int ni = ts.intersect(st.pos(), navDir(), S(o.surfaceTolerance), is);
+        // Intersection::closestOrder (Intersection.hpp:132-149)
+        auto closer = [](const Intersection<S>& a, const Intersection<S>& b) {
+          if (!a.valid() && b.valid()) return false;
+          if (a.valid() && !b.valid()) return true;
+          return abs(a.pathLength) < abs(b.pathLength);
+        };
+        int closest = 0;
+        for (int i = 1; i < ni; ++i)
+          if (closer(is[i], is[closest])) closest = i;
+        targetReached = ni > 0 && is[closest].status == IStatus::onSurface;
+        for (int i = 0; i < ni; ++i)
+          if (is[i].valid() &&
+              (double)is[i].pathLength < std::numeric_limits<double>::max() + kOnSurfaceTolerance) {
+            // updateSingleSurfaceStatus (SteppingHelper.hpp:41-78), Actor
+            // step size: on surface or reachable, the same constraint
+            st.stepSize.release(kActor);
+            st.stepSize.update((double)is[i].pathLength, kActor);
+            break;
+          }
+      }
+      if (targetReached) {
+        // stepper.boundState on the target with covariance transport
+        Vec<S, 6> bp;
+        if (!freeToBound(st.pars, sf[target], bp)) return CK_TRACK_NOT_ON_SURFACE;
+        transportCovarianceToBound(st, sf[target]);
+        p.fitted = true;
+        p.fittedPars = bp;
+        p.fittedCov = st.cov;
+      }
+      if (complete || pathReached || targetReached) finished = true;
       return CK_TRACK_OK;
     };
     auto checkAbort = [&]() -> bool {
@@ -2002,11 +2091,11 @@ struct Fitter {
     auto nextTargetNav = [&]() -> bool {
       currentSurface = -1;
       if (navigationBreak) return false;
-      ++surfaceIndex;
-      while (surfaceIndex < nSeq) {
+      surfaceIndex += propDir;
+      while (surfaceIndex >= 0 && surfaceIndex < nSeq) {
         const Surface<S>& s = sf[seq[surfaceIndex]];
         Intersection<S> is[2];
-        int ni = s.intersect(st.pos(), st.dir(), S(o.surfaceTolerance), is);
+        int ni = s.intersect(st.pos(), navDir(), S(o.surfaceTolerance), is);
         for (int i = 0; i < ni; ++i) {
           S pl = is[i].pathLength;
           if (is[i].valid() && pl > S(o.nearLimit) &&
@@ -2016,7 +2105,7 @@ struct Fitter {
             return true;
           }
         }
-        ++surfaceIndex;
+        surfaceIndex += propDir;
       }
       navigationBreak = true;
       return false;
@@ -2024,7 +2113,7 @@ struct Fitter {
     // updateSingleSurfaceStatus, boundary tolerance Infinite
     auto surfaceStatus = [&](int sid, int idx) -> IStatus {
       Intersection<S> is[2];
-      sf[sid].intersect(st.pos(), st.dir(), S(o.surfaceTolerance), is);
+      sf[sid].intersect(st.pos(), navDir(), S(o.surfaceTolerance), is);
       Intersection<S> x = is[idx];
       if (x.status == IStatus::onSurface) {
         st.stepSize.release(kNav);
@@ -2061,7 +2150,7 @@ struct Fitter {
       unsigned steps = 0;
       for (; err == CK_TRACK_OK && steps < o.maxSteps; ++steps) {
         S h;
-        int se = eigenStep(st, field, o, h);
+        int se = eigenStep(st, field, o, h, propDir);
         if (se != kStepOk) {
           err = se == kStepField ? CK_TRACK_FIELD_OUT_OF_BOUNDS
                                  : (se == kStepStalled ? CK_TRACK_STEP_SIZE_STALLED
@@ -2093,31 +2182,105 @@ struct Fitter {
       if (err == CK_TRACK_OK && !terminated) err = CK_TRACK_STEP_COUNT_LIMIT;
     }
     (void)missedActive;
+    p.lastMeasurementIndex = lastMeasurementIndex;
+    p.measurementStates = measurementStates;
+    return err;
+  }
+
+  // KalmanFitter::fit_impl (KalmanFitter.hpp:860-985): the forward filter,
+  // then either the smoother or the reversed filter, then the extrapolation
+  // to the reference surface.
+  int fit(const Surface<S>& startSurface, const Vec<S, 6>& startPars, const Mat<S, 6, 6>& startCov,
+          float mass, float absQ, int absPdg, const int* seq, int nSeq,
+          const std::vector<MeasRec<S>>& meas, TrackOut& out) const {
+    auto findMeas = [&](int sid) -> int {
+      for (size_t i = 0; i < meas.size(); ++i)
+        if (meas[i].surface == sid) return (int)i;
+      return -1;
+    };
+    Pass fwd;
+    int err = filterPass(startSurface, -2, startPars, startCov, mass, absQ, absPdg, seq, nSeq, meas,
+                         1, -1, fwd);
     out.states.clear();
     if (err != CK_TRACK_OK) {
       out.status = err;
       return err;
     }
-    if (measurementStates == 0) {
+    if (fwd.measurementStates == 0) {
       out.status = CK_TRACK_NO_MEASUREMENT_FOUND;
       return out.status;
     }
+    std::vector<IState>& states = fwd.states;
     // the track: states 0..lastMeasurementIndex (linear chain)
-    int tip = lastMeasurementIndex;
+    int tip = fwd.lastMeasurementIndex;
     int lastMeas = -1;
     for (int k = tip; k >= 0; --k)
       if ((states[k].flags & CK_FLAG_HAS_MEASUREMENT) && !(states[k].flags & CK_FLAG_IS_OUTLIER)) {
         lastMeas = k;
         break;
       }
-    // shareFrom(Filtered -> Smoothed) on the last measurement state and on the tip
+    // shareFrom(Filtered -> Smoothed) on the last measurement state
+    // (KalmanFitter.hpp:889-891)
     states[lastMeas].smth = states[lastMeas].filt;
     states[lastMeas].smthCov = states[lastMeas].filtCov;
     states[lastMeas].smoothedSharesFiltered = true;
-    states[tip].smth = states[tip].filt;
-    states[tip].smthCov = states[tip].filtCov;
     int status = CK_TRACK_OK;
-    if (o.smoother == CK_SMOOTHER_MBF) {
+    bool haveTrackParams = false;
+    // KalmanFitter.hpp:897-900 with SimpleReverseFilteringLogic
+    // (Examples/Algorithms/TrackFitting/src/KalmanFitterFunction.cpp:50-58)
+    const bool reverse =
+        o.reverseFiltering ||
+        std::abs(1.0 / (double)states[lastMeas].filt[4]) <= o.reverseMomThreshold;
+    if (reverse) {
+      // KalmanFitter.hpp:901-945: filter backwards from the last measurement
+      // state (its parameters, covariance scaled), towards the reference
+      // surface; the first measurement state's smoothed parameters are the
+      // reversed pass's last filtered ones. No other state has smoothed
+      // parameters (NaN here).
+      int first = -1;
+      for (int k = 0; k <= tip && first < 0; ++k)
+        if ((states[k].flags & CK_FLAG_HAS_MEASUREMENT) && !(states[k].flags & CK_FLAG_IS_OUTLIER))
+          first = k;
+      const IState& ls = states[lastMeas];
+      Mat<S, 6, 6> c = ls.filtCov;
+      for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) c.a[i][j] = c.a[i][j] * S(o.reverseCovScaling);
+      Pass rev;
+      int e = filterPass((*surfaces)[ls.surface], ls.surface, ls.filt, c, mass, absQ, absPdg, seq,
+                         nSeq, meas, -1, o.referenceSurface, rev);
+      if (e == CK_TRACK_OK && rev.measurementStates == 0) e = CK_TRACK_NO_MEASUREMENT_FOUND;
+      int revLast = -1;
+      for (int k = rev.lastMeasurementIndex; e == CK_TRACK_OK && k >= 0 && revLast < 0; --k)
+        if ((rev.states[k].flags & CK_FLAG_HAS_MEASUREMENT) &&
+            !(rev.states[k].flags & CK_FLAG_IS_OUTLIER))
+          revLast = k;
+      if (e == CK_TRACK_OK && rev.states[revLast].surface != states[first].surface)
+        e = CK_TRACK_INCONSISTENT_STATES;
+      if (e != CK_TRACK_OK) {
+        out.status = e;
+        return e;
+      }
+      const S nan = S(std::numeric_limits<double>::quiet_NaN());
+      for (int k = 0; k <= tip; ++k)
+        if (k != lastMeas)
+          for (int i = 0; i < 6; ++i) {
+            states[k].smth[i] = nan;
+            for (int j = 0; j < 6; ++j) states[k].smthCov.a[i][j] = nan;
+          }
+      states[first].smth = rev.states[revLast].filt;
+      states[first].smthCov = rev.states[revLast].filtCov;
+      if (rev.fitted) {
+        put6(out.trackParams, rev.fittedPars);
+        put36(out.trackCov, rev.fittedCov);
+        out.hasTrackParams = true;
+        haveTrackParams = true;
+      }
+    } else {
+      // the smoother starts by sharing the tip's filtered parameters
+      states[tip].smth = states[tip].filt;
+      states[tip].smthCov = states[tip].filtCov;
+    }
+    if (!reverse && o.smoother == CK_SMOOTHER_MBF) {
       // MbfSmoother::operator() (MbfSmoother.hpp:48-90): backwards from the
       // tip with zero lambdas; the first state updates no lambdas
       Mat<S, 6, 6> L = Mat<S, 6, 6>::zero();
@@ -2144,7 +2307,7 @@ struct Fitter {
       }
     }
     // GainMatrixSmoother::operator() (GainMatrixSmoother.hpp:43-99)
-    for (int k = tip - 1; k >= 0 && o.smoother != CK_SMOOTHER_MBF; --k) {
+    for (int k = tip - 1; k >= 0 && o.smoother != CK_SMOOTHER_MBF && !reverse; --k) {
       IState& ts = states[k];
       const IState& pv = states[k + 1];
       if (!smoothStep(ts.filt, ts.filtCov, pv.pred, pv.predCov, pv.jac, pv.smth, pv.smthCov,
@@ -2188,7 +2351,7 @@ struct Fitter {
         out.ndf += ts.measDim;
       }
     }
-    if (o.referenceSurface >= 0) {
+    if (o.referenceSurface >= 0 && !haveTrackParams) {
       // KalmanFitter.hpp:959-972: the fit fails when the extrapolation does
       const int e = extrapolate(states, tip, mass, absQ, absPdg, out);
       if (e != CK_TRACK_OK) {

@@ -33,7 +33,9 @@ def compare(gpu, ora, rtol=1e-9, fields=("predicted", "filtered", "smoothed"), e
     rep["surface_mismatch"] = int(np.sum((gpu.view("state_surface") != ora.view("state_surface")) & valid))
 
     def rel(a, b, floor):
-        return np.abs(a - b) / np.maximum(np.maximum(np.abs(a), np.abs(b)), floor)
+        # (0 against 0 with a zero floor counts as equal)
+        return np.abs(a - b) / np.maximum(np.maximum(np.maximum(np.abs(a), np.abs(b)), floor),
+                                          1e-300)
 
     m = valid
     for name in ("state_path_length", "state_chi2"):
@@ -45,6 +47,13 @@ def compare(gpu, ora, rtol=1e-9, fields=("predicted", "filtered", "smoothed"), e
         ca, cb = gpu.view(name + "_cov"), ora.view(name + "_cov")
         if pa is None or pb is None:
             continue
+        # states without such parameters (reverse filtering: no smoothed
+        # parameters but on the first and last measurement state) hold NaN
+        # on both sides: the NaN positions must agree, the rest is compared
+        for x, y, key in ((pa, pb, name), (ca, cb, name + "_cov")):
+            rep[key + "_nan_mismatch"] = int(np.sum((np.isnan(x) != np.isnan(y))[m]))
+        pa, pb = np.nan_to_num(pa, nan=0.0), np.nan_to_num(pb, nan=0.0)
+        ca, cb = np.nan_to_num(ca, nan=0.0), np.nan_to_num(cb, nan=0.0)
         sig = _sig(cb)
         rp = rel(pa, pb, sig)[m]
         rep[name] = float(rp.max()) if rp.size else 0.0

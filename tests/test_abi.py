@@ -83,6 +83,6 @@ def test_unsupported_extensions_rejected_before_device_use(cklib):
     from acts_gb300 import fitter
 
     L = fitter.lib()
-    o = abi.default_options(reverse_filtering=1)
+    o = abi.default_options(smoother=7)
     st = L.ck_fit_batch(None, C.byref(o), None, None, None)
     assert st == abi.CK_ERR_INVALID_ARGUMENT  # NULL handle checked first

@@ -141,3 +141,51 @@ def test_mixed_precision_perigee_parameters():
     rel = d / np.maximum(np.abs(o), sig)
     print("perigee max rel %.3g" % rel.max())
     assert rel.max() <= REL_BOUND
+
+
+@pytest.mark.gpu
+def test_mixed_precision_reverse_filtering():
+    """Reverse filtering in the mixed form (the reversed pass with the form's
+    FP32 stepper) against the FP64 oracle: the statuses, the states without
+    smoothed parameters (NaN), and the smoothed parameters of the first
+    (reverse-filtered) and last measurement states and the perigee
+    parameters within the relative bound of the smoothed parameters."""
+    from acts_gb300 import generate
+    from acts_gb300.fitter import CudaKalman
+
+    det = generate.Detector(abi.CKG_BARREL, perigee=True)
+    n = 20000
+    b = generate.generate(det, n, seed=13)
+    kw = dict(reference_surface=det.perigee, reverse_filtering=1)
+    comps = abi.OUT_SMOOTHED | abi.OUT_REFERENCE
+    ora = Results(n, 12, comps)
+    kforacle.fit_batch(det, b, abi.default_options(**kw), ora,
+                       n_threads=kforacle.hardware_threads())
+    fit = CudaKalman.for_detector(det)
+    try:
+        mix = fit.fit_batch(b, abi.default_options(precision=abi.PRECISION_MIXED, **kw),
+                            max_states=12, components=comps)
+    finally:
+        fit.close()
+    assert np.mean(mix.status == ora.status) > 0.999
+    ok = (mix.status == 0) & (ora.status == 0)
+    ok &= ora.chi2_sum < GOOD_CHI2NDF * np.maximum(ora.ndf, 1)
+    assert ok.mean() > 0.99
+    valid = np.arange(12)[None, :] < ora.n_states[:, None]
+    valid &= ok[:, None]
+    a, o = mix.view("smoothed"), ora.view("smoothed")
+    np.testing.assert_array_equal(np.isnan(a[..., 0])[valid], np.isnan(o[..., 0])[valid])
+    has = valid & ~np.isnan(o[..., 0])
+    sig = np.sqrt(np.abs(ora.view("smoothed_cov")[..., [0, 7, 14, 21, 28, 35]]))
+    d = np.abs(a - o)
+    d[..., 2] = np.abs((a[..., 2] - o[..., 2] + np.pi) % (2 * np.pi) - np.pi)
+    rel = d[has] / np.maximum(np.abs(o[has]), sig[has])
+    print("reverse filtering: smoothed max rel %.3g" % rel.max())
+    assert rel.max() <= REL_BOUND
+    a, o = mix.track("track_params")[ok], ora.track("track_params")[ok]
+    sig = np.sqrt(ora.track("track_cov")[ok][:, [0, 7, 14, 21, 28, 35]])
+    d = np.abs(a - o)
+    d[:, 2] = np.abs((a[:, 2] - o[:, 2] + np.pi) % (2 * np.pi) - np.pi)
+    rel = d / np.maximum(np.abs(o), sig)
+    print("reverse filtering: perigee max rel %.3g" % rel.max())
+    assert rel.max() <= REL_BOUND

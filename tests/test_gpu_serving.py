@@ -129,17 +129,18 @@ def test_oversized_event_rejected(fitter_factory):
 
 
 @pytest.mark.gpu
-def test_serving_with_reference_surface():
+@pytest.mark.parametrize("reverse", [0, 1], ids=["smoother", "reverse_filtering"])
+def test_serving_with_reference_surface(reverse):
     """Events fitted through the serving loop with extrapolation to a
-    perigee surface: every event's perigee parameters (and states) equal its
-    fit alone."""
+    perigee surface (or reverse filtering towards it): every event's perigee
+    parameters equal its fit alone."""
     from acts_gb300.fitter import CudaKalman
 
     det = generate.Detector(abi.CKG_UNEVEN, perigee=True)
     fit = CudaKalman.for_detector(det)
     comps = abi.OUT_SMOOTHED | abi.OUT_REFERENCE
     opt = abi.default_options(precision=abi.PRECISION_MIXED, outlier_chi2_cut=15.0,
-                              reference_surface=det.perigee)
+                              reference_surface=det.perigee, reverse_filtering=reverse)
     sizes = generate.event_sizes(9, 10, lo=100, hi=3000)
     evs = _events(det, sizes, seed=41)
     srv = FitServer(fit, opt, memory_budget_bytes=2 << 30, n_streams=2, max_states=24,

@@ -126,16 +126,19 @@ def test_static_scratch_rejects_oversized_batch(fitter_factory):
 
 
 @pytest.mark.gpu
-def test_static_scratch_with_reference_surface():
+@pytest.mark.parametrize("reverse", [0, 1], ids=["smoother", "reverse_filtering"])
+def test_static_scratch_with_reference_surface(reverse):
     """ck_fit_batch_static with extrapolation to a perigee surface (its start
-    states in the static array too) gives ck_fit_batch's perigee parameters."""
+    states in the static array too), or with reverse filtering towards it,
+    gives ck_fit_batch's perigee parameters."""
     from acts_gb300 import generate
     from acts_gb300.fitter import CudaKalman
 
     det = generate.Detector(abi.CKG_BARREL, perigee=True)
     b = generate.generate(det, N_TRACKS, seed=29)
     dev = torch.device("cuda", 0)
-    opt = abi.default_options(precision=abi.PRECISION_MIXED, reference_surface=det.perigee)
+    opt = abi.default_options(precision=abi.PRECISION_MIXED, reference_surface=det.perigee,
+                              reverse_filtering=reverse)
     fit = CudaKalman.for_detector(det)
     try:
         bi, keep_in = _device_in(b, dev)
