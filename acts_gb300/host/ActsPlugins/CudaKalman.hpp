@@ -141,6 +141,9 @@ struct TrackState {
   }
   bool isOutlier() const { return typeFlags & CK_FLAG_IS_OUTLIER; }
   bool isHole() const { return typeFlags & CK_FLAG_IS_HOLE; }
+  // TrackStateProxy::hasSmoothed: with reverse filtering only the first and
+  // the last measurement state carry smoothed parameters (NaN elsewhere)
+  bool hasSmoothed() const { return smoothed[0] == smoothed[0]; }
 };
 
 // Minimal TrackContainer: tracks own a contiguous range of states in
