@@ -98,9 +98,31 @@ int main() {
     chi2 += b.chi2;
     ndf += b.nDoF;
   }
+  // reverse filtering: smoothed parameters on the first and the last
+  // measurement state only (TrackStateProxy::hasSmoothed)
+  {
+    KalmanFitterOptions rev = opts;
+    rev.options.reverse_filtering = 1;
+    TrackContainer tc;
+    std::vector<Result<size_t>> rr = fitter.fitBatch(inputs.data(), n, rev, tc);
+    for (int t = 0; t < n; ++t) {
+      if (!rr[t].ok()) return 7;
+      const Track& tr = tc.tracks[rr[t].value()];
+      const TrackState* s = tc.trackStates(rr[t].value());
+      size_t first = tr.nStates, last = 0;
+      for (size_t k = 0; k < tr.nStates; ++k)
+        if (s[k].isMeasurement()) {
+          if (first == tr.nStates) first = k;
+          last = k;
+        }
+      for (size_t k = 0; k < tr.nStates; ++k)
+        if (s[k].hasSmoothed() != (k == first || k == last)) return 8;
+      if (tr.nMeasurements != batch.tracks[rs[t].value()].nMeasurements) return 9;
+    }
+  }
   // an option outside the declared extension set is rejected, not emulated
   KalmanFitterOptions bad;
-  bad.options.reverse_filtering = 1;
+  bad.options.smoother = 7;
   bool threw = false;
   try {
     TrackContainer tc;
