@@ -416,7 +416,7 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
       ++launches;
     }
     if (opt.reference_surface >= 0) {
-      e = launchExtrapolate(fp, st);
+      e = launchExtrapolate(fp, opt.precision, st);
       if (e != cudaSuccess) return cudaFail(e, "extrapolation kernel launch");
       ++launches;
     }

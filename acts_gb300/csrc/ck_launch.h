@@ -57,8 +57,8 @@ inline cudaError_t launchReverseOutput(const FitParams& fp, int precision, cudaS
                                          : launchReverseOutputFP64(fp, st);
 }
 // extrapolation of every successfully smoothed track to the reference
-// surface (FP64 in both forms; ck_extrapolate.cu)
-cudaError_t launchExtrapolate(const FitParams& fp, cudaStream_t st);
+// surface (with the form's stepper; ck_extrapolate.cu)
+cudaError_t launchExtrapolate(const FitParams& fp, int precision, cudaStream_t st);
 constexpr int kExtrapolateBlock = 64;
 
 }  // namespace ck

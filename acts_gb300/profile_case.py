@@ -28,9 +28,12 @@ def main(argv=None):
                     help="forward-filter kernel variant (default: the handle's default)")
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--blocks-per-sm", type=int, default=0)
+    ap.add_argument("--perigee", action="store_true",
+                    help="extrapolate to a perigee surface at the origin")
+    ap.add_argument("--reverse", action="store_true", help="reverse filtering")
     a = ap.parse_args(argv)
     preset = PRESETS[a.preset]
-    det = generate.Detector(preset)
+    det = generate.Detector(preset, perigee=a.perigee)
     b = generate.generate(det, a.tracks, seed=a.seed)
     ms = a.max_states or (10 if preset != abi.CKG_UNEVEN else 20)
     fit = CudaKalman.for_detector(det, use_graph=False)
@@ -39,9 +42,11 @@ def main(argv=None):
         if a.variant >= 0:
             fit.set_launch_config(prec, a.variant, a.threads, a.blocks_per_sm)
         opt = abi.default_options(precision=prec,
-                                  outlier_chi2_cut=15.0 if preset == abi.CKG_UNEVEN else float("inf"))
+                                  outlier_chi2_cut=15.0 if preset == abi.CKG_UNEVEN else float("inf"),
+                                  reference_surface=det.perigee, reverse_filtering=int(a.reverse))
+        comps = abi.OUT_SMOOTHED | (abi.OUT_REFERENCE if a.perigee else 0)
         for _ in range(a.repeat):
-            fit.fit_batch(b, opt, max_states=ms, components=abi.OUT_SMOOTHED)
+            fit.fit_batch(b, opt, max_states=ms, components=comps)
             print("%s %s %d tracks: kernel %.3f ms" % (a.preset, name, a.tracks, fit.last_kernel_ms()))
     fit.close()
     return 0
