@@ -321,6 +321,7 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
   cudaError_t e;
   int32_t* dTicket = (int32_t*)c.ticket.p;
   int launches = 0;
+  h->lastChunks = 0;
   cudaMemsetAsync(dTicket, 0, sizeof(int32_t), st);
   if (n > 0) cudaMemsetAsync(c.tip.p, 0xff, sizeof(int32_t) * (size_t)n, st);
   const int32_t* perm = nullptr;
@@ -648,8 +649,205 @@ ck_status ck_destroy(ck_handle* h) {
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->evMid) cudaEventDestroy(h->evMid);
+  for (cudaEvent_t ev : h->chunkTiming) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : h->chunkSync) cudaEventDestroy(ev);
+  if (h->copyIn) cudaStreamDestroy(h->copyIn);
+  if (h->copyOut) cudaStreamDestroy(h->copyOut);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
+  return CK_OK;
+}
+
+namespace {
+
+// Host batches of at least two chunks are pipelined: the inputs of chunk c+1
+// travel on one copy stream while chunk c is fitted on the caller's stream
+// and the outputs of chunk c-1 travel back on a second copy stream, so the
+// transfers hide behind the kernels. A chunk is a view of the full device
+// input arrays (the CSR offsets are absolute: the chunk shifts only its
+// offset and per-track arrays by its first track); its outputs fill their own
+// block of the device output buffers (SoA over the chunk's tracks) and reach
+// the caller's layout with one 2D copy per array (rows: states x components).
+constexpr int kChunkTracks = 262144;
+
+ck_status ensureChunkResources(ck_handle* h, int chunks) {
+  cudaError_t e;
+  if (!h->copyIn && (e = cudaStreamCreateWithFlags(&h->copyIn, cudaStreamNonBlocking)) != cudaSuccess)
+    return cudaFail(e, "copy stream");
+  if (!h->copyOut && (e = cudaStreamCreateWithFlags(&h->copyOut, cudaStreamNonBlocking)) != cudaSuccess)
+    return cudaFail(e, "copy stream");
+  while ((int)h->chunkTiming.size() < 3 * chunks) {
+    cudaEvent_t ev;
+    if ((e = cudaEventCreate(&ev)) != cudaSuccess) return cudaFail(e, "chunk event");
+    h->chunkTiming.push_back(ev);
+  }
+  while ((int)h->chunkSync.size() < 2 * chunks + 2) {
+    cudaEvent_t ev;
+    if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess)
+      return cudaFail(e, "chunk event");
+    h->chunkSync.push_back(ev);
+  }
+  return CK_OK;
+}
+
+}  // namespace
+
+// The chunked host path (both sides in host memory, n >= 2 chunks); the
+// options and arrays are validated by the caller.
+ck_status fitBatchHostChunked(ck_handle* h, const ck_options& opt, const ck_batch_in& in,
+                              const ck_batch_out& out, cudaStream_t st) {
+  const int n = in.n_tracks;
+  const int chunks = (n + kChunkTracks - 1) / kChunkTracks;
+  const int per = (n + chunks - 1) / chunks;
+  const int ms = out.max_states;
+  const Tune tn = h->tune[opt.precision];
+  ck_status s = ensureChunkResources(h, chunks);
+  if (s != CK_OK) return s;
+  cudaError_t e;
+  const int32_t* so = in.seq_offsets;
+  const int32_t* mo = in.meas_offsets;
+  // ---- device input arrays (full size) and what one track / one CSR entry holds
+  struct In {
+    const void* src;
+    int kind;  // 0 offsets (n + 1), 1 per sequence entry, 2 per measurement, 3 per track
+    size_t elem;
+    const void** dst;
+  } ins[] = {
+      {in.seq_offsets, 0, 4, nullptr},       {in.seq_surfaces, 1, 4, nullptr},
+      {in.meas_offsets, 0, 4, nullptr},      {in.meas_surfaces, 2, 4, nullptr},
+      {in.meas_values, 2, 16, nullptr},      {in.meas_cov, 2, 32, nullptr},
+      {in.start_params, 3, 48, nullptr},     {in.start_cov, 3, 288, nullptr},
+      {in.start_frames, 3, 96, nullptr},     {in.particle, 3, 8, nullptr},
+      {in.particle_pdg, 3, 4, nullptr},      {in.meas_subspace, 2, 4, nullptr},
+  };
+  static_assert(sizeof(ins) / sizeof(ins[0]) == kInputArrays, "input arrays");
+  const size_t nSeq = (size_t)so[n], nMeas = (size_t)mo[n];
+  auto total = [&](int kind) -> size_t {
+    return kind == 0 ? (size_t)n + 1 : kind == 1 ? nSeq : kind == 2 ? nMeas : (size_t)n;
+  };
+  for (int i = 0; i < kInputArrays; ++i) {
+    if (!ins[i].src) {
+      if (i >= 10) continue;
+      return fail(CK_ERR_INVALID_ARGUMENT, "input array missing");
+    }
+    if ((e = h->inBufs[i].ensure(total(ins[i].kind) * ins[i].elem)) != cudaSuccess)
+      return cudaFail(e, "input buffer");
+  }
+  // ---- device output buffers: per track, per state (rows ms x C) or per
+  // track component (rows C)
+  struct Out {
+    void* host;
+    int rows;  // copy rows of one track column
+    size_t elem;
+  } outs[] = {
+      {out.status, 1, 4},       {out.n_states, 1, 4},           {out.n_measurements, 1, 4},
+      {out.n_holes, 1, 4},      {out.n_outliers, 1, 4},         {out.ndf, 1, 4},
+      {out.chi2_sum, 1, 8},     {out.state_surface, ms, 4},     {out.state_flags, ms, 4},
+      {out.state_path_length, ms, 8}, {out.state_chi2, ms, 8},  {out.predicted, 6 * ms, 8},
+      {out.predicted_cov, 36 * ms, 8}, {out.filtered, 6 * ms, 8}, {out.filtered_cov, 36 * ms, 8},
+      {out.smoothed, 6 * ms, 8}, {out.smoothed_cov, 36 * ms, 8}, {out.jacobian, 36 * ms, 8},
+      {out.track_params, 6, 8}, {out.track_cov, 36, 8},
+  };
+  static_assert(sizeof(outs) / sizeof(outs[0]) == kOutArrays, "output arrays");
+  for (int i = 0; i < kOutArrays; ++i)
+    if (outs[i].host && (e = h->outBufs[i].ensure((size_t)n * outs[i].rows * outs[i].elem)) !=
+                            cudaSuccess)
+      return cudaFail(e, "output buffer");
+  if ((s = preparePipeline(h, h->ctx, per, ms, opt.precision, needsExtStart(opt))) != CK_OK)
+    return s;
+  cudaEvent_t* sync = h->chunkSync.data();
+  cudaEvent_t evStart = sync[2 * chunks], evDone = sync[2 * chunks + 1];
+  cudaEventRecord(evStart, st);
+  cudaStreamWaitEvent(h->copyIn, evStart, 0);
+  cudaStreamWaitEvent(h->copyOut, evStart, 0);
+  size_t h2d = 0, d2h = 0;
+  int launches = 0;
+  for (int c = 0; c < chunks; ++c) {
+    const int t0 = c * per, t1 = std::min(n, t0 + per), nc = t1 - t0;
+    // inputs of this chunk
+    for (int i = 0; i < kInputArrays; ++i) {
+      if (!ins[i].src) continue;
+      size_t a, b;
+      switch (ins[i].kind) {
+        case 0: a = t0, b = t1 + 1; break;
+        case 1: a = so[t0], b = so[t1]; break;
+        case 2: a = mo[t0], b = mo[t1]; break;
+        default: a = t0, b = t1; break;
+      }
+      const size_t bytes = (b - a) * ins[i].elem;
+      if (bytes &&
+          (e = cudaMemcpyAsync((char*)h->inBufs[i].p + a * ins[i].elem,
+                               (const char*)ins[i].src + a * ins[i].elem, bytes,
+                               cudaMemcpyHostToDevice, h->copyIn)) != cudaSuccess)
+        return cudaFail(e, "input copy");
+      h2d += bytes;
+    }
+    cudaEventRecord(sync[2 * c], h->copyIn);
+    // the chunk's views
+    ck_batch_in din = in;
+    din.memory = CK_MEM_DEVICE;
+    din.n_tracks = nc;
+    const void** dins[] = {(const void**)&din.seq_offsets, (const void**)&din.seq_surfaces,
+                           (const void**)&din.meas_offsets, (const void**)&din.meas_surfaces,
+                           (const void**)&din.meas_values, (const void**)&din.meas_cov,
+                           (const void**)&din.start_params, (const void**)&din.start_cov,
+                           (const void**)&din.start_frames, (const void**)&din.particle,
+                           (const void**)&din.particle_pdg, (const void**)&din.meas_subspace};
+    for (int i = 0; i < kInputArrays; ++i) {
+      if (!ins[i].src) {
+        *dins[i] = nullptr;
+        continue;
+      }
+      const size_t shift = (ins[i].kind == 0 || ins[i].kind == 3) ? (size_t)t0 * ins[i].elem : 0;
+      *dins[i] = (const char*)h->inBufs[i].p + shift;
+    }
+    ck_batch_out dout = out;
+    dout.memory = CK_MEM_DEVICE;
+    void** douts[] = {(void**)&dout.status, (void**)&dout.n_states, (void**)&dout.n_measurements,
+                      (void**)&dout.n_holes, (void**)&dout.n_outliers, (void**)&dout.ndf,
+                      (void**)&dout.chi2_sum, (void**)&dout.state_surface,
+                      (void**)&dout.state_flags, (void**)&dout.state_path_length,
+                      (void**)&dout.state_chi2, (void**)&dout.predicted,
+                      (void**)&dout.predicted_cov, (void**)&dout.filtered,
+                      (void**)&dout.filtered_cov, (void**)&dout.smoothed,
+                      (void**)&dout.smoothed_cov, (void**)&dout.jacobian,
+                      (void**)&dout.track_params, (void**)&dout.track_cov};
+    for (int i = 0; i < kOutArrays; ++i)
+      if (outs[i].host)
+        *douts[i] = (char*)h->outBufs[i].p + (size_t)t0 * outs[i].rows * outs[i].elem;
+    // the fit of this chunk, timed with its own events
+    cudaStreamWaitEvent(st, sync[2 * c], 0);
+    std::swap(h->ev0, h->chunkTiming[3 * c]);
+    std::swap(h->evMid, h->chunkTiming[3 * c + 1]);
+    std::swap(h->ev1, h->chunkTiming[3 * c + 2]);
+    s = enqueuePipeline(h, h->ctx, opt, din, dout, tn, st, true, gridBlocksFor(h, tn));
+    std::swap(h->ev0, h->chunkTiming[3 * c]);
+    std::swap(h->evMid, h->chunkTiming[3 * c + 1]);
+    std::swap(h->ev1, h->chunkTiming[3 * c + 2]);
+    if (s != CK_OK) return s;
+    launches += h->lastLaunches;
+    cudaEventRecord(sync[2 * c + 1], st);
+    // its outputs, into the caller's layout
+    cudaStreamWaitEvent(h->copyOut, sync[2 * c + 1], 0);
+    for (int i = 0; i < kOutArrays; ++i) {
+      if (!outs[i].host) continue;
+      const size_t w = (size_t)nc * outs[i].elem;
+      char* dst = (char*)outs[i].host + (size_t)t0 * outs[i].elem;
+      const char* src = (const char*)*douts[i];
+      if ((e = cudaMemcpy2DAsync(dst, (size_t)n * outs[i].elem, src, w, w, outs[i].rows,
+                                 cudaMemcpyDeviceToHost, h->copyOut)) != cudaSuccess)
+        return cudaFail(e, "output copy");
+      d2h += w * outs[i].rows;
+    }
+  }
+  cudaEventRecord(evDone, h->copyOut);
+  cudaStreamWaitEvent(st, evDone, 0);
+  h->lastLaunches = launches;
+  h->lastChunks = chunks;
+  h->lastTimed = true;
+  h->lastH2D = h2d;
+  h->lastD2H = d2h;
+  if ((e = cudaGetLastError()) != cudaSuccess) return cudaFail(e, "batch pipeline");
   return CK_OK;
 }
 
@@ -681,6 +879,13 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
       return fail(CK_ERR_INVALID_ARGUMENT, "offsets missing");
     const int nSeq = in->seq_offsets[n], nMeas = in->meas_offsets[n];
     if (nSeq < 0 || nMeas < 0) return fail(CK_ERR_INVALID_ARGUMENT, "negative CSR size");
+    if (out->memory == CK_MEM_HOST && n >= 2 * kChunkTracks) {
+      // (chunk boundaries need monotone offsets)
+      for (int t = 0; t < n; ++t)
+        if (in->seq_offsets[t + 1] < in->seq_offsets[t] || in->meas_offsets[t + 1] < in->meas_offsets[t])
+          return fail(CK_ERR_INVALID_ARGUMENT, "decreasing CSR offsets");
+      return fitBatchHostChunked(h, *opt, *in, *out, st);
+    }
     struct Item {
       const void* src;
       size_t bytes;
@@ -838,6 +1043,12 @@ ck_status ck_last_kernel_ms(ck_handle* h, double* ms) {
   if (!h || !ms) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
   if (!h->lastTimed) return fail(CK_ERR_NOT_READY, "no timed batch");
   cudaSetDevice(h->device);
+  if (h->lastChunks > 0) {
+    double a = 0, b = 0;
+    ck_status s = ck_last_kernel_split_ms(h, &a, &b);
+    *ms = a + b;
+    return s;
+  }
   cudaError_t e = cudaEventSynchronize(h->ev1);
   if (e != cudaSuccess) return cudaFail(e, "event synchronize");
   float f = 0;
@@ -851,6 +1062,22 @@ ck_status ck_last_kernel_split_ms(ck_handle* h, double* filter_ms, double* smoot
   if (!h || !filter_ms || !smoother_ms) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
   if (!h->lastTimed) return fail(CK_ERR_NOT_READY, "no timed batch");
   cudaSetDevice(h->device);
+  if (h->lastChunks > 0) {
+    // a chunked host batch: the sum over its chunks
+    double fa = 0, fb = 0;
+    for (int c = 0; c < h->lastChunks; ++c) {
+      float a = 0, b = 0;
+      cudaError_t e = cudaEventSynchronize(h->chunkTiming[3 * c + 2]);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&a, h->chunkTiming[3 * c], h->chunkTiming[3 * c + 1]);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&b, h->chunkTiming[3 * c + 1], h->chunkTiming[3 * c + 2]);
+      if (e != cudaSuccess) return cudaFail(e, "event elapsed");
+      fa += a;
+      fb += b;
+    }
+    *filter_ms = fa;
+    *smoother_ms = fb;
+    return CK_OK;
+  }
   cudaError_t e = cudaEventSynchronize(h->ev1);
   if (e != cudaSuccess) return cudaFail(e, "event synchronize");
   float a = 0, b = 0;

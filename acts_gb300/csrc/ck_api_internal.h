@@ -125,5 +125,11 @@ struct ck_handle {
   cudaGraphExec_t graphExec = nullptr;
   ck::GraphKey graphKey;
   int graphLaunches = 0;
+  // chunked host batches: the copy streams, one (ev0, evMid, ev1) timing
+  // triplet per chunk of the last call, and the ordering events
+  cudaStream_t copyIn = nullptr, copyOut = nullptr;
+  std::vector<cudaEvent_t> chunkTiming;  // 3 per chunk
+  std::vector<cudaEvent_t> chunkSync;    // 2 per chunk + 2
+  int lastChunks = 0;
   std::mutex mu;
 };

@@ -1,0 +1,44 @@
+"""Large host-memory batches run as chunks whose transfers overlap the fits
+of their neighbours (ck_fit_batch, both sides in host memory, at least two
+chunks of 262,144 tracks): the outputs equal those of the same tracks fitted
+in calls below the chunking size, bit for bit, in the caller's SoA layout."""
+import numpy as np
+import pytest
+
+from acts_gb300 import abi, generate
+
+N = 600000
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [abi.PRECISION_MIXED, abi.PRECISION_FP64])
+def test_chunked_host_batch_equals_unchunked(precision):
+    from acts_gb300.fitter import CudaKalman
+
+    det = generate.Detector(abi.CKG_BARREL, perigee=True)
+    b = generate.generate(det, N, seed=31)
+    opt = abi.default_options(precision=precision, reference_surface=det.perigee,
+                              outlier_chi2_cut=15.0)
+    comps = abi.OUT_SMOOTHED | abi.OUT_REFERENCE
+    fit = CudaKalman.for_detector(det)
+    try:
+        whole = fit.fit_batch(b, opt, max_states=10, components=comps)
+        assert fit.last_kernel_ms() > 0
+        h2d, d2h = fit.last_transfer_bytes()
+        assert h2d > 0 and d2h > 0
+        halves = [np.arange(0, N // 2), np.arange(N // 2, N)]
+        parts = [fit.fit_batch(b.subset(i), opt, max_states=10, components=comps) for i in halves]
+    finally:
+        fit.close()
+    assert (whole.status == 0).mean() > 0.99
+    for name in ("status", "n_states", "n_measurements", "ndf", "chi2_sum"):
+        np.testing.assert_array_equal(getattr(whole, name),
+                                      np.concatenate([getattr(p, name) for p in parts]))
+    for name in ("state_flags", "state_surface", "smoothed", "smoothed_cov"):
+        a = whole.view(name)
+        for i, p in zip(halves, parts):
+            np.testing.assert_array_equal(a[i], p.view(name), err_msg=name)
+    for name in ("track_params", "track_cov"):
+        a = whole.track(name)
+        for i, p in zip(halves, parts):
+            np.testing.assert_array_equal(a[i], p.track(name), err_msg=name)
