@@ -34,10 +34,12 @@ def test_chunked_host_batch_equals_unchunked(precision):
     for name in ("status", "n_states", "n_measurements", "ndf", "chi2_sum"):
         np.testing.assert_array_equal(getattr(whole, name),
                                       np.concatenate([getattr(p, name) for p in parts]))
+    # (state slots past a track's n_states are not written)
     for name in ("state_flags", "state_surface", "smoothed", "smoothed_cov"):
         a = whole.view(name)
         for i, p in zip(halves, parts):
-            np.testing.assert_array_equal(a[i], p.view(name), err_msg=name)
+            valid = np.arange(10)[None, :] < p.n_states[:, None]
+            np.testing.assert_array_equal(a[i][valid], p.view(name)[valid], err_msg=name)
     for name in ("track_params", "track_cov"):
         a = whole.track(name)
         for i, p in zip(halves, parts):
