@@ -40,7 +40,9 @@ def test_chunked_host_batch_equals_unchunked(precision):
         for i, p in zip(halves, parts):
             valid = np.arange(10)[None, :] < p.n_states[:, None]
             np.testing.assert_array_equal(a[i][valid], p.view(name)[valid], err_msg=name)
+    # (failed fits leave their track parameters unwritten)
     for name in ("track_params", "track_cov"):
         a = whole.track(name)
         for i, p in zip(halves, parts):
-            np.testing.assert_array_equal(a[i], p.track(name), err_msg=name)
+            ok = p.status == 0
+            np.testing.assert_array_equal(a[i][ok], p.track(name)[ok], err_msg=name)
