@@ -668,7 +668,11 @@ namespace {
 // offset and per-track arrays by its first track); its outputs fill their own
 // block of the device output buffers (SoA over the chunk's tracks) and reach
 // the caller's layout with one 2D copy per array (rows: states x components).
-constexpr int kChunkTracks = 262144;
+constexpr int kDefaultChunkTracks = 524288;
+
+int chunkTracksOf(const ck_handle* h) {
+  return h->chunkTracks == 0 ? kDefaultChunkTracks : h->chunkTracks;
+}
 
 ck_status ensureChunkResources(ck_handle* h, int chunks) {
   cudaError_t e;
@@ -697,7 +701,8 @@ ck_status ensureChunkResources(ck_handle* h, int chunks) {
 ck_status fitBatchHostChunked(ck_handle* h, const ck_options& opt, const ck_batch_in& in,
                               const ck_batch_out& out, cudaStream_t st) {
   const int n = in.n_tracks;
-  const int chunks = (n + kChunkTracks - 1) / kChunkTracks;
+  const int chunkTracks = chunkTracksOf(h);
+  const int chunks = (n + chunkTracks - 1) / chunkTracks;
   const int per = (n + chunks - 1) / chunks;
   const int ms = out.max_states;
   const Tune tn = h->tune[opt.precision];
@@ -879,7 +884,7 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
       return fail(CK_ERR_INVALID_ARGUMENT, "offsets missing");
     const int nSeq = in->seq_offsets[n], nMeas = in->meas_offsets[n];
     if (nSeq < 0 || nMeas < 0) return fail(CK_ERR_INVALID_ARGUMENT, "negative CSR size");
-    if (out->memory == CK_MEM_HOST && n >= 2 * kChunkTracks) {
+    if (out->memory == CK_MEM_HOST && chunkTracksOf(h) > 0 && n >= 2 * chunkTracksOf(h)) {
       // (chunk boundaries need monotone offsets)
       for (int t = 0; t < n; ++t)
         if (in->seq_offsets[t + 1] < in->seq_offsets[t] || in->meas_offsets[t + 1] < in->meas_offsets[t])
@@ -1127,6 +1132,13 @@ ck_status ck_set_grid_blocks(ck_handle* h, int32_t precision, int32_t blocks) {
     return fail(CK_ERR_INVALID_ARGUMENT, "bad precision, or negative block count");
   std::lock_guard<std::mutex> lock(h->mu);
   h->tune[precision].grid = blocks;
+  return CK_OK;
+}
+
+ck_status ck_set_host_chunk_tracks(ck_handle* h, int32_t tracks) {
+  if (!h) return fail(CK_ERR_INVALID_ARGUMENT, "NULL handle");
+  std::lock_guard<std::mutex> lock(h->mu);
+  h->chunkTracks = tracks;
   return CK_OK;
 }
 

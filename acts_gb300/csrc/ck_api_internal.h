@@ -131,5 +131,6 @@ struct ck_handle {
   std::vector<cudaEvent_t> chunkTiming;  // 3 per chunk
   std::vector<cudaEvent_t> chunkSync;    // 2 per chunk + 2
   int lastChunks = 0;
+  int chunkTracks = 0;  // 0: kDefaultChunkTracks; < 0: never chunk
   std::mutex mu;
 };

@@ -45,6 +45,9 @@ namespace ck {
 #define CK_NI CK_D
 
 enum Phase { PH_FETCH = 0, PH_STEP = 1, PH_SURFACE = 2, PH_DONE = 3 };
+// Runge-Kutta trials per round of the compaction kernels when at most one
+// warp's worth of a block's tracks steps
+constexpr int kTailStepsPerRound = 32;
 
 // ChargeHypothesis::extractMomentum (ChargeHypothesis.hpp:70-90)
 template <typename P>
@@ -1872,7 +1875,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) fitKernel(FitParams fp) {
 // threads of the warp that run this call together).
 template <typename P, typename CV, bool F2B, bool REV>
 __device__ __forceinline__ void advanceSlot(const FitParams& fp, Lane<P, CV, F2B, REV>& L, int c,
-                                            int lane) {
+                                            int lane, int spr) {
   if (c == PH_FETCH) {
     const unsigned act = __activemask();
     const int leader = __ffs(act) - 1;
@@ -1890,8 +1893,8 @@ __device__ __forceinline__ void advanceSlot(const FitParams& fp, Lane<P, CV, F2B
         L.start(fp, q, fp.perm ? __ldg(&fp.perm[q]) : q);
     }
   } else if (c == PH_STEP) {
-    // up to steps_per_round Runge-Kutta trials while the track stays in STEP
-    for (int k = 0; k < fp.steps_per_round && L.phase == PH_STEP; ++k) L.step(fp, L.q);
+    // up to spr Runge-Kutta trials while the track stays in STEP
+    for (int k = 0; k < spr && L.phase == PH_STEP; ++k) L.step(fp, L.q);
   } else {
     L.surface(fp, L.q);
   }
@@ -1948,9 +1951,14 @@ __global__ void __launch_bounds__(S, 1) fitKernelCompact(FitParams fp) {
     __syncthreads();
     if (tid < nItems) {
       const int slot = items[tid];
+      // At most one warp's worth of tracks stepping (the end of the queue,
+      // where a track running into the step limit would otherwise take a
+      // round of the block's phase vote per few trials): many trials per
+      // round. Results do not depend on the trials per round.
+      const int spr = nItems <= 32 ? max(fp.steps_per_round, kTailStepsPerRound) : fp.steps_per_round;
       // the phase step works on a register copy of the slot's state
       LaneT L = st[slot];
-      advanceSlot(fp, L, c, lane);
+      advanceSlot(fp, L, c, lane, spr);
       st[slot] = L;
     }
     __syncthreads();

@@ -65,6 +65,7 @@ def lib():
         L.ck_sync.argtypes = [C.c_void_p]
         L.ck_set_steps_per_round.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
         L.ck_set_grid_blocks.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+        L.ck_set_host_chunk_tracks.argtypes = [C.c_void_p, C.c_int32]
         L.ck_last_kernel_split_ms.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         L.ck_atan2_mixed.argtypes = [C.c_void_p, C.c_int32, P(C.c_double), P(C.c_double),
                                      P(C.c_double)]
@@ -300,6 +301,10 @@ class CudaKalman:
     def set_grid_blocks(self, precision, blocks):
         """Grid of the forward-filter kernel (0: the whole GPU)."""
         _check(lib().ck_set_grid_blocks(self._h, int(precision), int(blocks)))
+
+    def set_host_chunk_tracks(self, tracks):
+        """Tracks per chunk of host-memory batches (0: default; < 0: never chunk)."""
+        _check(lib().ck_set_host_chunk_tracks(self._h, int(tracks)))
 
     def last_launch_count(self):
         n = C.c_int32()

@@ -21,6 +21,7 @@ def test_chunked_host_batch_equals_unchunked(precision):
                               outlier_chi2_cut=15.0)
     comps = abi.OUT_SMOOTHED | abi.OUT_REFERENCE
     fit = CudaKalman.for_detector(det)
+    fit.set_host_chunk_tracks(250000)  # three chunks
     try:
         whole = fit.fit_batch(b, opt, max_states=10, components=comps)
         assert fit.last_kernel_ms() > 0
