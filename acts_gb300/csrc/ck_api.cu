@@ -668,7 +668,10 @@ namespace {
 // offset and per-track arrays by its first track); its outputs fill their own
 // block of the device output buffers (SoA over the chunk's tracks) and reach
 // the caller's layout with one 2D copy per array (rows: states x components).
-constexpr int kDefaultChunkTracks = 524288;
+// (a fit launch carries a few ms of work that does not shrink with the batch
+// — measured on GB300, barrel tracks, mixed: 8 ms for 125k tracks, 30 ms for
+// 1M — so chunks stay large: a 1M-track host batch runs as two)
+constexpr int kDefaultChunkTracks = 500000;
 
 int chunkTracksOf(const ck_handle* h) {
   return h->chunkTracks == 0 ? kDefaultChunkTracks : h->chunkTracks;

@@ -447,7 +447,7 @@ ck_status ck_set_grid_blocks(ck_handle* h, int32_t precision, int32_t blocks);
 /* Chunking of host-memory batches (both sides in host memory): a batch of at
  * least two chunks is fitted chunk by chunk while the inputs of the next
  * chunk and the outputs of the previous one travel on copy streams. `tracks`:
- * tracks per chunk (0: the default, 524288; a negative value: never chunk). */
+ * tracks per chunk (0: the default, 500000; a negative value: never chunk). */
 ck_status ck_set_host_chunk_tracks(ck_handle* h, int32_t tracks);
 
 /* Enables (default) or disables ordering the work queue by descending
