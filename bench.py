@@ -281,10 +281,10 @@ def accuracy_report(b, r64, rmx, n):
 # Per-track figures of the ncu capture summarised in
 # profiles/fit_smooth_kernels_barrel200k.md (barrel, 200k tracks, ten states).
 NCU_PER_TRACK = {
-    "mixed_filter_fp64_flops": 8.73e3, "mixed_filter_fp32_flops": 33.4e3,
-    "mixed_filter_dram_bytes": 5.93e3, "mixed_filter_fp64_pipe_busy": 0.605,
-    "fp64_filter_fp64_flops": 43.9e3, "fp64_filter_dram_bytes": 10.42e3,
-    "fp64_filter_fp64_pipe_busy": 0.668}
+    "mixed_filter_fp64_flops": 8.72e3, "mixed_filter_fp32_flops": 33.4e3,
+    "mixed_filter_dram_bytes": 6.07e3, "mixed_filter_fp64_pipe_busy": 0.572,
+    "fp64_filter_fp64_flops": 43.9e3, "fp64_filter_dram_bytes": 10.26e3,
+    "fp64_filter_fp64_pipe_busy": 0.645}
 
 
 def best_of_tune_log(log):
