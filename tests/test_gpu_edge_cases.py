@@ -95,13 +95,17 @@ def test_empty_batch(fitter_factory):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("max_states", [24, 6, 1])
-def test_ragged_edge_case_batch(fitter_factory, max_states):
+@pytest.mark.parametrize("reverse", [0, 1], ids=["smoother", "reverse_filtering"])
+def test_ragged_edge_case_batch(fitter_factory, max_states, reverse):
     """max_states 6 and 1: the longer tracks end in TooManyStates, as the
-    oracle's (and the reference's) state container would overflow."""
+    oracle's (and the reference's) state container would overflow. With
+    reverse filtering the reversed pass meets the same special tracks (one
+    measurement: its first and last measurement state are one; links beyond
+    the sequence: neither pass completes)."""
     det = detector(abi.CKG_BARREL)
     src = batch(abi.CKG_BARREL, 16)
     b = _ragged(src, CASES)
-    opt = abi.default_options()
+    opt = abi.default_options(reverse_filtering=reverse)
     ora = Results(b.n, max_states)
     kforacle.fit_batch(det, b, opt, ora, n_threads=1)
     gpu = fitter_factory(abi.CKG_BARREL).fit_batch(b, opt, max_states=max_states)

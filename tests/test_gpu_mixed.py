@@ -93,7 +93,7 @@ def test_mixed_precision_accuracy(fitter_factory, preset, smoother, extra):
     sig = np.sqrt(np.abs(ora.view("smoothed_cov")[..., [0, 7, 14, 21, 28, 35]]))
     d = np.abs(a - o)
     d[..., 2] = np.abs((a[..., 2] - o[..., 2] + np.pi) % (2 * np.pi) - np.pi)
-    rel = (d / np.maximum(np.abs(o), sig))[meas]
+    rel = d[meas] / np.maximum(np.abs(o[meas]), sig[meas])
     print("precision %d: max rel %.3g p99 %.3g" % (precision, rel.max(), np.quantile(rel, 0.99)))
     # with the free-to-bound correction the unscented transform samples the
     # square root of the free covariance, which the FP32 transport perturbs

@@ -117,3 +117,41 @@ def test_algorithm_matches_batch_fit_and_oracle():
     kforacle.fit_batch(det, sub, opt, ora, n_threads=kforacle.hardware_threads())
     rep = compare(got, ora, 1e-9)
     assert_parity(rep, 1e-9)
+
+
+def test_csv_event_round_trip(tmp_path):
+    """An event written as the examples' per-event CSV files (measurements
+    with local_key, proto tracks) and read back gives the same batch; a
+    measurement of phi is rejected."""
+    from acts_gb300 import io_csv
+
+    det = generate.Detector(abi.CKG_STRIPS)
+    b = generate.generate(det, 30, seed=4)
+    store = _event(b, empty=())
+    gids = [(1 << 56) | (s + 1) << 20 for s in range(det.n_surfaces)]   # synthetic identifiers
+    mpath = io_csv.per_event_filepath(str(tmp_path), "measurements.csv", 7)
+    ppath = io_csv.per_event_filepath(str(tmp_path), "prototracks.csv", 7)
+    assert mpath.endswith("event000000007-measurements.csv")
+    io_csv.write_measurements(mpath, store["measurements"], gids)
+    io_csv.write_proto_tracks(ppath, store["prototracks"])
+    meas, ids = io_csv.read_measurements(mpath, {g: s for s, g in enumerate(gids)})
+    protos = io_csv.read_proto_tracks(ppath, ids, n_tracks=b.n)
+    store2 = dict(store, measurements=meas, prototracks=protos)
+    r1, r2 = _Recorder(), _Recorder()
+    TrackFittingAlgorithm(TrackFittingAlgorithm.Config(fit=r1)).execute(store)
+    TrackFittingAlgorithm(TrackFittingAlgorithm.Config(fit=r2)).execute(store2)
+    a, c = r1.calls[0][0], r2.calls[0][0]
+    for name in ("meas_offsets", "meas_surfaces", "meas_subspace", "seq_surfaces"):
+        np.testing.assert_array_equal(getattr(a, name), getattr(c, name), err_msg=name)
+    # values and variances round-trip through the text exactly (repr)
+    sub = a.meas_subspace
+    np.testing.assert_array_equal(a.meas_values.reshape(-1, 2)[:, 0], c.meas_values.reshape(-1, 2)[:, 0])
+    two = sub == abi.MEAS_LOC01
+    np.testing.assert_array_equal(a.meas_values.reshape(-1, 2)[two], c.meas_values.reshape(-1, 2)[two])
+    np.testing.assert_array_equal(a.meas_cov.reshape(-1, 4)[:, [0, 3]][two], c.meas_cov.reshape(-1, 4)[:, [0, 3]][two])
+    text = open(mpath).read().splitlines()
+    cols = text[1].split(",")
+    cols[2] = str(1 << 3)    # phi
+    open(mpath, "w").write("\n".join([text[0], ",".join(cols)] + text[2:]) + "\n")
+    with pytest.raises(ValueError):
+        io_csv.read_measurements(mpath, {g: s for s, g in enumerate(gids)})
