@@ -11,14 +11,16 @@ N = 600000
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", [abi.PRECISION_MIXED, abi.PRECISION_FP64])
-def test_chunked_host_batch_equals_unchunked(precision):
+@pytest.mark.parametrize("precision,reverse", [(abi.PRECISION_MIXED, 0), (abi.PRECISION_FP64, 0),
+                                               (abi.PRECISION_MIXED, 1)],
+                         ids=["mixed", "fp64", "mixed_reverse_filtering"])
+def test_chunked_host_batch_equals_unchunked(precision, reverse):
     from acts_gb300.fitter import CudaKalman
 
     det = generate.Detector(abi.CKG_BARREL, perigee=True)
     b = generate.generate(det, N, seed=31)
     opt = abi.default_options(precision=precision, reference_surface=det.perigee,
-                              outlier_chi2_cut=15.0)
+                              outlier_chi2_cut=15.0, reverse_filtering=reverse)
     comps = abi.OUT_SMOOTHED | abi.OUT_REFERENCE
     fit = CudaKalman.for_detector(det)
     fit.set_host_chunk_tracks(250000)  # three chunks
@@ -40,6 +42,7 @@ def test_chunked_host_batch_equals_unchunked(precision):
         a = whole.view(name)
         for i, p in zip(halves, parts):
             valid = np.arange(10)[None, :] < p.n_states[:, None]
+            # (reverse filtering: NaN where a state has no smoothed parameters)
             np.testing.assert_array_equal(a[i][valid], p.view(name)[valid], err_msg=name)
     # (failed fits leave their track parameters unwritten)
     for name in ("track_params", "track_cov"):
