@@ -314,7 +314,9 @@ ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, int
 // smoother kernel.
 ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
                           const ck_batch_in& din, const ck_batch_out& dout, const Tune& tn,
-                          cudaStream_t st, bool timed, int gridBlocks) {
+                          cudaStream_t st, bool timed, int gridBlocks, const cudaEvent_t* timing) {
+  const cudaEvent_t ev0 = timing ? timing[0] : h->ev0, evMid = timing ? timing[1] : h->evMid,
+                    ev1 = timing ? timing[2] : h->ev1;
   const int n = din.n_tracks;
   const int grid = gridBlocks;
   const int maxStates = dout.max_states;
@@ -390,13 +392,13 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive)
       recFlags = cudaEventRecordExternal;
-    cudaEventRecordWithFlags(h->ev0, st, recFlags);
+    cudaEventRecordWithFlags(ev0, st, recFlags);
   }
   if (n > 0) {
     e = launchFit(fp, opt.precision, tn, fitGrid, st);
     if (e != cudaSuccess) return cudaFail(e, "fit kernel launch");
     ++launches;
-    if (timed) cudaEventRecordWithFlags(h->evMid, st, recFlags);
+    if (timed) cudaEventRecordWithFlags(evMid, st, recFlags);
     if (anyReverse(opt)) {
       // the reversed pass: the 256-slot compaction kernel, one block per SM,
       // over the same queue (the tracks the reverse-filtering logic selects)
@@ -422,7 +424,7 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
       ++launches;
     }
   }
-  if (timed) cudaEventRecordWithFlags(h->ev1, st, recFlags);
+  if (timed) cudaEventRecordWithFlags(ev1, st, recFlags);
   h->lastLaunches = launches;
   h->lastTimed = timed;
   return CK_OK;
@@ -825,13 +827,8 @@ ck_status fitBatchHostChunked(ck_handle* h, const ck_options& opt, const ck_batc
         *douts[i] = (char*)h->outBufs[i].p + (size_t)t0 * outs[i].rows * outs[i].elem;
     // the fit of this chunk, timed with its own events
     cudaStreamWaitEvent(st, sync[2 * c], 0);
-    std::swap(h->ev0, h->chunkTiming[3 * c]);
-    std::swap(h->evMid, h->chunkTiming[3 * c + 1]);
-    std::swap(h->ev1, h->chunkTiming[3 * c + 2]);
-    s = enqueuePipeline(h, h->ctx, opt, din, dout, tn, st, true, gridBlocksFor(h, tn));
-    std::swap(h->ev0, h->chunkTiming[3 * c]);
-    std::swap(h->evMid, h->chunkTiming[3 * c + 1]);
-    std::swap(h->ev1, h->chunkTiming[3 * c + 2]);
+    s = enqueuePipeline(h, h->ctx, opt, din, dout, tn, st, true, gridBlocksFor(h, tn),
+                        h->chunkTiming.data() + 3 * c);
     if (s != CK_OK) return s;
     launches += h->lastLaunches;
     cudaEventRecord(sync[2 * c + 1], st);

@@ -90,9 +90,12 @@ inline size_t sortCountsBytes(int n) { return sizeof(int32_t) * 64 * (size_t)sor
 size_t recordBytesPerTrack(int maxStates, int precision);
 ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, int precision,
                           bool extrapolate);
+// `timing`: the (start, filter end, end) events a timed pipeline records;
+// null: the handle's own
 ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
                           const ck_batch_in& din, const ck_batch_out& dout, const Tune& tn,
-                          cudaStream_t st, bool timed, int gridBlocks);
+                          cudaStream_t st, bool timed, int gridBlocks,
+                          const cudaEvent_t* timing = nullptr);
 int gridBlocksFor(ck_handle* h, const Tune& tn);
 
 }  // namespace ck
