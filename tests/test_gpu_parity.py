@@ -54,6 +54,10 @@ CASES = [
      dict(reverse_filtering=1, outlier_chi2_cut=4.0), 0.6),
     ("barrel_reverse_free_to_bound_correction", abi.CKG_BARREL, 1000,
      dict(reverse_filtering=1, free_to_bound_correction=1), 0.99),
+    ("telescope_reverse_filtering", abi.CKG_TELESCOPE, 1000, dict(reverse_filtering=1), 0.99),
+    ("uneven_reverse_early_termination_mbf_threshold", abi.CKG_UNEVEN, 2000,
+     dict(outlier_chi2_cut=15.0, early_termination=1, smoother=abi.SMOOTHER_MBF,
+          reverse_filtering_mom_threshold=1.5), 0.9),
 ]
 
 
@@ -106,6 +110,8 @@ REF_CASES = [
      dict(reverse_filtering=1, outlier_chi2_cut=4.0, min_ok=0.6)),
     ("uneven_perigee_reverse_early_termination", abi.CKG_UNEVEN, 2000,
      dict(reverse_filtering=1, outlier_chi2_cut=15.0, early_termination=1, min_ok=0.9)),
+    ("strips_perigee_reverse", abi.CKG_STRIPS, 1000,
+     dict(reverse_filtering=1, outlier_chi2_cut=15.0, min_ok=0.95)),
     ("barrel_perigee_last", abi.CKG_BARREL, 1000, dict(reference_strategy=abi.EXTRAPOLATE_LAST)),
     ("uneven_perigee_first_or_last", abi.CKG_UNEVEN, 2000,
      dict(outlier_chi2_cut=15.0, early_termination=1,
