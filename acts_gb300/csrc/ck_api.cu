@@ -703,8 +703,8 @@ ck_status ensureChunkResources(ck_handle* h, int chunks) {
 
 // The chunked host path (both sides in host memory, n >= 2 chunks); the
 // options and arrays are validated by the caller.
-ck_status fitBatchHostChunked(ck_handle* h, const ck_options& opt, const ck_batch_in& in,
-                              const ck_batch_out& out, cudaStream_t st) {
+static ck_status fitBatchHostChunked(ck_handle* h, const ck_options& opt, const ck_batch_in& in,
+                                     const ck_batch_out& out, cudaStream_t st) {
   const int n = in.n_tracks;
   const int chunkTracks = chunkTracksOf(h);
   const int chunks = (n + chunkTracks - 1) / chunkTracks;
