@@ -14,7 +14,8 @@
 // Rules of use:
 //   - inputs and outputs must already be in device memory;
 //   - the scratch holds kStaticScratchBytes (32 MiB); a batch that needs more
-//     (see ck_static_scratch_bytes) is rejected with CK_ERR_SCRATCH_LIMIT;
+//     (ck_static_scratch_bytes_for gives the exact figure for a call's
+//     options) is rejected with CK_ERR_SCRATCH_LIMIT;
 //   - nothing in the scratch has to start at zero: every call clears the
 //     queue ticket itself and writes the length histograms, each track's tip
 //     and its records before reading them;
@@ -92,6 +93,12 @@ int64_t ck_static_scratch_bytes(int32_t n_tracks, int32_t max_states, int32_t pr
   return (int64_t)layoutFor(n_tracks, max_states, precision, false).total;
 }
 
+int64_t ck_static_scratch_bytes_for(const ck_options* opt, int32_t n_tracks, int32_t max_states) {
+  if (!opt || n_tracks < 0 || max_states <= 0) return -1;
+  if (validateOptions(opt) != CK_OK) return -1;
+  return (int64_t)layoutFor(n_tracks, max_states, opt->precision, needsExtStart(*opt)).total;
+}
+
 int64_t ck_static_scratch_capacity(void) { return (int64_t)kStaticScratchBytes; }
 
 ck_status ck_fit_batch_static(ck_handle* h, const ck_options* opt, const ck_batch_in* in,
@@ -139,7 +146,11 @@ ck_status ck_fit_batch_static(ck_handle* h, const ck_options* opt, const ck_batc
   const Tune tn = h->tune[opt->precision];
   h->lastH2D = 0;
   h->lastD2H = 0;
-  return enqueuePipeline(h, c, *opt, *in, *out, tn, st, false, gridBlocksFor(h, tn));
+  s = enqueuePipeline(h, c, *opt, *in, *out, tn, st, false, gridBlocksFor(h, tn));
+  if (s != CK_OK) return s;
+  // (launch errors of the pipeline's memsets and kernels)
+  if ((e = cudaGetLastError()) != cudaSuccess) return cudaFail(e, "batch pipeline");
+  return CK_OK;
 }
 
 }  // extern "C"

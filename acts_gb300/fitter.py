@@ -61,6 +61,8 @@ def lib():
                                           P(abi.ck_batch_out), C.c_void_p]
         L.ck_static_scratch_bytes.argtypes = [C.c_int32, C.c_int32, C.c_int32]
         L.ck_static_scratch_bytes.restype = C.c_int64
+        L.ck_static_scratch_bytes_for.argtypes = [P(abi.ck_options), C.c_int32, C.c_int32]
+        L.ck_static_scratch_bytes_for.restype = C.c_int64
         L.ck_static_scratch_capacity.restype = C.c_int64
         L.ck_sync.argtypes = [C.c_void_p]
         L.ck_set_steps_per_round.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
@@ -276,6 +278,12 @@ class CudaKalman:
     @staticmethod
     def static_scratch_bytes(n_tracks, max_states, precision):
         return lib().ck_static_scratch_bytes(int(n_tracks), int(max_states), int(precision))
+
+    @staticmethod
+    def static_scratch_bytes_for(options, n_tracks, max_states):
+        """Exact scratch bytes of a ck_fit_batch_static call with these
+        options (extrapolation start states included)."""
+        return lib().ck_static_scratch_bytes_for(C.byref(options), int(n_tracks), int(max_states))
 
     @staticmethod
     def static_scratch_capacity():

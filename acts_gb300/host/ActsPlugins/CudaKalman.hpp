@@ -20,7 +20,7 @@
 // The ACTS types this build cannot include (Eigen/Boost are not available)
 // are represented by small structs with the same fields; a build against a
 // real ACTS installation maps Acts::BoundTrackParameters, SourceLink and
-// VectorMultiTrajectory onto them one to one (see INTEGRATION.md).
+// VectorMultiTrajectory onto them one to one.
 #pragma once
 
 #include <array>

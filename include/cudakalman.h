@@ -388,7 +388,7 @@ ck_status ck_sync(ck_handle* h);
  * per device, shared by all handles. For callers that must not call the
  * device allocator once running (cudaMalloc/cudaFree can synchronise the
  * device; ck_fit_batch grows its buffers on demand). A batch needing more
- * than the array (ck_static_scratch_bytes) fails with CK_ERR_SCRATCH_LIMIT.
+ * than the array (ck_static_scratch_bytes_for) fails with CK_ERR_SCRATCH_LIMIT.
  * Nothing in the array has to start at zero. Calls whose device work
  * overlaps (other streams or handles on the same device, unordered) race on
  * the array. Make the first call before capturing the stream: it resolves
@@ -396,10 +396,17 @@ ck_status ck_sync(ck_handle* h);
 ck_status ck_fit_batch_static(ck_handle* h, const ck_options* opt,
                               const ck_batch_in* in, ck_batch_out* out, void* stream);
 /* Scratch bytes ck_fit_batch_static needs for a batch (-1 on bad sizes), and
- * the size of the static array. No counterpart in the reference. With a
- * reference surface (options.reference_surface >= 0) a batch needs 448 bytes
- * per track more (two extrapolation start states). */
+ * the size of the static array. No counterpart in the reference.
+ * ck_static_scratch_bytes counts the records, queue and tips only: a call
+ * with a reference surface (options.reference_surface >= 0), reverse
+ * filtering or a reverse-filtering momentum threshold also holds two
+ * extrapolation start states per track (448 bytes), and every area is
+ * rounded up to 256 bytes. ck_static_scratch_bytes_for gives the exact
+ * figure a call with these options checks against the capacity (-1 on bad
+ * sizes or invalid options). */
 int64_t ck_static_scratch_bytes(int32_t n_tracks, int32_t max_states, int32_t precision);
+int64_t ck_static_scratch_bytes_for(const ck_options* options, int32_t n_tracks,
+                                    int32_t max_states);
 int64_t ck_static_scratch_capacity(void);
 
 /* Kernel-only timing of the most recent batch (CUDA events recorded on the

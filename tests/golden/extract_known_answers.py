@@ -1,8 +1,8 @@
 """Extracts the known-answer constants of the reference's own unit tests into
 tests/golden/reference_known_answers.json.
 
-Run in a checkout that has the reference sources (path given as argv[1],
-default /root/reference). The JSON is committed, so tests never read the
+Run with the path of a checkout of the reference sources as its one
+argument. The JSON is committed, so tests never read the
 reference at run time. Sources parsed (paths relative to the acts repo):
   Tests/UnitTests/Core/TrackFitting/GainMatrixUpdaterTests.cpp  (Update, UpdateFailed)
   Tests/UnitTests/Core/TrackFitting/GainMatrixSmootherTests.cpp (Smooth)
@@ -175,7 +175,9 @@ def silicon(src):
 
 
 def main():
-    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: extract_known_answers.py <path of the reference sources>")
+    src = sys.argv[1]
     out = {"updater": updater(src), "smoother": smoother(src), "mbf_smoother": mbf_smoother(src),
            "line_surface": line_surface(src),
            "corrected_free_to_bound": corrected_free_to_bound(src),

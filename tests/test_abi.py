@@ -86,3 +86,23 @@ def test_unsupported_extensions_rejected_before_device_use(cklib):
     o = abi.default_options(smoother=7)
     st = L.ck_fit_batch(None, C.byref(o), None, None, None)
     assert st == abi.CK_ERR_INVALID_ARGUMENT  # NULL handle checked first
+
+
+def test_static_scratch_query_counts_extrapolation_slots(cklib):
+    """ck_static_scratch_bytes_for counts the two extrapolation start states
+    per track that a reference surface, reverse filtering or the momentum
+    threshold adds (host arithmetic, no device)."""
+    from acts_gb300.fitter import CudaKalman
+
+    n, ms = 1000, 10
+    base = CudaKalman.static_scratch_bytes(n, ms, abi.PRECISION_MIXED)
+    plain = CudaKalman.static_scratch_bytes_for(abi.default_options(precision=abi.PRECISION_MIXED),
+                                               n, ms)
+    assert plain == base
+    for kw in (dict(reference_surface=0), dict(reverse_filtering=1),
+               dict(reverse_filtering_mom_threshold=1.0)):
+        o = abi.default_options(precision=abi.PRECISION_MIXED, **kw)
+        got = CudaKalman.static_scratch_bytes_for(o, n, ms)
+        assert got >= base + 448 * n, (kw, got, base)
+        assert (got - base) % 256 == 0
+    assert CudaKalman.static_scratch_bytes_for(abi.default_options(smoother=7), n, ms) == -1

@@ -158,3 +158,37 @@ def test_static_scratch_with_reference_surface(reverse):
     assert np.array_equal(s0, s1)
     assert (s0 == 0).mean() > 0.99
     assert np.array_equal(p0, p1) and np.array_equal(c0, c1)
+
+
+@pytest.mark.gpu
+def test_static_scratch_allocates_nothing():
+    """The entry point's promise: once its first call on the device has
+    resolved the array (which may load the module), later calls take no
+    device memory, even for a batch larger than any before it. Free device
+    memory is read with cudaMemGetInfo around such a call; every input and
+    output is allocated before the first reading."""
+    from acts_gb300 import generate
+    from acts_gb300.fitter import CudaKalman
+
+    det = generate.Detector(abi.CKG_BARREL, perigee=True)
+    dev = torch.device("cuda", 0)
+    small, large = 200, 2 * N_TRACKS
+    opt = abi.default_options(precision=abi.PRECISION_FP64, reference_surface=det.perigee)
+    fit = CudaKalman.for_detector(det)
+    try:
+        assert fit.static_scratch_bytes_for(opt, large, MAX_STATES) <= fit.static_scratch_capacity()
+        bs, keep_s = _device_in(generate.generate(det, small, seed=5), dev)
+        bl, keep_l = _device_in(generate.generate(det, large, seed=6), dev)
+        os_, keep_os = _device_out(small, dev)
+        ol, keep_ol = _device_out(large, dev)
+        fit.fit_batch_static(opt, bs, os_)
+        fit.sync()
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info(dev)
+        fit.fit_batch_static(opt, bl, ol)
+        fit.sync()
+        free1, _ = torch.cuda.mem_get_info(dev)
+        assert free1 == free0, (free0, free1)
+        assert (keep_ol["status"].cpu().numpy() == 0).mean() > 0.99
+    finally:
+        fit.close()
