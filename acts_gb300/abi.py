@@ -38,6 +38,7 @@ TRACK_STATUS = {
     15: "InconsistentTrackStates",
 }
 
+TRACK_FIELD_OUT_OF_BOUNDS = 9
 TRACK_INCONSISTENT_STATES = 15
 
 FLAG_HAS_MEASUREMENT = 1 << 0
@@ -215,6 +216,75 @@ class ck_batch_out(C.Structure):
         ("track_params", P_f64),
         ("track_cov", P_f64),
     ]
+
+
+class ck_propagate_in(C.Structure):
+    _fields_ = [
+        ("n", C.c_int32),
+        ("memory", C.c_int32),
+        ("start_params", P_f64),
+        ("start_cov", P_f64),
+        ("start_frames", P_f64),
+        ("particle", P_f32),
+        ("target", P_i32),
+        ("path_limit", P_f64),
+    ]
+
+
+class ck_propagate_out(C.Structure):
+    _fields_ = [
+        ("status", P_i32),
+        ("end_params", P_f64),
+        ("end_cov", P_f64),
+        ("jacobian", P_f64),
+        ("end_frames", P_f64),
+        ("path_length", P_f64),
+        ("steps", P_i32),
+    ]
+
+
+class Propagation:
+    """Host arrays of a batch of propagations (ck_propagate's layout): the
+    inputs per track, the outputs [c, n] (structure of arrays)."""
+
+    def __init__(self, start_params, start_frames, particle, path_limit, start_cov=None,
+                 target=None):
+        f64 = lambda x: np.ascontiguousarray(x, np.float64)
+        self.start_params = f64(start_params).reshape(-1, 6)
+        self.n = len(self.start_params)
+        self.start_frames = f64(start_frames).reshape(self.n, 12)
+        self.particle = np.ascontiguousarray(particle, np.float32).reshape(self.n, 2)
+        self.path_limit = f64(path_limit).reshape(self.n)
+        self.start_cov = None if start_cov is None else f64(start_cov).reshape(self.n, 36)
+        self.target = None if target is None else np.ascontiguousarray(target, np.int32)
+        n = self.n
+        self.status = np.full(n, 11, np.int32)
+        self.end_params = np.zeros((6, n))
+        self.end_cov = np.zeros((36, n))
+        self.jacobian = np.zeros((36, n))
+        self.end_frames = np.zeros((n, 12))
+        self.path_length = np.zeros(n)
+        self.steps = np.zeros(n, np.int32)
+
+    def as_in(self):
+        i = ck_propagate_in()
+        i.n = self.n
+        i.memory = MEM_HOST
+        i.start_params = ptr(self.start_params, C.c_double)
+        i.start_cov = ptr(self.start_cov, C.c_double)
+        i.start_frames = ptr(self.start_frames, C.c_double)
+        i.particle = ptr(self.particle, C.c_float)
+        i.target = ptr(self.target, C.c_int32)
+        i.path_limit = ptr(self.path_limit, C.c_double)
+        return i
+
+    def as_out(self):
+        o = ck_propagate_out()
+        o.status = ptr(self.status, C.c_int32)
+        for name in ("end_params", "end_cov", "jacobian", "end_frames", "path_length"):
+            setattr(o, name, ptr(getattr(self, name), C.c_double))
+        o.steps = ptr(self.steps, C.c_int32)
+        return o
 
 
 class ck_server_config(C.Structure):

@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(kExtrapolateBlock) extrapolateKernel(FitParams
     }
     L.startExtrapolation(fp, q, t, *from, dist);
     // bounded: every step either ends the lane or counts towards maxSteps
-    while (L.phase == PH_STEP) L.template step<true>(fp, q);
+    while (L.phase == PH_STEP) L.template step<kStepExtrapolate>(fp, q);
   }
 }
 

@@ -45,6 +45,12 @@ namespace ck {
 #define CK_NI CK_D
 
 enum Phase { PH_FETCH = 0, PH_STEP = 1, PH_SURFACE = 2, PH_DONE = 3 };
+// What follows an accepted Runge-Kutta step: the fit's navigation and actor
+// (kStepFit), the aborters of the extrapolation to the reference line
+// (kStepExtrapolate), or those of a plain propagation (kStepPropagate).
+enum StepMode { kStepFit = 0, kStepExtrapolate = 1, kStepPropagate = 2 };
+// SurfaceReached's near limit (StandardAborters.hpp:76): -100 um
+constexpr double kTargetNearLimit = -0.1;
 // Runge-Kutta trials per round of the compaction kernels when at most half
 // of a block's slots step
 constexpr int kTailStepsPerRound = 32;
@@ -1083,10 +1089,10 @@ struct Lane {
   }
 
   // STEP: one Runge-Kutta trial (EigenStepper::step, EigenStepper.ipp:168-388)
-  // EXTRAP: the lane extrapolates to the reference surface (signed step
-  // direction, the aborters after each step); the fit kernels instantiate
-  // the forward-only step without that code
-  template <bool EXTRAP = false>
+  // MODE (StepMode): the lane fits, extrapolates to the reference surface or
+  // propagates (signed step direction, the aborters after each step); the
+  // fit kernels instantiate the forward-only step without the other code
+  template <int MODE = kStepFit>
   CK_D void step(const FitParams& fp, int slot) {
     const DevOptions& o = fp.opt;
     if (!stepStarted) {
@@ -1095,7 +1101,7 @@ struct Lane {
         return;
       }
       initialH = stepValue();
-      if constexpr (EXTRAP || REV) initialH *= dirSign;  // EigenStepper.ipp:272
+      if constexpr (MODE != kStepFit || REV) initialH *= dirSign;  // EigenStepper.ipp:272
       hd = initialH;
       trials = 0;
       stepStarted = true;
@@ -1292,9 +1298,13 @@ struct Lane {
     // post-step navigation (Propagator.ipp:113-141)
     cNav = kNotSet;
     cActor = kNotSet;
-    if constexpr (EXTRAP) {
+    if constexpr (MODE == kStepExtrapolate) {
       // no navigation target and no actors; the aborters decide
       if (extrapolationAbort(fp)) finishExtrapolation(fp);
+      return;
+    }
+    if constexpr (MODE == kStepPropagate) {
+      if (propagationAbort(fp)) finishPropagation(fp);
       return;
     }
     if (haveTarget) {
@@ -1471,6 +1481,13 @@ struct Lane {
       }
     const ck_batch_out& out = fp.out;
     const size_t n = (size_t)fp.n_tracks;
+    if (fp.prop.jac) {
+      // (the propagation entry's transport Jacobian)
+#pragma unroll
+      for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = 0; j < 6; ++j) fp.prop.jac[(size_t)(i * 6 + j) * n + t] = J[i][j];
+    }
     if (out.track_cov) {
 #pragma unroll
       for (int i = 0; i < 6; ++i)
@@ -1490,6 +1507,195 @@ struct Lane {
       for (int i = 0; i < 6; ++i) out.track_params[(size_t)i * n + t] = b[i];
     }
     return true;
+  }
+
+  // -------------------------------------------- propagation (ck_propagate)
+  // Propagator<EigenStepper<>, VoidNavigator>::propagate(start[, target],
+  // options) (Propagator.ipp:25-260): no navigation targets and no actors;
+  // after every accepted step the aborters in list order — SurfaceReached on
+  // the target (StandardAborters.hpp:94-155), then PathLimitReached with the
+  // loop-protected limit (StandardAborters.hpp:41-61, LoopProtection.hpp:
+  // 19-72). The direction is the sign of the path limit.
+  CK_D void startPropagation(const FitParams& fp, int track) {
+    t = track;
+    q = track;
+    const double limit = __ldg(&fp.prop.path_limit[t]);
+    targetSurf = fp.prop.target ? __ldg(&fp.prop.target[t]) : -1;
+    if (targetSurf < -1 || targetSurf >= fp.n_surfaces) {
+      fail(fp, CK_TRACK_INVALID_INPUT);
+      return;
+    }
+    dirSign = limit < 0.0 ? -1.0 : 1.0;  // Direction::fromScalar
+    {
+      double sp[6];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) sp[i] = __ldg(&fp.start_params[6 * (size_t)t + i]);
+      Surf<double> start;
+      start.loadPlane(fp.start_frames + 12 * (size_t)t);
+      boundToFree(start, sp);
+      initT(start);
+      if (fp.start_cov) {
+        const double* sc = fp.start_cov + 36 * (size_t)t;
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+#pragma unroll
+          for (int j = i; j < 6; ++j) cov[sidx(i, j)] = toP<CV>(__ldg(&sc[i * 6 + j]));
+      } else {
+#pragma unroll
+        for (int i = 0; i < 21; ++i) cov[i] = CV(0);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 7; ++i) deriv[i] = P(0);
+    pathAcc = 0.0;
+    cNav = kNotSet;
+    cActor = kNotSet;
+    cUser = fp.opt.maxStepSize;
+    cAcc = fp.opt.initialStepSize;
+    mass = __ldg(&fp.particle[2 * (size_t)t]);
+    absQ = __ldg(&fp.particle[2 * (size_t)t + 1]);
+    pdg = 211;
+    coasting = false;
+    finished = false;
+    stepStarted = false;
+    steps = 0;
+    haveTarget = false;
+    navigationBreak = true;
+    currentSurface = -1;
+    extrapolating = true;
+    propLimit = loopLimit(fp, limit, false);
+    phase = PH_STEP;
+    if (propagationAbort(fp)) finishPropagation(fp);  // pre-propagation check
+  }
+
+  CK_D bool propagationAbort(const FitParams& fp) {
+    if (targetSurf >= 0) {
+      Surf<double> ts;
+      ts.load(fp.surfaces + targetSurf);
+      const double nd[3] = {dirSign * dir[0], dirSign * dir[1], dirSign * dir[2]};
+      const double tol = fp.opt.surfaceTolerance;
+      double path[2] = {0.0, 0.0};
+      int st[2] = {0, 0};
+      int ni = 1;
+      if (ts.type == CK_SURFACE_LINE) {
+        double u = 0.0;
+        if (lineIntersect(ts, pos, nd, tol, u)) {
+          path[0] = u;
+          st[0] = fabs(u) > fabs(tol) ? 1 : 2;
+        }
+      } else if constexpr (sizeof(P) == sizeof(float)) {
+        ni = intersectMixed(ts, pos, nd, tol, path, st);
+      } else {
+        ni = intersect(ts, pos, nd, tol, path, st);
+      }
+      // the closest intersection (Intersection::closestOrder: valid ones
+      // first, then the smallest |path|) decides whether the target is
+      // reached; the first valid one beyond the near limit steers the actor
+      // step constraint (updateSingleSurfaceStatus)
+      int best = -1;
+      for (int i = 0; i < ni; ++i)
+        if (st[i] != 0 && (best < 0 || fabs(path[i]) < fabs(path[best]))) best = i;
+      for (int i = 0; i < ni; ++i)
+        if (st[i] != 0 && path[i] > kTargetNearLimit && path[i] < kNotSet + kOnSurfaceTolerance) {
+          cActor = kNotSet;
+          cupdate(cActor, path[i]);
+          break;
+        }
+      if (best >= 0 && st[best] == 2) return true;
+    }
+    return pathLimitReached(fp, propLimit);
+  }
+
+  // Propagator::makeResult: the bound state on the target (CovarianceEngine
+  // boundState) or the curvilinear state at the end point (curvilinearState,
+  // the plane through the end point with the curvilinear unit vectors)
+  CK_D void finishPropagation(const FitParams& fp) {
+    const size_t n = (size_t)fp.n_tracks;
+    Surf<double> sf;
+    bool curvilinear = false;
+    if (targetSurf >= 0) {
+      sf.load(fp.surfaces + targetSurf);
+      if (sf.type == CK_SURFACE_LINE) {
+        if (!writeReferenceState(fp)) {
+          fail(fp, CK_TRACK_NOT_ON_SURFACE);
+          return;
+        }
+        endPropagationOutputs(fp);
+        return;
+      }
+    } else {
+      // createCurvilinearUnitVectors (UnitVectors.hpp:94-150)
+      double u[3] = {-dir[1], dir[0], 0.0};
+      const double sc = sqrt(u[0] * u[0] + u[1] * u[1]);
+      if (sc < 16.0 * 2.220446049250313e-16) {  // 16 epsilon
+        u[0] = 1.0;
+        u[1] = 0.0;
+      } else {
+        u[0] /= sc;
+        u[1] /= sc;
+      }
+      double v[3] = {dir[1] * u[2] - dir[2] * u[1], dir[2] * u[0] - dir[0] * u[2],
+                     dir[0] * u[1] - dir[1] * u[0]};
+      const double vn = 1.0 / sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        v[i] *= vn;
+        sf.R[i * 3 + 0] = u[i];
+        sf.R[i * 3 + 1] = v[i];
+        sf.R[i * 3 + 2] = dir[i];
+        sf.c[i] = pos[i];
+      }
+      sf.radius = 0.0;
+      sf.type = CK_SURFACE_PLANE;
+      curvilinear = true;
+    }
+    double l[3];
+    local(sf, l);
+    double b[6];
+    if (!freeToBound(fp, sf, l, b)) {
+      fail(fp, CK_TRACK_NOT_ON_SURFACE);
+      return;
+    }
+    if (curvilinear) b[0] = b[1] = 0.0;  // BoundTrackParameters::createCurvilinear
+    Surf<P> sp;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) sp.R[i] = (P)sf.R[i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) sp.c[i] = (P)sf.c[i];
+    sp.radius = (P)sf.radius;
+    sp.type = sf.type;
+    CV J[36];
+    transportToBound(sf, sp, l, J, false);
+    const ck_batch_out& out = fp.out;
+    if (out.track_params) {
+#pragma unroll
+      for (int i = 0; i < 6; ++i) out.track_params[(size_t)i * n + t] = b[i];
+    }
+    if (out.track_cov) {
+#pragma unroll
+      for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = 0; j < 6; ++j) out.track_cov[(size_t)(i * 6 + j) * n + t] = (double)cov[sidx(i, j)];
+    }
+    if (fp.prop.jac) {
+#pragma unroll
+      for (int i = 0; i < 36; ++i) fp.prop.jac[(size_t)i * n + t] = (double)J[i];
+    }
+    if (curvilinear && fp.prop.frames) {
+      double* fr = fp.prop.frames + 12 * (size_t)t;
+#pragma unroll
+      for (int i = 0; i < 9; ++i) fr[i] = sf.R[i];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) fr[9 + i] = sf.c[i];
+    }
+    endPropagationOutputs(fp);
+  }
+
+  CK_D void endPropagationOutputs(const FitParams& fp) {
+    if (fp.prop.path) fp.prop.path[t] = pathAcc;
+    if (fp.prop.steps) fp.prop.steps[t] = (int32_t)steps;
+    fp.out.status[t] = CK_TRACK_OK;
+    phase = PH_DONE;
   }
 
   // SURFACE: the actor on the reached surface

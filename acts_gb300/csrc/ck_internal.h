@@ -112,6 +112,18 @@ struct ExtStart {
 };
 static_assert(sizeof(ExtStart) == 224, "extrapolation start layout");
 
+// The propagation entry's per-track targets and path limits (inputs) and its
+// outputs (ck_propagate_out; end parameters and covariance go through
+// FitParams::out.track_params / track_cov). Unused (NULL) in the fit.
+struct PropIO {
+  const int32_t* target;
+  const double* path_limit;
+  double* jac;     // [36][n] transport Jacobian, or NULL
+  double* frames;  // [n*12] end plane without a target, or NULL
+  double* path;    // [n], or NULL
+  int32_t* steps;  // [n], or NULL
+};
+
 struct FitParams {
   int n_tracks;
   int n_queue;  // number of slots in the work queue (= n_tracks)
@@ -161,6 +173,7 @@ struct FitParams {
   int ref_strategy;
   ExtStart* ext;
   DevOptions extOpt;
+  PropIO prop;
 };
 
 }  // namespace ck

@@ -135,15 +135,18 @@ __global__ void materialKernel(int n, MatConst mc, const DevSurface* __restrict_
   out[4 * i + 3] = e.varQoP;
 }
 
+// getField in the stepper scalar P: the positions rounded to P as the
+// Runge-Kutta stages round them (FP32 in the mixed form)
+template <typename P>
 __global__ void fieldKernel(int n, DevField F, const double* __restrict__ pos, double* out,
                             int32_t* status) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
-  double B[3] = {0, 0, 0};
+  const P p[3] = {toP<P>(pos[3 * i]), toP<P>(pos[3 * i + 1]), toP<P>(pos[3 * i + 2])};
+  P B[3] = {0, 0, 0};
   const bool ok = getField(F, p, B);
   status[i] = ok ? 0 : CK_TRACK_FIELD_OUT_OF_BOUNDS;
-  for (int c = 0; c < 3; ++c) out[3 * i + c] = ok ? B[c] : 0.0;
+  for (int c = 0; c < 3; ++c) out[3 * i + c] = ok ? (double)B[c] : 0.0;
 }
 
 // Scratch arena for one synchronous unit call.
@@ -373,7 +376,14 @@ ck_status ck_atan2_mixed(ck_handle* h, int32_t n, const double* y, const double*
 
 ck_status ck_field_lookup(ck_handle* h, int32_t n, const double* pos, double* out,
                           int32_t* status) {
+  return ck_field_lookup_precision(h, CK_PRECISION_FP64, n, pos, out, status);
+}
+
+ck_status ck_field_lookup_precision(ck_handle* h, int32_t precision, int32_t n, const double* pos,
+                                    double* out, int32_t* status) {
   if (!h || n < 0 || !pos || !out || !status) return fail(CK_ERR_INVALID_ARGUMENT, "bad argument");
+  if (precision != CK_PRECISION_FP64 && precision != CK_PRECISION_MIXED)
+    return fail(CK_ERR_INVALID_ARGUMENT, "unknown precision");
   if (n == 0) return CK_OK;
   std::lock_guard<std::mutex> lock(h->mu);
   cudaSetDevice(h->device);
@@ -385,8 +395,12 @@ ck_status ck_field_lookup(ck_handle* h, int32_t n, const double* pos, double* ou
   if (e != cudaSuccess) return cudaFail(e, "unit buffer");
   cudaStream_t st = h->stream;
   cudaMemcpyAsync(a.at<double>(tP), pos, 24 * n, cudaMemcpyHostToDevice, st);
-  fieldKernel<<<(n + 127) / 128, 128, 0, st>>>(n, h->field, a.at<double>(tP), a.at<double>(tO),
-                                               a.at<int32_t>(tS));
+  if (precision == CK_PRECISION_FP64)
+    fieldKernel<double><<<(n + 127) / 128, 128, 0, st>>>(n, h->field, a.at<double>(tP),
+                                                         a.at<double>(tO), a.at<int32_t>(tS));
+  else
+    fieldKernel<float><<<(n + 127) / 128, 128, 0, st>>>(n, h->field, a.at<double>(tP),
+                                                        a.at<double>(tO), a.at<int32_t>(tS));
   cudaMemcpyAsync(out, a.at<double>(tO), 24 * n, cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(status, a.at<int32_t>(tS), 4 * n, cudaMemcpyDeviceToHost, st);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cudaFail(e, "field kernel");

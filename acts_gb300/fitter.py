@@ -89,6 +89,10 @@ def lib():
                                           abi.P_f64, abi.P_f32, abi.P_f32, abi.P_i32, C.c_int32,
                                           C.c_int32, abi.P_f64]
         L.ck_field_lookup.argtypes = [C.c_void_p, C.c_int32, abi.P_f64, abi.P_f64, abi.P_i32]
+        L.ck_propagate.argtypes = [C.c_void_p, P(abi.ck_options), P(abi.ck_propagate_in),
+                                   P(abi.ck_propagate_out), C.c_void_p]
+        L.ck_field_lookup_precision.argtypes = [C.c_void_p, C.c_int32, C.c_int32, abi.P_f64,
+                                                abi.P_f64, abi.P_i32]
         L.ck_fp_peak_gflops.argtypes = [C.c_void_p, C.c_int32, P(C.c_double)]
         L.ck_abi_struct_sizes.argtypes = [P(C.c_int64), C.c_int32]
         L.ck_abi_struct_sizes.restype = None
@@ -436,12 +440,23 @@ class CudaKalman:
                                          int(ms), int(el), abi.ptr(out, C.c_double)))
         return out
 
-    def field_lookup(self, pos):
+    def propagate(self, options, prop):
+        """ck_propagate on an abi.Propagation (host arrays, filled in place):
+        Propagator::propagate(start[, target], options) with the fitter's
+        stepper in the options' precision form."""
+        i, o = prop.as_in(), prop.as_out()
+        _check(lib().ck_propagate(self._h, C.byref(options), C.byref(i), C.byref(o), None))
+        return prop
+
+    def field_lookup(self, pos, precision=abi.PRECISION_FP64):
+        """getField on the device in a form's stepper arithmetic (FP64, or
+        the mixed form's FP32 lookup)."""
         pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
         out = np.zeros_like(pos)
         st = np.zeros(len(pos), np.int32)
-        _check(lib().ck_field_lookup(self._h, len(pos), abi.ptr(pos, C.c_double),
-                                     abi.ptr(out, C.c_double), abi.ptr(st, C.c_int32)))
+        _check(lib().ck_field_lookup_precision(self._h, int(precision), len(pos),
+                                               abi.ptr(pos, C.c_double), abi.ptr(out, C.c_double),
+                                               abi.ptr(st, C.c_int32)))
         return out, st
 
 

@@ -553,6 +553,62 @@ ck_status ck_material_effects(ck_handle* h, int32_t n, const int32_t* surface,
  * field); out[3*n] in GeV/(e*mm); status per point. Host pointers. */
 ck_status ck_field_lookup(ck_handle* h, int32_t n, const double* pos,
                           double* out, int32_t* status);
+/* The same lookup in a precision form's stepper arithmetic: FP64, or the
+ * mixed form's FP32 lookup (positions rounded to float, trilinear weights
+ * and interpolation in float) that its Runge-Kutta stages evaluate. */
+ck_status ck_field_lookup_precision(ck_handle* h, int32_t precision, int32_t n,
+                                    const double* pos, double* out, int32_t* status);
+
+/* ------------------------------------------------------- propagation */
+/* A batch of independent propagations of bound track parameters with the
+ * fitter's stepper (the same Runge-Kutta, transport and intersection code as
+ * the fit, in the options' precision form):
+ *   Propagator<EigenStepper<>, VoidNavigator>::propagate(start, options) and
+ *   ::propagate(start, target, options)
+ *   (Core/include/Acts/Propagator/Propagator.ipp:25-260) with the
+ *   SurfaceReached aborter on the target (StandardAborters.hpp:66-155) and
+ *   PathLimitReached with loop protection (StandardAborters.hpp:24-62,
+ *   detail/LoopProtection.hpp:19-72); no actors, no material.
+ * Each propagation runs in the direction of the sign of its path limit (a
+ * target is reached forward with a positive limit). With a target its end
+ * parameters are bound on the target (Propagator::makeResult's boundState);
+ * without one they are curvilinear at the end point (loc0 = loc1 = 0 on the
+ * plane through the end point normal to the direction, its frame the
+ * curvilinear unit vectors of UnitVectors.hpp:94-150), and the frame is
+ * returned in end_frames, so that the result can start another propagation.
+ * Options used: precision, step_tolerance, step_size_cutoff,
+ * initial_step_size, max_step_size, max_rk_step_trials, max_steps,
+ * loop_protection, loop_fraction, surface_tolerance. Per-track status as the
+ * fit's (CK_TRACK_*). Inputs use the per-track layout of ck_batch_in,
+ * outputs the structure-of-arrays layout of ck_batch_out's track_params
+ * (element c of track t at [c * n + t]). */
+typedef struct ck_propagate_in {
+  int32_t n;
+  int32_t memory;              /* CK_MEM_HOST or CK_MEM_DEVICE (inputs and outputs) */
+  const double* start_params;  /* [n*6] bound parameters on the start plane  */
+  const double* start_cov;     /* [n*36] row-major, or NULL: no covariance   */
+  const double* start_frames;  /* [n*12] start plane as in ck_batch_in        */
+  const float* particle;       /* [n*2] (mass GeV, |q|)                       */
+  const int32_t* target;       /* [n] surface-table index of the target
+                                  (plane, cylinder or line), -1: none; NULL:
+                                  no targets                                  */
+  const double* path_limit;    /* [n] signed path limit (mm)                  */
+} ck_propagate_in;
+
+typedef struct ck_propagate_out {
+  int32_t* status;       /* [n] CK_TRACK_*                                     */
+  double* end_params;    /* [6][n] bound parameters at the end                 */
+  double* end_cov;       /* [36][n] transported covariance, or NULL            */
+  double* jacobian;      /* [36][n] bound-to-bound transport Jacobian from the
+                            start surface to the end surface, or NULL          */
+  double* end_frames;    /* [n*12] the end plane of a propagation without a
+                            target (ck_batch_in layout), or NULL               */
+  double* path_length;   /* [n] signed path length, or NULL                    */
+  int32_t* steps;        /* [n] accepted Runge-Kutta steps, or NULL            */
+} ck_propagate_out;
+
+ck_status ck_propagate(ck_handle* h, const ck_options* options, const ck_propagate_in* in,
+                       ck_propagate_out* out, void* stream);
 
 /* ------------------------------------------------------------- serving */
 

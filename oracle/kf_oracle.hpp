@@ -1354,6 +1354,161 @@ void transportCovarianceToBound(Stepper<S>& st, const Surface<S>& s, bool correc
     st.jacToGlobal = s.boundToFreeJacobian(pos, dir);
 }
 
+// ------------------------------------------------------------ propagation
+// Propagator<EigenStepper<>, VoidNavigator>::propagate(start[, target],
+// options) (Propagator.ipp:25-260): EigenStepper::initialize from bound
+// parameters on a plane, the stepping loop without navigation targets and
+// actors, the aborters in list order after every step — SurfaceReached on
+// the target (StandardAborters.hpp:66-155; its near limit -100 um) and
+// PathLimitReached (StandardAborters.hpp:24-62) with the loop protection of
+// LoopProtection.hpp:19-72 — and makeResult: the bound state on the target
+// (CovarianceEngine.cpp:29-63) or the curvilinear state at the end point
+// (CovarianceEngine.cpp:65-99, JacobianEngine.cpp:61-82, UnitVectors.hpp:
+// 94-150). The direction is Direction::fromScalar(pathLimit).
+struct PropResult {
+  int status = CK_TRACK_OK;
+  Vec<double, 6> params;
+  Mat<double, 6, 6> cov, jacobian;
+  double frame[12] = {0};  // the curvilinear end plane (no target)
+  double pathLength = 0;
+  int steps = 0;
+};
+
+template <typename S>
+PropResult propagate(const Field<S>& field, const Options& o, const Surface<S>& start,
+                     const Vec<S, 6>& startParams, const Mat<S, 6, 6>& startCov, float mass,
+                     float absQ, const Surface<S>* target, double pathLimit) {
+  using std::abs;
+  PropResult r;
+  const int propDir = pathLimit < 0 ? -1 : 1;
+  Stepper<S> st;
+  st.mass = mass;
+  st.absQ = absQ;
+  st.pars = boundToFree(start, startParams);
+  st.cov = startCov;
+  st.jacToGlobal = start.boundToFreeJacobian(st.pos(), st.dir());
+  st.jacobian = Mat<S, 6, 6>::identity();
+  st.jacTransport = Mat<S, 8, 8>::identity();
+  st.derivative = Vec<S, 8>::zero();
+  st.stepSize = ConstrainedStep();
+  st.stepSize.accuracy = o.initialStepSize;
+  st.stepSize.values[kUser] = o.maxStepSize;
+  double limit = pathLimit;
+  if (o.loopProtection) {
+    V3<S> B;
+    if (field.get(st.pos(), B)) {
+      const double Bn = (double)norm(B);
+      if (Bn != 0) {
+        const double helix = propDir * 2 * kPi * (double)st.absoluteMomentum() / Bn;
+        const double loop = o.loopFraction * helix;
+        if (std::abs(loop) < std::abs(limit)) limit = loop;
+      }
+    }
+  }
+  auto checkAbort = [&]() -> bool {
+    if (target) {
+      V3<S> d = st.dir();
+      for (int i = 0; i < 3; ++i) d[i] = S(double(propDir)) * d[i];
+      Intersection<S> is[2];
+      int n = target->intersect(st.pos(), d, S(o.surfaceTolerance), is);
+      if (target->type == CK_SURFACE_LINE && n == 0) {
+        is[0] = Intersection<S>{S(0.0), IStatus::unreachable};
+        n = 1;
+      }
+      // MultiIntersection::closest (Intersection::closestOrder)
+      int best = -1;
+      for (int i = 0; i < n; ++i)
+        if (is[i].valid() && (best < 0 || abs(is[i].pathLength) < abs(is[best].pathLength)))
+          best = i;
+      const bool reached = best >= 0 && is[best].status == IStatus::onSurface;
+      for (int i = 0; i < n; ++i) {
+        const double pl = (double)is[i].pathLength;
+        if (is[i].valid() && pl > -0.1 &&
+            pl < std::numeric_limits<double>::max() + kOnSurfaceTolerance) {
+          // updateSingleSurfaceStatus (SteppingHelper.hpp:41-78)
+          st.stepSize.release(kActor);
+          st.stepSize.update(pl, kActor);
+          break;
+        }
+      }
+      if (reached) return true;
+    }
+    const double dist = std::abs(limit) - std::abs((double)st.pathAccumulated);
+    if (std::abs(dist) < std::abs(o.surfaceTolerance)) return true;
+    st.stepSize.update(dist, kActor);
+    return false;
+  };
+  if (!checkAbort()) {
+    bool terminated = false;
+    for (unsigned s = 0; s < o.maxSteps; ++s) {
+      S h;
+      const int se = eigenStep(st, field, o, h, propDir);
+      if (se != kStepOk) {
+        r.status = se == kStepField ? CK_TRACK_FIELD_OUT_OF_BOUNDS
+                                    : (se == kStepStalled ? CK_TRACK_STEP_SIZE_STALLED
+                                                          : CK_TRACK_STEP_ADJUST_FAILED);
+        return r;
+      }
+      st.stepSize.release(kNav);
+      st.stepSize.release(kActor);
+      if (checkAbort()) {
+        terminated = true;
+        break;
+      }
+    }
+    if (!terminated) {
+      r.status = CK_TRACK_STEP_COUNT_LIMIT;
+      return r;
+    }
+  }
+  Surface<S> end;
+  bool curvilinear = false;
+  if (target) {
+    end = *target;
+  } else {
+    // the curvilinear frame (UnitVectors.hpp:94-150) at the end point
+    const V3<S> d = st.dir();
+    V3<S> u{{-d[1], d[0], S(0.0)}};
+    const S sc = std::sqrt(u[0] * u[0] + u[1] * u[1]);
+    if (sc < S(16.0 * std::numeric_limits<double>::epsilon())) {
+      u[0] = S(1.0);
+      u[1] = S(0.0);
+    } else {
+      u[0] = u[0] / sc;
+      u[1] = u[1] / sc;
+    }
+    V3<S> v = normalized(cross(d, u));
+    end.type = CK_SURFACE_PLANE;
+    for (int i = 0; i < 3; ++i) {
+      end.R[i][0] = u[i];
+      end.R[i][1] = v[i];
+      end.R[i][2] = d[i];
+      end.c[i] = st.pars[i];
+      r.frame[i * 3 + 0] = (double)u[i];
+      r.frame[i * 3 + 1] = (double)v[i];
+      r.frame[i * 3 + 2] = (double)d[i];
+      r.frame[9 + i] = (double)st.pars[i];
+    }
+    curvilinear = true;
+  }
+  Vec<S, 6> bp;
+  if (!freeToBound(st.pars, end, bp)) {
+    r.status = CK_TRACK_NOT_ON_SURFACE;
+    return r;
+  }
+  transportCovarianceToBound(st, end);
+  if (curvilinear) bp[0] = bp[1] = S(0.0);
+  for (int i = 0; i < 6; ++i) r.params[i] = (double)bp[i];
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) {
+      r.cov.a[i][j] = (double)st.cov.a[i][j];
+      r.jacobian.a[i][j] = (double)st.jacobian.a[i][j];
+    }
+  r.pathLength = (double)st.pathAccumulated;
+  r.steps = st.nSteps;
+  return r;
+}
+
 // -------------------------------------------------------------- KF output
 struct TrackOut {
   int status = CK_TRACK_NOT_PROCESSED;

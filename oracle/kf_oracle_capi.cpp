@@ -339,6 +339,56 @@ void kfo_field_lookup(const ck_field* f, int n, const double* pos, double* outB,
   }
 }
 
+// The propagation restatement on a batch in ck_propagate's layout (inputs
+// per track, outputs [c * n + t]); host arrays; the options' stepper fields.
+void kfo_propagate(const ck_options* opt, int n_surfaces, const ck_surface* surfaces,
+                   const ck_field* field, const ck_propagate_in* in, ck_propagate_out* out,
+                   int n_threads) {
+  std::vector<Surface<double>> sf;
+  for (int i = 0; i < n_surfaces; ++i) sf.push_back(Surface<double>::fromCk(surfaces[i]));
+  const Field<double> F = Field<double>::make(*field);
+  const Options o = Options::fromCk(*opt, false);
+  const int n = in->n;
+  std::atomic<int> next{0};
+  auto worker = [&]() {
+    while (true) {
+      const int t = next.fetch_add(1);
+      if (t >= n) break;
+      const Surface<double> start = Surface<double>::plane(in->start_frames + 12 * (size_t)t);
+      const Vec<double, 6> p = get6<double>(in->start_params + 6 * (size_t)t);
+      Mat<double, 6, 6> c = Mat<double, 6, 6>::zero();
+      if (in->start_cov) c = get36<double>(in->start_cov + 36 * (size_t)t);
+      const int tg = in->target ? in->target[t] : -1;
+      PropResult r;
+      if (tg < -1 || tg >= n_surfaces) {
+        r.status = CK_TRACK_INVALID_INPUT;
+      } else {
+        r = propagate(F, o, start, p, c, in->particle[2 * (size_t)t], in->particle[2 * (size_t)t + 1],
+                      tg >= 0 ? &sf[tg] : nullptr, in->path_limit[t]);
+      }
+      out->status[t] = r.status;
+      if (r.status != CK_TRACK_OK) continue;
+      for (int i = 0; i < 6; ++i) out->end_params[(size_t)i * n + t] = r.params[i];
+      for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+          if (out->end_cov) out->end_cov[(size_t)(i * 6 + j) * n + t] = r.cov.a[i][j];
+          if (out->jacobian) out->jacobian[(size_t)(i * 6 + j) * n + t] = r.jacobian.a[i][j];
+        }
+      if (out->end_frames && tg < 0)
+        for (int i = 0; i < 12; ++i) out->end_frames[12 * (size_t)t + i] = r.frame[i];
+      if (out->path_length) out->path_length[t] = r.pathLength;
+      if (out->steps) out->steps[t] = r.steps;
+    }
+  };
+  if (n_threads <= 1) {
+    worker();
+  } else {
+    std::vector<std::thread> th;
+    for (int i = 0; i < n_threads; ++i) th.emplace_back(worker);
+    for (auto& x : th) x.join();
+  }
+}
+
 // Counts how often glibc logf differs from the correctly rounded float
 // logarithm used by both implementations, over n inputs.
 int kfo_logf_mismatch(int n, const float* x) {

@@ -50,6 +50,10 @@ def lib():
         L.kfo_field_lookup.restype = None
         L.kfo_field_lookup.argtypes = [C.POINTER(abi.ck_field), C.c_int, abi.P_f64, abi.P_f64,
                                        abi.P_i32]
+        L.kfo_propagate.restype = None
+        L.kfo_propagate.argtypes = [C.POINTER(abi.ck_options), C.c_int, C.POINTER(abi.ck_surface),
+                                    C.POINTER(abi.ck_field), C.POINTER(abi.ck_propagate_in),
+                                    C.POINTER(abi.ck_propagate_out), C.c_int]
         L.kfo_logf_mismatch.restype = C.c_int
         L.kfo_logf_mismatch.argtypes = [C.c_int, abi.P_f32]
         L.kfo_hardware_threads.restype = C.c_int
@@ -171,6 +175,16 @@ def field_lookup(field, pos):
     lib().kfo_field_lookup(C.byref(field), len(pos), abi.ptr(pos, C.c_double),
                            abi.ptr(out, C.c_double), abi.ptr(st, C.c_int32))
     return out, st
+
+
+def propagate(surfaces, field, options, prop, n_threads=1):
+    """The propagation restatement on an abi.Propagation (filled in place);
+    `surfaces` a ctypes array of ck_surface (the target table)."""
+    i, o = prop.as_in(), prop.as_out()
+    n_surf = len(surfaces) if surfaces is not None else 0
+    lib().kfo_propagate(C.byref(options), n_surf, surfaces, C.byref(field), C.byref(i),
+                        C.byref(o), n_threads)
+    return prop
 
 
 def logf_mismatch(x):

@@ -26,9 +26,7 @@ def compare(gpu, ora, rtol=1e-9, fields=("predicted", "filtered", "smoothed"), e
     for name in ("n_states", "n_measurements", "n_holes", "n_outliers", "ndf"):
         rep[name + "_mismatch"] = int(np.sum(getattr(gpu, name)[ok] != getattr(ora, name)[ok]))
     ms = gpu.max_states
-    valid = np.zeros((gpu.n, ms), bool)
-    for t in np.nonzero(ok)[0]:
-        valid[t, : gpu.n_states[t]] = True
+    valid = (np.arange(ms)[None, :] < gpu.n_states[:, None]) & ok[:, None]
     rep["flags_mismatch"] = int(np.sum((gpu.view("state_flags") != ora.view("state_flags")) & valid))
     rep["surface_mismatch"] = int(np.sum((gpu.view("state_surface") != ora.view("state_surface")) & valid))
 

@@ -46,10 +46,11 @@ def test_generator_exports_every_declared_symbol():
 
 def test_struct_layouts_match(cklib):
     cklib.ck_abi_struct_sizes.argtypes = [C.POINTER(C.c_int64), C.c_int32]
-    out = (C.c_int64 * 7)()
-    cklib.ck_abi_struct_sizes(out, 7)
+    out = (C.c_int64 * 9)()
+    cklib.ck_abi_struct_sizes(out, 9)
     mirrors = [abi.ck_surface, abi.ck_field, abi.ck_options, abi.ck_config, abi.ck_batch_in,
-               abi.ck_batch_out, abi.ck_server_config]
+               abi.ck_batch_out, abi.ck_server_config, abi.ck_propagate_in,
+               abi.ck_propagate_out]
     assert [C.sizeof(m) for m in mirrors] == list(out)
 
 

@@ -46,26 +46,49 @@ def _pulls(res, b):
     return [np.std(np.clip(np.array(p), -10, 10)) for p in out]
 
 
+# The uneven workload (the batched-events and serving configurations): the
+# trilinear grid field map read in FP32 by the mixed form's stages, holes,
+# 10-sigma outliers and the chi2 outlier cut of 15. Its options are part of
+# the case ("opts"); the other keys of `extra` are fit options too.
+UNEVEN = dict(outlier_chi2_cut=15.0)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("preset,smoother,extra",
                          [(abi.CKG_BARREL, abi.SMOOTHER_GAIN_MATRIX, {}),
                           (abi.CKG_BARREL, abi.SMOOTHER_MBF, {}),
                           (abi.CKG_STRIPS, abi.SMOOTHER_GAIN_MATRIX, {}),
                           (abi.CKG_BARREL, abi.SMOOTHER_GAIN_MATRIX,
-                           {"free_to_bound_correction": 1})],
-                         ids=["gain_matrix", "mbf", "strips", "free_to_bound_correction"])
+                           {"free_to_bound_correction": 1}),
+                          (abi.CKG_UNEVEN, abi.SMOOTHER_GAIN_MATRIX, {"opts": UNEVEN}),
+                          (abi.CKG_UNEVEN, abi.SMOOTHER_GAIN_MATRIX,
+                           {"opts": dict(UNEVEN, early_termination=1)}),
+                          (abi.CKG_UNEVEN, abi.SMOOTHER_MBF,
+                           {"opts": dict(UNEVEN, early_termination=1)})],
+                         ids=["gain_matrix", "mbf", "strips", "free_to_bound_correction",
+                              "uneven_grid_field", "uneven_grid_field_early_termination",
+                              "uneven_grid_field_mbf"])
 def test_mixed_precision_accuracy(fitter_factory, preset, smoother, extra):
     precision = abi.PRECISION_MIXED
-    n = 20000
+    extra = dict(extra)
+    opts = extra.pop("opts", {})
+    n = 20000 if preset != abi.CKG_UNEVEN else 40000
     det = detector(preset)
     b = batch(preset, n, seed=13)
-    ora = Results(n, 12)
-    kforacle.fit_batch(det, b, abi.default_options(smoother=smoother, **extra), ora,
+    ms = 12 if preset != abi.CKG_UNEVEN else 22
+    ora = Results(n, ms)
+    kforacle.fit_batch(det, b, abi.default_options(smoother=smoother, **extra, **opts), ora,
                        n_threads=kforacle.hardware_threads())
     mix = fitter_factory(preset).fit_batch(
-        b, abi.default_options(precision=precision, smoother=smoother, **extra), max_states=12)
+        b, abi.default_options(precision=precision, smoother=smoother, **extra, **opts),
+        max_states=ms)
     agree = np.mean(mix.status == ora.status)
+    print("status agreement %.6f, fitted %d" % (agree, int((ora.status == 0).sum())))
     assert agree > 0.999, agree
+    if preset == abi.CKG_UNEVEN:
+        # enough fitted tracks for the bounds to mean something (without
+        # early termination ~40 % of the tracks coast out of the map)
+        assert (ora.status == 0).sum() > 0.5 * n
     ok = (mix.status == 0) & (ora.status == 0)
     # the bound applies to valid fits: tracks whose FP64 fit is broken (the
     # cylinder phi = +-pi seam, chi2/ndf in the millions) are chaotic in any
@@ -78,7 +101,7 @@ def test_mixed_precision_accuracy(fitter_factory, preset, smoother, extra):
         # looping tracks the correction throws off the cylinders (|loc0|
         # beyond the circumference) are broken in any precision
         loc0 = np.abs(ora.view("smoothed")[..., 0])
-        inside = np.arange(12)[None, :] < ora.n_states[:, None]
+        inside = np.arange(ms)[None, :] < ora.n_states[:, None]
         broken = ((loc0 > 2 * np.pi * 1100.0) & inside).any(axis=1)
         assert (good & broken).sum() <= 5e-4 * n
         good &= ~broken

@@ -191,6 +191,36 @@ def test_field_lookup_matches_oracle(fitter_factory):
     np.testing.assert_allclose(g[ok], o[ok], rtol=1e-12, atol=1e-18)
 
 
+# FP32 field lookup of the mixed form against the FP64 oracle: the float
+# nodes are exact in both; the position rounded to float (ulp 2.4e-4 mm at
+# 3 m), the float trilinear weights and the float interpolation each give a
+# few 1e-7 of the field scale, so every component must agree with the FP64
+# lookup within 2e-6 of the map's maximum |B|.
+FIELD_FP32_BOUND = 2e-6
+
+
+@pytest.mark.gpu
+def test_field_lookup_fp32_matches_oracle(fitter_factory):
+    det = detector(abi.CKG_UNEVEN)
+    fit = fitter_factory(abi.CKG_UNEVEN)
+    rng = np.random.default_rng(4)
+    pts = rng.uniform([-1600, -1600, -3100], [1600, 1600, 3100], size=(50000, 3))
+    g, gs = fit.field_lookup(pts, abi.PRECISION_MIXED)
+    o, os_ = kforacle.field_lookup(det.field, pts)
+    # the status differs only where rounding to float moves a point across
+    # the map's edge (a float ulp from it)
+    edge = np.zeros(len(pts), bool)
+    for i, (lo, hi) in enumerate(((-1500.0, 1500.0), (-1500.0, 1500.0), (-3000.0, 3000.0))):
+        edge |= (np.abs(pts[:, i] - lo) < 1e-3) | (np.abs(pts[:, i] - hi) < 1e-3)
+    assert np.array_equal(gs[~edge], os_[~edge])
+    ok = (gs == 0) & (os_ == 0)
+    assert ok.sum() > 25000
+    scale = np.abs(o[ok]).max()
+    err = np.abs(g[ok] - o[ok]).max() / scale
+    print("FP32 field lookup: max |dB| / max |B| = %.3g" % err)
+    assert err <= FIELD_FP32_BOUND
+
+
 @pytest.mark.gpu
 def test_mixed_form_atan2_matches_correctly_rounded(fitter_factory):
     """The mixed form's table-driven FP64 atan2 against numpy's arctan2 on
