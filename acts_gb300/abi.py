@@ -73,6 +73,7 @@ OUT_FILTERED = 1 << 1
 OUT_SMOOTHED = 1 << 2
 OUT_JACOBIAN = 1 << 3
 OUT_REFERENCE = 1 << 4
+OUT_PACKED_COV = 1 << 5
 EXTRAPOLATE_FIRST = 0
 EXTRAPOLATE_LAST = 1
 EXTRAPOLATE_FIRST_OR_LAST = 2

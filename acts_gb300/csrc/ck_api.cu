@@ -746,6 +746,7 @@ static ck_status fitBatchHostChunked(ck_handle* h, const ck_options& opt, const 
   }
   // ---- device output buffers: per track, per state (rows ms x C) or per
   // track component (rows C)
+  const int cc = covComponents(out);
   struct Out {
     void* host;
     int rows;  // copy rows of one track column
@@ -755,8 +756,8 @@ static ck_status fitBatchHostChunked(ck_handle* h, const ck_options& opt, const 
       {out.n_holes, 1, 4},      {out.n_outliers, 1, 4},         {out.ndf, 1, 4},
       {out.chi2_sum, 1, 8},     {out.state_surface, ms, 4},     {out.state_flags, ms, 4},
       {out.state_path_length, ms, 8}, {out.state_chi2, ms, 8},  {out.predicted, 6 * ms, 8},
-      {out.predicted_cov, 36 * ms, 8}, {out.filtered, 6 * ms, 8}, {out.filtered_cov, 36 * ms, 8},
-      {out.smoothed, 6 * ms, 8}, {out.smoothed_cov, 36 * ms, 8}, {out.jacobian, 36 * ms, 8},
+      {out.predicted_cov, cc * ms, 8}, {out.filtered, 6 * ms, 8}, {out.filtered_cov, cc * ms, 8},
+      {out.smoothed, 6 * ms, 8}, {out.smoothed_cov, cc * ms, 8}, {out.jacobian, 36 * ms, 8},
       {out.track_params, 6, 8}, {out.track_cov, 36, 8},
   };
   static_assert(sizeof(outs) / sizeof(outs[0]) == kOutArrays, "output arrays");
@@ -955,11 +956,11 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
         {(void**)&dout.state_path_length, compBytes(n, ms, 1, 8)},
         {(void**)&dout.state_chi2, compBytes(n, ms, 1, 8)},
         {(void**)&dout.predicted, compBytes(n, ms, 6, 8)},
-        {(void**)&dout.predicted_cov, compBytes(n, ms, 36, 8)},
+        {(void**)&dout.predicted_cov, compBytes(n, ms, covComponents(*out), 8)},
         {(void**)&dout.filtered, compBytes(n, ms, 6, 8)},
-        {(void**)&dout.filtered_cov, compBytes(n, ms, 36, 8)},
+        {(void**)&dout.filtered_cov, compBytes(n, ms, covComponents(*out), 8)},
         {(void**)&dout.smoothed, compBytes(n, ms, 6, 8)},
-        {(void**)&dout.smoothed_cov, compBytes(n, ms, 36, 8)},
+        {(void**)&dout.smoothed_cov, compBytes(n, ms, covComponents(*out), 8)},
         {(void**)&dout.jacobian, compBytes(n, ms, 36, 8)},
         {(void**)&dout.track_params, sizeof(double) * 6 * (size_t)n},
         {(void**)&dout.track_cov, sizeof(double) * 36 * (size_t)n},

@@ -75,6 +75,11 @@ inline bool anyReverse(const ck_options& o) {
 }
 inline bool needsExtStart(const ck_options& o) { return o.reference_surface >= 0 || anyReverse(o); }
 DevOptions toDevOptions(const ck_options& o);
+// components per state of the covariance arrays of a ck_batch_out (21 packed,
+// 36 full)
+inline int covComponents(const ck_batch_out& o) {
+  return (o.components & CK_OUT_PACKED_COV) ? 21 : 36;
+}
 MatConst makeMatConst();
 DevSurface toDevSurface(const ck_surface& s);
 size_t recordStateBytes(int precision);

@@ -1982,37 +1982,55 @@ struct Smoother {
       chi2sum += c2;
       ndf += (sub & 1) + (sub >> 1);
     }
+    // CK_OUT_PACKED_COV: the upper triangle (21) instead of the full matrix
+    const bool packed = (out.components & CK_OUT_PACKED_COV) != 0;
     if (out.smoothed) {
 #pragma unroll
       for (int i = 0; i < 6; ++i) out.smoothed[at(6, i)] = sm[i];
+      if (packed) {
 #pragma unroll
-      for (int i = 0; i < 6; ++i)
+        for (int i = 0; i < 21; ++i) out.smoothed_cov[at(21, i)] = toDi(Ps[i]);
+      } else {
 #pragma unroll
-        for (int j = i; j < 6; ++j) {
-          const double v = toDi(Ps[sidx(i, j)]);
-          out.smoothed_cov[at(36, i * 6 + j)] = v;
-          if (j != i) out.smoothed_cov[at(36, j * 6 + i)] = v;
-        }
+        for (int i = 0; i < 6; ++i)
+#pragma unroll
+          for (int j = i; j < 6; ++j) {
+            const double v = toDi(Ps[sidx(i, j)]);
+            out.smoothed_cov[at(36, i * 6 + j)] = v;
+            if (j != i) out.smoothed_cov[at(36, j * 6 + i)] = v;
+          }
+      }
     }
     if (out.filtered) {
 #pragma unroll
       for (int i = 0; i < 6; ++i)
         out.filtered[at(6, i)] = filtOverride ? sm[i] : rec.p(k, kRecFilt + i);
+      if (packed) {
 #pragma unroll
-      for (int i = 0; i < 6; ++i)
+        for (int i = 0; i < 21; ++i)
+          out.filtered_cov[at(21, i)] = (double)(filtOverride ? Ps[i] : rec.m(k, kRecFiltCov + i));
+      } else {
 #pragma unroll
-        for (int j = 0; j < 6; ++j)
-          out.filtered_cov[at(36, i * 6 + j)] =
-              (double)(filtOverride ? Ps[sidx(i, j)] : rec.m(k, kRecFiltCov + sidx(i, j)));
+        for (int i = 0; i < 6; ++i)
+#pragma unroll
+          for (int j = 0; j < 6; ++j)
+            out.filtered_cov[at(36, i * 6 + j)] =
+                (double)(filtOverride ? Ps[sidx(i, j)] : rec.m(k, kRecFiltCov + sidx(i, j)));
+      }
     }
     if (out.predicted) {
 #pragma unroll
       for (int i = 0; i < 6; ++i) out.predicted[at(6, i)] = rec.p(k, kRecPred + i);
+      if (packed) {
 #pragma unroll
-      for (int i = 0; i < 6; ++i)
+        for (int i = 0; i < 21; ++i) out.predicted_cov[at(21, i)] = (double)rec.m(k, kRecPredCov + i);
+      } else {
 #pragma unroll
-        for (int j = 0; j < 6; ++j)
-          out.predicted_cov[at(36, i * 6 + j)] = (double)rec.m(k, kRecPredCov + sidx(i, j));
+        for (int i = 0; i < 6; ++i)
+#pragma unroll
+          for (int j = 0; j < 6; ++j)
+            out.predicted_cov[at(36, i * 6 + j)] = (double)rec.m(k, kRecPredCov + sidx(i, j));
+      }
     }
     if (out.jacobian) {
 #pragma unroll

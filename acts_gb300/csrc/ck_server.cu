@@ -68,6 +68,7 @@ struct Event {
 // Output components computed by the server.
 struct OutSpec {
   bool sm, fi, pr, jac;
+  bool packed;  // CK_OUT_PACKED_COV: covariance arrays of 21 components
 };
 
 struct Slot {
@@ -155,13 +156,19 @@ struct ck_server {
     const size_t k = kPlannedSurfacesPerTrack;
     const size_t in = 2 * 4 + k * 4 + k * (4 + 16 + 32 + 4) + 48 + 288 + 96 + 8 + 4;
     size_t out = 7 * 8 + (size_t)maxStates * 24;
-    if (spec.sm) out += (size_t)maxStates * 42 * 8;
-    if (spec.fi) out += (size_t)maxStates * 42 * 8;
-    if (spec.pr) out += (size_t)maxStates * 42 * 8;
+    const size_t pc = spec.packed ? 27 : 42;
+    if (spec.sm) out += (size_t)maxStates * pc * 8;
+    if (spec.fi) out += (size_t)maxStates * pc * 8;
+    if (spec.pr) out += (size_t)maxStates * pc * 8;
     if (spec.jac) out += (size_t)maxStates * 36 * 8;
     if (opt.reference_surface >= 0) out += 42 * 8;
     if (needsExtStart(opt)) out += 2 * sizeof(ExtStart);
     return in + out + recordBytesPerTrack(maxStates, opt.precision);
+  }
+  // components of output array `field` (the covariance arrays may be packed)
+  int comp(int field) const {
+    if (spec.packed && (field == 12 || field == 14 || field == 16)) return 21;
+    return kOutComp[field];
   }
   bool computes(int field) const {
     switch (field) {
@@ -196,7 +203,7 @@ ck_status slotAlloc(ck_server* s, Slot& sl) {
   size_t pout = 0;
   for (int i = 0; i < kOutArrays; ++i) {
     if (!s->computes(i)) continue;
-    const size_t bytes = kOutElem[i] * kOutComp[i] * (kPerState[i] ? S : cap);
+    const size_t bytes = kOutElem[i] * s->comp(i) * (kPerState[i] ? S : cap);
     if ((e = sl.dout[i].ensure(bytes)) != cudaSuccess) return cudaFail(e, "server output");
     pout += (bytes + 255) & ~(size_t)255;
   }
@@ -218,7 +225,7 @@ void stagedBases(ck_server* s, Slot& sl, size_t base[kOutArrays]) {
   for (int i = 0; i < kOutArrays; ++i) {
     base[i] = off;
     if (!s->computes(i)) continue;
-    off += (kOutElem[i] * kOutComp[i] * (kPerState[i] ? S : n) + 255) & ~(size_t)255;
+    off += (kOutElem[i] * s->comp(i) * (kPerState[i] ? S : n) + 255) & ~(size_t)255;
   }
 }
 
@@ -306,6 +313,7 @@ ck_status launchSlot(ck_server* s, Slot& sl) {
   din.meas_subspace = (const int32_t*)sl.din[11].p;
   ck_batch_out dout{};
   dout.max_states = s->cfg.max_states;
+  dout.components = s->cfg.components;
   dout.memory = CK_MEM_DEVICE;
   void** f[kOutArrays];
   outFields(dout, f);
@@ -336,7 +344,7 @@ ck_status launchSlot(ck_server* s, Slot& sl) {
         const size_t el = kOutElem[i];
         const char* src = (const char*)sl.dout[i].p + el * t0;
         // rows of the SoA array: components (x states)
-        const size_t rows = (kPerState[i] ? (size_t)ms : 1) * (size_t)kOutComp[i];
+        const size_t rows = (kPerState[i] ? (size_t)ms : 1) * (size_t)s->comp(i);
         if (rows == 1)
           e = cudaMemcpyAsync(*g[i], src, el * m, cudaMemcpyDefault, sl.stream);
         else
@@ -353,7 +361,7 @@ ck_status launchSlot(ck_server* s, Slot& sl) {
     const size_t S = (size_t)n * ms;
     for (int i = 0; i < kOutArrays; ++i) {
       if (!sl.dout[i].cap) continue;
-      const size_t bytes = kOutElem[i] * kOutComp[i] * (kPerState[i] ? S : (size_t)n);
+      const size_t bytes = kOutElem[i] * s->comp(i) * (kPerState[i] ? S : (size_t)n);
       if ((e = cudaMemcpyAsync((char*)sl.pinOut + base[i], sl.dout[i].p, bytes,
                                cudaMemcpyDeviceToHost, sl.stream)) != cudaSuccess)
         return cudaFail(e, "server staged copy");
@@ -381,7 +389,7 @@ void harvestSlot(ck_server* s, Slot& sl) {
         const size_t el = kOutElem[i];
         const char* src = (const char*)sl.pinOut + base[i] + el * t0;
         char* dst = (char*)*g[i];
-        const int rows = (kPerState[i] ? ms : 1) * kOutComp[i];
+        const int rows = (kPerState[i] ? ms : 1) * s->comp(i);
         for (int r = 0; r < rows; ++r)
           std::memcpy(dst + el * m * (size_t)r, src + el * n * (size_t)r, el * m);
       }
@@ -505,7 +513,8 @@ ck_status ck_server_create(ck_handle* h, const ck_options* opt, const ck_server_
   s->opt = *opt;
   s->cfg = *cfg;
   s->spec = {(cfg->components & CK_OUT_SMOOTHED) != 0, (cfg->components & CK_OUT_FILTERED) != 0,
-             (cfg->components & CK_OUT_PREDICTED) != 0, (cfg->components & CK_OUT_JACOBIAN) != 0};
+             (cfg->components & CK_OUT_PREDICTED) != 0, (cfg->components & CK_OUT_JACOBIAN) != 0,
+             (cfg->components & CK_OUT_PACKED_COV) != 0};
   s->tune = h->tune[opt->precision];
   s->tune.spr = cfg->steps_per_round > 0 ? cfg->steps_per_round : kServerStepsPerRound;
   s->tune.grid = 0;

@@ -264,13 +264,15 @@ class CudaKalman {
     const size_t S = static_cast<size_t>(ms) * n;
     std::vector<int32_t> status(n), nStates(n), nMeas(n), nHoles(n), nOut(n), ndf(n), surf(S);
     std::vector<uint32_t> flags(S);
-    std::vector<double> chi2(n), path(S), schi2(S), pr(6 * S), prc(36 * S), fi(6 * S), fic(36 * S),
-        sm(6 * S), smc(36 * S), jac(36 * S), tp(6 * n), tc(36 * n);
+    // covariances cross the boundary packed (upper triangles, 21 values) and
+    // are unfolded into the container's full matrices below
+    std::vector<double> chi2(n), path(S), schi2(S), pr(6 * S), prc(21 * S), fi(6 * S), fic(21 * S),
+        sm(6 * S), smc(21 * S), jac(36 * S), tp(6 * n), tc(36 * n);
     const bool ref = options.options.reference_surface >= 0;
     ck_batch_out out{};
     out.max_states = ms;
     out.components = CK_OUT_PREDICTED | CK_OUT_FILTERED | CK_OUT_SMOOTHED | CK_OUT_JACOBIAN |
-                     (ref ? CK_OUT_REFERENCE : 0u);
+                     CK_OUT_PACKED_COV | (ref ? CK_OUT_REFERENCE : 0u);
     if (ref) {
       out.track_params = tp.data();
       out.track_cov = tc.data();
@@ -330,12 +332,14 @@ class CudaKalman {
           st.filtered[c] = fi[at(k, 6, c, t)];
           st.smoothed[c] = sm[at(k, 6, c, t)];
         }
-        for (size_t c = 0; c < 36; ++c) {
-          st.predictedCovariance[c] = prc[at(k, 36, c, t)];
-          st.filteredCovariance[c] = fic[at(k, 36, c, t)];
-          st.smoothedCovariance[c] = smc[at(k, 36, c, t)];
-          st.jacobian[c] = jac[at(k, 36, c, t)];
-        }
+        for (size_t i = 0, c = 0; i < 6; ++i)
+          for (size_t j = i; j < 6; ++j, ++c) {
+            const size_t u = i * 6 + j, l = j * 6 + i;
+            st.predictedCovariance[u] = st.predictedCovariance[l] = prc[at(k, 21, c, t)];
+            st.filteredCovariance[u] = st.filteredCovariance[l] = fic[at(k, 21, c, t)];
+            st.smoothedCovariance[u] = st.smoothedCovariance[l] = smc[at(k, 21, c, t)];
+          }
+        for (size_t c = 0; c < 36; ++c) st.jacobian[c] = jac[at(k, 36, c, t)];
         container.states.push_back(st);
       }
       container.tracks.push_back(tr);

@@ -11,6 +11,11 @@ import numpy as np
 from . import abi
 
 
+# index of full-matrix entry (i, j) in the packed upper triangle (row by row)
+UNPACK = np.array([[(min(i, j) * (11 - min(i, j))) // 2 + max(i, j) for j in range(6)]
+                   for i in range(6)]).reshape(36)
+
+
 class Results:
     def __init__(self, n, max_states=24, components=abi.OUT_ALL):
         self.n = n
@@ -28,12 +33,13 @@ class Results:
         self.state_flags = z(1, np.uint32)
         self.state_path_length = z(1, np.float64)
         self.state_chi2 = z(1, np.float64)
+        cc = 21 if components & abi.OUT_PACKED_COV else 36
         self.predicted = z(6, np.float64) if components & abi.OUT_PREDICTED else None
-        self.predicted_cov = z(36, np.float64) if components & abi.OUT_PREDICTED else None
+        self.predicted_cov = z(cc, np.float64) if components & abi.OUT_PREDICTED else None
         self.filtered = z(6, np.float64) if components & abi.OUT_FILTERED else None
-        self.filtered_cov = z(36, np.float64) if components & abi.OUT_FILTERED else None
+        self.filtered_cov = z(cc, np.float64) if components & abi.OUT_FILTERED else None
         self.smoothed = z(6, np.float64) if components & abi.OUT_SMOOTHED else None
-        self.smoothed_cov = z(36, np.float64) if components & abi.OUT_SMOOTHED else None
+        self.smoothed_cov = z(cc, np.float64) if components & abi.OUT_SMOOTHED else None
         self.jacobian = z(36, np.float64) if components & abi.OUT_JACOBIAN else None
         ref = components & abi.OUT_REFERENCE
         self.track_params = np.zeros(6 * n, np.float64) if ref else None
@@ -60,12 +66,15 @@ class Results:
         return None if a is None else a.reshape(-1, self.n).T
 
     def view(self, name, k=None):
-        """Array `name` as [n, max_states, C] (or [n, max_states] for scalars)."""
+        """Array `name` as [n, max_states, C] (or [n, max_states] for scalars);
+        packed covariances (CK_OUT_PACKED_COV) are unfolded to C = 36."""
         a = getattr(self, name)
         if a is None:
             return None
         c = a.size // (self.max_states * self.n)
         v = a.reshape(self.max_states, c, self.n).transpose(2, 0, 1)
+        if c == 21:
+            return v[..., UNPACK]
         return v[..., 0] if c == 1 else v
 
     def track_states(self, t, name):
@@ -103,6 +112,8 @@ class TorchResults:
         for name, per, dt in self._SPEC:
             if name in self._COMP and not components & self._COMP[name]:
                 continue
+            if per == -36 and name != "jacobian" and components & abi.OUT_PACKED_COV:
+                per = -21
             size = n * (per if per > 0 else -per * max_states)
             dtype = getattr(torch, dt)
             if self.pinned:

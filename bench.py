@@ -18,6 +18,9 @@ Reported (one JSON line, rank 0):
   e2e       the mixed form through the C ABI with pinned host buffers:
             host->device copy of the inputs, the fit, device->host copy of
             the smoothed parameters and covariances inside the timed region.
+  Outputs of both: per state the surface, flags, path length, chi2, the
+  smoothed parameters and the smoothed covariance as its upper triangle
+  (CK_OUT_PACKED_COV: the 21 distinct entries of the symmetric matrix).
   roofline  fit kernel: algorithmic FP64 flops (reference formulation,
             counted by the oracle's counting scalar on a sample) per launch /
             kernel time, against the FP64 FMA peak measured live.
@@ -146,7 +149,7 @@ def device_outputs(n, max_states, torch, dev):
     keep = {}
     bo = abi.ck_batch_out()
     bo.max_states = max_states
-    bo.components = abi.OUT_SMOOTHED
+    bo.components = abi.OUT_SMOOTHED | abi.OUT_PACKED_COV
     bo.memory = abi.MEM_DEVICE
     spec = {"status": (n, torch.int32, C.c_int32), "n_states": (n, torch.int32, C.c_int32),
             "n_measurements": (n, torch.int32, C.c_int32), "n_holes": (n, torch.int32, C.c_int32),
@@ -157,7 +160,7 @@ def device_outputs(n, max_states, torch, dev):
             "state_path_length": (n * max_states, torch.float64, C.c_double),
             "state_chi2": (n * max_states, torch.float64, C.c_double),
             "smoothed": (n * max_states * 6, torch.float64, C.c_double),
-            "smoothed_cov": (n * max_states * 36, torch.float64, C.c_double)}
+            "smoothed_cov": (n * max_states * 21, torch.float64, C.c_double)}
     for name, (size, dt, ct) in spec.items():
         t = torch.zeros(size, dtype=dt, device=dev)
         keep[name] = t
@@ -191,7 +194,7 @@ def host_pinned_outputs(n, max_states, torch):
     keep = {}
     bo = abi.ck_batch_out()
     bo.max_states = max_states
-    bo.components = abi.OUT_SMOOTHED
+    bo.components = abi.OUT_SMOOTHED | abi.OUT_PACKED_COV
     bo.memory = abi.MEM_HOST
     spec = {"status": (n, torch.int32, C.c_int32), "n_states": (n, torch.int32, C.c_int32),
             "n_measurements": (n, torch.int32, C.c_int32), "n_holes": (n, torch.int32, C.c_int32),
@@ -202,7 +205,7 @@ def host_pinned_outputs(n, max_states, torch):
             "state_path_length": (n * max_states, torch.float64, C.c_double),
             "state_chi2": (n * max_states, torch.float64, C.c_double),
             "smoothed": (n * max_states * 6, torch.float64, C.c_double),
-            "smoothed_cov": (n * max_states * 36, torch.float64, C.c_double)}
+            "smoothed_cov": (n * max_states * 21, torch.float64, C.c_double)}
     for name, (size, dt, ct) in spec.items():
         t = torch.zeros(size, dtype=dt).pin_memory()
         keep[name] = t
@@ -227,9 +230,10 @@ def accuracy_report(b, r64, rmx, n):
     fl = r64["state_flags"].reshape(ms, r64["N"])[:, :n].T
     sm64 = r64["smoothed"].reshape(ms, 6, r64["N"])[:, :, :n].transpose(2, 0, 1)
     smmx = rmx["smoothed"].reshape(ms, 6, rmx["N"])[:, :, :n].transpose(2, 0, 1)
-    cv64 = r64["smoothed_cov"].reshape(ms, 36, r64["N"])[:, :, :n].transpose(2, 0, 1)
-    cvmx = rmx["smoothed_cov"].reshape(ms, 36, rmx["N"])[:, :, :n].transpose(2, 0, 1)
-    diag = [0, 7, 14, 21, 28, 35]
+    # (packed upper triangles: the diagonal entries at 0, 6, 11, 15, 18, 20)
+    cv64 = r64["smoothed_cov"].reshape(ms, 21, r64["N"])[:, :, :n].transpose(2, 0, 1)
+    cvmx = rmx["smoothed_cov"].reshape(ms, 21, rmx["N"])[:, :, :n].transpose(2, 0, 1)
+    diag = [0, 6, 11, 15, 18, 20]
     sig64 = np.sqrt(np.abs(cv64[..., diag]))
     meas = ((fl & abi.FLAG_HAS_MEASUREMENT) != 0) & ((fl & abi.FLAG_IS_OUTLIER) == 0)
     meas &= ok[:, None]
@@ -527,7 +531,7 @@ def native_arm(args):
                        "precision": "mixed (stepper, transport, field in FP32; update, "
                                     "inverses, chi2 in FP64)",
                        "l2": "inputs ~1 GB per step > 129 MB L2 (no flush needed)",
-                       "max_states": ms, "outputs": "smoothed parameters + covariances"},
+                       "max_states": ms, "outputs": "smoothed parameters + covariances (packed upper triangles)"},
             "fp64": {"value": round(results["fp64"]["tracks_per_s"], 1), "unit": "tracks/s",
                      "ms_per_step": round(results["fp64"]["ms_per_step"], 3),
                      "mixed_over_fp64": round(mixed["tracks_per_s"] /

@@ -318,7 +318,13 @@ enum {
   CK_OUT_FILTERED = 1u << 1,
   CK_OUT_SMOOTHED = 1u << 2,
   CK_OUT_JACOBIAN = 1u << 3,
-  CK_OUT_REFERENCE = 1u << 4   /* track parameters at the reference surface */
+  CK_OUT_REFERENCE = 1u << 4,  /* track parameters at the reference surface */
+  /* The per-state covariance arrays (predicted_cov, filtered_cov,
+   * smoothed_cov) hold each symmetric matrix once, as its upper triangle
+   * row by row ((0,0), (0,1), ..., (0,5), (1,1), ..., (5,5)): C = 21 instead
+   * of 36, the same values, 42 % fewer bytes to move. The Jacobian and
+   * track_cov keep C = 36. */
+  CK_OUT_PACKED_COV = 1u << 5
 };
 
 /* Results of a batch. Arrays the component mask does not select may be NULL.
@@ -342,11 +348,11 @@ typedef struct ck_batch_out {
   double* state_path_length; /* accumulated path at the state (C = 1)        */
   double* state_chi2;        /* filtered chi2 of measurement states (C = 1)  */
   double* predicted;         /* C = 6  */
-  double* predicted_cov;     /* C = 36 */
+  double* predicted_cov;     /* C = 36 (21 with CK_OUT_PACKED_COV) */
   double* filtered;          /* C = 6  */
-  double* filtered_cov;      /* C = 36 */
+  double* filtered_cov;      /* C = 36 (21 with CK_OUT_PACKED_COV) */
   double* smoothed;          /* C = 6  */
-  double* smoothed_cov;      /* C = 36 */
+  double* smoothed_cov;      /* C = 36 (21 with CK_OUT_PACKED_COV) */
   double* jacobian;          /* C = 36, transport from the previous state   */
   /* per track [C * n_tracks], element c of track t at [c * n_tracks + t]:
    * the track's parameters and covariance at the reference surface
