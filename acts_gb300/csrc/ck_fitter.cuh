@@ -861,7 +861,7 @@ struct Lane {
         if (targetReached) {
           // the fitted parameters: the bound state on the target
           // (KalmanFitter.hpp:398-412)
-          if (!writeReferenceState(fp)) return CK_TRACK_NOT_ON_SURFACE;
+          if (!writeReferenceState(fp, fp.ref_surface)) return CK_TRACK_NOT_ON_SURFACE;
           fp.ext[2 * (size_t)slot].fitted = 1;
         }
       }
@@ -1400,7 +1400,7 @@ struct Lane {
   }
 
   CK_D void finishExtrapolation(const FitParams& fp) {
-    if (!writeReferenceState(fp)) {
+    if (!writeReferenceState(fp, fp.ref_surface)) {
       fail(fp, CK_TRACK_NOT_ON_SURFACE);
       return;
     }
@@ -1413,9 +1413,10 @@ struct Lane {
   // path derivative (LineSurface.cpp:102-115,224-251), C <- J C J^T, and the
   // bound parameters (LineSurface::globalToLocal, LineSurface.cpp:70-96);
   // false when the position is not on the line
-  CK_D bool writeReferenceState(const FitParams& fp) {
+  // (sid: the line surface's table index)
+  CK_D bool writeReferenceState(const FitParams& fp, int sid) {
     Surf<double> ts;
-    ts.load(fp.surfaces + fp.ref_surface);
+    ts.load(fp.surfaces + sid);
     const double z0[3] = {ts.R[2], ts.R[5], ts.R[8]};
     double d0[3] = {z0[1] * dir[2] - z0[2] * dir[1], z0[2] * dir[0] - z0[0] * dir[2],
                     z0[0] * dir[1] - z0[1] * dir[0]};
@@ -1616,7 +1617,7 @@ struct Lane {
     if (targetSurf >= 0) {
       sf.load(fp.surfaces + targetSurf);
       if (sf.type == CK_SURFACE_LINE) {
-        if (!writeReferenceState(fp)) {
+        if (!writeReferenceState(fp, targetSurf)) {
           fail(fp, CK_TRACK_NOT_ON_SURFACE);
           return;
         }
@@ -2195,6 +2196,127 @@ __global__ void __launch_bounds__(S, 1) fitKernelCompact(FitParams fp) {
 template <typename P, typename CV, int S>
 constexpr size_t compactSmemBytes() {
   return sizeof(Lane<P, CV>) * S + sizeof(int) * S;
+}
+
+// Persistent forward-filter kernel with warp-autonomous phase pools. The
+// state of every track in flight lives in shared memory (one Lane per slot,
+// S slots, more slots than the T threads of the block). A slot waiting for
+// a phase step sits in that phase's pool, a bit mask in shared memory. Each
+// warp on its own, without block barriers: counts the pools, claims up to 32
+// slots of the fullest one (atomicAnd on the mask words), advances them by
+// one phase step on its lanes, and returns each slot to the pool of its new
+// phase (atomicOr), or retires it when the work queue is empty. With S > T
+// the pools hold S - T slots or more while every warp is busy, so a warp
+// finds full sets of one phase; no warp waits for the slowest item of a
+// block-wide round. A warp leaves when all pools are empty: slots still in
+// flight belong to warps that are running and that claim them again after
+// returning them, so every slot is finished, and nothing spins.
+template <typename P, typename CV, int S, int T>
+__global__ void __launch_bounds__(T, 1) fitKernelPool(FitParams fp) {
+  static_assert(S % 32 == 0 && S / 32 <= 32 && T % 32 == 0, "pool shape");
+  constexpr int W = S / 32;  // mask words per phase
+  extern __shared__ __align__(16) unsigned char smem[];
+  using LaneT = Lane<P, CV>;
+  LaneT* st = reinterpret_cast<LaneT*>(smem);
+  __shared__ unsigned pool[3][W];
+  __shared__ int items[T / 32][32];
+  const unsigned FULL = 0xffffffffu;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // slots that take tracks: all of them for large batches; a small batch
+  // spreads over all blocks
+  const int perBlock = (fp.n_queue + (int)gridDim.x - 1) / (int)gridDim.x;
+  const int active = min(S, max(1, perBlock));
+  for (int sl = tid; sl < S; sl += T) {
+    st[sl].phase = sl < active ? PH_FETCH : PH_DONE;
+    st[sl].t = -1;
+    st[sl].q = -1;
+  }
+  if (tid < W) {
+    const int lo = tid * 32;
+    const int k = min(32, max(0, active - lo));
+    pool[PH_FETCH][tid] = k == 32 ? FULL : ((1u << k) - 1u);
+    pool[PH_STEP][tid] = 0u;
+    pool[PH_SURFACE][tid] = 0u;
+  }
+  __syncthreads();
+  volatile unsigned* vpool = &pool[0][0];
+  while (true) {
+    // pool sizes (lane w < W reads word w of every pool)
+    unsigned w0 = 0u, w1 = 0u, w2 = 0u;
+    if (lane < W) {
+      w0 = vpool[PH_FETCH * W + lane];
+      w1 = vpool[PH_STEP * W + lane];
+      w2 = vpool[PH_SURFACE * W + lane];
+    }
+    const int n0 = __reduce_add_sync(FULL, __popc(w0));
+    const int n1 = __reduce_add_sync(FULL, __popc(w1));
+    const int n2 = __reduce_add_sync(FULL, __popc(w2));
+    int c = -1, best = 0;
+    if (n1 > best) {
+      c = PH_STEP;
+      best = n1;
+    }
+    if (n2 > best) {
+      c = PH_SURFACE;
+      best = n2;
+    }
+    if (n0 > best) {
+      c = PH_FETCH;
+      best = n0;
+    }
+    if (c < 0) break;  // every pool empty
+    // claim up to 32 slots of pool c: word w gives at most what the words
+    // before it left of 32
+    const unsigned word = c == PH_FETCH ? w0 : (c == PH_STEP ? w1 : w2);
+    const int cnt = __popc(word);
+    int before = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int v = __shfl_up_sync(FULL, before, d);
+      if (lane >= d) before += v;
+    }
+    before -= cnt;  // exclusive prefix
+    const int want = max(0, min(cnt, 32 - before));
+    unsigned take = 0u, rest = word;
+    for (int i = 0; i < want; ++i) {
+      const unsigned b = rest & (0u - rest);
+      take |= b;
+      rest ^= b;
+    }
+    unsigned got = 0u;
+    if (take) got = atomicAnd(&pool[c][lane], ~take) & take;
+    const int gc = __popc(got);
+    int base = gc;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int v = __shfl_up_sync(FULL, base, d);
+      if (lane >= d) base += v;
+    }
+    const int total = __shfl_sync(FULL, base, 31);
+    base -= gc;
+    for (unsigned g = got; g; g &= g - 1u) items[warp][base++] = lane * 32 + (__ffs(g) - 1);
+    __syncwarp();
+    if (total == 0) continue;  // another warp took them first
+    __threadfence_block();     // (acquire: the claimed slots' states)
+    if (lane < total) {
+      const int slot = items[warp][lane];
+      // few items: many Runge-Kutta trials per claim (the end of the queue,
+      // small batches); results do not depend on the trials per claim
+      const int spr = total <= 16 ? max(fp.steps_per_round, kTailStepsPerRound)
+                                  : fp.steps_per_round;
+      LaneT L = st[slot];
+      advanceSlot(fp, L, c, lane, spr);
+      st[slot] = L;
+      __threadfence_block();  // (release: the state before the slot is published)
+      if (L.phase != PH_DONE) atomicOr(&pool[L.phase][slot >> 5], 1u << (slot & 31));
+    }
+    __syncwarp();
+  }
+}
+
+template <typename P, typename CV, int S>
+constexpr size_t poolSmemBytes() {
+  return sizeof(Lane<P, CV>) * S;
 }
 
 // Smoother kernel: one lane per queue position; lanes of a warp hold tracks

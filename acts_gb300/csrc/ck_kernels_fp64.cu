@@ -28,6 +28,12 @@ cudaError_t launchFitFP64(const FitParams& fp, int variant, int grid, int block,
     case 3:
       fitKernelCompact<double, double, 256><<<grid, 256, compactSmemBytes<double, double, 256>(), st>>>(fp);
       break;
+    case 5:
+      fitKernelPool<double, double, 320, 256><<<grid, 256, poolSmemBytes<double, double, 320>(), st>>>(fp);
+      break;
+    case 6:
+      fitKernelPool<double, double, 256, 256><<<grid, 256, poolSmemBytes<double, double, 256>(), st>>>(fp);
+      break;
     default:
       fitKernelCompact<double, double, 128><<<grid, 128, compactSmemBytes<double, double, 128>(), st>>>(fp);
       break;
@@ -51,6 +57,14 @@ int occupancyFP64(int variant, int tpb) {
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelCompact<double, double, 256>, 256,
                                                     compactSmemBytes<double, double, 256>());
       break;
+    case 5:
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelPool<double, double, 320, 256>, 256,
+                                                    poolSmemBytes<double, double, 320>());
+      break;
+    case 6:
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelPool<double, double, 256, 256>, 256,
+                                                    poolSmemBytes<double, double, 256>());
+      break;
     default:
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelCompact<double, double, 128>, 128,
                                                     compactSmemBytes<double, double, 128>());
@@ -60,7 +74,15 @@ int occupancyFP64(int variant, int tpb) {
 }
 
 cudaError_t configureFP64() {
-  cudaError_t e = cudaFuncSetAttribute(fitKernelCompact<double, double, 256, true>,
+  cudaError_t e = cudaFuncSetAttribute(fitKernelPool<double, double, 320, 256>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)poolSmemBytes<double, double, 320>());
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(fitKernelPool<double, double, 256, 256>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)poolSmemBytes<double, double, 256>());
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(fitKernelCompact<double, double, 256, true>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)compactSmemBytes<double, double, 256>());
   if (e != cudaSuccess) return e;

@@ -30,6 +30,12 @@ cudaError_t launchFitMixed(const FitParams& fp, int variant, int grid, int block
     case 3:
       fitKernelCompact<float, float, 256><<<grid, 256, compactSmemBytes<float, float, 256>(), st>>>(fp);
       break;
+    case 5:
+      fitKernelPool<float, float, 384, 256><<<grid, 256, poolSmemBytes<float, float, 384>(), st>>>(fp);
+      break;
+    case 6:
+      fitKernelPool<float, float, 448, 256><<<grid, 256, poolSmemBytes<float, float, 448>(), st>>>(fp);
+      break;
     default:
       fitKernelCompact<float, float, 128><<<grid, 128, compactSmemBytes<float, float, 128>(), st>>>(fp);
       break;
@@ -38,7 +44,15 @@ cudaError_t launchFitMixed(const FitParams& fp, int variant, int grid, int block
 }
 
 cudaError_t configureMixed() {
-  cudaError_t e = cudaFuncSetAttribute(fitKernelCompact<float, float, 256, true>,
+  cudaError_t e = cudaFuncSetAttribute(fitKernelPool<float, float, 384, 256>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)poolSmemBytes<float, float, 384>());
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(fitKernelPool<float, float, 448, 256>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)poolSmemBytes<float, float, 448>());
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(fitKernelCompact<float, float, 256, true>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)compactSmemBytes<float, float, 256>());
   if (e != cudaSuccess) return e;
@@ -72,6 +86,14 @@ int occupancyMixed(int variant, int tpb) {
     case 3:
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelCompact<float, float, 256>, 256,
                                                     compactSmemBytes<float, float, 256>());
+      break;
+    case 5:
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelPool<float, float, 384, 256>, 256,
+                                                    poolSmemBytes<float, float, 384>());
+      break;
+    case 6:
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelPool<float, float, 448, 256>, 256,
+                                                    poolSmemBytes<float, float, 448>());
       break;
     default:
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelCompact<float, float, 128>, 128,

@@ -9,15 +9,19 @@ namespace ck {
 
 // Forward-filter kernel variants: 0-2 per-warp phase scheduling with
 // register caps of 255 / 168 / 128 (1 / 3 / 4 resident 128-thread blocks);
-// 3-4 block-level phase compaction with 256 / 128 slots per block.
-constexpr int kNumFitVariants = 5;
+// 3-4 block-level phase compaction with 256 / 128 slots per block; 5-6
+// warp-autonomous phase pools, 256 threads with more slots (5: 384 mixed /
+// 320 FP64; 6: 448 mixed / 256 FP64).
+constexpr int kNumFitVariants = 7;
 constexpr int kFitMaxBlock = 128;
 constexpr int kDefaultVariant = 3;
 // Runge-Kutta trials per round of the compaction kernels by precision
 // (FP64, mixed): measured best on the barrel and uneven workloads
 constexpr int kDefaultStepsPerRound[2] = {2, 3};
 // block size a variant requires (0: any multiple of 32 up to kFitMaxBlock)
-inline int variantBlock(int variant) { return variant == 3 ? 256 : (variant == 4 ? 128 : 0); }
+inline int variantBlock(int variant) {
+  return (variant == 3 || variant >= 5) ? 256 : (variant == 4 ? 128 : 0);
+}
 inline bool validLaunch(int variant, int tpb) {
   if (variant < 0 || variant >= kNumFitVariants) return false;
   const int vb = variantBlock(variant);

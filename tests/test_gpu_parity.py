@@ -149,8 +149,10 @@ def test_fp64_parity_reference_surface(name, preset, n, kw):
 
 
 # every forward-filter kernel variant: per-warp phase scheduling with the
-# three register caps, block-level phase compaction with 256 and 128 slots
-VARIANTS = [(0, 128, 2), (1, 128, 3), (2, 128, 4), (3, 256, 1), (4, 128, 2)]
+# three register caps, block-level phase compaction with 256 and 128 slots,
+# warp-autonomous phase pools with two slot counts
+VARIANTS = [(0, 128, 2), (1, 128, 3), (2, 128, 4), (3, 256, 1), (4, 128, 2), (5, 256, 1),
+            (6, 256, 1)]
 
 
 @pytest.mark.gpu
@@ -174,3 +176,32 @@ def test_fp64_parity_every_kernel_variant(variant, tpb, bps):
     rep = compare(gpu, ora, RTOL)
     assert rep["n_ok"] >= 0.5 * n
     assert_parity(rep, RTOL)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [300, 5000])
+def test_mixed_results_independent_of_kernel_variant(n):
+    """The forward-filter variants only schedule: a track's arithmetic does
+    not depend on which slot, warp or round advances it, so every variant of
+    the mixed form gives bit-identical results (small and large batches)."""
+    from acts_gb300.fitter import CudaKalman
+
+    preset = abi.CKG_UNEVEN
+    det = detector(preset)
+    b = batch(preset, n, seed=23)
+    opt = abi.default_options(precision=abi.PRECISION_MIXED, outlier_chi2_cut=15.0)
+    fit = CudaKalman.for_detector(det)
+    outs = []
+    try:
+        for variant, tpb, bps in VARIANTS:
+            fit.set_launch_config(abi.PRECISION_MIXED, variant, tpb, bps)
+            outs.append(fit.fit_batch(b, opt, max_states=24, components=abi.OUT_ALL))
+    finally:
+        fit.close()
+    ref = outs[0]
+    valid = np.arange(24)[None, :] < ref.n_states[:, None]
+    for (variant, _, _), r in zip(VARIANTS[1:], outs[1:]):
+        np.testing.assert_array_equal(r.status, ref.status, err_msg="v%d" % variant)
+        for name in ("state_flags", "smoothed", "smoothed_cov", "filtered", "jacobian"):
+            np.testing.assert_array_equal(r.view(name)[valid], ref.view(name)[valid],
+                                          err_msg="v%d %s" % (variant, name))

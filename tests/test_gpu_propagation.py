@@ -52,7 +52,7 @@ def test_jacobian_engine_identities(precision):
     table, prop = jacobian_engine_case()
     pc.CudaBackend(precision).propagate(pc.constant_field(2.0), table, prop,
                                         abi.default_options())
-    check_jacobian_engine(prop)
+    check_jacobian_engine(prop, 1e-12 if precision == abi.PRECISION_FP64 else 1e-6)
 
 
 def _rel(a, b, floor):

@@ -173,7 +173,7 @@ def test_static_scratch_allocates_nothing():
     det = generate.Detector(abi.CKG_BARREL, perigee=True)
     dev = torch.device("cuda", 0)
     small, large = 200, 2 * N_TRACKS
-    opt = abi.default_options(precision=abi.PRECISION_FP64, reference_surface=det.perigee)
+    opt = abi.default_options(precision=abi.PRECISION_MIXED, reference_surface=det.perigee)
     fit = CudaKalman.for_detector(det)
     try:
         assert fit.static_scratch_bytes_for(opt, large, MAX_STATES) <= fit.static_scratch_capacity()
