@@ -12,7 +12,7 @@ The tolerance is the parity definition of the plain form (tests/parity.py):
 statuses, state counts, surfaces and flags bit-exact; parameters within 1e-9
 of max(|x|, sigma_x); covariance entries within 1e-9 of
 max(|C_ij|, sqrt(C_ii C_jj)); Jacobian entries within 1e-9 of
-max(|J_ij|, 1e-6 max_k |J_ik|); path lengths and chi2 within 1e-9 of
+max(|J_ij|, 1e-4 max_k |J_ik|); path lengths and chi2 within 1e-9 of
 max(|x|, 1). Broken fits — chi2/ndf above 1000, the barrel tracks whose
 prediction and measurement straddle a cylinder's phi = +-pi seam and get a
 residual of 2 pi R (2e-4 of the tracks) — are fitted identically up to the

@@ -4,12 +4,13 @@ datasets and tolerances; tests/propagation_cases.py) in both precision
 forms, the JacobianEngine identities, and FP64 parity with the oracle's
 propagation restatement: statuses and step counts equal, end parameters,
 covariances, Jacobians and path lengths within 1e-9 (floors as in the fit
-parity: sigma, sqrt(C_ii C_jj), 1e-6 of the Jacobian row, 1 mm)."""
+parity: sigma, sqrt(C_ii C_jj), 1e-4 of the Jacobian row, 1 mm)."""
 import numpy as np
 import pytest
 
 import propagation_cases as pc
 from acts_gb300 import abi
+from parity import JAC_ROW_FLOOR
 from test_oracle_propagation import check_jacobian_engine, jacobian_engine_case
 
 FORMS = [abi.PRECISION_FP64, abi.PRECISION_MIXED]
@@ -75,7 +76,7 @@ def test_fp64_parity_with_oracle(tesla, kind):
     rp = dp.T / np.maximum(np.maximum(np.abs(g.end_params.T), np.abs(o.end_params.T)), sig)
     rc = _rel(g.end_cov.T, o.end_cov.T, (sig[:, :, None] * sig[:, None, :]).reshape(-1, 36))
     jo = o.jacobian.T.reshape(-1, 6, 6)
-    rowmax = np.abs(jo).max(axis=2, keepdims=True) * 1e-6
+    rowmax = np.abs(jo).max(axis=2, keepdims=True) * JAC_ROW_FLOOR
     rj = _rel(g.jacobian.T, o.jacobian.T, np.broadcast_to(rowmax, jo.shape).reshape(-1, 36))
     rl = _rel(g.path_length, o.path_length, 1.0)
     rep = {"params": rp.max(), "cov": rc.max(), "jac": rj.max(), "path": rl.max()}
