@@ -85,6 +85,7 @@ struct Slot {
   std::vector<std::unique_ptr<Event>> events;
   int nTracks = 0, nSeq = 0, nMeas = 0;
   bool busy = false;
+  bool harvesting = false;  // done on the GPU; the delivery thread copies its results
 };
 
 // element size and components per ck_batch_out array, in the order of
@@ -144,6 +145,12 @@ struct ck_server {
   std::deque<std::unique_ptr<Event>> pending;
   std::deque<std::unique_ptr<Event>> finished;
   std::thread worker;
+  // delivery of pageable host results: the slots whose staged results the
+  // delivery thread de-strides (with helper threads), off the request loop
+  std::thread delivery;
+  std::deque<Slot*> toHarvest;
+  std::condition_variable cvHarvest;
+  int copyThreads = 1;
   bool stop = false;
   ck_status error = CK_OK;
   std::string errorMsg;
@@ -371,11 +378,21 @@ ck_status launchSlot(ck_server* s, Slot& sl) {
   return CK_OK;
 }
 
-// Completes a finished slot: host copies of the staged events' results.
+// Completes a finished slot: host copies of the staged events' results
+// (the rows of every staged array, split over the server's copy threads:
+// de-striding into pageable memory is bound by page faults and memory
+// bandwidth, which several cores share out).
 void harvestSlot(ck_server* s, Slot& sl) {
   const int n = sl.nTracks, ms = s->cfg.max_states;
   size_t base[kOutArrays];
   stagedBases(s, sl, base);
+  struct Row {
+    char* dst;
+    const char* src;
+    size_t bytes;
+  };
+  std::vector<Row> rows;
+  size_t total = 0;
   int t0 = 0;
   for (auto& evp : sl.events) {
     Event& ev = *evp;
@@ -389,14 +406,26 @@ void harvestSlot(ck_server* s, Slot& sl) {
         const size_t el = kOutElem[i];
         const char* src = (const char*)sl.pinOut + base[i] + el * t0;
         char* dst = (char*)*g[i];
-        const int rows = (kPerState[i] ? ms : 1) * s->comp(i);
-        for (int r = 0; r < rows; ++r)
-          std::memcpy(dst + el * m * (size_t)r, src + el * n * (size_t)r, el * m);
+        const int nr = (kPerState[i] ? ms : 1) * s->comp(i);
+        for (int r = 0; r < nr; ++r)
+          rows.push_back({dst + el * m * (size_t)r, src + el * n * (size_t)r, el * m});
+        total += el * m * (size_t)nr;
       }
     }
-    ev.latencyMs = std::chrono::duration<double, std::milli>(Clock::now() - ev.submitted).count();
     t0 += m;
   }
+  // one thread per 4 MB, at most the server's copy threads
+  const int nt = (int)std::max<size_t>(1, std::min<size_t>(s->copyThreads, total >> 22));
+  auto work = [&](int k) {
+    for (size_t r = k; r < rows.size(); r += nt) std::memcpy(rows[r].dst, rows[r].src, rows[r].bytes);
+  };
+  std::vector<std::thread> helpers;
+  for (int k = 1; k < nt; ++k) helpers.emplace_back(work, k);
+  work(0);
+  for (auto& h : helpers) h.join();
+  const auto now = Clock::now();
+  for (auto& evp : sl.events)
+    evp->latencyMs = std::chrono::duration<double, std::milli>(now - evp->submitted).count();
 }
 
 void finishSlot(ck_server* s, Slot& sl, ck_status st) {
@@ -417,6 +446,25 @@ void finishSlot(ck_server* s, Slot& sl, ck_status st) {
   s->cvDone.notify_all();
 }
 
+// The delivery thread: de-strides the staged (pageable) results of finished
+// slots, so that the request loop keeps admitting and launching meanwhile;
+// the slot is free again once its results are in place.
+void deliveryLoop(ck_server* s) {
+  std::unique_lock<std::mutex> lock(s->mu);
+  while (true) {
+    s->cvHarvest.wait(lock, [&] { return s->stop || !s->toHarvest.empty(); });
+    if (s->toHarvest.empty()) break;  // stopping, nothing left
+    Slot* sl = s->toHarvest.front();
+    s->toHarvest.pop_front();
+    lock.unlock();
+    harvestSlot(s, *sl);
+    lock.lock();
+    sl->harvesting = false;
+    finishSlot(s, *sl, CK_OK);
+    s->cvWork.notify_one();
+  }
+}
+
 void workerLoop(ck_server* s) {
   cudaSetDevice(s->h->device);
   const size_t planned = (size_t)kPlannedSurfacesPerTrack * (size_t)s->capacity;
@@ -425,7 +473,7 @@ void workerLoop(ck_server* s) {
     // completion of in-flight slots
     for (auto& slp : s->slots) {
       Slot& sl = *slp;
-      if (!sl.busy) continue;
+      if (!sl.busy || sl.harvesting) continue;
       cudaError_t q = cudaEventQuery(sl.done);
       if (q == cudaErrorNotReady) continue;
       ck_status st = CK_OK;
@@ -434,9 +482,18 @@ void workerLoop(ck_server* s) {
         s->error = st;
         s->errorMsg = g_lastError;
       } else {
-        lock.unlock();
-        harvestSlot(s, sl);
-        lock.lock();
+        bool staged = false;
+        for (auto& ev : sl.events) staged |= ev->staged;
+        if (staged) {
+          // pageable results: the delivery thread copies them
+          sl.harvesting = true;
+          s->toHarvest.push_back(&sl);
+          s->cvHarvest.notify_one();
+          continue;
+        }
+        const auto now = Clock::now();
+        for (auto& ev : sl.events)
+          ev->latencyMs = std::chrono::duration<double, std::milli>(now - ev->submitted).count();
       }
       finishSlot(s, sl, st);
     }
@@ -472,12 +529,18 @@ void workerLoop(ck_server* s) {
         finishSlot(s, sl, st);
       }
     }
-    bool anyBusy = false;
-    for (auto& slp : s->slots) anyBusy |= slp->busy;
+    bool anyBusy = false, anyGpu = false;
+    for (auto& slp : s->slots) {
+      anyBusy |= slp->busy;
+      anyGpu |= slp->busy && !slp->harvesting;
+    }
     if (s->stop && !anyBusy && s->pending.empty()) break;
-    if (anyBusy) {
+    if (anyGpu) {
       // poll in-flight work at a short interval
       s->cvWork.wait_for(lock, std::chrono::microseconds(50));
+    } else if (anyBusy) {
+      // slots in delivery: the delivery thread notifies when one frees
+      s->cvWork.wait_for(lock, std::chrono::milliseconds(1));
     } else {
       s->cvWork.wait(lock, [&] { return s->stop || !s->pending.empty(); });
     }
@@ -537,7 +600,9 @@ ck_status ck_server_create(ck_handle* h, const ck_options* opt, const ck_server_
       return st;
     }
   }
+  s->copyThreads = (int)std::max(1u, std::min(8u, std::thread::hardware_concurrency() / 2));
   s->worker = std::thread(workerLoop, s.get());
+  s->delivery = std::thread(deliveryLoop, s.get());
   *out = s.release();
   return CK_OK;
 }
@@ -646,6 +711,8 @@ ck_status ck_server_destroy(ck_server* s) {
   }
   s->cvWork.notify_all();
   if (s->worker.joinable()) s->worker.join();
+  s->cvHarvest.notify_all();
+  if (s->delivery.joinable()) s->delivery.join();
   cudaSetDevice(s->h->device);
   for (auto& slp : s->slots) {
     Slot& sl = *slp;

@@ -553,36 +553,6 @@ def native_arm(args):
     return 0
 
 
-class PinnedBatch:
-    """A Batch's input arrays copied to page-locked host memory."""
-
-    def __init__(self, b, torch):
-        self.n = b.n
-        self._keep = {}
-        self._src = b
-
-    def pin(self, torch):
-        from acts_gb300 import abi
-
-        bi = abi.ck_batch_in()
-        bi.n_tracks = self.n
-        bi.memory = abi.MEM_HOST
-        for name, ct in (("seq_offsets", C.c_int32), ("seq_surfaces", C.c_int32),
-                         ("meas_offsets", C.c_int32), ("meas_surfaces", C.c_int32),
-                         ("meas_values", C.c_double), ("meas_cov", C.c_double),
-                         ("start_params", C.c_double), ("start_cov", C.c_double),
-                         ("start_frames", C.c_double), ("particle", C.c_float),
-                         ("particle_pdg", C.c_int32)):
-            t = torch.from_numpy(getattr(self._src, name)).pin_memory()
-            self._keep[name] = t
-            setattr(bi, name, C.cast(C.c_void_p(t.data_ptr()), C.POINTER(ct)))
-        self._bi = bi
-        return self
-
-    def as_batch_in(self):
-        return self._bi
-
-
 def batched_events_report(torch, dev, steps, warmup, autotune, seed=91, n_events=50,
                           mean_tracks=5000.0, max_states=20):
     """The batched uneven-events configuration: 50 events with Poisson(5,000)
@@ -640,15 +610,58 @@ def batched_events_report(torch, dev, steps, warmup, autotune, seed=91, n_events
     return rep
 
 
-def serving_report(torch, precisions=("mixed", "fp64"), event_tracks=10000, pool=12, seed=77,
-                   max_states=20):
-    """Continuous-batching serving loop on 10k-track events of the uneven
-    workload (20-cylinder barrel, 4-20 hits, holes, outliers, grid field):
-    inputs in page-locked host memory, results written into device buffers
-    (and, at one load, into page-locked and into pageable host buffers).
-    Capacity is measured by saturating the server; then Poisson arrivals at
-    fractions of it; p50/p99 event latency (submit -> results in place) and
-    sustained tracks/s per offered load."""
+class EventPool:
+    """Events of the serving configuration as slices of one pool of uneven
+    tracks in page-locked host memory: event i takes `sizes[i]` consecutive
+    pool tracks from a random start, with its own CSR offsets rebased to 0
+    (the other arrays are pointers into the pool)."""
+
+    PER_TRACK = (("start_params", C.c_double, 6), ("start_cov", C.c_double, 36),
+                 ("start_frames", C.c_double, 12), ("particle", C.c_float, 2),
+                 ("particle_pdg", C.c_int32, 1))
+    PER_SEQ = (("seq_surfaces", C.c_int32, 1),)
+    PER_MEAS = (("meas_surfaces", C.c_int32, 1), ("meas_values", C.c_double, 2),
+                ("meas_cov", C.c_double, 4))
+
+    def __init__(self, b, torch):
+        self.b = b
+        self.keep = {}
+        for name, ct, k in self.PER_TRACK + self.PER_SEQ + self.PER_MEAS:
+            self.keep[name] = torch.from_numpy(getattr(b, name)).pin_memory()
+        self.so = np.asarray(b.seq_offsets)
+        self.mo = np.asarray(b.meas_offsets)
+
+    def event(self, start, m):
+        from acts_gb300 import abi
+
+        a, e = start, start + m
+        so = np.ascontiguousarray(self.so[a:e + 1] - self.so[a], np.int32)
+        mo = np.ascontiguousarray(self.mo[a:e + 1] - self.mo[a], np.int32)
+        bi = abi.ck_batch_in()
+        bi.n_tracks = m
+        bi.memory = abi.MEM_HOST
+        bi.seq_offsets = abi.ptr(so, C.c_int32)
+        bi.meas_offsets = abi.ptr(mo, C.c_int32)
+        for group, first in ((self.PER_TRACK, a), (self.PER_SEQ, int(self.so[a])),
+                             (self.PER_MEAS, int(self.mo[a]))):
+            for name, ct, k in group:
+                t = self.keep[name]
+                addr = t.data_ptr() + first * k * t.element_size()
+                setattr(bi, name, C.cast(C.c_void_p(addr), C.POINTER(ct)))
+        return bi, (so, mo)
+
+
+def serving_report(torch, n_events=10000, seed=77, max_states=20, pool_tracks=400000,
+                   lo=100, hi=20000):
+    """The serving configuration: events with log-uniform 100-20,000 tracks
+    of the uneven workload (20-cylinder barrel, 4-20 hits, holes, outliers,
+    grid field), arriving as a Poisson process at an offered rate swept from
+    10 % to 120 % of the measured capacity, admitted against a 40 GB device
+    budget by the continuous-batching server; inputs in page-locked host
+    memory, results written to device buffers (at half load also to
+    page-locked and to pageable host buffers). Reports per load the
+    sustained tracks/s and p50/p99 submit-to-results latency of all events
+    and of the events with 8,000-12,000 tracks."""
     import threading
 
     from acts_gb300 import abi, generate
@@ -657,97 +670,125 @@ def serving_report(torch, precisions=("mixed", "fp64"), event_tracks=10000, pool
     from acts_gb300.serving import FitServer
 
     det = generate.Detector(abi.CKG_UNEVEN)
-    events = [PinnedBatch(generate.generate(det, event_tracks, seed=seed + i,
-                                            first_track=i * event_tracks), torch).pin(torch)
-              for i in range(pool)]
-    fit = CudaKalman.for_detector(det)
+    pool = EventPool(generate.generate(det, pool_tracks, seed=seed), torch)
+    sizes = generate.event_sizes(seed, n_events, -1.0, lo, hi)
     rng = np.random.default_rng(seed)
-    n_buf = 160
-    dev_results = [TorchResults(event_tracks, max_states, abi.OUT_SMOOTHED, device="cuda:0")
-                   for _ in range(n_buf)]
-    report = {"workload": "uneven barrel events of %d tracks (4-20 hits, holes 10 %%, outliers "
-                          "5 %%, grid field), Poisson arrivals; inputs in page-locked host "
-                          "memory" % event_tracks,
+    starts = rng.integers(0, pool_tracks - hi, n_events)
+    mean = float(sizes.mean())
+    comps = abi.OUT_SMOOTHED | abi.OUT_PACKED_COV
+    fit = CudaKalman.for_detector(det)
+    report = {"workload": "%d events, log-uniform %d-%d tracks (mean %.0f) of the uneven "
+                          "workload (4-20 hits, holes 10 %%, outliers 5 %%, grid field), "
+                          "Poisson arrivals; inputs in page-locked host memory"
+                          % (n_events, lo, hi, mean),
               "memory_budget_gb": 40, "streams": 3, "max_states": max_states,
               "launch": "each co-batch on the SMs / (streams - 1) blocks, 6 Runge-Kutta trials "
                         "per scheduling round (the server's defaults)"}
-    # the kernel time of one event alone (whole GPU, device-resident)
-    one = generate.generate(det, event_tracks, seed=seed)
-    for name in precisions:
+
+    class _Lat:
+        def __init__(self):
+            self.lat, self.done = {}, threading.Event()
+
+    for name in ("mixed", "fp64"):
         prec = abi.PRECISION_MIXED if name == "mixed" else abi.PRECISION_FP64
         opt = abi.default_options(precision=prec, outlier_chi2_cut=15.0)
-        for _ in range(3):
-            fit.fit_batch(one, opt, max_states=max_states, components=abi.OUT_SMOOTHED)
         srv = FitServer(fit, opt, memory_budget_bytes=40 << 30, n_streams=3,
-                        max_states=max_states, max_batch_tracks=8 * event_tracks)
+                        max_states=max_states, max_batch_tracks=8 * hi, components=comps)
 
-        def run(n_events, rate, first_id, results_of):
-            lat = {}
-            done = threading.Event()
+        def run(idx, rate, results_of):
+            """Submits events idx (Poisson arrivals at `rate` events/s; 0:
+            back to back); returns {event: latency ms} and the wall time."""
+            st = _Lat()
+            n_ev = len(idx)
+            held = {}
 
             def poller():
-                while len(lat) < n_events:
+                while len(st.lat) < n_ev:
                     r = srv.poll(timeout_ms=200)
                     if r is not None:
-                        lat[r[0]] = r[2]
-                done.set()
+                        st.lat[r[0]] = r[2]
+                        held.pop(r[0], None)
+                st.done.set()
 
             th = threading.Thread(target=poller, daemon=True)
             th.start()
             t0 = time.perf_counter()
-            gaps = rng.exponential(1.0 / rate, n_events) if rate else np.zeros(n_events)
+            gaps = rng.exponential(1.0 / rate, n_ev) if rate else np.zeros(n_ev)
             t_next = t0
-            for i in range(n_events):
-                t_next += gaps[i]
+            for k, i in enumerate(idx):
+                t_next += gaps[k]
                 while True:
                     dt = t_next - time.perf_counter()
                     if dt <= 0:
                         break
-                    time.sleep(min(dt, 0.001))
-                srv.submit(first_id + i, events[i % pool], results_of(i))
-            done.wait(120)
-            wall = time.perf_counter() - t0
-            return np.array(list(lat.values())), wall
+                    time.sleep(min(dt, 0.0005))
+                bi, keep = pool.event(int(starts[i]), int(sizes[i]))
+                res = results_of(int(sizes[i]))
+                held[int(i)] = (keep, res)
+                srv.submit(int(i), _Wrap(bi), res)
+            st.done.wait(600)
+            return st.lat, time.perf_counter() - t0
 
-        on_device = lambda i: dev_results[i % n_buf]
-        run(2 * pool, 0, 0, on_device)  # warm-up
-        n_cap = n_buf
-        v, wall = run(n_cap, 0, 1000, on_device)
-        cap_events = n_cap / wall
-        res = {"capacity_tracks_per_s": round(cap_events * event_tracks, 1),
-               "results": "device memory", "loads": []}
-        loads = (0.1, 0.3, 0.5, 0.8, 1.0, 1.2) if name == "mixed" else (0.1, 0.5, 1.0)
-        nid = 10000
-        for f in loads:
-            rate = f * cap_events
-            n_ev = int(min(n_buf, max(40, rate * 1.0)))
-            v, wall = run(n_ev, rate, nid, on_device)
-            nid += n_ev
-            res["loads"].append({"offered_fraction": f, "events": n_ev,
-                                 "offered_tracks_per_s": round(rate * event_tracks, 1),
-                                 "sustained_tracks_per_s": round(n_ev * event_tracks / wall, 1),
-                                 "p50_ms": round(float(np.percentile(v, 50)), 3),
-                                 "p99_ms": round(float(np.percentile(v, 99)), 3)})
+        def stats(lat, idx, wall):
+            v = np.array([lat[int(i)] for i in idx])
+            m = sizes[idx]
+            sel = (m >= 8000) & (m <= 12000)
+            out = {"events": int(len(idx)),
+                   "sustained_tracks_per_s": round(float(m.sum()) / wall, 1),
+                   "p50_ms": round(float(np.percentile(v, 50)), 3),
+                   "p99_ms": round(float(np.percentile(v, 99)), 3)}
+            if sel.sum() >= 10:
+                out["events_8k_12k"] = int(sel.sum())
+                out["p50_ms_8k_12k"] = round(float(np.percentile(v[sel], 50)), 3)
+                out["p99_ms_8k_12k"] = round(float(np.percentile(v[sel], 99)), 3)
+            return out
+
+        on_device = lambda m: TorchResults(m, max_states, comps, device="cuda:0")
+        run(np.arange(50), 0, on_device)  # warm-up
+        cap_idx = np.arange(2000 if name == "mixed" else 500)
+        lat, wall = run(cap_idx, 0, on_device)
+        cap_tracks = float(sizes[cap_idx].sum()) / wall
+        res = {"capacity_tracks_per_s": round(cap_tracks, 1), "results": "device memory",
+               "loads": []}
+        if name == "mixed":
+            plan = ((0.1, 2500), (0.3, n_events), (0.5, n_events), (0.8, n_events),
+                    (1.0, n_events), (1.2, n_events))
+        else:
+            plan = ((0.1, 800), (0.5, 1000), (1.0, 1000), (1.2, 1000))
+        for f, cnt in plan:
+            idx = np.arange(cnt)
+            rate = f * cap_tracks / mean
+            lat, wall = run(idx, rate, on_device)
+            entry = {"offered_fraction": f, "offered_tracks_per_s": round(rate * mean, 1)}
+            entry.update(stats(lat, idx, wall))
+            res["loads"].append(entry)
+            log("serving %s %.1f: %s" % (name, f, entry))
         if name == "mixed":
             # results delivered to host memory at half load
-            pinned = [TorchResults(event_tracks, max_states, abi.OUT_SMOOTHED, device="pinned")
-                      for _ in range(40)]
-            host = [Results(event_tracks, max_states, abi.OUT_SMOOTHED) for _ in range(40)]
-            for label, bufs in (("page-locked host memory", pinned), ("pageable host memory", host)):
-                rate = 0.5 * cap_events
-                v, wall = run(40, rate, nid, lambda i: bufs[i])
-                nid += 40
-                res.setdefault("host_delivery", []).append(
-                    {"results": label, "offered_fraction": 0.5, "events": 40,
-                     "p50_ms": round(float(np.percentile(v, 50)), 3),
-                     "p99_ms": round(float(np.percentile(v, 99)), 3)})
-            del pinned, host
+            for label, dev_kind in (("page-locked host memory", "pinned"),
+                                    ("pageable host memory", None)):
+                mk = ((lambda m: TorchResults(m, max_states, comps, device="pinned"))
+                      if dev_kind else (lambda m: Results(m, max_states, comps)))
+                idx = np.arange(600)
+                lat, wall = run(idx, 0.5 * cap_tracks / mean, mk)
+                entry = {"results": label, "offered_fraction": 0.5}
+                entry.update(stats(lat, idx, wall))
+                res.setdefault("host_delivery", []).append(entry)
         srv.close()
-        fit.fit_batch(one, opt, max_states=max_states, components=abi.OUT_SMOOTHED)
-        res["kernel_ms_one_event_whole_gpu"] = round(fit.last_kernel_ms(), 3)
         report[name] = res
     fit.close()
     return report
+
+
+class _Wrap:
+    """A ready ck_batch_in for FitServer.submit."""
+
+    def __init__(self, bi):
+        self.bi = bi
+        self.n = bi.n_tracks
+
+    def as_batch_in(self):
+        return self.bi
 
 
 class _Null:
