@@ -604,6 +604,81 @@ CK_D bool getGridField(const DevField& F, const P p[3], P B[3]) {
   return true;
 }
 
+// The field cell last used by a track slot, in shared memory: the eight
+// grid nodes of the cell and its linear index (-1: none). A lookup in the
+// same cell takes the nodes from here instead of gathering them from L2/HBM
+// again (the reference's InterpolatedBFieldMap cell cache,
+// InterpolatedBFieldMap.hpp:238-264; on the uneven workload 56-62 % of the
+// lookups fall in the cell of the lookup before). The cell is identified by
+// the bin indices the lookup computes, so a cached lookup evaluates exactly
+// the expressions of an uncached one.
+struct CellCache {
+  float4 v[8];
+  int key;
+  int pad[3];
+};
+
+template <typename P>
+CK_D bool getGridFieldCached(const DevField& F, const P p[3], P B[3], CellCache* cell) {
+  int bin[3];
+  P f[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    P mn, width, upper;
+    gridConstants(F, i, mn, width, upper);
+    if (p[i] < mn || p[i] >= upper) return false;
+    P u = (p[i] - mn) / width;
+    int bb = (int)floor(u);
+    bb = max(0, min(bb, F.n[i] - 2));
+    bin[i] = bb;
+    P ll = mn + (P)bb * width;
+    P ur = mn + (P)(bb + 1) * width;
+    f[i] = (p[i] - ll) / (ur - ll);
+  }
+  const size_t nz = F.n[2], nyz = (size_t)F.n[1] * F.n[2];
+  const size_t base = bin[0] * nyz + bin[1] * nz + bin[2];
+  const int key = (int)base;
+  float4 v[8];
+  if (cell->key == key) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) v[c] = cell->v[c];
+  } else {
+#pragma unroll
+    for (int cx = 0; cx < 2; ++cx)
+#pragma unroll
+      for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+        for (int cz = 0; cz < 2; ++cz)
+          v[cx * 4 + cy * 2 + cz] = __ldg(&F.nodes[base + cx * nyz + cy * nz + cz]);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) cell->v[c] = v[c];
+    cell->key = key;
+  }
+  P r[4][3];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    r[i][0] = (P(1) - f[2]) * (P)v[2 * i].x + f[2] * (P)v[2 * i + 1].x;
+    r[i][1] = (P(1) - f[2]) * (P)v[2 * i].y + f[2] * (P)v[2 * i + 1].y;
+    r[i][2] = (P(1) - f[2]) * (P)v[2 * i].z + f[2] * (P)v[2 * i + 1].z;
+  }
+  P s0[3], s1[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    s0[c] = (P(1) - f[1]) * r[0][c] + f[1] * r[1][c];
+    s1[c] = (P(1) - f[1]) * r[2][c] + f[1] * r[3][c];
+  }
+  const P unit = (P)0.000299792458;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) B[c] = ((P(1) - f[0]) * s0[c] + f[0] * s1[c]) * unit;
+  return true;
+}
+
+template <typename P>
+CK_D bool getFieldCached(const DevField& F, const P p[3], P B[3], CellCache* cell) {
+  if (F.kind == CK_FIELD_CONSTANT) return getField(F, p, B);
+  return getGridFieldCached(F, p, B, cell);
+}
+
 // --------------------------------------------------------------- material
 // Interactions.cpp (float physics) with un-contracted float arithmetic.
 struct RelQ {

@@ -119,8 +119,22 @@ CK_D bool reverseSelected(const FitParams& fp, int q, int tip) {
 // it writes no records, only its latest filtered measurement state (the
 // extrapolation start slot 0) and, when it reaches the reference surface,
 // the track parameters there.
-template <typename P, typename CV, bool F2B = false, bool REV = false>
-struct Lane {
+// The shared-memory field cell of a lane's slot (kernels that stage the
+// field grid); empty for the others
+template <bool CELL>
+struct CellSlot {
+  CK_D CellCache* cellPtr() const { return nullptr; }
+};
+template <>
+struct CellSlot<true> {
+  CellCache* cell;
+  CK_D CellCache* cellPtr() const { return cell; }
+};
+
+// CELL: the field lookups of the Runge-Kutta stages go through the slot's
+// shared-memory cell cache (getFieldCached)
+template <typename P, typename CV, bool F2B = false, bool REV = false, bool CELL = false>
+struct Lane : CellSlot<CELL> {
   // ---- identity: track index and queue position (which indexes the records)
   int phase;
   int t;
@@ -1088,6 +1102,14 @@ struct Lane {
     prePropagation(fp, slot);
   }
 
+  // the field at a Runge-Kutta stage point
+  CK_D bool stageField(const FitParams& fp, const P p[3], P B[3]) const {
+    if constexpr (CELL)
+      return getFieldCached(fp.field, p, B, this->cellPtr());
+    else
+      return getField(fp.field, p, B);
+  }
+
   // STEP: one Runge-Kutta trial (EigenStepper::step, EigenStepper.ipp:168-388)
   // MODE (StepMode): the lane fits, extrapolates to the reference surface or
   // propagates (signed step direction, the aborters after each step); the
@@ -1111,7 +1133,7 @@ struct Lane {
     const P dir[3] = {toP<P>(this->dir[0]), toP<P>(this->dir[1]), toP<P>(this->dir[2])};
     const P qop = toP<P>(this->qop);
     P B1[3], B2[3], B3[3];
-    if (!getField(fp.field, pp, B1)) {
+    if (!stageField(fp, pp, B1)) {
       fail(fp, CK_TRACK_FIELD_OUT_OF_BOUNDS);
       return;
     }
@@ -1126,7 +1148,7 @@ struct Lane {
     P p1[3], tt[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) p1[i] = pp[i] + hh * dir[i] + h2 * P(0.125) * k1[i];
-    if (!getField(fp.field, p1, B2)) {
+    if (!stageField(fp, p1, B2)) {
       fail(fp, CK_TRACK_FIELD_OUT_OF_BOUNDS);
       return;
     }
@@ -1142,7 +1164,7 @@ struct Lane {
     k3[2] = qop * (tt[0] * B2[1] - tt[1] * B2[0]);
 #pragma unroll
     for (int i = 0; i < 3; ++i) p1[i] = pp[i] + h * dir[i] + h2 * P(0.5) * k3[i];
-    if (!getField(fp.field, p1, B3)) {
+    if (!stageField(fp, p1, B3)) {
       fail(fp, CK_TRACK_FIELD_OUT_OF_BOUNDS);
       return;
     }
@@ -2098,9 +2120,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) fitKernel(FitParams fp) {
 // carries are the FP64 throughput it gets.
 // One phase step of a slot; fetching threads take one ticket per warp (the
 // threads of the warp that run this call together).
-template <typename P, typename CV, bool F2B, bool REV>
-__device__ __forceinline__ void advanceSlot(const FitParams& fp, Lane<P, CV, F2B, REV>& L, int c,
-                                            int lane, int spr) {
+template <typename P, typename CV, bool F2B, bool REV, bool CELL>
+__device__ __forceinline__ void advanceSlot(const FitParams& fp, Lane<P, CV, F2B, REV, CELL>& L,
+                                            int c, int lane, int spr) {
   if (c == PH_FETCH) {
     const unsigned act = __activemask();
     const int leader = __ffs(act) - 1;
@@ -2211,12 +2233,14 @@ constexpr size_t compactSmemBytes() {
 // block-wide round. A warp leaves when all pools are empty: slots still in
 // flight belong to warps that are running and that claim them again after
 // returning them, so every slot is finished, and nothing spins.
-template <typename P, typename CV, int S, int T>
+// CELL: each slot also holds its field cell in shared memory (after the
+// lanes), the grid-field workloads' variant.
+template <typename P, typename CV, int S, int T, bool CELL = false>
 __global__ void __launch_bounds__(T, 1) fitKernelPool(FitParams fp) {
   static_assert(S % 32 == 0 && S / 32 <= 32 && T % 32 == 0, "pool shape");
   constexpr int W = S / 32;  // mask words per phase
   extern __shared__ __align__(16) unsigned char smem[];
-  using LaneT = Lane<P, CV>;
+  using LaneT = Lane<P, CV, false, false, CELL>;
   LaneT* st = reinterpret_cast<LaneT*>(smem);
   __shared__ unsigned pool[3][W];
   __shared__ int items[T / 32][32];
@@ -2230,6 +2254,12 @@ __global__ void __launch_bounds__(T, 1) fitKernelPool(FitParams fp) {
     st[sl].phase = sl < active ? PH_FETCH : PH_DONE;
     st[sl].t = -1;
     st[sl].q = -1;
+    if constexpr (CELL) {
+      constexpr size_t off = (sizeof(LaneT) * S + 15) & ~(size_t)15;
+      CellCache* cells = reinterpret_cast<CellCache*>(smem + off);
+      cells[sl].key = -1;
+      st[sl].cell = cells + sl;
+    }
   }
   if (tid < W) {
     const int lo = tid * 32;
@@ -2314,9 +2344,10 @@ __global__ void __launch_bounds__(T, 1) fitKernelPool(FitParams fp) {
   }
 }
 
-template <typename P, typename CV, int S>
+template <typename P, typename CV, int S, bool CELL = false>
 constexpr size_t poolSmemBytes() {
-  return sizeof(Lane<P, CV>) * S;
+  return ((sizeof(Lane<P, CV, false, false, CELL>) * S + 15) & ~(size_t)15) +
+         (CELL ? sizeof(CellCache) * S : 0);
 }
 
 // Smoother kernel: one lane per queue position; lanes of a warp hold tracks
