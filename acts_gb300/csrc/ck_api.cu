@@ -1117,6 +1117,15 @@ ck_status ck_get_launch_config(ck_handle* h, int32_t precision, int32_t* tpb, in
   return CK_OK;
 }
 
+ck_status ck_get_launch_variant(ck_handle* h, int32_t precision, int32_t* variant,
+                                int32_t* steps_per_round) {
+  if (!h || !variant || !steps_per_round || precision < 0 || precision >= CK_NUM_PRECISIONS)
+    return fail(CK_ERR_INVALID_ARGUMENT, "bad argument");
+  *variant = h->tune[precision].variant;
+  *steps_per_round = h->tune[precision].spr;
+  return CK_OK;
+}
+
 ck_status ck_set_launch_config(ck_handle* h, int32_t precision, int32_t variant, int32_t tpb,
                                int32_t bps) {
   if (!h || precision < 0 || precision >= CK_NUM_PRECISIONS || !validLaunch(variant, tpb) ||

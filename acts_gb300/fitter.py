@@ -75,6 +75,7 @@ def lib():
         L.ck_last_launch_count.argtypes = [C.c_void_p, P(C.c_int32)]
         L.ck_last_transfer_bytes.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64)]
         L.ck_get_launch_config.argtypes = [C.c_void_p, C.c_int32, P(C.c_int32), P(C.c_int32)]
+        L.ck_get_launch_variant.argtypes = [C.c_void_p, C.c_int32, P(C.c_int32), P(C.c_int32)]
         L.ck_set_launch_config.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
         L.ck_sort_queue.argtypes = [C.c_void_p, C.c_int32]
         L.ck_autotune.argtypes = [C.c_void_p, P(abi.ck_options), P(abi.ck_batch_in),
@@ -332,6 +333,12 @@ class CudaKalman:
         t, b = C.c_int32(), C.c_int32()
         _check(lib().ck_get_launch_config(self._h, precision, C.byref(t), C.byref(b)))
         return t.value, b.value
+
+    def launch_variant(self, precision):
+        """(forward-filter kernel variant, Runge-Kutta trials per round)."""
+        v, spr = C.c_int32(), C.c_int32()
+        _check(lib().ck_get_launch_variant(self._h, int(precision), C.byref(v), C.byref(spr)))
+        return v.value, spr.value
 
     def set_launch_config(self, precision, variant, tpb, bps):
         _check(lib().ck_set_launch_config(self._h, precision, variant, tpb, bps))

@@ -282,13 +282,41 @@ def accuracy_report(b, r64, rmx, n):
             "chi2ndf_fp64": c64, "chi2ndf_mixed": cmx}
 
 
-# Per-track figures of the ncu capture summarised in
-# profiles/fit_smooth_kernels_barrel200k.md (barrel, 200k tracks, ten states).
-NCU_PER_TRACK = {
-    "mixed_filter_fp64_flops": 8.72e3, "mixed_filter_fp32_flops": 33.4e3,
-    "mixed_filter_dram_bytes": 6.07e3, "mixed_filter_fp64_pipe_busy": 0.572,
-    "fp64_filter_fp64_flops": 43.9e3, "fp64_filter_dram_bytes": 10.26e3,
-    "fp64_filter_fp64_pipe_busy": 0.645}
+# Forward-filter kernel of a precision form and variant (ck_set_launch_config),
+# as ncu names its template instance
+_VARIANT_KERNELS = {
+    "float": {0: "fitKernel<float, float, 128, 1>", 1: "fitKernel<float, float, 128, 3>",
+              2: "fitKernel<float, float, 128, 4>",
+              3: "fitKernelCompact<float, float, 256, false, false>",
+              4: "fitKernelCompact<float, float, 128, false, false>",
+              5: "fitKernelPool<float, float, 384, 256, false>",
+              6: "fitKernelPool<float, float, 448, 256, false>",
+              7: "fitKernelPool<float, float, 320, 256, true>"},
+    "double": {0: "fitKernel<double, double, 128, 1>", 1: "fitKernel<double, double, 128, 3>",
+               2: "fitKernel<double, double, 128, 4>",
+               3: "fitKernelCompact<double, double, 256, false, false>",
+               4: "fitKernelCompact<double, double, 128, false, false>",
+               5: "fitKernelPool<double, double, 320, 256, false>",
+               6: "fitKernelPool<double, double, 256, 256, false>",
+               7: "fitKernelPool<double, double, 256, 256, true>"}}
+COUNTERS = os.path.join(ROOT, "profiles", "fit_kernel_counters.txt")
+
+
+def kernel_counters(scalar, variant):
+    """The committed ncu per-track counters of a forward-filter kernel, when
+    they were captured from the sources that run now (else None, reason)."""
+    from acts_gb300 import profile_counters
+
+    name = _VARIANT_KERNELS[scalar].get(variant)
+    if not os.path.exists(COUNTERS):
+        return None, "no counters file"
+    src, lines = profile_counters.parse(COUNTERS)
+    if src != profile_counters.source_hash():
+        return None, "counters captured from other kernel sources (%s)" % src
+    for ln in lines:
+        if name and name in ln["kernel"]:
+            return ln, name
+    return None, "no capture of %s" % name
 
 
 def best_of_tune_log(log):
@@ -465,40 +493,51 @@ def native_arm(args):
         return 0
 
     # ---- roofline of the dominant kernel of the mixed step: the forward
-    # filter fitKernel*<float,float>. It is bound by the FP64 pipe. The
-    # algorithmic FP64 work of the mixed formulation per track and its DRAM
-    # bytes per track come from the ncu capture summarised in
-    # profiles/fit_smooth_kernels_barrel200k.md (same kernels, 200k-track
-    # case; both scale with the track count); the duration is measured here.
+    # filter, bound by the FP64 pipe. Its FP64 flops and DRAM bytes per track
+    # come from the committed ncu counters of the kernel variant launched,
+    # valid while their source hash matches the sources that run (both scale
+    # with the track count); the duration is measured here.
     from oracle import kforacle
 
     flops = kforacle.count_flops(det, b, forms["fp64"], 0, 300)
     peak64 = fit.fp_peak_gflops(abi.PRECISION_FP64) / 1e3
     peak32 = fit.fp_peak_gflops(abi.PRECISION_MIXED) / 1e3
-    per_track = NCU_PER_TRACK
     fwd_mx = results["mixed"]["filter_kernel_ms"] * 1e-3
     fwd_64 = results["fp64"]["filter_kernel_ms"] * 1e-3
-    ach_mx = per_track["mixed_filter_fp64_flops"] * n / fwd_mx / 1e12
-    ach_64 = per_track["fp64_filter_fp64_flops"] * n / fwd_64 / 1e12
-    roofline = {"bound": "fp64", "kernel": "fitKernelCompact<float,float> (mixed forward filter)",
-                "achieved": round(ach_mx, 4), "peak": round(peak64, 4), "unit": "TFLOP/s",
-                "frac": round(ach_mx / peak64, 4),
-                "traffic": int(per_track["mixed_filter_dram_bytes"] * n),
-                "algorithmic_flops_per_track": per_track["mixed_filter_fp64_flops"],
-                "flops_definition": "FP64 flops of the mixed formulation's forward filter per "
-                                    "track (the FP32 work, %.1f kflop/track, runs on a 63x "
-                                    "faster pipe), counted by ncu" %
-                                    (per_track["mixed_filter_fp32_flops"] / 1e3),
+    cm, why_m = kernel_counters("float", fit.launch_variant(abi.PRECISION_MIXED)[0])
+    c64, why_64 = kernel_counters("double", fit.launch_variant(abi.PRECISION_FP64)[0])
+    roofline = {"bound": "fp64", "unit": "TFLOP/s", "peak": round(peak64, 4),
                 "duration_ms": round(fwd_mx * 1e3, 3),
-                "fp64_pipe_busy_ncu": per_track["mixed_filter_fp64_pipe_busy"],
                 "peak_source": "measured live: FP64 FMA loop (ck_fp_peak_gflops); "
                                "MEASURED_PEAKS.json holds no FP64 figure",
-                "traffic_source": "ncu dram__bytes_read+write per track x tracks",
-                "fp64_form": {"kernel": "fitKernelCompact<double,double>",
-                              "achieved": round(ach_64, 4), "frac": round(ach_64 / peak64, 4),
-                              "duration_ms": round(fwd_64 * 1e3, 3),
-                              "fp64_pipe_busy_ncu": per_track["fp64_filter_fp64_pipe_busy"],
-                              "traffic": int(per_track["fp64_filter_dram_bytes"] * n)},
+                "counters_source": "profiles/fit_kernel_counters.txt (ncu per-track counts of "
+                                   "the launched kernel; source hash checked)"}
+    if cm is not None:
+        ach_mx = cm["fp64_flops"] * n / fwd_mx / 1e12
+        roofline.update({
+            "kernel": why_m + " (mixed forward filter)",
+            "achieved": round(ach_mx, 4), "frac": round(ach_mx / peak64, 4),
+            "traffic": int(cm["dram_bytes"] * n),
+            "algorithmic_flops_per_track": round(cm["fp64_flops"], 1),
+            "flops_definition": "FP64 flops of the mixed formulation's forward filter per "
+                                "track (its FP32 work, %.1f kflop/track, runs on a 63x faster "
+                                "pipe), counted by ncu" % (cm["fp32_flops"] / 1e3),
+            "fp64_pipe_busy_ncu": cm["fp64_pipe_busy"],
+            "fp32_frac": round(cm["fp32_flops"] * n / fwd_mx / 1e12 / peak32, 4)})
+    else:
+        roofline.update({"kernel": "mixed forward filter", "achieved": None, "frac": None,
+                         "traffic": None, "counters_missing": why_m})
+    if c64 is not None:
+        ach_64 = c64["fp64_flops"] * n / fwd_64 / 1e12
+        roofline["fp64_form"] = {"kernel": why_64, "achieved": round(ach_64, 4),
+                                 "frac": round(ach_64 / peak64, 4),
+                                 "duration_ms": round(fwd_64 * 1e3, 3),
+                                 "fp64_pipe_busy_ncu": c64["fp64_pipe_busy"],
+                                 "traffic": int(c64["dram_bytes"] * n)}
+    else:
+        roofline["fp64_form"] = {"duration_ms": round(fwd_64 * 1e3, 3), "frac": None,
+                                 "counters_missing": why_64}
+    roofline.update({
                 "reference_formulation": {
                     "flops_per_track": round(flops["flops"], 1),
                     "definition": "FP64 flops of the reference's dense formulation (8x8 "
@@ -508,11 +547,11 @@ def native_arm(args):
                                                      (results["mixed"]["kernel_ms"] * 1e-3) / 1e12, 3),
                     "equivalent_tflops_fp64": round(flops["flops"] * n /
                                                     (results["fp64"]["kernel_ms"] * 1e-3) / 1e12, 3)},
-                "fp32_peak_tflops": round(peak32, 3)}
+                "fp32_peak_tflops": round(peak32, 3)})
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
         roofline["hbm_gbs_of_measured"] = round(roofline["traffic"] / fwd_mx / 1e9 / peaks["hbm_gbs"], 5)
-    except (OSError, KeyError, ValueError, ZeroDivisionError):
+    except (OSError, KeyError, ValueError, ZeroDivisionError, TypeError):
         pass
 
     acc = accuracy_report(b, snapshots["fp64"], snapshots["mixed"], min(n, 100000))

@@ -435,12 +435,18 @@ ck_status ck_last_transfer_bytes(ck_handle* h, int64_t* h2d_bytes,
 ck_status ck_get_launch_config(ck_handle* h, int32_t precision,
                                int32_t* threads_per_block,
                                int32_t* blocks_per_sm);
+/* The forward-filter kernel variant of a precision form (see
+ * ck_set_launch_config) and its Runge-Kutta trials per scheduling round. */
+ck_status ck_get_launch_variant(ck_handle* h, int32_t precision, int32_t* variant,
+                                int32_t* steps_per_round);
 
 /* Pins the launch shape of the forward-filter kernel: variant (0-2
  * per-warp phase scheduling with register caps of 255 / 168 / 128 per
  * thread and any multiple of 32 up to 128 threads per block; 3 and 4
- * block-level phase compaction with 256 and 128 threads per block), threads
- * per block and resident blocks per SM. */
+ * block-level phase compaction with 256 and 128 threads per block; 5-7
+ * warp-autonomous phase pools with 256 threads per block and more track
+ * slots than threads, 7 with each slot's field cell in shared memory),
+ * threads per block and resident blocks per SM. */
 ck_status ck_set_launch_config(ck_handle* h, int32_t precision, int32_t variant,
                                int32_t threads_per_block, int32_t blocks_per_sm);
 
