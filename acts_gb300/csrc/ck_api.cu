@@ -244,12 +244,12 @@ size_t compBytes(int n, int maxStates, int C, size_t elem) {
 void loadTuneCache(ck_handle* h) {
   if (h->cachePath.empty()) return;
   std::ifstream f(h->cachePath);
-  int p, v, tpb, bps, spr;
-  while (f >> p >> v >> tpb >> bps >> spr) {
+  int p, v, tpb, bps, spr, stg;
+  while (f >> p >> v >> tpb >> bps >> spr >> stg) {
     if (p < 0 || p >= CK_NUM_PRECISIONS || !validLaunch(v, tpb) || bps <= 0 || spr < 1 ||
         spr > 64)
       continue;
-    h->tune[p] = {v, tpb, bps, spr, 1};
+    h->tune[p] = {v, tpb, bps, spr, 1, 0, stg ? 1 : 0};
   }
 }
 
@@ -259,7 +259,7 @@ void saveTuneCache(ck_handle* h) {
   for (int p = 0; p < CK_NUM_PRECISIONS; ++p)
     if (h->tune[p].tuned)
       f << p << " " << h->tune[p].variant << " " << h->tune[p].tpb << " " << h->tune[p].bps << " "
-        << h->tune[p].spr << "\n";
+        << h->tune[p].spr << " " << h->tune[p].staged << "\n";
 }
 
 cudaError_t launchFit(const FitParams& fp, int precision, const Tune& tn, int grid,
@@ -371,6 +371,7 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
   fp.surfaces = h->dSurfaces;
   fp.trig = h->dTrig;
   fp.steps_per_round = tn.spr > 0 ? tn.spr : 1;
+  fp.smooth_staged = tn.staged;
   fp.n_surfaces = h->nSurfaces;
   fp.field = h->field;
   fp.mc = h->mc;
@@ -624,6 +625,7 @@ ck_status ck_create(const ck_config* cfg, ck_handle** out) {
     h->tune[p].bps = cfg->blocks_per_sm > 0 ? cfg->blocks_per_sm : 0;
     h->tune[p].spr = kDefaultStepsPerRound[p];
     h->tune[p].tuned = 0;
+    h->tune[p].staged = kDefaultSmootherStaged;
   }
   loadTuneCache(h);
   for (int p = 0; p < CK_NUM_PRECISIONS; ++p) {
@@ -1134,7 +1136,16 @@ ck_status ck_set_launch_config(ck_handle* h, int32_t precision, int32_t variant,
   std::lock_guard<std::mutex> lock(h->mu);
   int maxB = occupancyBlocks(precision, variant, tpb);
   if (bps > maxB) return fail(CK_ERR_INVALID_ARGUMENT, "more blocks per SM than fit");
-  h->tune[precision] = {variant, tpb, bps, h->tune[precision].spr, 1, h->tune[precision].grid};
+  h->tune[precision] = {variant, tpb, bps, h->tune[precision].spr, 1, h->tune[precision].grid,
+                        h->tune[precision].staged};
+  return CK_OK;
+}
+
+ck_status ck_set_smoother_staging(ck_handle* h, int32_t precision, int32_t enable) {
+  if (!h || precision < 0 || precision >= CK_NUM_PRECISIONS)
+    return fail(CK_ERR_INVALID_ARGUMENT, "bad precision");
+  std::lock_guard<std::mutex> lock(h->mu);
+  h->tune[precision].staged = enable ? 1 : 0;
   return CK_OK;
 }
 
@@ -1197,15 +1208,27 @@ ck_status ck_autotune(ck_handle* h, const ck_options* opt, const ck_batch_in* in
       if (!validLaunch(v, tpb)) continue;
       const int maxB = occupancyBlocks(p, v, tpb);
       if (maxB <= 0) continue;
+      const int stg = h->tune[p].staged;
       if (variantBlock(v)) {
-        for (int spr = 1; spr <= 4; ++spr) cands.push_back({v, tpb, maxB, spr, 1});
+        for (int spr = 1; spr <= 4; ++spr) cands.push_back({v, tpb, maxB, spr, 1, 0, stg});
       } else {
         const int bs[3] = {maxB, std::max(1, (maxB * 3) / 4), std::max(1, maxB / 2)};
         for (int i = 0; i < 3; ++i)
-          if (i == 0 || bs[i] != bs[i - 1]) cands.push_back({v, tpb, bs[i], 1, 1});
+          if (i == 0 || bs[i] != bs[i - 1]) cands.push_back({v, tpb, bs[i], 1, 1, 0, stg});
       }
     }
-  for (const Tune& cand : cands) {
+  // the best launch shape, then the same with the other smoother kernel
+  // (gain-matrix smoother only)
+  const size_t nShapes = cands.size();
+  for (size_t ci = 0; ci <= nShapes; ++ci) {
+    Tune cand;
+    if (ci < nShapes) {
+      cand = cands[ci];
+    } else {
+      if (opt->smoother != CK_SMOOTHER_GAIN_MATRIX || bestMs >= 1e30) break;
+      cand = best;
+      cand.staged = 1 - best.staged;
+    }
     {
       std::lock_guard<std::mutex> lock(h->mu);
       h->tune[p] = cand;
@@ -1220,8 +1243,8 @@ ck_status ck_autotune(ck_handle* h, const ck_options* opt, const ck_batch_in* in
     }
     const double ms = tot / 2;
     char buf[128];
-    std::snprintf(buf, sizeof(buf), "v%d tpb%d bps%d spr%d %.3fms; ", cand.variant, cand.tpb,
-                  cand.bps, cand.spr, ms);
+    std::snprintf(buf, sizeof(buf), "v%d tpb%d bps%d spr%d stg%d %.3fms; ", cand.variant,
+                  cand.tpb, cand.bps, cand.spr, cand.staged, ms);
     log += buf;
     if (ms < bestMs) {
       bestMs = ms;

@@ -29,6 +29,7 @@ struct Tune {
   int spr;      // Runge-Kutta trials per round (compaction variants)
   int tuned;
   int grid;     // blocks of the fit kernel's grid; 0: SMs * bps
+  int staged;   // smoother with warp-cooperative record staging
 };
 
 // Identity of a captured batch pipeline.

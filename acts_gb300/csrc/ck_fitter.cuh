@@ -35,6 +35,8 @@
 // tolerance is resolvable.
 #pragma once
 
+#include <type_traits>
+
 #include "ck_device.cuh"
 
 namespace ck {
@@ -1769,6 +1771,37 @@ struct Smoother {
   int nM, nH, nO, ndf;
   double chi2sum;
 
+  // the per-track set-up of run(): the first and last measurement states, the
+  // extrapolation start slots, zero counters (the staged kernel's entry)
+  CK_D void begin(const FitParams& fp, int queuePos, int track, int tip) {
+    t = track;
+    q = queuePos;
+    lastMeas = tip;
+    firstMeas = -1;
+    const Rec<CV> rec(fp, q);
+    if (fp.ext) {
+      fp.ext[2 * (size_t)q].surface = -1;
+      fp.ext[2 * (size_t)q].fitted = 0;
+      fp.ext[2 * (size_t)q + 1].surface = -1;
+      for (int k = 0; k <= tip; ++k) {
+        const uint32_t fl = (uint32_t)rec.s(k).flags;
+        if ((fl & CK_FLAG_HAS_MEASUREMENT) && !(fl & CK_FLAG_IS_OUTLIER)) {
+          firstMeas = k;
+          break;
+        }
+      }
+    }
+    for (int k = tip; k >= 0; --k) {
+      const uint32_t fl = (uint32_t)rec.s(k).flags;
+      if ((fl & CK_FLAG_HAS_MEASUREMENT) && !(fl & CK_FLAG_IS_OUTLIER)) {
+        lastMeas = k;
+        break;
+      }
+    }
+    nM = nH = nO = ndf = 0;
+    chi2sum = 0.0;
+  }
+
   CK_D void run(const FitParams& fp, int queuePos, int track, int tip) {
     t = track;
     q = queuePos;
@@ -1970,8 +2003,13 @@ struct Smoother {
 
   CK_D void writeState(const FitParams& fp, int k, const double sm[6], const CV Ps[21],
                        bool filtOverride) {
+    writeStateRec(fp, k, Rec<CV>(fp, q).s(k), sm, Ps, filtOverride);
+  }
+
+  // the outputs of state k from its record `rs` (in global memory, or staged)
+  CK_D void writeStateRec(const FitParams& fp, int k, const RecState<CV>& rs, const double sm[6],
+                          const CV Ps[21], bool filtOverride) {
     const ck_batch_out& out = fp.out;
-    const Rec<CV> rec(fp, q);
     if (fp.ext && (k == firstMeas || k == lastMeas)) {
       // its smoothed parameters (TrackStateProxy::parameters) for the
       // extrapolation; slot 0 first, slot 1 last
@@ -1982,12 +2020,11 @@ struct Smoother {
         for (int i = 0; i < 6; ++i) es.par[i] = sm[i];
 #pragma unroll
         for (int i = 0; i < 21; ++i) es.cov[i] = (double)Ps[i];
-        es.surface = rec.s(k).surface;
+        es.surface = rs.surface;
       }
     }
     const size_t n = (size_t)fp.n_tracks;
     auto at = [&](int C, int c) -> size_t { return ((size_t)k * C + c) * n + t; };
-    const RecState<CV>& rs = rec.s(k);
     const uint32_t fl = (uint32_t)rs.flags & kRecFlagMask;
     const int sub = ((uint32_t)rs.flags >> kRecSubShift) & 3u;
     const double c2 = rs.chi2;
@@ -2027,37 +2064,37 @@ struct Smoother {
     if (out.filtered) {
 #pragma unroll
       for (int i = 0; i < 6; ++i)
-        out.filtered[at(6, i)] = filtOverride ? sm[i] : rec.p(k, kRecFilt + i);
+        out.filtered[at(6, i)] = filtOverride ? sm[i] : rs.par[kRecFilt + i];
       if (packed) {
 #pragma unroll
         for (int i = 0; i < 21; ++i)
-          out.filtered_cov[at(21, i)] = (double)(filtOverride ? Ps[i] : rec.m(k, kRecFiltCov + i));
+          out.filtered_cov[at(21, i)] = (double)(filtOverride ? Ps[i] : rs.mat[kRecFiltCov + i]);
       } else {
 #pragma unroll
         for (int i = 0; i < 6; ++i)
 #pragma unroll
           for (int j = 0; j < 6; ++j)
             out.filtered_cov[at(36, i * 6 + j)] =
-                (double)(filtOverride ? Ps[sidx(i, j)] : rec.m(k, kRecFiltCov + sidx(i, j)));
+                (double)(filtOverride ? Ps[sidx(i, j)] : rs.mat[kRecFiltCov + sidx(i, j)]);
       }
     }
     if (out.predicted) {
 #pragma unroll
-      for (int i = 0; i < 6; ++i) out.predicted[at(6, i)] = rec.p(k, kRecPred + i);
+      for (int i = 0; i < 6; ++i) out.predicted[at(6, i)] = rs.par[kRecPred + i];
       if (packed) {
 #pragma unroll
-        for (int i = 0; i < 21; ++i) out.predicted_cov[at(21, i)] = (double)rec.m(k, kRecPredCov + i);
+        for (int i = 0; i < 21; ++i) out.predicted_cov[at(21, i)] = (double)rs.mat[kRecPredCov + i];
       } else {
 #pragma unroll
         for (int i = 0; i < 6; ++i)
 #pragma unroll
           for (int j = 0; j < 6; ++j)
-            out.predicted_cov[at(36, i * 6 + j)] = (double)rec.m(k, kRecPredCov + sidx(i, j));
+            out.predicted_cov[at(36, i * 6 + j)] = (double)rs.mat[kRecPredCov + sidx(i, j)];
       }
     }
     if (out.jacobian) {
 #pragma unroll
-      for (int i = 0; i < 36; ++i) out.jacobian[at(36, i)] = (double)rec.m(k, kRecJac + i);
+      for (int i = 0; i < 36; ++i) out.jacobian[at(36, i)] = (double)rs.mat[kRecJac + i];
     }
   }
 };
@@ -2363,6 +2400,99 @@ __global__ void __launch_bounds__(BLOCK) reverseOutputKernel(FitParams fp) {
     Smoother<CV> S;
     S.runReverse(fp, q, fp.perm ? __ldg(&fp.perm[q]) : q, tip);
   }
+}
+
+// Smoother kernel with warp-cooperative record staging: one lane per queue
+// position as in smoothKernel, but the state records are read coalesced.
+// Iteration j of a warp smooths state k = tip - j of every lane's track: the
+// 32 records (one per lane, 432 / 744 B each, contiguous) are copied into
+// shared memory by the whole warp in 16 / 8 B chunks, consecutive lanes
+// reading consecutive chunks, so every DRAM sector of a record is fetched
+// once; the previous iteration's records (state k + 1) stay staged in the
+// second buffer. Only the RTS gain-matrix smoother takes this path.
+template <typename CV, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) smoothKernelStaged(FitParams fp) {
+  using R = RecState<CV>;
+  using Chunk = typename std::conditional<sizeof(R) % 16 == 0, uint4, uint2>::type;
+  constexpr int NCH = (int)(sizeof(R) / sizeof(Chunk));
+  static_assert(sizeof(R) % sizeof(Chunk) == 0, "record chunks");
+  extern __shared__ __align__(16) unsigned char smem[];
+  R* buf = reinterpret_cast<R*>(smem);  // [2][BLOCK]
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wbase = threadIdx.x & ~31;
+  const R* recs = static_cast<const R*>(fp.rec);
+  const int ms = fp.max_states;
+  for (int q0 = blockIdx.x * BLOCK; q0 < fp.n_queue; q0 += gridDim.x * BLOCK) {
+    const int q = q0 + threadIdx.x;
+    int tip = q < fp.n_queue ? fp.tip[q] : -1;
+    // (tracks the reverse-filtering logic selects take the reversed pass)
+    if (tip >= 0 && fp.opt.reverseMomThreshold > 0.0 && reverseSelected<CV>(fp, q, tip)) tip = -1;
+    const int iters = __reduce_max_sync(FULL, tip + 1);
+    Smoother<CV> S;
+    double ps[6];
+    CV Psp[21];
+    bool ok = tip >= 0;
+    if (ok) S.begin(fp, q, fp.perm ? __ldg(&fp.perm[q]) : q, tip);
+    for (int j = 0; j < iters; ++j) {
+      // stage state k = tip - j of every lane with such a state
+      const int myK = ok && tip - j >= 0 ? tip - j : -1;
+      R* cur = buf + (size_t)(j & 1) * BLOCK;
+      R* prev = buf + (size_t)((j + 1) & 1) * BLOCK;
+      __syncwarp();
+      for (int i = lane; i < 32 * NCH; i += 32) {
+        const int L = i / NCH, c = i - L * NCH;
+        const int kL = __shfl_sync(FULL, myK, L);  // (every lane takes part)
+        const int qL = q0 + wbase + L;
+        if (kL >= 0) {
+          const Chunk* src = reinterpret_cast<const Chunk*>(recs + (size_t)qL * ms + kL);
+          reinterpret_cast<Chunk*>(cur + wbase + L)[c] = src[c];
+        }
+      }
+      __syncwarp();
+      if (myK < 0) continue;
+      const R& rk = cur[threadIdx.x];
+      if (j == 0) {
+        // the tip's smoothed state is its filtered state
+#pragma unroll
+        for (int i = 0; i < 6; ++i) ps[i] = rk.par[kRecFilt + i];
+#pragma unroll
+        for (int i = 0; i < 21; ++i) Psp[i] = rk.mat[kRecFiltCov + i];
+        S.writeStateRec(fp, myK, rk, ps, Psp, false);
+        if (myK == 0) S.finish(fp, tip);
+        continue;
+      }
+      const R& rn = prev[threadIdx.x];  // state k + 1
+      double filt[6], pp[6], sm[6];
+      CV Pf[21], Ppp[21], J[36], Ps[21];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) filt[i] = rk.par[kRecFilt + i];
+#pragma unroll
+      for (int i = 0; i < 21; ++i) Pf[i] = rk.mat[kRecFiltCov + i];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) pp[i] = rn.par[kRecPred + i];
+#pragma unroll
+      for (int i = 0; i < 21; ++i) Ppp[i] = rn.mat[kRecPredCov + i];
+#pragma unroll
+      for (int i = 0; i < 36; ++i) J[i] = rn.mat[kRecJac + i];
+      if (!smoothStep<CV>(filt, Pf, pp, Ppp, J, ps, Psp, sm, Ps)) {
+        S.failSmooth(fp);
+        ok = false;
+        continue;
+      }
+      S.writeStateRec(fp, myK, rk, sm, Ps, myK == S.lastMeas);
+#pragma unroll
+      for (int i = 0; i < 6; ++i) ps[i] = sm[i];
+#pragma unroll
+      for (int i = 0; i < 21; ++i) Psp[i] = Ps[i];
+      if (myK == 0) S.finish(fp, tip);
+    }
+    __syncwarp();
+  }
+}
+
+template <typename CV, int BLOCK>
+constexpr size_t stagedSmoothSmemBytes() {
+  return 2 * sizeof(RecState<CV>) * BLOCK;
 }
 
 template <typename CV, int BLOCK>

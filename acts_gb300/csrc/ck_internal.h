@@ -157,6 +157,9 @@ struct FitParams {
   // Runge-Kutta trials a STEP item of the compaction kernels may take in one
   // round (>= 1)
   int steps_per_round;
+  // the RTS smoother reads its records through warp-cooperative staging in
+  // shared memory (smoothKernelStaged) instead of per lane
+  int smooth_staged;
   int max_states;
   // outputs (device memory, ck_batch_out layout)
   ck_batch_out out;

@@ -81,7 +81,11 @@ int occupancyFP64(int variant, int tpb) {
 }
 
 cudaError_t configureFP64() {
-  cudaError_t e = cudaFuncSetAttribute(fitKernelPool<double, double, 256, 256, true>,
+  cudaError_t e = cudaFuncSetAttribute(smoothKernelStaged<double, kSmoothBlock>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)stagedSmoothSmemBytes<double, kSmoothBlock>());
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(fitKernelPool<double, double, 256, 256, true>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)poolSmemBytes<double, double, 256, true>());
   if (e != cudaSuccess) return e;
@@ -108,7 +112,11 @@ cudaError_t configureFP64() {
 
 cudaError_t launchSmoothFP64(const FitParams& fp, cudaStream_t st) {
   const int grid = (fp.n_queue + kSmoothBlock - 1) / kSmoothBlock;
-  smoothKernel<double, kSmoothBlock><<<grid, kSmoothBlock, 0, st>>>(fp);
+  if (fp.smooth_staged && fp.opt.smoother == CK_SMOOTHER_GAIN_MATRIX)
+    smoothKernelStaged<double, kSmoothBlock>
+        <<<grid, kSmoothBlock, stagedSmoothSmemBytes<double, kSmoothBlock>(), st>>>(fp);
+  else
+    smoothKernel<double, kSmoothBlock><<<grid, kSmoothBlock, 0, st>>>(fp);
   return cudaGetLastError();
 }
 

@@ -47,7 +47,11 @@ cudaError_t launchFitMixed(const FitParams& fp, int variant, int grid, int block
 }
 
 cudaError_t configureMixed() {
-  cudaError_t e = cudaFuncSetAttribute(fitKernelPool<float, float, 320, 256, true>,
+  cudaError_t e = cudaFuncSetAttribute(smoothKernelStaged<float, kSmoothBlock>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)stagedSmoothSmemBytes<float, kSmoothBlock>());
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(fitKernelPool<float, float, 320, 256, true>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)poolSmemBytes<float, float, 320, true>());
   if (e != cudaSuccess) return e;
@@ -74,7 +78,11 @@ cudaError_t configureMixed() {
 
 cudaError_t launchSmoothMixed(const FitParams& fp, cudaStream_t st) {
   const int grid = (fp.n_queue + kSmoothBlock - 1) / kSmoothBlock;
-  smoothKernel<float, kSmoothBlock><<<grid, kSmoothBlock, 0, st>>>(fp);
+  if (fp.smooth_staged && fp.opt.smoother == CK_SMOOTHER_GAIN_MATRIX)
+    smoothKernelStaged<float, kSmoothBlock>
+        <<<grid, kSmoothBlock, stagedSmoothSmemBytes<float, kSmoothBlock>(), st>>>(fp);
+  else
+    smoothKernel<float, kSmoothBlock><<<grid, kSmoothBlock, 0, st>>>(fp);
   return cudaGetLastError();
 }
 

@@ -20,6 +20,8 @@ constexpr int kDefaultVariant = 3;
 // Runge-Kutta trials per round of the compaction kernels by precision
 // (FP64, mixed): measured best on the barrel and uneven workloads
 constexpr int kDefaultStepsPerRound[2] = {2, 3};
+// the RTS smoother reads its records through warp-cooperative staging
+constexpr int kDefaultSmootherStaged = 0;
 // block size a variant requires (0: any multiple of 32 up to kFitMaxBlock)
 inline int variantBlock(int variant) {
   return (variant == 3 || variant >= 5) ? 256 : (variant == 4 ? 128 : 0);

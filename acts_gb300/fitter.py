@@ -67,6 +67,7 @@ def lib():
         L.ck_sync.argtypes = [C.c_void_p]
         L.ck_set_steps_per_round.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
         L.ck_set_grid_blocks.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+        L.ck_set_smoother_staging.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
         L.ck_set_host_chunk_tracks.argtypes = [C.c_void_p, C.c_int32]
         L.ck_last_kernel_split_ms.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         L.ck_atan2_mixed.argtypes = [C.c_void_p, C.c_int32, P(C.c_double), P(C.c_double),
@@ -310,6 +311,11 @@ class CudaKalman:
 
     def set_steps_per_round(self, precision, steps):
         _check(lib().ck_set_steps_per_round(self._h, int(precision), int(steps)))
+
+    def set_smoother_staging(self, precision, enable):
+        """RTS smoother with warp-cooperative record staging (1) or per-lane
+        record reads (0); identical results."""
+        _check(lib().ck_set_smoother_staging(self._h, int(precision), int(enable)))
 
     def set_grid_blocks(self, precision, blocks):
         """Grid of the forward-filter kernel (0: the whole GPU)."""

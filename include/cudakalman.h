@@ -435,6 +435,11 @@ ck_status ck_last_transfer_bytes(ck_handle* h, int64_t* h2d_bytes,
 ck_status ck_get_launch_config(ck_handle* h, int32_t precision,
                                int32_t* threads_per_block,
                                int32_t* blocks_per_sm);
+/* The RTS smoother kernel of a precision form: 0 reads each state's record
+ * per lane from global memory, 1 stages the records of a warp's 32 tracks in
+ * shared memory with coalesced warp-wide copies first (gain-matrix smoother;
+ * the MbfSmoother always reads per lane). Results are identical. */
+ck_status ck_set_smoother_staging(ck_handle* h, int32_t precision, int32_t enable);
 /* The forward-filter kernel variant of a precision form (see
  * ck_set_launch_config) and its Runge-Kutta trials per scheduling round. */
 ck_status ck_get_launch_variant(ck_handle* h, int32_t precision, int32_t* variant,

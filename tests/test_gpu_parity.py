@@ -206,3 +206,42 @@ def test_mixed_results_independent_of_kernel_variant(n):
         for name in ("state_flags", "smoothed", "smoothed_cov", "filtered", "jacobian"):
             np.testing.assert_array_equal(r.view(name)[valid], ref.view(name)[valid],
                                           err_msg="v%d %s" % (variant, name))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_MIXED],
+                         ids=["fp64", "mixed"])
+@pytest.mark.parametrize("kw", [dict(outlier_chi2_cut=15.0),
+                                dict(outlier_chi2_cut=15.0, reverse_filtering_mom_threshold=1.5,
+                                     early_termination=1)],
+                         ids=["uneven", "uneven_momentum_threshold"])
+def test_staged_smoother_equals_per_lane(precision, kw):
+    """The smoother with warp-cooperative record staging gives the per-lane
+    smoother's results bit for bit (statuses, counts, every output state,
+    the extrapolation to the perigee that starts from smoothed states)."""
+    from acts_gb300 import generate
+    from acts_gb300.fitter import CudaKalman
+
+    det = generate.Detector(abi.CKG_UNEVEN, perigee=True)
+    b = generate.generate(det, 4000, seed=29)
+    opt = abi.default_options(precision=precision, reference_surface=det.perigee, **kw)
+    comps = abi.OUT_ALL | abi.OUT_REFERENCE
+    fit = CudaKalman.for_detector(det)
+    outs = []
+    try:
+        for staged in (0, 1):
+            fit.set_smoother_staging(precision, staged)
+            outs.append(fit.fit_batch(b, opt, max_states=24, components=comps))
+    finally:
+        fit.close()
+    a, s = outs
+    assert (a.status == 0).mean() > 0.5
+    for name in ("status", "n_states", "n_measurements", "n_holes", "n_outliers", "ndf",
+                 "chi2_sum"):
+        np.testing.assert_array_equal(getattr(a, name), getattr(s, name), err_msg=name)
+    valid = np.arange(24)[None, :] < a.n_states[:, None]
+    for name in ("state_flags", "state_chi2", "smoothed", "smoothed_cov", "filtered",
+                 "filtered_cov", "predicted", "jacobian"):
+        np.testing.assert_array_equal(a.view(name)[valid], s.view(name)[valid], err_msg=name)
+    ok = a.status == 0
+    np.testing.assert_array_equal(a.track("track_params")[ok], s.track("track_params")[ok])
