@@ -556,12 +556,12 @@ CK_D void gridConstants(const DevField& F, int i, P& mn, P& width, P& upper) {
   }
 }
 
+// The cell of a point (0-based lower node per axis) and its fractional
+// position in it, with the axis arithmetic of the reference's equidistant
+// Axis; false outside the map's [min, max) range. Every multiply-add is an
+// explicit fma, so that each lookup function evaluates the same roundings.
 template <typename P>
-CK_D bool getGridField(const DevField& F, const P p[3], P B[3]) {
-  // InterpolatedBFieldMap::getField with the equidistant axes of
-  // fieldMapXYZ and the trilinear interpolate (z, then y, then x)
-  int bin[3];
-  P f[3];
+CK_D bool gridCell(const DevField& F, const P p[3], int bin[3], P f[3]) {
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     P mn, width, upper;
@@ -571,10 +571,46 @@ CK_D bool getGridField(const DevField& F, const P p[3], P B[3]) {
     int bb = (int)floor(u);  // 0-based lower node
     bb = max(0, min(bb, F.n[i] - 2));
     bin[i] = bb;
-    P ll = mn + (P)bb * width;
-    P ur = mn + (P)(bb + 1) * width;
+    P ll = fma((P)bb, width, mn);
+    P ur = fma((P)(bb + 1), width, mn);
     f[i] = (p[i] - ll) / (ur - ll);
   }
+  return true;
+}
+
+// (1 - t) a + t b as one rounded product and one fma
+template <typename P>
+CK_D P lerpF(P t, P a, P b) {
+  return fma(t, b, (P(1) - t) * a);
+}
+
+// Interpolation (Interpolation.hpp:96-120): the eight nodes reduced along z,
+// then y, then x; the result converted from Tesla to the internal unit
+template <typename P>
+CK_D void trilinear(const float4 v[8], const P f[3], P B[3]) {
+  P r[4][3];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    r[i][0] = lerpF(f[2], (P)v[2 * i].x, (P)v[2 * i + 1].x);
+    r[i][1] = lerpF(f[2], (P)v[2 * i].y, (P)v[2 * i + 1].y);
+    r[i][2] = lerpF(f[2], (P)v[2 * i].z, (P)v[2 * i + 1].z);
+  }
+  const P unit = (P)0.000299792458;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const P s0 = lerpF(f[1], r[0][c], r[1][c]);
+    const P s1 = lerpF(f[1], r[2][c], r[3][c]);
+    B[c] = lerpF(f[0], s0, s1) * unit;
+  }
+}
+
+template <typename P>
+CK_D bool getGridField(const DevField& F, const P p[3], P B[3]) {
+  // InterpolatedBFieldMap::getField with the equidistant axes of
+  // fieldMapXYZ and the trilinear interpolate (z, then y, then x)
+  int bin[3];
+  P f[3];
+  if (!gridCell(F, p, bin, f)) return false;
   const size_t nz = F.n[2], nyz = (size_t)F.n[1] * F.n[2];
   const size_t base = bin[0] * nyz + bin[1] * nz + bin[2];
   float4 v[8];
@@ -585,22 +621,7 @@ CK_D bool getGridField(const DevField& F, const P p[3], P B[3]) {
 #pragma unroll
       for (int cz = 0; cz < 2; ++cz)
         v[cx * 4 + cy * 2 + cz] = __ldg(&F.nodes[base + cx * nyz + cy * nz + cz]);
-  P r[4][3];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    r[i][0] = (P(1) - f[2]) * (P)v[2 * i].x + f[2] * (P)v[2 * i + 1].x;
-    r[i][1] = (P(1) - f[2]) * (P)v[2 * i].y + f[2] * (P)v[2 * i + 1].y;
-    r[i][2] = (P(1) - f[2]) * (P)v[2 * i].z + f[2] * (P)v[2 * i + 1].z;
-  }
-  P s0[3], s1[3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    s0[c] = (P(1) - f[1]) * r[0][c] + f[1] * r[1][c];
-    s1[c] = (P(1) - f[1]) * r[2][c] + f[1] * r[3][c];
-  }
-  const P unit = (P)0.000299792458;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) B[c] = ((P(1) - f[0]) * s0[c] + f[0] * s1[c]) * unit;
+  trilinear(v, f, B);
   return true;
 }
 
@@ -622,19 +643,7 @@ template <typename P>
 CK_D bool getGridFieldCached(const DevField& F, const P p[3], P B[3], CellCache* cell) {
   int bin[3];
   P f[3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    P mn, width, upper;
-    gridConstants(F, i, mn, width, upper);
-    if (p[i] < mn || p[i] >= upper) return false;
-    P u = (p[i] - mn) / width;
-    int bb = (int)floor(u);
-    bb = max(0, min(bb, F.n[i] - 2));
-    bin[i] = bb;
-    P ll = mn + (P)bb * width;
-    P ur = mn + (P)(bb + 1) * width;
-    f[i] = (p[i] - ll) / (ur - ll);
-  }
+  if (!gridCell(F, p, bin, f)) return false;
   const size_t nz = F.n[2], nyz = (size_t)F.n[1] * F.n[2];
   const size_t base = bin[0] * nyz + bin[1] * nz + bin[2];
   const int key = (int)base;
@@ -654,22 +663,7 @@ CK_D bool getGridFieldCached(const DevField& F, const P p[3], P B[3], CellCache*
     for (int c = 0; c < 8; ++c) cell->v[c] = v[c];
     cell->key = key;
   }
-  P r[4][3];
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    r[i][0] = (P(1) - f[2]) * (P)v[2 * i].x + f[2] * (P)v[2 * i + 1].x;
-    r[i][1] = (P(1) - f[2]) * (P)v[2 * i].y + f[2] * (P)v[2 * i + 1].y;
-    r[i][2] = (P(1) - f[2]) * (P)v[2 * i].z + f[2] * (P)v[2 * i + 1].z;
-  }
-  P s0[3], s1[3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    s0[c] = (P(1) - f[1]) * r[0][c] + f[1] * r[1][c];
-    s1[c] = (P(1) - f[1]) * r[2][c] + f[1] * r[3][c];
-  }
-  const P unit = (P)0.000299792458;
-#pragma unroll
-  for (int c = 0; c < 3; ++c) B[c] = ((P(1) - f[0]) * s0[c] + f[0] * s1[c]) * unit;
+  trilinear(v, f, B);
   return true;
 }
 

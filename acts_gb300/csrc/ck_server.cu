@@ -600,7 +600,7 @@ ck_status ck_server_create(ck_handle* h, const ck_options* opt, const ck_server_
       return st;
     }
   }
-  s->copyThreads = (int)std::max(1u, std::min(8u, std::thread::hardware_concurrency() / 2));
+  s->copyThreads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
   s->worker = std::thread(workerLoop, s.get());
   s->delivery = std::thread(deliveryLoop, s.get());
   *out = s.release();

@@ -60,6 +60,14 @@ class Results:
             setattr(o, name, abi.ptr(getattr(self, name), C.c_double))
         return o
 
+    def as_batch_out_view(self, m):
+        """A ck_batch_out for m <= n tracks over the start of these arrays
+        (the SoA layout of m tracks: element c of state k of track t at
+        [(k * C + c) * m + t]), for reusing one buffer across events."""
+        o = self.as_batch_out()
+        assert m <= self.n
+        return o
+
     def track(self, name):
         """Per-track array `name` (track_params / track_cov) as [n, C]."""
         a = getattr(self, name)
