@@ -559,7 +559,7 @@ CK_D void gridConstants(const DevField& F, int i, P& mn, P& width, P& upper) {
 // The cell of a point (0-based lower node per axis) and its fractional
 // position in it, with the axis arithmetic of the reference's equidistant
 // Axis; false outside the map's [min, max) range. Every multiply-add is an
-// explicit fma, so that each lookup function evaluates the same roundings.
+// explicit fma, so that the roundings do not depend on the inlining context.
 template <typename P>
 CK_D bool gridCell(const DevField& F, const P p[3], int bin[3], P f[3]) {
 #pragma unroll
@@ -623,54 +623,6 @@ CK_D bool getGridField(const DevField& F, const P p[3], P B[3]) {
         v[cx * 4 + cy * 2 + cz] = __ldg(&F.nodes[base + cx * nyz + cy * nz + cz]);
   trilinear(v, f, B);
   return true;
-}
-
-// The field cell last used by a track slot, in shared memory: the eight
-// grid nodes of the cell and its linear index (-1: none). A lookup in the
-// same cell takes the nodes from here instead of gathering them from L2/HBM
-// again (the reference's InterpolatedBFieldMap cell cache,
-// InterpolatedBFieldMap.hpp:238-264; on the uneven workload 56-62 % of the
-// lookups fall in the cell of the lookup before). The cell is identified by
-// the bin indices the lookup computes, so a cached lookup evaluates exactly
-// the expressions of an uncached one.
-struct CellCache {
-  float4 v[8];
-  int key;
-  int pad[3];
-};
-
-template <typename P>
-CK_D bool getGridFieldCached(const DevField& F, const P p[3], P B[3], CellCache* cell) {
-  int bin[3];
-  P f[3];
-  if (!gridCell(F, p, bin, f)) return false;
-  const size_t nz = F.n[2], nyz = (size_t)F.n[1] * F.n[2];
-  const size_t base = bin[0] * nyz + bin[1] * nz + bin[2];
-  const int key = (int)base;
-  float4 v[8];
-  if (cell->key == key) {
-#pragma unroll
-    for (int c = 0; c < 8; ++c) v[c] = cell->v[c];
-  } else {
-#pragma unroll
-    for (int cx = 0; cx < 2; ++cx)
-#pragma unroll
-      for (int cy = 0; cy < 2; ++cy)
-#pragma unroll
-        for (int cz = 0; cz < 2; ++cz)
-          v[cx * 4 + cy * 2 + cz] = __ldg(&F.nodes[base + cx * nyz + cy * nz + cz]);
-#pragma unroll
-    for (int c = 0; c < 8; ++c) cell->v[c] = v[c];
-    cell->key = key;
-  }
-  trilinear(v, f, B);
-  return true;
-}
-
-template <typename P>
-CK_D bool getFieldCached(const DevField& F, const P p[3], P B[3], CellCache* cell) {
-  if (F.kind == CK_FIELD_CONSTANT) return getField(F, p, B);
-  return getGridFieldCached(F, p, B, cell);
 }
 
 // --------------------------------------------------------------- material

@@ -121,22 +121,8 @@ CK_D bool reverseSelected(const FitParams& fp, int q, int tip) {
 // it writes no records, only its latest filtered measurement state (the
 // extrapolation start slot 0) and, when it reaches the reference surface,
 // the track parameters there.
-// The shared-memory field cell of a lane's slot (kernels that stage the
-// field grid); empty for the others
-template <bool CELL>
-struct CellSlot {
-  CK_D CellCache* cellPtr() const { return nullptr; }
-};
-template <>
-struct CellSlot<true> {
-  CellCache* cell;
-  CK_D CellCache* cellPtr() const { return cell; }
-};
-
-// CELL: the field lookups of the Runge-Kutta stages go through the slot's
-// shared-memory cell cache (getFieldCached)
-template <typename P, typename CV, bool F2B = false, bool REV = false, bool CELL = false>
-struct Lane : CellSlot<CELL> {
+template <typename P, typename CV, bool F2B = false, bool REV = false>
+struct Lane {
   // ---- identity: track index and queue position (which indexes the records)
   int phase;
   int t;
@@ -1106,10 +1092,7 @@ struct Lane : CellSlot<CELL> {
 
   // the field at a Runge-Kutta stage point
   CK_D bool stageField(const FitParams& fp, const P p[3], P B[3]) const {
-    if constexpr (CELL)
-      return getFieldCached(fp.field, p, B, this->cellPtr());
-    else
-      return getField(fp.field, p, B);
+    return getField(fp.field, p, B);
   }
 
   // STEP: one Runge-Kutta trial (EigenStepper::step, EigenStepper.ipp:168-388)
@@ -2157,8 +2140,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) fitKernel(FitParams fp) {
 // carries are the FP64 throughput it gets.
 // One phase step of a slot; fetching threads take one ticket per warp (the
 // threads of the warp that run this call together).
-template <typename P, typename CV, bool F2B, bool REV, bool CELL>
-__device__ __forceinline__ void advanceSlot(const FitParams& fp, Lane<P, CV, F2B, REV, CELL>& L,
+template <typename P, typename CV, bool F2B, bool REV>
+__device__ __forceinline__ void advanceSlot(const FitParams& fp, Lane<P, CV, F2B, REV>& L,
                                             int c, int lane, int spr) {
   if (c == PH_FETCH) {
     const unsigned act = __activemask();
@@ -2270,14 +2253,12 @@ constexpr size_t compactSmemBytes() {
 // block-wide round. A warp leaves when all pools are empty: slots still in
 // flight belong to warps that are running and that claim them again after
 // returning them, so every slot is finished, and nothing spins.
-// CELL: each slot also holds its field cell in shared memory (after the
-// lanes), the grid-field workloads' variant.
-template <typename P, typename CV, int S, int T, bool CELL = false>
+template <typename P, typename CV, int S, int T>
 __global__ void __launch_bounds__(T, 1) fitKernelPool(FitParams fp) {
   static_assert(S % 32 == 0 && S / 32 <= 32 && T % 32 == 0, "pool shape");
   constexpr int W = S / 32;  // mask words per phase
   extern __shared__ __align__(16) unsigned char smem[];
-  using LaneT = Lane<P, CV, false, false, CELL>;
+  using LaneT = Lane<P, CV>;
   LaneT* st = reinterpret_cast<LaneT*>(smem);
   __shared__ unsigned pool[3][W];
   __shared__ int items[T / 32][32];
@@ -2291,12 +2272,6 @@ __global__ void __launch_bounds__(T, 1) fitKernelPool(FitParams fp) {
     st[sl].phase = sl < active ? PH_FETCH : PH_DONE;
     st[sl].t = -1;
     st[sl].q = -1;
-    if constexpr (CELL) {
-      constexpr size_t off = (sizeof(LaneT) * S + 15) & ~(size_t)15;
-      CellCache* cells = reinterpret_cast<CellCache*>(smem + off);
-      cells[sl].key = -1;
-      st[sl].cell = cells + sl;
-    }
   }
   if (tid < W) {
     const int lo = tid * 32;
@@ -2381,10 +2356,9 @@ __global__ void __launch_bounds__(T, 1) fitKernelPool(FitParams fp) {
   }
 }
 
-template <typename P, typename CV, int S, bool CELL = false>
+template <typename P, typename CV, int S>
 constexpr size_t poolSmemBytes() {
-  return ((sizeof(Lane<P, CV, false, false, CELL>) * S + 15) & ~(size_t)15) +
-         (CELL ? sizeof(CellCache) * S : 0);
+  return sizeof(Lane<P, CV>) * S;
 }
 
 // Smoother kernel: one lane per queue position; lanes of a warp hold tracks

@@ -34,9 +34,6 @@ cudaError_t launchFitFP64(const FitParams& fp, int variant, int grid, int block,
     case 6:
       fitKernelPool<double, double, 256, 256><<<grid, 256, poolSmemBytes<double, double, 256>(), st>>>(fp);
       break;
-    case 7:
-      fitKernelPool<double, double, 256, 256, true><<<grid, 256, poolSmemBytes<double, double, 256, true>(), st>>>(fp);
-      break;
     default:
       fitKernelCompact<double, double, 128><<<grid, 128, compactSmemBytes<double, double, 128>(), st>>>(fp);
       break;
@@ -68,10 +65,6 @@ int occupancyFP64(int variant, int tpb) {
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelPool<double, double, 256, 256>, 256,
                                                     poolSmemBytes<double, double, 256>());
       break;
-    case 7:
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelPool<double, double, 256, 256, true>, 256,
-                                                    poolSmemBytes<double, double, 256, true>());
-      break;
     default:
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelCompact<double, double, 128>, 128,
                                                     compactSmemBytes<double, double, 128>());
@@ -84,10 +77,6 @@ cudaError_t configureFP64() {
   cudaError_t e = cudaFuncSetAttribute(smoothKernelStaged<double, kSmoothBlock>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)stagedSmoothSmemBytes<double, kSmoothBlock>());
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(fitKernelPool<double, double, 256, 256, true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)poolSmemBytes<double, double, 256, true>());
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(fitKernelPool<double, double, 320, 256>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,

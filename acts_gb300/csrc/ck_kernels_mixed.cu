@@ -36,9 +36,6 @@ cudaError_t launchFitMixed(const FitParams& fp, int variant, int grid, int block
     case 6:
       fitKernelPool<float, float, 448, 256><<<grid, 256, poolSmemBytes<float, float, 448>(), st>>>(fp);
       break;
-    case 7:
-      fitKernelPool<float, float, 320, 256, true><<<grid, 256, poolSmemBytes<float, float, 320, true>(), st>>>(fp);
-      break;
     default:
       fitKernelCompact<float, float, 128><<<grid, 128, compactSmemBytes<float, float, 128>(), st>>>(fp);
       break;
@@ -50,10 +47,6 @@ cudaError_t configureMixed() {
   cudaError_t e = cudaFuncSetAttribute(smoothKernelStaged<float, kSmoothBlock>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)stagedSmoothSmemBytes<float, kSmoothBlock>());
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(fitKernelPool<float, float, 320, 256, true>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)poolSmemBytes<float, float, 320, true>());
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(fitKernelPool<float, float, 384, 256>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -109,10 +102,6 @@ int occupancyMixed(int variant, int tpb) {
     case 6:
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelPool<float, float, 448, 256>, 256,
                                                     poolSmemBytes<float, float, 448>());
-      break;
-    case 7:
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelPool<float, float, 320, 256, true>, 256,
-                                                    poolSmemBytes<float, float, 320, true>());
       break;
     default:
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fitKernelCompact<float, float, 128>, 128,

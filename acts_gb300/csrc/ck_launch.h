@@ -11,10 +11,8 @@ namespace ck {
 // register caps of 255 / 168 / 128 (1 / 3 / 4 resident 128-thread blocks);
 // 3-4 block-level phase compaction with 256 / 128 slots per block; 5-6
 // warp-autonomous phase pools, 256 threads with more slots (5: 384 mixed /
-// 320 FP64; 6: 448 mixed / 256 FP64); 7 phase pools whose slots also keep
-// their field cell in shared memory (320 mixed / 256 FP64 slots; the grid
-// field workloads).
-constexpr int kNumFitVariants = 8;
+// 320 FP64; 6: 448 mixed / 256 FP64).
+constexpr int kNumFitVariants = 7;
 constexpr int kFitMaxBlock = 128;
 constexpr int kDefaultVariant = 3;
 // Runge-Kutta trials per round of the compaction kernels by precision

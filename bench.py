@@ -289,16 +289,14 @@ _VARIANT_KERNELS = {
               2: "fitKernel<float, float, 128, 4>",
               3: "fitKernelCompact<float, float, 256, false, false>",
               4: "fitKernelCompact<float, float, 128, false, false>",
-              5: "fitKernelPool<float, float, 384, 256, false>",
-              6: "fitKernelPool<float, float, 448, 256, false>",
-              7: "fitKernelPool<float, float, 320, 256, true>"},
+              5: "fitKernelPool<float, float, 384, 256>",
+              6: "fitKernelPool<float, float, 448, 256>"},
     "double": {0: "fitKernel<double, double, 128, 1>", 1: "fitKernel<double, double, 128, 3>",
                2: "fitKernel<double, double, 128, 4>",
                3: "fitKernelCompact<double, double, 256, false, false>",
                4: "fitKernelCompact<double, double, 128, false, false>",
-               5: "fitKernelPool<double, double, 320, 256, false>",
-               6: "fitKernelPool<double, double, 256, 256, false>",
-               7: "fitKernelPool<double, double, 256, 256, true>"}}
+               5: "fitKernelPool<double, double, 320, 256>",
+               6: "fitKernelPool<double, double, 256, 256>"}}
 COUNTERS = os.path.join(ROOT, "profiles", "fit_kernel_counters.txt")
 
 
@@ -314,9 +312,14 @@ def kernel_counters(scalar, variant):
     if src != profile_counters.source_hash():
         return None, "counters captured from other kernel sources (%s)" % src
     for ln in lines:
-        if name and name in ln["kernel"]:
+        if name and _kernel_key(name) in _kernel_key(ln["kernel"]):
             return ln, name
     return None, "no capture of %s" % name
+
+
+def _kernel_key(name):
+    """A kernel name as ncu may print it: template booleans as 0/1, no spaces."""
+    return name.replace("false", "0").replace("true", "1").replace(" ", "")
 
 
 def best_of_tune_log(log):

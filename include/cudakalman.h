@@ -448,9 +448,9 @@ ck_status ck_get_launch_variant(ck_handle* h, int32_t precision, int32_t* varian
 /* Pins the launch shape of the forward-filter kernel: variant (0-2
  * per-warp phase scheduling with register caps of 255 / 168 / 128 per
  * thread and any multiple of 32 up to 128 threads per block; 3 and 4
- * block-level phase compaction with 256 and 128 threads per block; 5-7
+ * block-level phase compaction with 256 and 128 threads per block; 5-6
  * warp-autonomous phase pools with 256 threads per block and more track
- * slots than threads, 7 with each slot's field cell in shared memory),
+ * slots than threads),
  * threads per block and resident blocks per SM. */
 ck_status ck_set_launch_config(ck_handle* h, int32_t precision, int32_t variant,
                                int32_t threads_per_block, int32_t blocks_per_sm);

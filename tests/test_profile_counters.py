@@ -28,7 +28,7 @@ def _csv(tmp_path):
             "sm__warps_active.avg.pct_of_peak_sustained_active": "12.5"}
     q = lambda xs: ",".join('"%s"' % x for x in xs)
     rows = [q(cols), q(units),
-            q(["0", "void ck::fitKernelPool<float, float, 384, 256, false>(ck::FitParams)"] +
+            q(["0", "void ck::fitKernelPool<float, float, 384, 256>(ck::FitParams)"] +
               [vals[m] for m in pc.METRICS]),
             q(["1", "void ck::smoothKernel<float, 128>(ck::FitParams)"] +
               [vals[m] for m in pc.METRICS])]
@@ -48,7 +48,7 @@ def test_counters_round_trip(tmp_path):
     assert src == pc.source_hash()
     assert len(lines) == 1  # the smoother is not a forward filter
     ln = lines[0]
-    assert "fitKernelPool<float, float, 384, 256, false>" in ln["kernel"]
+    assert "fitKernelPool<float, float, 384, 256>" in ln["kernel"]
     assert ln["fp64_flops"] == (2 * 1000 + 500 + 250) / 10
     assert ln["fp32_flops"] == (2 * 4000 + 10 + 20) / 10
     assert ln["dram_bytes"] == 4000000 / 10
@@ -65,3 +65,25 @@ def test_bench_names_every_variant():
     n = int(text.split("constexpr int kNumFitVariants = ")[1].split(";")[0])
     for scalar in ("float", "double"):
         assert sorted(bench._VARIANT_KERNELS[scalar]) == list(range(n))
+
+
+def test_bench_matches_ncu_kernel_names(tmp_path, monkeypatch):
+    """ncu prints template booleans as 0/1: the bench finds the launched
+    variant's line either way, and only while the source hash matches."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    out = tmp_path / "counters.txt"
+    out.write_text("source %s\n"
+                   "kernel=void fitKernelCompact<float, float, 256, 0, 0>(FitParams) | "
+                   "fp64_flops=8722.0 fp32_flops=33411.7 dram_bytes=6058.6 conversions=1655.8 "
+                   "fp64_pipe_busy=0.574 warps_active=0.125 duration_ms=12.900\n"
+                   % pc.source_hash())
+    monkeypatch.setattr(bench, "COUNTERS", str(out))
+    ln, name = bench.kernel_counters("float", 3)
+    assert ln is not None and ln["fp64_flops"] == 8722.0, name
+    ln, why = bench.kernel_counters("double", 3)
+    assert ln is None and "no capture" in why
+    out.write_text(out.read_text().replace(pc.source_hash(), "0" * 16))
+    ln, why = bench.kernel_counters("float", 3)
+    assert ln is None and "other kernel sources" in why
