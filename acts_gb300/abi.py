@@ -38,7 +38,13 @@ TRACK_STATUS = {
     15: "InconsistentTrackStates",
 }
 
+TRACK_OK = 0
+TRACK_UPDATE_FAILED = 1
+TRACK_STEP_COUNT_LIMIT = 4
+TRACK_NOT_ON_SURFACE = 8
 TRACK_FIELD_OUT_OF_BOUNDS = 9
+TRACK_TOO_MANY_STATES = 10
+TRACK_INVALID_INPUT = 12
 TRACK_INCONSISTENT_STATES = 15
 
 FLAG_HAS_MEASUREMENT = 1 << 0
@@ -286,6 +292,173 @@ class Propagation:
             setattr(o, name, ptr(getattr(self, name), C.c_double))
         o.steps = ptr(self.steps, C.c_int32)
         return o
+
+
+class ck_ckf_options(C.Structure):
+    _fields_ = [
+        ("chi2_cut", C.c_double),
+        ("chi2_cut_outlier", C.c_double),
+        ("max_candidates", C.c_int32),
+        ("min_measurements", C.c_int32),
+        ("max_holes", C.c_int32),
+        ("max_outliers", C.c_int32),
+        ("max_holes_and_outliers", C.c_int32),
+        ("target_surface", C.c_int32),
+        ("max_states", C.c_int32),
+        ("max_tracks", C.c_int32),
+        ("max_branches", C.c_int32),
+        ("end_of_world", C.c_int32),
+    ]
+
+
+INT32_MAX = 2147483647
+
+
+def ckf_options(**kw):
+    """ck_ckf_options with ck_ckf_options_default's values, then `kw`."""
+    o = ck_ckf_options()
+    o.chi2_cut = 15.0
+    o.chi2_cut_outlier = float("inf")
+    o.max_candidates = 1
+    o.min_measurements = 0
+    o.max_holes = INT32_MAX
+    o.max_outliers = INT32_MAX
+    o.max_holes_and_outliers = INT32_MAX
+    o.target_surface = -1
+    o.max_states = 64
+    o.max_tracks = 16
+    o.max_branches = 16
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise AttributeError(k)
+        setattr(o, k, v)
+    return o
+
+
+class ck_ckf_in(C.Structure):
+    _fields_ = [
+        ("n_seeds", C.c_int32),
+        ("memory", C.c_int32),
+        ("seq_offsets", P_i32),
+        ("seq_surfaces", P_i32),
+        ("start_params", P_f64),
+        ("start_cov", P_f64),
+        ("start_frames", P_f64),
+        ("particle", P_f32),
+        ("particle_pdg", P_i32),
+        ("n_meas", C.c_int32),
+        ("n_surfaces", C.c_int32),
+        ("surf_meas_offsets", P_i32),
+        ("meas_values", P_f64),
+        ("meas_cov", P_f64),
+        ("meas_subspace", P_i32),
+    ]
+
+
+CKF_OUT_INT = ("status", "n_tracks", "n_states")
+CKF_TRACK_FIELDS = (("track_tip", np.int32, 1), ("track_n_measurements", np.int32, 1),
+                    ("track_n_holes", np.int32, 1), ("track_n_outliers", np.int32, 1),
+                    ("track_ndf", np.int32, 1), ("track_chi2", np.float64, 1),
+                    ("track_params", np.float64, 6), ("track_cov", np.float64, 21))
+CKF_STATE_FIELDS = (("state_prev", np.int32, 1), ("state_surface", np.int32, 1),
+                    ("state_flags", np.uint32, 1), ("state_measurement", np.int32, 1),
+                    ("state_chi2", np.float64, 1), ("state_path_length", np.float64, 1),
+                    ("predicted", np.float64, 6), ("predicted_cov", np.float64, 21),
+                    ("filtered", np.float64, 6), ("filtered_cov", np.float64, 21),
+                    ("jacobian", np.float64, 36))
+_CTYPE = {np.int32: C.c_int32, np.uint32: C.c_uint32, np.float64: C.c_double}
+
+
+class ck_ckf_out(C.Structure):
+    _fields_ = ([(name, P_i32) for name in CKF_OUT_INT] +
+                [(name, C.POINTER(_CTYPE[t])) for name, t, _ in CKF_TRACK_FIELDS] +
+                [(name, C.POINTER(_CTYPE[t])) for name, t, _ in CKF_STATE_FIELDS])
+
+
+class TrackFinding:
+    """Host arrays of one track-finding call (ck_find_tracks's layout): the
+    seeds with their surface sequences, the event's measurements grouped by
+    surface, and the found tracks and track states per seed."""
+
+    def __init__(self, seq_offsets, seq_surfaces, start_params, start_cov, start_frames,
+                 particle, surf_meas_offsets, meas_values, meas_cov, meas_subspace=None,
+                 particle_pdg=None, max_states=64, max_tracks=16):
+        i32 = lambda x: np.ascontiguousarray(x, np.int32)
+        f64 = lambda x: np.ascontiguousarray(x, np.float64)
+        self.seq_offsets = i32(seq_offsets)
+        self.n = len(self.seq_offsets) - 1
+        self.seq_surfaces = i32(seq_surfaces)
+        self.start_params = f64(start_params).reshape(self.n, 6)
+        self.start_cov = f64(start_cov).reshape(self.n, 36)
+        self.start_frames = f64(start_frames).reshape(self.n, 12)
+        self.particle = np.ascontiguousarray(particle, np.float32).reshape(self.n, 2)
+        self.particle_pdg = None if particle_pdg is None else i32(particle_pdg)
+        self.surf_meas_offsets = i32(surf_meas_offsets)
+        self.n_surfaces = len(self.surf_meas_offsets) - 1
+        self.meas_values = f64(meas_values).reshape(-1, 2)
+        self.n_meas = len(self.meas_values)
+        self.meas_cov = f64(meas_cov).reshape(self.n_meas, 4)
+        self.meas_subspace = None if meas_subspace is None else i32(meas_subspace)
+        self.max_states = max_states
+        self.max_tracks = max_tracks
+        n = self.n
+        for name in CKF_OUT_INT:
+            setattr(self, name, np.zeros(n, np.int32))
+        self.status[:] = 11
+        for name, t, c in CKF_TRACK_FIELDS:
+            setattr(self, name, np.zeros((n, max_tracks) + ((c,) if c > 1 else ()), t))
+        for name, t, c in CKF_STATE_FIELDS:
+            setattr(self, name, np.zeros((n, max_states) + ((c,) if c > 1 else ()), t))
+
+    def options(self, **kw):
+        """ck_ckf_options with this container's capacities."""
+        kw.setdefault("max_states", self.max_states)
+        kw.setdefault("max_tracks", self.max_tracks)
+        if kw["max_states"] > self.max_states or kw["max_tracks"] > self.max_tracks:
+            raise ValueError("capacities above the container's")
+        return ckf_options(**kw)
+
+    def as_in(self):
+        i = ck_ckf_in()
+        i.n_seeds = self.n
+        i.memory = MEM_HOST
+        i.seq_offsets = ptr(self.seq_offsets, C.c_int32)
+        i.seq_surfaces = ptr(self.seq_surfaces, C.c_int32)
+        i.start_params = ptr(self.start_params, C.c_double)
+        i.start_cov = ptr(self.start_cov, C.c_double)
+        i.start_frames = ptr(self.start_frames, C.c_double)
+        i.particle = ptr(self.particle, C.c_float)
+        i.particle_pdg = ptr(self.particle_pdg, C.c_int32)
+        i.n_meas = self.n_meas
+        i.n_surfaces = self.n_surfaces
+        i.surf_meas_offsets = ptr(self.surf_meas_offsets, C.c_int32)
+        i.meas_values = ptr(self.meas_values, C.c_double)
+        i.meas_cov = ptr(self.meas_cov, C.c_double)
+        i.meas_subspace = ptr(self.meas_subspace, C.c_int32)
+        return i
+
+    def as_out(self):
+        o = ck_ckf_out()
+        for name in CKF_OUT_INT:
+            setattr(o, name, ptr(getattr(self, name), C.c_int32))
+        for name, t, _ in CKF_TRACK_FIELDS + CKF_STATE_FIELDS:
+            setattr(o, name, ptr(getattr(self, name), _CTYPE[t]))
+        return o
+
+    def track_states(self, s, k):
+        """State indices of found track k of seed s, first to last."""
+        out = []
+        i = int(self.track_tip[s, k])
+        while i >= 0:
+            out.append(i)
+            i = int(self.state_prev[s, i])
+        return out[::-1]
+
+    def track_measurements(self, s, k):
+        """Measurement indices of the measurement states (outliers included)
+        of found track k of seed s, first to last."""
+        return [int(self.state_measurement[s, i]) for i in self.track_states(s, k)
+                if self.state_flags[s, i] & FLAG_HAS_MEASUREMENT]
 
 
 class ck_server_config(C.Structure):

@@ -30,7 +30,7 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 # translation units of libcudakalman.so
 CUDA_SOURCES = ["ck_kernels_fp64.cu", "ck_kernels_mixed.cu", "ck_units.cu", "ck_api.cu", "ck_static.cu",
                 "ck_server.cu", "ck_extrapolate.cu", "ck_reverse_fp64.cu", "ck_reverse_mixed.cu",
-                "ck_propagate.cu"]
+                "ck_propagate.cu", "ck_ckf.cu"]
 CUDA_HEADERS = ["ck_device.cuh", "ck_fitter.cuh", "ck_internal.h", "ck_api_internal.h", "ck_launch.h"]
 
 

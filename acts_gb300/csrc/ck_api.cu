@@ -509,7 +509,8 @@ void ck_abi_struct_sizes(int64_t* out, int32_t n) {
                        (int64_t)sizeof(ck_options),   (int64_t)sizeof(ck_config),
                        (int64_t)sizeof(ck_batch_in),  (int64_t)sizeof(ck_batch_out),
                        (int64_t)sizeof(ck_server_config), (int64_t)sizeof(ck_propagate_in),
-                       (int64_t)sizeof(ck_propagate_out)};
+                       (int64_t)sizeof(ck_propagate_out), (int64_t)sizeof(ck_ckf_options),
+                       (int64_t)sizeof(ck_ckf_in),        (int64_t)sizeof(ck_ckf_out)};
   for (int i = 0; i < n && i < (int)(sizeof(s) / sizeof(s[0])); ++i) out[i] = s[i];
 }
 

@@ -1,0 +1,765 @@
+// ck_ckf.cu — ck_find_tracks: combinatorial Kalman filter track finding
+// from seeds, the GPU counterpart of
+//   CombinatorialKalmanFilter<Propagator<EigenStepper<>, DirectNavigator>,
+//       TrackContainer>::findTracks(initialParameters, options, tracks)
+//   (Core/include/Acts/TrackFinding/CombinatorialKalmanFilter.hpp:1191-1335)
+// with the default TrackStateCreator / MeasurementSelector and the examples'
+// branch stopper (Examples/Algorithms/TrackFinding/src/
+// TrackFindingAlgorithm.cpp:203-261).
+//
+// One thread per seed runs the whole depth-first search: the fitter's own
+// stepper, navigator, covariance transport, material and Kalman update (the
+// Lane of ck_fitter.cuh, its step in the kStepCkf mode) under the CKF actor
+// below. The seed's track states go straight into the output arrays (the
+// reset to a branch reads its outermost state back from there); the stack
+// of active branches lives in device scratch. Every loop is bounded: the
+// accepted steps of all branches of a seed by maxSteps (the propagator's
+// step counter is shared, as in the reference), the Runge-Kutta trials of a
+// step by maxRungeKuttaStepTrials, the candidates by the surface's
+// measurements, the states, tracks and branches by their capacities.
+#include <cuda_runtime.h>
+#include <math_constants.h>
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "ck_api_internal.h"
+#include "ck_fitter.cuh"
+
+using namespace ck;
+
+namespace {
+
+constexpr int kCkfBlock = 64;
+constexpr int kCkfMaxCandidates = 16;
+
+// A branch (the reference's TrackProxy of an active branch): its tip state
+// and summary counters
+struct CkfBranch {
+  int tip, nMeas, nHoles, nOutliers, ndf, pad;
+  double chi2;
+};
+
+struct CkfParams {
+  ck_ckf_options o;
+  // the target's bounds (0: unbounded): rectangle half lengths of a plane,
+  // the half length in z of a cylinder
+  double targetHalfX, targetHalfY, targetHalfZ;
+  const int32_t* surf_meas_off;  // [n_surfaces + 1]
+  ck_ckf_out out;                // device pointers
+  CkfBranch* branches;           // [n_seeds * max_branches]
+};
+
+template <typename P, typename CV>
+struct CkfLane : Lane<P, CV> {
+  using B = Lane<P, CV>;
+  using B::absQ;
+  using B::cAcc;
+  using B::cActor;
+  using B::cNav;
+  using B::coasting;
+  using B::cov;
+  using B::cUser;
+  using B::currentSurface;
+  using B::deriv;
+  using B::dirSign;
+  using B::extrapolating;
+  using B::finished;
+  using B::haveTarget;
+  using B::mass;
+  using B::navigationBreak;
+  using B::nSeq;
+  using B::pathAcc;
+  using B::pdg;
+  using B::phase;
+  using B::seq0;
+  using B::stepStarted;
+  using B::steps;
+  using B::surfaceIndex;
+  using B::targetIdx;
+  using B::targetSurf;
+
+  int nStatesC, nTracksC, nActive;
+  int ckfStart;  // the surface the current branch restarted from (-1: the seed's plane)
+  double pathLimit;
+  bool pathLimitSet, done;
+
+  CK_D CkfBranch* stack(const CkfParams& cp) const {
+    return cp.branches + (size_t)this->t * cp.o.max_branches;
+  }
+  CK_D size_t stateIdx(const CkfParams& cp, int k) const {
+    return (size_t)this->t * cp.o.max_states + k;
+  }
+
+  // ------------------------------------------------------------ outputs
+  CK_D void writeState(const CkfParams& cp, int k, int sid, int prev, int meas, uint32_t flags,
+                       double chi2, const double pred[6], const CV Cp[21], const CV J[36]) const {
+    const ck_ckf_out& o = cp.out;
+    const size_t i = stateIdx(cp, k);
+    o.state_prev[i] = prev;
+    o.state_surface[i] = sid;
+    o.state_flags[i] = flags;
+    if (o.state_measurement) o.state_measurement[i] = meas;
+    if (o.state_chi2) o.state_chi2[i] = chi2;
+    if (o.state_path_length) o.state_path_length[i] = pathAcc;
+    if (o.predicted)
+      for (int c = 0; c < 6; ++c) o.predicted[i * 6 + c] = pred[c];
+    if (o.predicted_cov)
+      for (int c = 0; c < 21; ++c) o.predicted_cov[i * 21 + c] = (double)Cp[c];
+    if (o.jacobian)
+      for (int c = 0; c < 36; ++c) o.jacobian[i * 36 + c] = (double)J[c];
+  }
+  CK_D void writeFiltered(const CkfParams& cp, int k, const double f[6], const CV F[21]) const {
+    const size_t i = stateIdx(cp, k);
+    for (int c = 0; c < 6; ++c) cp.out.filtered[i * 6 + c] = f[c];
+    for (int c = 0; c < 21; ++c) cp.out.filtered_cov[i * 21 + c] = (double)F[c];
+  }
+
+  // storeLastActiveBranch: the branch on top becomes a found track, with its
+  // bound parameters on the target surface when it reached it
+  CK_D int store(const CkfParams& cp, const double* params, const CV* pc) {
+    if (nTracksC >= cp.o.max_tracks) return CK_TRACK_TOO_MANY_STATES;
+    const CkfBranch b = stack(cp)[nActive - 1];
+    const ck_ckf_out& o = cp.out;
+    const size_t i = (size_t)this->t * cp.o.max_tracks + nTracksC++;
+    o.track_tip[i] = b.tip;
+    if (o.track_n_measurements) o.track_n_measurements[i] = b.nMeas;
+    if (o.track_n_holes) o.track_n_holes[i] = b.nHoles;
+    if (o.track_n_outliers) o.track_n_outliers[i] = b.nOutliers;
+    if (o.track_ndf) o.track_ndf[i] = b.ndf;
+    if (o.track_chi2) o.track_chi2[i] = b.chi2;
+    if (o.track_params)
+      for (int c = 0; c < 6; ++c) o.track_params[i * 6 + c] = params ? params[c] : CUDART_NAN;
+    if (o.track_cov)
+      for (int c = 0; c < 21; ++c) o.track_cov[i * 21 + c] = pc ? (double)pc[c] : CUDART_NAN;
+    return CK_TRACK_OK;
+  }
+
+  // the examples' branch stopper: 0 continue, 1 stop and keep, 2 stop and drop
+  CK_D static int stopper(const CkfParams& cp, const CkfBranch& b) {
+    const bool tooMany = b.nHoles > cp.o.max_holes || b.nOutliers > cp.o.max_outliers ||
+                         (long long)b.nHoles + b.nOutliers > cp.o.max_holes_and_outliers;
+    if (!tooMany) return 0;
+    return b.nMeas >= cp.o.min_measurements ? 1 : 2;
+  }
+
+  // the actor's targetReached (a SurfaceReached with an unlimited near
+  // limit, StandardAborters.hpp:94-155): reached when the navigator's
+  // current surface is the target; else the closest intersection within
+  // the target's bounds (BoundaryTolerance::None) decides, and the first
+  // one steers the actor step constraint
+  CK_D bool targetCheck(const FitParams& fp, const CkfParams& cp) {
+    const int tsid = cp.o.target_surface;
+    if (tsid < 0) return false;
+    if (currentSurface == tsid) return true;
+    double path[2];
+    int st[2];
+    const int ni = this->intersectSurf(fp, tsid, path, st);
+    Surf<double> ts;
+    ts.load(fp.surfaces + tsid);
+    for (int i = 0; i < ni; ++i) {
+      if (st[i] == 0) continue;
+      double p[3], l[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) p[k] = this->pos[k] + path[i] * this->dir[k];
+      ts.toLocal3(p, l);
+      bool inside = true;
+      if (ts.type == CK_SURFACE_CYLINDER && cp.targetHalfZ > 0)
+        inside = fabs(l[2]) < fabs(cp.targetHalfZ + fp.opt.surfaceTolerance);
+      else if (ts.type == CK_SURFACE_PLANE && cp.targetHalfX > 0 && cp.targetHalfY > 0)
+        inside = l[0] >= -cp.targetHalfX && l[0] <= cp.targetHalfX && l[1] >= -cp.targetHalfY &&
+                 l[1] <= cp.targetHalfY;
+      if (!inside) st[i] = 0;
+    }
+    int best = -1;
+    for (int i = 0; i < ni; ++i)
+      if (st[i] != 0 && (best < 0 || fabs(path[i]) < fabs(path[best]))) best = i;
+    for (int i = 0; i < ni; ++i)
+      if (st[i] != 0 && path[i] < kNotSet + kOnSurfaceTolerance) {
+        cActor = kNotSet;
+        cupdate(cActor, path[i]);
+        break;
+      }
+    return best >= 0 && st[best] == 2;
+  }
+
+  // EigenStepper::initialize from bound parameters on a surface
+  CK_D void initialize(const FitParams& fp, const Surf<double>& sf, const double b[6]) {
+    this->boundToFree(sf, b);
+    this->initT(sf);
+#pragma unroll
+    for (int i = 0; i < 7; ++i) deriv[i] = P(0);
+    pathAcc = 0.0;
+    cNav = kNotSet;
+    cActor = kNotSet;
+    cUser = fp.opt.maxStepSize;
+    cAcc = fp.opt.initialStepSize;
+  }
+
+  // Actor::reset (CombinatorialKalmanFilter.hpp:470-531): the propagation
+  // restarts from the outermost state of the branch on top of the stack
+  CK_D int reset(const FitParams& fp, const CkfParams& cp) {
+    if (nActive == 0) {
+      done = true;
+      return CK_TRACK_OK;
+    }
+    const int tip = stack(cp)[nActive - 1].tip;
+    // (a branch below the top always holds a state of its own)
+    if (tip < 0 || tip >= nStatesC) return CK_TRACK_INCONSISTENT_STATES;
+    const size_t i = stateIdx(cp, tip);
+    const int sid = cp.out.state_surface[i];
+    double f[6];
+    for (int c = 0; c < 6; ++c) f[c] = cp.out.filtered[i * 6 + c];
+    Surf<double> sf;
+    sf.load(fp.surfaces + sid);
+    initialize(fp, sf, f);
+    for (int c = 0; c < 21; ++c) cov[c] = toP<CV>(cp.out.filtered_cov[i * 21 + c]);
+    // DirectNavigator::initialize: the current surface is the start surface,
+    // the sequence index the one before it
+    currentSurface = sid;
+    surfaceIndex = -1;
+    for (int k = 0; k < nSeq; ++k)
+      if (__ldg(&fp.seq_surf[seq0 + k]) == sid) {
+        surfaceIndex = k - 1;
+        break;
+      }
+    navigationBreak = false;
+    ckfStart = sid;
+    // the post-update material of the start surface
+    Surf<P> spv;
+    if constexpr (sizeof(P) == sizeof(float)) spv.load(fp.surfaces + sid);
+    const Surf<P>& sp = pickSurf<P>(sf, spv);
+    double l[3];
+    this->local(sf, l);
+    if (!this->material(fp, sid, sf, sp, l, 2)) return CK_TRACK_NOT_ON_SURFACE;
+    pathLimit = this->loopLimit(fp, kNotSet, true);
+    targetCheck(fp, cp);
+    return CK_TRACK_OK;
+  }
+
+  // Actor::filter (CombinatorialKalmanFilter.hpp:556-782) on surface sid
+  CK_D int filter(const FitParams& fp, const CkfParams& cp, int sid) {
+    const int sflags = __ldg(&fp.surfaces[sid].flags);
+    const bool sensitive = (sflags & CK_SURF_SENSITIVE) != 0;
+    const bool hasMat = (sflags & CK_SURF_MATERIAL) != 0;
+    if (!sensitive && !hasMat) return CK_TRACK_OK;  // passive
+    if (!sensitive) return CK_TRACK_INVALID_INPUT;  // material-only: not supported
+    Surf<double> sf;
+    sf.load(fp.surfaces + sid);
+    Surf<P> spv;
+    if constexpr (sizeof(P) == sizeof(float)) spv.load(fp.surfaces + sid);
+    const Surf<P>& sp = pickSurf<P>(sf, spv);
+    double l[3];
+    this->local(sf, l);
+    CV J[36];
+    this->transportToBound(sf, sp, l, J, false);
+    // pre-update material (none on the surface the branch restarted from)
+    if (sid != ckfStart && !this->material(fp, sid, sf, sp, l, 1))
+      return CK_TRACK_NOT_ON_SURFACE;
+    double bp[6];
+    if (!this->freeToBound(fp, sf, l, bp)) return CK_TRACK_NOT_ON_SURFACE;
+    double Pp[21];
+#pragma unroll
+    for (int i = 0; i < 21; ++i) Pp[i] = toD(cov[i]);
+    constexpr bool kFastRcp = sizeof(P) == sizeof(float);
+    CkfBranch* stk = stack(cp);
+    const int prevTip = stk[nActive - 1].tip;
+
+    // TrackStateCreator + MeasurementSelector (MeasurementSelector.ipp:19-124):
+    // the predicted chi2 of every measurement on the surface; those below
+    // the cut, ascending (ties in input order), at most max_candidates; none
+    // below: the smallest becomes an outlier when below the outlier cut
+    const int m0 = __ldg(&cp.surf_meas_off[sid]), m1 = __ldg(&cp.surf_meas_off[sid + 1]);
+    int selM[kCkfMaxCandidates];
+    double selC[kCkfMaxCandidates];
+    int nSel = 0, nPassed = 0, minM = -1;
+    double minChi2 = kNotSet;
+    const int K = cp.o.max_candidates;
+    for (int m = m0; m < m1; ++m) {
+      const int sub = fp.meas_sub ? __ldg(&fp.meas_sub[m]) : CK_MEAS_LOC01;
+      if (sub < CK_MEAS_LOC0 || sub > CK_MEAS_LOC01) return CK_TRACK_INVALID_INPUT;
+      double V[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) V[c] = __ldg(&fp.meas_cov[4 * (size_t)m + c]);
+      const double c2 = predictedChi2Sub<kFastRcp>(bp, Pp, sub, __ldg(&fp.meas_val[2 * (size_t)m]),
+                                                   __ldg(&fp.meas_val[2 * (size_t)m + 1]), V);
+      if (c2 < minChi2) {
+        minChi2 = c2;
+        minM = m;
+      }
+      if (!(c2 >= cp.o.chi2_cut)) {
+        ++nPassed;
+        int pos = nSel;
+        while (pos > 0 && selC[pos - 1] > c2) --pos;
+        if (pos < K) {
+          for (int j = (nSel < K ? nSel : K - 1); j > pos; --j) {
+            selM[j] = selM[j - 1];
+            selC[j] = selC[j - 1];
+          }
+          selM[pos] = m;
+          selC[pos] = c2;
+          if (nSel < K) ++nSel;
+        }
+      }
+    }
+    bool isOutlier = false;
+    if (nPassed == 0 && minM >= 0 && minChi2 < cp.o.chi2_cut_outlier) {
+      selM[0] = minM;
+      selC[0] = minChi2;
+      nSel = 1;
+      isOutlier = true;
+    }
+    const uint32_t matFlag = hasMat ? CK_FLAG_HAS_MATERIAL : 0u;
+    if (nSel > 0) {
+      const int first = nStatesC;
+      if (first + nSel > cp.o.max_states) return CK_TRACK_TOO_MANY_STATES;
+      for (int i = 0; i < nSel; ++i)
+        writeState(cp, first + i, sid, prevTip, selM[i],
+                   CK_FLAG_HAS_PARAMETERS | CK_FLAG_HAS_MEASUREMENT | matFlag |
+                       (isOutlier ? CK_FLAG_IS_OUTLIER : 0u),
+                   selC[i], bp, cov, J);
+      nStatesC += nSel;
+      // processNewTrackStates (:836-898): the new branches from the worst
+      // candidate to the best, the best on top of the stack
+      const CkfBranch root = stk[nActive - 1];
+      --nActive;
+      int onSurface = 0;
+      for (int i = nSel - 1; i >= 0; --i) {
+        CkfBranch b = root;
+        b.tip = first + i;
+        if (isOutlier) {
+          writeFiltered(cp, b.tip, bp, cov);
+          ++b.nOutliers;
+        } else {
+          const int m = selM[i];
+          const int sub = fp.meas_sub ? __ldg(&fp.meas_sub[m]) : CK_MEAS_LOC01;
+          double V[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) V[c] = __ldg(&fp.meas_cov[4 * (size_t)m + c]);
+          double filt[6], F[21], c2 = 0.0;
+          if (!kalmanUpdateSub<kFastRcp>(bp, Pp, sub, __ldg(&fp.meas_val[2 * (size_t)m]),
+                                         __ldg(&fp.meas_val[2 * (size_t)m + 1]), V,
+                                         fp.opt.joseph != 0, filt, F, c2))
+            return CK_TRACK_UPDATE_FAILED;
+          CV Fc[21];
+#pragma unroll
+          for (int c = 0; c < 21; ++c) Fc[c] = toP<CV>(F[c]);
+          writeFiltered(cp, b.tip, filt, Fc);
+          if (cp.out.state_chi2) cp.out.state_chi2[stateIdx(cp, b.tip)] = c2;
+          ++b.nMeas;
+          b.ndf += (sub & 1) + ((sub >> 1) & 1);
+          b.chi2 = b.chi2 + c2;
+        }
+        if (nActive >= cp.o.max_branches) return CK_TRACK_TOO_MANY_STATES;
+        stk[nActive++] = b;
+        const int r = stopper(cp, b);
+        if (r == 0) {
+          ++onSurface;
+        } else {
+          if (r == 1) {
+            const int e = store(cp, nullptr, nullptr);
+            if (e != CK_TRACK_OK) return e;
+          }
+          --nActive;
+        }
+      }
+      if (onSurface == 0) return reset(fp, cp);
+    } else {
+      // a hole: a sensitive surface without a selected measurement
+      if (nStatesC >= cp.o.max_states) return CK_TRACK_TOO_MANY_STATES;
+      const int k = nStatesC++;
+      writeState(cp, k, sid, prevTip, -1, CK_FLAG_HAS_PARAMETERS | CK_FLAG_IS_HOLE | matFlag, 0.0,
+                 bp, cov, J);
+      writeFiltered(cp, k, bp, cov);
+      CkfBranch& b = stk[nActive - 1];
+      b.tip = k;
+      ++b.nHoles;
+      const int r = stopper(cp, b);
+      if (r != 0) {
+        if (r == 1) {
+          const int e = store(cp, nullptr, nullptr);
+          if (e != CK_TRACK_OK) return e;
+        }
+        --nActive;
+        return reset(fp, cp);
+      }
+    }
+    // the stepper continues with the filtered parameters of the branch on
+    // top when its state is a measurement (EigenStepper::update)
+    const size_t ci = stateIdx(cp, stk[nActive - 1].tip);
+    const uint32_t cf = cp.out.state_flags[ci];
+    if ((cf & CK_FLAG_HAS_MEASUREMENT) && !(cf & CK_FLAG_IS_OUTLIER)) {
+      double f[6];
+      for (int c = 0; c < 6; ++c) f[c] = cp.out.filtered[ci * 6 + c];
+      this->updateFree(sf, bp, f, l);
+      for (int c = 0; c < 21; ++c) cov[c] = toP<CV>(cp.out.filtered_cov[ci * 21 + c]);
+      this->initTP(sp);
+      this->local(sf, l);
+    }
+    if (!this->material(fp, sid, sf, sp, l, 2)) return CK_TRACK_NOT_ON_SURFACE;
+    return CK_TRACK_OK;
+  }
+
+  // Actor::act (CombinatorialKalmanFilter.hpp:330-448)
+  CK_D int act(const FitParams& fp, const CkfParams& cp) {
+    if (!pathLimitSet) {
+      pathLimit = this->loopLimit(fp, kNotSet, true);
+      pathLimitSet = true;
+    }
+    if (currentSurface >= 0) {
+      const int r = filter(fp, cp, currentSurface);
+      if (r != CK_TRACK_OK) return r;
+      if (done) return CK_TRACK_OK;
+    }
+    // (the reference evaluates both aborters before it acts on the first
+    // that fired: both step-size constraints are updated)
+    const bool pathReached = this->pathLimitReached(fp, pathLimit);
+    const bool targetReached = targetCheck(fp, cp);
+    if (!pathReached && !targetReached) return CK_TRACK_OK;
+    int e;
+    if (!pathReached) {
+      // the branch's parameters: the bound state on the target surface
+      const int tsid = cp.o.target_surface;
+      Surf<double> sf;
+      sf.load(fp.surfaces + tsid);
+      Surf<P> spv;
+      if constexpr (sizeof(P) == sizeof(float)) spv.load(fp.surfaces + tsid);
+      const Surf<P>& sp = pickSurf<P>(sf, spv);
+      double l[3], bp[6];
+      this->local(sf, l);
+      if (!this->freeToBound(fp, sf, l, bp)) return CK_TRACK_NOT_ON_SURFACE;
+      CV J[36];
+      this->transportToBound(sf, sp, l, J, false);
+      cNav = kNotSet;
+      e = store(cp, bp, cov);
+    } else {
+      e = store(cp, nullptr, nullptr);
+    }
+    if (e != CK_TRACK_OK) return e;
+    --nActive;
+    return reset(fp, cp);
+  }
+
+  // the seed: validation, EigenStepper::initialize on the seed's plane, the
+  // pre-propagation actor call and the first target (Propagator.ipp:25-96)
+  CK_D int begin(const FitParams& fp, const CkfParams& cp, int seed) {
+    this->t = seed;
+    this->q = seed;
+    seq0 = __ldg(&fp.seq_off[seed]);
+    nSeq = __ldg(&fp.seq_off[seed + 1]) - seq0;
+    nStatesC = 0;
+    nTracksC = 0;
+    nActive = 0;
+    if (nSeq < 0) return CK_TRACK_INVALID_INPUT;
+    for (int i = 0; i < nSeq; ++i) {
+      const int sid = __ldg(&fp.seq_surf[seq0 + i]);
+      if (sid < 0 || sid >= fp.n_surfaces || __ldg(&fp.surfaces[sid].type) == CK_SURFACE_LINE)
+        return CK_TRACK_INVALID_INPUT;
+    }
+    {
+      double sp[6];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) sp[i] = __ldg(&fp.start_params[6 * (size_t)seed + i]);
+      Surf<double> start;
+      start.loadPlane(fp.start_frames + 12 * (size_t)seed);
+      initialize(fp, start, sp);
+      const double* sc = fp.start_cov + 36 * (size_t)seed;
+#pragma unroll
+      for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int j = i; j < 6; ++j) cov[sidx(i, j)] = toP<CV>(__ldg(&sc[i * 6 + j]));
+    }
+    mass = __ldg(&fp.particle[2 * (size_t)seed]);
+    absQ = __ldg(&fp.particle[2 * (size_t)seed + 1]);
+    pdg = fp.pdg ? __ldg(&fp.pdg[seed]) : 211;
+    dirSign = 1.0;
+    extrapolating = false;
+    coasting = false;
+    finished = false;
+    stepStarted = false;
+    steps = 0;
+    surfaceIndex = -1;
+    navigationBreak = false;
+    currentSurface = -1;  // the seed's plane is not a table surface
+    haveTarget = false;
+    targetSurf = -1;
+    targetIdx = 0;
+    ckfStart = -1;
+    pathLimit = kNotSet;
+    pathLimitSet = false;
+    done = false;
+    CkfBranch root;
+    root.tip = -1;
+    root.nMeas = root.nHoles = root.nOutliers = root.ndf = root.pad = 0;
+    root.chi2 = 0.0;
+    stack(cp)[0] = root;
+    nActive = 1;
+    int e = act(fp, cp);
+    if (e != CK_TRACK_OK || done) return e;
+    e = nextTarget(fp, cp, false);
+    if (e != CK_TRACK_OK || done) return e;
+    phase = PH_STEP;
+    return CK_TRACK_OK;
+  }
+
+  // the navigator's next target (Propagator.ipp:79-96, 166-181); with
+  // end_of_world a branch whose navigator has no surface of the sequence
+  // left ends there, kept, as EndOfWorldReached ends it in Actor::act
+  // (CombinatorialKalmanFilter.hpp:392-436), and the next branch restarts
+  // (each pass pops a branch: bounded)
+  CK_D int nextTarget(const FitParams& fp, const CkfParams& cp, bool release) {
+    while (true) {
+      if (!haveTarget) {
+        if (release) cNav = kNotSet;
+        int e;
+        haveTarget = this->getNextTarget(fp, e);
+        if (e != CK_TRACK_OK) return e;
+      }
+      if (!(cp.o.end_of_world && navigationBreak)) return CK_TRACK_OK;
+      int e = store(cp, nullptr, nullptr);
+      if (e != CK_TRACK_OK) return e;
+      --nActive;
+      e = reset(fp, cp);
+      if (e != CK_TRACK_OK || done) return e;
+      release = true;
+    }
+  }
+};
+
+template <typename P, typename CV>
+__global__ void __launch_bounds__(kCkfBlock) ckfKernel(FitParams fp, CkfParams cp) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < fp.n_tracks;
+       s += gridDim.x * blockDim.x) {
+    CkfLane<P, CV> L;
+    int e = L.begin(fp, cp, s);
+    bool ok = e == CK_TRACK_OK;
+    if (ok && !L.done) {
+      // Propagator::propagate's stepping loop (Propagator.ipp:98-186): each
+      // pass takes one accepted step (or fails), so maxSteps bounds it
+      while (true) {
+        while (L.phase == PH_STEP) L.template step<kStepCkf>(fp, s);
+        if (L.phase != PH_SURFACE) {  // the step failed: status written
+          ok = false;
+          e = -1;
+          break;
+        }
+        e = L.act(fp, cp);
+        if (e != CK_TRACK_OK) {
+          ok = false;
+          break;
+        }
+        if (L.done) break;
+        e = L.nextTarget(fp, cp, true);
+        if (e != CK_TRACK_OK) {
+          ok = false;
+          break;
+        }
+        if (L.done) break;
+        L.phase = PH_STEP;
+      }
+    }
+    if (e > 0) cp.out.status[s] = e;
+    if (ok) cp.out.status[s] = CK_TRACK_OK;
+    cp.out.n_tracks[s] = ok ? L.nTracksC : 0;
+    cp.out.n_states[s] = ok ? L.nStatesC : 0;
+  }
+}
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace
+
+extern "C" void ck_ckf_options_default(ck_ckf_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->chi2_cut = 15.0;
+  o->chi2_cut_outlier = INFINITY;
+  o->max_candidates = 1;
+  o->min_measurements = 0;
+  o->max_holes = INT32_MAX;
+  o->max_outliers = INT32_MAX;
+  o->max_holes_and_outliers = INT32_MAX;
+  o->target_surface = -1;
+  o->max_states = 64;
+  o->max_tracks = 16;
+  o->max_branches = 16;
+}
+
+extern "C" ck_status ck_find_tracks(ck_handle* h, const ck_options* opt, const ck_ckf_options* ck,
+                                    const ck_ckf_in* in, ck_ckf_out* out, void* stream) {
+  if (!h || !ck || !in || !out) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
+  ck_status vs = validateOptions(opt);
+  if (vs != CK_OK) return vs;
+  const int n = in->n_seeds;
+  if (n < 0 || in->n_meas < 0) return fail(CK_ERR_INVALID_ARGUMENT, "negative count");
+  if (in->memory != CK_MEM_HOST && in->memory != CK_MEM_DEVICE)
+    return fail(CK_ERR_INVALID_ARGUMENT, "unknown memory kind");
+  if (in->n_surfaces != h->nSurfaces)
+    return fail(CK_ERR_INVALID_ARGUMENT, "n_surfaces differs from the handle's surface table");
+  if (ck->max_candidates < 1 || ck->max_candidates > kCkfMaxCandidates)
+    return fail(CK_ERR_INVALID_ARGUMENT, "max_candidates outside 1..16");
+  if (ck->max_states < 1 || ck->max_tracks < 1 || ck->max_branches < 1)
+    return fail(CK_ERR_INVALID_ARGUMENT, "a capacity below 1");
+  if (ck->target_surface < -1 || ck->target_surface >= h->nSurfaces)
+    return fail(CK_ERR_INVALID_ARGUMENT, "target surface out of range");
+  if (ck->target_surface >= 0 && h->hostSurfaces[ck->target_surface].type == CK_SURFACE_LINE)
+    return fail(CK_ERR_INVALID_ARGUMENT, "the target surface must be a plane or a cylinder");
+  if (n == 0) return CK_OK;
+  if (!in->seq_offsets || !in->seq_surfaces || !in->start_params || !in->start_cov ||
+      !in->start_frames || !in->particle || !in->surf_meas_offsets ||
+      (in->n_meas > 0 && (!in->meas_values || !in->meas_cov)))
+    return fail(CK_ERR_INVALID_ARGUMENT, "a required input array is NULL");
+  if (!out->status || !out->n_tracks || !out->n_states || !out->track_tip || !out->state_prev ||
+      !out->state_surface || !out->state_flags || !out->filtered || !out->filtered_cov)
+    return fail(CK_ERR_INVALID_ARGUMENT, "a required output array is NULL");
+  const bool host = in->memory == CK_MEM_HOST;
+  if (host) {
+    // the grouping of the measurements by surface, checked where it is readable
+    const int32_t* so = in->surf_meas_offsets;
+    bool bad = so[0] != 0 || so[h->nSurfaces] != in->n_meas;
+    for (int s = 0; s < h->nSurfaces && !bad; ++s) bad = so[s + 1] < so[s];
+    for (int s = 0; s < n && !bad; ++s) bad = in->seq_offsets[s + 1] < in->seq_offsets[s];
+    if (bad) return fail(CK_ERR_INVALID_ARGUMENT, "offsets not a non-decreasing partition");
+  }
+  std::lock_guard<std::mutex> lock(h->mu);
+  cudaError_t e = cudaSetDevice(h->device);
+  if (e != cudaSuccess) return cudaFail(e, "set device");
+  cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
+
+  const size_t nn = (size_t)n, S = (size_t)ck->max_states * nn, T = (size_t)ck->max_tracks * nn;
+  const size_t nSeqAll = host ? (size_t)in->seq_offsets[n] : 0;
+  const size_t nm = (size_t)in->n_meas, ns1 = (size_t)h->nSurfaces + 1;
+  struct Arr {
+    const void* src;
+    void* dst;
+    size_t bytes;
+    bool input;
+  };
+  Arr arrs[] = {
+      {in->seq_offsets, nullptr, 4 * (nn + 1), true},
+      {in->seq_surfaces, nullptr, 4 * nSeqAll, true},
+      {in->start_params, nullptr, 48 * nn, true},
+      {in->start_cov, nullptr, 288 * nn, true},
+      {in->start_frames, nullptr, 96 * nn, true},
+      {in->particle, nullptr, 8 * nn, true},
+      {in->particle_pdg, nullptr, 4 * nn, true},
+      {in->surf_meas_offsets, nullptr, 4 * ns1, true},
+      {in->meas_values, nullptr, 16 * nm, true},
+      {in->meas_cov, nullptr, 32 * nm, true},
+      {in->meas_subspace, nullptr, 4 * nm, true},
+      {out->status, nullptr, 4 * nn, false},
+      {out->n_tracks, nullptr, 4 * nn, false},
+      {out->n_states, nullptr, 4 * nn, false},
+      {out->track_tip, nullptr, 4 * T, false},
+      {out->track_n_measurements, nullptr, 4 * T, false},
+      {out->track_n_holes, nullptr, 4 * T, false},
+      {out->track_n_outliers, nullptr, 4 * T, false},
+      {out->track_ndf, nullptr, 4 * T, false},
+      {out->track_chi2, nullptr, 8 * T, false},
+      {out->track_params, nullptr, 48 * T, false},
+      {out->track_cov, nullptr, 168 * T, false},
+      {out->state_prev, nullptr, 4 * S, false},
+      {out->state_surface, nullptr, 4 * S, false},
+      {out->state_flags, nullptr, 4 * S, false},
+      {out->state_measurement, nullptr, 4 * S, false},
+      {out->state_chi2, nullptr, 8 * S, false},
+      {out->state_path_length, nullptr, 8 * S, false},
+      {out->predicted, nullptr, 48 * S, false},
+      {out->predicted_cov, nullptr, 168 * S, false},
+      {out->filtered, nullptr, 48 * S, false},
+      {out->filtered_cov, nullptr, 168 * S, false},
+      {out->jacobian, nullptr, 288 * S, false}};
+  constexpr int kArrs = sizeof(arrs) / sizeof(arrs[0]);
+  // device scratch: the fail path's tip array and the branch stacks
+  const size_t tipBytes = align256(4 * nn);
+  const size_t brBytes = align256(sizeof(CkfBranch) * (size_t)ck->max_branches * nn);
+  size_t total = tipBytes + brBytes;
+  if (host)
+    for (int i = 0; i < kArrs; ++i)
+      if (arrs[i].src) total += align256(arrs[i].bytes);
+  if ((e = h->unitBuf.ensure(total)) != cudaSuccess) return cudaFail(e, "track-finding buffer");
+  char* base = (char*)h->unitBuf.p;
+  size_t off = tipBytes + brBytes;
+  for (int i = 0; i < kArrs; ++i) {
+    if (!arrs[i].src) continue;
+    if (host) {
+      arrs[i].dst = base + off;
+      off += align256(arrs[i].bytes);
+      if (arrs[i].input && arrs[i].bytes)
+        cudaMemcpyAsync(arrs[i].dst, arrs[i].src, arrs[i].bytes, cudaMemcpyHostToDevice, st);
+    } else {
+      arrs[i].dst = const_cast<void*>(arrs[i].src);
+    }
+  }
+  FitParams fp;
+  std::memset(&fp, 0, sizeof(fp));
+  fp.n_tracks = n;
+  fp.n_queue = n;
+  fp.seq_off = (const int32_t*)arrs[0].dst;
+  fp.seq_surf = (const int32_t*)arrs[1].dst;
+  fp.start_params = (const double*)arrs[2].dst;
+  fp.start_cov = (const double*)arrs[3].dst;
+  fp.start_frames = (const double*)arrs[4].dst;
+  fp.particle = (const float*)arrs[5].dst;
+  fp.pdg = (const int32_t*)arrs[6].dst;
+  fp.meas_val = (const double*)arrs[8].dst;
+  fp.meas_cov = (const double*)arrs[9].dst;
+  fp.meas_sub = (const int32_t*)arrs[10].dst;
+  fp.out.status = (int32_t*)arrs[11].dst;
+  fp.tip = (int32_t*)base;
+  fp.max_states = 1;
+  fp.lanes_per_warp = 32;
+  fp.steps_per_round = 1;
+  fp.surfaces = h->dSurfaces;
+  fp.n_surfaces = h->nSurfaces;
+  fp.trig = h->dTrig;
+  fp.field = h->field;
+  fp.mc = h->mc;
+  fp.opt = toDevOptions(*opt);
+  fp.ref_surface = -1;
+  CkfParams cp;
+  std::memset(&cp, 0, sizeof(cp));
+  cp.o = *ck;
+  if (ck->target_surface >= 0) {
+    const ck_surface& t = h->hostSurfaces[ck->target_surface];
+    cp.targetHalfX = t.half_x;
+    cp.targetHalfY = t.half_y;
+    cp.targetHalfZ = t.half_length_z;
+  }
+  cp.surf_meas_off = (const int32_t*)arrs[7].dst;
+  cp.branches = (CkfBranch*)(base + tipBytes);
+  int32_t** outInts[] = {&cp.out.status,        &cp.out.n_tracks,         &cp.out.n_states,
+                         &cp.out.track_tip,     &cp.out.track_n_measurements,
+                         &cp.out.track_n_holes, &cp.out.track_n_outliers, &cp.out.track_ndf};
+  for (int i = 0; i < 8; ++i) *outInts[i] = (int32_t*)arrs[11 + i].dst;
+  cp.out.track_chi2 = (double*)arrs[19].dst;
+  cp.out.track_params = (double*)arrs[20].dst;
+  cp.out.track_cov = (double*)arrs[21].dst;
+  cp.out.state_prev = (int32_t*)arrs[22].dst;
+  cp.out.state_surface = (int32_t*)arrs[23].dst;
+  cp.out.state_flags = (uint32_t*)arrs[24].dst;
+  cp.out.state_measurement = (int32_t*)arrs[25].dst;
+  cp.out.state_chi2 = (double*)arrs[26].dst;
+  cp.out.state_path_length = (double*)arrs[27].dst;
+  cp.out.predicted = (double*)arrs[28].dst;
+  cp.out.predicted_cov = (double*)arrs[29].dst;
+  cp.out.filtered = (double*)arrs[30].dst;
+  cp.out.filtered_cov = (double*)arrs[31].dst;
+  cp.out.jacobian = (double*)arrs[32].dst;
+  const int grid = (n + kCkfBlock - 1) / kCkfBlock;
+  if (opt->precision == CK_PRECISION_MIXED)
+    ckfKernel<float, float><<<grid, kCkfBlock, 0, st>>>(fp, cp);
+  else
+    ckfKernel<double, double><<<grid, kCkfBlock, 0, st>>>(fp, cp);
+  if ((e = cudaGetLastError()) != cudaSuccess) return cudaFail(e, "track-finding kernel launch");
+  if (host) {
+    for (int i = 0; i < kArrs; ++i)
+      if (arrs[i].src && !arrs[i].input)
+        cudaMemcpyAsync(const_cast<void*>(arrs[i].src), arrs[i].dst, arrs[i].bytes,
+                        cudaMemcpyDeviceToHost, st);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cudaFail(e, "track-finding kernel");
+  }
+  h->lastLaunches = 1;
+  return CK_OK;
+}

@@ -49,8 +49,10 @@ namespace ck {
 enum Phase { PH_FETCH = 0, PH_STEP = 1, PH_SURFACE = 2, PH_DONE = 3 };
 // What follows an accepted Runge-Kutta step: the fit's navigation and actor
 // (kStepFit), the aborters of the extrapolation to the reference line
-// (kStepExtrapolate), or those of a plain propagation (kStepPropagate).
-enum StepMode { kStepFit = 0, kStepExtrapolate = 1, kStepPropagate = 2 };
+// (kStepExtrapolate), those of a plain propagation (kStepPropagate), or the
+// navigator's post-step update alone, the track finder's actor running in
+// its own loop (kStepCkf: the lane returns in the SURFACE phase).
+enum StepMode { kStepFit = 0, kStepExtrapolate = 1, kStepPropagate = 2, kStepCkf = 3 };
 // SurfaceReached's near limit (StandardAborters.hpp:76): -100 um
 constexpr double kTargetNearLimit = -0.1;
 // Runge-Kutta trials per round of the compaction kernels when at most half
@@ -1312,6 +1314,20 @@ struct Lane {
     }
     if constexpr (MODE == kStepPropagate) {
       if (propagationAbort(fp)) finishPropagation(fp);
+      return;
+    }
+    if constexpr (MODE == kStepCkf) {
+      // a branch restart keeps the target of the branch before it
+      // (DirectNavigator::checkTargetValid is always true) while the
+      // sequence index restarts at the new branch's surface; a target reached
+      // with the index before the sequence start sets no current surface
+      if (haveTarget) {
+        const int post = surfaceStatus(fp, targetSurf, targetIdx);
+        if (post == 2 && !navigationBreak && surfaceIndex >= 0 && surfaceIndex < nSeq)
+          currentSurface = __ldg(&fp.seq_surf[seq0 + surfaceIndex]);
+        if (post != 1) haveTarget = false;
+      }
+      phase = PH_SURFACE;
       return;
     }
     if (haveTarget) {

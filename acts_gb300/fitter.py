@@ -93,6 +93,10 @@ def lib():
         L.ck_field_lookup.argtypes = [C.c_void_p, C.c_int32, abi.P_f64, abi.P_f64, abi.P_i32]
         L.ck_propagate.argtypes = [C.c_void_p, P(abi.ck_options), P(abi.ck_propagate_in),
                                    P(abi.ck_propagate_out), C.c_void_p]
+        L.ck_find_tracks.argtypes = [C.c_void_p, P(abi.ck_options), P(abi.ck_ckf_options),
+                                     P(abi.ck_ckf_in), P(abi.ck_ckf_out), C.c_void_p]
+        L.ck_ckf_options_default.argtypes = [P(abi.ck_ckf_options)]
+        L.ck_ckf_options_default.restype = None
         L.ck_field_lookup_precision.argtypes = [C.c_void_p, C.c_int32, C.c_int32, abi.P_f64,
                                                 abi.P_f64, abi.P_i32]
         L.ck_fp_peak_gflops.argtypes = [C.c_void_p, C.c_int32, P(C.c_double)]
@@ -460,6 +464,15 @@ class CudaKalman:
         i, o = prop.as_in(), prop.as_out()
         _check(lib().ck_propagate(self._h, C.byref(options), C.byref(i), C.byref(o), None))
         return prop
+
+    def find_tracks(self, options, ckf_options, tf):
+        """ck_find_tracks on an abi.TrackFinding (host arrays, filled in
+        place): CombinatorialKalmanFilter::findTracks from each seed along
+        its surface sequence, in the options' precision form."""
+        i, o = tf.as_in(), tf.as_out()
+        _check(lib().ck_find_tracks(self._h, C.byref(options), C.byref(ckf_options), C.byref(i),
+                                    C.byref(o), None))
+        return tf
 
     def field_lookup(self, pos, precision=abi.PRECISION_FP64):
         """getField on the device in a form's stepper arithmetic (FP64, or

@@ -190,3 +190,30 @@ def event_sizes(seed, n_events, mean=-1.0, lo=100, hi=20000):
     out = np.zeros(n_events, np.int32)
     lib().ckg_event_sizes(seed, n_events, mean, lo, hi, abi.ptr(out, C.c_int32))
     return out
+
+
+def ckf_event(detector, batch, max_states=64, max_tracks=16):
+    """The batch's tracks as one event for track finding (an
+    abi.TrackFinding): every track's start parameters become a seed with the
+    track's surface sequence; all measurements of the batch, grouped by
+    surface (stable: within a surface in track order), are the candidates.
+    `meas_track` gives the generating track of each grouped measurement and
+    `meas_index` its index in the batch."""
+    n = batch.n
+    nm = int(batch.meas_offsets[-1])
+    ms = np.asarray(batch.meas_surfaces[:nm])
+    order = np.argsort(ms, kind="stable")
+    counts = np.bincount(ms, minlength=detector.n_surfaces)
+    offs = np.zeros(detector.n_surfaces + 1, np.int32)
+    offs[1:] = np.cumsum(counts)
+    track_of = np.repeat(np.arange(n, dtype=np.int32), np.diff(batch.meas_offsets))
+    sub = None if batch.meas_subspace is None else np.asarray(batch.meas_subspace[:nm])[order]
+    tf = abi.TrackFinding(batch.seq_offsets, batch.seq_surfaces, batch.start_params,
+                          batch.start_cov, batch.start_frames, batch.particle, offs,
+                          batch.meas_values.reshape(-1, 2)[:nm][order],
+                          batch.meas_cov.reshape(-1, 4)[:nm][order], meas_subspace=sub,
+                          particle_pdg=batch.particle_pdg, max_states=max_states,
+                          max_tracks=max_tracks)
+    tf.meas_track = track_of[order]
+    tf.meas_index = order.astype(np.int64)
+    return tf

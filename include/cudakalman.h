@@ -126,8 +126,9 @@ typedef struct ck_surface {
   double rotation[9];    /* row-major 3x3, columns = local x, y, z axes     */
   double center[3];
   double radius;         /* cylinder radius (mm)                            */
-  double half_length_z;  /* cylinder bounds (used by the generator only)    */
-  double half_x, half_y; /* plane rectangle bounds (generator only)         */
+  double half_length_z;  /* cylinder bounds (0: unbounded)                  */
+  double half_x, half_y; /* plane rectangle bounds (0: unbounded); bounds
+                            apply to the target of ck_find_tracks only      */
   float mat_thickness;   /* slab thickness (mm)                             */
   float mat_x0, mat_l0;  /* radiation / nuclear interaction length (mm)     */
   float mat_ar, mat_z;   /* relative atomic mass, nuclear charge            */
@@ -487,7 +488,9 @@ const char* ck_autotune_log(ck_handle* h);
 ck_status ck_fp_peak_gflops(ck_handle* h, int32_t precision, double* gflops);
 
 /* sizeof() of ck_surface, ck_field, ck_options, ck_config, ck_batch_in,
- * ck_batch_out, ck_server_config (in that order), for binding checks. */
+ * ck_batch_out, ck_server_config, ck_propagate_in, ck_propagate_out,
+ * ck_ckf_options, ck_ckf_in, ck_ckf_out (in that order; the first n), for
+ * binding checks. */
 void ck_abi_struct_sizes(int64_t* out, int32_t n);
 
 /* Runs the autotuner for `precision` on the given device-resident batch:
@@ -626,6 +629,114 @@ typedef struct ck_propagate_out {
 
 ck_status ck_propagate(ck_handle* h, const ck_options* options, const ck_propagate_in* in,
                        ck_propagate_out* out, void* stream);
+
+/* ------------------------------------------- combinatorial track finding */
+/* Combinatorial Kalman filter track finding from seeds:
+ *   CombinatorialKalmanFilter<Propagator<EigenStepper<>, DirectNavigator>,
+ *       TrackContainer>::findTracks(initialParameters, options, tracks)
+ *   (Core/include/Acts/TrackFinding/CombinatorialKalmanFilter.hpp:1191-1335,
+ *    Actor::act / filter / reset / processNewTrackStates :250-900)
+ * with the default TrackStateCreator and MeasurementSelector
+ * (TrackStateCreator.hpp:60-310, MeasurementSelector.ipp:19-124) and the
+ * examples' branch stopper (Examples/Algorithms/TrackFinding/src/
+ * TrackFindingAlgorithm.cpp:185-261), on the fitter's stepper, navigator and
+ * updater in the options' precision form. Each seed follows its surface
+ * sequence (the DirectNavigator's); on a sensitive surface the measurements
+ * of that surface are the candidates: their predicted chi2 against the cut
+ * selects up to max_candidates (ascending chi2), each opening a branch
+ * (depth-first, the best first); none selected: the best becomes an outlier
+ * when its chi2 is below chi2_cut_outlier, else a hole. A branch ends on the
+ * target surface (its bound parameters become the track's), at the
+ * loop-protection path limit, or when the branch stopper stops it (kept
+ * with enough measurements); every branch that ends kept is a found track.
+ * Material-only surfaces in a sequence are not supported (the track fails
+ * with CK_TRACK_INVALID_INPUT). Errors of a seed's search (stepper, field,
+ * the propagator's step limit over all its branches, a capacity below)
+ * fail the seed: status set, no tracks. */
+typedef struct ck_ckf_options {
+  double chi2_cut;           /* MeasurementSelectorCuts::chi2CutOff (15)          */
+  double chi2_cut_outlier;   /* chi2CutOffOutlier (+inf: always an outlier)       */
+  int32_t max_candidates;    /* numMeasurementsCutOff (1)                         */
+  int32_t min_measurements;  /* branch stopper: TrackSelector cuts (0, and       */
+  int32_t max_holes;         /*   INT32_MAX for the maxima: no stopping)          */
+  int32_t max_outliers;
+  int32_t max_holes_and_outliers;
+  int32_t target_surface;    /* CombinatorialKalmanFilterOptions::targetSurface:
+                                a plane or cylinder of the table; -1: none     */
+  int32_t max_states;        /* track-state capacity per seed (64)               */
+  int32_t max_tracks;        /* found-track capacity per seed (16)               */
+  int32_t max_branches;      /* active-branch capacity per seed (16)             */
+  int32_t end_of_world;      /* 1: a branch ends (kept) as soon as the navigator
+                                has no surface of the seed's sequence left
+                                ahead, before a further step, as the end of
+                                the world ends it with the reference's
+                                geometry Navigator; 0 (default): the
+                                DirectNavigator's behaviour, where only the
+                                loop protection, the target or the stopper end
+                                a branch (without a field and a target the
+                                seed runs into the step limit; on a field map
+                                it may leave the map)                          */
+} ck_ckf_options;
+
+void ck_ckf_options_default(ck_ckf_options* options);
+
+/* Seeds (start parameters on a plane, as ck_batch_in) with their surface
+ * sequences, and the event's measurements grouped by surface: the
+ * measurements of surface s are [surf_meas_offsets[s], surf_meas_offsets[s+1])
+ * in the caller's order (the candidate order). */
+typedef struct ck_ckf_in {
+  int32_t n_seeds;
+  int32_t memory;                    /* CK_MEM_HOST or CK_MEM_DEVICE (in and out) */
+  const int32_t* seq_offsets;        /* [n_seeds+1]                            */
+  const int32_t* seq_surfaces;
+  const double* start_params;        /* [n_seeds*6]                            */
+  const double* start_cov;           /* [n_seeds*36]                           */
+  const double* start_frames;        /* [n_seeds*12]                           */
+  const float* particle;             /* [n_seeds*2] (mass GeV, |q|)            */
+  const int32_t* particle_pdg;       /* [n_seeds] or NULL (211)                */
+  int32_t n_meas;
+  int32_t n_surfaces;                /* the handle's table size                */
+  const int32_t* surf_meas_offsets;  /* [n_surfaces+1]                          */
+  const double* meas_values;         /* [n_meas*2] (1D: first slot)            */
+  const double* meas_cov;            /* [n_meas*4]                             */
+  const int32_t* meas_subspace;      /* [n_meas] CK_MEAS_*, or NULL (all 2D)   */
+} ck_ckf_in;
+
+/* Results. Per seed s: its found tracks k < n_tracks[s] at [s*max_tracks + k]
+ * (the order the search keeps them in) and its track states i < n_states[s]
+ * at [s*max_states + i] (creation order; a track is the chain of states from
+ * its tip back along state_prev). Vector and matrix arrays hold C values per
+ * element: element c of state i of seed s at [(s*max_states + i)*C + c];
+ * covariances packed as upper triangles (C = 21), Jacobians C = 36. */
+typedef struct ck_ckf_out {
+  int32_t* status;                /* [n_seeds] CK_TRACK_*                      */
+  int32_t* n_tracks;              /* [n_seeds]                                 */
+  int32_t* n_states;              /* [n_seeds]                                 */
+  int32_t* track_tip;             /* state index of the track's last state     */
+  int32_t* track_n_measurements;
+  int32_t* track_n_holes;
+  int32_t* track_n_outliers;
+  int32_t* track_ndf;
+  double* track_chi2;
+  double* track_params;           /* C = 6 on the target surface (NaN: none)   */
+  double* track_cov;              /* C = 21                                    */
+  int32_t* state_prev;            /* previous state of the branch, -1: first   */
+  int32_t* state_surface;
+  uint32_t* state_flags;          /* CK_FLAG_*                                 */
+  int32_t* state_measurement;     /* measurement index, -1 for holes            */
+  double* state_chi2;             /* measurement states: the filtered chi2;
+                                     outliers: the predicted chi2              */
+  double* state_path_length;
+  double* predicted;              /* C = 6 */
+  double* predicted_cov;          /* C = 21 */
+  double* filtered;               /* C = 6 (outliers and holes: predicted)     */
+  double* filtered_cov;           /* C = 21 */
+  double* jacobian;               /* C = 36, transport from the previous state */
+} ck_ckf_out;
+
+ck_status ck_find_tracks(ck_handle* h, const ck_options* options,
+                         const ck_ckf_options* ckf, const ck_ckf_in* in,
+                         ck_ckf_out* out, void* stream);
 
 /* ------------------------------------------------------------- serving */
 

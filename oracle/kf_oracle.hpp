@@ -2315,8 +2315,15 @@ struct Fitter {
         st.stepSize.release(kNav);
         st.stepSize.release(kActor);
         if (haveTarget) {
+          // a branch restart keeps the previous branch's target
+          // (DirectNavigator::checkTargetValid is always true) while the
+          // sequence index restarts; with the index before the sequence
+          // start no current surface is set (the reference's navSurface()
+          // would throw there)
           IStatus post = surfaceStatus(targetSurf, targetIdx);
-          if (post == IStatus::onSurface && !navigationBreak) currentSurface = seq[surfaceIndex];
+          if (post == IStatus::onSurface && !navigationBreak && surfaceIndex >= 0 &&
+              surfaceIndex < nSeq)
+            currentSurface = seq[surfaceIndex];
           if (post != IStatus::reachable) haveTarget = false;
         }
         err = act();
@@ -2339,6 +2346,522 @@ struct Fitter {
     (void)missedActive;
     p.lastMeasurementIndex = lastMeasurementIndex;
     p.measurementStates = measurementStates;
+    return err;
+  }
+
+  // ---------------------------------------------------- track finding (CKF)
+  // A track state of the CKF's trajectory and a branch (TrackProxy: its tip
+  // and summary counters).
+  struct CkfState {
+    int surface = -1, prev = -1, meas = -1;
+    uint32_t flags = 0;
+    S chi2 = S(0.0), pathLength = S(0.0);
+    Vec<S, 6> pred, filt;
+    Mat<S, 6, 6> predCov, filtCov, jac;
+  };
+  struct CkfBranch {
+    int tip = -1;
+    int nMeas = 0, nHoles = 0, nOutliers = 0, ndf = 0;
+    S chi2 = S(0.0);
+    bool hasParams = false;
+    Vec<S, 6> params;
+    Mat<S, 6, 6> cov;
+  };
+  struct CkfCuts {
+    double chi2Cut, chi2CutOutlier;
+    int maxCandidates, minMeasurements, maxHoles, maxOutliers, maxHolesAndOutliers;
+    int target, maxStates, maxTracks, maxBranches;
+    // the end of the seed's sequence ends a branch as the end of the world
+    // ends it with the geometry Navigator (EndOfWorldReached)
+    bool endOfWorld;
+    // the target's bounds (0: unbounded): rectangle half lengths of a
+    // plane, the half length in z of a cylinder
+    double targetHalfX, targetHalfY, targetHalfZ;
+  };
+  // the event's measurements grouped by surface
+  struct CkfMeas {
+    const int* offsets;  // [n_surfaces + 1]
+    const double* values;
+    const double* cov;
+    const int* sub;  // or nullptr
+    MeasRec<S> get(int m, int sid) const {
+      MeasRec<S> r;
+      r.surface = sid;
+      r.sub = sub ? sub[m] : CK_MEAS_LOC01;
+      for (int c = 0; c < 2; ++c) r.v[c] = values[2 * (size_t)m + c];
+      for (int c = 0; c < 4; ++c) r.cov[c] = cov[4 * (size_t)m + c];
+      return r;
+    }
+  };
+
+  // CombinatorialKalmanFilter::findTracks
+  // (CombinatorialKalmanFilter.hpp:1191-1335) with the DirectNavigator over
+  // `seq`: the propagation loop of Propagator.ipp:25-210 with the CKF actor
+  // (Actor::act :322-448, filter :548-822, processNewTrackStates :836-898,
+  // addNonSourcelinkState :900-946, reset :460-531), the default
+  // TrackStateCreator (TrackStateCreator.hpp:89-296) with the
+  // MeasurementSelector (MeasurementSelector.ipp:19-124, single cut bin) and
+  // the examples' branch stopper (TrackFindingAlgorithm.cpp:203-261). The
+  // propagator's step counter runs over all branches of the seed; the CKF's
+  // path aborter is the loop protection alone (a stub replaces the
+  // propagator's own). Returns CK_TRACK_OK or the error of the search.
+  int ckfSeed(const Surface<S>& startSurface, const Vec<S, 6>& startPars,
+              const Mat<S, 6, 6>& startCov, float mass, float absQ, int absPdg, const int* seq,
+              int nSeq, const CkfMeas& M, const CkfCuts& cuts, std::vector<CkfState>& states,
+              std::vector<CkfBranch>& tracks) const {
+    using std::abs;
+    const std::vector<Surface<S>>& sf = *surfaces;
+    states.clear();
+    tracks.clear();
+    Stepper<S> st;
+    st.mass = mass;
+    st.absQ = absQ;
+    st.absPdg = absPdg;
+    // EigenStepper::initialize (EigenStepper.ipp:37-70)
+    auto initialize = [&](const Surface<S>& s, const Vec<S, 6>& bp, const Mat<S, 6, 6>& c) {
+      st.pars = boundToFree(s, bp);
+      st.pathAccumulated = S(0.0);
+      st.nSteps = 0;
+      st.stepSize = ConstrainedStep();
+      st.stepSize.accuracy = o.initialStepSize;
+      st.stepSize.values[kUser] = o.maxStepSize;
+      st.cov = c;
+      st.jacToGlobal = s.boundToFreeJacobian(st.pos(), st.dir());
+      st.jacobian = Mat<S, 6, 6>::identity();
+      st.jacTransport = Mat<S, 8, 8>::identity();
+      st.derivative = Vec<S, 8>::zero();
+    };
+    initialize(startSurface, startPars, startCov);
+
+    auto loopLimit = [&]() -> double {
+      double limit = std::numeric_limits<double>::max();  // (release)
+      if (!o.loopProtection) return limit;
+      V3<S> B;
+      if (!field.get(st.pos(), B)) return limit;
+      double Bn = (double)norm(B);
+      if (Bn == 0) return limit;
+      double ll = o.loopFraction * (2 * kPi * (double)st.absoluteMomentum() / Bn);
+      if (std::abs(ll) < std::abs(limit)) limit = ll;
+      return limit;
+    };
+    double pathLimit = std::numeric_limits<double>::max();
+    bool pathLimitSet = false;
+    auto pathLimitCheck = [&]() -> bool {
+      double distance = std::abs(pathLimit) - std::abs((double)st.pathAccumulated);
+      if (std::abs(distance) < std::abs(o.surfaceTolerance)) return true;
+      st.stepSize.update(distance, kActor);
+      return false;
+    };
+
+    // navigator (DirectNavigator.hpp:222-348)
+    int surfaceIndex = -1;
+    bool navigationBreak = false;
+    int currentSurface = -1;  // the seed's plane is not in the table
+    int targetSurf = -1, targetIdx = 0;
+    bool haveTarget = false;
+    auto nextTargetNav = [&]() -> bool {
+      currentSurface = -1;
+      if (navigationBreak) return false;
+      ++surfaceIndex;
+      while (surfaceIndex >= 0 && surfaceIndex < nSeq) {
+        Intersection<S> is[2];
+        const int ni = sf[seq[surfaceIndex]].intersect(st.pos(), st.dir(), S(o.surfaceTolerance), is);
+        for (int i = 0; i < ni; ++i) {
+          S pl = is[i].pathLength;
+          if (is[i].valid() && pl > S(o.nearLimit) &&
+              pl < S(std::numeric_limits<double>::max()) + S(kOnSurfaceTolerance)) {
+            targetSurf = seq[surfaceIndex];
+            targetIdx = i;
+            return true;
+          }
+        }
+        ++surfaceIndex;
+      }
+      navigationBreak = true;
+      return false;
+    };
+    auto surfaceStatus = [&](int sid, int idx) -> IStatus {
+      Intersection<S> is[2];
+      sf[sid].intersect(st.pos(), st.dir(), S(o.surfaceTolerance), is);
+      Intersection<S> x = is[idx];
+      if (x.valid()) {
+        st.stepSize.release(kNav);
+        st.stepSize.update((double)x.pathLength, kNav);
+      }
+      return x.status;
+    };
+    auto getNextTarget = [&](int& e) -> bool {
+      e = CK_TRACK_OK;
+      for (unsigned i = 0; i < o.maxTargetSkipping; ++i) {
+        if (!nextTargetNav()) return false;
+        IStatus stt = surfaceStatus(targetSurf, targetIdx);
+        if (stt == IStatus::onSurface) continue;
+        if (stt == IStatus::reachable) return true;
+      }
+      e = CK_TRACK_NEXT_TARGET_LIMIT;
+      return false;
+    };
+
+    // PointwiseMaterialInteraction (forward; mode 1 pre, 2 post); on the
+    // navigator's start surface (the surface a branch restarts from) only
+    // the post-update part applies (PointwiseMaterialInteraction.cpp:16-29)
+    int startSid = -1;
+    auto material = [&](int sid, const Surface<S>& s, int mode) -> bool {
+      if (sid == startSid) mode &= 2;
+      if (mode == 0 || !s.hasMaterial) return true;
+      V3<S> pos = st.pos(), dir = st.dir();
+      S pc = s.pathCorrection(pos, dir);
+      S loc[2];
+      if (!s.globalToLocal(pos, dir, S(kOnSurfaceTolerance), loc)) return false;
+      Slab slab = s.slab;
+      if (!slab.isVacuum()) {
+        const double split = (double)s.splitFactor;
+        const double factor = mode == 1 ? 1.0 - split : split;
+        if (factor == 0.0) return true;
+        slab.scaleThickness((float)factor);
+      }
+      slab.scaleThickness((float)(double)pc);
+      if (slab.isVacuum()) return true;
+      const float qOverPf = (float)(double)st.qop();
+      MatEffects e = computeMaterialEffects<S>(mc, slab, st.absPdg, (double)st.mass,
+                                               (double)st.absQ, dir, qOverPf,
+                                               o.multipleScattering, o.energyLoss);
+      const double massd = (double)st.mass;
+      const double momentum = (double)st.absoluteMomentum();
+      const double nextE = std::sqrt(massd * massd + momentum * momentum) - e.eLoss;
+      double nextP = 0.0;
+      if (massd < nextE) {
+        double am = std::abs(massd);
+        nextP = std::sqrt((nextE - am) * (nextE + am));
+      }
+      nextP = std::max(10 * kMeV, nextP);
+      const float signedQ = (float)std::copysign((double)st.absQ, (double)qOverPf);
+      st.pars[7] = S((double)signedQ / nextP);
+      auto upd = [](S var, double change) { return S(std::max(0.0, (double)var + change)); };
+      st.cov.a[2][2] = upd(st.cov.a[2][2], e.variancePhi);
+      st.cov.a[3][3] = upd(st.cov.a[3][3], e.varianceTheta);
+      st.cov.a[4][4] = upd(st.cov.a[4][4], e.varianceQoverP);
+      return true;
+    };
+
+    std::vector<CkfBranch> active(1);
+    bool finished = false;
+    int err = CK_TRACK_OK;
+
+    auto store = [&]() -> int {
+      if ((int)tracks.size() >= cuts.maxTracks) return CK_TRACK_TOO_MANY_STATES;
+      tracks.push_back(active.back());
+      return CK_TRACK_OK;
+    };
+    // the examples' branch stopper: 0 continue, 1 stop and keep, 2 stop and drop
+    auto stopper = [&](const CkfBranch& b) -> int {
+      const bool tooMany = b.nHoles > cuts.maxHoles || b.nOutliers > cuts.maxOutliers ||
+                           b.nHoles + b.nOutliers > cuts.maxHolesAndOutliers;
+      if (!tooMany) return 0;
+      return b.nMeas >= cuts.minMeasurements ? 1 : 2;
+    };
+    auto targetCheck = [&](bool& reached) {
+      // SurfaceReached with an unlimited near limit (the actor's
+      // targetReached, CombinatorialKalmanFilter.hpp:259;
+      // StandardAborters.hpp:94-155): reached when the navigator's current
+      // surface is the target, else when the closest intersection within
+      // the target's bounds (BoundaryTolerance::None) is on the surface
+      reached = false;
+      if (cuts.target < 0) return;
+      if (currentSurface == cuts.target) {
+        reached = true;
+        return;
+      }
+      const Surface<S>& ts = sf[cuts.target];
+      Intersection<S> is[2];
+      const int ni = ts.intersect(st.pos(), st.dir(), S(o.surfaceTolerance), is);
+      for (int i = 0; i < ni; ++i) {
+        if (!is[i].valid()) continue;
+        V3<S> p;
+        for (int k = 0; k < 3; ++k) p[k] = st.pos()[k] + is[i].pathLength * st.dir()[k];
+        const V3<S> l = ts.toLocal3(p);
+        bool inside = true;
+        if (ts.type == CK_SURFACE_CYLINDER && cuts.targetHalfZ > 0)
+          inside = abs((double)l[2]) < abs(cuts.targetHalfZ + o.surfaceTolerance);
+        else if (ts.type == CK_SURFACE_PLANE && cuts.targetHalfX > 0 && cuts.targetHalfY > 0)
+          inside = (double)l[0] >= -cuts.targetHalfX && (double)l[0] <= cuts.targetHalfX &&
+                   (double)l[1] >= -cuts.targetHalfY && (double)l[1] <= cuts.targetHalfY;
+        if (!inside) is[i].status = IStatus::unreachable;
+      }
+      int best = -1;
+      for (int i = 0; i < ni; ++i)
+        if (is[i].valid() && (best < 0 || abs(is[i].pathLength) < abs(is[best].pathLength)))
+          best = i;
+      reached = best >= 0 && is[best].status == IStatus::onSurface;
+      for (int i = 0; i < ni; ++i)
+        if (is[i].valid() &&
+            (double)is[i].pathLength < std::numeric_limits<double>::max() + kOnSurfaceTolerance) {
+          st.stepSize.release(kActor);
+          st.stepSize.update((double)is[i].pathLength, kActor);
+          break;
+        }
+    };
+    // Actor::reset: the next active branch from its outermost state
+    auto reset = [&]() -> int {
+      if (active.empty()) {
+        finished = true;
+        return CK_TRACK_OK;
+      }
+      const CkfState& cs = states[active.back().tip];
+      const Surface<S>& s = sf[cs.surface];
+      initialize(s, cs.filt, cs.filtCov);
+      currentSurface = cs.surface;
+      surfaceIndex = -1;
+      for (int k = 0; k < nSeq; ++k)
+        if (seq[k] == cs.surface) {
+          surfaceIndex = k - 1;
+          break;
+        }
+      navigationBreak = false;
+      startSid = cs.surface;
+      if (!material(cs.surface, s, 2)) return CK_TRACK_NOT_ON_SURFACE;
+      pathLimit = loopLimit();
+      bool dummy;
+      targetCheck(dummy);
+      return CK_TRACK_OK;
+    };
+    auto filter = [&](int sid) -> int {
+      const Surface<S>& s = sf[sid];
+      if (!s.sensitive && !s.hasMaterial) return CK_TRACK_OK;  // passive
+      if (!s.sensitive) return CK_TRACK_INVALID_INPUT;          // material-only
+      transportCovarianceToBound(st, s);
+      if (!material(sid, s, 1)) return CK_TRACK_NOT_ON_SURFACE;
+      Vec<S, 6> bp;
+      if (!freeToBound(st.pars, s, bp)) return CK_TRACK_NOT_ON_SURFACE;
+      const int prevTip = active.back().tip;
+      // TrackStateCreator + MeasurementSelector
+      const int m0 = M.offsets[sid], m1 = M.offsets[sid + 1];
+      struct Cand {
+        int m;
+        S chi2;
+      };
+      std::vector<Cand> cands;
+      for (int m = m0; m < m1; ++m) {
+        const MeasRec<S> mr = M.get(m, sid);
+        if (mr.sub < CK_MEAS_LOC0 || mr.sub > CK_MEAS_LOC01) return CK_TRACK_INVALID_INPUT;
+        cands.push_back({m, predictedChi2Sub(bp, st.cov, mr)});
+      }
+      std::vector<Cand> sel;
+      bool isOutlier = false;
+      if (!cands.empty()) {
+        S minChi2 = S(std::numeric_limits<double>::max());
+        int minIndex = -1;
+        std::vector<Cand> passed;
+        for (size_t i = 0; i < cands.size(); ++i) {
+          if (cands[i].chi2 < minChi2) {
+            minChi2 = cands[i].chi2;
+            minIndex = (int)i;
+          }
+          if (!(cands[i].chi2 >= S(cuts.chi2Cut))) passed.push_back(cands[i]);
+        }
+        if (passed.empty()) {
+          if (minChi2 < S(cuts.chi2CutOutlier)) {
+            sel.push_back(cands[minIndex]);
+            isOutlier = true;
+          }
+        } else {
+          std::stable_sort(passed.begin(), passed.end(),
+                           [](const Cand& a, const Cand& b) { return a.chi2 < b.chi2; });
+          const size_t k = std::min(passed.size(), (size_t)cuts.maxCandidates);
+          sel.assign(passed.begin(), passed.begin() + k);
+        }
+      }
+      const uint32_t matFlag = s.hasMaterial ? CK_FLAG_HAS_MATERIAL : 0u;
+      if (!sel.empty()) {
+        // new states (the selected candidates in ascending chi2)
+        const int first = (int)states.size();
+        if (first + (int)sel.size() > cuts.maxStates) return CK_TRACK_TOO_MANY_STATES;
+        for (const Cand& c : sel) {
+          CkfState x;
+          x.surface = sid;
+          x.prev = prevTip;
+          x.meas = c.m;
+          x.flags = CK_FLAG_HAS_PARAMETERS | CK_FLAG_HAS_MEASUREMENT | matFlag |
+                    (isOutlier ? CK_FLAG_IS_OUTLIER : 0u);
+          x.chi2 = c.chi2;
+          x.pathLength = st.pathAccumulated;
+          x.pred = bp;
+          x.predCov = st.cov;
+          x.jac = st.jacobian;
+          states.push_back(x);
+        }
+        // processNewTrackStates: the new branches from the worst candidate to
+        // the best (the best on top of the stack)
+        const CkfBranch root = active.back();
+        active.pop_back();
+        int onSurface = 0;
+        for (int i = (int)sel.size() - 1; i >= 0; --i) {
+          CkfBranch b = root;
+          b.tip = first + i;
+          CkfState& x = states[b.tip];
+          if (isOutlier) {
+            x.filt = x.pred;
+            x.filtCov = x.predCov;
+            ++b.nOutliers;
+          } else {
+            S c2;
+            const MeasRec<S> m = M.get(x.meas, sid);
+            if (!gainMatrixUpdateSub(x.pred, x.predCov, m, o.josephs, x.filt, x.filtCov, c2))
+              return CK_TRACK_UPDATE_FAILED;
+            x.chi2 = c2;
+            ++b.nMeas;
+            b.ndf += (m.sub & 1) + ((m.sub >> 1) & 1);
+            b.chi2 = b.chi2 + c2;
+          }
+          if ((int)active.size() >= cuts.maxBranches) return CK_TRACK_TOO_MANY_STATES;
+          active.push_back(b);
+          const int r = stopper(b);
+          if (r == 0) {
+            ++onSurface;
+          } else {
+            if (r == 1) {
+              const int e = store();
+              if (e != CK_TRACK_OK) return e;
+            }
+            active.pop_back();
+          }
+        }
+        if (onSurface == 0) return reset();
+      } else {
+        // a hole (a sensitive surface without a selected measurement)
+        if ((int)states.size() >= cuts.maxStates) return CK_TRACK_TOO_MANY_STATES;
+        CkfState x;
+        x.surface = sid;
+        x.prev = prevTip;
+        x.flags = CK_FLAG_HAS_PARAMETERS | CK_FLAG_IS_HOLE | matFlag;
+        x.pathLength = st.pathAccumulated;
+        x.pred = bp;
+        x.predCov = st.cov;
+        x.jac = st.jacobian;
+        x.filt = bp;
+        x.filtCov = st.cov;
+        states.push_back(x);
+        CkfBranch& b = active.back();
+        b.tip = (int)states.size() - 1;
+        ++b.nHoles;
+        const int r = stopper(b);
+        if (r != 0) {
+          if (r == 1) {
+            const int e = store();
+            if (e != CK_TRACK_OK) return e;
+          }
+          active.pop_back();
+          return reset();
+        }
+      }
+      const CkfState& cur = states[active.back().tip];
+      if ((cur.flags & CK_FLAG_HAS_MEASUREMENT) && !(cur.flags & CK_FLAG_IS_OUTLIER)) {
+        // stepper.update with the filtered parameters (EigenStepper.ipp:128-138)
+        st.pars = boundToFree(s, cur.filt);
+        st.cov = cur.filtCov;
+        st.jacToGlobal = s.boundToFreeJacobian(st.pos(), st.dir());
+      }
+      if (!material(sid, s, 2)) return CK_TRACK_NOT_ON_SURFACE;
+      return CK_TRACK_OK;
+    };
+    auto act = [&]() -> int {
+      if (!pathLimitSet) {
+        pathLimit = loopLimit();
+        pathLimitSet = true;
+      }
+      if (currentSurface >= 0) {
+        const int r = filter(currentSurface);
+        if (r != CK_TRACK_OK) return r;
+        if (finished) return CK_TRACK_OK;
+      }
+      const bool pathReached = pathLimitCheck();
+      bool targetReached = false;
+      targetCheck(targetReached);
+      if (pathReached || targetReached) {
+        if (!pathReached) {
+          Vec<S, 6> bp;
+          if (!freeToBound(st.pars, sf[cuts.target], bp)) return CK_TRACK_NOT_ON_SURFACE;
+          transportCovarianceToBound(st, sf[cuts.target]);
+          active.back().hasParams = true;
+          active.back().params = bp;
+          active.back().cov = st.cov;
+          st.stepSize.release(kNav);
+        }
+        const int e = store();
+        if (e != CK_TRACK_OK) return e;
+        active.pop_back();
+        return reset();
+      }
+      return CK_TRACK_OK;
+    };
+
+    // the navigator's next target (Propagator.ipp:79-96, 166-181); with
+    // endOfWorld a branch whose navigator has no surface of the sequence
+    // left ends there, kept, as EndOfWorldReached ends it in Actor::act
+    // (CombinatorialKalmanFilter.hpp:392-436), and the next branch restarts
+    auto nextTarget = [&](bool release) -> int {
+      while (true) {
+        if (!haveTarget) {
+          if (release) st.stepSize.release(kNav);
+          int e;
+          haveTarget = getNextTarget(e);
+          if (e != CK_TRACK_OK) return e;
+        }
+        if (!(cuts.endOfWorld && navigationBreak)) return CK_TRACK_OK;
+        int e = store();
+        if (e != CK_TRACK_OK) return e;
+        active.pop_back();
+        e = reset();
+        if (e != CK_TRACK_OK || finished) return e;
+        release = true;
+      }
+    };
+
+    // ---- Propagator::propagate (Propagator.ipp:25-210)
+    err = act();
+    if (err == CK_TRACK_OK && !finished) {
+      err = nextTarget(false);
+      bool terminated = finished;
+      unsigned steps = 0;
+      for (; err == CK_TRACK_OK && !terminated && steps < o.maxSteps; ++steps) {
+        S h;
+        int se = eigenStep(st, field, o, h, 1);
+        if (se != kStepOk) {
+          err = se == kStepField ? CK_TRACK_FIELD_OUT_OF_BOUNDS
+                                 : (se == kStepStalled ? CK_TRACK_STEP_SIZE_STALLED
+                                                       : CK_TRACK_STEP_ADJUST_FAILED);
+          break;
+        }
+        st.stepSize.release(kNav);
+        st.stepSize.release(kActor);
+        if (haveTarget) {
+          // a branch restart keeps the previous branch's target
+          // (DirectNavigator::checkTargetValid is always true) while the
+          // sequence index restarts; with the index before the sequence
+          // start no current surface is set (the reference's navSurface()
+          // would throw there)
+          IStatus post = surfaceStatus(targetSurf, targetIdx);
+          if (post == IStatus::onSurface && !navigationBreak && surfaceIndex >= 0 &&
+              surfaceIndex < nSeq)
+            currentSurface = seq[surfaceIndex];
+          if (post != IStatus::reachable) haveTarget = false;
+        }
+        err = act();
+        if (err != CK_TRACK_OK) break;
+        if (finished) {
+          terminated = true;
+          break;
+        }
+        err = nextTarget(true);
+        if (err != CK_TRACK_OK) break;
+        if (finished) {
+          terminated = true;
+          break;
+        }
+      }
+      if (err == CK_TRACK_OK && !terminated) err = CK_TRACK_STEP_COUNT_LIMIT;
+    }
+    if (err != CK_TRACK_OK) tracks.clear();
     return err;
   }
 

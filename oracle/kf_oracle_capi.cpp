@@ -389,6 +389,106 @@ void kfo_propagate(const ck_options* opt, int n_surfaces, const ck_surface* surf
   }
 }
 
+// The track-finding restatement on host arrays in ck_find_tracks's layout.
+void kfo_find_tracks(const ck_options* opt, int n_surfaces, const ck_surface* surfaces,
+                     const ck_field* field, const ck_ckf_options* ck, const ck_ckf_in* in,
+                     ck_ckf_out* out, int n_threads) {
+  Ctx ctx;
+  for (int i = 0; i < n_surfaces; ++i) ctx.surfaces.push_back(Surface<double>::fromCk(surfaces[i]));
+  ctx.fitter.surfaces = &ctx.surfaces;
+  ctx.fitter.field = Field<double>::make(*field);
+  ctx.fitter.mc = MatConst::make();
+  ctx.fitter.o = Options::fromCk(*opt, true);
+  using F = Fitter<double>;
+  F::CkfCuts cuts{ck->chi2_cut,        ck->chi2_cut_outlier, ck->max_candidates,
+                  ck->min_measurements, ck->max_holes,        ck->max_outliers,
+                  ck->max_holes_and_outliers, ck->target_surface, ck->max_states,
+                  ck->max_tracks,      ck->max_branches, ck->end_of_world != 0,
+                  0.0,                 0.0,                  0.0};
+  if (ck->target_surface >= 0 && ck->target_surface < n_surfaces) {
+    const ck_surface& t = surfaces[ck->target_surface];
+    cuts.targetHalfX = t.half_x;
+    cuts.targetHalfY = t.half_y;
+    cuts.targetHalfZ = t.half_length_z;
+  }
+  F::CkfMeas M{in->surf_meas_offsets, in->meas_values, in->meas_cov, in->meas_subspace};
+  const int n = in->n_seeds, S = ck->max_states, T = ck->max_tracks;
+  std::atomic<int> next{0};
+  auto worker = [&]() {
+    std::vector<F::CkfState> states;
+    std::vector<F::CkfBranch> tracks;
+    while (true) {
+      const int s = next.fetch_add(1);
+      if (s >= n) break;
+      int st = CK_TRACK_OK;
+      for (int k = in->seq_offsets[s]; k < in->seq_offsets[s + 1]; ++k) {
+        const int sid = in->seq_surfaces[k];
+        if (sid < 0 || sid >= n_surfaces || ctx.surfaces[sid].type == CK_SURFACE_LINE)
+          st = CK_TRACK_INVALID_INPUT;
+      }
+      states.clear();
+      tracks.clear();
+      if (st == CK_TRACK_OK) {
+        const Surface<double> start = Surface<double>::plane(in->start_frames + 12 * (size_t)s);
+        st = ctx.fitter.ckfSeed(start, get6<double>(in->start_params + 6 * (size_t)s),
+                                get36<double>(in->start_cov + 36 * (size_t)s),
+                                in->particle[2 * (size_t)s], in->particle[2 * (size_t)s + 1],
+                                in->particle_pdg ? in->particle_pdg[s] : 211,
+                                in->seq_surfaces + in->seq_offsets[s],
+                                in->seq_offsets[s + 1] - in->seq_offsets[s], M, cuts, states,
+                                tracks);
+      }
+      out->status[s] = st;
+      out->n_tracks[s] = st == CK_TRACK_OK ? (int)tracks.size() : 0;
+      out->n_states[s] = st == CK_TRACK_OK ? (int)states.size() : 0;
+      if (st != CK_TRACK_OK) continue;
+      for (int k = 0; k < (int)tracks.size(); ++k) {
+        const F::CkfBranch& b = tracks[k];
+        const size_t i = (size_t)s * T + k;
+        out->track_tip[i] = b.tip;
+        out->track_n_measurements[i] = b.nMeas;
+        out->track_n_holes[i] = b.nHoles;
+        out->track_n_outliers[i] = b.nOutliers;
+        out->track_ndf[i] = b.ndf;
+        out->track_chi2[i] = b.chi2;
+        for (int c = 0; c < 6; ++c)
+          out->track_params[i * 6 + c] = b.hasParams ? b.params[c] : std::nan("");
+        for (int r = 0, c = 0; r < 6; ++r)
+          for (int q = r; q < 6; ++q, ++c)
+            out->track_cov[i * 21 + c] = b.hasParams ? b.cov.a[r][q] : std::nan("");
+      }
+      for (int k = 0; k < (int)states.size(); ++k) {
+        const F::CkfState& x = states[k];
+        const size_t i = (size_t)s * S + k;
+        out->state_prev[i] = x.prev;
+        out->state_surface[i] = x.surface;
+        out->state_flags[i] = x.flags;
+        out->state_measurement[i] = x.meas;
+        out->state_chi2[i] = x.chi2;
+        out->state_path_length[i] = x.pathLength;
+        for (int c = 0; c < 6; ++c) {
+          out->predicted[i * 6 + c] = x.pred[c];
+          out->filtered[i * 6 + c] = x.filt[c];
+        }
+        for (int r = 0, c = 0; r < 6; ++r)
+          for (int q = r; q < 6; ++q, ++c) {
+            out->predicted_cov[i * 21 + c] = x.predCov.a[r][q];
+            out->filtered_cov[i * 21 + c] = x.filtCov.a[r][q];
+          }
+        for (int r = 0; r < 6; ++r)
+          for (int q = 0; q < 6; ++q) out->jacobian[i * 36 + r * 6 + q] = x.jac.a[r][q];
+      }
+    }
+  };
+  if (n_threads <= 1) {
+    worker();
+  } else {
+    std::vector<std::thread> th;
+    for (int i = 0; i < n_threads; ++i) th.emplace_back(worker);
+    for (auto& x : th) x.join();
+  }
+}
+
 // Counts how often glibc logf differs from the correctly rounded float
 // logarithm used by both implementations, over n inputs.
 int kfo_logf_mismatch(int n, const float* x) {

@@ -54,6 +54,11 @@ def lib():
         L.kfo_propagate.argtypes = [C.POINTER(abi.ck_options), C.c_int, C.POINTER(abi.ck_surface),
                                     C.POINTER(abi.ck_field), C.POINTER(abi.ck_propagate_in),
                                     C.POINTER(abi.ck_propagate_out), C.c_int]
+        L.kfo_find_tracks.restype = None
+        L.kfo_find_tracks.argtypes = [C.POINTER(abi.ck_options), C.c_int,
+                                      C.POINTER(abi.ck_surface), C.POINTER(abi.ck_field),
+                                      C.POINTER(abi.ck_ckf_options), C.POINTER(abi.ck_ckf_in),
+                                      C.POINTER(abi.ck_ckf_out), C.c_int]
         L.kfo_logf_mismatch.restype = C.c_int
         L.kfo_logf_mismatch.argtypes = [C.c_int, abi.P_f32]
         L.kfo_hardware_threads.restype = C.c_int
@@ -185,6 +190,14 @@ def propagate(surfaces, field, options, prop, n_threads=1):
     lib().kfo_propagate(C.byref(options), n_surf, surfaces, C.byref(field), C.byref(i),
                         C.byref(o), n_threads)
     return prop
+
+
+def find_tracks(surfaces, field, options, ckf_options, tf, n_threads=1):
+    """The track-finding restatement on an abi.TrackFinding (filled in place)."""
+    i, o = tf.as_in(), tf.as_out()
+    lib().kfo_find_tracks(C.byref(options), len(surfaces), surfaces, C.byref(field),
+                          C.byref(ckf_options), C.byref(i), C.byref(o), n_threads)
+    return tf
 
 
 def logf_mismatch(x):

@@ -46,11 +46,11 @@ def test_generator_exports_every_declared_symbol():
 
 def test_struct_layouts_match(cklib):
     cklib.ck_abi_struct_sizes.argtypes = [C.POINTER(C.c_int64), C.c_int32]
-    out = (C.c_int64 * 9)()
-    cklib.ck_abi_struct_sizes(out, 9)
+    out = (C.c_int64 * 12)()
+    cklib.ck_abi_struct_sizes(out, 12)
     mirrors = [abi.ck_surface, abi.ck_field, abi.ck_options, abi.ck_config, abi.ck_batch_in,
                abi.ck_batch_out, abi.ck_server_config, abi.ck_propagate_in,
-               abi.ck_propagate_out]
+               abi.ck_propagate_out, abi.ck_ckf_options, abi.ck_ckf_in, abi.ck_ckf_out]
     assert [C.sizeof(m) for m in mirrors] == list(out)
 
 
@@ -62,6 +62,12 @@ def test_api_version_and_defaults(cklib):
     ref = abi.default_options()
     for name, _ in abi.ck_options._fields_:
         assert getattr(o, name) == getattr(ref, name), name
+    # the track finder's defaults (MeasurementSelectorCuts, no branch stopping)
+    k = abi.ck_ckf_options()
+    cklib.ck_ckf_options_default(C.byref(k))
+    kref = abi.ckf_options()
+    for name, _ in abi.ck_ckf_options._fields_:
+        assert getattr(k, name) == getattr(kref, name), name
 
 
 def test_create_without_gpu_fails_loudly(cklib):
