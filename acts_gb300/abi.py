@@ -308,6 +308,8 @@ class ck_ckf_options(C.Structure):
         ("max_tracks", C.c_int32),
         ("max_branches", C.c_int32),
         ("end_of_world", C.c_int32),
+        ("lanes_per_seed", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 

@@ -109,6 +109,7 @@ int gridBlocksFor(ck_handle* h, const Tune& tn);
 struct ck_handle {
   int device = 0;
   int smCount = 1;
+  int lastCkfLanes = 0;  // lanes per seed of the last ck_find_tracks launch
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evMid = nullptr;
   ck::DevSurface* dSurfaces = nullptr;

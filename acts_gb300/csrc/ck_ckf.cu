@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 #include <math_constants.h>
 
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -51,7 +52,43 @@ struct CkfParams {
   CkfBranch* branches;           // [n_seeds * max_branches]
 };
 
-template <typename P, typename CV>
+// Group operations of the G lanes that share a seed (G divides 32; the
+// group's lanes are consecutive and run the same control flow on the same
+// data, so they meet at every shuffle)
+template <int G>
+CK_D unsigned groupMask() {
+  if constexpr (G == 32) {
+    return 0xffffffffu;
+  } else {
+    const int base = (threadIdx.x & 31) & ~(G - 1);
+    return ((1u << G) - 1u) << base;
+  }
+}
+// lexicographic minimum of (chi2, measurement index) over the group
+template <int G>
+CK_D void groupArgMin(unsigned mask, double& c, int& m) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    const double oc = __shfl_xor_sync(mask, c, o, G);
+    const int om = __shfl_xor_sync(mask, m, o, G);
+    if (oc < c || (oc == c && om < m)) {
+      c = oc;
+      m = om;
+    }
+  }
+}
+template <int G>
+CK_D int groupSum(unsigned mask, int v) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o, G);
+  return v;
+}
+
+// G lanes per seed: every lane of the group runs the seed's search on the
+// same values (identical stores to the same addresses); the candidate scan
+// of a surface is split over the group and merged by shuffles, with the
+// result of the serial scan (ties in input order).
+template <typename P, typename CV, int G>
 struct CkfLane : Lane<P, CV> {
   using B = Lane<P, CV>;
   using B::absQ;
@@ -276,9 +313,14 @@ struct CkfLane : Lane<P, CV> {
     int nSel = 0, nPassed = 0, minM = -1;
     double minChi2 = kNotSet;
     const int K = cp.o.max_candidates;
-    for (int m = m0; m < m1; ++m) {
+    const int gl = (int)(threadIdx.x & (G - 1));  // this lane's share: m0 + gl, m0 + gl + G, ...
+    bool badSub = false;
+    for (int m = m0 + gl; m < m1; m += G) {
       const int sub = fp.meas_sub ? __ldg(&fp.meas_sub[m]) : CK_MEAS_LOC01;
-      if (sub < CK_MEAS_LOC0 || sub > CK_MEAS_LOC01) return CK_TRACK_INVALID_INPUT;
+      if (sub < CK_MEAS_LOC0 || sub > CK_MEAS_LOC01) {
+        badSub = true;
+        break;
+      }
       double V[4];
 #pragma unroll
       for (int c = 0; c < 4; ++c) V[c] = __ldg(&fp.meas_cov[4 * (size_t)m + c]);
@@ -302,6 +344,38 @@ struct CkfLane : Lane<P, CV> {
           if (nSel < K) ++nSel;
         }
       }
+    }
+    if constexpr (G > 1) {
+      // merge the group's partial scans: counts, the first minimum, and the
+      // K smallest (chi2, index) pairs, popped one by one from the lanes'
+      // sorted lists
+      const unsigned mask = groupMask<G>();
+      if (groupSum<G>(mask, badSub ? 1 : 0)) return CK_TRACK_INVALID_INPUT;
+      nPassed = groupSum<G>(mask, nPassed);
+      double mc = minM >= 0 ? minChi2 : CUDART_INF;
+      int mm = minM >= 0 ? minM : INT_MAX;
+      groupArgMin<G>(mask, mc, mm);
+      minM = mm == INT_MAX ? -1 : mm;
+      minChi2 = mm == INT_MAX ? kNotSet : mc;
+      int outM[kCkfMaxCandidates];
+      double outC[kCkfMaxCandidates];
+      int h = 0, n = 0;
+      for (; n < K; ++n) {
+        double c = h < nSel ? selC[h] : CUDART_INF;
+        int m = h < nSel ? selM[h] : INT_MAX;
+        groupArgMin<G>(mask, c, m);
+        if (m == INT_MAX) break;
+        outC[n] = c;
+        outM[n] = m;
+        if (h < nSel && selM[h] == m) ++h;
+      }
+      nSel = n;
+      for (int i = 0; i < n; ++i) {
+        selC[i] = outC[i];
+        selM[i] = outM[i];
+      }
+    } else {
+      if (badSub) return CK_TRACK_INVALID_INPUT;
     }
     bool isOutlier = false;
     if (nPassed == 0 && minM >= 0 && minChi2 < cp.o.chi2_cut_outlier) {
@@ -527,11 +601,12 @@ struct CkfLane : Lane<P, CV> {
   }
 };
 
-template <typename P, typename CV>
+template <typename P, typename CV, int G>
 __global__ void __launch_bounds__(kCkfBlock) ckfKernel(FitParams fp, CkfParams cp) {
-  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < fp.n_tracks;
-       s += gridDim.x * blockDim.x) {
-    CkfLane<P, CV> L;
+  static_assert(G >= 1 && G <= 32 && (32 % G) == 0, "lanes per seed");
+  for (int s = (int)((blockIdx.x * blockDim.x + threadIdx.x) / G); s < fp.n_tracks;
+       s += (int)(gridDim.x * blockDim.x / G)) {
+    CkfLane<P, CV, G> L;
     int e = L.begin(fp, cp, s);
     bool ok = e == CK_TRACK_OK;
     if (ok && !L.done) {
@@ -586,6 +661,8 @@ extern "C" void ck_ckf_options_default(ck_ckf_options* o) {
   o->max_branches = 16;
 }
 
+extern "C" int32_t ck_last_ckf_lanes(ck_handle* h) { return h ? h->lastCkfLanes : 0; }
+
 extern "C" ck_status ck_find_tracks(ck_handle* h, const ck_options* opt, const ck_ckf_options* ck,
                                     const ck_ckf_in* in, ck_ckf_out* out, void* stream) {
   if (!h || !ck || !in || !out) return fail(CK_ERR_INVALID_ARGUMENT, "NULL argument");
@@ -599,6 +676,11 @@ extern "C" ck_status ck_find_tracks(ck_handle* h, const ck_options* opt, const c
     return fail(CK_ERR_INVALID_ARGUMENT, "n_surfaces differs from the handle's surface table");
   if (ck->max_candidates < 1 || ck->max_candidates > kCkfMaxCandidates)
     return fail(CK_ERR_INVALID_ARGUMENT, "max_candidates outside 1..16");
+  {
+    const int g = ck->lanes_per_seed;
+    if (g != 0 && g != 1 && g != 2 && g != 4 && g != 8 && g != 16 && g != 32)
+      return fail(CK_ERR_INVALID_ARGUMENT, "lanes_per_seed not 0, 1, 2, 4, 8, 16 or 32");
+  }
   if (ck->max_states < 1 || ck->max_tracks < 1 || ck->max_branches < 1)
     return fail(CK_ERR_INVALID_ARGUMENT, "a capacity below 1");
   if (ck->target_surface < -1 || ck->target_surface >= h->nSurfaces)
@@ -747,11 +829,48 @@ extern "C" ck_status ck_find_tracks(ck_handle* h, const ck_options* opt, const c
   cp.out.filtered = (double*)arrs[30].dst;
   cp.out.filtered_cov = (double*)arrs[31].dst;
   cp.out.jacobian = (double*)arrs[32].dst;
-  const int grid = (n + kCkfBlock - 1) / kCkfBlock;
-  if (opt->precision == CK_PRECISION_MIXED)
-    ckfKernel<float, float><<<grid, kCkfBlock, 0, st>>>(fp, cp);
-  else
-    ckfKernel<double, double><<<grid, kCkfBlock, 0, st>>>(fp, cp);
+  const bool mixed = opt->precision == CK_PRECISION_MIXED;
+  int G = ck->lanes_per_seed;
+  if (G == 0) {
+    // automatic: more lanes per seed while the GPU has room for them and
+    // the surfaces hold enough candidates to share (the propagation runs
+    // on every lane of a group, the candidate scan is split)
+    int bps = 0;
+    if (mixed)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ckfKernel<float, float, 1>, kCkfBlock, 0);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ckfKernel<double, double, 1>, kCkfBlock,
+                                                    0);
+    const long long slots = (long long)h->smCount * std::max(bps, 1) * kCkfBlock;
+    int used = 0;
+    if (host) {
+      for (int s = 0; s < h->nSurfaces; ++s)
+        used += in->surf_meas_offsets[s + 1] > in->surf_meas_offsets[s] ? 1 : 0;
+    }
+    const double perSurface = (double)in->n_meas / std::max(1, used ? used : h->nSurfaces);
+    G = 1;
+    while (G < 32 && (long long)n * G * 2 <= slots && perSurface >= 4.0 * G) G *= 2;
+  }
+  const int grid = (int)(((long long)n * G + kCkfBlock - 1) / kCkfBlock);
+#define CK_CKF_LAUNCH(GG)                                                   \
+  case GG:                                                                 \
+    if (mixed)                                                             \
+      ckfKernel<float, float, GG><<<grid, kCkfBlock, 0, st>>>(fp, cp);     \
+    else                                                                   \
+      ckfKernel<double, double, GG><<<grid, kCkfBlock, 0, st>>>(fp, cp);   \
+    break;
+  switch (G) {
+    CK_CKF_LAUNCH(1)
+    CK_CKF_LAUNCH(2)
+    CK_CKF_LAUNCH(4)
+    CK_CKF_LAUNCH(8)
+    CK_CKF_LAUNCH(16)
+    CK_CKF_LAUNCH(32)
+    default:
+      return fail(CK_ERR_INVALID_ARGUMENT, "lanes_per_seed not 0, 1, 2, 4, 8, 16 or 32");
+  }
+#undef CK_CKF_LAUNCH
+  h->lastCkfLanes = G;
   if ((e = cudaGetLastError()) != cudaSuccess) return cudaFail(e, "track-finding kernel launch");
   if (host) {
     for (int i = 0; i < kArrs; ++i)

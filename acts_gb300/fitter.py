@@ -97,6 +97,8 @@ def lib():
                                      P(abi.ck_ckf_in), P(abi.ck_ckf_out), C.c_void_p]
         L.ck_ckf_options_default.argtypes = [P(abi.ck_ckf_options)]
         L.ck_ckf_options_default.restype = None
+        L.ck_last_ckf_lanes.argtypes = [C.c_void_p]
+        L.ck_last_ckf_lanes.restype = C.c_int32
         L.ck_field_lookup_precision.argtypes = [C.c_void_p, C.c_int32, C.c_int32, abi.P_f64,
                                                 abi.P_f64, abi.P_i32]
         L.ck_fp_peak_gflops.argtypes = [C.c_void_p, C.c_int32, P(C.c_double)]
@@ -470,9 +472,20 @@ class CudaKalman:
         place): CombinatorialKalmanFilter::findTracks from each seed along
         its surface sequence, in the options' precision form."""
         i, o = tf.as_in(), tf.as_out()
-        _check(lib().ck_find_tracks(self._h, C.byref(options), C.byref(ckf_options), C.byref(i),
-                                    C.byref(o), None))
+        self.find_tracks_raw(options, ckf_options, i, o)
         return tf
+
+    def find_tracks_raw(self, options, ckf_options, ck_in, ck_out, stream=None):
+        """ck_find_tracks on ck_ckf_in / ck_ckf_out structures (host or
+        device memory); `stream` a cudaStream_t as an integer (None: the
+        handle's stream)."""
+        _check(lib().ck_find_tracks(self._h, C.byref(options), C.byref(ckf_options),
+                                    C.byref(ck_in), C.byref(ck_out),
+                                    None if stream is None else C.c_void_p(stream)))
+
+    def last_ckf_lanes(self):
+        """Lanes per seed of the last track-finding launch."""
+        return int(lib().ck_last_ckf_lanes(self._h))
 
     def field_lookup(self, pos, precision=abi.PRECISION_FP64):
         """getField on the device in a form's stepper arithmetic (FP64, or

@@ -564,6 +564,7 @@ def native_arm(args):
     events = (batched_events_report(torch, dev, args.steps, args.warmup, args.autotune)
               if args.events else None)
     serving = serving_report(torch) if args.serving else None
+    ckf = ckf_report(torch, dev, args.steps, args.warmup) if args.ckf else None
     mixed = results["mixed"]
     line = {"metric": "tracks/s fitted (FP64 vs mixed, same accuracy); p50/p99 event latency",
             "value": round(mixed["tracks_per_s"], 1), "unit": "tracks/s", "n_gpus": world,
@@ -584,7 +585,7 @@ def native_arm(args):
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "ms_per_step": round(e2e_ms, 3), "path": "ck_fit_batch, host memory"},
             "roofline": roofline, "accuracy": acc, "cpu_baseline": cpu,
-            "batched_events": events, "serving": serving,
+            "batched_events": events, "serving": serving, "track_finding": ckf,
             "clocks": clocks.summary(),
             "gpu_launches": int(mixed["launches_per_step"] * args.steps),
             "kernel": {"mixed": mixed, "fp64": results["fp64"]},
@@ -593,6 +594,91 @@ def native_arm(args):
     if world > 1:
         torch.distributed.barrier()
     return 0
+
+
+def ckf_report(torch, dev, steps, warmup, n_seeds=10000, seed=95, sample_seeds=1000):
+    """Track finding (ck_find_tracks): one barrel event of 10,000 pions
+    (100,000 measurements, 10,000 on each of the 10 cylinder layers); every
+    track's start parameters are a seed with its surface sequence; chi2 cut
+    15, one candidate per surface, branches ended by loop protection. Times
+    the device-resident call (CUDA events on the launching stream) and the
+    host-memory call (wall clock, copies included) for both forms, the
+    oracle on a sample of the seeds (the whole event's measurements) on all
+    host threads, and checks the FP64 results of that sample against it."""
+    from acts_gb300 import abi, generate
+    from acts_gb300.fitter import CudaKalman
+    from oracle import kforacle
+
+    det = generate.Detector(abi.CKG_BARREL)
+    b = generate.generate(det, n_seeds, seed=seed)
+    tf = generate.ckf_event(det, b, max_states=24, max_tracks=4)
+    ko = tf.options(chi2_cut=15.0, max_branches=8)
+    fit = CudaKalman.for_detector(det)
+    stream = torch.cuda.current_stream(dev)
+    report = {"workload": "barrel event: %d seeds, %d measurements (%d per layer), chi2 cut 15, "
+                          "1 candidate per surface" % (n_seeds, tf.n_meas, tf.n_meas // 10),
+              "unit": "seeds/s"}
+    keep = {}
+    di = tf.as_in()
+    di.memory = abi.MEM_DEVICE
+    for name, _ in abi.ck_ckf_in._fields_:
+        v = getattr(tf, name, None)
+        if isinstance(v, np.ndarray):
+            t = torch.from_numpy(np.ascontiguousarray(v)).to(dev)
+            keep[name] = t
+            setattr(di, name, C.cast(C.c_void_p(t.data_ptr()), type(getattr(di, name))))
+    do = tf.as_out()
+    for name, _ in abi.ck_ckf_out._fields_:
+        t = torch.from_numpy(np.ascontiguousarray(getattr(tf, name))).to(dev)
+        keep["out_" + name] = t
+        setattr(do, name, C.cast(C.c_void_p(t.data_ptr()), type(getattr(do, name))))
+    for name in ("fp64", "mixed"):
+        prec = abi.PRECISION_MIXED if name == "mixed" else abi.PRECISION_FP64
+        opt = abi.default_options(precision=prec)
+        for _ in range(max(warmup, 1)):
+            fit.find_tracks_raw(opt, ko, di, do, stream.cuda_stream)
+        torch.cuda.synchronize(dev)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(steps):
+            fit.find_tracks_raw(opt, ko, di, do, stream.cuda_stream)
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = ev0.elapsed_time(ev1) / steps
+        host = generate.ckf_event(det, b, max_states=24, max_tracks=4)
+        fit.find_tracks(opt, ko, host)  # warm the host path's staging buffer
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            fit.find_tracks(opt, ko, host)
+        e2e = (time.perf_counter() - t0) / steps * 1e3
+        report[name] = {"seeds_per_s": round(n_seeds / (ms / 1e3), 1), "ms": round(ms, 3),
+                        "e2e_seeds_per_s": round(n_seeds / (e2e / 1e3), 1),
+                        "e2e_ms": round(e2e, 3), "lanes_per_seed": fit.last_ckf_lanes(),
+                        "tracks_found": int(host.n_tracks.sum()),
+                        "status_ok": int((host.status == 0).sum())}
+        if name == "fp64":
+            gpu64 = host
+    fit.close()
+    # oracle on the first `sample_seeds` seeds against the whole event
+    S = sample_seeds
+    so = tf.seq_offsets[:S + 1]
+    sub = abi.TrackFinding(so, tf.seq_surfaces[:so[-1]], tf.start_params[:S], tf.start_cov[:S],
+                           tf.start_frames[:S], tf.particle[:S], tf.surf_meas_offsets,
+                           tf.meas_values, tf.meas_cov, meas_subspace=tf.meas_subspace,
+                           particle_pdg=tf.particle_pdg[:S], max_states=24, max_tracks=4)
+    threads = kforacle.hardware_threads()
+    t0 = time.perf_counter()
+    kforacle.find_tracks(det.surfaces, det.field, abi.default_options(), ko, sub,
+                         n_threads=threads)
+    cpu_s = time.perf_counter() - t0
+    report["cpu_baseline"] = {"value": round(S / cpu_s, 1), "unit": "seeds/s", "cores": threads,
+                              "kind": "port", "sample": "%d seeds of the event" % S}
+    same = int(sum(1 for s in range(S)
+                   if gpu64.status[s] == sub.status[s] and gpu64.n_tracks[s] == sub.n_tracks[s]
+                   and all(gpu64.track_measurements(s, k) == sub.track_measurements(s, k)
+                           for k in range(sub.n_tracks[s]))))
+    report["fp64_parity_sample"] = {"seeds": S, "identical_tracks": same}
+    return report
 
 
 def batched_events_report(torch, dev, steps, warmup, autotune, seed=91, n_events=50,
@@ -880,6 +966,8 @@ def main():
                     help="skip the serving-loop latency measurement")
     ap.add_argument("--no-events", dest="events", action="store_false",
                     help="skip the batched uneven-events (grid field) measurement")
+    ap.add_argument("--no-ckf", dest="ckf", action="store_false",
+                    help="skip the track-finding (CKF) measurement")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the default launch configuration")
     args = ap.parse_args()

@@ -676,6 +676,13 @@ typedef struct ck_ckf_options {
                                 a branch (without a field and a target the
                                 seed runs into the step limit; on a field map
                                 it may leave the map)                          */
+  int32_t lanes_per_seed;    /* GPU lanes that share a seed's search: 1, 2, 4,
+                                8, 16 or 32 (the candidate scan of a surface is
+                                split over them; results do not depend on it);
+                                0 (default): chosen from the seed count and the
+                                measurements per surface. No counterpart in the
+                                reference (a scheduling knob)                  */
+  int32_t reserved;
 } ck_ckf_options;
 
 void ck_ckf_options_default(ck_ckf_options* options);
@@ -737,6 +744,9 @@ typedef struct ck_ckf_out {
 ck_status ck_find_tracks(ck_handle* h, const ck_options* options,
                          const ck_ckf_options* ckf, const ck_ckf_in* in,
                          ck_ckf_out* out, void* stream);
+
+/* Lanes per seed of the handle's last ck_find_tracks launch (0: none yet). */
+int32_t ck_last_ckf_lanes(ck_handle* h);
 
 /* ------------------------------------------------------------- serving */
 

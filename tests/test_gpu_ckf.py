@@ -141,7 +141,7 @@ def test_fp64_parity(case):
         tf = generate.ckf_event(det, generate.generate(det, 1000, seed=22), max_states=128,
                                 max_tracks=32)
         opt = abi.default_options(max_steps=100000)
-        kw = dict(chi2_cut=30.0, max_candidates=2, chi2_cut_outlier=200.0, max_branches=32)
+        kw = dict(chi2_cut=300.0, max_candidates=3, chi2_cut_outlier=500.0, max_branches=32)
     elif case == "barrel_stopper":
         det = generate.Detector(abi.CKG_BARREL)
         tf = generate.ckf_event(det, generate.generate(det, 2000, seed=23))
@@ -252,3 +252,33 @@ def test_invalid_arguments_are_rejected():
             fit.find_tracks(abi.default_options(), bad.options(), bad)
     finally:
         fit.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_MIXED],
+                         ids=["fp64", "mixed"])
+def test_lanes_per_seed_do_not_change_results(precision):
+    """Splitting a surface's candidate scan over 2-32 lanes and merging by
+    shuffles gives the serial scan's selection: every output bit-identical."""
+    det = generate.Detector(abi.CKG_BARREL)
+    tf = generate.ckf_event(det, generate.generate(det, 1500, seed=29), max_states=128,
+                            max_tracks=32)
+    opt = abi.default_options(precision=precision, max_steps=100000)
+    fit = _fitter(det)
+    outs = []
+    try:
+        for g in (1, 2, 4, 8, 16, 32):
+            r = _copy(tf)
+            fit.find_tracks(opt, tf.options(chi2_cut=30.0, max_candidates=3, max_branches=32,
+                                            chi2_cut_outlier=100.0, lanes_per_seed=g), r)
+            assert fit.last_ckf_lanes() == g
+            outs.append(r)
+        fit.find_tracks(opt, tf.options(chi2_cut=30.0, max_candidates=3, max_branches=32,
+                                        chi2_cut_outlier=100.0), _copy(tf))
+        print("automatic lanes per seed:", fit.last_ckf_lanes())
+    finally:
+        fit.close()
+    assert (outs[0].n_tracks > 1).any()
+    for r in outs[1:]:
+        rep = compare(r, outs[0])
+        assert all(v == 0.0 for v in rep.values()), rep
