@@ -50,7 +50,135 @@ struct CkfParams {
   const int32_t* surf_meas_off;  // [n_surfaces + 1]
   ck_ckf_out out;                // device pointers
   CkfBranch* branches;           // [n_seeds * max_branches]
+  // the candidates of each surface sorted along one local axis (windowed
+  // search); see surfaceIndexKernel
+  const double* sortedKey;  // [n_meas], per surface segment
+  const int32_t* sortedIdx;
+  const int32_t* surfAxis;  // [n_surfaces]: 0 / 1 sorted along loc0 / loc1, -1 not
+                            // sorted (linear scan), -2 an invalid subspace
+  const double* surfVmax;   // [n_surfaces] largest measurement variance on that axis
 };
+
+// A surface's candidates sorted by their measured value along one local axis
+// a (lexicographic (value, index)), where every measurement of the surface
+// measures a: the predicted chi2 of a candidate is at least
+// r_a^2 / (V_aa + P_aa) (the Schur complement of the 2x2 residual
+// covariance), so a search outward from the predicted value can stop once
+// that bound passes the cut (and, while nothing passed, the smallest chi2
+// found, for the outlier) — the selection is the full scan's.
+constexpr int kCkfSortMax = 16384;
+constexpr int kCkfSortThreads = 1024;
+
+__global__ void __launch_bounds__(kCkfSortThreads)
+surfaceIndexKernel(const int32_t* __restrict__ off, const double* __restrict__ val,
+                   const double* __restrict__ cov, const int32_t* __restrict__ sub, int nSurf,
+                   double* __restrict__ key, int32_t* __restrict__ idx, int32_t* __restrict__ axis,
+                   double* __restrict__ vmax) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* sk = reinterpret_cast<double*>(smem);
+  int32_t* si = reinterpret_cast<int32_t*>(smem + sizeof(double) * kCkfSortMax);
+  __shared__ int has0, has1, bad;
+  __shared__ double vm0, vm1;
+  const int s = blockIdx.x;
+  if (s >= nSurf) return;
+  const int m0 = off[s], m1 = off[s + 1], L = m1 - m0;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    has0 = has1 = bad = 0;
+    vm0 = vm1 = 0.0;
+  }
+  __syncthreads();
+  // which axes the surface's measurements measure, and their largest variance
+  int h0 = 0, h1 = 0, b = 0;
+  double v0 = 0.0, v1 = 0.0;
+  for (int i = tid; i < L; i += blockDim.x) {
+    const int m = m0 + i;
+    const int sb = sub ? sub[m] : CK_MEAS_LOC01;
+    if (sb < CK_MEAS_LOC0 || sb > CK_MEAS_LOC01) {
+      b = 1;
+      continue;
+    }
+    const double a0 = val[2 * (size_t)m], a1 = val[2 * (size_t)m + 1];
+    const double c0 = cov[4 * (size_t)m], c3 = cov[4 * (size_t)m + 3];
+    if (sb == CK_MEAS_LOC0) {
+      h0 = 1;
+      b |= !(a0 == a0) || !(c0 == c0);
+      v0 = fmax(v0, c0);
+    } else if (sb == CK_MEAS_LOC1) {
+      h1 = 1;
+      b |= !(a0 == a0) || !(c0 == c0);
+      v1 = fmax(v1, c0);
+    } else {
+      b |= !(a0 == a0) || !(a1 == a1) || !(c0 == c0) || !(c3 == c3);
+      v0 = fmax(v0, c0);
+      v1 = fmax(v1, c3);
+    }
+  }
+  if (h0) atomicOr(&has0, 1);
+  if (h1) atomicOr(&has1, 1);
+  if (b) atomicOr(&bad, 1);
+  // (non-negative doubles order as their bit patterns)
+  atomicMax(reinterpret_cast<unsigned long long*>(&vm0), (unsigned long long)__double_as_longlong(v0));
+  atomicMax(reinterpret_cast<unsigned long long*>(&vm1), (unsigned long long)__double_as_longlong(v1));
+  __syncthreads();
+  int a;
+  bool invalidSub = false;
+  if (bad) {
+    // an invalid subspace fails the scan of this surface; a NaN value or
+    // variance leaves the surface unsorted
+    for (int i = 0; i < L && !invalidSub; ++i) {
+      const int sb = sub ? sub[m0 + i] : CK_MEAS_LOC01;
+      invalidSub = sb < CK_MEAS_LOC0 || sb > CK_MEAS_LOC01;
+    }
+    a = invalidSub ? -2 : -1;
+  } else {
+    a = (has0 && has1) ? -1 : (has1 ? 1 : 0);
+  }
+  if (L > kCkfSortMax && a >= 0) a = -1;
+  if (tid == 0) {
+    axis[s] = a;
+    vmax[s] = a == 1 ? vm1 : vm0;
+  }
+  if (a < 0 || L == 0) return;
+  int P = 1;
+  while (P < L) P <<= 1;
+  for (int i = tid; i < P; i += blockDim.x) {
+    if (i < L) {
+      const int m = m0 + i;
+      const int sb = sub ? sub[m] : CK_MEAS_LOC01;
+      // (a 1D measurement holds its value in the first slot)
+      sk[i] = (a == 1 && sb == CK_MEAS_LOC01) ? val[2 * (size_t)m + 1] : val[2 * (size_t)m];
+      si[i] = m;
+    } else {
+      sk[i] = CUDART_INF;
+      si[i] = INT_MAX;
+    }
+  }
+  __syncthreads();
+  // bitonic sort, lexicographic (value, index)
+  for (int k = 2; k <= P; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = tid; i < P; i += blockDim.x) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const double ka = sk[i], kb = sk[ixj];
+          const int ia = si[i], ib = si[ixj];
+          const bool aGreater = ka > kb || (ka == kb && ia > ib);
+          if (((i & k) == 0) == aGreater) {
+            sk[i] = kb;
+            sk[ixj] = ka;
+            si[i] = ib;
+            si[ixj] = ia;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  for (int i = tid; i < L; i += blockDim.x) {
+    key[m0 + i] = sk[i];
+    idx[m0 + i] = si[i];
+  }
+}
 
 // Group operations of the G lanes that share a seed (G divides 32; the
 // group's lanes are consecutive and run the same control flow on the same
@@ -86,8 +214,10 @@ CK_D int groupSum(unsigned mask, int v) {
 
 // G lanes per seed: every lane of the group runs the seed's search on the
 // same values (identical stores to the same addresses); the candidate scan
-// of a surface is split over the group and merged by shuffles, with the
-// result of the serial scan (ties in input order).
+// of a surface is split over the group and merged by shuffles into the
+// serial scan's selection (ties in input order). With G = 1 a surface whose
+// candidates are sorted along one axis is searched outward from the
+// prediction instead (the same selection).
 template <typename P, typename CV, int G>
 struct CkfLane : Lane<P, CV> {
   using B = Lane<P, CV>;
@@ -315,25 +445,22 @@ struct CkfLane : Lane<P, CV> {
     const int K = cp.o.max_candidates;
     const int gl = (int)(threadIdx.x & (G - 1));  // this lane's share: m0 + gl, m0 + gl + G, ...
     bool badSub = false;
-    for (int m = m0 + gl; m < m1; m += G) {
-      const int sub = fp.meas_sub ? __ldg(&fp.meas_sub[m]) : CK_MEAS_LOC01;
-      if (sub < CK_MEAS_LOC0 || sub > CK_MEAS_LOC01) {
-        badSub = true;
-        break;
-      }
+    // one candidate: its predicted chi2 into the first minimum and the
+    // sorted selection, both lexicographic in (chi2, index)
+    auto consider = [&](int m, int sub) -> double {
       double V[4];
 #pragma unroll
       for (int c = 0; c < 4; ++c) V[c] = __ldg(&fp.meas_cov[4 * (size_t)m + c]);
       const double c2 = predictedChi2Sub<kFastRcp>(bp, Pp, sub, __ldg(&fp.meas_val[2 * (size_t)m]),
                                                    __ldg(&fp.meas_val[2 * (size_t)m + 1]), V);
-      if (c2 < minChi2) {
+      if (c2 < minChi2 || (c2 == minChi2 && m < minM)) {
         minChi2 = c2;
         minM = m;
       }
       if (!(c2 >= cp.o.chi2_cut)) {
         ++nPassed;
         int pos = nSel;
-        while (pos > 0 && selC[pos - 1] > c2) --pos;
+        while (pos > 0 && (selC[pos - 1] > c2 || (selC[pos - 1] == c2 && selM[pos - 1] > m))) --pos;
         if (pos < K) {
           for (int j = (nSel < K ? nSel : K - 1); j > pos; --j) {
             selM[j] = selM[j - 1];
@@ -343,6 +470,52 @@ struct CkfLane : Lane<P, CV> {
           selC[pos] = c2;
           if (nSel < K) ++nSel;
         }
+      }
+      return c2;
+    };
+    const int axis = m1 > m0 ? __ldg(&cp.surfAxis[sid]) : -1;
+    if (axis == -2) {
+      badSub = true;
+    } else if (G == 1 && axis >= 0) {
+      // windowed: outward from the predicted value along the sorted axis,
+      // the nearer side first; a side ends where the chi2 bound can no
+      // longer pass the cut nor (while nothing passed) undercut the
+      // smallest chi2 below the outlier cut. The bound carries a relative
+      // margin of 1e-5 for the rounding of the computed chi2.
+      const double pk = bp[axis];
+      const double den = __ldg(&cp.surfVmax[sid]) + Pp[sidx(axis, axis)];
+      const double* key = cp.sortedKey;
+      int lo = m0, hi = m1;  // first key >= pk
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&key[mid]) < pk)
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+      int L = lo - 1, R = lo;
+      while (true) {
+        const double dl = L >= m0 ? pk - __ldg(&key[L]) : CUDART_INF;
+        const double dr = R < m1 ? __ldg(&key[R]) - pk : CUDART_INF;
+        const bool left = dl < dr;
+        const double d = left ? dl : dr;
+        if (!(d < CUDART_INF)) break;
+        const double lb = d * d / den * (1.0 - 1e-5);
+        const bool more = lb < cp.o.chi2_cut ||
+                          (nPassed == 0 && lb <= minChi2 && lb < cp.o.chi2_cut_outlier);
+        if (!more) break;
+        const int pos = left ? L-- : R++;
+        const int m = __ldg(&cp.sortedIdx[pos]);
+        consider(m, fp.meas_sub ? __ldg(&fp.meas_sub[m]) : CK_MEAS_LOC01);
+      }
+    } else {
+      for (int m = m0 + gl; m < m1; m += G) {
+        const int sub = fp.meas_sub ? __ldg(&fp.meas_sub[m]) : CK_MEAS_LOC01;
+        if (sub < CK_MEAS_LOC0 || sub > CK_MEAS_LOC01) {
+          badSub = true;
+          break;
+        }
+        consider(m, sub);
       }
     }
     if constexpr (G > 1) {
@@ -753,16 +926,20 @@ extern "C" ck_status ck_find_tracks(ck_handle* h, const ck_options* opt, const c
       {out->filtered_cov, nullptr, 168 * S, false},
       {out->jacobian, nullptr, 288 * S, false}};
   constexpr int kArrs = sizeof(arrs) / sizeof(arrs[0]);
-  // device scratch: the fail path's tip array and the branch stacks
+  // device scratch: the fail path's tip array, the branch stacks and the
+  // surfaces' sorted candidates
   const size_t tipBytes = align256(4 * nn);
   const size_t brBytes = align256(sizeof(CkfBranch) * (size_t)ck->max_branches * nn);
-  size_t total = tipBytes + brBytes;
+  const size_t keyBytes = align256(8 * nm), idxBytes = align256(4 * nm);
+  const size_t axBytes = align256(4 * ns1), vmBytes = align256(8 * ns1);
+  const size_t scratchBytes = tipBytes + brBytes + keyBytes + idxBytes + axBytes + vmBytes;
+  size_t total = scratchBytes;
   if (host)
     for (int i = 0; i < kArrs; ++i)
       if (arrs[i].src) total += align256(arrs[i].bytes);
   if ((e = h->unitBuf.ensure(total)) != cudaSuccess) return cudaFail(e, "track-finding buffer");
   char* base = (char*)h->unitBuf.p;
-  size_t off = tipBytes + brBytes;
+  size_t off = scratchBytes;
   for (int i = 0; i < kArrs; ++i) {
     if (!arrs[i].src) continue;
     if (host) {
@@ -811,6 +988,29 @@ extern "C" ck_status ck_find_tracks(ck_handle* h, const ck_options* opt, const c
   }
   cp.surf_meas_off = (const int32_t*)arrs[7].dst;
   cp.branches = (CkfBranch*)(base + tipBytes);
+  {
+    char* p = base + tipBytes + brBytes;
+    double* key = (double*)p;
+    int32_t* idx = (int32_t*)(p + keyBytes);
+    int32_t* ax = (int32_t*)(p + keyBytes + idxBytes);
+    double* vm = (double*)(p + keyBytes + idxBytes + axBytes);
+    static std::once_flag smemOnce;
+    static cudaError_t smemErr = cudaSuccess;
+    std::call_once(smemOnce, [] {
+      smemErr = cudaFuncSetAttribute(surfaceIndexKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(12 * kCkfSortMax));
+    });
+    if (smemErr != cudaSuccess) return cudaFail(smemErr, "surface index kernel attributes");
+    if (h->nSurfaces > 0)
+      surfaceIndexKernel<<<h->nSurfaces, kCkfSortThreads, 12 * kCkfSortMax, st>>>(
+          cp.surf_meas_off, fp.meas_val, fp.meas_cov, fp.meas_sub, h->nSurfaces, key, idx, ax,
+          vm);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cudaFail(e, "surface index kernel launch");
+    cp.sortedKey = key;
+    cp.sortedIdx = idx;
+    cp.surfAxis = ax;
+    cp.surfVmax = vm;
+  }
   int32_t** outInts[] = {&cp.out.status,        &cp.out.n_tracks,         &cp.out.n_states,
                          &cp.out.track_tip,     &cp.out.track_n_measurements,
                          &cp.out.track_n_holes, &cp.out.track_n_outliers, &cp.out.track_ndf};
@@ -830,27 +1030,9 @@ extern "C" ck_status ck_find_tracks(ck_handle* h, const ck_options* opt, const c
   cp.out.filtered_cov = (double*)arrs[31].dst;
   cp.out.jacobian = (double*)arrs[32].dst;
   const bool mixed = opt->precision == CK_PRECISION_MIXED;
-  int G = ck->lanes_per_seed;
-  if (G == 0) {
-    // automatic: more lanes per seed while the GPU has room for them and
-    // the surfaces hold enough candidates to share (the propagation runs
-    // on every lane of a group, the candidate scan is split)
-    int bps = 0;
-    if (mixed)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ckfKernel<float, float, 1>, kCkfBlock, 0);
-    else
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ckfKernel<double, double, 1>, kCkfBlock,
-                                                    0);
-    const long long slots = (long long)h->smCount * std::max(bps, 1) * kCkfBlock;
-    int used = 0;
-    if (host) {
-      for (int s = 0; s < h->nSurfaces; ++s)
-        used += in->surf_meas_offsets[s + 1] > in->surf_meas_offsets[s] ? 1 : 0;
-    }
-    const double perSurface = (double)in->n_meas / std::max(1, used ? used : h->nSurfaces);
-    G = 1;
-    while (G < 32 && (long long)n * G * 2 <= slots && perSurface >= 4.0 * G) G *= 2;
-  }
+  // (0: one lane per seed; the windowed candidate search visits few
+  // candidates, and a group replicates the propagation on every lane)
+  const int G = ck->lanes_per_seed > 0 ? ck->lanes_per_seed : 1;
   const int grid = (int)(((long long)n * G + kCkfBlock - 1) / kCkfBlock);
 #define CK_CKF_LAUNCH(GG)                                                   \
   case GG:                                                                 \
@@ -879,6 +1061,6 @@ extern "C" ck_status ck_find_tracks(ck_handle* h, const ck_options* opt, const c
                         cudaMemcpyDeviceToHost, st);
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cudaFail(e, "track-finding kernel");
   }
-  h->lastLaunches = 1;
+  h->lastLaunches = 2;
   return CK_OK;
 }

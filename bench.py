@@ -614,7 +614,7 @@ def ckf_report(torch, dev, steps, warmup, n_seeds=10000, seed=95, sample_seeds=1
     tf = generate.ckf_event(det, b, max_states=24, max_tracks=4)
     ko = tf.options(chi2_cut=15.0, max_branches=8)
     fit = CudaKalman.for_detector(det)
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)  # (a stream of its own: the events see the launches)
     report = {"workload": "barrel event: %d seeds, %d measurements (%d per layer), chi2 cut 15, "
                           "1 candidate per surface" % (n_seeds, tf.n_meas, tf.n_meas // 10),
               "unit": "seeds/s"}

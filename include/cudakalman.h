@@ -676,12 +676,18 @@ typedef struct ck_ckf_options {
                                 a branch (without a field and a target the
                                 seed runs into the step limit; on a field map
                                 it may leave the map)                          */
-  int32_t lanes_per_seed;    /* GPU lanes that share a seed's search: 1, 2, 4,
-                                8, 16 or 32 (the candidate scan of a surface is
-                                split over them; results do not depend on it);
-                                0 (default): chosen from the seed count and the
-                                measurements per surface. No counterpart in the
-                                reference (a scheduling knob)                  */
+  int32_t lanes_per_seed;    /* GPU lanes that share a seed's search: 0 or 1
+                                (default): one lane, whose candidate search
+                                walks outward from the prediction over the
+                                surface's candidates sorted along a measured
+                                axis; 2, 4, 8, 16 or 32: the lanes split a full
+                                scan of every surface (for few seeds on
+                                surfaces with many candidates). The selection
+                                is the same; floating-point values agree to
+                                the parity tolerance (each kernel instance
+                                contracts multiply-adds its own way). No
+                                counterpart in the reference (a scheduling
+                                knob)                                          */
   int32_t reserved;
 } ck_ckf_options;
 

@@ -1,7 +1,7 @@
 """Track-finding cases shared by the oracle and GPU tests.
 
 cubic_telescope(): the reference's CKF unit-test setup
-(Tests/UnitTests/Core/TrackFinding/CombinatorialKalmanFilterTests.cpp:86-258
+(Tests/UnitTests/Core/TrackFinding/CombinatorialKalmanFilterTests.cpp:84-105, 204-257
 with Tests/CommonHelpers/src/CubicTrackingGeometry.cpp:28-104): six planes
 normal to the x axis at x = -2, -1, 1 -+ 1 mm, 2 -+ 1 mm (the last four
 rotated by +-0.026 rad about their normal), 0.5 mm of beryllium each; pixel
