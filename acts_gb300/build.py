@@ -30,8 +30,9 @@ GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 # translation units of libcudakalman.so
 CUDA_SOURCES = ["ck_kernels_fp64.cu", "ck_kernels_mixed.cu", "ck_units.cu", "ck_api.cu", "ck_static.cu",
                 "ck_server.cu", "ck_extrapolate.cu", "ck_reverse_fp64.cu", "ck_reverse_mixed.cu",
-                "ck_propagate.cu", "ck_ckf.cu"]
-CUDA_HEADERS = ["ck_device.cuh", "ck_fitter.cuh", "ck_internal.h", "ck_api_internal.h", "ck_launch.h"]
+                "ck_propagate.cu", "ck_ckf.cu", "ck_simulate.cu"]
+CUDA_HEADERS = ["ck_device.cuh", "ck_fitter.cuh", "ck_internal.h", "ck_api_internal.h", "ck_launch.h",
+                "ck_simulate.h"]
 
 
 def _run(cmd, cwd=None):
@@ -52,10 +53,11 @@ def build_generator(force=False):
     os.makedirs(LIBDIR, exist_ok=True)
     out = os.path.join(LIBDIR, "libckgen.so")
     src = os.path.join(CSRC, "ck_generate.cpp")
-    deps = [src, os.path.join(INCLUDE, "ckgen.h"), os.path.join(INCLUDE, "cudakalman.h")]
+    deps = [src, os.path.join(CSRC, "ck_simulate.h"), os.path.join(INCLUDE, "ckgen.h"),
+            os.path.join(INCLUDE, "cudakalman.h")]
     if force or _stale(out, deps):
-        _run([CXX, "-O2", "-std=c++17", "-fPIC", "-shared", "-I" + INCLUDE, src, "-o", out,
-              "-lpthread"])
+        _run([CXX, "-O2", "-std=c++17", "-fPIC", "-shared", "-I" + INCLUDE, "-I" + CSRC, src,
+              "-o", out, "-lpthread"])
     return out
 
 

@@ -652,6 +652,7 @@ ck_status ck_destroy(ck_handle* h) {
   if (h->dSurfaces) cudaFree(h->dSurfaces);
   if (h->dTrig) cudaFree(h->dTrig);
   if (h->dNodes) cudaFree(h->dNodes);
+  if (h->dGenSurfaces) cudaFree(h->dGenSurfaces);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->evMid) cudaEventDestroy(h->evMid);

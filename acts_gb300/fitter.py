@@ -99,6 +99,8 @@ def lib():
         L.ck_ckf_options_default.restype = None
         L.ck_last_ckf_lanes.argtypes = [C.c_void_p]
         L.ck_last_ckf_lanes.restype = C.c_int32
+        L.ck_simulate.argtypes = [C.c_void_p, C.c_int32, C.c_uint64, C.c_int64, C.c_int32,
+                                  P(abi.ckg_out), C.c_void_p]
         L.ck_field_lookup_precision.argtypes = [C.c_void_p, C.c_int32, C.c_int32, abi.P_f64,
                                                 abi.P_f64, abi.P_i32]
         L.ck_fp_peak_gflops.argtypes = [C.c_void_p, C.c_int32, P(C.c_double)]
@@ -482,6 +484,27 @@ class CudaKalman:
         _check(lib().ck_find_tracks(self._h, C.byref(options), C.byref(ckf_options),
                                     C.byref(ck_in), C.byref(ck_out),
                                     None if stream is None else C.c_void_p(stream)))
+
+    def simulate(self, preset, n_tracks, seed=1, first_track=0, cap=24, device="cuda:0"):
+        """ck_simulate: tracks [first_track, first_track + n_tracks) of a
+        generator preset simulated and digitised on the GPU through this
+        handle's surfaces and field; returns a generate.DeviceBatch (torch
+        tensors in device memory, CSR rows of at most `cap` entries)."""
+        import torch
+
+        from .generate import DeviceBatch
+
+        b = DeviceBatch(n_tracks, cap, torch, device, strips=preset == abi.CKG_STRIPS)
+        o = b.as_ckg_out()
+        torch.cuda.synchronize(device)  # (the allocations precede the launches)
+        stream = torch.cuda.current_stream(device)
+        s = stream.cuda_stream
+        _check(lib().ck_simulate(self._h, int(preset), int(seed), int(first_track), int(n_tracks),
+                                 C.byref(o), C.c_void_p(s) if s else None))
+        if not s:
+            self.sync()
+        torch.cuda.synchronize(device)
+        return b.trim()
 
     def last_ckf_lanes(self):
         """Lanes per seed of the last track-finding launch."""

@@ -217,3 +217,84 @@ def ckf_event(detector, batch, max_states=64, max_tracks=16):
     tf.meas_track = track_of[order]
     tf.meas_index = order.astype(np.int64)
     return tf
+
+
+class DeviceBatch:
+    """A generated batch in device memory (torch tensors) in the layout of
+    ckg_out / ck_batch_in, as ck_simulate writes it."""
+
+    INT = ("seq_offsets", "seq_surfaces", "meas_offsets", "meas_surfaces", "particle_pdg")
+    DBL = ("meas_values", "meas_cov", "start_params", "start_cov", "start_frames",
+           "truth_meas", "truth_start")
+
+    def __init__(self, n, cap, torch, device, strips=False):
+        self.n, self.cap, self.device = n, cap, device
+        t = lambda k, dt: torch.empty(k, dtype=dt, device=device)
+        self.seq_offsets = t(n + 1, torch.int32)
+        self.meas_offsets = t(n + 1, torch.int32)
+        self.seq_surfaces = t(max(n * cap, 1), torch.int32)
+        self.meas_surfaces = t(max(n * cap, 1), torch.int32)
+        self.meas_values = t(max(n * cap * 2, 1), torch.float64)
+        self.meas_cov = t(max(n * cap * 4, 1), torch.float64)
+        self.truth_meas = t(max(n * cap * 6, 1), torch.float64)
+        self.meas_outlier = t(max(n * cap, 1), torch.uint8)
+        self.start_params = t(n * 6, torch.float64)
+        self.start_cov = t(n * 36, torch.float64)
+        self.start_frames = t(n * 12, torch.float64)
+        self.truth_start = t(n * 6, torch.float64)
+        self.particle = t(n * 2, torch.float32)
+        self.particle_pdg = t(n, torch.int32)
+        self.meas_subspace = t(max(n * cap, 1), torch.int32) if strips else None
+
+    @staticmethod
+    def _p(x, ct):
+        return None if x is None else C.cast(C.c_void_p(x.data_ptr()), C.POINTER(ct))
+
+    def as_ckg_out(self):
+        o = abi.ckg_out()
+        o.max_per_track = self.cap
+        for name in self.INT:
+            setattr(o, name, self._p(getattr(self, name), C.c_int32))
+        for name in self.DBL:
+            setattr(o, name, self._p(getattr(self, name), C.c_double))
+        o.particle = self._p(self.particle, C.c_float)
+        o.meas_outlier = self._p(self.meas_outlier, C.c_uint8)
+        o.meas_subspace = self._p(self.meas_subspace, C.c_int32)
+        return o
+
+    def trim(self):
+        """Views of the filled part of the row arrays."""
+        ns = int(self.seq_offsets[-1])
+        nm = int(self.meas_offsets[-1])
+        self.seq_surfaces = self.seq_surfaces[:ns]
+        self.meas_surfaces = self.meas_surfaces[:nm]
+        self.meas_values = self.meas_values[:2 * nm]
+        self.meas_cov = self.meas_cov[:4 * nm]
+        self.truth_meas = self.truth_meas[:6 * nm]
+        self.meas_outlier = self.meas_outlier[:nm]
+        if self.meas_subspace is not None:
+            self.meas_subspace = self.meas_subspace[:nm]
+        return self
+
+    def as_batch_in(self):
+        """A ck_batch_in over the device arrays (memory = device)."""
+        b = abi.ck_batch_in()
+        b.n_tracks = self.n
+        b.memory = abi.MEM_DEVICE
+        for name in ("seq_offsets", "seq_surfaces", "meas_offsets", "meas_surfaces",
+                     "particle_pdg"):
+            setattr(b, name, self._p(getattr(self, name), C.c_int32))
+        for name in ("meas_values", "meas_cov", "start_params", "start_cov", "start_frames"):
+            setattr(b, name, self._p(getattr(self, name), C.c_double))
+        b.particle = self._p(self.particle, C.c_float)
+        b.meas_subspace = self._p(self.meas_subspace, C.c_int32)
+        return b
+
+    def to_host(self):
+        """The same batch as a host Batch."""
+        out = Batch(self.n, 1)
+        for name in self.INT + self.DBL + ("meas_outlier",):
+            setattr(out, name, getattr(self, name).cpu().numpy())
+        out.particle = self.particle.cpu().numpy()
+        out.meas_subspace = None if self.meas_subspace is None else self.meas_subspace.cpu().numpy()
+        return out

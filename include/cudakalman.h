@@ -754,6 +754,22 @@ ck_status ck_find_tracks(ck_handle* h, const ck_options* options,
 /* Lanes per seed of the handle's last ck_find_tracks launch (0: none yet). */
 int32_t ck_last_ckf_lanes(ck_handle* h);
 
+/* ------------------------------------------- event generation on device */
+/* Truth simulation and digitisation of tracks [first_track, first_track +
+ * n_tracks) of a generator preset (ckgen.h: CKG_*) through the handle's
+ * surface table and field, on the GPU: the Fatras-like simulation of the
+ * host generator ckg_generate (a fixed-step RK4 truth trajectory, Highland
+ * kicks and Bethe loss at the material layers, smeared measurements, holes
+ * and outliers as the preset asks), from the same source, one thread per
+ * track. `out` holds DEVICE pointers in ckg_out's layout (struct ckg_out,
+ * ckgen.h; compact CSR rows with their offsets, at most max_per_track rows
+ * per track); asynchronous on `stream` (NULL: the handle's). Results are
+ * the host generator's up to floating-point rounding: the device's own
+ * libm and multiply-add contraction. */
+struct ckg_out;
+ck_status ck_simulate(ck_handle* h, int32_t preset, uint64_t seed, int64_t first_track,
+                      int32_t n_tracks, struct ckg_out* out, void* stream);
+
 /* ------------------------------------------------------------- serving */
 
 /* Continuous-batching serving loop (host request thread + device-resident
