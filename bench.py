@@ -351,6 +351,16 @@ def cpu_baseline(det, b, opt, budget_s=10.0):
                       "here: Eigen/Boost absent)" % (count, dt, cores)}
 
 
+def bench_config(n, max_states):
+    """The workload description both arms print."""
+    return {"workload": WORKLOAD, "tracks_per_step_per_gpu": n,
+            "precision": "mixed (stepper, transport, field in FP32; update, inverses, chi2 in "
+                         "FP64)",
+            "l2": "inputs ~1 GB per step > 129 MB L2 (no flush needed)",
+            "max_states": max_states,
+            "outputs": "smoothed parameters + covariances (packed upper triangles)"}
+
+
 def reference_arm(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -358,7 +368,8 @@ def reference_arm(args):
     from acts_gb300 import abi
     from oracle import kforacle
 
-    det, b = make_workload(min(args.tracks, 400000), 0)
+    # the native arm's workload; each step fits a bounded sample of it
+    det, b = make_workload(args.tracks, 0)
     opt = abi.default_options()
     cores = os.cpu_count() or 1
     probe = min(b.n, 4000)
@@ -377,12 +388,12 @@ def reference_arm(args):
             "impl": "reference", "value": value, "unit": "tracks/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD,
-                                            "tracks_per_step": per_step},
+            "data": "synthetic", "config": bench_config(args.tracks, 10),
             "cpu_baseline": {"value": value, "unit": "tracks/s", "cores": cores, "kind": "port",
-                             "sample": "%d barrel tracks per step on %d host threads (C++ "
-                                       "restatement of the reference fit; the reference needs "
-                                       "Eigen/Boost, absent here)" % (per_step, cores)},
+                             "sample": "%d of the workload's %d barrel tracks per step, on "
+                                       "%d host threads (C++ restatement of the reference fit in "
+                                       "FP64; the reference needs Eigen/Boost, absent here)"
+                                       % (per_step, b.n, cores)},
             "e2e": {"value": value, "unit": "tracks/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -572,11 +583,7 @@ def native_arm(args):
             "ms_per_step": round(mixed["ms_per_step"], 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "tracks_per_step_per_gpu": n,
-                       "precision": "mixed (stepper, transport, field in FP32; update, "
-                                    "inverses, chi2 in FP64)",
-                       "l2": "inputs ~1 GB per step > 129 MB L2 (no flush needed)",
-                       "max_states": ms, "outputs": "smoothed parameters + covariances (packed upper triangles)"},
+            "config": bench_config(n, ms),
             "fp64": {"value": round(results["fp64"]["tracks_per_s"], 1), "unit": "tracks/s",
                      "ms_per_step": round(results["fp64"]["ms_per_step"], 3),
                      "mixed_over_fp64": round(mixed["tracks_per_s"] /
