@@ -354,6 +354,8 @@ class ck_ckf_in(C.Structure):
         ("meas_values", P_f64),
         ("meas_cov", P_f64),
         ("meas_subspace", P_i32),
+        ("n_events", C.c_int32),
+        ("seed_event", P_i32),
     ]
 
 
@@ -384,7 +386,8 @@ class TrackFinding:
 
     def __init__(self, seq_offsets, seq_surfaces, start_params, start_cov, start_frames,
                  particle, surf_meas_offsets, meas_values, meas_cov, meas_subspace=None,
-                 particle_pdg=None, max_states=64, max_tracks=16):
+                 particle_pdg=None, max_states=64, max_tracks=16, n_events=1,
+                 seed_event=None):
         i32 = lambda x: np.ascontiguousarray(x, np.int32)
         f64 = lambda x: np.ascontiguousarray(x, np.float64)
         self.seq_offsets = i32(seq_offsets)
@@ -396,7 +399,9 @@ class TrackFinding:
         self.particle = np.ascontiguousarray(particle, np.float32).reshape(self.n, 2)
         self.particle_pdg = None if particle_pdg is None else i32(particle_pdg)
         self.surf_meas_offsets = i32(surf_meas_offsets)
-        self.n_surfaces = len(self.surf_meas_offsets) - 1
+        self.n_events = int(n_events)
+        self.seed_event = None if seed_event is None else i32(seed_event)
+        self.n_surfaces = (len(self.surf_meas_offsets) - 1) // max(self.n_events, 1)
         self.meas_values = f64(meas_values).reshape(-1, 2)
         self.n_meas = len(self.meas_values)
         self.meas_cov = f64(meas_cov).reshape(self.n_meas, 4)
@@ -437,6 +442,8 @@ class TrackFinding:
         i.meas_values = ptr(self.meas_values, C.c_double)
         i.meas_cov = ptr(self.meas_cov, C.c_double)
         i.meas_subspace = ptr(self.meas_subspace, C.c_int32)
+        i.n_events = self.n_events
+        i.seed_event = ptr(self.seed_event, C.c_int32)
         return i
 
     def as_out(self):

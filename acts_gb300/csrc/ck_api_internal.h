@@ -111,6 +111,7 @@ struct ck_handle {
   int smCount = 1;
   int lastCkfLanes = 0;  // lanes per seed of the last ck_find_tracks launch
   void* dGenSurfaces = nullptr;  // the surface table as ck_surface (ck_simulate)
+  bool ckfSortSmemSet = false;   // the candidate sort kernel's shared-memory attribute
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evMid = nullptr;
   ck::DevSurface* dSurfaces = nullptr;

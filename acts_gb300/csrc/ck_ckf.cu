@@ -47,16 +47,18 @@ struct CkfParams {
   // the target's bounds (0: unbounded): rectangle half lengths of a plane,
   // the half length in z of a cylinder
   double targetHalfX, targetHalfY, targetHalfZ;
-  const int32_t* surf_meas_off;  // [n_surfaces + 1]
+  const int32_t* surf_meas_off;  // [n_events * n_surfaces + 1]
+  const int32_t* seed_event;     // [n_seeds] or NULL (event 0)
+  int n_events;
   ck_ckf_out out;                // device pointers
   CkfBranch* branches;           // [n_seeds * max_branches]
   // the candidates of each surface sorted along one local axis (windowed
   // search); see surfaceIndexKernel
   const double* sortedKey;  // [n_meas], per surface segment
   const int32_t* sortedIdx;
-  const int32_t* surfAxis;  // [n_surfaces]: 0 / 1 sorted along loc0 / loc1, -1 not
-                            // sorted (linear scan), -2 an invalid subspace
-  const double* surfVmax;   // [n_surfaces] largest measurement variance on that axis
+  const int32_t* surfAxis;  // [n_events * n_surfaces]: 0 / 1 sorted along loc0 /
+                            // loc1, -1 not sorted (linear scan), -2 an invalid subspace
+  const double* surfVmax;   // largest measurement variance on that axis
 };
 
 // A surface's candidates sorted by their measured value along one local axis
@@ -71,7 +73,7 @@ constexpr int kCkfSortThreads = 1024;
 
 __global__ void __launch_bounds__(kCkfSortThreads)
 surfaceIndexKernel(const int32_t* __restrict__ off, const double* __restrict__ val,
-                   const double* __restrict__ cov, const int32_t* __restrict__ sub, int nSurf,
+                   const double* __restrict__ cov, const int32_t* __restrict__ sub, int nSeg,
                    double* __restrict__ key, int32_t* __restrict__ idx, int32_t* __restrict__ axis,
                    double* __restrict__ vmax) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -79,8 +81,8 @@ surfaceIndexKernel(const int32_t* __restrict__ off, const double* __restrict__ v
   int32_t* si = reinterpret_cast<int32_t*>(smem + sizeof(double) * kCkfSortMax);
   __shared__ int has0, has1, bad;
   __shared__ double vm0, vm1;
-  const int s = blockIdx.x;
-  if (s >= nSurf) return;
+  const int s = blockIdx.x;  // segment: event * n_surfaces + surface
+  if (s >= nSeg) return;
   const int m0 = off[s], m1 = off[s + 1], L = m1 - m0;
   const int tid = threadIdx.x;
   if (tid == 0) {
@@ -248,6 +250,7 @@ struct CkfLane : Lane<P, CV> {
   using B::targetSurf;
 
   int nStatesC, nTracksC, nActive;
+  int evBase;    // first segment of the seed's event (event * n_surfaces)
   int ckfStart;  // the surface the current branch restarted from (-1: the seed's plane)
   double pathLimit;
   bool pathLimitSet, done;
@@ -437,7 +440,8 @@ struct CkfLane : Lane<P, CV> {
     // the predicted chi2 of every measurement on the surface; those below
     // the cut, ascending (ties in input order), at most max_candidates; none
     // below: the smallest becomes an outlier when below the outlier cut
-    const int m0 = __ldg(&cp.surf_meas_off[sid]), m1 = __ldg(&cp.surf_meas_off[sid + 1]);
+    const int seg = evBase + sid;
+    const int m0 = __ldg(&cp.surf_meas_off[seg]), m1 = __ldg(&cp.surf_meas_off[seg + 1]);
     int selM[kCkfMaxCandidates];
     double selC[kCkfMaxCandidates];
     int nSel = 0, nPassed = 0, minM = -1;
@@ -473,7 +477,7 @@ struct CkfLane : Lane<P, CV> {
       }
       return c2;
     };
-    const int axis = m1 > m0 ? __ldg(&cp.surfAxis[sid]) : -1;
+    const int axis = m1 > m0 ? __ldg(&cp.surfAxis[seg]) : -1;
     if (axis == -2) {
       badSub = true;
     } else if (G == 1 && axis >= 0) {
@@ -483,7 +487,7 @@ struct CkfLane : Lane<P, CV> {
       // smallest chi2 below the outlier cut. The bound carries a relative
       // margin of 1e-5 for the rounding of the computed chi2.
       const double pk = bp[axis];
-      const double den = __ldg(&cp.surfVmax[sid]) + Pp[sidx(axis, axis)];
+      const double den = __ldg(&cp.surfVmax[seg]) + Pp[sidx(axis, axis)];
       const double* key = cp.sortedKey;
       int lo = m0, hi = m1;  // first key >= pk
       while (lo < hi) {
@@ -699,6 +703,11 @@ struct CkfLane : Lane<P, CV> {
     nTracksC = 0;
     nActive = 0;
     if (nSeq < 0) return CK_TRACK_INVALID_INPUT;
+    {
+      const int ev = cp.seed_event ? __ldg(&cp.seed_event[seed]) : 0;
+      if (ev < 0 || ev >= cp.n_events) return CK_TRACK_INVALID_INPUT;
+      evBase = ev * fp.n_surfaces;
+    }
     for (int i = 0; i < nSeq; ++i) {
       const int sid = __ldg(&fp.seq_surf[seq0 + i]);
       if (sid < 0 || sid >= fp.n_surfaces || __ldg(&fp.surfaces[sid].type) == CK_SURFACE_LINE)
@@ -868,14 +877,24 @@ extern "C" ck_status ck_find_tracks(ck_handle* h, const ck_options* opt, const c
   if (!out->status || !out->n_tracks || !out->n_states || !out->track_tip || !out->state_prev ||
       !out->state_surface || !out->state_flags || !out->filtered || !out->filtered_cov)
     return fail(CK_ERR_INVALID_ARGUMENT, "a required output array is NULL");
+  if (in->n_events < 0) return fail(CK_ERR_INVALID_ARGUMENT, "n_events < 0");
+  const int nEv = std::max(in->n_events, 1);
+  if ((long long)nEv * h->nSurfaces >= INT_MAX)
+    return fail(CK_ERR_INVALID_ARGUMENT, "n_events x n_surfaces too large");
+  const int nSeg = nEv * h->nSurfaces;
   const bool host = in->memory == CK_MEM_HOST;
   if (host) {
-    // the grouping of the measurements by surface, checked where it is readable
+    // the grouping of the measurements by event and surface, and the seeds'
+    // events, checked where they are readable
     const int32_t* so = in->surf_meas_offsets;
-    bool bad = so[0] != 0 || so[h->nSurfaces] != in->n_meas;
-    for (int s = 0; s < h->nSurfaces && !bad; ++s) bad = so[s + 1] < so[s];
+    bool bad = so[0] != 0 || so[nSeg] != in->n_meas;
+    for (int s = 0; s < nSeg && !bad; ++s) bad = so[s + 1] < so[s];
     for (int s = 0; s < n && !bad; ++s) bad = in->seq_offsets[s + 1] < in->seq_offsets[s];
     if (bad) return fail(CK_ERR_INVALID_ARGUMENT, "offsets not a non-decreasing partition");
+    if (in->seed_event)
+      for (int s = 0; s < n; ++s)
+        if (in->seed_event[s] < 0 || in->seed_event[s] >= nEv)
+          return fail(CK_ERR_INVALID_ARGUMENT, "seed_event outside [0, n_events)");
   }
   std::lock_guard<std::mutex> lock(h->mu);
   cudaError_t e = cudaSetDevice(h->device);
@@ -884,7 +903,7 @@ extern "C" ck_status ck_find_tracks(ck_handle* h, const ck_options* opt, const c
 
   const size_t nn = (size_t)n, S = (size_t)ck->max_states * nn, T = (size_t)ck->max_tracks * nn;
   const size_t nSeqAll = host ? (size_t)in->seq_offsets[n] : 0;
-  const size_t nm = (size_t)in->n_meas, ns1 = (size_t)h->nSurfaces + 1;
+  const size_t nm = (size_t)in->n_meas, ns1 = (size_t)nSeg + 1;
   struct Arr {
     const void* src;
     void* dst;
@@ -903,6 +922,7 @@ extern "C" ck_status ck_find_tracks(ck_handle* h, const ck_options* opt, const c
       {in->meas_values, nullptr, 16 * nm, true},
       {in->meas_cov, nullptr, 32 * nm, true},
       {in->meas_subspace, nullptr, 4 * nm, true},
+      {in->seed_event, nullptr, 4 * nn, true},
       {out->status, nullptr, 4 * nn, false},
       {out->n_tracks, nullptr, 4 * nn, false},
       {out->n_states, nullptr, 4 * nn, false},
@@ -965,7 +985,7 @@ extern "C" ck_status ck_find_tracks(ck_handle* h, const ck_options* opt, const c
   fp.meas_val = (const double*)arrs[8].dst;
   fp.meas_cov = (const double*)arrs[9].dst;
   fp.meas_sub = (const int32_t*)arrs[10].dst;
-  fp.out.status = (int32_t*)arrs[11].dst;
+  fp.out.status = (int32_t*)arrs[12].dst;
   fp.tip = (int32_t*)base;
   fp.max_states = 1;
   fp.lanes_per_warp = 32;
@@ -987,6 +1007,8 @@ extern "C" ck_status ck_find_tracks(ck_handle* h, const ck_options* opt, const c
     cp.targetHalfZ = t.half_length_z;
   }
   cp.surf_meas_off = (const int32_t*)arrs[7].dst;
+  cp.seed_event = (const int32_t*)arrs[11].dst;
+  cp.n_events = nEv;
   cp.branches = (CkfBranch*)(base + tipBytes);
   {
     char* p = base + tipBytes + brBytes;
@@ -994,17 +1016,16 @@ extern "C" ck_status ck_find_tracks(ck_handle* h, const ck_options* opt, const c
     int32_t* idx = (int32_t*)(p + keyBytes);
     int32_t* ax = (int32_t*)(p + keyBytes + idxBytes);
     double* vm = (double*)(p + keyBytes + idxBytes + axBytes);
-    static std::once_flag smemOnce;
-    static cudaError_t smemErr = cudaSuccess;
-    std::call_once(smemOnce, [] {
-      smemErr = cudaFuncSetAttribute(surfaceIndexKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)(12 * kCkfSortMax));
-    });
-    if (smemErr != cudaSuccess) return cudaFail(smemErr, "surface index kernel attributes");
-    if (h->nSurfaces > 0)
-      surfaceIndexKernel<<<h->nSurfaces, kCkfSortThreads, 12 * kCkfSortMax, st>>>(
-          cp.surf_meas_off, fp.meas_val, fp.meas_cov, fp.meas_sub, h->nSurfaces, key, idx, ax,
-          vm);
+    if (!h->ckfSortSmemSet) {  // (a per-device attribute: set on the handle's device)
+      if ((e = cudaFuncSetAttribute(surfaceIndexKernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(12 * kCkfSortMax))) != cudaSuccess)
+        return cudaFail(e, "surface index kernel attributes");
+      h->ckfSortSmemSet = true;
+    }
+    if (nSeg > 0)
+      surfaceIndexKernel<<<nSeg, kCkfSortThreads, 12 * kCkfSortMax, st>>>(
+          cp.surf_meas_off, fp.meas_val, fp.meas_cov, fp.meas_sub, nSeg, key, idx, ax, vm);
     if ((e = cudaGetLastError()) != cudaSuccess) return cudaFail(e, "surface index kernel launch");
     cp.sortedKey = key;
     cp.sortedIdx = idx;
@@ -1014,21 +1035,21 @@ extern "C" ck_status ck_find_tracks(ck_handle* h, const ck_options* opt, const c
   int32_t** outInts[] = {&cp.out.status,        &cp.out.n_tracks,         &cp.out.n_states,
                          &cp.out.track_tip,     &cp.out.track_n_measurements,
                          &cp.out.track_n_holes, &cp.out.track_n_outliers, &cp.out.track_ndf};
-  for (int i = 0; i < 8; ++i) *outInts[i] = (int32_t*)arrs[11 + i].dst;
-  cp.out.track_chi2 = (double*)arrs[19].dst;
-  cp.out.track_params = (double*)arrs[20].dst;
-  cp.out.track_cov = (double*)arrs[21].dst;
-  cp.out.state_prev = (int32_t*)arrs[22].dst;
-  cp.out.state_surface = (int32_t*)arrs[23].dst;
-  cp.out.state_flags = (uint32_t*)arrs[24].dst;
-  cp.out.state_measurement = (int32_t*)arrs[25].dst;
-  cp.out.state_chi2 = (double*)arrs[26].dst;
-  cp.out.state_path_length = (double*)arrs[27].dst;
-  cp.out.predicted = (double*)arrs[28].dst;
-  cp.out.predicted_cov = (double*)arrs[29].dst;
-  cp.out.filtered = (double*)arrs[30].dst;
-  cp.out.filtered_cov = (double*)arrs[31].dst;
-  cp.out.jacobian = (double*)arrs[32].dst;
+  for (int i = 0; i < 8; ++i) *outInts[i] = (int32_t*)arrs[12 + i].dst;
+  cp.out.track_chi2 = (double*)arrs[20].dst;
+  cp.out.track_params = (double*)arrs[21].dst;
+  cp.out.track_cov = (double*)arrs[22].dst;
+  cp.out.state_prev = (int32_t*)arrs[23].dst;
+  cp.out.state_surface = (int32_t*)arrs[24].dst;
+  cp.out.state_flags = (uint32_t*)arrs[25].dst;
+  cp.out.state_measurement = (int32_t*)arrs[26].dst;
+  cp.out.state_chi2 = (double*)arrs[27].dst;
+  cp.out.state_path_length = (double*)arrs[28].dst;
+  cp.out.predicted = (double*)arrs[29].dst;
+  cp.out.predicted_cov = (double*)arrs[30].dst;
+  cp.out.filtered = (double*)arrs[31].dst;
+  cp.out.filtered_cov = (double*)arrs[32].dst;
+  cp.out.jacobian = (double*)arrs[33].dst;
   const bool mixed = opt->precision == CK_PRECISION_MIXED;
   // (0: one lane per seed; the windowed candidate search visits few
   // candidates, and a group replicates the propagation on every lane)

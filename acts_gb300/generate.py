@@ -192,6 +192,37 @@ def event_sizes(seed, n_events, mean=-1.0, lo=100, hi=20000):
     return out
 
 
+def ckf_events(detector, batch, sizes, max_states=64, max_tracks=16):
+    """The batch's tracks as consecutive events of `sizes` tracks each, for
+    one track-finding call over all of them: every track is a seed of its
+    event; the measurements are grouped by event, then surface (stable).
+    `meas_track` / `meas_index` as in ckf_event."""
+    sizes = np.asarray(sizes, np.int64)
+    n = batch.n
+    if sizes.sum() != n:
+        raise ValueError("event sizes do not add up to the batch")
+    n_ev = len(sizes)
+    seed_event = np.repeat(np.arange(n_ev, dtype=np.int32), sizes)
+    nm = int(batch.meas_offsets[-1])
+    ms = np.asarray(batch.meas_surfaces[:nm]).astype(np.int64)
+    track_of = np.repeat(np.arange(n, dtype=np.int32), np.diff(batch.meas_offsets))
+    seg = seed_event[track_of].astype(np.int64) * detector.n_surfaces + ms
+    order = np.argsort(seg, kind="stable")
+    counts = np.bincount(seg, minlength=n_ev * detector.n_surfaces)
+    offs = np.zeros(n_ev * detector.n_surfaces + 1, np.int32)
+    offs[1:] = np.cumsum(counts)
+    sub = None if batch.meas_subspace is None else np.asarray(batch.meas_subspace[:nm])[order]
+    tf = abi.TrackFinding(batch.seq_offsets, batch.seq_surfaces, batch.start_params,
+                          batch.start_cov, batch.start_frames, batch.particle, offs,
+                          batch.meas_values.reshape(-1, 2)[:nm][order],
+                          batch.meas_cov.reshape(-1, 4)[:nm][order], meas_subspace=sub,
+                          particle_pdg=batch.particle_pdg, max_states=max_states,
+                          max_tracks=max_tracks, n_events=n_ev, seed_event=seed_event)
+    tf.meas_track = track_of[order]
+    tf.meas_index = order.astype(np.int64)
+    return tf
+
+
 def ckf_event(detector, batch, max_states=64, max_tracks=16):
     """The batch's tracks as one event for track finding (an
     abi.TrackFinding): every track's start parameters become a seed with the

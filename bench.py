@@ -603,28 +603,10 @@ def native_arm(args):
     return 0
 
 
-def ckf_report(torch, dev, steps, warmup, n_seeds=10000, seed=95, sample_seeds=1000):
-    """Track finding (ck_find_tracks): one barrel event of 10,000 pions
-    (100,000 measurements, 10,000 on each of the 10 cylinder layers); every
-    track's start parameters are a seed with its surface sequence; chi2 cut
-    15, one candidate per surface, branches ended by loop protection. Times
-    the device-resident call (CUDA events on the launching stream) and the
-    host-memory call (wall clock, copies included) for both forms, the
-    oracle on a sample of the seeds (the whole event's measurements) on all
-    host threads, and checks the FP64 results of that sample against it."""
-    from acts_gb300 import abi, generate
-    from acts_gb300.fitter import CudaKalman
-    from oracle import kforacle
+def _ckf_device(tf, torch, dev):
+    """Device copies of a TrackFinding's arrays: (ck_ckf_in, ck_ckf_out, keep)."""
+    from acts_gb300 import abi
 
-    det = generate.Detector(abi.CKG_BARREL)
-    b = generate.generate(det, n_seeds, seed=seed)
-    tf = generate.ckf_event(det, b, max_states=24, max_tracks=4)
-    ko = tf.options(chi2_cut=15.0, max_branches=8)
-    fit = CudaKalman.for_detector(det)
-    stream = torch.cuda.Stream(dev)  # (a stream of its own: the events see the launches)
-    report = {"workload": "barrel event: %d seeds, %d measurements (%d per layer), chi2 cut 15, "
-                          "1 candidate per surface" % (n_seeds, tf.n_meas, tf.n_meas // 10),
-              "unit": "seeds/s"}
     keep = {}
     di = tf.as_in()
     di.memory = abi.MEM_DEVICE
@@ -639,30 +621,86 @@ def ckf_report(torch, dev, steps, warmup, n_seeds=10000, seed=95, sample_seeds=1
         t = torch.from_numpy(np.ascontiguousarray(getattr(tf, name))).to(dev)
         keep["out_" + name] = t
         setattr(do, name, C.cast(C.c_void_p(t.data_ptr()), type(getattr(do, name))))
+    return di, do, keep
+
+
+def _ckf_time(fit, opt, ko, tf, make_host, torch, dev, steps, warmup):
+    """Device-resident ms per call (CUDA events on a stream of its own) and
+    host-memory ms per call (wall clock), with the host call's results."""
+    stream = torch.cuda.Stream(dev)
+    di, do, keep = _ckf_device(tf, torch, dev)
+    torch.cuda.synchronize(dev)
+    for _ in range(max(warmup, 1)):
+        fit.find_tracks_raw(opt, ko, di, do, stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        fit.find_tracks_raw(opt, ko, di, do, stream.cuda_stream)
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = ev0.elapsed_time(ev1) / steps
+    del keep
+    host = make_host()
+    fit.find_tracks(opt, ko, host)  # (warms the host path's staging buffer)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        fit.find_tracks(opt, ko, host)
+    return ms, (time.perf_counter() - t0) / steps * 1e3, host
+
+
+def ckf_report(torch, dev, steps, warmup, n_seeds=10000, seed=95, sample_seeds=1000,
+               n_events=50, event_mean=2000.0):
+    """Track finding (ck_find_tracks) on the barrel workload, chi2 cut 15,
+    one candidate per surface, branches ended by loop protection:
+    * one event of 10,000 pions (100,000 measurements, 10,000 on each of the
+      10 cylinder layers), every track's start parameters a seed with its
+      surface sequence;
+    * 50 events of Poisson(2,000) pions in one call (each seed sees its own
+      event's measurements).
+    Times the device-resident call (CUDA events on the launching stream) and
+    the host-memory call (wall clock, copies included) for both forms, the
+    oracle on a sample of the single event's seeds (against the whole
+    event's measurements) on all host threads, and checks the FP64 results
+    of that sample against it."""
+    from acts_gb300 import abi, generate
+    from acts_gb300.fitter import CudaKalman
+    from oracle import kforacle
+
+    det = generate.Detector(abi.CKG_BARREL)
+    b = generate.generate(det, n_seeds, seed=seed)
+    tf = generate.ckf_event(det, b, max_states=24, max_tracks=4)
+    ko = tf.options(chi2_cut=15.0, max_branches=8)
+    sizes = generate.event_sizes(seed, n_events, mean=event_mean)
+    bm = generate.generate(det, int(sizes.sum()), seed=seed + 1)
+    tfm = generate.ckf_events(det, bm, sizes, max_states=24, max_tracks=4)
+    fit = CudaKalman.for_detector(det)
+    report = {"workload": "barrel: one event of %d seeds, %d measurements (%d per layer); and %d "
+                          "events of Poisson(%d) seeds (%d seeds) in one call; chi2 cut 15, 1 "
+                          "candidate per surface" % (n_seeds, tf.n_meas, tf.n_meas // 10,
+                                                     n_events, event_mean, tfm.n),
+              "unit": "seeds/s"}
     for name in ("fp64", "mixed"):
         prec = abi.PRECISION_MIXED if name == "mixed" else abi.PRECISION_FP64
         opt = abi.default_options(precision=prec)
-        for _ in range(max(warmup, 1)):
-            fit.find_tracks_raw(opt, ko, di, do, stream.cuda_stream)
-        torch.cuda.synchronize(dev)
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        ev0.record(stream)
-        for _ in range(steps):
-            fit.find_tracks_raw(opt, ko, di, do, stream.cuda_stream)
-        ev1.record(stream)
-        torch.cuda.synchronize(dev)
-        ms = ev0.elapsed_time(ev1) / steps
-        host = generate.ckf_event(det, b, max_states=24, max_tracks=4)
-        fit.find_tracks(opt, ko, host)  # warm the host path's staging buffer
-        t0 = time.perf_counter()
-        for _ in range(steps):
-            fit.find_tracks(opt, ko, host)
-        e2e = (time.perf_counter() - t0) / steps * 1e3
+        ms, e2e, host = _ckf_time(fit, opt, ko, tf,
+                                  lambda: generate.ckf_event(det, b, max_states=24, max_tracks=4),
+                                  torch, dev, steps, warmup)
+        msm, e2em, hostm = _ckf_time(fit, opt, ko, tfm,
+                                     lambda: generate.ckf_events(det, bm, sizes, max_states=24,
+                                                                 max_tracks=4),
+                                     torch, dev, steps, warmup)
         report[name] = {"seeds_per_s": round(n_seeds / (ms / 1e3), 1), "ms": round(ms, 3),
                         "e2e_seeds_per_s": round(n_seeds / (e2e / 1e3), 1),
                         "e2e_ms": round(e2e, 3), "lanes_per_seed": fit.last_ckf_lanes(),
                         "tracks_found": int(host.n_tracks.sum()),
-                        "status_ok": int((host.status == 0).sum())}
+                        "status_ok": int((host.status == 0).sum()),
+                        "events": {"seeds_per_s": round(tfm.n / (msm / 1e3), 1),
+                                   "ms": round(msm, 3),
+                                   "e2e_seeds_per_s": round(tfm.n / (e2em / 1e3), 1),
+                                   "e2e_ms": round(e2em, 3),
+                                   "tracks_found": int(hostm.n_tracks.sum()),
+                                   "status_ok": int((hostm.status == 0).sum())}}
         if name == "fp64":
             gpu64 = host
     fit.close()
@@ -679,7 +717,7 @@ def ckf_report(torch, dev, steps, warmup, n_seeds=10000, seed=95, sample_seeds=1
                          n_threads=threads)
     cpu_s = time.perf_counter() - t0
     report["cpu_baseline"] = {"value": round(S / cpu_s, 1), "unit": "seeds/s", "cores": threads,
-                              "kind": "port", "sample": "%d seeds of the event" % S}
+                              "kind": "port", "sample": "%d seeds of the 10,000-seed event" % S}
     same = int(sum(1 for s in range(S)
                    if gpu64.status[s] == sub.status[s] and gpu64.n_tracks[s] == sub.n_tracks[s]
                    and all(gpu64.track_measurements(s, k) == sub.track_measurements(s, k)

@@ -694,9 +694,12 @@ typedef struct ck_ckf_options {
 void ck_ckf_options_default(ck_ckf_options* options);
 
 /* Seeds (start parameters on a plane, as ck_batch_in) with their surface
- * sequences, and the event's measurements grouped by surface: the
- * measurements of surface s are [surf_meas_offsets[s], surf_meas_offsets[s+1])
- * in the caller's order (the candidate order). */
+ * sequences, and the events' measurements grouped by event and surface: the
+ * candidates of seed i on surface s are the measurements
+ * [surf_meas_offsets[e*n_surfaces + s], surf_meas_offsets[e*n_surfaces + s + 1])
+ * of its event e = seed_event[i], in the caller's order (the candidate
+ * order). One call searches the seeds of many events; each seed sees only
+ * its event's measurements. */
 typedef struct ck_ckf_in {
   int32_t n_seeds;
   int32_t memory;                    /* CK_MEM_HOST or CK_MEM_DEVICE (in and out) */
@@ -709,10 +712,13 @@ typedef struct ck_ckf_in {
   const int32_t* particle_pdg;       /* [n_seeds] or NULL (211)                */
   int32_t n_meas;
   int32_t n_surfaces;                /* the handle's table size                */
-  const int32_t* surf_meas_offsets;  /* [n_surfaces+1]                          */
+  const int32_t* surf_meas_offsets;  /* [n_events*n_surfaces+1]                 */
   const double* meas_values;         /* [n_meas*2] (1D: first slot)            */
   const double* meas_cov;            /* [n_meas*4]                             */
   const int32_t* meas_subspace;      /* [n_meas] CK_MEAS_*, or NULL (all 2D)   */
+  int32_t n_events;                  /* events in the call (0 counts as 1)     */
+  const int32_t* seed_event;         /* [n_seeds] event of each seed, or NULL
+                                        (all in event 0)                       */
 } ck_ckf_in;
 
 /* Results. Per seed s: its found tracks k < n_tracks[s] at [s*max_tracks + k]

@@ -5,6 +5,7 @@
 // Inputs and outputs use the public structs of include/cudakalman.h so that
 // the oracle and the CUDA fitter are fed from and compared on the very same
 // arrays.
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -421,6 +422,10 @@ void kfo_find_tracks(const ck_options* opt, int n_surfaces, const ck_surface* su
       const int s = next.fetch_add(1);
       if (s >= n) break;
       int st = CK_TRACK_OK;
+      const int ev = in->seed_event ? in->seed_event[s] : 0;
+      if (ev < 0 || ev >= std::max(in->n_events, 1)) st = CK_TRACK_INVALID_INPUT;
+      F::CkfMeas Me = M;  // the seed's event's measurements
+      Me.offsets = in->surf_meas_offsets + (size_t)std::max(ev, 0) * n_surfaces;
       for (int k = in->seq_offsets[s]; k < in->seq_offsets[s + 1]; ++k) {
         const int sid = in->seq_surfaces[k];
         if (sid < 0 || sid >= n_surfaces || ctx.surfaces[sid].type == CK_SURFACE_LINE)
@@ -435,7 +440,7 @@ void kfo_find_tracks(const ck_options* opt, int n_surfaces, const ck_surface* su
                                 in->particle[2 * (size_t)s], in->particle[2 * (size_t)s + 1],
                                 in->particle_pdg ? in->particle_pdg[s] : 211,
                                 in->seq_surfaces + in->seq_offsets[s],
-                                in->seq_offsets[s + 1] - in->seq_offsets[s], M, cuts, states,
+                                in->seq_offsets[s + 1] - in->seq_offsets[s], Me, cuts, states,
                                 tracks);
       }
       out->status[s] = st;

@@ -296,3 +296,52 @@ def test_unsorted_surface_falls_back_to_the_full_scan():
     gpu, ora = _run(det, tf, abi.default_options(), chi2_cut=DMAX, max_candidates=2,
                     target_surface=det.target, max_branches=32)
     _check(gpu, ora)
+
+
+def _copy_events(tf):
+    r = _copy(tf)
+    r.n_events, r.seed_event = tf.n_events, tf.seed_event
+    r.n_surfaces = tf.n_surfaces
+    return r
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_MIXED],
+                         ids=["fp64", "mixed"])
+def test_events_in_one_call(precision):
+    """Twenty events in one launch: the oracle's result (FP64), and for both
+    forms exactly the results of one call per event."""
+    det = generate.Detector(abi.CKG_UNEVEN)
+    sizes = generate.event_sizes(9, 20, mean=400.0)
+    b = generate.generate(det, int(sizes.sum()), seed=42)
+    tf = generate.ckf_events(det, b, sizes, max_states=32, max_tracks=8)
+    opt = abi.default_options(precision=precision)
+    ko = tf.options(chi2_cut=15.0, max_candidates=2, end_of_world=1)
+    gpu = _copy_events(tf)
+    fit = _fitter(det)
+    try:
+        fit.find_tracks(opt, ko, gpu)
+        if precision == abi.PRECISION_FP64:
+            ora = _copy_events(tf)
+            kforacle.find_tracks(det.surfaces, det.field, opt, ko, ora,
+                                 n_threads=kforacle.hardware_threads())
+            _check(gpu, ora)
+        start = 0
+        for m in sizes:
+            if m == 0:
+                continue
+            one = generate.ckf_event(det, b.subset(np.arange(start, start + int(m))),
+                                     max_states=32, max_tracks=8)
+            fit.find_tracks(opt, ko, one)
+            base = int(b.meas_offsets[start])
+            for s in range(int(m)):
+                got = [[int(tf.meas_index[x]) for x in gpu.track_measurements(start + s, k)]
+                       for k in range(gpu.n_tracks[start + s])]
+                want = [[int(one.meas_index[x]) + base for x in one.track_measurements(s, k)]
+                        for k in range(one.n_tracks[s])]
+                assert got == want
+            np.testing.assert_array_equal(gpu.track_chi2[start:start + int(m)],
+                                          one.track_chi2[:int(m)])
+            start += int(m)
+    finally:
+        fit.close()

@@ -219,3 +219,28 @@ def test_target_cylinder_around_the_seeds_is_reached_behind():
     assert (tf.status == 0).all() and (tf.n_tracks == 1).all()
     assert (tf.n_states == 0).all() and (tf.track_tip[:, 0] == -1).all()
     assert np.isfinite(tf.track_params[:, 0]).all()
+
+
+def test_events_are_independent():
+    """Several events in one call: each seed searches only its event's
+    measurements, with the result of a call per event."""
+    det = generate.Detector(abi.CKG_BARREL)
+    b = generate.generate(det, 600, seed=41)
+    sizes = [100, 250, 0, 250]
+    multi = _find(det, generate.ckf_events(det, b, sizes), chi2_cut=15.0)
+    assert (multi.status == 0).all()
+    start = 0
+    for m in sizes:
+        if m == 0:
+            continue
+        one = _find(det, generate.ckf_event(det, b.subset(np.arange(start, start + m))),
+                    chi2_cut=15.0)
+        base = int(b.meas_offsets[start])
+        for s in range(m):
+            got = [[int(multi.meas_index[x]) for x in multi.track_measurements(start + s, k)]
+                   for k in range(multi.n_tracks[start + s])]
+            want = [[int(one.meas_index[x]) + base for x in one.track_measurements(s, k)]
+                    for k in range(one.n_tracks[s])]
+            assert got == want
+            assert multi.track_chi2[start + s, 0] == one.track_chi2[s, 0]
+        start += m
