@@ -721,7 +721,8 @@ typedef struct ck_ckf_in {
                                         (all in event 0)                       */
 } ck_ckf_in;
 
-/* Results. Per seed s: its found tracks k < n_tracks[s] at [s*max_tracks + k]
+/* Results (entries beyond a seed's n_tracks / n_states are unspecified).
+ * Per seed s: its found tracks k < n_tracks[s] at [s*max_tracks + k]
  * (the order the search keeps them in) and its track states i < n_states[s]
  * at [s*max_states + i] (creation order; a track is the chain of states from
  * its tip back along state_prev). Vector and matrix arrays hold C values per
