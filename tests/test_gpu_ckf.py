@@ -129,7 +129,8 @@ def test_zero_field_forward_on_gpu():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", ["telescope", "barrel_branching", "barrel_stopper",
-                                  "uneven_end_of_world", "uneven_leaves_map", "target_behind"])
+                                  "uneven_end_of_world", "uneven_leaves_map", "target_behind",
+                                  "strips"])
 def test_fp64_parity(case):
     opt = abi.default_options()
     if case == "telescope":
@@ -154,6 +155,11 @@ def test_fp64_parity(case):
         det = generate.Detector(abi.CKG_UNEVEN)
         tf = generate.ckf_event(det, generate.generate(det, 1000, seed=25))
         kw = dict(chi2_cut=15.0)
+    elif case == "strips":
+        # 1D loc0 and loc1 strips on the outer layers: windows along either axis
+        det = generate.Detector(abi.CKG_STRIPS)
+        tf = generate.ckf_event(det, generate.generate(det, 2000, seed=27))
+        kw = dict(chi2_cut=15.0, max_candidates=2, chi2_cut_outlier=100.0, max_branches=32)
     else:
         base = generate.Detector(abi.CKG_BARREL)
         det = WithTarget(base)
