@@ -16,6 +16,10 @@
 // reference would return. fitBatch() takes many tracks at once (the per-track
 // loop of TrackFittingAlgorithm::execute,
 // Examples/Algorithms/TrackFitting/src/TrackFittingAlgorithm.cpp:117-170).
+// findTracks() is CombinatorialKalmanFilter::findTracks
+// (Core/include/Acts/TrackFinding/CombinatorialKalmanFilter.hpp:1191-1335)
+// for many seeds of one or more events at once, with the default
+// MeasurementSelector and the examples' branch stopper.
 //
 // The ACTS types this build cannot include (Eigen/Boost are not available)
 // are represented by small structs with the same fields; a build against a
@@ -131,6 +135,7 @@ struct KalmanFitterOptions {
 // (EventData/VectorMultiTrajectory.hpp:187-200).
 struct TrackState {
   int surface = -1;
+  int sourceLink = -1;  // findTracks: index of the state's measurement in the input (-1: none)
   uint32_t typeFlags = 0;
   double pathLength = 0;
   double chi2 = 0;
@@ -164,6 +169,27 @@ struct TrackContainer {
   std::vector<TrackState> states;
   std::vector<Track> tracks;
   const TrackState* trackStates(size_t track) const { return states.data() + tracks[track].firstState; }
+};
+
+// CombinatorialKalmanFilterOptions with the propagator options, the
+// MeasurementSelector cuts (one bin) and the examples' branch stopper
+// (TrackSelector::Config): ck_ckf_options (cudakalman.h).
+struct CombinatorialKalmanFilterOptions {
+  ck_options options;
+  ck_ckf_options ckf;
+  CombinatorialKalmanFilterOptions() {
+    ck_options_default(&options);
+    ck_ckf_options_default(&ckf);
+  }
+};
+
+// One seed of a track-finding call: the initial parameters, the
+// DirectNavigator surface sequence and the event whose measurements it sees.
+struct SeedInput {
+  BoundTrackParameters start;
+  const int* surfaceSequence = nullptr;
+  size_t nSurfaces = 0;
+  int event = 0;
 };
 
 // One track of a batch.
@@ -344,6 +370,169 @@ class CudaKalman {
       }
       container.tracks.push_back(tr);
       results.push_back(Result<size_t>::success(container.tracks.size() - 1));
+    }
+    return results;
+  }
+
+  // Finds the tracks of n seeds among the measurements of their events
+  // (measurementEvent[i]: the event of measurement i; NULL: all in event 0).
+  // Every found track is appended to the container (its states in
+  // propagation order, sourceLink set on measurement and outlier states,
+  // smoothed parameters NaN: the search does not smooth); one Result per
+  // seed: the container indices of its tracks, or the seed's error.
+  std::vector<Result<std::vector<size_t>>> findTracks(
+      const SeedInput* seeds, size_t n, const SourceLink* measurements, size_t nMeas,
+      const CombinatorialKalmanFilterOptions& options, TrackContainer& container,
+      int nEvents = 1, const int* measurementEvent = nullptr) const {
+    const int nS = static_cast<int>(m_cfg.surfaces.size());
+    const int nEv = nEvents < 1 ? 1 : nEvents;
+    // measurements grouped by (event, surface), stable: the candidate order
+    std::vector<int64_t> key(nMeas);
+    std::vector<size_t> order(nMeas);
+    std::vector<int32_t> offs(static_cast<size_t>(nEv) * nS + 1, 0);
+    for (size_t i = 0; i < nMeas; ++i) {
+      const int ev = measurementEvent ? measurementEvent[i] : 0;
+      const int sf = measurements[i].surface;
+      if (ev < 0 || ev >= nEv || sf < 0 || sf >= nS)
+        throw std::invalid_argument("measurement event or surface out of range");
+      key[i] = static_cast<int64_t>(ev) * nS + sf;
+      ++offs[key[i] + 1];
+    }
+    for (size_t k = 1; k < offs.size(); ++k) offs[k] += offs[k - 1];
+    {
+      std::vector<int32_t> fill(offs.begin(), offs.end() - 1);
+      for (size_t i = 0; i < nMeas; ++i) order[fill[key[i]]++] = i;
+    }
+    std::vector<double> mv(2 * nMeas), mc(4 * nMeas);
+    std::vector<int32_t> msub(nMeas);
+    for (size_t j = 0; j < nMeas; ++j) {
+      const SourceLink& sl = measurements[order[j]];
+      mv[2 * j] = sl.value[0];
+      mv[2 * j + 1] = sl.value[1];
+      for (int c = 0; c < 4; ++c) mc[4 * j + c] = sl.covariance[c];
+      msub[j] = sl.subspace;
+    }
+    std::vector<int32_t> seqOff(n + 1, 0), seq, pdg(n), sev(n);
+    std::vector<double> sp(6 * n), sc(36 * n), frames(12 * n);
+    std::vector<float> part(2 * n);
+    for (size_t t = 0; t < n; ++t) {
+      const SeedInput& si = seeds[t];
+      for (size_t k = 0; k < si.nSurfaces; ++k) seq.push_back(si.surfaceSequence[k]);
+      seqOff[t + 1] = static_cast<int32_t>(seq.size());
+      std::memcpy(&sp[6 * t], si.start.parameters.data(), 6 * sizeof(double));
+      std::memcpy(&sc[36 * t], si.start.covariance.data(), 36 * sizeof(double));
+      std::memcpy(&frames[12 * t], si.start.planeRotation.data(), 9 * sizeof(double));
+      std::memcpy(&frames[12 * t + 9], si.start.planeCenter.data(), 3 * sizeof(double));
+      part[2 * t] = si.start.mass;
+      part[2 * t + 1] = si.start.absCharge;
+      pdg[t] = si.start.absPdg;
+      sev[t] = si.event;
+    }
+    ck_ckf_in in{};
+    in.n_seeds = static_cast<int32_t>(n);
+    in.memory = CK_MEM_HOST;
+    in.seq_offsets = seqOff.data();
+    in.seq_surfaces = seq.data();
+    in.start_params = sp.data();
+    in.start_cov = sc.data();
+    in.start_frames = frames.data();
+    in.particle = part.data();
+    in.particle_pdg = pdg.data();
+    in.n_meas = static_cast<int32_t>(nMeas);
+    in.n_surfaces = nS;
+    in.surf_meas_offsets = offs.data();
+    in.meas_values = mv.data();
+    in.meas_cov = mc.data();
+    in.meas_subspace = msub.data();
+    in.n_events = nEv;
+    in.seed_event = sev.data();
+    const size_t T = static_cast<size_t>(options.ckf.max_tracks) * n;
+    const size_t S = static_cast<size_t>(options.ckf.max_states) * n;
+    std::vector<int32_t> status(n), nTr(n), nSt(n), tip(T), tnm(T), tnh(T), tno(T), tndf(T),
+        prev(S), surf(S), meas(S);
+    std::vector<uint32_t> flags(S);
+    std::vector<double> tchi2(T), tpar(6 * T), tcov(21 * T), schi2(S), path(S), pr(6 * S),
+        prc(21 * S), fi(6 * S), fic(21 * S), jac(36 * S);
+    ck_ckf_out out{};
+    out.status = status.data();
+    out.n_tracks = nTr.data();
+    out.n_states = nSt.data();
+    out.track_tip = tip.data();
+    out.track_n_measurements = tnm.data();
+    out.track_n_holes = tnh.data();
+    out.track_n_outliers = tno.data();
+    out.track_ndf = tndf.data();
+    out.track_chi2 = tchi2.data();
+    out.track_params = tpar.data();
+    out.track_cov = tcov.data();
+    out.state_prev = prev.data();
+    out.state_surface = surf.data();
+    out.state_flags = flags.data();
+    out.state_measurement = meas.data();
+    out.state_chi2 = schi2.data();
+    out.state_path_length = path.data();
+    out.predicted = pr.data();
+    out.predicted_cov = prc.data();
+    out.filtered = fi.data();
+    out.filtered_cov = fic.data();
+    out.jacobian = jac.data();
+    ck_status st = ck_find_tracks(m_handle, &options.options, &options.ckf, &in, &out, nullptr);
+    if (st != CK_OK) throw std::runtime_error(std::string("ck_find_tracks: ") + ck_last_error());
+
+    auto unpack = [](const double* p, BoundMatrix& m) {
+      for (size_t i = 0, c = 0; i < 6; ++i)
+        for (size_t j = i; j < 6; ++j, ++c) m[i * 6 + j] = m[j * 6 + i] = p[c];
+    };
+    const double nan = std::numeric_limits<double>::quiet_NaN();
+    std::vector<Result<std::vector<size_t>>> results;
+    results.reserve(n);
+    for (size_t s = 0; s < n; ++s) {
+      if (status[s] != CK_TRACK_OK) {
+        results.push_back(Result<std::vector<size_t>>::failure(status[s]));
+        continue;
+      }
+      std::vector<size_t> found;
+      for (int k = 0; k < nTr[s]; ++k) {
+        const size_t ti = s * options.ckf.max_tracks + k;
+        std::vector<int> chain;
+        for (int i = tip[ti]; i >= 0; i = prev[s * options.ckf.max_states + i]) chain.push_back(i);
+        Track tr;
+        tr.firstState = container.states.size();
+        tr.nStates = chain.size();
+        tr.nMeasurements = static_cast<size_t>(tnm[ti]);
+        tr.nHoles = static_cast<size_t>(tnh[ti]);
+        tr.nOutliers = static_cast<size_t>(tno[ti]);
+        tr.nDoF = static_cast<size_t>(tndf[ti]);
+        tr.chi2 = tchi2[ti];
+        if (tpar[6 * ti] == tpar[6 * ti]) {  // parameters on the target surface
+          tr.referenceSurface = options.ckf.target_surface;
+          for (size_t c = 0; c < 6; ++c) tr.parameters[c] = tpar[6 * ti + c];
+          BoundMatrix m{};
+          unpack(&tcov[21 * ti], m);
+          for (size_t c = 0; c < 36; ++c) tr.covariance[c] = m[c];
+        }
+        for (auto it = chain.rbegin(); it != chain.rend(); ++it) {
+          const size_t i = s * options.ckf.max_states + *it;
+          TrackState ts;
+          ts.surface = surf[i];
+          ts.typeFlags = flags[i];
+          ts.pathLength = path[i];
+          ts.chi2 = schi2[i];
+          ts.sourceLink = meas[i] >= 0 ? static_cast<int>(order[meas[i]]) : -1;
+          for (size_t c = 0; c < 6; ++c) {
+            ts.predicted[c] = pr[6 * i + c];
+            ts.filtered[c] = fi[6 * i + c];
+            ts.smoothed[c] = nan;
+          }
+          unpack(&prc[21 * i], ts.predictedCovariance);
+          unpack(&fic[21 * i], ts.filteredCovariance);
+          for (size_t c = 0; c < 36; ++c) ts.jacobian[c] = jac[36 * i + c];
+          container.states.push_back(ts);
+        }
+        container.tracks.push_back(tr);
+        found.push_back(container.tracks.size() - 1);
+      }
+      results.push_back(Result<std::vector<size_t>>::success(found));
     }
     return results;
   }

@@ -1,6 +1,7 @@
 // Exercises the C++ facade ActsPlugins::CudaKalman the way a reference user
 // calls KalmanFitter::fit: per track (iterator range of source links, start
-// parameters, options, surface sequence, track container) and batched.
+// parameters, options, surface sequence, track container) and batched; and
+// CombinatorialKalmanFilter::findTracks over the same event's measurements.
 // Exit code 0 on success. Needs a GPU.
 #include <cmath>
 #include <cstdio>
@@ -131,6 +132,42 @@ int main() {
     threw = true;
   }
   if (!threw) return 6;
+  // track finding: every track's start parameters as a seed among all the
+  // event's measurements (CombinatorialKalmanFilter::findTracks)
+  {
+    std::vector<SourceLink> all;
+    std::vector<int> owner;
+    for (int t = 0; t < n; ++t)
+      for (const SourceLink& sl : links[t]) {
+        all.push_back(sl);
+        owner.push_back(t);
+      }
+    std::vector<SeedInput> seeds(n);
+    for (int t = 0; t < n; ++t) {
+      seeds[t].start = inputs[t].start;
+      seeds[t].surfaceSequence = seqs[t].data();
+      seeds[t].nSurfaces = seqs[t].size();
+    }
+    CombinatorialKalmanFilterOptions co;
+    co.ckf.chi2_cut = 15.0;
+    TrackContainer found;
+    std::vector<Result<std::vector<size_t>>> fr =
+        fitter.findTracks(seeds.data(), n, all.data(), all.size(), co, found);
+    size_t own = 0, hits = 0;
+    for (int t = 0; t < n; ++t) {
+      if (!fr[t].ok() || fr[t].value().size() != 1) return 10;
+      const size_t k = fr[t].value()[0];
+      const TrackState* st = found.trackStates(k);
+      for (size_t i = 0; i < found.tracks[k].nStates; ++i) {
+        if (st[i].sourceLink < 0) continue;
+        ++hits;
+        own += owner[st[i].sourceLink] == t ? 1 : 0;
+        if (!(st[i].filteredCovariance[0] > 0) || st[i].hasSmoothed()) return 11;
+      }
+    }
+    if (hits < 9 * static_cast<size_t>(n) || own < hits * 95 / 100) return 12;
+    std::printf("findTracks ok: %d seeds, %zu of %zu hits their own\n", n, own, hits);
+  }
   std::printf("facade ok: %d tracks, chi2/ndf %.3f\n", n, chi2 / ndf);
   return 0;
 }

@@ -1,5 +1,6 @@
 """C++ facade (acts_gb300/host/ActsPlugins/CudaKalman.hpp): compiles on CPU;
-per-track and batched fits through it on the GPU agree bit for bit."""
+per-track and batched fits through it on the GPU agree bit for bit; track
+finding through it finds each seed's own hits."""
 import os
 import subprocess
 
@@ -34,3 +35,4 @@ def test_facade_runs_on_gpu(tmp_path):
     print(r.stdout)
     assert r.returncode == 0, r.stdout
     assert "facade ok" in r.stdout
+    assert "findTracks ok" in r.stdout
