@@ -429,9 +429,14 @@ struct CkfLane : Lane<P, CV> {
       return CK_TRACK_NOT_ON_SURFACE;
     double bp[6];
     if (!this->freeToBound(fp, sf, l, bp)) return CK_TRACK_NOT_ON_SURFACE;
+    // the mixed form's predicted chi2 and update run in FP32 on its float
+    // covariance (as in its fit)
+    constexpr bool kF32 = sizeof(CV) == sizeof(float);
     double Pp[21];
+    if constexpr (!kF32) {
 #pragma unroll
-    for (int i = 0; i < 21; ++i) Pp[i] = toD(cov[i]);
+      for (int i = 0; i < 21; ++i) Pp[i] = toD(cov[i]);
+    }
     constexpr bool kFastRcp = sizeof(P) == sizeof(float);
     CkfBranch* stk = stack(cp);
     const int prevTip = stk[nActive - 1].tip;
@@ -455,8 +460,13 @@ struct CkfLane : Lane<P, CV> {
       double V[4];
 #pragma unroll
       for (int c = 0; c < 4; ++c) V[c] = __ldg(&fp.meas_cov[4 * (size_t)m + c]);
-      const double c2 = predictedChi2Sub<kFastRcp>(bp, Pp, sub, __ldg(&fp.meas_val[2 * (size_t)m]),
-                                                   __ldg(&fp.meas_val[2 * (size_t)m + 1]), V);
+      double c2;
+      if constexpr (kF32)
+        c2 = predictedChi2SubF(bp, cov, sub, __ldg(&fp.meas_val[2 * (size_t)m]),
+                               __ldg(&fp.meas_val[2 * (size_t)m + 1]), V);
+      else
+        c2 = predictedChi2Sub<kFastRcp>(bp, Pp, sub, __ldg(&fp.meas_val[2 * (size_t)m]),
+                                        __ldg(&fp.meas_val[2 * (size_t)m + 1]), V);
       if (c2 < minChi2 || (c2 == minChi2 && m < minM)) {
         minChi2 = c2;
         minM = m;
@@ -487,7 +497,7 @@ struct CkfLane : Lane<P, CV> {
       // smallest chi2 below the outlier cut. The bound carries a relative
       // margin of 1e-5 for the rounding of the computed chi2.
       const double pk = bp[axis];
-      const double den = __ldg(&cp.surfVmax[seg]) + Pp[sidx(axis, axis)];
+      const double den = __ldg(&cp.surfVmax[seg]) + toD(cov[sidx(axis, axis)]);
       const double* key = cp.sortedKey;
       int lo = m0, hi = m1;  // first key >= pk
       while (lo < hi) {
@@ -588,14 +598,21 @@ struct CkfLane : Lane<P, CV> {
           double V[4];
 #pragma unroll
           for (int c = 0; c < 4; ++c) V[c] = __ldg(&fp.meas_cov[4 * (size_t)m + c]);
-          double filt[6], F[21], c2 = 0.0;
-          if (!kalmanUpdateSub<kFastRcp>(bp, Pp, sub, __ldg(&fp.meas_val[2 * (size_t)m]),
-                                         __ldg(&fp.meas_val[2 * (size_t)m + 1]), V,
-                                         fp.opt.joseph != 0, filt, F, c2))
-            return CK_TRACK_UPDATE_FAILED;
+          double filt[6], c2 = 0.0;
           CV Fc[21];
+          const double mv0 = __ldg(&fp.meas_val[2 * (size_t)m]);
+          const double mv1 = __ldg(&fp.meas_val[2 * (size_t)m + 1]);
+          if constexpr (kF32) {
+            if (!kalmanUpdateSubF(bp, cov, sub, mv0, mv1, V, fp.opt.joseph != 0, filt, Fc, c2))
+              return CK_TRACK_UPDATE_FAILED;
+          } else {
+            double F[21];
+            if (!kalmanUpdateSub<kFastRcp>(bp, Pp, sub, mv0, mv1, V, fp.opt.joseph != 0, filt, F,
+                                           c2))
+              return CK_TRACK_UPDATE_FAILED;
 #pragma unroll
-          for (int c = 0; c < 21; ++c) Fc[c] = toP<CV>(F[c]);
+            for (int c = 0; c < 21; ++c) Fc[c] = toP<CV>(F[c]);
+          }
           writeFiltered(cp, b.tip, filt, Fc);
           if (cp.out.state_chi2) cp.out.state_chi2[stateIdx(cp, b.tip)] = c2;
           ++b.nMeas;

@@ -995,6 +995,98 @@ CK_D bool kalmanUpdateSub(const double pred[6], const double Pp[21], int sub, do
   return true;
 }
 
+// kalmanUpdateSub in FP32 (the mixed form): the same algebra on the float
+// covariance the mixed form stores, with the residuals formed in FP64 and
+// the parameter correction K r added to the FP64 parameters; the gain, the
+// covariance update and the chi2 run on the FP32 pipe.
+CK_D bool kalmanUpdateSubF(const double pred[6], const float P[21], int sub, double m0, double m1,
+                           const double Vin[4], bool joseph, double filt[6], float F[21],
+                           double& chi2) {
+  const bool two = sub == CK_MEAS_LOC01;
+  const bool a1 = sub == CK_MEAS_LOC1;
+  const float V0 = d2f(Vin[0]), V1 = two ? d2f(Vin[1]) : 0.0f, V2 = two ? d2f(Vin[2]) : 0.0f,
+              V3 = two ? d2f(Vin[3]) : 0.0f;
+  float ra[6], r1[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    r1[j] = P[sidx(1, j)];
+    ra[j] = a1 ? r1[j] : P[sidx(0, j)];
+  }
+  const float s00 = (a1 ? ra[1] : ra[0]) + V0, s01 = two ? ra[1] + V1 : 0.0f,
+              s10 = two ? r1[0] + V2 : 0.0f, s11 = two ? r1[1] + V3 : 1.0f;
+  const float idet = 1.0f / (s00 * s11 - s01 * s10);
+  const float i00 = s11 * idet, i01 = -s01 * idet, i10 = -s10 * idet, i11 = s00 * idet;
+  float K[6][2];
+  bool nan = false;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    const float pa = a1 ? P[sidx(i, 1)] : P[sidx(i, 0)], p1 = P[sidx(i, 1)];
+    K[i][0] = pa * i00 + p1 * i10;
+    K[i][1] = two ? pa * i01 + p1 * i11 : 0.0f;
+    nan |= isnan(K[i][0]) || isnan(K[i][1]);
+  }
+  if (nan) return false;
+  const float r0 = d2f(m0 - (a1 ? pred[1] : pred[0]));
+  const float rr1 = two ? d2f(m1 - pred[1]) : 0.0f;
+#pragma unroll
+  for (int i = 0; i < 6; ++i) filt[i] = pred[i] + (double)(K[i][0] * r0 + K[i][1] * rr1);
+  normalizePhiTheta(filt[2], filt[3]);
+  if (!joseph) {
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int j = i; j < 6; ++j)
+        F[sidx(i, j)] = P[sidx(i, j)] - (K[i][0] * ra[j] + K[i][1] * r1[j]);
+  } else {
+    float AP[6][6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int j = 0; j < 6; ++j)
+        AP[i][j] = P[sidx(i, j)] - (K[i][0] * ra[j] + K[i][1] * r1[j]);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      const float kv0 = K[i][0] * V0 + K[i][1] * V2;
+      const float kv1 = K[i][0] * V1 + K[i][1] * V3;
+      const float apa = a1 ? AP[i][1] : AP[i][0];
+#pragma unroll
+      for (int j = i; j < 6; ++j) {
+        const float apat = AP[i][j] - (apa * K[j][0] + AP[i][1] * K[j][1]);
+        F[sidx(i, j)] = apat + (kv0 * K[j][0] + kv1 * K[j][1]);
+      }
+    }
+  }
+  const float s0 = d2f(m0 - (a1 ? filt[1] : filt[0]));
+  const float s1 = two ? d2f(m1 - filt[1]) : 0.0f;
+  const float ka0 = a1 ? K[1][0] : K[0][0], ka1 = a1 ? K[1][1] : K[0][1];
+  const float b00 = 1.0f - ka0, b01 = -ka1, b10 = -K[1][0], b11 = 1.0f - K[1][1];
+  const float c00 = b00 * V0 + b01 * V2, c01 = two ? b00 * V1 + b01 * V3 : 0.0f,
+              c10 = two ? b10 * V0 + b11 * V2 : 0.0f, c11 = two ? b10 * V1 + b11 * V3 : 1.0f;
+  const float jdet = 1.0f / (c00 * c11 - c01 * c10);
+  const float t0 = s0 * (c11 * jdet) + s1 * (-c10 * jdet);
+  const float t1 = s0 * (-c01 * jdet) + s1 * (c00 * jdet);
+  chi2 = (double)(t0 * s0 + t1 * s1);
+  return true;
+}
+
+// predictedChi2Sub in FP32 on the mixed form's float covariance (residuals
+// formed in FP64)
+CK_D double predictedChi2SubF(const double pred[6], const float P[21], int sub, double m0,
+                              double m1, const double Vin[4]) {
+  const bool two = sub == CK_MEAS_LOC01;
+  const bool a1 = sub == CK_MEAS_LOC1;
+  const float r0 = d2f(m0 - (a1 ? pred[1] : pred[0]));
+  const float r1 = two ? d2f(m1 - pred[1]) : 0.0f;
+  const float s00 = d2f(Vin[0]) + (a1 ? P[sidx(1, 1)] : P[sidx(0, 0)]);
+  const float s01 = two ? d2f(Vin[1]) + P[sidx(0, 1)] : 0.0f;
+  const float s10 = two ? d2f(Vin[2]) + P[sidx(1, 0)] : 0.0f;
+  const float s11 = two ? d2f(Vin[3]) + P[sidx(1, 1)] : 1.0f;
+  const float idet = 1.0f / (s00 * s11 - s01 * s10);
+  const float t0 = r0 * (s11 * idet) + r1 * (-s10 * idet);
+  const float t1 = r0 * (-s01 * idet) + r1 * (s00 * idet);
+  return (double)(t0 * r0 + t1 * r1);
+}
+
 // calculatePredictedChi2 for either subspace (as kalmanUpdateSub)
 template <bool FASTRCP = false>
 CK_D double predictedChi2Sub(const double pred[6], const double Pp[21], int sub, double m0,

@@ -735,9 +735,15 @@ struct Lane {
       // (the reversed pass's states are not part of the track: no records)
       if (!REV && nStates >= fp.max_states) return CK_TRACK_TOO_MANY_STATES;
       const int k = nStates++;
+      // the mixed form's update and predicted chi2 run in FP32 on its float
+      // covariance (with the free-to-bound correction, whose unscented
+      // transform is sensitive to it, in FP64)
+      constexpr bool kF32Update = sizeof(CV) == sizeof(float) && !F2B;
       double Pp[21];
+      if constexpr (!kF32Update) {
 #pragma unroll
-      for (int i = 0; i < 21; ++i) Pp[i] = toD(cov[i]);
+        for (int i = 0; i < 21; ++i) Pp[i] = toD(cov[i]);
+      }
       if constexpr (!REV) {
 #pragma unroll
         for (int i = 0; i < 6; ++i) rec.p(k, kRecPred + i) = bp[i];
@@ -757,14 +763,27 @@ struct Lane {
       flags |= (uint32_t)sub << kRecSubShift;
       bool outlier = false;
       constexpr bool kFastRcp = sizeof(P) == sizeof(float);
-      if (fp.opt.useOutlierCut)
-        outlier = predictedChi2Sub<kFastRcp>(bp, Pp, sub, mv0, mv1, V) > fp.opt.outlierChi2Cut;
+      if (fp.opt.useOutlierCut) {
+        if constexpr (kF32Update)
+          outlier = predictedChi2SubF(bp, cov, sub, mv0, mv1, V) > fp.opt.outlierChi2Cut;
+        else
+          outlier = predictedChi2Sub<kFastRcp>(bp, Pp, sub, mv0, mv1, V) > fp.opt.outlierChi2Cut;
+      }
       double chi2 = 0.0;
       if (!outlier) {
-        double filt[6], F[21];
+        double filt[6];
+        CV F[21];
         const bool joseph = fp.opt.joseph != 0;
-        if (!kalmanUpdateSub<kFastRcp>(bp, Pp, sub, mv0, mv1, V, joseph, filt, F, chi2))
-          return CK_TRACK_UPDATE_FAILED;
+        if constexpr (kF32Update) {
+          if (!kalmanUpdateSubF(bp, cov, sub, mv0, mv1, V, joseph, filt, F, chi2))
+            return CK_TRACK_UPDATE_FAILED;
+        } else {
+          double Fd[21];
+          if (!kalmanUpdateSub<kFastRcp>(bp, Pp, sub, mv0, mv1, V, joseph, filt, Fd, chi2))
+            return CK_TRACK_UPDATE_FAILED;
+#pragma unroll
+          for (int i = 0; i < 21; ++i) F[i] = toP<CV>(Fd[i]);
+        }
         flags |= CK_FLAG_HAS_MEASUREMENT;
         if constexpr (REV) {
           // the latest filtered measurement state of the reversed pass
@@ -773,7 +792,7 @@ struct Lane {
 #pragma unroll
           for (int i = 0; i < 6; ++i) es.par[i] = filt[i];
 #pragma unroll
-          for (int i = 0; i < 21; ++i) es.cov[i] = (double)toP<CV>(F[i]);
+          for (int i = 0; i < 21; ++i) es.cov[i] = (double)F[i];
           es.surface = sid;
         } else {
 #pragma unroll
@@ -782,7 +801,7 @@ struct Lane {
         updateFree(sf, bp, filt, l);
 #pragma unroll
         for (int i = 0; i < 21; ++i) {
-          cov[i] = toP<CV>(F[i]);
+          cov[i] = F[i];
           if constexpr (!REV) rec.m(k, kRecFiltCov + i) = cov[i];
         }
         initTP(sp);
