@@ -45,6 +45,26 @@ class Results:
         self.track_params = np.zeros(6 * n, np.float64) if ref else None
         self.track_cov = np.zeros(36 * n, np.float64) if ref else None
 
+    ARRAYS = ("status", "n_states", "n_measurements", "n_holes", "n_outliers", "ndf",
+              "chi2_sum", "state_surface", "state_flags", "state_path_length", "state_chi2",
+              "predicted", "predicted_cov", "filtered", "filtered_cov", "smoothed",
+              "smoothed_cov", "jacobian", "track_params", "track_cov")
+
+    def pinned(self):
+        """Moves the buffers to page-locked host memory (torch pin_memory),
+        which the fit writes in place from the device; returns self."""
+        import torch
+
+        self._pinned = []
+        for name in self.ARRAYS:
+            a = getattr(self, name)
+            if a is None:
+                continue
+            t = torch.from_numpy(a).pin_memory()
+            self._pinned.append(t)
+            setattr(self, name, t.numpy())
+        return self
+
     def as_batch_out(self):
         o = abi.ck_batch_out()
         o.max_states = self.max_states
