@@ -5,6 +5,10 @@
 * acts_gb300/_lib/libckgen.so — the synthetic event generator (g++).
 * oracle/_build/libkforacle.so — the CPU oracle used by tests and the CPU
   baseline (make -C oracle).
+* acts_gb300/_acts_gb300_ext*.so — the pybind11 module of
+  makeKalmanFitterFunction over the C ABI, when pybind11 is importable
+  (skipped otherwise; acts_gb300.track_fitting covers the same through
+  ctypes).
 
 Nothing is installed outside the repository; outputs are git-ignored.
 """
@@ -61,6 +65,25 @@ def build_generator(force=False):
     return out
 
 
+def build_pybind(force=False):
+    """The pybind11 module, linked against libcudakalman.so (rpath $ORIGIN/_lib).
+    Returns its path, or None when pybind11 is not importable."""
+    try:
+        import pybind11
+    except ImportError:
+        return None
+    import sysconfig
+
+    out = os.path.join(HERE, "_acts_gb300_ext" + sysconfig.get_config_var("EXT_SUFFIX"))
+    src = os.path.join(CSRC, "ck_pybind.cpp")
+    if force or _stale(out, [src, os.path.join(INCLUDE, "cudakalman.h")]):
+        _run([CXX, "-O2", "-std=c++17", "-fPIC", "-shared", "-fvisibility=hidden",
+              "-I" + INCLUDE, "-I" + pybind11.get_include(),
+              "-I" + sysconfig.get_paths()["include"], src, "-o", out,
+              "-L" + LIBDIR, "-lcudakalman", "-Wl,-rpath,$ORIGIN/_lib"])
+    return out
+
+
 def build_oracle(force=False):
     odir = os.path.join(ROOT, "oracle")
     if force:
@@ -106,6 +129,7 @@ def build_all(force=False, oracle=True, verbose=False):
         res = {"generator": f_gen.result(), "cuda": f_cuda.result()[0]}
         if f_ora is not None:
             res["oracle"] = f_ora.result()
+    res["pybind"] = build_pybind(force)
     return res
 
 
