@@ -282,9 +282,6 @@ size_t recordBytesPerTrack(int maxStates, int precision) {
   return (size_t)maxStates * recordStateBytes(precision) + 2 * sizeof(int32_t);
 }
 
-// Allocates (grow-only) the scratch of a batch pipeline: the track-state
-// records of n tracks, the queue permutation and the tips. Never called
-// while a stream is being captured.
 ck_status validateReference(const ck_handle* h, const ck_options* o) {
   if (o->reference_surface < 0) return CK_OK;
   if (o->reference_surface >= h->nSurfaces)
@@ -294,6 +291,9 @@ ck_status validateReference(const ck_handle* h, const ck_options* o) {
   return CK_OK;
 }
 
+// Allocates (grow-only) the scratch of a batch pipeline: the track-state
+// records of n tracks, the queue permutation, the tips and the tail-smoothing
+// marks. Never called while a stream is being captured.
 ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, int precision,
                           bool extrapolate) {
   (void)h;
@@ -304,7 +304,8 @@ ck_status preparePipeline(ck_handle* h, FitContext& c, int n, int maxStates, int
       (e = c.perm.ensure((size_t)n * sizeof(int32_t) + 16)) ||
       (e = c.tip.ensure((size_t)n * sizeof(int32_t) + 16)) ||
       (e = c.sortCounts.ensure(sortCountsBytes(n))) ||
-      (e = c.ticket.ensure(sizeof(int32_t))))
+      (e = c.smoothed.ensure((size_t)n + 16)) ||
+      (e = c.ticket.ensure(2 * sizeof(int32_t))))
     return cudaFail(e, "scratch allocation");
   return CK_OK;
 }
@@ -324,7 +325,7 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
   int32_t* dTicket = (int32_t*)c.ticket.p;
   int launches = 0;
   h->lastChunks = 0;
-  cudaMemsetAsync(dTicket, 0, sizeof(int32_t), st);
+  cudaMemsetAsync(dTicket, 0, 2 * sizeof(int32_t), st);  // queue and tail-smoothing tickets
   if (n > 0) cudaMemsetAsync(c.tip.p, 0xff, sizeof(int32_t) * (size_t)n, st);
   const int32_t* perm = nullptr;
   if (h->sortQueue && n > 0) {
@@ -379,6 +380,15 @@ ck_status enqueuePipeline(ck_handle* h, FitContext& c, const ck_options& opt,
   fp.ref_surface = opt.reference_surface;
   fp.ref_strategy = opt.reference_strategy;
   fp.ext = needsExtStart(opt) ? (ExtStart*)c.ext.p : nullptr;
+  // smoothing in the forward filter's tail: the compaction kernels (variants
+  // 3 and 4, and the free-to-bound correction's), without reverse filtering
+  if (h->tailSmoothing && n > 0 && c.smoothed.p && c.smoothed.cap >= (size_t)n &&
+      c.ticket.cap >= 2 * sizeof(int32_t) && !anyReverse(opt) &&
+      (f2b || tn.variant == 3 || tn.variant == 4)) {
+    cudaMemsetAsync(c.smoothed.p, 0, (size_t)n, st);
+    fp.smoothed = (uint8_t*)c.smoothed.p;
+    fp.smooth_ticket = dTicket + 1;
+  }
   {
     // the extrapolation's propagator options: the reference's defaults
     // (KalmanFitter.hpp:960-961 constructs them without the fit's options)
@@ -888,15 +898,17 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
   if (in->memory == CK_MEM_HOST && n > 0) {
     if (!in->seq_offsets || !in->meas_offsets)
       return fail(CK_ERR_INVALID_ARGUMENT, "offsets missing");
+    // (the kernels read the CSR rows [off[t], off[t + 1]) of the copied
+    // arrays, and chunk boundaries cut them: the offsets must be a
+    // non-decreasing partition)
+    if (in->seq_offsets[0] < 0 || in->meas_offsets[0] < 0)
+      return fail(CK_ERR_INVALID_ARGUMENT, "negative CSR offset");
+    for (int t = 0; t < n; ++t)
+      if (in->seq_offsets[t + 1] < in->seq_offsets[t] || in->meas_offsets[t + 1] < in->meas_offsets[t])
+        return fail(CK_ERR_INVALID_ARGUMENT, "decreasing CSR offsets");
     const int nSeq = in->seq_offsets[n], nMeas = in->meas_offsets[n];
-    if (nSeq < 0 || nMeas < 0) return fail(CK_ERR_INVALID_ARGUMENT, "negative CSR size");
-    if (out->memory == CK_MEM_HOST && chunkTracksOf(h) > 0 && n >= 2 * chunkTracksOf(h)) {
-      // (chunk boundaries need monotone offsets)
-      for (int t = 0; t < n; ++t)
-        if (in->seq_offsets[t + 1] < in->seq_offsets[t] || in->meas_offsets[t + 1] < in->meas_offsets[t])
-          return fail(CK_ERR_INVALID_ARGUMENT, "decreasing CSR offsets");
+    if (out->memory == CK_MEM_HOST && chunkTracksOf(h) > 0 && n >= 2 * chunkTracksOf(h))
       return fitBatchHostChunked(h, *opt, *in, *out, st);
-    }
     struct Item {
       const void* src;
       size_t bytes;
@@ -1002,7 +1014,9 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
     key.scratch[3] = h->ctx.perm.p;
     key.scratch[4] = h->ctx.ticket.p;
     key.scratch[5] = h->ctx.tip.p;
+    key.scratch[6] = h->ctx.smoothed.p;
     key.sort = h->sortQueue;
+    key.tailSmoothing = h->tailSmoothing;
     if (!h->graphExec || std::memcmp(&key, &h->graphKey, sizeof(key)) != 0) {
       if (h->graphExec) {
         cudaGraphExecDestroy(h->graphExec);
@@ -1175,6 +1189,13 @@ ck_status ck_set_steps_per_round(ck_handle* h, int32_t precision, int32_t steps)
     cudaGraphExecDestroy(h->graphExec);
     h->graphExec = nullptr;
   }
+  return CK_OK;
+}
+
+ck_status ck_set_tail_smoothing(ck_handle* h, int32_t enable) {
+  if (!h) return fail(CK_ERR_INVALID_ARGUMENT, "NULL handle");
+  std::lock_guard<std::mutex> lock(h->mu);
+  h->tailSmoothing = enable != 0;
   return CK_OK;
 }
 

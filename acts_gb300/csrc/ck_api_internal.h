@@ -39,8 +39,9 @@ struct GraphKey {
   ck_options opt;
   Tune tune;
   cudaStream_t stream;
-  void* scratch[6];
+  void* scratch[7];
   bool sort;
+  bool tailSmoothing;
   GraphKey() { std::memset(this, 0, sizeof(*this)); }
 };
 
@@ -51,8 +52,10 @@ int occupancyBlocks(int precision, int variant, int tpb);
 // owns one per stream.
 struct FitContext {
   DevBuf rec, perm, ticket, tip, sortCounts;
-  DevBuf ext;  // extrapolation start states (reference surface set)
+  DevBuf ext;       // extrapolation start states (reference surface set)
+  DevBuf smoothed;  // per queue position: smoothed in the forward filter's tail
   void release() {
+    smoothed.release();
     ext.release();
     sortCounts.release();
     tip.release();
@@ -127,6 +130,8 @@ struct ck_handle {
   std::string tuneLog;
   int useGraph = 1;
   bool sortQueue = true;
+  // smoothing in the compaction kernels' tail (ck_set_tail_smoothing)
+  bool tailSmoothing = true;
   ck::DevBuf inBufs[ck::kInputArrays];
   ck::DevBuf outBufs[ck::kOutArrays];
   ck::FitContext ctx;

@@ -1773,7 +1773,10 @@ struct Lane {
         return;
       }
     } else {
-      fp.tip[slot] = lastMeasurementIndex;
+      // (with smoothing in the tail the tip publishes the track: its records
+      // are ordered before it for the blocks that read them)
+      if (fp.smoothed) __threadfence();
+      *(volatile int32_t*)&fp.tip[slot] = lastMeasurementIndex;
     }
     phase = PH_FETCH;
   }
@@ -2202,6 +2205,33 @@ __device__ __forceinline__ void advanceSlot(const FitParams& fp, Lane<P, CV, F2B
   }
 }
 
+// Smoothing in the forward filter's tail, by a warp whose block has no
+// forward work left: claims 32 queue positions at a time, in queue order,
+// and smooths those whose forward pass has ended successfully (tip >= 0,
+// published after the track's records); positions still in flight, or
+// failed, are left to the smoother kernel. Nothing waits: each position is
+// claimed once, and the smoother kernel, launched after this kernel, takes
+// every successful track not marked smoothed.
+template <typename CV>
+__device__ __noinline__ void smoothInTail(const FitParams& fp) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  while (true) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(fp.smooth_ticket, 32);
+    base = __shfl_sync(FULL, base, 0);
+    if (base >= fp.n_queue) return;
+    const int q = base + lane;
+    const int tip = q < fp.n_queue ? *(const volatile int32_t*)&fp.tip[q] : -1;
+    if (tip >= 0) {
+      __threadfence();  // (the records, after the tip that published them)
+      Smoother<CV> S;
+      S.run(fp, q, fp.perm ? __ldg(&fp.perm[q]) : q, tip);
+      fp.smoothed[q] = 1;
+    }
+  }
+}
+
 template <typename P, typename CV, int S, bool F2B = false, bool REV = false>
 __global__ void __launch_bounds__(S, 1) fitKernelCompact(FitParams fp) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -2267,6 +2297,9 @@ __global__ void __launch_bounds__(S, 1) fitKernelCompact(FitParams fp) {
       st[slot] = L;
     }
     __syncthreads();
+  }
+  if constexpr (!REV) {
+    if (fp.smoothed) smoothInTail<CV>(fp);
   }
 }
 
@@ -2434,6 +2467,7 @@ __global__ void __launch_bounds__(BLOCK) smoothKernelStaged(FitParams fp) {
   for (int q0 = blockIdx.x * BLOCK; q0 < fp.n_queue; q0 += gridDim.x * BLOCK) {
     const int q = q0 + threadIdx.x;
     int tip = q < fp.n_queue ? fp.tip[q] : -1;
+    if (tip >= 0 && fp.smoothed && fp.smoothed[q]) tip = -1;  // smoothed in the filter's tail
     // (tracks the reverse-filtering logic selects take the reversed pass)
     if (tip >= 0 && fp.opt.reverseMomThreshold > 0.0 && reverseSelected<CV>(fp, q, tip)) tip = -1;
     const int iters = __reduce_max_sync(FULL, tip + 1);
@@ -2510,6 +2544,7 @@ __global__ void __launch_bounds__(BLOCK) smoothKernel(FitParams fp) {
        q += gridDim.x * blockDim.x) {
     const int tip = fp.tip[q];
     if (tip < 0) continue;
+    if (fp.smoothed && fp.smoothed[q]) continue;  // smoothed in the filter's tail
     // (tracks the reverse-filtering logic selects take the reversed pass)
     if (fp.opt.reverseMomThreshold > 0.0 && reverseSelected<CV>(fp, q, tip)) continue;
     Smoother<CV> S;

@@ -177,6 +177,12 @@ struct FitParams {
   ExtStart* ext;
   DevOptions extOpt;
   PropIO prop;
+  // Smoothing in the forward filter's tail (compaction kernels): a block
+  // whose slots are all done smooths finished tracks, claimed in queue order
+  // by the ticket smooth_ticket; smoothed[q] = 1 marks them for the smoother
+  // kernel, which takes the rest. NULL: the smoother kernel smooths all.
+  uint8_t* smoothed;
+  int32_t* smooth_ticket;
 };
 
 }  // namespace ck

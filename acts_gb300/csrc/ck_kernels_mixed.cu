@@ -1,8 +1,9 @@
 // ck_kernels_mixed.cu — instantiations of the mixed-precision fit kernel:
 // Runge-Kutta stages, Jacobian transport, field interpolation and covariance
 // transport in FP32, with the free parameters accumulated in FP64 from the
-// FP32 stage increments; Kalman update (Joseph form when selected), 2x2
-// inverse, smoother-gain inverse, bound-parameter conversion and chi2 in FP64.
+// FP32 stage increments; the Kalman update (gain, 2x2 inverse, covariance
+// update, chi2) in FP32 on FP64 residuals; smoother-gain inverse and
+// bound-parameter conversion in FP64.
 #include "ck_fitter.cuh"
 #include "ck_launch.h"
 

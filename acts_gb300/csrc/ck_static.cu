@@ -40,7 +40,7 @@ namespace {
 
 constexpr size_t kStaticScratchBytes = size_t(32) << 20;
 constexpr size_t kAlign = 256;
-constexpr size_t kTicketBytes = 256;  // the queue ticket
+constexpr size_t kTicketBytes = 256;  // the queue and tail-smoothing tickets
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_staticScratch[kStaticScratchBytes];
@@ -52,7 +52,7 @@ size_t roundUp(size_t b) { return (b + kAlign - 1) & ~(kAlign - 1); }
 
 // Scratch layout for n tracks of up to maxStates states.
 struct Layout {
-  size_t rec, perm, tip, sortCounts, ticket, ext, total;
+  size_t rec, perm, tip, sortCounts, ticket, smoothed, ext, total;
 };
 
 // ext: the extrapolation start states (only with a reference surface)
@@ -64,8 +64,9 @@ Layout layoutFor(int n, int maxStates, int precision, bool ext) {
   l.tip = roundUp((size_t)n * sizeof(int32_t));
   l.sortCounts = roundUp(sortCountsBytes(n));
   l.ticket = kTicketBytes;
+  l.smoothed = roundUp((size_t)n);
   l.ext = ext ? roundUp((size_t)n * 2 * sizeof(ExtStart)) : 0;
-  l.total = l.rec + l.perm + l.tip + l.sortCounts + l.ticket + l.ext;
+  l.total = l.rec + l.perm + l.tip + l.sortCounts + l.ticket + l.smoothed + l.ext;
   return l;
 }
 
@@ -141,6 +142,7 @@ ck_status ck_fit_batch_static(ck_handle* h, const ck_options* opt, const ck_batc
   view(c.tip, l.tip);
   view(c.sortCounts, l.sortCounts);
   view(c.ticket, l.ticket);
+  view(c.smoothed, l.smoothed);
   if (l.ext) view(c.ext, l.ext);
   cudaStream_t st = stream ? (cudaStream_t)stream : h->stream;
   const Tune tn = h->tune[opt->precision];

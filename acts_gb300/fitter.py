@@ -79,6 +79,7 @@ def lib():
         L.ck_get_launch_variant.argtypes = [C.c_void_p, C.c_int32, P(C.c_int32), P(C.c_int32)]
         L.ck_set_launch_config.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
         L.ck_sort_queue.argtypes = [C.c_void_p, C.c_int32]
+        L.ck_set_tail_smoothing.argtypes = [C.c_void_p, C.c_int32]
         L.ck_autotune.argtypes = [C.c_void_p, P(abi.ck_options), P(abi.ck_batch_in),
                                   P(abi.ck_batch_out)]
         L.ck_autotune_log.restype = C.c_char_p
@@ -373,6 +374,11 @@ class CudaKalman:
 
     def sort_queue(self, enable):
         _check(lib().ck_sort_queue(self._h, int(enable)))
+
+    def set_tail_smoothing(self, enable):
+        """Smoothing in the forward filter's tail (default on; results do not
+        depend on it)."""
+        _check(lib().ck_set_tail_smoothing(self._h, int(enable)))
 
     def autotune(self, options, batch_in_device, batch_out_device):
         _check(lib().ck_autotune(self._h, C.byref(options), C.byref(batch_in_device),

@@ -1,11 +1,13 @@
-"""Per-track hardware counters of the forward-filter kernels, for the
-roofline the bench reports.
+"""Per-track hardware counters of the forward-filter kernels and of the
+smoother kernel, for the roofline the bench reports (the forward filter
+smooths most tracks in its tail; the smoother kernel takes the rest, so the
+pair's counters add up to the filter and smoother work of every track).
 
     python -m acts_gb300.profile_counters --csv prof.csv --tracks 200000 \
         --command "<the ncu command line>" > profiles/fit_kernel_counters.txt
 
 reads an ncu `--csv --page raw` capture of `acts_gb300.profile_case` (the
-metrics of METRICS below, one or more forward-filter launches of known
+metrics of METRICS below, forward-filter and smoother launches of known
 track count) and writes one line per captured kernel with its per-track
 FP64 and FP32 flops (an FMA counts 2; thread-level, predicated-on), DRAM
 bytes, FP64-pipe conversions and duration, headed by the hash of the kernel
@@ -50,7 +52,7 @@ def summarise(rows, tracks):
     out = []
     for r in rows:
         name = r.get("Kernel Name") or r.get("Function Name") or ""
-        if "fitKernel" not in name:
+        if "fitKernel" not in name and "smoothKernel" not in name:
             continue
         g = lambda m: _num(r[m]) if m in r and r[m] not in ("", "n/a") else float("nan")
         fp64 = 2 * g(METRICS[3]) + g(METRICS[4]) + g(METRICS[5])
@@ -101,7 +103,7 @@ def main(argv=None):
     ap.add_argument("--command", required=True)
     a = ap.parse_args(argv)
     rows = summarise(read_rows(a.csv), a.tracks)
-    print("# Forward-filter kernels: per-track counters from one ncu capture (%d tracks)"
+    print("# Forward-filter and smoother kernels: per-track counters from one ncu capture (%d tracks)"
           % a.tracks)
     print("# command: %s" % a.command)
     print("# flops count an FMA as 2 (thread-level, predicated-on lanes); dram = read + write")

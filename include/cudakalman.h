@@ -343,7 +343,8 @@ typedef struct ck_batch_out {
   int32_t* n_outliers;
   int32_t* ndf;
   double* chi2_sum;          /* sum of measurement-state chi2                */
-  /* per state [max_states * C * n_tracks] */
+  /* per state [max_states * C * n_tracks]; slots k >= n_states[t] are
+   * unspecified */
   int32_t* state_surface;    /* surface id (C = 1)                           */
   uint32_t* state_flags;     /* CK_FLAG_* (C = 1)                            */
   double* state_path_length; /* accumulated path at the state (C = 1)        */
@@ -472,12 +473,20 @@ ck_status ck_set_grid_blocks(ck_handle* h, int32_t precision, int32_t blocks);
 /* Chunking of host-memory batches (both sides in host memory): a batch of at
  * least two chunks is fitted chunk by chunk while the inputs of the next
  * chunk and the outputs of the previous one travel on copy streams. `tracks`:
- * tracks per chunk (0: the default, 500000; a negative value: never chunk). */
+ * tracks per chunk (0: the default, 500000; a negative value: never chunk).
+ * Results do not depend on it. */
 ck_status ck_set_host_chunk_tracks(ck_handle* h, int32_t tracks);
 
 /* Enables (default) or disables ordering the work queue by descending
  * surface-sequence length before the fit. */
 ck_status ck_sort_queue(ck_handle* h, int32_t enable);
+
+/* Enables (default) or disables smoothing in the forward filter's tail: in
+ * the compaction kernels, a block whose tracks have all ended smooths
+ * finished tracks of the batch while the last tracks are still propagating;
+ * the smoother kernel takes the rest. Results do not depend on it. Not with
+ * reverse filtering. No counterpart in the reference (a scheduling knob). */
+ck_status ck_set_tail_smoothing(ck_handle* h, int32_t enable);
 
 /* Text log of the last autotuner sweep (variant, block, blocks/SM, ms). */
 const char* ck_autotune_log(ck_handle* h);

@@ -120,5 +120,9 @@ def test_ragged_edge_case_batch(fitter_factory, max_states, reverse):
     assert_parity(rep, RTOL)
     ok = ora.status == 0
     # the duplicate link: the first one (input order) is the state's measurement
+    # (slots past a track's n_states are not written: compare its states)
     if max_states == 24 and ok[4]:
-        np.testing.assert_array_equal(gpu.view("state_surface")[4], ora.view("state_surface")[4])
+        k = ora.n_states[4]
+        assert gpu.n_states[4] == k
+        np.testing.assert_array_equal(gpu.view("state_surface")[4][:k],
+                                      ora.view("state_surface")[4][:k])

@@ -1,7 +1,10 @@
 """Large host-memory batches run as chunks whose transfers overlap the fits
 of their neighbours (ck_fit_batch, both sides in host memory, at least two
-chunks of 262,144 tracks): the outputs equal those of the same tracks fitted
-in calls below the chunking size, bit for bit, in the caller's SoA layout."""
+chunks): the outputs equal those of the same tracks fitted in calls below the
+chunking size, bit for bit, in the caller's SoA layout, for every output
+component, with reverse filtering and with the extrapolation to a reference
+surface. Host CSR offsets that are not a non-decreasing partition are
+rejected."""
 import numpy as np
 import pytest
 
@@ -50,3 +53,48 @@ def test_chunked_host_batch_equals_unchunked(precision, reverse):
         for i, p in zip(halves, parts):
             ok = p.status == 0
             np.testing.assert_array_equal(a[i][ok], p.track(name)[ok], err_msg=name)
+
+
+@pytest.mark.gpu
+def test_uneven_chunks_every_component():
+    from acts_gb300.fitter import CudaKalman
+
+    det = generate.Detector(abi.CKG_UNEVEN)
+    n = 160000
+    b = generate.generate(det, n, seed=37)
+    opt = abi.default_options(precision=abi.PRECISION_MIXED, outlier_chi2_cut=15.0,
+                              smoother=abi.SMOOTHER_MBF)
+    comps = abi.OUT_ALL | abi.OUT_PACKED_COV
+    fit = CudaKalman.for_detector(det)
+    try:
+        fit.set_host_chunk_tracks(-1)  # never chunk
+        ref = fit.fit_batch(b, opt, max_states=24, components=comps)
+        fit.set_host_chunk_tracks(23456)  # seven chunks, the last one short
+        got = fit.fit_batch(b, opt, max_states=24, components=comps)
+    finally:
+        fit.close()
+    for name in got.ARRAYS:
+        a, w = getattr(got, name), getattr(ref, name)
+        if w is None:
+            continue
+        if name in ("status", "n_states", "n_measurements", "n_holes", "n_outliers", "ndf",
+                    "chi2_sum"):
+            np.testing.assert_array_equal(a, w, err_msg=name)
+            continue
+        valid = np.arange(24)[None, :] < ref.n_states[:, None]
+        np.testing.assert_array_equal(got.view(name)[valid], ref.view(name)[valid], err_msg=name)
+
+
+@pytest.mark.gpu
+def test_decreasing_host_offsets_rejected():
+    from acts_gb300.fitter import CudaKalman, CudaKalmanError
+
+    det = generate.Detector(abi.CKG_BARREL)
+    b = generate.generate(det, 100, seed=3)
+    b.seq_offsets[51] = b.seq_offsets[49]  # row 50 runs backwards
+    fit = CudaKalman.for_detector(det)
+    try:
+        with pytest.raises(CudaKalmanError, match="decreasing CSR offsets"):
+            fit.fit_batch(b, abi.default_options(), max_states=12)
+    finally:
+        fit.close()

@@ -1,7 +1,8 @@
 """The roofline counters pipeline on the host: an ncu raw CSV of forward-
-filter launches becomes per-track counters, written and parsed back with the
-kernel-source hash; the bench's variant-to-kernel table covers every
-variant of both forms."""
+filter and smoother launches becomes per-track counters, written and parsed
+back with the kernel-source hash; the bench adds the launched filter's line
+and the smoother's; its variant-to-kernel table covers every variant of both
+forms."""
 import io
 import os
 import sys
@@ -46,7 +47,8 @@ def test_counters_round_trip(tmp_path):
     out.write_text(buf.getvalue())
     src, lines = pc.parse(str(out))
     assert src == pc.source_hash()
-    assert len(lines) == 1  # the smoother is not a forward filter
+    assert len(lines) == 2  # the forward filter and the smoother
+    assert "smoothKernel<float, 128>" in lines[1]["kernel"]
     ln = lines[0]
     assert "fitKernelPool<float, float, 384, 256>" in ln["kernel"]
     assert ln["fp64_flops"] == (2 * 1000 + 500 + 250) / 10
@@ -78,12 +80,20 @@ def test_bench_matches_ncu_kernel_names(tmp_path, monkeypatch):
                    "kernel=void fitKernelCompact<float, float, 256, 0, 0>(FitParams) | "
                    "fp64_flops=8722.0 fp32_flops=33411.7 dram_bytes=6058.6 conversions=1655.8 "
                    "fp64_pipe_busy=0.574 warps_active=0.125 duration_ms=12.900\n"
+                   "kernel=void smoothKernel<float, 128>(FitParams) | "
+                   "fp64_flops=10.0 fp32_flops=20.0 dram_bytes=30.0 conversions=1.0 "
+                   "fp64_pipe_busy=0.1 warps_active=0.1 duration_ms=0.040\n"
+                   "kernel=void fitKernelCompact<double, double, 256, 0, 0>(FitParams) | "
+                   "fp64_flops=43871.1 fp32_flops=2626.1 dram_bytes=10252.2 conversions=314.9 "
+                   "fp64_pipe_busy=0.644 warps_active=0.125 duration_ms=41.876\n"
                    % pc.source_hash())
     monkeypatch.setattr(bench, "COUNTERS", str(out))
     ln, name = bench.kernel_counters("float", 3)
-    assert ln is not None and ln["fp64_flops"] == 8722.0, name
+    # (the filter's line plus the smoother's)
+    assert ln is not None and ln["fp64_flops"] == 8732.0 and ln["dram_bytes"] == 6088.6, name
+    assert ln["fp64_pipe_busy"] == 0.574 and "smoothKernel<float, 128>" in name
     ln, why = bench.kernel_counters("double", 3)
-    assert ln is None and "no capture" in why
+    assert ln is None and "no capture of smoothKernel<double, 128>" in why
     out.write_text(out.read_text().replace(pc.source_hash(), "0" * 16))
     ln, why = bench.kernel_counters("float", 3)
     assert ln is None and "other kernel sources" in why
