@@ -557,7 +557,8 @@ ck_status ck_create(const ck_config* cfg, ck_handle** out) {
   if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaEventCreate(&h->ev0)) != cudaSuccess ||
       (e = cudaEventCreate(&h->ev1)) != cudaSuccess ||
-      (e = cudaEventCreate(&h->evMid)) != cudaSuccess) {
+      (e = cudaEventCreate(&h->evMid)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&h->lastCall, cudaEventDisableTiming)) != cudaSuccess) {
     delete h;
     return cudaFail(e, "stream/event creation");
   }
@@ -657,6 +658,10 @@ ck_status ck_destroy(ck_handle* h) {
   if (h->graphExec) cudaGraphExecDestroy(h->graphExec);
   for (auto& b : h->inBufs) b.release();
   for (auto& b : h->outBufs) b.release();
+  for (auto& set : h->chunkIn)
+    for (auto& b : set) b.release();
+  for (cudaEvent_t ev : h->inFree)
+    if (ev) cudaEventDestroy(ev);
   h->ctx.release();
   h->unitBuf.release();
   if (h->dSurfaces) cudaFree(h->dSurfaces);
@@ -666,6 +671,7 @@ ck_status ck_destroy(ck_handle* h) {
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->evMid) cudaEventDestroy(h->evMid);
+  if (h->lastCall) cudaEventDestroy(h->lastCall);
   for (cudaEvent_t ev : h->chunkTiming) cudaEventDestroy(ev);
   for (cudaEvent_t ev : h->chunkSync) cudaEventDestroy(ev);
   if (h->copyIn) cudaStreamDestroy(h->copyIn);
@@ -680,7 +686,9 @@ namespace {
 // Host batches of at least two chunks are pipelined: the inputs of chunk c+1
 // travel on one copy stream while chunk c is fitted on the caller's stream
 // and the outputs of chunk c-1 travel back on a second copy stream, so the
-// transfers hide behind the kernels. A chunk is a view of the full device
+// transfers hide behind the kernels. The device inputs alternate between two
+// sets from call to call, so that a call's first inputs travel while the
+// previous call's last chunk is still being fitted. A chunk is a view of the full device
 // input arrays (the CSR offsets are absolute: the chunk shifts only its
 // offset and per-track arrays by its first track); its outputs fill their own
 // block of the device output buffers (SoA over the chunk's tracks) and reach
@@ -711,7 +719,26 @@ ck_status ensureChunkResources(ck_handle* h, int chunks) {
       return cudaFail(e, "chunk event");
     h->chunkSync.push_back(ev);
   }
+  for (cudaEvent_t& ev : h->inFree)
+    if (!ev && (e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess)
+      return cudaFail(e, "chunk event");
   return CK_OK;
+}
+
+// Chunk boundaries of a host batch: equal chunks, but a shorter last one.
+// Every chunk's fit launch pays the same floor (its longest track), so the
+// split does not change the kernel time; the copy of the last chunk's
+// outputs is the one transfer that no fit hides (the first chunk's inputs
+// travel while the previous call's last chunk runs), so the last chunk is
+// the small one.
+constexpr double kLastChunkWeight = 0.43;
+
+std::vector<int> chunkBounds(int n, int chunks) {
+  std::vector<int> b(chunks + 1);
+  const double wsum = (chunks - 1) + kLastChunkWeight;
+  for (int c = 0; c < chunks; ++c) b[c] = (int)((double)n * c / wsum);
+  b[chunks] = n;
+  return b;
 }
 
 }  // namespace
@@ -723,11 +750,16 @@ static ck_status fitBatchHostChunked(ck_handle* h, const ck_options& opt, const 
   const int n = in.n_tracks;
   const int chunkTracks = chunkTracksOf(h);
   const int chunks = (n + chunkTracks - 1) / chunkTracks;
-  const int per = (n + chunks - 1) / chunks;
+  const std::vector<int> bounds = chunkBounds(n, chunks);
+  int per = 0;  // the largest chunk
+  for (int c = 0; c < chunks; ++c) per = std::max(per, bounds[c + 1] - bounds[c]);
   const int ms = out.max_states;
   const Tune tn = h->tune[opt.precision];
   ck_status s = ensureChunkResources(h, chunks);
   if (s != CK_OK) return s;
+  const int set = h->inSet;
+  h->inSet ^= 1;
+  DevBuf* inBufs = h->chunkIn[set];
   cudaError_t e;
   const int32_t* so = in.seq_offsets;
   const int32_t* mo = in.meas_offsets;
@@ -755,7 +787,7 @@ static ck_status fitBatchHostChunked(ck_handle* h, const ck_options& opt, const 
       if (i >= 10) continue;
       return fail(CK_ERR_INVALID_ARGUMENT, "input array missing");
     }
-    if ((e = h->inBufs[i].ensure(total(ins[i].kind) * ins[i].elem)) != cudaSuccess)
+    if ((e = inBufs[i].ensure(total(ins[i].kind) * ins[i].elem)) != cudaSuccess)
       return cudaFail(e, "input buffer");
   }
   // ---- device output buffers: per track, per state (rows ms x C) or per
@@ -784,12 +816,14 @@ static ck_status fitBatchHostChunked(ck_handle* h, const ck_options& opt, const 
   cudaEvent_t* sync = h->chunkSync.data();
   cudaEvent_t evStart = sync[2 * chunks], evDone = sync[2 * chunks + 1];
   cudaEventRecord(evStart, st);
-  cudaStreamWaitEvent(h->copyIn, evStart, 0);
+  // (the inputs wait only for the kernels of the call before last, which
+  // read this input set; the outputs for everything before this call)
+  cudaStreamWaitEvent(h->copyIn, h->inFree[set], 0);
   cudaStreamWaitEvent(h->copyOut, evStart, 0);
   size_t h2d = 0, d2h = 0;
   int launches = 0;
   for (int c = 0; c < chunks; ++c) {
-    const int t0 = c * per, t1 = std::min(n, t0 + per), nc = t1 - t0;
+    const int t0 = bounds[c], t1 = bounds[c + 1], nc = t1 - t0;
     // inputs of this chunk
     for (int i = 0; i < kInputArrays; ++i) {
       if (!ins[i].src) continue;
@@ -802,7 +836,7 @@ static ck_status fitBatchHostChunked(ck_handle* h, const ck_options& opt, const 
       }
       const size_t bytes = (b - a) * ins[i].elem;
       if (bytes &&
-          (e = cudaMemcpyAsync((char*)h->inBufs[i].p + a * ins[i].elem,
+          (e = cudaMemcpyAsync((char*)inBufs[i].p + a * ins[i].elem,
                                (const char*)ins[i].src + a * ins[i].elem, bytes,
                                cudaMemcpyHostToDevice, h->copyIn)) != cudaSuccess)
         return cudaFail(e, "input copy");
@@ -825,7 +859,7 @@ static ck_status fitBatchHostChunked(ck_handle* h, const ck_options& opt, const 
         continue;
       }
       const size_t shift = (ins[i].kind == 0 || ins[i].kind == 3) ? (size_t)t0 * ins[i].elem : 0;
-      *dins[i] = (const char*)h->inBufs[i].p + shift;
+      *dins[i] = (const char*)inBufs[i].p + shift;
     }
     ck_batch_out dout = out;
     dout.memory = CK_MEM_DEVICE;
@@ -861,6 +895,8 @@ static ck_status fitBatchHostChunked(ck_handle* h, const ck_options& opt, const 
       d2h += w * outs[i].rows;
     }
   }
+  // this input set is free once the last chunk's kernels have run
+  cudaEventRecord(h->inFree[set], st);
   cudaEventRecord(evDone, h->copyOut);
   cudaStreamWaitEvent(st, evDone, 0);
   h->lastLaunches = launches;
@@ -892,6 +928,16 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
   const int n = in->n_tracks;
   const Tune tn = h->tune[opt->precision];
   cudaError_t e;
+  // calls of one handle run on the device in call order, whatever their
+  // streams: they share the staging buffers and the scratch
+  if (h->lastCallStream && h->lastCallStream != st) cudaStreamWaitEvent(st, h->lastCall, 0);
+  auto done = [&](ck_status s) {
+    if (s == CK_OK) {
+      cudaEventRecord(h->lastCall, st);
+      h->lastCallStream = st;
+    }
+    return s;
+  };
 
   // ---- inputs
   ck_batch_in din = *in;
@@ -908,7 +954,7 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
         return fail(CK_ERR_INVALID_ARGUMENT, "decreasing CSR offsets");
     const int nSeq = in->seq_offsets[n], nMeas = in->meas_offsets[n];
     if (out->memory == CK_MEM_HOST && chunkTracksOf(h) > 0 && n >= 2 * chunkTracksOf(h))
-      return fitBatchHostChunked(h, *opt, *in, *out, st);
+      return done(fitBatchHostChunked(h, *opt, *in, *out, st));
     struct Item {
       const void* src;
       size_t bytes;
@@ -1051,7 +1097,7 @@ ck_status ck_fit_batch(ck_handle* h, const ck_options* opt, const ck_batch_in* i
   }
   h->lastD2H = d2h;
   if ((e = cudaGetLastError()) != cudaSuccess) return cudaFail(e, "batch pipeline");
-  return CK_OK;
+  return done(CK_OK);
 }
 
 ck_status ck_sync(ck_handle* h) {

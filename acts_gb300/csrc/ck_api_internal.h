@@ -148,6 +148,17 @@ struct ck_handle {
   std::vector<cudaEvent_t> chunkTiming;  // 3 per chunk
   std::vector<cudaEvent_t> chunkSync;    // 2 per chunk + 2
   int lastChunks = 0;
+  // their device inputs, two sets used by turns: a call's inputs travel
+  // while the previous call's last chunks are fitted; inFree[s] is recorded
+  // after the last kernel that reads set s
+  ck::DevBuf chunkIn[2][ck::kInputArrays];
+  cudaEvent_t inFree[2] = {nullptr, nullptr};
+  int inSet = 0;
+  // the end of the last ck_fit_batch on the device, and its stream: a call
+  // on another stream waits for it (calls share the staging buffers and the
+  // scratch)
+  cudaEvent_t lastCall = nullptr;
+  cudaStream_t lastCallStream = nullptr;
   int chunkTracks = 0;  // 0: kDefaultChunkTracks; < 0: never chunk
   std::mutex mu;
 };

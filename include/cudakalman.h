@@ -385,7 +385,10 @@ ck_status ck_destroy(ck_handle* h);
  * for the declared extension set (pass-through calibrator, GainMatrixUpdater,
  * GainMatrixSmoother, predicted-chi2 outlier finder). Asynchronous on
  * `stream` (NULL = the handle's stream); host-memory batches are staged
- * through pinned buffers. Call ck_sync() before reading host outputs. */
+ * through the handle's device buffers, and successive calls of one handle
+ * run on the device in call order, whatever their streams. Call ck_sync()
+ * (or synchronize `stream`) before reading host outputs, and keep host
+ * inputs unchanged until then. */
 ck_status ck_fit_batch(ck_handle* h, const ck_options* opt,
                        const ck_batch_in* in, ck_batch_out* out, void* stream);
 ck_status ck_sync(ck_handle* h);

@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from acts_gb300 import abi, generate
+from acts_gb300.results import Results
 
 N = 600000
 
@@ -98,3 +99,40 @@ def test_decreasing_host_offsets_rejected():
             fit.fit_batch(b, abi.default_options(), max_states=12)
     finally:
         fit.close()
+
+
+@pytest.mark.gpu
+def test_back_to_back_chunked_calls():
+    """Chunked calls issued without synchronizing in between (the next call's
+    inputs travel while the previous call's last chunk is fitted, into the
+    other input set), one of them on another stream: each call's results
+    equal those of the same batch fitted alone."""
+    import ctypes as C
+
+    import torch
+
+    from acts_gb300.fitter import CudaKalman
+
+    det = generate.Detector(abi.CKG_BARREL)
+    batches = [generate.generate(det, 90000, seed=80 + i) for i in range(3)]
+    opt = abi.default_options(precision=abi.PRECISION_MIXED)
+    comps = abi.OUT_SMOOTHED | abi.OUT_PACKED_COV
+    fit = CudaKalman.for_detector(det)
+    try:
+        fit.set_host_chunk_tracks(-1)
+        alone = [fit.fit_batch(b, opt, max_states=12, components=comps) for b in batches]
+        fit.set_host_chunk_tracks(30000)  # three chunks per call
+        other = torch.cuda.Stream()
+        res = [Results(b.n, 12, comps) for b in batches]
+        keep = [(b.as_batch_in(), r.as_batch_out()) for b, r in zip(batches, res)]
+        for k, (bi, bo) in enumerate(keep):
+            sp = C.c_void_p(other.cuda_stream) if k == 1 else None
+            fit.fit_batch_raw(opt, bi, bo, sp)
+        fit.sync()
+    finally:
+        fit.close()
+    for r, a in zip(res, alone):
+        np.testing.assert_array_equal(r.status, a.status)
+        valid = np.arange(12)[None, :] < a.n_states[:, None]
+        for name in ("smoothed", "smoothed_cov", "state_surface"):
+            np.testing.assert_array_equal(r.view(name)[valid], a.view(name)[valid], err_msg=name)
