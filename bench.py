@@ -364,8 +364,9 @@ def cpu_baseline(det, b, opt, budget_s=10.0):
 def bench_config(n, max_states):
     """The workload description both arms print."""
     return {"workload": WORKLOAD, "tracks_per_step_per_gpu": n,
-            "precision": "mixed (stepper, transport, field in FP32; update, inverses, chi2 in "
-                         "FP64)",
+            "precision": "mixed (stepper, transport, field and the Kalman update in FP32; "
+                         "parameter accumulation, smoother-gain inverse and bound-parameter "
+                         "conversions in FP64)",
             "l2": "inputs ~1 GB per step > 129 MB L2 (no flush needed)",
             "max_states": max_states,
             "outputs": "smoothed parameters + covariances (packed upper triangles)"}
