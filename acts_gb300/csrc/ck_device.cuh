@@ -843,6 +843,63 @@ CK_D void inverse6(const T* __restrict__ Cp, double inv[36]) {
   }
 }
 
+// 6x6 inverse of a symmetric positive-definite matrix given packed, in FP64
+// (the mixed form's smoother gain): the LDL^T factorisation without pivoting
+// (Golub and Van Loan, Matrix Computations, 4th ed., section 4.1), A = L D L^T
+// with L unit lower triangular, then A^-1 = W^T D^-1 W with W = L^-1. One
+// reciprocal per pivot (rcpRefined); about half the FP64 operations of the
+// pivoted LU inverse, no pivot search. Writes the upper triangle, packed.
+template <typename T>
+CK_D void inverseSym6(const T* __restrict__ Cp, double X[21]) {
+  double L[6][6], d[6], rd[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    double v[6];
+#pragma unroll
+    for (int k = 0; k < j; ++k) v[k] = L[j][k] * d[k];
+    double s = toDi(Cp[sidx(j, j)]);
+#pragma unroll
+    for (int k = 0; k < j; ++k) s = fma(-L[j][k], v[k], s);
+    d[j] = s;
+    rd[j] = rcpRefined(s);
+#pragma unroll
+    for (int i = j + 1; i < 6; ++i) {
+      double t = toDi(Cp[sidx(i, j)]);
+#pragma unroll
+      for (int k = 0; k < j; ++k) t = fma(-L[i][k], v[k], t);
+      L[i][j] = t * rd[j];
+    }
+  }
+  // W = L^-1, unit lower triangular: column by column, W[i][j] for i > j
+  double W[6][6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+#pragma unroll
+    for (int i = j + 1; i < 6; ++i) {
+      double t = -L[i][j];
+#pragma unroll
+      for (int k = j + 1; k < i; ++k) t = fma(-L[i][k], W[k][j], t);
+      W[i][j] = t;
+    }
+  }
+  // X = W^T D^-1 W: X[i][j] = sum over k >= max(i, j) of W[k][i] rd[k] W[k][j]
+  double U[6][6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+#pragma unroll
+    for (int i = 0; i < k; ++i) U[k][i] = W[k][i] * rd[k];
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = i; j < 6; ++j) {
+      // k = j term: W[j][j] = 1
+      double s = (i == j) ? rd[j] : U[j][i];
+#pragma unroll
+      for (int k = j + 1; k < 6; ++k) s = fma(U[k][i], W[k][j], s);
+      X[sidx(i, j)] = s;
+    }
+}
+
 // ------------------------------------------------------ Kalman update (N=2)
 // GainMatrixUpdater::visitMeasurementImpl<2>. pred/P packed symmetric;
 // writes filt and F (packed). Returns false on NaN gain (UpdateFailed).
@@ -1252,8 +1309,25 @@ template <typename GP>
 CK_D bool smoothStep(const double filt[6], const GP Pf[21], const double pp[6], const GP Ppp[21],
                      const GP* J, const double ps[6], const GP Psp[21], double sm[6],
                      GP Ps[21]) {
-  double inv[36];
-  inverse6<GP, sizeof(GP) == sizeof(float)>(Ppp, inv);
+  // the inverse of Ppp in FP64, as GP: the pivoted LU inverse of the
+  // reference (plain form), the symmetric LDL^T inverse (mixed form)
+  GP invg[36];
+  if constexpr (sizeof(GP) == sizeof(float)) {
+    double X[21];
+    inverseSym6<GP>(Ppp, X);
+    GP xg[21];
+#pragma unroll
+    for (int i = 0; i < 21; ++i) xg[i] = toPi<GP>(X[i]);
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+      for (int j = 0; j < 6; ++j) invg[i * 6 + j] = xg[sidx(i, j)];
+  } else {
+    double inv[36];
+    inverse6<GP>(Ppp, inv);
+#pragma unroll
+    for (int i = 0; i < 36; ++i) invg[i] = toPi<GP>(inv[i]);
+  }
   // G = (Pf J^T) Pinv
   GP PJ[36];
 #pragma unroll
@@ -1265,9 +1339,6 @@ CK_D bool smoothStep(const double filt[6], const GP Pf[21], const double pp[6], 
       for (int k = 0; k < 6; ++k) s += Pf[sidx(i, k)] * J[j * 6 + k];
       PJ[i * 6 + j] = s;
     }
-  GP invg[36];
-#pragma unroll
-  for (int i = 0; i < 36; ++i) invg[i] = toPi<GP>(inv[i]);
   GP G[36];
   bool nan = false;
 #pragma unroll
