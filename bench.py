@@ -239,7 +239,9 @@ def accuracy_report(b, r64, rmx, n):
     meas &= ok[:, None]
     d = np.abs(smmx - sm64)
     d[..., 2] = np.abs((smmx[..., 2] - sm64[..., 2] + np.pi) % (2 * np.pi) - np.pi)
-    rel = d / np.maximum(np.abs(sm64), sig64)
+    # (entries beyond a track's states are zero in both fits: 0/0, not used)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        rel = d / np.maximum(np.abs(sm64), sig64)
     relm = rel[meas]
     # pulls against truth at the measurement states (smoothed loc0, loc1, phi, theta, q/p)
     surf = r64["state_surface"].reshape(ms, r64["N"])[:, :n].T
