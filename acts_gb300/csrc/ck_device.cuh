@@ -281,35 +281,62 @@ CK_D int intersect(const Surf<P>& s, const P pos[3], const P dir[3], P tol, P pa
 // is solved in FP32 (root nearest to zero as c/q) and each root is refined
 // by one Newton step on the FP64 quadratic, so the path to the surface is
 // FP64-accurate (the final step lands on the surface as in the plain form).
+// `coarse`: a root beyond this path length (of a quadratic with well
+// separated roots) keeps its FP32 value, unrefined. The navigator passes
+// twice its accuracy step size plus 1 mm: such a root is neither on the
+// surface nor the binding step-size constraint, refined or not, so the
+// propagation is the same.
 CK_D int intersectMixed(const Surf<double>& s, const double pos[3], const double dir[3],
-                        double tol, double path[2], int st[2]) {
+                        double tol, double path[2], int st[2], double coarse = kNotSet) {
+  // (finite roots only; the default refines every root)
+  const bool useCoarse = coarse < 1e30;
+  const float farf = useCoarse ? d2f(coarse) : 0.0f;
+  auto isFar = [&](float t) { return useCoarse && t > farf && t <= 3.4e38f; };
+  // (every multiply-add is an explicit fma and every product feeding an add an
+  // explicit __dmul_rn, so that the roundings do not depend on the kernel
+  // instance the code is inlined into)
   if (s.type == CK_SURFACE_PLANE) {
-    const double denom = dir[0] * s.R[2] + dir[1] * s.R[5] + dir[2] * s.R[8];
+    const double denom = fma(dir[2], s.R[8], fma(dir[1], s.R[5], __dmul_rn(dir[0], s.R[2])));
     if (denom == 0.0) {
       path[0] = 0.0;
       st[0] = 0;
       return 1;
     }
-    const double num =
-        s.R[2] * (s.c[0] - pos[0]) + s.R[5] * (s.c[1] - pos[1]) + s.R[8] * (s.c[2] - pos[2]);
+    const double num = fma(s.R[8], s.c[2] - pos[2],
+                           fma(s.R[5], s.c[1] - pos[1], __dmul_rn(s.R[2], s.c[0] - pos[0])));
     // FP32 quotient refined by one FP64 residual step
     const float denomf = d2f(denom);
-    const double p0 = toD(d2f(num) / denomf);
-    const double pl = p0 + toD(d2f(num - p0 * denom) / denomf);
+    const float p0f = d2f(num) / denomf;
+    const double p0 = toD(p0f);
+    const double pl = isFar(p0f) ? p0 : p0 + toD(d2f(fma(-p0, denom, num)) / denomf);
     path[0] = pl;
     st[0] = statusOf(pl, tol);
     return 1;
   }
-  const double a0 = s.R[2], a1 = s.R[5], a2 = s.R[8];
-  const double pc0 = pos[0] - s.c[0], pc1 = pos[1] - s.c[1], pc2 = pos[2] - s.c[2];
-  const double px0 = pc1 * a2 - pc2 * a1, px1 = pc2 * a0 - pc0 * a2, px2 = pc0 * a1 - pc1 * a0;
-  const double lx0 = dir[1] * a2 - dir[2] * a1, lx1 = dir[2] * a0 - dir[0] * a2,
-               lx2 = dir[0] * a1 - dir[1] * a0;
-  const double ad = lx0 * lx0 + lx1 * lx1 + lx2 * lx2;
-  const double bd = 2.0 * (lx0 * px0 + lx1 * px1 + lx2 * px2);
-  const double ccd = (px0 * px0 + px1 * px1 + px2 * px2) - s.radius * s.radius;
+  double ad, bd, ccd;
+  const double r2 = __dmul_rn(s.radius, s.radius);
+  if (s.R[2] == 0.0 && s.R[5] == 0.0 && s.R[8] == 1.0) {
+    // axis along global z: the cross products with the axis are
+    // (pc1, -pc0, 0) and (dir1, -dir0, 0); the same roundings as the general
+    // expressions below give for this axis
+    const double pc0 = pos[0] - s.c[0], pc1 = pos[1] - s.c[1];
+    ad = fma(dir[0], dir[0], __dmul_rn(dir[1], dir[1]));
+    bd = 2.0 * fma(dir[0], pc0, __dmul_rn(dir[1], pc1));
+    ccd = fma(pc0, pc0, __dmul_rn(pc1, pc1)) - r2;
+  } else {
+    const double a0 = s.R[2], a1 = s.R[5], a2 = s.R[8];
+    const double pc0 = pos[0] - s.c[0], pc1 = pos[1] - s.c[1], pc2 = pos[2] - s.c[2];
+    const double px0 = fma(pc1, a2, -__dmul_rn(pc2, a1)), px1 = fma(pc2, a0, -__dmul_rn(pc0, a2)),
+                 px2 = fma(pc0, a1, -__dmul_rn(pc1, a0));
+    const double lx0 = fma(dir[1], a2, -__dmul_rn(dir[2], a1)),
+                 lx1 = fma(dir[2], a0, -__dmul_rn(dir[0], a2)),
+                 lx2 = fma(dir[0], a1, -__dmul_rn(dir[1], a0));
+    ad = fma(lx2, lx2, fma(lx1, lx1, __dmul_rn(lx0, lx0)));
+    bd = 2.0 * fma(lx2, px2, fma(lx1, px1, __dmul_rn(lx0, px0)));
+    ccd = fma(px2, px2, fma(px1, px1, __dmul_rn(px0, px0))) - r2;
+  }
   const float a = d2f(ad), b = d2f(bd), cc = d2f(ccd);
-  const float disc = b * b - 4.0f * a * cc;
+  const float disc = fmaf(b, b, -__fmul_rn(4.0f * a, cc));
   if (!(disc >= 0.0f)) {
     st[0] = st[1] = 0;
     path[0] = path[1] = 0.0;
@@ -317,10 +344,14 @@ CK_D int intersectMixed(const Surf<double>& s, const double pos[3], const double
   }
   const float sq = sqrtf(disc);
   const float q = -0.5f * (b + (b > 0.0f ? sq : -sq));
+  // roots apart by more than 1 % of |b| / a: each FP32 root within ~1e-5 of its
+  // value, far from the other
+  const bool separated = disc > 1e-4f * (b * b);
   auto refine = [&](float t0f) -> double {
+    if (separated && isFar(t0f)) return toD(t0f);
     const double t0 = toD(t0f);
-    const double f = (ad * t0 + bd) * t0 + ccd;
-    const double df = 2.0 * ad * t0 + bd;
+    const double f = fma(fma(ad, t0, bd), t0, ccd);
+    const double df = fma(2.0 * ad, t0, bd);
     return df != 0.0 ? t0 - toD(d2f(f) / d2f(df)) : t0;
   };
   const double first = refine(q / a);

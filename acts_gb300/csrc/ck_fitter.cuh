@@ -216,8 +216,10 @@ struct Lane {
   }
 
   // Surface::intersect in double (BoundaryTolerance::Infinite), along the
-  // direction of travel (the navigator's direction times the momentum's)
-  CK_NI int intersectSurf(const FitParams& fp, int sid, double path[2], int st[2]) const {
+  // direction of travel (the navigator's direction times the momentum's);
+  // `coarse` as intersectMixed's (mixed form)
+  CK_NI int intersectSurf(const FitParams& fp, int sid, double path[2], int st[2],
+                          double coarse = kNotSet) const {
     Surf<double> sf;
     sf.load(fp.surfaces + sid);
     double nd[3] = {dir[0], dir[1], dir[2]};
@@ -227,7 +229,7 @@ struct Lane {
       nd[2] = -dir[2];
     }
     if constexpr (sizeof(P) == sizeof(float)) {
-      return intersectMixed(sf, pos, nd, fp.opt.surfaceTolerance, path, st);
+      return intersectMixed(sf, pos, nd, fp.opt.surfaceTolerance, path, st, coarse);
     } else {
       return intersect(sf, pos, nd, fp.opt.surfaceTolerance, path, st);
     }
@@ -431,7 +433,10 @@ struct Lane {
   CK_D int surfaceStatus(const FitParams& fp, int sid, int idx) {
     double path[2];
     int st[2];
-    intersectSurf(fp, sid, path, st);
+    // the next step is min(|min(cNav, cActor, cUser)|, cAcc): a path beyond
+    // 2 cAcc + 1 mm neither binds it nor is on the surface, so the mixed form
+    // keeps such a path's FP32 value (the step and the status are the same)
+    intersectSurf(fp, sid, path, st, 2.0 * fabs(cAcc) + 1.0);
     const double pl = idx ? path[1] : path[0];
     const int stt = idx ? st[1] : st[0];
     if (stt != 0) {
