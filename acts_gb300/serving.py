@@ -69,8 +69,15 @@ class FitServer:
             results = Results(batch.n, self.max_states, self.components)
         bi = batch.as_batch_in()
         bo = results.as_batch_out()
-        _check(_bind().ck_server_submit(self._s, int(event_id), C.byref(bi), C.byref(bo)))
-        self._inflight[int(event_id)] = (batch, results, bi, bo)
+        # registered before the submission: the event can finish, and another
+        # thread poll it, before ck_server_submit has returned to this one
+        key = int(event_id)
+        self._inflight[key] = (batch, results, bi, bo)
+        try:
+            _check(_bind().ck_server_submit(self._s, key, C.byref(bi), C.byref(bo)))
+        except Exception:
+            self._inflight.pop(key, None)
+            raise
 
     def poll(self, timeout_ms=100):
         """(event_id, results, latency_ms) of one finished event, or None."""
@@ -82,7 +89,7 @@ class FitServer:
             return None
         entry = self._inflight.pop(eid.value, None)
         _check(st)
-        return eid.value, entry[1], lat.value
+        return eid.value, entry[1] if entry is not None else None, lat.value
 
     def stats(self):
         a, b, c, d = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()

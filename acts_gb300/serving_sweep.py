@@ -70,12 +70,14 @@ def main(argv=None):
             lat, done, held = {}, threading.Event(), {}
 
             def poller():
-                while len(lat) < len(idx):
-                    r = srv.poll(timeout_ms=200)
-                    if r is not None:
-                        lat[r[0]] = r[2]
-                        held.pop(r[0], None)
-                done.set()
+                try:
+                    while len(lat) < len(idx):
+                        r = srv.poll(timeout_ms=200)
+                        if r is not None:
+                            lat[r[0]] = r[2]
+                            held.pop(r[0], None)
+                finally:
+                    done.set()
 
             threading.Thread(target=poller, daemon=True).start()
             t0 = time.perf_counter()

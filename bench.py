@@ -892,12 +892,14 @@ def serving_report(torch, n_events=10000, seed=77, max_states=20, pool_tracks=40
             held = {}
 
             def poller():
-                while len(st.lat) < n_ev:
-                    r = srv.poll(timeout_ms=200)
-                    if r is not None:
-                        st.lat[r[0]] = r[2]
-                        held.pop(r[0], None)
-                st.done.set()
+                try:
+                    while len(st.lat) < n_ev:
+                        r = srv.poll(timeout_ms=200)
+                        if r is not None:
+                            st.lat[r[0]] = r[2]
+                            held.pop(r[0], None)
+                finally:
+                    st.done.set()
 
             th = threading.Thread(target=poller, daemon=True)
             th.start()
